@@ -1,0 +1,338 @@
+"""Benchmark: MHD cell-updates/s per RK4 step on the 21M-cell mixed-precision shell.
+
+Workload: Yin-Yang spherical shell r in [0.7, 1.0] R_sun, per panel 96 x 192 x 576
+cells in 16^3 blocks (5,184 blocks, 21,233,664 cells), 8 variables, polytrope
+background (n = 1.5, density contrast 100), seeded entropy bump + dipole B +
+random-phase Kolmogorov velocity (rms Mach 0.01). One "step" is one full
+ModAdvance_rk4: CFL reduction, four RK stages with a ghost exchange after each,
+the artificial-diffusion pass and its exchange. FP32 state and stencil RHS,
+FP64 p1 assembly, CFL reduction and dt.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N>1 (under torchrun): every rank advances its own replica of the shell on its
+GPU ("replicas only": the shell is not partitioned across GPUs); value is the
+sum of cell-updates over ranks divided by the max time over ranks.
+
+--impl reference times the CPU restatement of the reference algorithm (the
+oracle; the Fortran reference cannot be built here) on the host cores, on a
+bounded sample of the same workload (a shell of 16^3 blocks with the same
+physics, 108 blocks / 442,368 cells), and prints the same JSON line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MHD cell-updates/s per RK4 step"
+UNIT = "cell-updates/s"
+STATE_BYTES_PER_VAR = 4          # FP32 stored state
+NVAR = 8
+# algorithmic bytes per interior cell per RK4 step: 4 stages x (read u_s,
+# read u^n, write u_s+1) + diffusion (read, write) = 14 state passes of 8
+# variables, plus the CFL pass reading 6 variables
+BYTES_PER_CELL_STEP = NVAR * STATE_BYTES_PER_VAR * 14 + 6 * STATE_BYTES_PER_VAR   # 472
+STAGE_BYTES_PER_CELL = NVAR * STATE_BYTES_PER_VAR * 3                            # 96 per stage launch
+DIFF_BYTES_PER_CELL = NVAR * STATE_BYTES_PER_VAR * 2                             # 64
+WORKLOAD = "yinyang_shell_mhd_21M_mixed"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(name):
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_launch_full_size:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(n_gpus):
+    """torchrun env -> (rank, world, local_rank, dist module or None)."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+        return rank, world, local, dist
+    return 0, 1, 0, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def reduce_max(dist, x):
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(dist, x):
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def cpu_sample_config():
+    """Bounded CPU sample of the workload: same physics and 16^3 blocks, per
+    panel 32 x 48 x 144 cells (108 blocks, 442,368 cells)."""
+    from falcon_gb300 import config
+    return config.make_config(block=(16, 16, 16), root_tiles=(1, 3, 9), radial_levels=1, radial_option=1,
+                              amr=(), precision=config.PREC_FP64)
+
+
+def time_oracle(steps, warmup, budget_s=25.0):
+    """Time the CPU oracle on the bounded sample with all host threads."""
+    import oracle
+    from falcon_gb300 import synth
+    cfg = cpu_sample_config()
+    o = oracle.Oracle(cfg)
+    u0 = synth.initial_state(cfg, o.block_ranges(), o.block_flags(), seed=1002)
+    o.set_state(u0)
+    o.exchange()
+    o.exchange()
+    for _ in range(warmup):
+        o.step()
+    cells = o.nblocks * 16 ** 3
+    done, t0 = 0, time.perf_counter()
+    while done < steps:
+        o.step()
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    el = time.perf_counter() - t0
+    return cells * done / el, oracle.num_threads(), "%d steps of the %d-cell 16^3-block shell (%d blocks)" % (
+        done, cells, o.nblocks)
+
+
+def run_reference(args, rank, world, dist):
+    if rank != 0:
+        return
+    value, cores, sample = time_oracle(max(args.steps, 1), min(args.warmup, 1))
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "cells": 21233664, "blocks": 5184, "block": [16, 16, 16],
+                   "sample": "cpu sample shell, same physics"},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args, rank, world, local, dist):
+    import falcon_gb300 as fg
+    from falcon_gb300 import config
+    fg.build()
+    cfg = config.shell_mixed_21m(device=local)
+    f = fg.Falcon(cfg)
+    cells = f.interior_cells
+    f.init_synthetic(kind=1, seed=1002, mach=0.01)
+    f.exchange()
+    f.exchange()
+    # ---- device-resident throughput (value)
+    f.run_steps(args.warmup)
+    f.synchronize()
+    barrier(dist)
+    f.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    f.timer_start()
+    f.run_steps(args.steps)
+    ms = f.timer_stop()
+    f.synchronize()
+    clk = clocks.stop()
+    barrier(dist)
+    ms_max = reduce_max(dist, ms)
+    total_cells = reduce_sum(dist, float(cells * args.steps))
+    value = total_cells / (ms_max / 1e3)
+    launches_per_step = 2 + 4 * 3 + 3
+
+    # ---- per-kernel times (events around every launch) for the roofline
+    f.set_kernel_timing(True)
+    f.reset_kernel_stats()
+    f.run_steps(2)
+    f.synchronize()
+    stats = f.kernel_stats()
+    f.set_kernel_timing(False)
+    tot = sum(v[0] for v in stats.values()) or 1.0
+    top = max(stats, key=lambda k: stats[k][0])
+    avg_ms = stats[top][0] / max(stats[top][1], 1)
+    per_cell = {"stage": STAGE_BYTES_PER_CELL, "diffusion": DIFF_BYTES_PER_CELL}.get(top)
+    hbm, peak_kind = peaks()
+    roof = None
+    if per_cell is not None:
+        ach = cells * per_cell / (avg_ms / 1e3) / 1e9
+        roof = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                "traffic": profile_traffic("stage_mixed_21m.txt"), "kernel": "k_stage<float,16,16,16,2>",
+                "algorithmic_bytes_per_launch": cells * per_cell, "avg_launch_ms": avg_ms,
+                "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind}
+    step_ach = cells * BYTES_PER_CELL_STEP / (ms_max / args.steps / 1e3) / 1e9
+    shares = {k: round(v[0] / tot, 4) for k, v in stats.items()}
+
+    # ---- end to end through the C ABI with host buffers: every step uploads
+    # the FP64 Fortran-layout state from pinned host memory, advances, and
+    # downloads the new state (the drop-in keeps Tree%LocalBlocks authoritative)
+    host = np.empty(f.shape, dtype=np.float64)
+    f.pin_host(host)
+    f.download_state_into(host)
+    k_e2e = max(1, min(args.steps, 10))
+    f.synchronize()
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(k_e2e):
+        f.upload_state_raw(host)
+        f.advance_rk4(want_dt=True)
+        f.download_state_into(host)
+    e2e_s = time.perf_counter() - t0
+    barrier(dist)
+    e2e_s = reduce_max(dist, e2e_s)
+    e2e_val = reduce_sum(dist, float(cells * k_e2e)) / e2e_s
+    f.unpin_host(host)
+    nbytes = host.nbytes
+    # resident variant: the state stays on the GPU, dt comes back every step
+    t0 = time.perf_counter()
+    for _ in range(k_e2e):
+        f.advance_rk4(want_dt=True)
+    res_s = reduce_max(dist, time.perf_counter() - t0)
+    res_val = reduce_sum(dist, float(cells * k_e2e)) / res_s
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, cores, sample = time_oracle(3, 1, budget_s=20.0)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "cells": cells, "blocks": f.nblocks, "block": [16, 16, 16],
+                       "ghost_layers": 2, "nvar": 8, "precision": "mixed",
+                       "l2": "inputs larger than L2 (state %.0f MB per buffer)" % (cells * 8 * 4 * (20 / 16) ** 3 / 1e6),
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "roofline": roof,
+            "step_roofline": {"achieved": step_ach, "peak": hbm, "unit": "GB/s", "frac": step_ach / hbm,
+                              "algorithmic_bytes_per_cell_step": BYTES_PER_CELL_STEP},
+            "kernel_time_share": shares,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                    "mode": "state uploaded and downloaded (FP64, pinned) every step"},
+            "e2e_resident": {"value": res_val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 8},
+            "gpu_launches": launches_per_step * args.steps,
+            "clocks": clk,
+        }
+        print(json.dumps(line))
+    f.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 0)
+    rank, world, local, dist = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world, dist)
+    else:
+        run_ours(args, rank, world, local, dist)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,228 @@
+"""falcon_gb300 -- GB300-native per-step hot path of the Falcon solar MHD code.
+
+Python face of the C ABI in include/falcon_gb300.h (ctypes). It mirrors the
+reference's step interface:
+
+    Falcon.timestep()      ModTimeStep_Dynamo + MPI MIN  (3_6/ModTimeStep.f90:10-30)
+    Falcon.advance_rk4()   ModAdvance_rk4                (3_6/ModAdvance.f90:18-112)
+    Falcon.exchange()      ModCommunication_SendRecvGC_new(Tree,.false.)
+                                                         (3_6/ModCommunication.f90:655-795)
+
+There is no CPU fallback: every call goes to the CUDA library, and a missing or
+unloadable library raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import config
+from .config import (Config, GhostEntry, PREC_FP64, PREC_MIXED, NVAR, VAR_NAMES,
+                     make_config, shell_fp64_cpu, shell_mixed_21m, tiny)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libfalcon_gb300.so")
+
+OK = 0
+ERR_INVALID_ARG = -1
+ERR_CUDA = -2
+ERR_NAN_DETECTED = -3
+ERR_TIMEOUT = -4
+ERR_NOT_CONVERGED = -5
+ERR_BOUNDS = -6
+ERR_UNCOVERED_GHOST = -7
+ERR_NO_DEVICE = -8
+
+# every symbol declared in include/falcon_gb300.h
+EXPORTS = (
+    "falcon_create", "falcon_destroy", "falcon_last_error", "falcon_num_blocks", "falcon_block_ranges",
+    "falcon_block_flags", "falcon_get_background", "falcon_ghost_count", "falcon_ghost_map",
+    "falcon_upload_state", "falcon_download_state", "falcon_init_synthetic", "falcon_exchange",
+    "falcon_timestep", "falcon_step_rk4", "falcon_run_steps", "falcon_synchronize",
+    "falcon_set_kernel_timing", "falcon_kernel_stats", "falcon_reset_kernel_stats", "falcon_timer_start",
+    "falcon_timer_stop", "falcon_device_bytes", "falcon_pin_host", "falcon_unpin_host",
+)
+
+_lib = None
+
+
+class FalconError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("falcon error %d: %s" % (code, msg))
+        self.code = code
+
+
+def build(force=False):
+    from .build import build as _b
+    return _b(force=force)
+
+
+def lib():
+    """Load the CUDA library (raises if it is absent: there is no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise FalconError(ERR_NO_DEVICE, "libfalcon_gb300.so is not built; run falcon_gb300.build()")
+        L = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        for n in EXPORTS:
+            getattr(L, n).restype = C.c_int
+        L.falcon_destroy.restype = None
+        L.falcon_create.argtypes = [C.POINTER(vp), C.POINTER(Config)]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Falcon:
+    """One Yin-Yang shell on one GPU (device=-1: host-side setup only)."""
+
+    def __init__(self, cfg):
+        self.L = lib()
+        self.cfg = cfg
+        h = C.c_void_p()
+        rc = self.L.falcon_create(C.byref(h), C.byref(cfg))
+        self.h = h
+        if rc != OK:
+            msg = self.last_error()
+            self.L.falcon_destroy(h)
+            self.h = None
+            raise FalconError(rc, msg)
+        nb, ny = C.c_int32(), C.c_int32()
+        self.L.falcon_num_blocks(self.h, C.byref(nb), C.byref(ny))
+        self.nblocks, self.nblocks_yin = nb.value, ny.value
+        t = cfg.tree
+        self.shape = (self.nblocks, NVAR, t.nk + 2 * t.ng, t.nj + 2 * t.ng, t.ni + 2 * t.ng)
+        self.interior_cells = self.nblocks * t.ni * t.nj * t.nk
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.falcon_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def last_error(self):
+        buf = C.create_string_buffer(1024)
+        self.L.falcon_last_error(self.h, buf, C.c_size_t(1024))
+        return buf.value.decode()
+
+    def _ck(self, rc):
+        if rc != OK:
+            raise FalconError(rc, self.last_error())
+
+    # ---- host-side queries
+    def block_ranges(self):
+        out = np.zeros((self.nblocks, 3, 2))
+        self._ck(self.L.falcon_block_ranges(self.h, _ptr(out)))
+        return out
+
+    def block_flags(self):
+        out = np.zeros(self.nblocks, dtype=np.int32)
+        self._ck(self.L.falcon_block_flags(self.h, _ptr(out)))
+        return out
+
+    def background(self):
+        t = self.cfg.tree
+        out = np.zeros((self.nblocks, config.NPROF, t.ni + 2 * t.ng))
+        self._ck(self.L.falcon_get_background(self.h, _ptr(out)))
+        return out
+
+    def ghost_count(self):
+        n = C.c_int64()
+        self._ck(self.L.falcon_ghost_count(self.h, C.byref(n)))
+        return n.value
+
+    def ghost_map(self):
+        n = self.ghost_count()
+        arr = (GhostEntry * n)()
+        self._ck(self.L.falcon_ghost_map(self.h, arr, C.c_int64(n)))
+        dt = np.dtype([("tblock", "<i4"), ("ti", "<i4"), ("tj", "<i4"), ("tk", "<i4"),
+                       ("sblock", "<i4"), ("pad_", "<i4"), ("src_x", "<f8", (3,))])
+        return np.frombuffer((C.c_char * (n * dt.itemsize)).from_address(C.addressof(arr)),
+                             dtype=dt, count=n).copy()
+
+    # ---- state
+    def upload_state(self, u):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        if u.shape != self.shape:
+            raise ValueError("state shape %s != %s" % (u.shape, self.shape))
+        self._ck(self.L.falcon_upload_state(self.h, _ptr(u)))
+
+    def download_state(self):
+        u = np.empty(self.shape)
+        self._ck(self.L.falcon_download_state(self.h, _ptr(u)))
+        return u
+
+    def upload_state_raw(self, u):
+        """Upload without shape/dtype conversion (u: C-contiguous float64 of self.shape)."""
+        self._ck(self.L.falcon_upload_state(self.h, _ptr(u)))
+
+    def download_state_into(self, u):
+        self._ck(self.L.falcon_download_state(self.h, _ptr(u)))
+        return u
+
+    def pin_host(self, a):
+        self._ck(self.L.falcon_pin_host(self.h, _ptr(a), C.c_size_t(a.nbytes)))
+
+    def unpin_host(self, a):
+        self._ck(self.L.falcon_unpin_host(self.h, _ptr(a)))
+
+    def init_synthetic(self, kind=0, seed=1001, mach=0.01):
+        self._ck(self.L.falcon_init_synthetic(self.h, C.c_int32(kind), C.c_uint64(seed), C.c_double(mach)))
+
+    # ---- the hot path
+    def exchange(self):
+        self._ck(self.L.falcon_exchange(self.h))
+
+    def timestep(self):
+        dt = C.c_double()
+        self._ck(self.L.falcon_timestep(self.h, C.byref(dt)))
+        return dt.value
+
+    def advance_rk4(self, want_dt=True):
+        dt = C.c_double()
+        self._ck(self.L.falcon_step_rk4(self.h, C.byref(dt) if want_dt else None))
+        return dt.value if want_dt else None
+
+    def run_steps(self, n):
+        self._ck(self.L.falcon_run_steps(self.h, C.c_int32(n)))
+
+    def synchronize(self):
+        self._ck(self.L.falcon_synchronize(self.h))
+
+    # ---- measurement
+    def set_kernel_timing(self, on):
+        self._ck(self.L.falcon_set_kernel_timing(self.h, C.c_int32(1 if on else 0)))
+
+    def kernel_stats(self):
+        names = C.create_string_buffer(1024)
+        ms = (C.c_double * 32)()
+        cnt = (C.c_int64 * 32)()
+        n = C.c_int32()
+        self._ck(self.L.falcon_kernel_stats(self.h, names, C.c_size_t(1024), ms, cnt, C.c_int32(32), C.byref(n)))
+        nm = names.value.decode().split("\n")
+        return {nm[k]: (ms[k], cnt[k]) for k in range(n.value)}
+
+    def reset_kernel_stats(self):
+        self._ck(self.L.falcon_reset_kernel_stats(self.h))
+
+    def timer_start(self):
+        self._ck(self.L.falcon_timer_start(self.h))
+
+    def timer_stop(self):
+        ms = C.c_double()
+        self._ck(self.L.falcon_timer_stop(self.h, C.byref(ms)))
+        return ms.value
+
+    def device_bytes(self):
+        b = C.c_int64()
+        self._ck(self.L.falcon_device_bytes(self.h, C.byref(b)))
+        return b.value

@@ -1,0 +1,575 @@
+// capi.cu -- the C ABI (include/falcon_gb300.h): context, device tables,
+// state transfer, the captured step graph and kernel timing.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/falcon_gb300.h"
+#include "host_setup.h"
+#include "kernels.cuh"
+#include "synth.cuh"
+
+using namespace falcon;
+
+namespace {
+const char* const kKernelNames[] = {"stage", "diffusion", "cfl", "finalize_dt", "ghost_fill"};
+enum { KN_STAGE = 0, KN_DIFF, KN_CFL, KN_FIN, KN_GHOST, KN_COUNT };
+}  // namespace
+
+struct falcon_ctx {
+    Grid grid;
+    std::string err;
+    falcon_config cfg;
+    bool on_device = false;
+    int device = -1;
+    cudaStream_t st = nullptr;
+    StepDims dims{};
+    size_t elem = 8;            // bytes per state element
+    void* U = nullptr;          // u^n (primitive_IV)
+    void* RK = nullptr;         // stage state (primitive_rk_IV)
+    double* stage64 = nullptr;  // FP64 staging buffer for mixed-mode transfers (lazy)
+    double *gi = nullptr, *gj = nullptr, *gs = nullptr;
+    float *gi_f = nullptr, *gj_f = nullptr, *gs_f = nullptr;
+    int32_t* flags = nullptr;
+    StepScalars* sc = nullptr;
+    int32_t *cp_dst = nullptr, *cp_src = nullptr, *ip_dst = nullptr, *ip_src = nullptr;
+    double *ip_w = nullptr, *ip_rot = nullptr;
+    uint8_t* ip_kind = nullptr;
+    GhostCopyList cp{};
+    GhostInterpList ip{};
+    cudaGraphExec_t graph = nullptr;
+    int64_t steps_done = 0;
+    int64_t dev_bytes = 0;
+    // timing
+    bool ktiming = false;
+    struct Rec { int k; cudaEvent_t a, b; };
+    std::vector<Rec> pending;
+    std::vector<cudaEvent_t> pool;
+    double kms[KN_COUNT] = {0};
+    int64_t kcount[KN_COUNT] = {0};
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    std::vector<void*> allocs;
+
+    int fail(int code, const std::string& m) { err = m; return code; }
+    int cuda_fail(cudaError_t e, const char* where) {
+        err = std::string(where) + ": " + cudaGetErrorString(e);
+        return FALCON_ERR_CUDA;
+    }
+    template <class P> cudaError_t alloc(P** p, size_t bytes) {
+        cudaError_t e = cudaMalloc((void**)p, bytes ? bytes : 16);
+        if (e == cudaSuccess) { allocs.push_back((void*)*p); dev_bytes += (int64_t)bytes; }
+        return e;
+    }
+    cudaEvent_t ev() {
+        if (pool.empty()) { cudaEvent_t e; cudaEventCreate(&e); return e; }
+        cudaEvent_t e = pool.back(); pool.pop_back(); return e;
+    }
+    Geometry geom() const { return Geometry{gi, gj, gs, gi_f, gj_f, gs_f, flags}; }
+    bool mixed() const { return cfg.precision == FALCON_PREC_MIXED; }
+};
+
+#define CK(call, where)                                         \
+    do {                                                        \
+        cudaError_t e_ = (call);                                \
+        if (e_ != cudaSuccess) return ctx->cuda_fail(e_, where); \
+    } while (0)
+
+namespace {
+
+// Launch one kernel, bracketed by events when per-kernel timing is on.
+template <class F> cudaError_t timed(falcon_ctx* ctx, int k, F&& f) {
+    if (!ctx->ktiming) return f();
+    cudaEvent_t a = ctx->ev(), b = ctx->ev();
+    cudaEventRecord(a, ctx->st);
+    cudaError_t e = f();
+    cudaEventRecord(b, ctx->st);
+    ctx->pending.push_back({k, a, b});
+    return e;
+}
+
+void collect(falcon_ctx* ctx) {
+    for (auto& r : ctx->pending) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+            ctx->kms[r.k] += ms;
+            ctx->kcount[r.k] += 1;
+        }
+        ctx->pool.push_back(r.a);
+        ctx->pool.push_back(r.b);
+    }
+    ctx->pending.clear();
+}
+
+cudaError_t ghost(falcon_ctx* ctx, void* u) {
+    return timed(ctx, KN_GHOST, [&] {
+        return ctx->mixed() ? launch_ghost_mixed(ctx->dims, ctx->cp, ctx->ip, (float*)u, ctx->st)
+                            : launch_ghost_fp64(ctx->dims, ctx->cp, ctx->ip, (double*)u, ctx->st);
+    });
+}
+
+cudaError_t cfl(falcon_ctx* ctx) {
+    cudaError_t e = timed(ctx, KN_CFL, [&] {
+        return ctx->mixed() ? launch_cfl_mixed(ctx->dims, ctx->geom(), (const float*)ctx->U, ctx->sc, ctx->st)
+                            : launch_cfl_fp64(ctx->dims, ctx->geom(), (const double*)ctx->U, ctx->sc, ctx->st);
+    });
+    if (e != cudaSuccess) return e;
+    return timed(ctx, KN_FIN, [&] { return launch_finalize_dt(ctx->sc, (int)ctx->steps_done, ctx->st); });
+}
+
+// One ModAdvance_rk4 (3_6/ModAdvance.f90:18-112) as a kernel sequence.
+cudaError_t enqueue_step(falcon_ctx* ctx) {
+    cudaError_t e = cfl(ctx);
+    if (e != cudaSuccess) return e;
+    for (int s = 1; s <= 4; ++s) {
+        void* in = (s == 1) ? ctx->U : ctx->RK;
+        void* out = (s < 4) ? ctx->RK : ctx->U;
+        e = timed(ctx, KN_STAGE, [&] {
+            return ctx->mixed()
+                       ? launch_stage_mixed(ctx->dims, ctx->geom(), (const float*)in, (const float*)ctx->U,
+                                            (float*)out, s, s == 1, ctx->sc, 1, ctx->st)
+                       : launch_stage_fp64(ctx->dims, ctx->geom(), (const double*)in, (const double*)ctx->U,
+                                           (double*)out, s, s == 1, ctx->sc, 1, ctx->st);
+        });
+        if (e != cudaSuccess) return e;
+        e = ghost(ctx, out);
+        if (e != cudaSuccess) return e;
+    }
+    e = timed(ctx, KN_DIFF, [&] {
+        return ctx->mixed() ? launch_diffusion_mixed(ctx->dims, ctx->geom(), (float*)ctx->U, ctx->sc, ctx->st)
+                            : launch_diffusion_fp64(ctx->dims, ctx->geom(), (double*)ctx->U, ctx->sc, ctx->st);
+    });
+    if (e != cudaSuccess) return e;
+    return ghost(ctx, ctx->U);
+}
+
+int check_nan(falcon_ctx* ctx) {
+    int32_t flag = 0, stp = -1;
+    cudaError_t e = cudaMemcpy(&flag, &ctx->sc->nan_flag, sizeof(int32_t), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "nan flag");
+    cudaMemcpy(&stp, &ctx->sc->nan_step, sizeof(int32_t), cudaMemcpyDeviceToHost);
+    if (flag) {
+        char buf[128];
+        snprintf(buf, sizeof buf, "NaN detected in the state at the start of step %d", stp);
+        ctx->err = buf;
+        return FALCON_ERR_NAN_DETECTED;
+    }
+    return FALCON_OK;
+}
+
+// global element offset of var 0 of padded cell (i,j,k) (Fortran indices) of block b
+inline int64_t cell_off(const Grid& g, int b, int i, int j, int k) {
+    return (int64_t)b * NV * g.ncell + ((int64_t)(k + 1) * g.njp + (j + 1)) * g.nip + (i + 1);
+}
+
+int setup_device(falcon_ctx* ctx) {
+    const Grid& g = ctx->grid;
+    const int nb = g.nblocks;
+    if ((int64_t)nb * NV * g.ncell >= (int64_t)INT32_MAX) return ctx->fail(FALCON_ERR_INVALID_ARG, "grid too large for 32-bit offsets");
+    const bool sup = (g.ni == 8 && g.nj == 8 && g.nk == 8) || (g.ni == 16 && g.nj == 16 && g.nk == 16);
+    if (!sup) return ctx->fail(FALCON_ERR_INVALID_ARG, "device kernels are built for 8^3 and 16^3 blocks");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return ctx->fail(FALCON_ERR_NO_DEVICE, "no CUDA device");
+    if (ctx->cfg.device >= ndev) return ctx->fail(FALCON_ERR_INVALID_ARG, "device ordinal out of range");
+    CK(cudaSetDevice(ctx->cfg.device), "cudaSetDevice");
+    ctx->device = ctx->cfg.device;
+    CK(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking), "stream");
+    CK(cudaEventCreate(&ctx->t0), "event");
+    CK(cudaEventCreate(&ctx->t1), "event");
+    ctx->dims = StepDims{nb, g.ni, g.nj, g.nk, g.nip, g.njp, g.nkp, g.ncell};
+    ctx->elem = ctx->mixed() ? 4 : 8;
+    const size_t sbytes = (size_t)nb * NV * g.ncell * ctx->elem;
+    CK(ctx->alloc(&ctx->U, sbytes), "alloc U");
+    CK(ctx->alloc(&ctx->RK, sbytes), "alloc RK");
+    CK(cudaMemsetAsync(ctx->U, 0, sbytes, ctx->st), "memset");
+    CK(cudaMemsetAsync(ctx->RK, 0, sbytes, ctx->st), "memset");
+
+    // geometry and background tables (3_6/ModBlock.f90:188-265, 288-438)
+    std::vector<double> gi((size_t)nb * GI_COUNT * g.nip), gj((size_t)nb * GJ_COUNT * g.njp), gs((size_t)nb * GS_COUNT);
+    const double ratio = ctx->cfg.phys.heating_ratio;
+    for (int b = 0; b < nb; ++b) {
+        double* I = &gi[(size_t)b * GI_COUNT * g.nip];
+        const double* P = &g.prof[(size_t)b * FALCON_NPROF * g.nip];
+        for (int i = 0; i < g.nip; ++i) {
+            const double r = g.xi[(size_t)b * g.nip + i];
+            const double gg = P[0 * g.nip + i], rho0 = P[1 * g.nip + i], p0 = P[2 * g.nip + i], T0 = P[3 * g.nip + i];
+            const double g1 = P[4 * g.nip + i], g3 = P[5 * g.nip + i];
+            const double heat = P[6 * g.nip + i] + P[7 * g.nip + i], Xi = P[8 * g.nip + i];
+            const double p0r0 = p0 / rho0, rho0T0 = rho0 * T0;
+            I[GI_R * g.nip + i] = r;
+            I[GI_R2 * g.nip + i] = r * r;
+            I[GI_RINV * g.nip + i] = 1. / r;
+            I[GI_R2INV * g.nip + i] = 1. / (r * r);
+            I[GI_A1 * g.nip + i] = g1 * p0r0;
+            I[GI_A2 * g.nip + i] = (g3 - 1.0) * rho0T0;
+            I[GI_RHO0 * g.nip + i] = rho0;
+            I[GI_RHO0INV * g.nip + i] = 1. / rho0;
+            I[GI_GOR0 * g.nip + i] = gg / rho0;
+            I[GI_HEAT * g.nip + i] = ratio * heat / rho0T0;
+            I[GI_XI2INV * g.nip + i] = 1.0 / (Xi * Xi);
+            I[GI_CS * g.nip + i] = 1. / Xi * std::sqrt(g1 * p0r0);
+        }
+        double* J = &gj[(size_t)b * GJ_COUNT * g.njp];
+        for (int j = 0; j < g.njp; ++j) {
+            const double t = g.xj[(size_t)b * g.njp + j];
+            J[GJ_SIN * g.njp + j] = std::sin(t);
+            J[GJ_SININV * g.njp + j] = 1. / std::sin(t);
+            J[GJ_COT * g.njp + j] = std::cos(t) / std::sin(t);
+        }
+        double* S = &gs[(size_t)b * GS_COUNT];
+        const double c = (double)(1.0f / 12.0f);   // the FP32 constant 1./12. of ModDerivative
+        S[GS_C1] = c / g.dx[3 * b];
+        S[GS_C2] = c / g.dx[3 * b + 1];
+        S[GS_C3] = c / g.dx[3 * b + 2];
+        S[GS_DXI] = g.dx[3 * b];
+        S[GS_DXJ] = g.dx[3 * b + 1];
+        S[GS_DXK] = g.dx[3 * b + 2];
+    }
+    std::vector<float> gif(gi.begin(), gi.end()), gjf(gj.begin(), gj.end()), gsf(gs.begin(), gs.end());
+    CK(ctx->alloc(&ctx->gi, gi.size() * 8), "alloc gi");
+    CK(ctx->alloc(&ctx->gj, gj.size() * 8), "alloc gj");
+    CK(ctx->alloc(&ctx->gs, gs.size() * 8), "alloc gs");
+    CK(ctx->alloc(&ctx->gi_f, gif.size() * 4), "alloc gi_f");
+    CK(ctx->alloc(&ctx->gj_f, gjf.size() * 4), "alloc gj_f");
+    CK(ctx->alloc(&ctx->gs_f, gsf.size() * 4), "alloc gs_f");
+    CK(ctx->alloc(&ctx->flags, (size_t)nb * 4), "alloc flags");
+    CK(cudaMemcpy(ctx->gi, gi.data(), gi.size() * 8, cudaMemcpyHostToDevice), "upload gi");
+    CK(cudaMemcpy(ctx->gj, gj.data(), gj.size() * 8, cudaMemcpyHostToDevice), "upload gj");
+    CK(cudaMemcpy(ctx->gs, gs.data(), gs.size() * 8, cudaMemcpyHostToDevice), "upload gs");
+    CK(cudaMemcpy(ctx->gi_f, gif.data(), gif.size() * 4, cudaMemcpyHostToDevice), "upload gi_f");
+    CK(cudaMemcpy(ctx->gj_f, gjf.data(), gjf.size() * 4, cudaMemcpyHostToDevice), "upload gj_f");
+    CK(cudaMemcpy(ctx->gs_f, gsf.data(), gsf.size() * 4, cudaMemcpyHostToDevice), "upload gs_f");
+    CK(cudaMemcpy(ctx->flags, g.flags.data(), (size_t)nb * 4, cudaMemcpyHostToDevice), "upload flags");
+
+    // ghost lists: exact same-panel copies (sorted by target for coalesced
+    // writes) and the rest (trilinear and/or rotated)
+    std::vector<std::pair<int32_t, int32_t>> copies;
+    std::vector<int32_t> idst, isrc;
+    std::vector<double> iw, irot;
+    std::vector<uint8_t> ikind;
+    for (const auto& e : g.ghosts) {
+        const int32_t d = (int32_t)cell_off(g, e.e.tblock, e.e.ti, e.e.tj, e.e.tk);
+        const int32_t s = (int32_t)cell_off(g, e.e.sblock, e.i0, e.j0, e.k0);
+        if (e.copy && !e.rotate) { copies.push_back({d, s}); continue; }
+        idst.push_back(d);
+        isrc.push_back(s);
+        iw.insert(iw.end(), {e.w[0], e.w[1], e.w[2]});
+        irot.insert(irot.end(), {e.rotate ? e.rot[0] : 0.0, e.rotate ? e.rot[1] : 0.0});
+        ikind.push_back((uint8_t)((e.copy ? 0 : 1) | (e.rotate ? 2 : 0)));
+    }
+    std::sort(copies.begin(), copies.end());
+    std::vector<int32_t> cdst(copies.size()), csrc(copies.size());
+    for (size_t q = 0; q < copies.size(); ++q) { cdst[q] = copies[q].first; csrc[q] = copies[q].second; }
+    CK(ctx->alloc(&ctx->cp_dst, cdst.size() * 4), "alloc ghosts");
+    CK(ctx->alloc(&ctx->cp_src, csrc.size() * 4), "alloc ghosts");
+    CK(ctx->alloc(&ctx->ip_dst, idst.size() * 4), "alloc ghosts");
+    CK(ctx->alloc(&ctx->ip_src, isrc.size() * 4), "alloc ghosts");
+    CK(ctx->alloc(&ctx->ip_w, iw.size() * 8), "alloc ghosts");
+    CK(ctx->alloc(&ctx->ip_rot, irot.size() * 8), "alloc ghosts");
+    CK(ctx->alloc(&ctx->ip_kind, ikind.size()), "alloc ghosts");
+    if (!cdst.empty()) {
+        CK(cudaMemcpy(ctx->cp_dst, cdst.data(), cdst.size() * 4, cudaMemcpyHostToDevice), "upload ghosts");
+        CK(cudaMemcpy(ctx->cp_src, csrc.data(), csrc.size() * 4, cudaMemcpyHostToDevice), "upload ghosts");
+    }
+    if (!idst.empty()) {
+        CK(cudaMemcpy(ctx->ip_dst, idst.data(), idst.size() * 4, cudaMemcpyHostToDevice), "upload ghosts");
+        CK(cudaMemcpy(ctx->ip_src, isrc.data(), isrc.size() * 4, cudaMemcpyHostToDevice), "upload ghosts");
+        CK(cudaMemcpy(ctx->ip_w, iw.data(), iw.size() * 8, cudaMemcpyHostToDevice), "upload ghosts");
+        CK(cudaMemcpy(ctx->ip_rot, irot.data(), irot.size() * 8, cudaMemcpyHostToDevice), "upload ghosts");
+        CK(cudaMemcpy(ctx->ip_kind, ikind.data(), ikind.size(), cudaMemcpyHostToDevice), "upload ghosts");
+    }
+    ctx->cp = GhostCopyList{(int64_t)cdst.size(), ctx->cp_dst, ctx->cp_src};
+    ctx->ip = GhostInterpList{(int64_t)idst.size(), ctx->ip_dst, ctx->ip_src, ctx->ip_w, ctx->ip_rot, ctx->ip_kind};
+
+    StepScalars s0{};
+    s0.min_ratio_bits = 0x7FF0000000000000ull;
+    s0.cfl = ctx->cfg.phys.cfl;
+    s0.nan_step = -1;
+    CK(ctx->alloc(&ctx->sc, sizeof(StepScalars)), "alloc scalars");
+    CK(cudaMemcpy(ctx->sc, &s0, sizeof s0, cudaMemcpyHostToDevice), "upload scalars");
+    CK(cudaStreamSynchronize(ctx->st), "sync");
+    ctx->on_device = true;
+    return FALCON_OK;
+}
+
+int need_device(falcon_ctx* ctx) {
+    if (!ctx) return FALCON_ERR_INVALID_ARG;
+    if (!ctx->on_device) return ctx->fail(FALCON_ERR_NO_DEVICE, "context was created without a device");
+    cudaSetDevice(ctx->device);
+    return FALCON_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int falcon_create(falcon_ctx** out, const falcon_config* cfg) {
+    if (!out || !cfg) return FALCON_ERR_INVALID_ARG;
+    falcon_ctx* ctx = new falcon_ctx();
+    *out = ctx;
+    ctx->cfg = *cfg;
+    if (cfg->precision != FALCON_PREC_FP64 && cfg->precision != FALCON_PREC_MIXED)
+        return ctx->fail(FALCON_ERR_INVALID_ARG, "unknown precision mode");
+    if (!(cfg->phys.cfl > 0.0)) return ctx->fail(FALCON_ERR_INVALID_ARG, "cfl must be positive");
+    std::string e = ctx->grid.build(*cfg);
+    if (!e.empty()) return ctx->fail(e.find("owner") != std::string::npos ? FALCON_ERR_UNCOVERED_GHOST : FALCON_ERR_INVALID_ARG, e);
+    if (cfg->device < 0) return FALCON_OK;
+    return setup_device(ctx);
+}
+
+void falcon_destroy(falcon_ctx* ctx) {
+    if (!ctx) return;
+    if (ctx->on_device) {
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->st);
+        if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+        for (auto& r : ctx->pending) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+        for (auto e : ctx->pool) cudaEventDestroy(e);
+        for (void* p : ctx->allocs) cudaFree(p);
+        if (ctx->t0) cudaEventDestroy(ctx->t0);
+        if (ctx->t1) cudaEventDestroy(ctx->t1);
+        cudaStreamDestroy(ctx->st);
+    }
+    delete ctx;
+}
+
+int falcon_last_error(const falcon_ctx* ctx, char* buf, size_t len) {
+    if (!ctx || !buf || len == 0) return FALCON_ERR_INVALID_ARG;
+    snprintf(buf, len, "%s", ctx->err.c_str());
+    return FALCON_OK;
+}
+
+int falcon_num_blocks(const falcon_ctx* ctx, int32_t* nb, int32_t* ny) {
+    if (!ctx || !nb || !ny) return FALCON_ERR_INVALID_ARG;
+    *nb = ctx->grid.nblocks;
+    *ny = ctx->grid.nblocks_yin;
+    return FALCON_OK;
+}
+
+int falcon_block_ranges(const falcon_ctx* ctx, double* r) {
+    if (!ctx || !r) return FALCON_ERR_INVALID_ARG;
+    std::memcpy(r, ctx->grid.ranges.data(), ctx->grid.ranges.size() * sizeof(double));
+    return FALCON_OK;
+}
+
+int falcon_block_flags(const falcon_ctx* ctx, int32_t* f) {
+    if (!ctx || !f) return FALCON_ERR_INVALID_ARG;
+    std::memcpy(f, ctx->grid.flags.data(), ctx->grid.flags.size() * sizeof(int32_t));
+    return FALCON_OK;
+}
+
+int falcon_get_background(const falcon_ctx* ctx, double* p) {
+    if (!ctx || !p) return FALCON_ERR_INVALID_ARG;
+    std::memcpy(p, ctx->grid.prof.data(), ctx->grid.prof.size() * sizeof(double));
+    return FALCON_OK;
+}
+
+int falcon_ghost_count(const falcon_ctx* ctx, int64_t* n) {
+    if (!ctx || !n) return FALCON_ERR_INVALID_ARG;
+    *n = (int64_t)ctx->grid.ghosts.size();
+    return FALCON_OK;
+}
+
+int falcon_ghost_map(const falcon_ctx* ctx, falcon_ghost_entry* out, int64_t cap) {
+    if (!ctx || !out) return FALCON_ERR_INVALID_ARG;
+    if (cap < (int64_t)ctx->grid.ghosts.size()) return FALCON_ERR_BOUNDS;
+    for (size_t q = 0; q < ctx->grid.ghosts.size(); ++q) out[q] = ctx->grid.ghosts[q].e;
+    return FALCON_OK;
+}
+
+int falcon_upload_state(falcon_ctx* ctx, const double* u) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    if (!u) return ctx->fail(FALCON_ERR_INVALID_ARG, "null state");
+    const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
+    if (ctx->mixed()) {
+        // FP64 host array -> device staging -> FP32 state (conversion on the GPU)
+        if (!ctx->stage64) CK(ctx->alloc(&ctx->stage64, n * 8), "alloc staging");
+        CK(cudaMemcpyAsync(ctx->stage64, u, n * 8, cudaMemcpyHostToDevice, ctx->st), "upload");
+        CK(launch_convert_state(ctx->stage64, (float*)ctx->U, (int64_t)n, ctx->st), "upload convert");
+    } else {
+        CK(cudaMemcpyAsync(ctx->U, u, n * 8, cudaMemcpyHostToDevice, ctx->st), "upload");
+    }
+    CK(cudaStreamSynchronize(ctx->st), "upload");
+    return FALCON_OK;
+}
+
+int falcon_download_state(falcon_ctx* ctx, double* u) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    if (!u) return ctx->fail(FALCON_ERR_INVALID_ARG, "null state");
+    const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
+    if (ctx->mixed()) {
+        if (!ctx->stage64) CK(ctx->alloc(&ctx->stage64, n * 8), "alloc staging");
+        CK(launch_widen_state((const float*)ctx->U, ctx->stage64, (int64_t)n, ctx->st), "download convert");
+        CK(cudaMemcpyAsync(u, ctx->stage64, n * 8, cudaMemcpyDeviceToHost, ctx->st), "download");
+    } else {
+        CK(cudaMemcpyAsync(u, ctx->U, n * 8, cudaMemcpyDeviceToHost, ctx->st), "download");
+    }
+    CK(cudaStreamSynchronize(ctx->st), "download");
+    return FALCON_OK;
+}
+
+int falcon_pin_host(falcon_ctx* ctx, void* p, size_t bytes) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    if (!p || !bytes) return ctx->fail(FALCON_ERR_INVALID_ARG, "null buffer");
+    CK(cudaHostRegister(p, bytes, cudaHostRegisterDefault), "cudaHostRegister");
+    return FALCON_OK;
+}
+
+int falcon_unpin_host(falcon_ctx* ctx, void* p) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    CK(cudaHostUnregister(p), "cudaHostUnregister");
+    return FALCON_OK;
+}
+
+int falcon_init_synthetic(falcon_ctx* ctx, int32_t kind, uint64_t seed, double mach) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    if (kind < 0 || kind > 1) return ctx->fail(FALCON_ERR_INVALID_ARG, "unknown synthetic kind");
+    std::string e = synth_initial_state(ctx->grid, ctx->geom(), ctx->U, ctx->mixed(), kind, seed, mach, ctx->st);
+    if (!e.empty()) return ctx->fail(FALCON_ERR_CUDA, e);
+    CK(cudaStreamSynchronize(ctx->st), "init");
+    return FALCON_OK;
+}
+
+int falcon_exchange(falcon_ctx* ctx) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    CK(ghost(ctx, ctx->U), "ghost fill");
+    CK(cudaStreamSynchronize(ctx->st), "ghost fill");
+    collect(ctx);
+    return FALCON_OK;
+}
+
+int falcon_timestep(falcon_ctx* ctx, double* dt_out) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    CK(cfl(ctx), "cfl");
+    double dt = 0;
+    CK(cudaMemcpyAsync(&dt, &ctx->sc->dt, sizeof dt, cudaMemcpyDeviceToHost, ctx->st), "dt");
+    CK(cudaStreamSynchronize(ctx->st), "dt");
+    collect(ctx);
+    if (dt_out) *dt_out = dt;
+    return check_nan(ctx);
+}
+
+static int run(falcon_ctx* ctx, int32_t n) {
+    if (ctx->ktiming) {
+        for (int32_t s = 0; s < n; ++s) {
+            CK(enqueue_step(ctx), "step");
+            ++ctx->steps_done;
+        }
+        return FALCON_OK;
+    }
+    if (!ctx->graph) {
+        cudaGraph_t gr;
+        CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal), "capture");
+        cudaError_t e = enqueue_step(ctx);
+        cudaError_t e2 = cudaStreamEndCapture(ctx->st, &gr);
+        if (e != cudaSuccess) return ctx->cuda_fail(e, "capture step");
+        if (e2 != cudaSuccess) return ctx->cuda_fail(e2, "end capture");
+        CK(cudaGraphInstantiate(&ctx->graph, gr, 0), "instantiate");
+        cudaGraphDestroy(gr);
+    }
+    for (int32_t s = 0; s < n; ++s) {
+        CK(cudaGraphLaunch(ctx->graph, ctx->st), "graph launch");
+        ++ctx->steps_done;
+    }
+    return FALCON_OK;
+}
+
+int falcon_step_rk4(falcon_ctx* ctx, double* dt_out) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    rc = run(ctx, 1);
+    if (rc) return rc;
+    if (dt_out) {
+        CK(cudaMemcpyAsync(dt_out, &ctx->sc->dt, sizeof(double), cudaMemcpyDeviceToHost, ctx->st), "dt");
+        CK(cudaStreamSynchronize(ctx->st), "dt");
+        collect(ctx);
+        return check_nan(ctx);
+    }
+    return FALCON_OK;
+}
+
+int falcon_run_steps(falcon_ctx* ctx, int32_t nsteps) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    if (nsteps < 0) return ctx->fail(FALCON_ERR_INVALID_ARG, "nsteps < 0");
+    return run(ctx, nsteps);
+}
+
+int falcon_synchronize(falcon_ctx* ctx) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(ctx->st), "synchronize");
+    collect(ctx);
+    return check_nan(ctx);
+}
+
+int falcon_set_kernel_timing(falcon_ctx* ctx, int32_t on) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    ctx->ktiming = on != 0;
+    return FALCON_OK;
+}
+
+int falcon_kernel_stats(falcon_ctx* ctx, char* names, size_t names_len, double* ms, int64_t* launches, int32_t cap,
+                        int32_t* n) {
+    if (!ctx || !n) return FALCON_ERR_INVALID_ARG;
+    if (ctx->on_device) { cudaStreamSynchronize(ctx->st); collect(ctx); }
+    *n = KN_COUNT;
+    std::string all;
+    for (int k = 0; k < KN_COUNT; ++k) {
+        all += kKernelNames[k];
+        all += "\n";
+        if (k < cap) {
+            if (ms) ms[k] = ctx->kms[k];
+            if (launches) launches[k] = ctx->kcount[k];
+        }
+    }
+    if (names && names_len) snprintf(names, names_len, "%s", all.c_str());
+    return FALCON_OK;
+}
+
+int falcon_reset_kernel_stats(falcon_ctx* ctx) {
+    if (!ctx) return FALCON_ERR_INVALID_ARG;
+    if (ctx->on_device) { cudaStreamSynchronize(ctx->st); collect(ctx); }
+    for (int k = 0; k < KN_COUNT; ++k) { ctx->kms[k] = 0; ctx->kcount[k] = 0; }
+    return FALCON_OK;
+}
+
+int falcon_timer_start(falcon_ctx* ctx) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    CK(cudaEventRecord(ctx->t0, ctx->st), "timer");
+    return FALCON_OK;
+}
+
+int falcon_timer_stop(falcon_ctx* ctx, double* ms) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    CK(cudaEventRecord(ctx->t1, ctx->st), "timer");
+    CK(cudaEventSynchronize(ctx->t1), "timer");
+    float f = 0.f;
+    CK(cudaEventElapsedTime(&f, ctx->t0, ctx->t1), "timer");
+    if (ms) *ms = f;
+    collect(ctx);
+    return FALCON_OK;
+}
+
+int falcon_device_bytes(const falcon_ctx* ctx, int64_t* bytes) {
+    if (!ctx || !bytes) return FALCON_ERR_INVALID_ARG;
+    *bytes = ctx->dev_bytes;
+    return FALCON_OK;
+}
+
+}  // extern "C"

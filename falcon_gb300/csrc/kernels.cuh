@@ -1,0 +1,118 @@
+// kernels.cuh -- device kernels of one RK4 step (templates).
+//
+// Instantiated twice:
+//   mhd_fp64.cu  (T = double, compiled with -fmad=false): every operation in the
+//                reference's order, bit-comparable with the CPU oracle;
+//   mhd_mixed.cu (T = float): FP32 state and stencil RHS, p1 assembled in FP64.
+//
+// Data layout in HBM (one state buffer):
+//   u[b][v][kp][jp][ip], ip fastest, padded extents nip=ni+4 etc. This is the
+//   reference's per-block Fortran array primitive(i,j,k,var) laid end to end
+//   (3_6/ModBlock.f90:275-277), so a block uploads/downloads with one memcpy.
+//
+// Stencil kernels run one CTA per block. The CTA owns an (i,j) interior column
+// per thread (KPAR columns deep in k) and marches in k with a ring of KPAR+4
+// shared-memory planes holding all 8 variables: every padded plane is read
+// from HBM exactly once, and because a plane is only overwritten after the
+// ring has moved past it, stages and the diffusion pass update in place.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace falcon {
+
+enum { V_RHO1 = 0, V_VR = 1, V_VT = 2, V_VP = 3, V_BR = 4, V_BT = 5, V_BP = 6, V_S1 = 7, NV = 8 };
+
+// per-block radial (i) tables, padded length nip
+enum {
+    GI_R = 0,      // r (cell centres incl. ghosts)
+    GI_R2,         // r*r
+    GI_RINV,       // 1./r
+    GI_R2INV,      // 1./(r*r)
+    GI_A1,         // gamma1 * (p0/rho0)          (p1 coefficient of rho1)
+    GI_A2,         // (gamma3-1) * (rho0*T0)      (p1 coefficient of s1)
+    GI_RHO0,       // rho0
+    GI_RHO0INV,    // 1./rho0
+    GI_GOR0,       // g/rho0
+    GI_HEAT,       // Artificial_heating_ratio*(diffusion+cooling)/(rho0*T0)
+    GI_XI2INV,     // 1./(Xi*Xi)
+    GI_CS,         // (1./Xi)*sqrt(gamma1*(p0/rho0))
+    GI_COUNT
+};
+// per-block theta (j) tables, padded length njp
+enum { GJ_SIN = 0, GJ_SININV, GJ_COT, GJ_COUNT };
+// per-block scalars
+enum { GS_C1 = 0, GS_C2, GS_C3, GS_DXI, GS_DXJ, GS_DXK, GS_COUNT };
+
+struct Geometry {
+    const double* gi;   // [b][GI_COUNT][nip]
+    const double* gj;   // [b][GJ_COUNT][njp]
+    const double* gs;   // [b][GS_COUNT]
+    const float* gi_f;  // FP32 copies for the mixed path
+    const float* gj_f;
+    const float* gs_f;
+    const int32_t* flags;  // bit0 yin, bit1 top, bit2 bottom
+};
+
+// Device-resident step scalars (written by the CFL finaliser, read by every
+// stage kernel; nothing goes back to the host inside a step).
+struct StepScalars {
+    unsigned long long min_ratio_bits;  // atomicMin accumulator of h/v_wave (positive doubles)
+    double dt;                          // CFL * min(h/v_wave), seeded with 1.e20 (FP32 literal)
+    double cfl;
+    float dt_stage_f[4];                // (float)(dt/(5-s)) for the mixed path
+    float dt_half_f;                    // (float)(0.5*dt)
+    int32_t nan_flag;                   // sticky: a NaN was seen in the state
+    int32_t nan_step;
+};
+
+struct GhostCopyList {   // ghost cells that are exact copies (all weights zero, same panel)
+    int64_t n;
+    const int32_t* dst;  // element offset of var 0 of the target ghost cell
+    const int32_t* src;  // element offset of var 0 of the source cell
+};
+struct GhostInterpList {  // trilinear (and/or Yin-Yang rotated) ghost cells
+    int64_t n;
+    const int32_t* dst;
+    const int32_t* src;     // offset of the base cell (i0,j0,k0)
+    const double* w;        // [n][3] weights wi, wj, wk
+    const double* rot;      // [n][2] rotation coefficients (0 if not rotated)
+    const uint8_t* kind;    // bit0: interpolate, bit1: rotate
+};
+
+struct StepDims {
+    int nblocks, ni, nj, nk, nip, njp, nkp, ncell;
+};
+
+// ---- launchers (defined in mhd_fp64.cu / mhd_mixed.cu) --------------------
+// stage s = 1..4; in: u_s, un: u^n, out: u_{s+1}; bc_writeback: 1 writes the
+// mirrored radial ghosts back into `in` (needed at s=1, where the diffusion
+// pass later reads them, 3_6/ModAdvance.f90:101-108)
+cudaError_t launch_stage_fp64(const StepDims& d, const Geometry& g, const double* in, const double* un,
+                              double* out, int stage, int bc_writeback, const StepScalars* sc,
+                              int heat_on, cudaStream_t st);
+cudaError_t launch_diffusion_fp64(const StepDims& d, const Geometry& g, double* u, const StepScalars* sc,
+                                  cudaStream_t st);
+cudaError_t launch_cfl_fp64(const StepDims& d, const Geometry& g, const double* u, StepScalars* sc,
+                            cudaStream_t st);
+cudaError_t launch_ghost_fp64(const StepDims& d, const GhostCopyList& cp, const GhostInterpList& ip,
+                              double* u, cudaStream_t st);
+
+cudaError_t launch_stage_mixed(const StepDims& d, const Geometry& g, const float* in, const float* un,
+                               float* out, int stage, int bc_writeback, const StepScalars* sc,
+                               int heat_on, cudaStream_t st);
+cudaError_t launch_diffusion_mixed(const StepDims& d, const Geometry& g, float* u, const StepScalars* sc,
+                                   cudaStream_t st);
+cudaError_t launch_cfl_mixed(const StepDims& d, const Geometry& g, const float* u, StepScalars* sc,
+                             cudaStream_t st);
+cudaError_t launch_ghost_mixed(const StepDims& d, const GhostCopyList& cp, const GhostInterpList& ip,
+                               float* u, cudaStream_t st);
+
+cudaError_t launch_finalize_dt(StepScalars* sc, int step_index, cudaStream_t st);
+cudaError_t launch_convert_state(const double* src, float* dst, int64_t n, cudaStream_t st);
+cudaError_t launch_widen_state(const float* src, double* dst, int64_t n, cudaStream_t st);
+
+// names of the kernels as they appear in profiles
+const char* const* kernel_names();
+
+}  // namespace falcon

@@ -1,0 +1,61 @@
+// mhd_fp64.cu -- FP64 instantiation of the step kernels.
+// Compiled with -fmad=false: no multiply-add contraction, so every result is
+// rounded exactly where the reference rounds (it is built without FMA).
+#include "launch_impl.cuh"
+
+namespace falcon {
+using impl::stage_any;
+using impl::diff_any;
+using impl::cfl_any;
+using impl::ghost_any;
+
+cudaError_t launch_stage_fp64(const StepDims& d, const Geometry& g, const double* in, const double* un, double* out,
+                              int stage, int bcw, const StepScalars* sc, int heat, cudaStream_t st) {
+    return stage_any<double>(d, g, in, un, out, stage, bcw, sc, heat, st);
+}
+cudaError_t launch_diffusion_fp64(const StepDims& d, const Geometry& g, double* u, const StepScalars* sc,
+                                  cudaStream_t st) {
+    return diff_any<double>(d, g, u, sc, st);
+}
+cudaError_t launch_cfl_fp64(const StepDims& d, const Geometry& g, const double* u, StepScalars* sc, cudaStream_t st) {
+    return cfl_any<double>(d, g, u, sc, st);
+}
+cudaError_t launch_ghost_fp64(const StepDims& d, const GhostCopyList& cp, const GhostInterpList& ip, double* u,
+                              cudaStream_t st) {
+    return ghost_any<double>(d, cp, ip, u, st);
+}
+
+// dt = min(1.e20, CFL*min(h/v_wave)) (3_6/ModTimeStep.f90:20-29); also the
+// per-stage FP32 factors of the mixed path and the reset of the accumulator.
+__global__ void k_finalize_dt(StepScalars* sc, int step_index) {
+    const double m = __longlong_as_double((long long)sc->min_ratio_bits);
+    const double dt = fmin((double)1.e20f, sc->cfl * m);
+    sc->dt = dt;
+    for (int s = 1; s <= 4; ++s) sc->dt_stage_f[s - 1] = (float)(dt / (double)(5.0f - (float)s));
+    sc->dt_half_f = (float)(0.5 * dt);
+    sc->min_ratio_bits = 0x7FF0000000000000ull;   // +inf for the next step
+    if (sc->nan_flag && sc->nan_step < 0) sc->nan_step = step_index;
+}
+cudaError_t launch_finalize_dt(StepScalars* sc, int step_index, cudaStream_t st) {
+    k_finalize_dt<<<1, 1, 0, st>>>(sc, step_index);
+    return cudaGetLastError();
+}
+
+__global__ void k_narrow(const double* s, float* d, int64_t n) {
+    for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x)
+        d[x] = (float)s[x];
+}
+__global__ void k_widen(const float* s, double* d, int64_t n) {
+    for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x)
+        d[x] = (double)s[x];
+}
+cudaError_t launch_convert_state(const double* src, float* dst, int64_t n, cudaStream_t st) {
+    k_narrow<<<1216, 256, 0, st>>>(src, dst, n);
+    return cudaGetLastError();
+}
+cudaError_t launch_widen_state(const float* src, double* dst, int64_t n, cudaStream_t st) {
+    k_widen<<<1216, 256, 0, st>>>(src, dst, n);
+    return cudaGetLastError();
+}
+
+}  // namespace falcon

@@ -1,0 +1,507 @@
+// mhd_impl.cuh -- kernel bodies shared by the FP64 and mixed instantiations.
+// Included by mhd_fp64.cu (T=double, -fmad=false) and mhd_mixed.cu (T=float).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "kernels.cuh"
+
+namespace falcon {
+namespace impl {
+
+// Precision policy. Exact: the reference's divisions stay divisions; the
+// mixed path multiplies by reciprocals tabulated on the host.
+template <class T> struct Pol;
+template <> struct Pol<double> {
+    static constexpr bool exact = true;
+    __device__ static __forceinline__ double dv(double a, double b, double binv) { return a / b; }
+    __device__ static __forceinline__ double mmthr() { return (double)1.e-30f; }
+    __device__ static __forceinline__ double mmscale() { return 1.e10; }
+};
+template <> struct Pol<float> {
+    static constexpr bool exact = false;
+    __device__ static __forceinline__ float dv(float a, float, float binv) { return a * binv; }
+    __device__ static __forceinline__ float mmthr() { return 1.e-30f; }
+    __device__ static __forceinline__ float mmscale() { return 1.e10f; }
+};
+
+// ModLinReconstruct_minmod for one value (3_6/ModLinReconstruct.f90:44-48).
+template <class T>
+__device__ __forceinline__ T minmod(T ul, T u, T ur) {
+    const T a = (ur - ul) * T(0.5);
+    const T b = T(2) * (ur - u);
+    const T c = T(2) * (u - ul);
+    T t;
+    if (Pol<T>::exact) {
+        t = fmax(T(0), a * b) * fmax(T(0), b * c) * Pol<T>::mmscale() - Pol<T>::mmthr();
+    } else {
+        // same test, factors reordered so the FP32 product stays in the normal range
+        t = (fmax(T(0), a * b) * Pol<T>::mmscale()) * fmax(T(0), b * c) - Pol<T>::mmthr();
+    }
+    const T s = copysign(T(0.5), t);
+    const T m = fmin(fmin(fabs(a), fabs(b)), fabs(c));
+    return (s + T(0.5)) * copysign(m, a);
+}
+
+template <class T> __device__ __forceinline__ const T* gi_ptr(const Geometry& g);
+template <> __device__ __forceinline__ const double* gi_ptr<double>(const Geometry& g) { return g.gi; }
+template <> __device__ __forceinline__ const float* gi_ptr<float>(const Geometry& g) { return g.gi_f; }
+template <class T> __device__ __forceinline__ const T* gj_ptr(const Geometry& g);
+template <> __device__ __forceinline__ const double* gj_ptr<double>(const Geometry& g) { return g.gj; }
+template <> __device__ __forceinline__ const float* gj_ptr<float>(const Geometry& g) { return g.gj_f; }
+template <class T> __device__ __forceinline__ const T* gs_ptr(const Geometry& g);
+template <> __device__ __forceinline__ const double* gs_ptr<double>(const Geometry& g) { return g.gs; }
+template <> __device__ __forceinline__ const float* gs_ptr<float>(const Geometry& g) { return g.gs_f; }
+
+template <class T, int NI, int NJ, int NK, int KPAR>
+struct Shape {
+    static constexpr int NG = 2, NIP = NI + 4, NJP = NJ + 4, NKP = NK + 4;
+    static constexpr int PL = NIP * NJP, W = KPAR + 4, NT = NI * NJ * KPAR;
+    static constexpr int NCELL = PL * NKP;
+    static constexpr int VPP = PL * (int)sizeof(T) / 16;   // 16-byte vectors per plane
+    static_assert((PL * sizeof(T)) % 16 == 0, "plane must be a multiple of 16 bytes");
+    static_assert(NK % KPAR == 0, "KPAR must divide NK");
+    // shared memory: A1/A2 (double) | tile[NV][W][PL] | p1[W][PL] | gi | gj | gs
+    static constexpr size_t off_tile = 2 * NIP * sizeof(double);
+    static constexpr size_t off_p1 = off_tile + (size_t)NV * W * PL * sizeof(T);
+    static constexpr size_t off_gi = off_p1 + (size_t)W * PL * sizeof(T);
+    static constexpr size_t off_gj = off_gi + (size_t)GI_COUNT * NIP * sizeof(T);
+    static constexpr size_t off_gs = off_gj + (size_t)GJ_COUNT * NJP * sizeof(T);
+    static constexpr size_t smem_stage = off_gs + GS_COUNT * sizeof(T);
+    static constexpr size_t smem_diff = off_gs + GS_COUNT * sizeof(T);   // p1 area unused but kept
+};
+
+// copy planes kp in [lo, hi) of all variables of block b into the ring
+template <class T, class S>
+__device__ __forceinline__ void load_planes(const T* blk, T* tile, int lo, int hi) {
+    const int np = hi - lo;
+    const int total = NV * np * S::VPP;
+    for (int x = threadIdx.x; x < total; x += S::NT) {
+        const int vec = x % S::VPP;
+        const int rest = x / S::VPP;
+        const int pl = rest % np;
+        const int v = rest / np;
+        const int kp = lo + pl;
+        const uint4* s = reinterpret_cast<const uint4*>(blk + ((size_t)v * S::NKP + kp) * S::PL) + vec;
+        uint4* d = reinterpret_cast<uint4*>(tile + ((size_t)v * S::W + (kp % S::W)) * S::PL) + vec;
+        *d = *s;
+    }
+}
+
+template <class T, class S>
+__device__ __forceinline__ void load_geometry(const Geometry& g, int b, T* gi, T* gj, T* gs, double* a12) {
+    const T* Gi = gi_ptr<T>(g) + (size_t)b * GI_COUNT * S::NIP;
+    const T* Gj = gj_ptr<T>(g) + (size_t)b * GJ_COUNT * S::NJP;
+    const T* Gs = gs_ptr<T>(g) + (size_t)b * GS_COUNT;
+    for (int x = threadIdx.x; x < GI_COUNT * S::NIP; x += S::NT) gi[x] = Gi[x];
+    for (int x = threadIdx.x; x < GJ_COUNT * S::NJP; x += S::NT) gj[x] = Gj[x];
+    for (int x = threadIdx.x; x < GS_COUNT; x += S::NT) gs[x] = Gs[x];
+    if (a12) {
+        const double* Gd = g.gi + (size_t)b * GI_COUNT * S::NIP;
+        for (int x = threadIdx.x; x < 2 * S::NIP; x += S::NT)
+            a12[x] = Gd[(x < S::NIP ? GI_A1 * S::NIP : GI_A2 * S::NIP - S::NIP) + x];
+    }
+}
+
+// Radial mirror boundary (3_6/ModBoundary.f90:10-55) on planes [lo,hi) of the
+// ring, whole rows including their theta ghosts; optionally written back.
+template <class T, class S>
+__device__ __forceinline__ void apply_bc(T* tile, int lo, int hi, int fl, T* wb) {
+    const bool top = fl & 2, bot = fl & 4;
+    if (!top && !bot) return;
+    const int np = hi - lo;
+    const int NI = S::NIP - 4;
+    // per variable sign: top mirrors rho1,vt,vp,s1,br; anti-mirrors vr,bt,bp.
+    // bottom mirrors rho1,vt,vp,s1,bt,bp; anti-mirrors vr,br.
+    const int total = np * S::NJP * NV * 2;
+    for (int x = threadIdx.x; x < total; x += S::NT) {
+        const int g = x & 1;
+        const int rest = x >> 1;
+        const int v = rest % NV;
+        const int rest2 = rest / NV;
+        const int j = rest2 % S::NJP;
+        const int kp = lo + rest2 / S::NJP;
+        T* row = tile + ((size_t)v * S::W + (kp % S::W)) * S::PL + j * S::NIP;
+        if (top) {
+            // Fortran i = ni+1+g <- 2*ni+1-i = ni-g ; padded index = Fortran + 1
+            const bool neg = (v == V_VR) || (v == V_BT) || (v == V_BP);
+            const T s = row[NI - g + 1];
+            const T val = neg ? -s : s;
+            row[NI + 2 + g] = val;
+            if (wb) wb[((size_t)v * S::NKP + kp) * S::PL + j * S::NIP + NI + 2 + g] = val;
+        }
+        if (bot) {
+            // Fortran i = -g <- 1-i = 1+g ; padded index = Fortran + 1
+            const bool neg = (v == V_VR) || (v == V_BR);
+            const T s = row[2 + g];
+            const T val = neg ? -s : s;
+            row[1 - g] = val;
+            if (wb) wb[((size_t)v * S::NKP + kp) * S::PL + j * S::NIP + 1 - g] = val;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// One RK stage of one block: boundary -> RHS (3_6/ModEquation.f90:24-162) ->
+// u_out = u^n + dt*R/(5-s) (3_6/ModAdvance.f90:87-93).
+template <class T, int NI, int NJ, int NK, int KPAR>
+__global__ void __launch_bounds__(NI* NJ* KPAR)
+k_stage(const T* in, const T* un, T* out, Geometry g, const StepScalars* sc, int stage, int bc_writeback,
+        int heat_on) {
+    using S = Shape<T, NI, NJ, NK, KPAR>;
+    constexpr int NIP = S::NIP, PL = S::PL, W = S::W, NCELL = S::NCELL;
+    extern __shared__ __align__(16) unsigned char smem[];
+    double* a12 = reinterpret_cast<double*>(smem);
+    T* tile = reinterpret_cast<T*>(smem + S::off_tile);
+    T* tp1 = reinterpret_cast<T*>(smem + S::off_p1);
+    T* gi = reinterpret_cast<T*>(smem + S::off_gi);
+    T* gj = reinterpret_cast<T*>(smem + S::off_gj);
+    T* gs = reinterpret_cast<T*>(smem + S::off_gs);
+
+    const int b = blockIdx.x;
+    const int fl = g.flags[b];
+    const T* blk_in = in + (size_t)b * NV * NCELL;
+    T* wb = bc_writeback ? const_cast<T*>(blk_in) : nullptr;
+    load_geometry<T, S>(g, b, gi, gj, gs, a12);
+
+    const int tid = threadIdx.x;
+    const int i = tid % NI, j = (tid / NI) % NJ, kq = tid / (NI * NJ);
+    const int ii = i + 2, jj = j + 2;
+    const T c1 = gs[GS_C1], c2 = gs[GS_C2], c3 = gs[GS_C3];
+    const T* GR = gi + GI_R * NIP;
+    const T* GR2 = gi + GI_R2 * NIP;
+    const T* GRHO0 = gi + GI_RHO0 * NIP;
+    const T* GSIN = gj + GJ_SIN * S::NJP;
+    const T rinv = gi[GI_RINV * NIP + ii], r2inv = gi[GI_R2INV * NIP + ii];
+    const T sinv = gj[GJ_SININV * S::NJP + jj], cot = gj[GJ_COT * S::NJP + jj];
+    const T sin_c = GSIN[jj];
+    const T rho0c = GRHO0[ii], rho0inv = gi[GI_RHO0INV * NIP + ii];
+    const T gor0 = gi[GI_GOR0 * NIP + ii], heat = gi[GI_HEAT * NIP + ii], xi2inv = gi[GI_XI2INV * NIP + ii];
+    const double dt = sc->dt;
+    const double divs = (double)(5.0f - (float)stage);
+    const float dtk = sc->dt_stage_f[stage - 1];
+
+    constexpr int nchunk = NK / KPAR;
+    for (int ch = 0; ch < nchunk; ++ch) {
+        const int k0 = 1 + ch * KPAR;  // first Fortran k of the chunk
+        const int lo = (ch == 0) ? 0 : k0 + 3;   // first padded plane not yet in the ring
+        const int hi = k0 + KPAR + 3;                                  // one past the last needed plane
+        __syncthreads();
+        load_planes<T, S>(blk_in, tile, lo, hi);
+        __syncthreads();
+        apply_bc<T, S>(tile, lo, hi, fl, wb);
+        __syncthreads();
+        // p1 = gamma1*(p0/rho0)*rho1 + (gamma3-1)*(rho0*T0)*s1, assembled in FP64
+        // (3_6/ModEquation.f90:40-46)
+        for (int x = tid; x < (hi - lo) * PL; x += S::NT) {
+            const int kp = lo + x / PL, c = x % PL, ic = c % NIP;
+            const int slot = kp % W;
+            const double r1 = (double)tile[(V_RHO1 * W + slot) * PL + c];
+            const double s1v = (double)tile[(V_S1 * W + slot) * PL + c];
+            tp1[slot * PL + c] = (T)(a12[ic] * r1 + a12[NIP + ic] * s1v);
+        }
+        __syncthreads();
+
+        const int k = k0 + kq;
+        const int kp = k + 1;
+        int sl[5];
+#pragma unroll
+        for (int d = 0; d < 5; ++d) sl[d] = (kp + d - 2) % W;
+        auto A = [&](int v, int di, int dj, int dk) -> T {
+            return tile[(v * W + sl[dk + 2]) * PL + (jj + dj) * NIP + ii + di];
+        };
+        auto P = [&](int di, int dj, int dk) -> T { return tp1[sl[dk + 2] * PL + (jj + dj) * NIP + ii + di]; };
+        // ModDerivative_1st_O4_3D (3_6/ModDerivative.f90:16-32)
+        auto D = [&](T c, auto f) -> T { return c * (((-f(2) + T(8) * f(1)) - T(8) * f(-1)) + f(-2)); };
+        const T vr = A(V_VR, 0, 0, 0), vt = A(V_VT, 0, 0, 0), vp = A(V_VP, 0, 0, 0);
+        const T br = A(V_BR, 0, 0, 0), bt = A(V_BT, 0, 0, 0), bp = A(V_BP, 0, 0, 0);
+        const T rho1 = A(V_RHO1, 0, 0, 0);
+
+        // Mass conservation: -div(rho0 v)/Xi^2 (3_6/ModEquation.f90:50-61, ModSpherical_div :104-159)
+        T Rrho;
+        {
+            T dA = D(c1, [&](int m) { return (GRHO0[ii + m] * A(V_VR, m, 0, 0)) * GR2[ii + m]; });
+            dA = dA * r2inv;
+            T d23 = D(c2, [&](int m) { return (rho0c * A(V_VT, 0, m, 0)) * GSIN[jj + m]; });
+            d23 = d23 + D(c3, [&](int m) { return rho0c * A(V_VP, 0, 0, m); });
+            d23 = d23 * sinv;
+            d23 = d23 * rinv;
+            Rrho = -(xi2inv * (dA + d23));
+        }
+        // A_dot_Grad_f (3_6/ModSpherical.f90:241-279)
+        auto adg = [&](int var) -> T {
+            T a = vr * D(c1, [&](int m) { return A(var, m, 0, 0); });
+            T t = vt * D(c2, [&](int m) { return A(var, 0, m, 0); });
+            a = a + t * rinv;
+            t = vp * D(c3, [&](int m) { return A(var, 0, 0, m); });
+            t = t * rinv;
+            a = a + sinv * t;
+            return a;
+        };
+        // Inertial force -(v.grad)v with curvature terms (3_6/ModSpherical.f90:281-343)
+        T Rvr, Rvt, Rvp;
+        {
+            T a1 = adg(V_VR), a2 = adg(V_VT), a3 = adg(V_VP);
+            T tmp = -(vt * vt) - vp * vp;
+            a1 = a1 + tmp * rinv;
+            tmp = -(vp * vp);
+            tmp = tmp * cot;
+            tmp = tmp + vt * vr;
+            a2 = a2 + tmp * rinv;
+            tmp = vp * vt;
+            tmp = tmp * cot;
+            tmp = tmp + vp * vr;
+            a3 = a3 + tmp * rinv;
+            Rvr = -a1; Rvt = -a2; Rvp = -a3;
+        }
+        // Pressure gradient -grad(p1)/rho0 (3_6/ModEquation.f90:79-92)
+        {
+            const T g1 = D(c1, [&](int m) { return P(m, 0, 0); });
+            T g2 = D(c2, [&](int m) { return P(0, m, 0); });
+            g2 = g2 * rinv;
+            T g3 = D(c3, [&](int m) { return P(0, 0, m); });
+            g3 = g3 * rinv;
+            g3 = g3 * sinv;
+            Rvr = Rvr - Pol<T>::dv(g1, rho0c, rho0inv);
+            Rvt = Rvt - Pol<T>::dv(g2, rho0c, rho0inv);
+            Rvp = Rvp - Pol<T>::dv(g3, rho0c, rho0inv);
+        }
+        // Lorentz force (curl B) x B / rho0 (3_6/ModEquation.f90:97-116, curl :38-102)
+        {
+            T k1 = D(c2, [&](int m) { return A(V_BP, 0, m, 0) * GSIN[jj + m]; }) -
+                   D(c3, [&](int m) { return A(V_BT, 0, 0, m); });
+            T k2 = D(c3, [&](int m) { return Pol<T>::dv(A(V_BR, 0, 0, m), sin_c, sinv); }) -
+                   D(c1, [&](int m) { return A(V_BP, m, 0, 0) * GR[ii + m]; });
+            T k3 = D(c1, [&](int m) { return A(V_BT, m, 0, 0) * GR[ii + m]; }) -
+                   D(c2, [&](int m) { return A(V_BR, 0, m, 0); });
+            k1 = k1 * rinv; k2 = k2 * rinv; k3 = k3 * rinv;
+            k1 = k1 * sinv;
+            const T x1 = k2 * bp - k3 * bt;
+            const T x2 = k3 * br - k1 * bp;
+            const T x3 = k1 * bt - k2 * br;
+            Rvr = Rvr + Pol<T>::dv(x1, rho0c, rho0inv);
+            Rvt = Rvt + Pol<T>::dv(x2, rho0c, rho0inv);
+            Rvp = Rvp + Pol<T>::dv(x3, rho0c, rho0inv);
+        }
+        // Buoyancy -(g/rho0) rho1 (3_6/ModEquation.f90:121-127)
+        Rvr = Rvr - gor0 * rho1;
+        // Entropy advection and heating (3_6/ModEquation.f90:132-151)
+        T Rs = -adg(V_S1);
+        Rs = Rs + heat;
+        (void)heat_on;
+        // Induction curl(v x B) (3_6/ModEquation.f90:154-162)
+        T RBr, RBt, RBp;
+        {
+            auto E1 = [&](int a, int bq, int c) { return A(V_VT, a, bq, c) * A(V_BP, a, bq, c) - A(V_VP, a, bq, c) * A(V_BT, a, bq, c); };
+            auto E2 = [&](int a, int bq, int c) { return A(V_VP, a, bq, c) * A(V_BR, a, bq, c) - A(V_VR, a, bq, c) * A(V_BP, a, bq, c); };
+            auto E3 = [&](int a, int bq, int c) { return A(V_VR, a, bq, c) * A(V_BT, a, bq, c) - A(V_VT, a, bq, c) * A(V_BR, a, bq, c); };
+            T q1 = D(c2, [&](int m) { return E3(0, m, 0) * GSIN[jj + m]; }) - D(c3, [&](int m) { return E2(0, 0, m); });
+            T q2 = D(c3, [&](int m) { return Pol<T>::dv(E1(0, 0, m), sin_c, sinv); }) -
+                   D(c1, [&](int m) { return E3(m, 0, 0) * GR[ii + m]; });
+            T q3 = D(c1, [&](int m) { return E2(m, 0, 0) * GR[ii + m]; }) - D(c2, [&](int m) { return E1(0, m, 0); });
+            q1 = q1 * rinv; q2 = q2 * rinv; q3 = q3 * rinv;
+            q1 = q1 * sinv;
+            RBr = q1; RBt = q2; RBp = q3;
+        }
+
+        // stage update
+        const size_t base = (size_t)b * NV * NCELL + (size_t)kp * PL + jj * NIP + ii;
+        const T R[NV] = {Rrho, Rvr, Rvt, Rvp, RBr, RBt, RBp, Rs};
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            const T u0 = un[base + (size_t)v * NCELL];
+            T o;
+            if (Pol<T>::exact) o = (T)((double)u0 + (dt * (double)R[v]) / divs);
+            else o = fmaf((float)dtk, (float)R[v], (float)u0);
+            out[base + (size_t)v * NCELL] = o;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Artificial diffusion with h=2 (3_6/ModDiffusion.f90:9-150) and the update
+// u += 0.5*dt*R (3_6/ModAdvance.f90:101-108), in place.
+template <class T, int NI, int NJ, int NK, int KPAR>
+__global__ void __launch_bounds__(NI* NJ* KPAR)
+k_diffusion(T* u, Geometry g, const StepScalars* sc) {
+    using S = Shape<T, NI, NJ, NK, KPAR>;
+    constexpr int NIP = S::NIP, PL = S::PL, W = S::W, NCELL = S::NCELL;
+    extern __shared__ __align__(16) unsigned char smem[];
+    T* tile = reinterpret_cast<T*>(smem + S::off_tile);
+    T* gi = reinterpret_cast<T*>(smem + S::off_gi);
+    T* gj = reinterpret_cast<T*>(smem + S::off_gj);
+    T* gs = reinterpret_cast<T*>(smem + S::off_gs);
+    const int b = blockIdx.x;
+    T* blk = u + (size_t)b * NV * NCELL;
+    load_geometry<T, S>(g, b, gi, gj, gs, nullptr);
+    const int tid = threadIdx.x;
+    const int i = tid % NI, j = (tid / NI) % NJ, kq = tid / (NI * NJ);
+    const int ii = i + 2, jj = j + 2;
+    const T* GCS = gi + GI_CS * NIP;
+    const T rc = gi[GI_R * NIP + ii];
+    const T den[3] = {gs[GS_DXI], gs[GS_DXJ] * rc, gs[GS_DXK] * rc * gj[GJ_SIN * S::NJP + jj]};
+    const double hdt = 0.5 * sc->dt;
+    const float hdt_f = sc->dt_half_f;
+    constexpr int nchunk = NK / KPAR;
+    for (int ch = 0; ch < nchunk; ++ch) {
+        const int k0 = 1 + ch * KPAR;
+        const int lo = (ch == 0) ? 0 : k0 + 3;
+        const int hi = k0 + KPAR + 3;
+        __syncthreads();
+        load_planes<T, S>(blk, tile, lo, hi);
+        __syncthreads();
+        const int kp = k0 + kq + 1;
+        int sl[5];
+#pragma unroll
+        for (int d = 0; d < 5; ++d) sl[d] = (kp + d - 2) % W;
+        auto A = [&](int v, int di, int dj, int dk) -> T {
+            return tile[(v * W + sl[dk + 2]) * PL + (jj + dj) * NIP + ii + di];
+        };
+        T R[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) R[v] = T(0);
+#pragma unroll
+        for (int dir = 0; dir < 3; ++dir) {
+            const int vd = V_VR + dir;   // velocity component along the direction
+            auto at = [&](int v, int m) -> T {
+                return dir == 0 ? A(v, m, 0, 0) : dir == 1 ? A(v, 0, m, 0) : A(v, 0, 0, m);
+            };
+            const T csm = dir == 0 ? GCS[ii - 1] : GCS[ii];
+            const T cs0 = GCS[ii];
+            const T csp = dir == 0 ? GCS[ii + 1] : GCS[ii];
+            const T cm = fabs(at(vd, -1)) + csm, c0 = fabs(at(vd, 0)) + cs0, cp = fabs(at(vd, 1)) + csp;
+#pragma unroll 1
+            for (int v = 0; v < NV; ++v) {
+                const T fm2 = at(v, -2), fm1 = at(v, -1), f0 = at(v, 0), fp1 = at(v, 1), fp2 = at(v, 2);
+                const T dm1 = minmod(fm2, fm1, f0);
+                const T d0 = minmod(fm1, f0, fp1);
+                const T dp1 = minmod(f0, fp1, fp2);
+                // face between cells -1 and 0
+                T num = ((f0 - d0 * T(0.5)) - fm1) - dm1 * T(0.5);
+                T phi = fmax(T(0), T(1) + T(2) * (num / (f0 - fm1) - T(1)));
+                T fL = -(T(0.5) * phi * num);
+                fL = fL * (c0 + cm) * T(0.5);
+                // face between cells 0 and +1
+                num = ((fp1 - dp1 * T(0.5)) - f0) - d0 * T(0.5);
+                phi = fmax(T(0), T(1) + T(2) * (num / (fp1 - f0) - T(1)));
+                T fR = -(T(0.5) * phi * num);
+                fR = fR * (cp + c0) * T(0.5);
+                R[v] = R[v] + (fL - fR) / den[dir];
+            }
+        }
+        const size_t base = (size_t)kp * PL + jj * NIP + ii;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            const T u0 = A(v, 0, 0, 0);
+            T o;
+            if (Pol<T>::exact) o = (T)((double)u0 + hdt * (double)R[v]);
+            else o = fmaf(hdt_f, (float)R[v], (float)u0);
+            blk[(size_t)v * NCELL + base] = o;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Wave speed (3_6/ModWaveSpeed.f90:8-27), h/v_wave min-reduction
+// (3_6/ModTimeStep.f90:10-30) and the NaN scan of 3_6/ModCheck.f90:12-71.
+template <class T>
+__global__ void __launch_bounds__(256) k_cfl(const T* u, Geometry g, StepScalars* sc, StepDims d) {
+    const int nint = d.ni * d.nj * d.nk;
+    const int b = blockIdx.y;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    double ratio = INFINITY;
+    int nan = 0;
+    if (q < nint) {
+        const int i = q % d.ni + 2, j = (q / d.ni) % d.nj + 2, k = q / (d.ni * d.nj) + 2;
+        const T* blk = u + (size_t)b * NV * d.ncell + ((size_t)k * d.njp + j) * d.nip + i;
+        T x[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            x[v] = blk[(size_t)v * d.ncell];
+            nan |= (x[v] != x[v]);
+        }
+        const T* Gi = gi_ptr<T>(g) + (size_t)b * GI_COUNT * d.nip;
+        const T* Gj = gj_ptr<T>(g) + (size_t)b * GJ_COUNT * d.njp;
+        const double* Gd = g.gi + (size_t)b * GI_COUNT * d.nip;
+        const double* Gs = g.gs + (size_t)b * GS_COUNT;
+        // h_LLL = min(dxi, r*dxj, r*sin(theta)*dxk) (3_6/ModBlock.f90:416-425), FP64
+        const double r = Gd[GI_R * d.nip + i];
+        const double st = g.gj[(size_t)b * GJ_COUNT * d.njp + GJ_SIN * d.njp + j];
+        const double h = fmin(fmin(Gs[GS_DXI], r * Gs[GS_DXJ]), r * st * Gs[GS_DXK]);
+        T w = Gi[GI_CS * d.nip + i] + sqrt(x[V_VR] * x[V_VR] + x[V_VT] * x[V_VT] + x[V_VP] * x[V_VP]);
+        w = w + sqrt(x[V_BR] * x[V_BR] + x[V_BT] * x[V_BT] + x[V_BP] * x[V_BP]) / sqrt(Gi[GI_RHO0 * d.nip + i]);
+        (void)Gj;
+        ratio = h / (double)w;
+        if (ratio != ratio) { nan = 1; ratio = INFINITY; }
+    }
+    // warp then block min; positive doubles order like their bit patterns
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        ratio = fmin(ratio, __shfl_xor_sync(0xffffffffu, ratio, o));
+        nan |= __shfl_xor_sync(0xffffffffu, nan, o);
+    }
+    __shared__ double wmin[8];
+    __shared__ int wnan[8];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) { wmin[wid] = ratio; wnan[wid] = nan; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = wmin[0];
+        int n = wnan[0];
+        for (int w2 = 1; w2 < (int)(blockDim.x >> 5); ++w2) { m = fmin(m, wmin[w2]); n |= wnan[w2]; }
+        atomicMin(&sc->min_ratio_bits, (unsigned long long)__double_as_longlong(m));
+        if (n) atomicOr(&sc->nan_flag, 1);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Ghost fill: the single-GPU form of ModCommunication_SendRecvGC_new
+// (3_6/ModCommunication.f90:655-795). Exact copies first, then trilinear
+// entries (3_6/ModMath.f90:283-291) with the Yin-Yang vector rotation
+// (3_6/ModYinYang.f90:58-60).
+template <class T>
+__global__ void __launch_bounds__(256) k_ghost_copy(T* u, GhostCopyList L, int ncell) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= L.n) return;
+    const int v = blockIdx.y;
+    const size_t off = (size_t)v * ncell;
+    u[(size_t)L.dst[e] + off] = u[(size_t)L.src[e] + off];
+}
+
+template <class T>
+__global__ void __launch_bounds__(128) k_ghost_interp(T* u, GhostInterpList L, int ncell, int nip, int pl) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= L.n) return;
+    const int kind = L.kind[e];
+    const size_t s = (size_t)L.src[e];
+    T val[NV];
+    if (kind & 1) {
+        const T wi = (T)L.w[3 * e], wj = (T)L.w[3 * e + 1], wk = (T)L.w[3 * e + 2];
+        const T ui = T(1) - wi, uj = T(1) - wj, uk = T(1) - wk;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            const T* f = u + s + (size_t)v * ncell;
+            val[v] = f[0] * ui * uj * uk + f[1] * wi * uj * uk + f[nip] * ui * wj * uk + f[pl] * ui * uj * wk +
+                     f[1 + nip] * wi * wj * uk + f[nip + pl] * ui * wj * wk + f[1 + pl] * wi * uj * wk +
+                     f[1 + nip + pl] * wi * wj * wk;
+        }
+    } else {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) val[v] = u[s + (size_t)v * ncell];
+    }
+    if (kind & 2) {
+        const T a = (T)L.rot[2 * e], c = (T)L.rot[2 * e + 1];
+        T x2 = val[V_BT], x3 = val[V_BP];
+        val[V_BT] = -(a * x2) - c * x3;
+        val[V_BP] = -(a * x3) + c * x2;
+        x2 = val[V_VT]; x3 = val[V_VP];
+        val[V_VT] = -(a * x2) - c * x3;
+        val[V_VP] = -(a * x3) + c * x2;
+    }
+    const size_t dd = (size_t)L.dst[e];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) u[dd + (size_t)v * ncell] = val[v];
+}
+
+}  // namespace impl
+}  // namespace falcon

@@ -1,0 +1,190 @@
+/*
+ * falcon_gb300.h -- C ABI of the GB300-native Falcon hot path.
+ *
+ * Plain C: fixed-width integers, doubles, opaque handles. No C++ or torch
+ * types cross this boundary, so an iso_c_binding shim (Fortran), ctypes
+ * (Python) or any C caller binds it directly.
+ *
+ * Conventions
+ *   - Every entry point returns int: FALCON_OK (0) or a negative FALCON_ERR_*.
+ *     No exception or longjmp crosses the ABI. falcon_last_error() returns the
+ *     message of the most recent failure on a context.
+ *   - The library owns all device memory. Host pointers are borrowed for the
+ *     duration of a call only.
+ *   - One host thread per context; a context is not re-entrant. All device work
+ *     of a context runs on one CUDA stream owned by the context.
+ *   - Block arrays use the reference's Fortran layout: primitive(i,j,k,var)
+ *     with bounds (-ng+1:ni+ng, -ng+1:nj+ng, -ng+1:nk+ng, 1:nvar), i fastest
+ *     (3_6/ModBlock.f90:275-277). Variables are rho1, vr, vt, vp, br, bt, bp, s1
+ *     (3_6/ModBlock.f90:153-162; psi is not stored, see falcon_physics).
+ *
+ * The entry points replace these reference interfaces:
+ *   falcon_create ........... YinYangTree_InitTree/ModAMR_set_grid/YinYangTree_SetAll
+ *                             (3_6/test1.f90:110-120) and ModCommunication_SetGCAll
+ *                             (3_6/ModCommunication.f90:22-64)
+ *   falcon_upload_state ..... writes Tree%LocalBlocks(:)%primitive_IV (3_6/ModBlock.f90:62)
+ *   falcon_download_state ... reads it back (for ModSave_DoAll / ModCheck)
+ *   falcon_exchange ......... ModCommunication_SendRecvGC_new(Tree,.false.)
+ *                             (3_6/ModCommunication.f90:655-795)
+ *   falcon_timestep ......... ModWaveSpeed_Dynamo + ModTimeStep_Dynamo + MPI MIN
+ *                             (3_6/ModWaveSpeed.f90:8-27, 3_6/ModTimeStep.f90:10-30,
+ *                             3_6/ModAdvance.f90:31-48)
+ *   falcon_step_rk4 ......... ModAdvance_rk4 (3_6/ModAdvance.f90:18-112)
+ */
+#ifndef FALCON_GB300_H
+#define FALCON_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define FALCON_OK                    0
+#define FALCON_ERR_INVALID_ARG      -1
+#define FALCON_ERR_CUDA             -2
+#define FALCON_ERR_NAN_DETECTED     -3  /* replaces MPI_Abort in 3_6/ModCheck.f90:38,61 */
+#define FALCON_ERR_TIMEOUT          -4
+#define FALCON_ERR_NOT_CONVERGED    -5
+#define FALCON_ERR_BOUNDS           -6
+#define FALCON_ERR_UNCOVERED_GHOST  -7  /* a non-radial ghost cell has no owner leaf */
+#define FALCON_ERR_NO_DEVICE        -8
+
+/* ---- precision modes ---------------------------------------------------- */
+/* FP64: every operation in IEEE double, no FMA contraction, same operation
+ *       order as the reference; bit-comparable with the CPU oracle.
+ * MIXED: state stored in FP32; stencil RHS and stage updates in FP32; the
+ *       linearised-EOS pressure p1 (where the background terms cancel) is
+ *       assembled in FP64; the CFL ratio, its min-reduction and dt are FP64. */
+#define FALCON_PREC_FP64   0
+#define FALCON_PREC_MIXED  1
+
+#define FALCON_MAX_AMR 16
+#define FALCON_NVAR 8
+/* number of 1D radial background profiles per block (see falcon_get_background) */
+#define FALCON_NPROF 9
+
+/* Grid/tree description: the values PARAM.in carries in #DOMAIN, #GRID,
+ * #RADIALGRID and #AMR (3_6/ModReadParameters.f90:60-106,408-483), plus a root
+ * tiling. root_tiles = {1,1,1} is the reference tree exactly; other values split
+ * each panel root once into root_tiles[0] x [1] x [2] children with the same
+ * formula YinYangTree_Divide uses for 2-way splits (3_6/ModYinYangTree.f90:245-255). */
+typedef struct falcon_tree_spec {
+    int32_t ni, nj, nk, ng;          /* cells per block, ghost layers */
+    int32_t root_tiles[3];           /* root tiling per panel (r, theta, phi) */
+    int32_t radial_levels;           /* #RADIALGRID rLevelInitial */
+    int32_t radial_option;           /* YinYangTree_Divide_r i_option (1,2,3) */
+    int32_t n_amr;                   /* #AMR nAMRs */
+    int32_t amr_divide[FALCON_MAX_AMR][3];   /* rtp_if_divide per AMR level */
+    int32_t amr_global[FALCON_MAX_AMR];      /* if_global */
+    double  amr_range[FALCON_MAX_AMR][3][2]; /* r in R_sun; theta, phi in rad */
+    double  r_range_rsun[2];         /* #DOMAIN r_range (R_sun) */
+} falcon_tree_spec;
+
+/* Physics switches of the Dynamo equations (3_6/ModEquation.f90:24-37). */
+typedef struct falcon_physics {
+    int32_t if_involve_B;            /* iEquation=1 with if_involve_B */
+    int32_t divb_option;             /* only 0 is supported (psi is not stored) */
+    double  cfl;                     /* #TIMESTEPPING CFL */
+    double  heating_ratio;           /* Artificial_heating_ratio */
+} falcon_physics;
+
+/* Synthetic background: an ideal-gas polytrope served through the same 1D
+ * profile interface as ModStratification_new_get_vars
+ * (3_6/ModStratification_new.f90:352-384). */
+typedef struct falcon_background_spec {
+    double  poly_n;                  /* polytropic index (1.5) */
+    double  density_contrast;        /* rho0(r_bottom)/rho0(r_top) (100) */
+    double  mu;                      /* mean molecular weight for T0 */
+    int32_t xi_mode;                 /* 0: Xi=1; 1: Xi=c_s/c_s(r_top) as ModStratification_new_calc_Xi */
+    int32_t pad_;
+} falcon_background_spec;
+
+typedef struct falcon_config {
+    falcon_tree_spec       tree;
+    falcon_physics         phys;
+    falcon_background_spec bg;
+    int32_t                precision; /* FALCON_PREC_* */
+    int32_t                device;    /* CUDA device ordinal */
+} falcon_config;
+
+typedef struct falcon_ctx falcon_ctx;
+
+/* One ghost-map entry: how ghost cell (ti,tj,tk) of block tblock is filled.
+ * Reference counterpart: one element of GC_source%ijk_list/xijk_list
+ * (3_6/ModBlock.f90:7-15, filled by 3_6/ModGC.f90:53-147 and
+ * 3_6/ModCommunication.f90:219-366). src_x are the ghost cell-centre
+ * coordinates converted to the source block's panel frame. Block ids are
+ * 0-based leaf numbers (iLeafNode-1); cell indices are the Fortran ones. */
+typedef struct falcon_ghost_entry {
+    int32_t tblock, ti, tj, tk;
+    int32_t sblock, pad_;
+    double  src_x[3];
+} falcon_ghost_entry;
+
+/* ---- lifetime ----------------------------------------------------------- */
+/* Builds the Yin-Yang tree, the block geometry, the background and the ghost
+ * map on the host, then allocates device state (unless device < 0, which
+ * builds the host side only: enough for the map and geometry queries). */
+int  falcon_create(falcon_ctx** out, const falcon_config* cfg);
+void falcon_destroy(falcon_ctx* ctx);
+int  falcon_last_error(const falcon_ctx* ctx, char* buf, size_t len);
+
+/* ---- host-side geometry and map queries (no GPU needed) --------------- */
+int  falcon_num_blocks(const falcon_ctx* ctx, int32_t* nblocks, int32_t* nblocks_yin);
+/* ranges[b][3][2] of each leaf block (rtp_range, 3_6/ModYinYangTree.f90:24) */
+int  falcon_block_ranges(const falcon_ctx* ctx, double* ranges);
+/* flags[b] = bit0 if_yin, bit1 if_top, bit2 if_bottom */
+int  falcon_block_flags(const falcon_ctx* ctx, int32_t* flags);
+/* prof[b][FALCON_NPROF][ni+2ng]: g, rho0, p0, T0, gamma1, gamma3, diffusion,
+ * cooling, Xi -- the outputs of ModStratification_new_get_vars at the cell
+ * centres (3_6/ModBlock.f90:232-249) */
+int  falcon_get_background(const falcon_ctx* ctx, double* prof);
+int  falcon_ghost_count(const falcon_ctx* ctx, int64_t* n);
+/* entries in the reference's order: target block ascending, then its
+ * GC_targets (first-appearance order of source leaves), then i-j-k loop order */
+int  falcon_ghost_map(const falcon_ctx* ctx, falcon_ghost_entry* out, int64_t cap);
+
+/* ---- state transfer (host pointers; blocking on the context stream) ---- */
+/* u: nblocks x (Fortran block array incl. ghosts), FP64. In MIXED mode the
+ * FP64<->FP32 conversion runs on the GPU through a device staging buffer. */
+int  falcon_upload_state(falcon_ctx* ctx, const double* u);
+int  falcon_download_state(falcon_ctx* ctx, double* u);
+/* Page-lock a host buffer so that state transfers run at full link speed
+ * (cudaHostRegister); unpin before freeing it. */
+int  falcon_pin_host(falcon_ctx* ctx, void* p, size_t bytes);
+int  falcon_unpin_host(falcon_ctx* ctx, void* p);
+/* synthetic initial condition generated on the device (seeded):
+ * kind 0: Gaussian entropy bump + dipole B (v = 0)
+ * kind 1: kind 0 plus a random-phase Kolmogorov velocity field (rms Mach mach) */
+int  falcon_init_synthetic(falcon_ctx* ctx, int32_t kind, uint64_t seed, double mach);
+
+/* ---- the hot path ------------------------------------------------------- */
+int  falcon_exchange(falcon_ctx* ctx);
+int  falcon_timestep(falcon_ctx* ctx, double* dt_out);
+/* One RK4 step + artificial diffusion. dt_out may be NULL (dt stays on the
+ * device). Returns FALCON_ERR_NAN_DETECTED if the wave-speed pass saw a NaN. */
+int  falcon_step_rk4(falcon_ctx* ctx, double* dt_out);
+/* nsteps back-to-back steps, captured as CUDA graphs after the first call. */
+int  falcon_run_steps(falcon_ctx* ctx, int32_t nsteps);
+int  falcon_synchronize(falcon_ctx* ctx);
+
+/* ---- measurement -------------------------------------------------------- */
+/* Per-kernel CUDA-event timing on the context stream (off by default). */
+int  falcon_set_kernel_timing(falcon_ctx* ctx, int32_t on);
+/* names: newline-separated kernel names; ms[i], launches[i] per kernel */
+int  falcon_kernel_stats(falcon_ctx* ctx, char* names, size_t names_len,
+                         double* ms, int64_t* launches, int32_t cap, int32_t* n);
+int  falcon_reset_kernel_stats(falcon_ctx* ctx);
+/* device-side event timing of the context stream */
+int  falcon_timer_start(falcon_ctx* ctx);
+int  falcon_timer_stop(falcon_ctx* ctx, double* ms);
+/* bytes of device memory held by the context */
+int  falcon_device_bytes(const falcon_ctx* ctx, int64_t* bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FALCON_GB300_H */

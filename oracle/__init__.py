@@ -1,0 +1,180 @@
+"""ctypes loader for the CPU oracle (oracle/falcon_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+cpu_baseline / --impl reference legs of bench.py, as the checker. The product
+package never imports this module.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "build", "liboracle.so")
+_lib = None
+
+
+def build(force=False):
+    """Compile the oracle with its Makefile (gcc, -ffp-contract=off)."""
+    if force or not os.path.exists(LIB_PATH) or (
+            os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "falcon_oracle.cpp"))):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        L.orc_create.restype = vp
+        L.orc_create.argtypes = [vp]
+        L.orc_destroy.argtypes = [vp]
+        for name in ("orc_num_blocks", "orc_block_ranges", "orc_block_flags", "orc_get_background",
+                     "orc_ghost_map", "orc_set_state", "orc_get_state", "orc_exchange",
+                     "orc_timestep", "orc_step", "orc_block_rhs", "orc_block_diffusion",
+                     "orc_block_grid"):
+            getattr(L, name).restype = C.c_int
+        L.orc_ghost_count.restype = C.c_int64
+        L.orc_ghost_count.argtypes = [vp]
+        L.orc_uncovered_ghosts.restype = C.c_int64
+        L.orc_uncovered_ghosts.argtypes = [vp]
+        L.orc_num_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Oracle:
+    """The reference step restated on the CPU, one instance per grid."""
+
+    def __init__(self, cfg):
+        self.L = lib()
+        self.cfg = cfg
+        self.h = self.L.orc_create(C.byref(cfg))
+        nb, ny = C.c_int32(), C.c_int32()
+        self.L.orc_num_blocks(C.c_void_p(self.h), C.byref(nb), C.byref(ny))
+        self.nblocks, self.nblocks_yin = nb.value, ny.value
+        t = cfg.tree
+        self.shape = (self.nblocks, 8, t.nk + 2 * t.ng, t.nj + 2 * t.ng, t.ni + 2 * t.ng)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.orc_destroy(C.c_void_p(self.h))
+            self.h = None
+
+    @property
+    def hp(self):
+        return C.c_void_p(self.h)
+
+    def block_ranges(self):
+        out = np.zeros((self.nblocks, 3, 2))
+        self.L.orc_block_ranges(self.hp, _ptr(out))
+        return out
+
+    def block_flags(self):
+        out = np.zeros(self.nblocks, dtype=np.int32)
+        self.L.orc_block_flags(self.hp, _ptr(out))
+        return out
+
+    def background(self):
+        t = self.cfg.tree
+        out = np.zeros((self.nblocks, 9, t.ni + 2 * t.ng))
+        self.L.orc_get_background(self.hp, _ptr(out))
+        return out
+
+    def ghost_count(self):
+        return int(self.L.orc_ghost_count(self.hp))
+
+    def uncovered_ghosts(self):
+        return int(self.L.orc_uncovered_ghosts(self.hp))
+
+    def ghost_map(self):
+        from falcon_gb300.config import GhostEntry
+        n = self.ghost_count()
+        arr = (GhostEntry * n)()
+        rc = self.L.orc_ghost_map(self.hp, arr, C.c_int64(n))
+        assert rc == 0
+        return ghost_entries_to_numpy(arr, n)
+
+    def set_state(self, u):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        assert u.shape == self.shape
+        self.L.orc_set_state(self.hp, _ptr(u))
+
+    def get_state(self):
+        u = np.zeros(self.shape)
+        self.L.orc_get_state(self.hp, _ptr(u))
+        return u
+
+    def exchange(self):
+        self.L.orc_exchange(self.hp)
+
+    def timestep(self):
+        dt = C.c_double()
+        self.L.orc_timestep(self.hp, C.byref(dt))
+        return dt.value
+
+    def step(self):
+        dt = C.c_double()
+        self.L.orc_step(self.hp, C.byref(dt))
+        return dt.value
+
+    def block_rhs(self, b, p):
+        t = self.cfg.tree
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        R = np.zeros((8, t.nk, t.nj, t.ni))
+        self.L.orc_block_rhs(self.hp, C.c_int32(b), _ptr(p), _ptr(R))
+        return R
+
+    def block_diffusion(self, b, p):
+        t = self.cfg.tree
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        R = np.zeros((8, t.nk, t.nj, t.ni))
+        self.L.orc_block_diffusion(self.hp, C.c_int32(b), _ptr(p), _ptr(R))
+        return R
+
+    def block_grid(self, b):
+        t = self.cfg.tree
+        xi = np.zeros(t.ni + 2 * t.ng)
+        xj = np.zeros(t.nj + 2 * t.ng)
+        xk = np.zeros(t.nk + 2 * t.ng)
+        d = np.zeros(3)
+        self.L.orc_block_grid(self.hp, C.c_int32(b), _ptr(xi), _ptr(xj), _ptr(xk), _ptr(d))
+        return xi, xj, xk, d
+
+
+def ghost_entries_to_numpy(arr, n):
+    """Structured array view of a ctypes GhostEntry array."""
+    dt = np.dtype([("tblock", "<i4"), ("ti", "<i4"), ("tj", "<i4"), ("tk", "<i4"),
+                   ("sblock", "<i4"), ("pad_", "<i4"), ("src_x", "<f8", (3,))])
+    buf = np.frombuffer((C.c_char * (n * dt.itemsize)).from_address(C.addressof(arr)), dtype=dt, count=n)
+    return buf.copy()
+
+
+def coord_conv(rtp):
+    out = np.zeros(3)
+    rtp = np.ascontiguousarray(rtp, dtype=np.float64)
+    lib().orc_coord_conv(_ptr(rtp), _ptr(out))
+    return out
+
+
+def vec_conv(rtp, v):
+    out = np.zeros(3)
+    rtp = np.ascontiguousarray(rtp, dtype=np.float64)
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    lib().orc_vec_conv(_ptr(rtp), _ptr(v), _ptr(out))
+    return out
+
+
+def set_threads(n):
+    lib().orc_set_threads(C.c_int(n))
+
+
+def num_threads():
+    return int(lib().orc_num_threads())

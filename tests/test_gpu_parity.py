@@ -1,0 +1,145 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle.
+
+FP64 mode must reproduce the oracle's state (every cell, ghosts included) to
+1e-12 relative per variable after every RK4 step; with no FMA contraction and
+the reference's operation order it is expected to be bit-identical. The mixed
+mode is checked against the FP64 GPU path (max and RMS error per variable,
+norm-wise max|d|/max|u_ref| <= 1e-6 over 100 steps).
+"""
+import numpy as np
+import pytest
+
+import falcon_gb300 as fg
+import oracle
+from falcon_gb300 import config, synth
+
+pytestmark = pytest.mark.gpu
+
+TOL_FP64 = 1e-12      # relative, norm-wise per variable
+TOL_MIXED = 1e-6
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built(built_lib):
+    return built_lib
+
+
+def _pair(mk, seed=1001):
+    cfg = mk()
+    f = fg.Falcon(cfg)
+    o = oracle.Oracle(mk())
+    u0 = synth.initial_state(cfg, o.block_ranges(), o.block_flags(), seed=seed)
+    f.upload_state(u0)
+    o.set_state(u0)
+    for x in (f, o):
+        x.exchange()
+        x.exchange()
+    return f, o
+
+
+def relerr(a, b):
+    """per-variable norm-wise error max|a-b| / max|b| over every cell."""
+    nv = a.shape[1]
+    d = np.abs(a - b).transpose(1, 0, 2, 3, 4).reshape(nv, -1).max(1)
+    s = np.abs(b).transpose(1, 0, 2, 3, 4).reshape(nv, -1).max(1)
+    return d / np.where(s > 0, s, 1.0)
+
+
+def test_exchange_matches_oracle_exactly():
+    f, o = _pair(config.tiny)
+    assert np.array_equal(f.download_state(), o.get_state())
+
+
+def test_timestep_matches_oracle_exactly():
+    f, o = _pair(config.tiny)
+    assert f.timestep() == o.timestep()
+
+
+def test_fp64_steps_tiny_bit_identical():
+    f, o = _pair(config.tiny)
+    for _ in range(3):
+        dtf = f.advance_rk4()
+        dto = o.step()
+        assert dtf == dto
+        a, b = f.download_state(), o.get_state()
+        assert np.isfinite(a).all()
+        assert np.array_equal(a, b), relerr(a, b)
+
+
+def test_fp64_ten_steps_cfg1_within_1e12():
+    """Plain FP64 Yin-Yang MHD, 864 blocks of 8^3: state after every step."""
+    f, o = _pair(config.shell_fp64_cpu)
+    worst = np.zeros(8)
+    for s in range(10):
+        dtf = f.advance_rk4()
+        dto = o.step()
+        assert abs(dtf - dto) <= TOL_FP64 * dto
+        e = relerr(f.download_state(), o.get_state())
+        worst = np.maximum(worst, e)
+        assert (e <= TOL_FP64).all(), (s, dict(zip(config.VAR_NAMES, e)))
+    print("fp64 worst relative error per var:", dict(zip(config.VAR_NAMES, worst)))
+
+
+def test_mixed_vs_fp64_gpu_100_steps():
+    """FP32 state/RHS with FP64 p1 assembly against the FP64 GPU path."""
+    mk64 = config.shell_fp64_cpu
+    mkmx = lambda **kw: config.shell_fp64_cpu(precision=config.PREC_MIXED, **kw)
+    a = fg.Falcon(mk64())
+    b = fg.Falcon(mkmx())
+    u0 = synth.initial_state(mk64(), a.block_ranges(), a.block_flags(), seed=1002)
+    for x in (a, b):
+        x.upload_state(u0)
+        x.exchange()
+        x.exchange()
+    for _ in range(100):
+        a.advance_rk4(want_dt=False)
+        b.advance_rk4(want_dt=False)
+    a.synchronize()
+    b.synchronize()
+    ua, ub = a.download_state(), b.download_state()
+    e = relerr(ub, ua)
+    rms = np.sqrt(((ub - ua) ** 2).transpose(1, 0, 2, 3, 4).reshape(8, -1).mean(1)) / \
+        np.abs(ua).transpose(1, 0, 2, 3, 4).reshape(8, -1).max(1).clip(1e-300)
+    print("mixed vs fp64 max:", dict(zip(config.VAR_NAMES, e)))
+    print("mixed vs fp64 rms:", dict(zip(config.VAR_NAMES, rms)))
+    active = np.abs(ua).reshape(ua.shape[0], 8, -1).max(axis=(0, 2)) > 0
+    assert (e[active] <= TOL_MIXED).all(), dict(zip(config.VAR_NAMES, e))
+
+
+def test_full_size_mixed_properties():
+    """21M cells, 5,184 blocks of 16^3: steps stay finite, the exchange is
+    idempotent (bit-exact), dt is positive and stable."""
+    f = fg.Falcon(config.shell_mixed_21m())
+    f.init_synthetic(kind=1, seed=1002, mach=0.01)
+    f.exchange()
+    f.exchange()
+    dts = [f.advance_rk4() for _ in range(3)]
+    assert all(d > 0 for d in dts)
+    assert max(dts) / min(dts) < 1.5
+    u1 = f.download_state()
+    f.exchange()
+    u2 = f.download_state()
+    assert np.isfinite(u1).all()
+    assert np.array_equal(u1, u2)
+
+
+def test_fp64_full_size_block16_vs_oracle_one_step():
+    """16^3 blocks in FP64: one step against the oracle on a reduced shell
+    (per panel 32 x 48 x 144 cells, 2 x 3 x 9 blocks)."""
+    mk = lambda **kw: config.make_config(block=(16, 16, 16), root_tiles=(1, 3, 9), radial_levels=1,
+                                         radial_option=1, amr=(), **kw)
+    f, o = _pair(mk)
+    dtf, dto = f.advance_rk4(), o.step()
+    assert dtf == dto
+    e = relerr(f.download_state(), o.get_state())
+    assert (e <= TOL_FP64).all(), dict(zip(config.VAR_NAMES, e))
+
+
+def test_nan_in_state_is_reported_not_trapped():
+    f, o = _pair(config.tiny)
+    u = f.download_state()
+    u[3, 7, 5, 5, 5] = np.nan
+    f.upload_state(u)
+    with pytest.raises(fg.FalconError) as e:
+        f.advance_rk4()
+    assert e.value.code == fg.ERR_NAN_DETECTED
