@@ -210,11 +210,20 @@ def run_reference(args, rank, world, dist):
     print(json.dumps(line))
 
 
+def small_config(device):
+    """Profiling case: the same shell and physics at 1/4 of the blocks per
+    panel (per panel 96 x 96 x 288 cells, 1,296 blocks of 16^3, 332 MB per
+    FP32 state buffer: larger than L2 but a few GB on the device)."""
+    from falcon_gb300 import config
+    return config.make_config(block=(16, 16, 16), root_tiles=(3, 3, 9), radial_levels=1, radial_option=1,
+                              amr=((0, 1, 1),), precision=config.PREC_MIXED, device=device)
+
+
 def run_ours(args, rank, world, local, dist):
     import falcon_gb300 as fg
     from falcon_gb300 import config
     fg.build()
-    cfg = config.shell_mixed_21m(device=local)
+    cfg = config.shell_mixed_21m(device=local) if args.workload == "full" else small_config(local)
     f = fg.Falcon(cfg)
     cells = f.interior_cells
     f.init_synthetic(kind=1, seed=1002, mach=0.01)
@@ -263,32 +272,35 @@ def run_ours(args, rank, world, local, dist):
     # ---- end to end through the C ABI with host buffers: every step uploads
     # the FP64 Fortran-layout state from pinned host memory, advances, and
     # downloads the new state (the drop-in keeps Tree%LocalBlocks authoritative)
-    host = np.empty(f.shape, dtype=np.float64)
-    f.pin_host(host)
-    f.download_state_into(host)
+    e2e_val = res_val = None
+    nbytes = 0
     k_e2e = max(1, min(args.steps, 10))
-    f.synchronize()
-    barrier(dist)
-    t0 = time.perf_counter()
-    for _ in range(k_e2e):
-        f.upload_state_raw(host)
-        f.advance_rk4(want_dt=True)
+    if not args.no_e2e:
+        host = np.empty(f.shape, dtype=np.float64)
+        f.pin_host(host)
         f.download_state_into(host)
-    e2e_s = time.perf_counter() - t0
-    barrier(dist)
-    e2e_s = reduce_max(dist, e2e_s)
-    e2e_val = reduce_sum(dist, float(cells * k_e2e)) / e2e_s
-    f.unpin_host(host)
-    nbytes = host.nbytes
-    # resident variant: the state stays on the GPU, dt comes back every step
-    t0 = time.perf_counter()
-    for _ in range(k_e2e):
-        f.advance_rk4(want_dt=True)
-    res_s = reduce_max(dist, time.perf_counter() - t0)
-    res_val = reduce_sum(dist, float(cells * k_e2e)) / res_s
+        f.synchronize()
+        barrier(dist)
+        t0 = time.perf_counter()
+        for _ in range(k_e2e):
+            f.upload_state_raw(host)
+            f.advance_rk4(want_dt=True)
+            f.download_state_into(host)
+        e2e_s = time.perf_counter() - t0
+        barrier(dist)
+        e2e_s = reduce_max(dist, e2e_s)
+        e2e_val = reduce_sum(dist, float(cells * k_e2e)) / e2e_s
+        f.unpin_host(host)
+        nbytes = host.nbytes
+        # resident variant: the state stays on the GPU, dt comes back every step
+        t0 = time.perf_counter()
+        for _ in range(k_e2e):
+            f.advance_rk4(want_dt=True)
+        res_s = reduce_max(dist, time.perf_counter() - t0)
+        res_val = reduce_sum(dist, float(cells * k_e2e)) / res_s
 
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and args.workload == "full":
         v, cores, sample = time_oracle(3, 1, budget_s=20.0)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
 
@@ -323,6 +335,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="full", choices=["full", "small"],
+                    help="small: the 1,296-block profiling case (not a bench line)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
     rank, world, local, dist = dist_setup(args.gpus)

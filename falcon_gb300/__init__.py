@@ -41,6 +41,7 @@ EXPORTS = (
     "falcon_timestep", "falcon_step_rk4", "falcon_run_steps", "falcon_synchronize",
     "falcon_set_kernel_timing", "falcon_kernel_stats", "falcon_reset_kernel_stats", "falcon_timer_start",
     "falcon_timer_stop", "falcon_device_bytes", "falcon_pin_host", "falcon_unpin_host",
+    "falcon_step_phase", "falcon_download_stage_state",
 )
 
 _lib = None
@@ -194,6 +195,14 @@ class Falcon:
 
     def run_steps(self, n):
         self._ck(self.L.falcon_run_steps(self.h, C.c_int32(n)))
+
+    def step_phase(self, phase):
+        self._ck(self.L.falcon_step_phase(self.h, C.c_int32(phase)))
+
+    def download_stage_state(self):
+        u = np.empty(self.shape)
+        self._ck(self.L.falcon_download_stage_state(self.h, _ptr(u)))
+        return u
 
     def synchronize(self):
         self._ck(self.L.falcon_synchronize(self.h))

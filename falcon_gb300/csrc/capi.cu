@@ -119,7 +119,7 @@ cudaError_t cfl(falcon_ctx* ctx) {
                             : launch_cfl_fp64(ctx->dims, ctx->geom(), (const double*)ctx->U, ctx->sc, ctx->st);
     });
     if (e != cudaSuccess) return e;
-    return timed(ctx, KN_FIN, [&] { return launch_finalize_dt(ctx->sc, (int)ctx->steps_done, ctx->st); });
+    return timed(ctx, KN_FIN, [&] { return launch_finalize_dt(ctx->sc, ctx->st); });
 }
 
 // One ModAdvance_rk4 (3_6/ModAdvance.f90:18-112) as a kernel sequence.
@@ -132,9 +132,9 @@ cudaError_t enqueue_step(falcon_ctx* ctx) {
         e = timed(ctx, KN_STAGE, [&] {
             return ctx->mixed()
                        ? launch_stage_mixed(ctx->dims, ctx->geom(), (const float*)in, (const float*)ctx->U,
-                                            (float*)out, s, s == 1, ctx->sc, 1, ctx->st)
+                                            (float*)out, s, 1, ctx->sc, 1, ctx->st)
                        : launch_stage_fp64(ctx->dims, ctx->geom(), (const double*)in, (const double*)ctx->U,
-                                           (double*)out, s, s == 1, ctx->sc, 1, ctx->st);
+                                           (double*)out, s, 1, ctx->sc, 1, ctx->st);
         });
         if (e != cudaSuccess) return e;
         e = ghost(ctx, out);
@@ -395,6 +395,8 @@ int falcon_upload_state(falcon_ctx* ctx, const double* u) {
     } else {
         CK(cudaMemcpyAsync(ctx->U, u, n * 8, cudaMemcpyHostToDevice, ctx->st), "upload");
     }
+    // primitive_rk_IV = primitive_IV, as the reference's initialisation leaves it
+    CK(cudaMemcpyAsync(ctx->RK, ctx->U, n * ctx->elem, cudaMemcpyDeviceToDevice, ctx->st), "upload");
     CK(cudaStreamSynchronize(ctx->st), "upload");
     return FALCON_OK;
 }
@@ -436,6 +438,8 @@ int falcon_init_synthetic(falcon_ctx* ctx, int32_t kind, uint64_t seed, double m
     if (kind < 0 || kind > 1) return ctx->fail(FALCON_ERR_INVALID_ARG, "unknown synthetic kind");
     std::string e = synth_initial_state(ctx->grid, ctx->geom(), ctx->U, ctx->mixed(), kind, seed, mach, ctx->st);
     if (!e.empty()) return ctx->fail(FALCON_ERR_CUDA, e);
+    const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
+    CK(cudaMemcpyAsync(ctx->RK, ctx->U, n * ctx->elem, cudaMemcpyDeviceToDevice, ctx->st), "init");
     CK(cudaStreamSynchronize(ctx->st), "init");
     return FALCON_OK;
 }
@@ -505,6 +509,50 @@ int falcon_run_steps(falcon_ctx* ctx, int32_t nsteps) {
     if (rc) return rc;
     if (nsteps < 0) return ctx->fail(FALCON_ERR_INVALID_ARG, "nsteps < 0");
     return run(ctx, nsteps);
+}
+
+int falcon_step_phase(falcon_ctx* ctx, int32_t phase) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    if (phase < 0 || phase > 5) return ctx->fail(FALCON_ERR_INVALID_ARG, "phase must be 0..5");
+    cudaError_t e = cudaSuccess;
+    if (phase == 0) {
+        e = cfl(ctx);
+    } else if (phase <= 4) {
+        const int s = phase;
+        void* in = (s == 1) ? ctx->U : ctx->RK;
+        void* out = (s < 4) ? ctx->RK : ctx->U;
+        e = ctx->mixed() ? launch_stage_mixed(ctx->dims, ctx->geom(), (const float*)in, (const float*)ctx->U,
+                                              (float*)out, s, 1, ctx->sc, 1, ctx->st)
+                         : launch_stage_fp64(ctx->dims, ctx->geom(), (const double*)in, (const double*)ctx->U,
+                                             (double*)out, s, 1, ctx->sc, 1, ctx->st);
+        if (e == cudaSuccess) e = ghost(ctx, out);
+    } else {
+        e = ctx->mixed() ? launch_diffusion_mixed(ctx->dims, ctx->geom(), (float*)ctx->U, ctx->sc, ctx->st)
+                         : launch_diffusion_fp64(ctx->dims, ctx->geom(), (double*)ctx->U, ctx->sc, ctx->st);
+        if (e == cudaSuccess) e = ghost(ctx, ctx->U);
+        if (e == cudaSuccess) ++ctx->steps_done;
+    }
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "phase");
+    CK(cudaStreamSynchronize(ctx->st), "phase");
+    collect(ctx);
+    return FALCON_OK;
+}
+
+int falcon_download_stage_state(falcon_ctx* ctx, double* u) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    if (!u) return ctx->fail(FALCON_ERR_INVALID_ARG, "null state");
+    const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
+    if (ctx->mixed()) {
+        if (!ctx->stage64) CK(ctx->alloc(&ctx->stage64, n * 8), "alloc staging");
+        CK(launch_widen_state((const float*)ctx->RK, ctx->stage64, (int64_t)n, ctx->st), "download convert");
+        CK(cudaMemcpyAsync(u, ctx->stage64, n * 8, cudaMemcpyDeviceToHost, ctx->st), "download");
+    } else {
+        CK(cudaMemcpyAsync(u, ctx->RK, n * 8, cudaMemcpyDeviceToHost, ctx->st), "download");
+    }
+    CK(cudaStreamSynchronize(ctx->st), "download");
+    return FALCON_OK;
 }
 
 int falcon_synchronize(falcon_ctx* ctx) {

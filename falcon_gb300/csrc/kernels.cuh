@@ -63,7 +63,9 @@ struct StepScalars {
     float dt_stage_f[4];                // (float)(dt/(5-s)) for the mixed path
     float dt_half_f;                    // (float)(0.5*dt)
     int32_t nan_flag;                   // sticky: a NaN was seen in the state
-    int32_t nan_step;
+    int32_t nan_step;                   // step counter value when it was first seen
+    int32_t step_counter;               // steps finalised so far (device side)
+    int32_t pad_;
 };
 
 struct GhostCopyList {   // ghost cells that are exact copies (all weights zero, same panel)
@@ -86,8 +88,9 @@ struct StepDims {
 
 // ---- launchers (defined in mhd_fp64.cu / mhd_mixed.cu) --------------------
 // stage s = 1..4; in: u_s, un: u^n, out: u_{s+1}; bc_writeback: 1 writes the
-// mirrored radial ghosts back into `in` (needed at s=1, where the diffusion
-// pass later reads them, 3_6/ModAdvance.f90:101-108)
+// mirrored radial ghosts back into `in`, as ModBoundary does in place
+// (3_6/ModBoundary.f90:10-55); the diffusion pass later reads those of u^n
+// (3_6/ModAdvance.f90:101-108)
 cudaError_t launch_stage_fp64(const StepDims& d, const Geometry& g, const double* in, const double* un,
                               double* out, int stage, int bc_writeback, const StepScalars* sc,
                               int heat_on, cudaStream_t st);
@@ -108,7 +111,7 @@ cudaError_t launch_cfl_mixed(const StepDims& d, const Geometry& g, const float* 
 cudaError_t launch_ghost_mixed(const StepDims& d, const GhostCopyList& cp, const GhostInterpList& ip,
                                float* u, cudaStream_t st);
 
-cudaError_t launch_finalize_dt(StepScalars* sc, int step_index, cudaStream_t st);
+cudaError_t launch_finalize_dt(StepScalars* sc, cudaStream_t st);
 cudaError_t launch_convert_state(const double* src, float* dst, int64_t n, cudaStream_t st);
 cudaError_t launch_widen_state(const float* src, double* dst, int64_t n, cudaStream_t st);
 

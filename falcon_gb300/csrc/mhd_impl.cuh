@@ -163,6 +163,7 @@ k_stage(const T* in, const T* un, T* out, Geometry g, const StepScalars* sc, int
     const T* blk_in = in + (size_t)b * NV * NCELL;
     T* wb = bc_writeback ? const_cast<T*>(blk_in) : nullptr;
     load_geometry<T, S>(g, b, gi, gj, gs, a12);
+    __syncthreads();   // the geometry tables are read by every thread below
 
     const int tid = threadIdx.x;
     const int i = tid % NI, j = (tid / NI) % NJ, kq = tid / (NI * NJ);
@@ -334,6 +335,7 @@ k_diffusion(T* u, Geometry g, const StepScalars* sc) {
     const int b = blockIdx.x;
     T* blk = u + (size_t)b * NV * NCELL;
     load_geometry<T, S>(g, b, gi, gj, gs, nullptr);
+    __syncthreads();   // the geometry tables are read by every thread below
     const int tid = threadIdx.x;
     const int i = tid % NI, j = (tid / NI) % NJ, kq = tid / (NI * NJ);
     const int ii = i + 2, jj = j + 2;

@@ -170,6 +170,13 @@ int  falcon_step_rk4(falcon_ctx* ctx, double* dt_out);
 /* nsteps back-to-back steps, captured as CUDA graphs after the first call. */
 int  falcon_run_steps(falcon_ctx* ctx, int32_t nsteps);
 int  falcon_synchronize(falcon_ctx* ctx);
+/* Verification: run one phase of ModAdvance_rk4 eagerly and synchronously.
+ * phase 0: wave speed + CFL dt (3_6/ModAdvance.f90:31-48); 1..4: RK stage s
+ * with its ghost exchange (:59-97); 5: artificial diffusion + exchange
+ * (:101-109). Phases 0,1,2,3,4,5 in order equal one falcon_step_rk4. */
+int  falcon_step_phase(falcon_ctx* ctx, int32_t phase);
+/* Download the stage buffer (primitive_rk_IV) in the falcon_download_state layout. */
+int  falcon_download_stage_state(falcon_ctx* ctx, double* u);
 
 /* ---- measurement -------------------------------------------------------- */
 /* Per-kernel CUDA-event timing on the context stream (off by default). */

@@ -35,13 +35,15 @@ def lib():
         for name in ("orc_num_blocks", "orc_block_ranges", "orc_block_flags", "orc_get_background",
                      "orc_ghost_map", "orc_set_state", "orc_get_state", "orc_exchange",
                      "orc_timestep", "orc_step", "orc_block_rhs", "orc_block_diffusion",
-                     "orc_block_grid"):
+                     "orc_block_grid", "orc_phase", "orc_get_stage_state"):
             getattr(L, name).restype = C.c_int
         L.orc_ghost_count.restype = C.c_int64
         L.orc_ghost_count.argtypes = [vp]
         L.orc_uncovered_ghosts.restype = C.c_int64
         L.orc_uncovered_ghosts.argtypes = [vp]
         L.orc_num_threads.restype = C.c_int
+        L.orc_dt.restype = C.c_double
+        L.orc_dt.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -124,6 +126,15 @@ class Oracle:
         dt = C.c_double()
         self.L.orc_step(self.hp, C.byref(dt))
         return dt.value
+
+    def phase(self, ph):
+        self.L.orc_phase(self.hp, C.c_int32(ph))
+        return self.L.orc_dt(self.hp)
+
+    def get_stage_state(self):
+        u = np.zeros(self.shape)
+        self.L.orc_get_stage_state(self.hp, _ptr(u))
+        return u
 
     def block_rhs(self, b, p):
         t = self.cfg.tree

@@ -314,6 +314,7 @@ struct Oracle {
     void wave_speed(Block& b);
     double timestep();
     void step();
+    void phase(int ph);
 };
 
 void Oracle::build() {
@@ -939,6 +940,53 @@ void Oracle::step() {
     exchange(false);
 }
 
+// One phase of step(): 0 wave speed + dt, 1..4 RK stage, 5 diffusion.
+void Oracle::phase(int ph) {
+    const int nint = ni * nj * nk;
+    const int nb = (int)blk.size();
+    if (ph == 0) {
+#pragma omp parallel for schedule(dynamic)
+        for (int b = 0; b < nb; ++b) wave_speed(blk[b]);
+        dt = timestep();
+        return;
+    }
+    if (ph <= 4) {
+        const int rk = ph;
+#pragma omp parallel for schedule(dynamic)
+        for (int ib = 0; ib < nb; ++ib) {
+            Block& b = blk[ib];
+            std::vector<double>& p = rk > 1 ? b.urk : b.u;
+            boundary(b, p);
+            equation(b, p);
+            std::vector<double>& out = rk < 4 ? b.urk : b.u;
+            const double div = (double)(5.0f - (float)rk);
+            for (int v = 0; v < nvar; ++v)
+                for (int k = 1; k <= nk; ++k)
+                    for (int j = 1; j <= nj; ++j)
+                        for (int i = 1; i <= ni; ++i) {
+                            int m = (int)((size_t)v * ncell) + idx(i, j, k);
+                            out[m] = b.u[m] + dt * b.R[(size_t)v * nint + iidx(i, j, k)] / div;
+                        }
+        }
+        exchange(rk < 4);
+        return;
+    }
+#pragma omp parallel for schedule(dynamic)
+    for (int ib = 0; ib < nb; ++ib) {
+        Block& b = blk[ib];
+        std::fill(b.R.begin(), b.R.end(), 0.0);
+        diffusion(b, b.u);
+        for (int v = 0; v < nvar; ++v)
+            for (int k = 1; k <= nk; ++k)
+                for (int j = 1; j <= nj; ++j)
+                    for (int i = 1; i <= ni; ++i) {
+                        int m = (int)((size_t)v * ncell) + idx(i, j, k);
+                        b.u[m] = b.u[m] + 0.5 * dt * b.R[(size_t)v * nint + iidx(i, j, k)];
+                    }
+    }
+    exchange(false);
+}
+
 }  // namespace orc
 
 // ---- C API used by the tests and by bench.py's CPU baseline -------------
@@ -1041,6 +1089,14 @@ int orc_get_state(void* h, double* u) {
     Oracle* o = (Oracle*)h;
     size_t n = (size_t)o->nvar * o->ncell;
     for (size_t b = 0; b < o->blk.size(); ++b) std::memcpy(u + n * b, o->blk[b].u.data(), n * sizeof(double));
+    return 0;
+}
+int orc_phase(void* h, int32_t ph) { ((Oracle*)h)->phase(ph); return 0; }
+double orc_dt(void* h) { return ((Oracle*)h)->dt; }
+int orc_get_stage_state(void* h, double* u) {
+    Oracle* o = (Oracle*)h;
+    size_t n = (size_t)o->nvar * o->ncell;
+    for (size_t b = 0; b < o->blk.size(); ++b) std::memcpy(u + n * b, o->blk[b].urk.data(), n * sizeof(double));
     return 0;
 }
 int orc_exchange(void* h) { ((Oracle*)h)->exchange(false); return 0; }
