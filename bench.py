@@ -245,7 +245,9 @@ def run_ours(args, rank, world, local, dist):
     ms_max = reduce_max(dist, ms)
     total_cells = reduce_sum(dist, float(cells * args.steps))
     value = total_cells / (ms_max / 1e3)
-    launches_per_step = 2 + 4 * 3 + 3
+    lists = f.ghost_list_sizes()
+    n_ghost_kernels = sum(1 for v in lists.values() if v > 0)
+    launches_per_step = 2 + 5 * (1 + n_ghost_kernels) - 1 + 1
 
     # ---- per-kernel times (events around every launch) for the roofline
     f.set_kernel_timing(True)
@@ -257,13 +259,17 @@ def run_ours(args, rank, world, local, dist):
     tot = sum(v[0] for v in stats.values()) or 1.0
     top = max(stats, key=lambda k: stats[k][0])
     avg_ms = stats[top][0] / max(stats[top][1], 1)
+    ghosts = sum(lists.values())
     per_cell = {"stage": STAGE_BYTES_PER_CELL, "diffusion": DIFF_BYTES_PER_CELL}.get(top)
+    if top == "ghost_fill":
+        # one exchange: every ghost cell reads and writes its 8 variables (FP32)
+        per_cell = ghosts * NVAR * 2 * STATE_BYTES_PER_VAR / cells
     hbm, peak_kind = peaks()
     roof = None
     if per_cell is not None:
         ach = cells * per_cell / (avg_ms / 1e3) / 1e9
         roof = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                "traffic": profile_traffic("stage_mixed_21m.txt"), "kernel": "k_stage<float,16,16,16,2>",
+                "traffic": profile_traffic("%s_mixed_21m.txt" % top), "kernel": top,
                 "algorithmic_bytes_per_launch": cells * per_cell, "avg_launch_ms": avg_ms,
                 "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind}
     step_ach = cells * BYTES_PER_CELL_STEP / (ms_max / args.steps / 1e3) / 1e9
@@ -317,6 +323,7 @@ def run_ours(args, rank, world, local, dist):
             "step_roofline": {"achieved": step_ach, "peak": hbm, "unit": "GB/s", "frac": step_ach / hbm,
                               "algorithmic_bytes_per_cell_step": BYTES_PER_CELL_STEP},
             "kernel_time_share": shares,
+            "tuning": f.tuning(), "ghost_lists": lists,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                     "mode": "state uploaded and downloaded (FP64, pinned) every step"},

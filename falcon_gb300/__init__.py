@@ -41,7 +41,12 @@ EXPORTS = (
     "falcon_timestep", "falcon_step_rk4", "falcon_run_steps", "falcon_synchronize",
     "falcon_set_kernel_timing", "falcon_kernel_stats", "falcon_reset_kernel_stats", "falcon_timer_start",
     "falcon_timer_stop", "falcon_device_bytes", "falcon_pin_host", "falcon_unpin_host",
-    "falcon_step_phase", "falcon_download_stage_state",
+    "falcon_step_phase", "falcon_download_stage_state", "falcon_ghost_list_sizes",
+    "falcon_tuning",
+    "falcon_solver_create", "falcon_solver_destroy", "falcon_solver_last_error", "falcon_solver_info",
+    "falcon_solver_problem_blocks", "falcon_solver_rhs", "falcon_solver_operator", "falcon_solver_halo_count",
+    "falcon_solver_halo_map", "falcon_solver_apply", "falcon_solver_solve", "falcon_solver_solution",
+    "falcon_solver_timestep",
 )
 
 _lib = None
@@ -230,6 +235,16 @@ class Falcon:
         ms = C.c_double()
         self._ck(self.L.falcon_timer_stop(self.h, C.byref(ms)))
         return ms.value
+
+    def tuning(self):
+        a, b = C.c_int32(), C.c_int32()
+        self._ck(self.L.falcon_tuning(self.h, C.byref(a), C.byref(b)))
+        return {"kpar_stage": a.value, "kpar_diffusion": b.value}
+
+    def ghost_list_sizes(self):
+        c = (C.c_int64 * 3)()
+        self._ck(self.L.falcon_ghost_list_sizes(self.h, c))
+        return {"copy": c[0], "linear": c[1], "trilinear": c[2]}
 
     def device_bytes(self):
         b = C.c_int64()

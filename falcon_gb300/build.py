@@ -27,6 +27,8 @@ UNITS = [
     ("synth.cu", []),
     ("capi.cu", []),
     ("host_setup.cpp", []),
+    ("solver.cu", ["-fmad=false"]),
+    ("solver_host.cpp", []),
 ]
 
 

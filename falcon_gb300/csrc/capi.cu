@@ -8,6 +8,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/falcon_gb300.h"
@@ -38,11 +39,9 @@ struct falcon_ctx {
     float *gi_f = nullptr, *gj_f = nullptr, *gs_f = nullptr;
     int32_t* flags = nullptr;
     StepScalars* sc = nullptr;
-    int32_t *cp_dst = nullptr, *cp_src = nullptr, *ip_dst = nullptr, *ip_src = nullptr;
-    double *ip_w = nullptr, *ip_rot = nullptr;
-    uint8_t* ip_kind = nullptr;
-    GhostCopyList cp{};
-    GhostInterpList ip{};
+    GhostLists gl{};
+    int64_t ghost_counts[3] = {0, 0, 0};   // copy, 1-D, general entries on the device
+    int kpar_stage = 0, kpar_diff = 0;      // chosen by the autotuner (0 = not tuned yet)
     cudaGraphExec_t graph = nullptr;
     int64_t steps_done = 0;
     int64_t dev_bytes = 0;
@@ -108,8 +107,8 @@ void collect(falcon_ctx* ctx) {
 
 cudaError_t ghost(falcon_ctx* ctx, void* u) {
     return timed(ctx, KN_GHOST, [&] {
-        return ctx->mixed() ? launch_ghost_mixed(ctx->dims, ctx->cp, ctx->ip, (float*)u, ctx->st)
-                            : launch_ghost_fp64(ctx->dims, ctx->cp, ctx->ip, (double*)u, ctx->st);
+        return ctx->mixed() ? launch_ghost_mixed(ctx->dims, ctx->gl, (float*)u, ctx->st)
+                            : launch_ghost_fp64(ctx->dims, ctx->gl, (double*)u, ctx->st);
     });
 }
 
@@ -132,20 +131,72 @@ cudaError_t enqueue_step(falcon_ctx* ctx) {
         e = timed(ctx, KN_STAGE, [&] {
             return ctx->mixed()
                        ? launch_stage_mixed(ctx->dims, ctx->geom(), (const float*)in, (const float*)ctx->U,
-                                            (float*)out, s, 1, ctx->sc, 1, ctx->st)
+                                            (float*)out, s, 1, ctx->sc, 1, ctx->kpar_stage, ctx->st)
                        : launch_stage_fp64(ctx->dims, ctx->geom(), (const double*)in, (const double*)ctx->U,
-                                           (double*)out, s, 1, ctx->sc, 1, ctx->st);
+                                           (double*)out, s, 1, ctx->sc, 1, ctx->kpar_stage, ctx->st);
         });
         if (e != cudaSuccess) return e;
         e = ghost(ctx, out);
         if (e != cudaSuccess) return e;
     }
     e = timed(ctx, KN_DIFF, [&] {
-        return ctx->mixed() ? launch_diffusion_mixed(ctx->dims, ctx->geom(), (float*)ctx->U, ctx->sc, ctx->st)
-                            : launch_diffusion_fp64(ctx->dims, ctx->geom(), (double*)ctx->U, ctx->sc, ctx->st);
+        return ctx->mixed() ? launch_diffusion_mixed(ctx->dims, ctx->geom(), (float*)ctx->U, ctx->sc, ctx->kpar_diff, ctx->st)
+                            : launch_diffusion_fp64(ctx->dims, ctx->geom(), (double*)ctx->U, ctx->sc, ctx->kpar_diff, ctx->st);
     });
     if (e != cudaSuccess) return e;
     return ghost(ctx, ctx->U);
+}
+
+// Autotuner: time every instantiated k-chunk depth of the stage and diffusion
+// kernels on this grid and keep the fastest. Runs on the stage buffer only
+// (dead between steps: stage 1 rewrites it), so the state is untouched.
+int autotune(falcon_ctx* ctx) {
+    if (ctx->kpar_stage && ctx->kpar_diff) return FALCON_OK;
+    int cand[8];
+    const int n = ctx->mixed() ? kpar_candidates_mixed(ctx->dims, cand) : kpar_candidates_fp64(ctx->dims, cand);
+    if (n == 0) return ctx->fail(FALCON_ERR_INVALID_ARG, "no kernel instantiation for this block size");
+    float best_s = 1e30f, best_d = 1e30f;
+    int ks = cand[0], kd = cand[0];
+    cudaEvent_t a = ctx->ev(), b = ctx->ev();
+    for (int q = 0; q < n; ++q) {
+        const int kp = cand[q];
+        for (int which = 0; which < 2; ++which) {
+            float tot = 0.f;
+            bool ok = true;
+            for (int rep = 0; rep < 4 && ok; ++rep) {
+                cudaEventRecord(a, ctx->st);
+                cudaError_t e;
+                if (which == 0)
+                    e = ctx->mixed() ? launch_stage_mixed(ctx->dims, ctx->geom(), (const float*)ctx->RK, (const float*)ctx->U,
+                                                          (float*)ctx->RK, 2, 1, ctx->sc, 1, kp, ctx->st)
+                                     : launch_stage_fp64(ctx->dims, ctx->geom(), (const double*)ctx->RK, (const double*)ctx->U,
+                                                         (double*)ctx->RK, 2, 1, ctx->sc, 1, kp, ctx->st);
+                else
+                    e = ctx->mixed() ? launch_diffusion_mixed(ctx->dims, ctx->geom(), (float*)ctx->RK, ctx->sc, kp, ctx->st)
+                                     : launch_diffusion_fp64(ctx->dims, ctx->geom(), (double*)ctx->RK, ctx->sc, kp, ctx->st);
+                cudaEventRecord(b, ctx->st);
+                if (e != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess) { ok = false; cudaGetLastError(); break; }
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, a, b);
+                if (rep > 0) tot += ms;   // the first launch pays for set-up
+            }
+            if (!ok) continue;
+            if (which == 0 && tot < best_s) { best_s = tot; ks = kp; }
+            if (which == 1 && tot < best_d) { best_d = tot; kd = kp; }
+        }
+    }
+    ctx->pool.push_back(a);
+    ctx->pool.push_back(b);
+    if (best_s >= 1e30f || best_d >= 1e30f) return ctx->fail(FALCON_ERR_CUDA, "autotune: no variant launched");
+    ctx->kpar_stage = ks;
+    ctx->kpar_diff = kd;
+    // undo the tuning launches' side effects: the device flags, and the stage
+    // buffer, which before the first step equals primitive_IV in the reference
+    CK(cudaMemsetAsync(&ctx->sc->nan_flag, 0, sizeof(int32_t), ctx->st), "autotune");
+    const size_t nelem = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
+    CK(cudaMemcpyAsync(ctx->RK, ctx->U, nelem * ctx->elem, cudaMemcpyDeviceToDevice, ctx->st), "autotune");
+    CK(cudaStreamSynchronize(ctx->st), "autotune");
+    return FALCON_OK;
 }
 
 int check_nan(falcon_ctx* ctx) {
@@ -246,45 +297,78 @@ int setup_device(falcon_ctx* ctx) {
     CK(cudaMemcpy(ctx->gs_f, gsf.data(), gsf.size() * 4, cudaMemcpyHostToDevice), "upload gs_f");
     CK(cudaMemcpy(ctx->flags, g.flags.data(), (size_t)nb * 4, cudaMemcpyHostToDevice), "upload flags");
 
-    // ghost lists: exact same-panel copies (sorted by target for coalesced
-    // writes) and the rest (trilinear and/or rotated)
+    // Ghost lists. FP64 keeps the reference's weights exactly (trilinear for
+    // every entry whose weights are not all exactly zero). The mixed path snaps
+    // weights within 1e-6 of 0 or 1 (an error of 1e-6*|du|, far below FP32
+    // resolution of the stencil inputs' differences) so aligned neighbours
+    // become plain copies and radial neighbours of other spacing 1-D blends.
+    // Copies and blends are sorted by target for coalesced writes.
+    const bool snap = ctx->mixed();
     std::vector<std::pair<int32_t, int32_t>> copies;
+    struct Lin { int32_t d, s, st; float w; };
+    std::vector<Lin> lins;
     std::vector<int32_t> idst, isrc;
     std::vector<double> iw, irot;
     std::vector<uint8_t> ikind;
+    const int32_t strides[3] = {1, g.nip, g.nip * g.njp};
     for (const auto& e : g.ghosts) {
+        int base[3] = {e.i0, e.j0, e.k0};
+        double w[3] = {e.w[0], e.w[1], e.w[2]};
+        if (snap)
+            for (int q = 0; q < 3; ++q) {
+                if (w[q] < 1e-6) w[q] = 0.0;
+                else if (w[q] > 1.0 - 1e-6) { w[q] = 0.0; base[q] += 1; }
+            }
+        const int nz = (w[0] != 0.0) + (w[1] != 0.0) + (w[2] != 0.0);
         const int32_t d = (int32_t)cell_off(g, e.e.tblock, e.e.ti, e.e.tj, e.e.tk);
-        const int32_t s = (int32_t)cell_off(g, e.e.sblock, e.i0, e.j0, e.k0);
-        if (e.copy && !e.rotate) { copies.push_back({d, s}); continue; }
+        const int32_t src = (int32_t)cell_off(g, e.e.sblock, base[0], base[1], base[2]);
+        if (!e.rotate && nz == 0) { copies.push_back({d, src}); continue; }
+        if (snap && !e.rotate && nz == 1) {
+            const int q = w[0] != 0.0 ? 0 : (w[1] != 0.0 ? 1 : 2);
+            lins.push_back({d, src, strides[q], (float)w[q]});
+            continue;
+        }
         idst.push_back(d);
-        isrc.push_back(s);
-        iw.insert(iw.end(), {e.w[0], e.w[1], e.w[2]});
+        isrc.push_back(src);
+        iw.insert(iw.end(), {w[0], w[1], w[2]});
         irot.insert(irot.end(), {e.rotate ? e.rot[0] : 0.0, e.rotate ? e.rot[1] : 0.0});
-        ikind.push_back((uint8_t)((e.copy ? 0 : 1) | (e.rotate ? 2 : 0)));
+        ikind.push_back((uint8_t)((nz ? 1 : 0) | (e.rotate ? 2 : 0)));
     }
     std::sort(copies.begin(), copies.end());
+    std::sort(lins.begin(), lins.end(), [](const Lin& a, const Lin& b) { return a.d < b.d; });
     std::vector<int32_t> cdst(copies.size()), csrc(copies.size());
     for (size_t q = 0; q < copies.size(); ++q) { cdst[q] = copies[q].first; csrc[q] = copies[q].second; }
-    CK(ctx->alloc(&ctx->cp_dst, cdst.size() * 4), "alloc ghosts");
-    CK(ctx->alloc(&ctx->cp_src, csrc.size() * 4), "alloc ghosts");
-    CK(ctx->alloc(&ctx->ip_dst, idst.size() * 4), "alloc ghosts");
-    CK(ctx->alloc(&ctx->ip_src, isrc.size() * 4), "alloc ghosts");
-    CK(ctx->alloc(&ctx->ip_w, iw.size() * 8), "alloc ghosts");
-    CK(ctx->alloc(&ctx->ip_rot, irot.size() * 8), "alloc ghosts");
-    CK(ctx->alloc(&ctx->ip_kind, ikind.size()), "alloc ghosts");
-    if (!cdst.empty()) {
-        CK(cudaMemcpy(ctx->cp_dst, cdst.data(), cdst.size() * 4, cudaMemcpyHostToDevice), "upload ghosts");
-        CK(cudaMemcpy(ctx->cp_src, csrc.data(), csrc.size() * 4, cudaMemcpyHostToDevice), "upload ghosts");
-    }
-    if (!idst.empty()) {
-        CK(cudaMemcpy(ctx->ip_dst, idst.data(), idst.size() * 4, cudaMemcpyHostToDevice), "upload ghosts");
-        CK(cudaMemcpy(ctx->ip_src, isrc.data(), isrc.size() * 4, cudaMemcpyHostToDevice), "upload ghosts");
-        CK(cudaMemcpy(ctx->ip_w, iw.data(), iw.size() * 8, cudaMemcpyHostToDevice), "upload ghosts");
-        CK(cudaMemcpy(ctx->ip_rot, irot.data(), irot.size() * 8, cudaMemcpyHostToDevice), "upload ghosts");
-        CK(cudaMemcpy(ctx->ip_kind, ikind.data(), ikind.size(), cudaMemcpyHostToDevice), "upload ghosts");
-    }
-    ctx->cp = GhostCopyList{(int64_t)cdst.size(), ctx->cp_dst, ctx->cp_src};
-    ctx->ip = GhostInterpList{(int64_t)idst.size(), ctx->ip_dst, ctx->ip_src, ctx->ip_w, ctx->ip_rot, ctx->ip_kind};
+    std::vector<int32_t> ldst(lins.size()), lsrc(lins.size()), lst(lins.size());
+    std::vector<float> lw(lins.size());
+    for (size_t q = 0; q < lins.size(); ++q) { ldst[q] = lins[q].d; lsrc[q] = lins[q].s; lst[q] = lins[q].st; lw[q] = lins[q].w; }
+    auto up = [&](auto** dptr, const auto& vec, const char* what) -> cudaError_t {
+        using E = typename std::remove_reference<decltype(vec)>::type::value_type;
+        cudaError_t e = ctx->alloc(dptr, vec.size() * sizeof(E));
+        if (e == cudaSuccess && !vec.empty()) e = cudaMemcpy(*dptr, vec.data(), vec.size() * sizeof(E), cudaMemcpyHostToDevice);
+        (void)what;
+        return e;
+    };
+    int32_t *cp_dst, *cp_src, *ln_dst, *ln_src, *ln_st, *ip_dst, *ip_src;
+    float* ln_w;
+    double *ip_w, *ip_rot;
+    uint8_t* ip_kind;
+    CK(up(&cp_dst, cdst, "ghosts"), "upload ghosts");
+    CK(up(&cp_src, csrc, "ghosts"), "upload ghosts");
+    CK(up(&ln_dst, ldst, "ghosts"), "upload ghosts");
+    CK(up(&ln_src, lsrc, "ghosts"), "upload ghosts");
+    CK(up(&ln_st, lst, "ghosts"), "upload ghosts");
+    CK(up(&ln_w, lw, "ghosts"), "upload ghosts");
+    CK(up(&ip_dst, idst, "ghosts"), "upload ghosts");
+    CK(up(&ip_src, isrc, "ghosts"), "upload ghosts");
+    CK(up(&ip_w, iw, "ghosts"), "upload ghosts");
+    CK(up(&ip_rot, irot, "ghosts"), "upload ghosts");
+    CK(up(&ip_kind, ikind, "ghosts"), "upload ghosts");
+    ctx->gl.cp = GhostCopyList{(int64_t)cdst.size(), cp_dst, cp_src};
+    ctx->gl.ln = GhostLinList{(int64_t)ldst.size(), ln_dst, ln_src, ln_st, ln_w};
+    ctx->gl.ip = GhostInterpList{(int64_t)idst.size(), ip_dst, ip_src, ip_w, ip_rot, ip_kind};
+    ctx->ghost_counts[0] = (int64_t)cdst.size();
+    ctx->ghost_counts[1] = (int64_t)ldst.size();
+    ctx->ghost_counts[2] = (int64_t)idst.size();
 
     StepScalars s0{};
     s0.min_ratio_bits = 0x7FF0000000000000ull;
@@ -466,6 +550,8 @@ int falcon_timestep(falcon_ctx* ctx, double* dt_out) {
 }
 
 static int run(falcon_ctx* ctx, int32_t n) {
+    int rc = autotune(ctx);
+    if (rc) return rc;
     if (ctx->ktiming) {
         for (int32_t s = 0; s < n; ++s) {
             CK(enqueue_step(ctx), "step");
@@ -515,6 +601,8 @@ int falcon_step_phase(falcon_ctx* ctx, int32_t phase) {
     int rc = need_device(ctx);
     if (rc) return rc;
     if (phase < 0 || phase > 5) return ctx->fail(FALCON_ERR_INVALID_ARG, "phase must be 0..5");
+    rc = autotune(ctx);
+    if (rc) return rc;
     cudaError_t e = cudaSuccess;
     if (phase == 0) {
         e = cfl(ctx);
@@ -523,13 +611,13 @@ int falcon_step_phase(falcon_ctx* ctx, int32_t phase) {
         void* in = (s == 1) ? ctx->U : ctx->RK;
         void* out = (s < 4) ? ctx->RK : ctx->U;
         e = ctx->mixed() ? launch_stage_mixed(ctx->dims, ctx->geom(), (const float*)in, (const float*)ctx->U,
-                                              (float*)out, s, 1, ctx->sc, 1, ctx->st)
+                                              (float*)out, s, 1, ctx->sc, 1, ctx->kpar_stage, ctx->st)
                          : launch_stage_fp64(ctx->dims, ctx->geom(), (const double*)in, (const double*)ctx->U,
-                                             (double*)out, s, 1, ctx->sc, 1, ctx->st);
+                                             (double*)out, s, 1, ctx->sc, 1, ctx->kpar_stage, ctx->st);
         if (e == cudaSuccess) e = ghost(ctx, out);
     } else {
-        e = ctx->mixed() ? launch_diffusion_mixed(ctx->dims, ctx->geom(), (float*)ctx->U, ctx->sc, ctx->st)
-                         : launch_diffusion_fp64(ctx->dims, ctx->geom(), (double*)ctx->U, ctx->sc, ctx->st);
+        e = ctx->mixed() ? launch_diffusion_mixed(ctx->dims, ctx->geom(), (float*)ctx->U, ctx->sc, ctx->kpar_diff, ctx->st)
+                         : launch_diffusion_fp64(ctx->dims, ctx->geom(), (double*)ctx->U, ctx->sc, ctx->kpar_diff, ctx->st);
         if (e == cudaSuccess) e = ghost(ctx, ctx->U);
         if (e == cudaSuccess) ++ctx->steps_done;
     }
@@ -611,6 +699,22 @@ int falcon_timer_stop(falcon_ctx* ctx, double* ms) {
     CK(cudaEventElapsedTime(&f, ctx->t0, ctx->t1), "timer");
     if (ms) *ms = f;
     collect(ctx);
+    return FALCON_OK;
+}
+
+int falcon_tuning(falcon_ctx* ctx, int32_t* kpar_stage, int32_t* kpar_diffusion) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    rc = autotune(ctx);
+    if (rc) return rc;
+    if (kpar_stage) *kpar_stage = ctx->kpar_stage;
+    if (kpar_diffusion) *kpar_diffusion = ctx->kpar_diff;
+    return FALCON_OK;
+}
+
+int falcon_ghost_list_sizes(const falcon_ctx* ctx, int64_t* counts) {
+    if (!ctx || !counts) return FALCON_ERR_INVALID_ARG;
+    for (int q = 0; q < 3; ++q) counts[q] = ctx->ghost_counts[q];
     return FALCON_OK;
 }
 

@@ -197,14 +197,15 @@ int Grid::find_leaf(const double* rtp, bool yin) const {
     return find_in(nodes, root, p);
 }
 
-std::string Grid::build(const falcon_config& c) {
+std::string Grid::build(const falcon_config& c, bool with_ghosts) {
     cfg = c;
     const falcon_tree_spec& t = c.tree;
     if (t.ni < 4 || t.nj < 4 || t.nk < 4 || t.ng != 2)
         return "block sizes must be >= 4 and ng must be 2 (fourth-order stencils)";
+    (void)with_ghosts;
     if (t.ni > 32 || t.nj > 32 || t.nk > 32) return "block sizes above 32 are not supported";
     if (c.phys.divb_option != 0) return "divb_option must be 0 (psi is not stored)";
-    if (!c.phys.if_involve_B) return "if_involve_B must be 1 (the MHD block layout with B active)";
+    if (with_ghosts && !c.phys.if_involve_B) return "if_involve_B must be 1 (the MHD block layout with B active)";
     if (t.radial_option < 1 || t.radial_option > 3) return "radial_option must be 1, 2 or 3";
     if (t.n_amr < 0 || t.n_amr > FALCON_MAX_AMR) return "n_amr out of range";
     for (int d = 0; d < 3; ++d)
@@ -297,6 +298,7 @@ std::string Grid::build(const falcon_config& c) {
         }
     }
 
+    if (!with_ghosts) return "";
     // ghost map: owners in i-j-k loop order (k fastest), grouped per source leaf
     // in first-appearance order (3_6/ModGC.f90:25-147)
     std::vector<std::vector<GhostMapEntry>> per(nblocks);

@@ -57,8 +57,9 @@ struct Grid {
     std::vector<GhostMapEntry> ghosts;    // canonical (reference) order
     int64_t uncovered = 0;                // non-radial ghosts without owner
 
-    // returns empty string on success, else the error message
-    std::string build(const falcon_config& c);
+    // returns empty string on success, else the error message; with_ghosts=false
+    // builds the tree, geometry and background only (the solvers' grids)
+    std::string build(const falcon_config& c, bool with_ghosts = true);
     int find_leaf(const double* rtp, bool yin) const;
 };
 

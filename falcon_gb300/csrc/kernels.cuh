@@ -62,7 +62,7 @@ struct StepScalars {
     double cfl;
     float dt_stage_f[4];                // (float)(dt/(5-s)) for the mixed path
     float dt_half_f;                    // (float)(0.5*dt)
-    int32_t nan_flag;                   // sticky: a NaN was seen in the state
+    int32_t nan_flag;                   // sticky: bit0 NaN seen in the state, bit1 a copy wait timed out
     int32_t nan_step;                   // step counter value when it was first seen
     int32_t step_counter;               // steps finalised so far (device side)
     int32_t pad_;
@@ -82,6 +82,20 @@ struct GhostInterpList {  // trilinear (and/or Yin-Yang rotated) ghost cells
     const uint8_t* kind;    // bit0: interpolate, bit1: rotate
 };
 
+struct GhostLinList {     // 1-D linear ghost cells (mixed path)
+    int64_t n;
+    const int32_t* dst;
+    const int32_t* src;
+    const int32_t* stride;  // element distance to the second point (1, nip or nip*njp)
+    const float* w;
+};
+
+struct GhostLists {
+    GhostCopyList cp;
+    GhostLinList ln;
+    GhostInterpList ip;
+};
+
 struct StepDims {
     int nblocks, ni, nj, nk, nip, njp, nkp, ncell;
 };
@@ -92,26 +106,27 @@ struct StepDims {
 // (3_6/ModBoundary.f90:10-55); the diffusion pass later reads those of u^n
 // (3_6/ModAdvance.f90:101-108)
 cudaError_t launch_stage_fp64(const StepDims& d, const Geometry& g, const double* in, const double* un,
-                              double* out, int stage, int bc_writeback, const StepScalars* sc,
-                              int heat_on, cudaStream_t st);
-cudaError_t launch_diffusion_fp64(const StepDims& d, const Geometry& g, double* u, const StepScalars* sc,
-                                  cudaStream_t st);
+                              double* out, int stage, int bc_writeback, StepScalars* sc,
+                              int heat_on, int kpar, cudaStream_t st);
+cudaError_t launch_diffusion_fp64(const StepDims& d, const Geometry& g, double* u, StepScalars* sc,
+                                  int kpar, cudaStream_t st);
 cudaError_t launch_cfl_fp64(const StepDims& d, const Geometry& g, const double* u, StepScalars* sc,
                             cudaStream_t st);
-cudaError_t launch_ghost_fp64(const StepDims& d, const GhostCopyList& cp, const GhostInterpList& ip,
-                              double* u, cudaStream_t st);
+cudaError_t launch_ghost_fp64(const StepDims& d, const GhostLists& gl, double* u, cudaStream_t st);
 
 cudaError_t launch_stage_mixed(const StepDims& d, const Geometry& g, const float* in, const float* un,
-                               float* out, int stage, int bc_writeback, const StepScalars* sc,
-                               int heat_on, cudaStream_t st);
-cudaError_t launch_diffusion_mixed(const StepDims& d, const Geometry& g, float* u, const StepScalars* sc,
-                                   cudaStream_t st);
+                               float* out, int stage, int bc_writeback, StepScalars* sc,
+                               int heat_on, int kpar, cudaStream_t st);
+cudaError_t launch_diffusion_mixed(const StepDims& d, const Geometry& g, float* u, StepScalars* sc,
+                                   int kpar, cudaStream_t st);
 cudaError_t launch_cfl_mixed(const StepDims& d, const Geometry& g, const float* u, StepScalars* sc,
                              cudaStream_t st);
-cudaError_t launch_ghost_mixed(const StepDims& d, const GhostCopyList& cp, const GhostInterpList& ip,
-                               float* u, cudaStream_t st);
+cudaError_t launch_ghost_mixed(const StepDims& d, const GhostLists& gl, float* u, cudaStream_t st);
 
 cudaError_t launch_finalize_dt(StepScalars* sc, cudaStream_t st);
+// k-chunk depths instantiated for this block size (returns the count)
+int kpar_candidates_fp64(const StepDims& d, int* out);
+int kpar_candidates_mixed(const StepDims& d, int* out);
 cudaError_t launch_convert_state(const double* src, float* dst, int64_t n, cudaStream_t st);
 cudaError_t launch_widen_state(const float* src, double* dst, int64_t n, cudaStream_t st);
 

@@ -7,13 +7,23 @@
 namespace falcon {
 namespace impl {
 
-template <class T> struct Cfg;   // KPAR per block size and precision
-template <> struct Cfg<double> { static constexpr int K8 = 4, K16 = 2; };
-template <> struct Cfg<float> { static constexpr int K8 = 8, K16 = 2; };
+// k-chunk depths (KPAR) instantiated per block size and precision; the
+// context's autotuner times them on its own grid and keeps the fastest.
+template <class T> struct Cand;
+template <> struct Cand<double> {
+    static constexpr int n8 = 2, n16 = 1;
+    static constexpr int k8[2] = {2, 4};
+    static constexpr int k16[1] = {1};
+};
+template <> struct Cand<float> {
+    static constexpr int n8 = 3, n16 = 3;
+    static constexpr int k8[3] = {2, 4, 8};
+    static constexpr int k16[3] = {1, 2, 4};
+};
 
 template <class T, int N, int KP>
 cudaError_t stage_n(const StepDims& d, const Geometry& g, const T* in, const T* un, T* out, int stage,
-                    int bcw, const StepScalars* sc, int heat, cudaStream_t st) {
+                    int bcw, StepScalars* sc, int heat, cudaStream_t st) {
     using S = Shape<T, N, N, N, KP>;
     static bool attr = false;
     if (!attr) {
@@ -27,7 +37,7 @@ cudaError_t stage_n(const StepDims& d, const Geometry& g, const T* in, const T* 
 }
 
 template <class T, int N, int KP>
-cudaError_t diff_n(const StepDims& d, const Geometry& g, T* u, const StepScalars* sc, cudaStream_t st) {
+cudaError_t diff_n(const StepDims& d, const Geometry& g, T* u, StepScalars* sc, cudaStream_t st) {
     using S = Shape<T, N, N, N, KP>;
     static bool attr = false;
     if (!attr) {
@@ -42,18 +52,35 @@ cudaError_t diff_n(const StepDims& d, const Geometry& g, T* u, const StepScalars
 
 template <class T>
 cudaError_t stage_any(const StepDims& d, const Geometry& g, const T* in, const T* un, T* out, int stage, int bcw,
-                      const StepScalars* sc, int heat, cudaStream_t st) {
-    if (d.ni == 8 && d.nj == 8 && d.nk == 8) return stage_n<T, 8, Cfg<T>::K8>(d, g, in, un, out, stage, bcw, sc, heat, st);
-    if (d.ni == 16 && d.nj == 16 && d.nk == 16)
-        return stage_n<T, 16, Cfg<T>::K16>(d, g, in, un, out, stage, bcw, sc, heat, st);
+                      StepScalars* sc, int heat, int kpar, cudaStream_t st) {
+#define FALCON_STAGE_CASE(N, K) \
+    if (d.ni == N && kpar == K) return stage_n<T, N, K>(d, g, in, un, out, stage, bcw, sc, heat, st);
+    if (d.ni != d.nj || d.ni != d.nk) return cudaErrorInvalidValue;
+    FALCON_STAGE_CASE(8, 2) FALCON_STAGE_CASE(8, 4)
+    FALCON_STAGE_CASE(16, 1)
+    if constexpr (!Pol<T>::exact) { FALCON_STAGE_CASE(8, 8) FALCON_STAGE_CASE(16, 2) FALCON_STAGE_CASE(16, 4) }
+#undef FALCON_STAGE_CASE
     return cudaErrorInvalidValue;
 }
 
 template <class T>
-cudaError_t diff_any(const StepDims& d, const Geometry& g, T* u, const StepScalars* sc, cudaStream_t st) {
-    if (d.ni == 8 && d.nj == 8 && d.nk == 8) return diff_n<T, 8, Cfg<T>::K8>(d, g, u, sc, st);
-    if (d.ni == 16 && d.nj == 16 && d.nk == 16) return diff_n<T, 16, Cfg<T>::K16>(d, g, u, sc, st);
+cudaError_t diff_any(const StepDims& d, const Geometry& g, T* u, StepScalars* sc, int kpar, cudaStream_t st) {
+#define FALCON_DIFF_CASE(N, K) \
+    if (d.ni == N && kpar == K) return diff_n<T, N, K>(d, g, u, sc, st);
+    if (d.ni != d.nj || d.ni != d.nk) return cudaErrorInvalidValue;
+    FALCON_DIFF_CASE(8, 2) FALCON_DIFF_CASE(8, 4)
+    FALCON_DIFF_CASE(16, 1)
+    if constexpr (!Pol<T>::exact) { FALCON_DIFF_CASE(8, 8) FALCON_DIFF_CASE(16, 2) FALCON_DIFF_CASE(16, 4) }
+#undef FALCON_DIFF_CASE
     return cudaErrorInvalidValue;
+}
+
+template <class T>
+int candidates(const StepDims& d, int* out) {
+    int n = 0;
+    if (d.ni == 8) for (int q = 0; q < Cand<T>::n8; ++q) out[n++] = Cand<T>::k8[q];
+    if (d.ni == 16) for (int q = 0; q < Cand<T>::n16; ++q) out[n++] = Cand<T>::k16[q];
+    return n;
 }
 
 template <class T>
@@ -65,15 +92,19 @@ cudaError_t cfl_any(const StepDims& d, const Geometry& g, const T* u, StepScalar
 }
 
 template <class T>
-cudaError_t ghost_any(const StepDims& d, const GhostCopyList& cp, const GhostInterpList& ip, T* u, cudaStream_t st) {
-    if (cp.n > 0) {
-        dim3 grid((unsigned)((cp.n + 255) / 256), NV);
-        k_ghost_copy<T><<<grid, 256, 0, st>>>(u, cp, d.ncell);
+cudaError_t ghost_any(const StepDims& d, const GhostLists& gl, T* u, cudaStream_t st) {
+    if (gl.cp.n > 0) {
+        k_ghost_copy<T><<<(unsigned)((gl.cp.n + 255) / 256), 256, 0, st>>>(u, gl.cp, d.ncell);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
-    if (ip.n > 0) {
-        k_ghost_interp<T><<<(unsigned)((ip.n + 127) / 128), 128, 0, st>>>(u, ip, d.ncell, d.nip, d.nip * d.njp);
+    if (gl.ln.n > 0) {
+        k_ghost_lin<T><<<(unsigned)((gl.ln.n + 255) / 256), 256, 0, st>>>(u, gl.ln, d.ncell);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    if (gl.ip.n > 0) {
+        k_ghost_interp<T><<<(unsigned)((gl.ip.n + 127) / 128), 128, 0, st>>>(u, gl.ip, d.ncell, d.nip, d.nip * d.njp);
         return cudaGetLastError();
     }
     return cudaSuccess;

@@ -10,19 +10,18 @@ using impl::cfl_any;
 using impl::ghost_any;
 
 cudaError_t launch_stage_fp64(const StepDims& d, const Geometry& g, const double* in, const double* un, double* out,
-                              int stage, int bcw, const StepScalars* sc, int heat, cudaStream_t st) {
-    return stage_any<double>(d, g, in, un, out, stage, bcw, sc, heat, st);
+                              int stage, int bcw, StepScalars* sc, int heat, int kpar, cudaStream_t st) {
+    return stage_any<double>(d, g, in, un, out, stage, bcw, sc, heat, kpar, st);
 }
-cudaError_t launch_diffusion_fp64(const StepDims& d, const Geometry& g, double* u, const StepScalars* sc,
-                                  cudaStream_t st) {
-    return diff_any<double>(d, g, u, sc, st);
+cudaError_t launch_diffusion_fp64(const StepDims& d, const Geometry& g, double* u, StepScalars* sc,
+                                  int kpar, cudaStream_t st) {
+    return diff_any<double>(d, g, u, sc, kpar, st);
 }
 cudaError_t launch_cfl_fp64(const StepDims& d, const Geometry& g, const double* u, StepScalars* sc, cudaStream_t st) {
     return cfl_any<double>(d, g, u, sc, st);
 }
-cudaError_t launch_ghost_fp64(const StepDims& d, const GhostCopyList& cp, const GhostInterpList& ip, double* u,
-                              cudaStream_t st) {
-    return ghost_any<double>(d, cp, ip, u, st);
+cudaError_t launch_ghost_fp64(const StepDims& d, const GhostLists& gl, double* u, cudaStream_t st) {
+    return ghost_any<double>(d, gl, u, st);
 }
 
 // dt = min(1.e20, CFL*min(h/v_wave)) (3_6/ModTimeStep.f90:20-29); also the
@@ -58,5 +57,7 @@ cudaError_t launch_widen_state(const float* src, double* dst, int64_t n, cudaStr
     k_widen<<<1216, 256, 0, st>>>(src, dst, n);
     return cudaGetLastError();
 }
+
+int kpar_candidates_fp64(const StepDims& d, int* out) { return impl::candidates<double>(d, out); }
 
 }  // namespace falcon

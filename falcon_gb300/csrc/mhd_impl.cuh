@@ -17,12 +17,15 @@ template <> struct Pol<double> {
     __device__ static __forceinline__ double dv(double a, double b, double binv) { return a / b; }
     __device__ static __forceinline__ double mmthr() { return (double)1.e-30f; }
     __device__ static __forceinline__ double mmscale() { return 1.e10; }
+    __device__ static __forceinline__ double ratio(double a, double b) { return a / b; }
 };
 template <> struct Pol<float> {
     static constexpr bool exact = false;
     __device__ static __forceinline__ float dv(float a, float, float binv) { return a * binv; }
     __device__ static __forceinline__ float mmthr() { return 1.e-30f; }
     __device__ static __forceinline__ float mmscale() { return 1.e10f; }
+    // limiter ratio: an approximate quotient is enough (0/0 still gives NaN -> phi = 0)
+    __device__ static __forceinline__ float ratio(float a, float b) { return __fdividef(a, b); }
 };
 
 // ModLinReconstruct_minmod for one value (3_6/ModLinReconstruct.f90:44-48).
@@ -53,39 +56,72 @@ template <class T> __device__ __forceinline__ const T* gs_ptr(const Geometry& g)
 template <> __device__ __forceinline__ const double* gs_ptr<double>(const Geometry& g) { return g.gs; }
 template <> __device__ __forceinline__ const float* gs_ptr<float>(const Geometry& g) { return g.gs_f; }
 
+// ---- TMA (bulk async copy) and mbarrier helpers ---------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// 1-D bulk copy global -> shared, completion counted on `bar` (16-byte aligned, size % 16 == 0)
+__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+// bounded wait on an mbarrier phase; false if it did not complete in max_iter polls
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int max_iter) {
+    for (int it = 0; it < max_iter; ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+constexpr int kWaitPolls = 1 << 22;   // each poll may suspend briefly; bounded overall
+
 template <class T, int NI, int NJ, int NK, int KPAR>
 struct Shape {
     static constexpr int NG = 2, NIP = NI + 4, NJP = NJ + 4, NKP = NK + 4;
-    static constexpr int PL = NIP * NJP, W = KPAR + 4, NT = NI * NJ * KPAR;
+    static constexpr int PL = NIP * NJP, NT = NI * NJ * KPAR;
+    static constexpr int W = 2 * KPAR + 4;    // ring: current window (KPAR+4) + the prefetched KPAR planes
+    static constexpr int WP = KPAR + 4;       // p1 window
     static constexpr int NCELL = PL * NKP;
-    static constexpr int VPP = PL * (int)sizeof(T) / 16;   // 16-byte vectors per plane
-    static_assert((PL * sizeof(T)) % 16 == 0, "plane must be a multiple of 16 bytes");
+    static constexpr uint32_t PLB = PL * (uint32_t)sizeof(T);   // bytes of one variable plane
+    static_assert(PLB % 16 == 0, "plane must be a multiple of 16 bytes");
     static_assert(NK % KPAR == 0, "KPAR must divide NK");
-    // shared memory: A1/A2 (double) | tile[NV][W][PL] | p1[W][PL] | gi | gj | gs
-    static constexpr size_t off_tile = 2 * NIP * sizeof(double);
+    // shared memory: mbarriers | A1/A2 (double) | tile[NV][W][PL] | p1[WP][PL] | gi | gj | gs
+    static constexpr size_t off_a12 = 16;
+    static constexpr size_t off_tile = off_a12 + ((2 * NIP * sizeof(double) + 15) / 16) * 16;
     static constexpr size_t off_p1 = off_tile + (size_t)NV * W * PL * sizeof(T);
-    static constexpr size_t off_gi = off_p1 + (size_t)W * PL * sizeof(T);
+    static constexpr size_t off_gi = off_p1 + (size_t)WP * PL * sizeof(T);
     static constexpr size_t off_gj = off_gi + (size_t)GI_COUNT * NIP * sizeof(T);
     static constexpr size_t off_gs = off_gj + (size_t)GJ_COUNT * NJP * sizeof(T);
     static constexpr size_t smem_stage = off_gs + GS_COUNT * sizeof(T);
-    static constexpr size_t smem_diff = off_gs + GS_COUNT * sizeof(T);   // p1 area unused but kept
+    static constexpr size_t smem_diff = smem_stage;
 };
 
-// copy planes kp in [lo, hi) of all variables of block b into the ring
+// Thread 0: bulk-copy planes kp in [lo,hi) of all variables of the block into
+// their ring slots, completing on `bar`.
 template <class T, class S>
-__device__ __forceinline__ void load_planes(const T* blk, T* tile, int lo, int hi) {
-    const int np = hi - lo;
-    const int total = NV * np * S::VPP;
-    for (int x = threadIdx.x; x < total; x += S::NT) {
-        const int vec = x % S::VPP;
-        const int rest = x / S::VPP;
-        const int pl = rest % np;
-        const int v = rest / np;
-        const int kp = lo + pl;
-        const uint4* s = reinterpret_cast<const uint4*>(blk + ((size_t)v * S::NKP + kp) * S::PL) + vec;
-        uint4* d = reinterpret_cast<uint4*>(tile + ((size_t)v * S::W + (kp % S::W)) * S::PL) + vec;
-        *d = *s;
-    }
+__device__ __forceinline__ void issue_planes(const T* blk, T* tile, int lo, int hi, uint64_t* bar) {
+    mbar_expect_tx(bar, (uint32_t)(NV * (hi - lo)) * S::PLB);
+    for (int v = 0; v < NV; ++v)
+        for (int kp = lo; kp < hi; ++kp)
+            tma_load_1d(tile + ((size_t)v * S::W + (kp % S::W)) * S::PL, blk + ((size_t)v * S::NKP + kp) * S::PL,
+                        S::PLB, bar);
 }
 
 template <class T, class S>
@@ -146,12 +182,13 @@ __device__ __forceinline__ void apply_bc(T* tile, int lo, int hi, int fl, T* wb)
 // u_out = u^n + dt*R/(5-s) (3_6/ModAdvance.f90:87-93).
 template <class T, int NI, int NJ, int NK, int KPAR>
 __global__ void __launch_bounds__(NI* NJ* KPAR)
-k_stage(const T* in, const T* un, T* out, Geometry g, const StepScalars* sc, int stage, int bc_writeback,
+k_stage(const T* in, const T* un, T* out, Geometry g, StepScalars* sc, int stage, int bc_writeback,
         int heat_on) {
     using S = Shape<T, NI, NJ, NK, KPAR>;
-    constexpr int NIP = S::NIP, PL = S::PL, W = S::W, NCELL = S::NCELL;
-    extern __shared__ __align__(16) unsigned char smem[];
-    double* a12 = reinterpret_cast<double*>(smem);
+    constexpr int NIP = S::NIP, PL = S::PL, W = S::W, WP = S::WP, NCELL = S::NCELL;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
+    double* a12 = reinterpret_cast<double*>(smem + S::off_a12);
     T* tile = reinterpret_cast<T*>(smem + S::off_tile);
     T* tp1 = reinterpret_cast<T*>(smem + S::off_p1);
     T* gi = reinterpret_cast<T*>(smem + S::off_gi);
@@ -162,6 +199,13 @@ k_stage(const T* in, const T* un, T* out, Geometry g, const StepScalars* sc, int
     const int fl = g.flags[b];
     const T* blk_in = in + (size_t)b * NV * NCELL;
     T* wb = bc_writeback ? const_cast<T*>(blk_in) : nullptr;
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) issue_planes<T, S>(blk_in, tile, 0, KPAR + 4, &bars[0]);
     load_geometry<T, S>(g, b, gi, gj, gs, a12);
     __syncthreads();   // the geometry tables are read by every thread below
 
@@ -185,12 +229,18 @@ k_stage(const T* in, const T* un, T* out, Geometry g, const StepScalars* sc, int
     constexpr int nchunk = NK / KPAR;
     for (int ch = 0; ch < nchunk; ++ch) {
         const int k0 = 1 + ch * KPAR;  // first Fortran k of the chunk
-        const int lo = (ch == 0) ? 0 : k0 + 3;   // first padded plane not yet in the ring
-        const int hi = k0 + KPAR + 3;                                  // one past the last needed plane
-        __syncthreads();
-        load_planes<T, S>(blk_in, tile, lo, hi);
-        __syncthreads();
+        const int lo = (ch == 0) ? 0 : k0 + 3;   // first padded plane new to this chunk
+        const int hi = k0 + KPAR + 3;            // one past the last plane it needs
+        __syncthreads();   // chunk ch-1 is done with the slots the prefetch below overwrites
+        if (threadIdx.x == 0 && ch + 1 < nchunk)
+            issue_planes<T, S>(blk_in, tile, hi, hi + KPAR, &bars[(ch + 1) & 1]);
+        if (!mbar_wait(&bars[ch & 1], (uint32_t)((ch >> 1) & 1), kWaitPolls)) {
+            atomicOr(&sc->nan_flag, 2);   // timed-out copy: reported as an error, no hang
+            mbar_wait(&bars[(ch + 1) & 1], (uint32_t)(((ch + 1) >> 1) & 1), kWaitPolls);
+            return;
+        }
         apply_bc<T, S>(tile, lo, hi, fl, wb);
+        fence_proxy_async();   // order these generic writes before later bulk copies into the slots
         __syncthreads();
         // p1 = gamma1*(p0/rho0)*rho1 + (gamma3-1)*(rho0*T0)*s1, assembled in FP64
         // (3_6/ModEquation.f90:40-46)
@@ -199,24 +249,35 @@ k_stage(const T* in, const T* un, T* out, Geometry g, const StepScalars* sc, int
             const int slot = kp % W;
             const double r1 = (double)tile[(V_RHO1 * W + slot) * PL + c];
             const double s1v = (double)tile[(V_S1 * W + slot) * PL + c];
-            tp1[slot * PL + c] = (T)(a12[ic] * r1 + a12[NIP + ic] * s1v);
+            tp1[(kp % WP) * PL + c] = (T)(a12[ic] * r1 + a12[NIP + ic] * s1v);
         }
         __syncthreads();
 
         const int k = k0 + kq;
         const int kp = k + 1;
-        int sl[5];
+        int sl[5], sp[5];
 #pragma unroll
-        for (int d = 0; d < 5; ++d) sl[d] = (kp + d - 2) % W;
+        for (int d = 0; d < 5; ++d) { sl[d] = (kp + d - 2) % W; sp[d] = (kp + d - 2) % WP; }
         auto A = [&](int v, int di, int dj, int dk) -> T {
             return tile[(v * W + sl[dk + 2]) * PL + (jj + dj) * NIP + ii + di];
         };
-        auto P = [&](int di, int dj, int dk) -> T { return tp1[sl[dk + 2] * PL + (jj + dj) * NIP + ii + di]; };
+        auto P = [&](int di, int dj, int dk) -> T { return tp1[sp[dk + 2] * PL + (jj + dj) * NIP + ii + di]; };
         // ModDerivative_1st_O4_3D (3_6/ModDerivative.f90:16-32)
         auto D = [&](T c, auto f) -> T { return c * (((-f(2) + T(8) * f(1)) - T(8) * f(-1)) + f(-2)); };
         const T vr = A(V_VR, 0, 0, 0), vt = A(V_VT, 0, 0, 0), vp = A(V_VP, 0, 0, 0);
         const T br = A(V_BR, 0, 0, 0), bt = A(V_BT, 0, 0, 0), bp = A(V_BP, 0, 0, 0);
         const T rho1 = A(V_RHO1, 0, 0, 0);
+        // u^n for the update, fetched before the stencil arithmetic so its
+        // latency overlaps it; at stage 1 the input is u^n and sits in the ring
+        const size_t base = (size_t)b * NV * NCELL + (size_t)kp * PL + jj * NIP + ii;
+        T u0s[NV];
+        if (stage == 1) {
+#pragma unroll
+            for (int v = 0; v < NV; ++v) u0s[v] = A(v, 0, 0, 0);
+        } else {
+#pragma unroll
+            for (int v = 0; v < NV; ++v) u0s[v] = un[base + (size_t)v * NCELL];
+        }
 
         // Mass conservation: -div(rho0 v)/Xi^2 (3_6/ModEquation.f90:50-61, ModSpherical_div :104-159)
         T Rrho;
@@ -306,11 +367,10 @@ k_stage(const T* in, const T* un, T* out, Geometry g, const StepScalars* sc, int
         }
 
         // stage update
-        const size_t base = (size_t)b * NV * NCELL + (size_t)kp * PL + jj * NIP + ii;
         const T R[NV] = {Rrho, Rvr, Rvt, Rvp, RBr, RBt, RBp, Rs};
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
-            const T u0 = un[base + (size_t)v * NCELL];
+            const T u0 = u0s[v];
             T o;
             if (Pol<T>::exact) o = (T)((double)u0 + (dt * (double)R[v]) / divs);
             else o = fmaf((float)dtk, (float)R[v], (float)u0);
@@ -324,16 +384,24 @@ k_stage(const T* in, const T* un, T* out, Geometry g, const StepScalars* sc, int
 // u += 0.5*dt*R (3_6/ModAdvance.f90:101-108), in place.
 template <class T, int NI, int NJ, int NK, int KPAR>
 __global__ void __launch_bounds__(NI* NJ* KPAR)
-k_diffusion(T* u, Geometry g, const StepScalars* sc) {
+k_diffusion(T* u, Geometry g, StepScalars* sc) {
     using S = Shape<T, NI, NJ, NK, KPAR>;
     constexpr int NIP = S::NIP, PL = S::PL, W = S::W, NCELL = S::NCELL;
-    extern __shared__ __align__(16) unsigned char smem[];
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
     T* tile = reinterpret_cast<T*>(smem + S::off_tile);
     T* gi = reinterpret_cast<T*>(smem + S::off_gi);
     T* gj = reinterpret_cast<T*>(smem + S::off_gj);
     T* gs = reinterpret_cast<T*>(smem + S::off_gs);
     const int b = blockIdx.x;
     T* blk = u + (size_t)b * NV * NCELL;
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) issue_planes<T, S>(blk, tile, 0, KPAR + 4, &bars[0]);
     load_geometry<T, S>(g, b, gi, gj, gs, nullptr);
     __syncthreads();   // the geometry tables are read by every thread below
     const int tid = threadIdx.x;
@@ -347,11 +415,14 @@ k_diffusion(T* u, Geometry g, const StepScalars* sc) {
     constexpr int nchunk = NK / KPAR;
     for (int ch = 0; ch < nchunk; ++ch) {
         const int k0 = 1 + ch * KPAR;
-        const int lo = (ch == 0) ? 0 : k0 + 3;
         const int hi = k0 + KPAR + 3;
         __syncthreads();
-        load_planes<T, S>(blk, tile, lo, hi);
-        __syncthreads();
+        if (threadIdx.x == 0 && ch + 1 < nchunk) issue_planes<T, S>(blk, tile, hi, hi + KPAR, &bars[(ch + 1) & 1]);
+        if (!mbar_wait(&bars[ch & 1], (uint32_t)((ch >> 1) & 1), kWaitPolls)) {
+            atomicOr(&sc->nan_flag, 2);
+            mbar_wait(&bars[(ch + 1) & 1], (uint32_t)(((ch + 1) >> 1) & 1), kWaitPolls);
+            return;
+        }
         const int kp = k0 + kq + 1;
         int sl[5];
 #pragma unroll
@@ -380,12 +451,12 @@ k_diffusion(T* u, Geometry g, const StepScalars* sc) {
                 const T dp1 = minmod(f0, fp1, fp2);
                 // face between cells -1 and 0
                 T num = ((f0 - d0 * T(0.5)) - fm1) - dm1 * T(0.5);
-                T phi = fmax(T(0), T(1) + T(2) * (num / (f0 - fm1) - T(1)));
+                T phi = fmax(T(0), T(1) + T(2) * (Pol<T>::ratio(num, f0 - fm1) - T(1)));
                 T fL = -(T(0.5) * phi * num);
                 fL = fL * (c0 + cm) * T(0.5);
                 // face between cells 0 and +1
                 num = ((fp1 - dp1 * T(0.5)) - f0) - d0 * T(0.5);
-                phi = fmax(T(0), T(1) + T(2) * (num / (fp1 - f0) - T(1)));
+                phi = fmax(T(0), T(1) + T(2) * (Pol<T>::ratio(num, fp1 - f0) - T(1)));
                 T fR = -(T(0.5) * phi * num);
                 fR = fR * (cp + c0) * T(0.5);
                 R[v] = R[v] + (fL - fR) / den[dir];
@@ -408,10 +479,13 @@ k_diffusion(T* u, Geometry g, const StepScalars* sc) {
 // (3_6/ModTimeStep.f90:10-30) and the NaN scan of 3_6/ModCheck.f90:12-71.
 template <class T>
 __global__ void __launch_bounds__(256) k_cfl(const T* u, Geometry g, StepScalars* sc, StepDims d) {
+    // R: the type the ratio and its block minimum are formed in (FP64 on the
+    // exact path, FP32 on the mixed path); the cross-block minimum is FP64.
+    using R = T;
     const int nint = d.ni * d.nj * d.nk;
     const int b = blockIdx.y;
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    double ratio = INFINITY;
+    R ratio = R(INFINITY);
     int nan = 0;
     if (q < nint) {
         const int i = q % d.ni + 2, j = (q / d.ni) % d.nj + 2, k = q / (d.ni * d.nj) + 2;
@@ -424,34 +498,31 @@ __global__ void __launch_bounds__(256) k_cfl(const T* u, Geometry g, StepScalars
         }
         const T* Gi = gi_ptr<T>(g) + (size_t)b * GI_COUNT * d.nip;
         const T* Gj = gj_ptr<T>(g) + (size_t)b * GJ_COUNT * d.njp;
-        const double* Gd = g.gi + (size_t)b * GI_COUNT * d.nip;
-        const double* Gs = g.gs + (size_t)b * GS_COUNT;
-        // h_LLL = min(dxi, r*dxj, r*sin(theta)*dxk) (3_6/ModBlock.f90:416-425), FP64
-        const double r = Gd[GI_R * d.nip + i];
-        const double st = g.gj[(size_t)b * GJ_COUNT * d.njp + GJ_SIN * d.njp + j];
-        const double h = fmin(fmin(Gs[GS_DXI], r * Gs[GS_DXJ]), r * st * Gs[GS_DXK]);
+        const T* Gs = gs_ptr<T>(g) + (size_t)b * GS_COUNT;
+        // h_LLL = min(dxi, r*dxj, r*sin(theta)*dxk) (3_6/ModBlock.f90:416-425)
+        const T r = Gi[GI_R * d.nip + i];
+        const T h = fmin(fmin(Gs[GS_DXI], r * Gs[GS_DXJ]), r * Gj[GJ_SIN * d.njp + j] * Gs[GS_DXK]);
         T w = Gi[GI_CS * d.nip + i] + sqrt(x[V_VR] * x[V_VR] + x[V_VT] * x[V_VT] + x[V_VP] * x[V_VP]);
         w = w + sqrt(x[V_BR] * x[V_BR] + x[V_BT] * x[V_BT] + x[V_BP] * x[V_BP]) / sqrt(Gi[GI_RHO0 * d.nip + i]);
-        (void)Gj;
-        ratio = h / (double)w;
-        if (ratio != ratio) { nan = 1; ratio = INFINITY; }
+        ratio = h / w;                     // the reference's h_LLL/v_wave
+        if (ratio != ratio) { nan = 1; ratio = R(INFINITY); }
     }
-    // warp then block min; positive doubles order like their bit patterns
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         ratio = fmin(ratio, __shfl_xor_sync(0xffffffffu, ratio, o));
         nan |= __shfl_xor_sync(0xffffffffu, nan, o);
     }
-    __shared__ double wmin[8];
+    __shared__ R wmin[8];
     __shared__ int wnan[8];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (lane == 0) { wmin[wid] = ratio; wnan[wid] = nan; }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double m = wmin[0];
+        R m = wmin[0];
         int n = wnan[0];
         for (int w2 = 1; w2 < (int)(blockDim.x >> 5); ++w2) { m = fmin(m, wmin[w2]); n |= wnan[w2]; }
-        atomicMin(&sc->min_ratio_bits, (unsigned long long)__double_as_longlong(m));
+        // positive doubles order like their bit patterns
+        atomicMin(&sc->min_ratio_bits, (unsigned long long)__double_as_longlong((double)m));
         if (n) atomicOr(&sc->nan_flag, 1);
     }
 }
@@ -465,9 +536,30 @@ template <class T>
 __global__ void __launch_bounds__(256) k_ghost_copy(T* u, GhostCopyList L, int ncell) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= L.n) return;
-    const int v = blockIdx.y;
-    const size_t off = (size_t)v * ncell;
-    u[(size_t)L.dst[e] + off] = u[(size_t)L.src[e] + off];
+    const size_t d = (size_t)L.dst[e], s = (size_t)L.src[e];
+    T v[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) v[q] = u[s + (size_t)q * ncell];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) u[d + (size_t)q * ncell] = v[q];
+}
+
+// one-dimensional linear interpolation (radial neighbours of different
+// spacing: the other two weights snapped to exactly 0), mixed path only
+template <class T>
+__global__ void __launch_bounds__(256) k_ghost_lin(T* u, GhostLinList L, int ncell) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= L.n) return;
+    const size_t d = (size_t)L.dst[e], s = (size_t)L.src[e], st = (size_t)L.stride[e];
+    const T w = (T)L.w[e], uw = T(1) - w;
+    T v[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        const T* f = u + s + (size_t)q * ncell;
+        v[q] = f[0] * uw + f[st] * w;
+    }
+#pragma unroll
+    for (int q = 0; q < NV; ++q) u[d + (size_t)q * ncell] = v[q];
 }
 
 template <class T>

@@ -1,0 +1,733 @@
+// solver.cu -- GPU multigrid-preconditioned flexible CG on the Yin-Yang grid.
+//
+// Reference algorithm: ModLinearSolver_Multigrid_CG / _V_cycle / _JCB_CG
+// (3_5/ModLinearSolver.f90:86-427) with the 7-point face-coefficient operator
+// (:15-84) and the 1-layer face-ghost halo (3_5/ModCommunication.f90:1497-1639).
+// GB300 form:
+//   - outer flexible CG in FP64 (dot products, residual norms and the true
+//     residual b-Ax in FP64), iterative refinement on the true residual;
+//   - V-cycle preconditioner in FP32: red-black Gauss-Seidel smoothing,
+//     restriction R = P^T (sum of 8 children), injection prolongation,
+//     Galerkin coarse operators;
+//   - every problem of a batch is advanced by the same launches: kernels index
+//     block -> problem, scalars are per problem, converged problems freeze.
+// Kernels are launched with one CTA row per block (grid.y = block), so a CTA
+// never mixes problems and its reductions go to one per-problem slot.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/falcon_gb300.h"
+#include "solver.h"
+
+namespace falcon {
+namespace sv {
+
+struct LevelDims {
+    int m0, m1, m2;        // interior
+    int p0, p1, p2;        // padded (m+2)
+    int nint, npad;
+};
+
+struct HaloList {
+    int64_t n;
+    const int32_t* dst;    // padded global offset
+    const int32_t* src;    // padded global offset of the base source cell
+    const int32_t* st;     // [n][3] element strides (0 where the weight is 0)
+    const double* w;       // [n][3]
+};
+
+struct Ops64 { const double *Aii, *Ai, *Aj, *Ak; };
+struct Ops32 { const float *Aii, *Ai, *Aj, *Ak; };
+
+__device__ __forceinline__ void cell_ijk(const LevelDims& d, int c, int& i, int& j, int& k) {
+    i = c % d.m0 + 1;
+    j = (c / d.m0) % d.m1 + 1;
+    k = c / (d.m0 * d.m1) + 1;
+}
+__device__ __forceinline__ size_t pidx(const LevelDims& d, int b, int i, int j, int k) {
+    return (size_t)b * d.npad + ((size_t)k * d.p1 + j) * d.p0 + i;
+}
+
+// y = A x over the interior, reference operand order (3_5/ModLinearSolver.f90:43-50)
+template <class T, class O>
+__device__ __forceinline__ T apply_A(const O& A, const LevelDims& d, const T* x, int b, int c, int i, int j, int k) {
+    const size_t P = pidx(d, b, i, j, k);
+    const size_t sj = d.p0, sk = (size_t)d.p0 * d.p1;
+    const size_t fi = ((size_t)b * d.m2 * d.m1 + (size_t)(k - 1) * d.m1 + (j - 1)) * (d.m0 + 1) + (i - 1);
+    const size_t fj = ((size_t)b * d.m2 * (d.m1 + 1) + (size_t)(k - 1) * (d.m1 + 1) + (j - 1)) * d.m0 + (i - 1);
+    const size_t fk = ((size_t)b * (d.m2 + 1) * d.m1 + (size_t)(k - 1) * d.m1 + (j - 1)) * d.m0 + (i - 1);
+    return A.Aii[(size_t)b * d.nint + c] * x[P] + A.Ai[fi] * x[P - 1] + A.Ai[fi + 1] * x[P + 1] + A.Aj[fj] * x[P - sj] +
+           A.Aj[fj + d.m0] * x[P + sj] + A.Ak[fk] * x[P - sk] + A.Ak[fk + (size_t)d.m0 * d.m1] * x[P + sk];
+}
+
+template <class T>
+__device__ __forceinline__ void block_sum_atomic(T v, double* slot) {
+    double s = (double)v;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __shared__ double ws[8];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += ws[w];
+        atomicAdd(slot, t);
+    }
+    __syncthreads();
+}
+
+// ---- halo fill (trilinear from the source interior) ------------------------
+template <class T>
+__global__ void k_halo(T* v, HaloList H) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= H.n) return;
+    const size_t s = (size_t)H.src[e];
+    const int a = H.st[3 * e], bq = H.st[3 * e + 1], c = H.st[3 * e + 2];
+    const T wi = (T)H.w[3 * e], wj = (T)H.w[3 * e + 1], wk = (T)H.w[3 * e + 2];
+    const T ui = T(1) - wi, uj = T(1) - wj, uk = T(1) - wk;
+    const T* f = v + s;
+    v[H.dst[e]] = f[0] * ui * uj * uk + f[a] * wi * uj * uk + f[bq] * ui * wj * uk + f[c] * ui * uj * wk +
+                  f[a + bq] * wi * wj * uk + f[bq + c] * ui * wj * wk + f[a + c] * wi * uj * wk + f[a + bq + c] * wi * wj * wk;
+}
+
+// ---- FP64 outer iteration ----------------------------------------------------
+struct Dots {
+    double *pAp, *pr, *zAp, *rr, *bb;
+    const int32_t* active;
+    const int32_t* bprob;
+};
+
+// Ap = A p; pAp += p.Ap; pr += p.r (per problem)
+__global__ void k_spmv_dots(Ops64 A, LevelDims d, const double* p, double* Ap, const double* r, Dots D) {
+    const int b = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+    double pa = 0, pr = 0;
+    if (c < d.nint) {
+        int i, j, k;
+        cell_ijk(d, c, i, j, k);
+        const double y = apply_A<double>(A, d, p, b, c, i, j, k);
+        const size_t q = (size_t)b * d.nint + c;
+        Ap[q] = y;
+        const double pv = p[pidx(d, b, i, j, k)];
+        pa = pv * y;
+        pr = pv * r[q];
+    }
+    const int pb = D.bprob[b];
+    block_sum_atomic(pa, &D.pAp[pb]);
+    block_sum_atomic(pr, &D.pr[pb]);
+}
+
+// alpha = p.r / p.Ap; x += alpha p; r -= alpha Ap; rr += r.r; rf = (float)r
+__global__ void k_update_xr(LevelDims d, double* x, const double* p, double* r, const double* Ap, float* rf, Dots D) {
+    const int b = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int pb = D.bprob[b];
+    const double alpha = D.active[pb] ? D.pr[pb] / D.pAp[pb] : 0.0;
+    double rr = 0;
+    if (c < d.nint) {
+        int i, j, k;
+        cell_ijk(d, c, i, j, k);
+        const size_t P = pidx(d, b, i, j, k), q = (size_t)b * d.nint + c;
+        x[P] = x[P] + alpha * p[P];
+        const double rv = r[q] - alpha * Ap[q];
+        r[q] = rv;
+        rf[q] = (float)rv;
+        rr = rv * rv;
+    }
+    block_sum_atomic(rr, &D.rr[pb]);
+}
+
+// r = b - A x (FP64 true residual); rr += r.r; rf = (float)r
+__global__ void k_residual64(Ops64 A, LevelDims d, const double* x, const double* bvec, double* r, float* rf, Dots D,
+                             int want_bb) {
+    const int b = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+    double rr = 0, bb = 0;
+    if (c < d.nint) {
+        int i, j, k;
+        cell_ijk(d, c, i, j, k);
+        const size_t q = (size_t)b * d.nint + c;
+        const double rv = bvec[q] - apply_A<double>(A, d, x, b, c, i, j, k);
+        r[q] = rv;
+        rf[q] = (float)rv;
+        rr = rv * rv;
+        bb = bvec[q] * bvec[q];
+    }
+    const int pb = D.bprob[b];
+    block_sum_atomic(rr, &D.rr[pb]);
+    if (want_bb) block_sum_atomic(bb, &D.bb[pb]);
+}
+
+// z (FP64, interior) from the preconditioner (FP32 padded z or the residual);
+// zAp += z.Ap
+__global__ void k_take_z(LevelDims d, const float* zf, const double* r, int use_r, double* z, const double* Ap, Dots D,
+                         int want_zAp) {
+    const int b = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+    double za = 0;
+    if (c < d.nint) {
+        int i, j, k;
+        cell_ijk(d, c, i, j, k);
+        const size_t q = (size_t)b * d.nint + c;
+        const double zv = use_r ? r[q] : (double)zf[pidx(d, b, i, j, k)];
+        z[q] = zv;
+        if (want_zAp) za = zv * Ap[q];
+    }
+    if (want_zAp) block_sum_atomic(za, &D.zAp[D.bprob[b]]);
+}
+
+// p = z + beta p, beta = -z.Ap / p.Ap (flexible CG, one-term A-orthogonalisation);
+// restart (beta = 0) when `restart`
+__global__ void k_update_p(LevelDims d, double* p, const double* z, Dots D, int restart) {
+    const int b = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.nint) return;
+    const int pb = D.bprob[b];
+    if (!D.active[pb]) return;
+    const double beta = restart ? 0.0 : -D.zAp[pb] / D.pAp[pb];
+    int i, j, k;
+    cell_ijk(d, c, i, j, k);
+    const size_t P = pidx(d, b, i, j, k);
+    p[P] = z[(size_t)b * d.nint + c] + beta * p[P];
+}
+
+// ---- FP32 V-cycle ------------------------------------------------------------
+__global__ void k_zero_f(float* v, size_t n) {
+    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (size_t)gridDim.x * blockDim.x) v[x] = 0.f;
+}
+
+// red-black Gauss-Seidel half sweep: z = (r - sum_nb A z_nb) / Aii on cells of one colour
+__global__ void k_rbgs(Ops32 A, LevelDims d, const float* r, float* z, int colour) {
+    const int b = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.nint) return;
+    int i, j, k;
+    cell_ijk(d, c, i, j, k);
+    if (((i + j + k) & 1) != colour) return;
+    const size_t P = pidx(d, b, i, j, k);
+    const size_t sj = d.p0, sk = (size_t)d.p0 * d.p1;
+    const size_t fi = ((size_t)b * d.m2 * d.m1 + (size_t)(k - 1) * d.m1 + (j - 1)) * (d.m0 + 1) + (i - 1);
+    const size_t fj = ((size_t)b * d.m2 * (d.m1 + 1) + (size_t)(k - 1) * (d.m1 + 1) + (j - 1)) * d.m0 + (i - 1);
+    const size_t fk = ((size_t)b * (d.m2 + 1) * d.m1 + (size_t)(k - 1) * d.m1 + (j - 1)) * d.m0 + (i - 1);
+    const float off = A.Ai[fi] * z[P - 1] + A.Ai[fi + 1] * z[P + 1] + A.Aj[fj] * z[P - sj] + A.Aj[fj + d.m0] * z[P + sj] +
+                      A.Ak[fk] * z[P - sk] + A.Ak[fk + (size_t)d.m0 * d.m1] * z[P + sk];
+    z[P] = (r[(size_t)b * d.nint + c] - off) / A.Aii[(size_t)b * d.nint + c];
+}
+
+// res = r - A z
+__global__ void k_resid32(Ops32 A, LevelDims d, const float* r, const float* z, float* res) {
+    const int b = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.nint) return;
+    int i, j, k;
+    cell_ijk(d, c, i, j, k);
+    const size_t q = (size_t)b * d.nint + c;
+    res[q] = r[q] - apply_A<float>(A, d, z, b, c, i, j, k);
+}
+
+// r_coarse(I) = sum of the 8 children of res_fine (R = P^T)
+__global__ void k_restrict(LevelDims f, LevelDims cd, const float* res, float* rc) {
+    const int b = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cd.nint) return;
+    const int I = c % cd.m0, J = (c / cd.m0) % cd.m1, K = c / (cd.m0 * cd.m1);
+    const float* R = res + (size_t)b * f.nint;
+    float s = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int i = 2 * I + (q & 1), j = 2 * J + ((q >> 1) & 1), k = 2 * K + (q >> 2);
+        s += R[((size_t)k * f.m1 + j) * f.m0 + i];
+    }
+    rc[(size_t)b * cd.nint + c] = s;
+}
+
+// z_fine(child) += z_coarse(I) (injection)
+__global__ void k_prolong_add(LevelDims f, LevelDims cd, const float* zc, float* zf) {
+    const int b = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= f.nint) return;
+    int i, j, k;
+    cell_ijk(f, c, i, j, k);
+    const int I = (i - 1) / 2 + 1, J = (j - 1) / 2 + 1, K = (k - 1) / 2 + 1;
+    zf[pidx(f, b, i, j, k)] += zc[pidx(cd, b, I, J, K)];
+}
+
+}  // namespace sv
+}  // namespace falcon
+
+using namespace falcon;
+using namespace falcon::sv;
+
+struct SvLevel {
+    LevelDims d{};
+    double *Aii = nullptr, *Ai = nullptr, *Aj = nullptr, *Ak = nullptr;
+    float *fAii = nullptr, *fAi = nullptr, *fAj = nullptr, *fAk = nullptr;
+    int32_t *hdst = nullptr, *hsrc = nullptr, *hst = nullptr;
+    double* hw = nullptr;
+    int64_t nh = 0;
+    float *z = nullptr, *r = nullptr, *res = nullptr;
+    HaloList halo() const { return HaloList{nh, hdst, hsrc, hst, hw}; }
+    Ops64 ops64() const { return Ops64{Aii, Ai, Aj, Ak}; }
+    Ops32 ops32() const { return Ops32{fAii, fAi, fAj, fAk}; }
+};
+
+struct falcon_solver {
+    SolverProblemSet S;
+    std::string err;
+    int device = 0;
+    cudaStream_t st = nullptr;
+    std::vector<SvLevel> lv;
+    double *x = nullptr, *p = nullptr, *r = nullptr, *Ap = nullptr, *z = nullptr, *bvec = nullptr;
+    double* dots = nullptr;       // [5][nproblems]
+    int32_t *active = nullptr, *bprob = nullptr;
+    std::vector<void*> allocs;
+    int nu_pre = 2, nu_post = 2, nu_coarse = 16;
+    double dt_conduction = 0;
+    int fail(int c, const std::string& m) { err = m; return c; }
+    template <class P> cudaError_t alloc(P** ptr, size_t bytes) {
+        cudaError_t e = cudaMalloc((void**)ptr, bytes ? bytes : 16);
+        if (e == cudaSuccess) { allocs.push_back(*ptr); cudaMemsetAsync(*ptr, 0, bytes ? bytes : 16, st); }
+        return e;
+    }
+    Dots D() const {
+        const int n = S.nproblems;
+        return Dots{dots, dots + n, dots + 2 * n, dots + 3 * n, dots + 4 * n, active, bprob};
+    }
+};
+
+#define SCK(call, where)                                                                    \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess) return sv->fail(FALCON_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+namespace {
+
+dim3 grid_cells(const LevelDims& d, int nblocks) { return dim3((unsigned)((d.nint + 255) / 256), (unsigned)nblocks); }
+
+template <class T> cudaError_t halo_fill(falcon_solver* sv, int l, T* v) {
+    const SvLevel& L = sv->lv[l];
+    if (L.nh == 0) return cudaSuccess;
+    k_halo<T><<<(unsigned)((L.nh + 255) / 256), 256, 0, sv->st>>>(v, L.halo());
+    return cudaGetLastError();
+}
+
+// z_0 = M r_0: one V-cycle on the FP32 residual stored in lv[0].r
+cudaError_t vcycle(falcon_solver* sv) {
+    const int nl = (int)sv->lv.size(), nb = sv->S.nblocks;
+    cudaError_t e = cudaSuccess;
+    auto smooth = [&](int l, int sweeps, bool reverse) {
+        SvLevel& L = sv->lv[l];
+        for (int s = 0; s < sweeps && e == cudaSuccess; ++s)
+            for (int h = 0; h < 2 && e == cudaSuccess; ++h) {
+                e = halo_fill<float>(sv, l, L.z);
+                if (e != cudaSuccess) break;
+                k_rbgs<<<grid_cells(L.d, nb), 256, 0, sv->st>>>(L.ops32(), L.d, L.r, L.z, reverse ? 1 - h : h);
+                e = cudaGetLastError();
+            }
+    };
+    for (int l = 0; l < nl && e == cudaSuccess; ++l) {
+        SvLevel& L = sv->lv[l];
+        k_zero_f<<<1216, 256, 0, sv->st>>>(L.z, (size_t)nb * L.d.npad);
+        e = cudaGetLastError();
+        smooth(l, l == nl - 1 ? sv->nu_coarse : sv->nu_pre, false);
+        if (l + 1 < nl && e == cudaSuccess) {
+            e = halo_fill<float>(sv, l, L.z);
+            if (e != cudaSuccess) break;
+            k_resid32<<<grid_cells(L.d, nb), 256, 0, sv->st>>>(L.ops32(), L.d, L.r, L.z, L.res);
+            SvLevel& C = sv->lv[l + 1];
+            k_restrict<<<grid_cells(C.d, nb), 256, 0, sv->st>>>(L.d, C.d, L.res, C.r);
+            e = cudaGetLastError();
+        }
+    }
+    for (int l = nl - 2; l >= 0 && e == cudaSuccess; --l) {
+        SvLevel& L = sv->lv[l];
+        SvLevel& C = sv->lv[l + 1];
+        k_prolong_add<<<grid_cells(L.d, nb), 256, 0, sv->st>>>(L.d, C.d, C.z, L.z);
+        e = cudaGetLastError();
+        smooth(l, sv->nu_post, true);
+    }
+    return e;
+}
+
+int setup(falcon_solver* sv) {
+    SolverProblemSet& S = sv->S;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return sv->fail(FALCON_ERR_NO_DEVICE, "no CUDA device");
+    SCK(cudaSetDevice(sv->device), "cudaSetDevice");
+    SCK(cudaStreamCreateWithFlags(&sv->st, cudaStreamNonBlocking), "stream");
+    const int nb = S.nblocks;
+    sv->lv.resize(S.nlevels);
+    for (int l = 0; l < S.nlevels; ++l) {
+        const SolverLevel& H = S.L[l];
+        SvLevel& L = sv->lv[l];
+        L.d.m0 = H.m[0]; L.d.m1 = H.m[1]; L.d.m2 = H.m[2];
+        L.d.p0 = H.m[0] + 2; L.d.p1 = H.m[1] + 2; L.d.p2 = H.m[2] + 2;
+        L.d.nint = H.nint();
+        L.d.npad = L.d.p0 * L.d.p1 * L.d.p2;
+        auto up64 = [&](double** d, const std::vector<double>& h) -> cudaError_t {
+            cudaError_t e = sv->alloc(d, h.size() * 8);
+            if (e == cudaSuccess) e = cudaMemcpy(*d, h.data(), h.size() * 8, cudaMemcpyHostToDevice);
+            return e;
+        };
+        auto up32 = [&](float** d, const std::vector<double>& h) -> cudaError_t {
+            std::vector<float> f(h.begin(), h.end());
+            cudaError_t e = sv->alloc(d, f.size() * 4);
+            if (e == cudaSuccess) e = cudaMemcpy(*d, f.data(), f.size() * 4, cudaMemcpyHostToDevice);
+            return e;
+        };
+        SCK(up64(&L.Aii, H.Aii), "operator");
+        SCK(up64(&L.Ai, H.Ai), "operator");
+        SCK(up64(&L.Aj, H.Aj), "operator");
+        SCK(up64(&L.Ak, H.Ak), "operator");
+        SCK(up32(&L.fAii, H.Aii), "operator");
+        SCK(up32(&L.fAi, H.Ai), "operator");
+        SCK(up32(&L.fAj, H.Aj), "operator");
+        SCK(up32(&L.fAk, H.Ak), "operator");
+        // halo entries -> padded offsets and strides
+        const size_t n = H.halo.size();
+        std::vector<int32_t> dst(n), src(n), stv(3 * n);
+        std::vector<double> w(3 * n);
+        const int32_t strides[3] = {1, L.d.p0, L.d.p0 * L.d.p1};
+        for (size_t q = 0; q < n; ++q) {
+            const HaloEntry& h = H.halo[q];
+            dst[q] = (int32_t)(h.tb * (int64_t)L.d.npad + ((int64_t)h.tk * L.d.p1 + h.tj) * L.d.p0 + h.ti);
+            src[q] = (int32_t)(h.sb * (int64_t)L.d.npad + ((int64_t)h.k0 * L.d.p1 + h.j0) * L.d.p0 + h.i0);
+            for (int dd = 0; dd < 3; ++dd) {
+                w[3 * q + dd] = h.w[dd];
+                stv[3 * q + dd] = h.w[dd] != 0.0 ? strides[dd] : 0;
+            }
+        }
+        L.nh = (int64_t)n;
+        SCK(sv->alloc(&L.hdst, n * 4), "halo");
+        SCK(sv->alloc(&L.hsrc, n * 4), "halo");
+        SCK(sv->alloc(&L.hst, 3 * n * 4), "halo");
+        SCK(sv->alloc(&L.hw, 3 * n * 8), "halo");
+        if (n) {
+            SCK(cudaMemcpy(L.hdst, dst.data(), n * 4, cudaMemcpyHostToDevice), "halo");
+            SCK(cudaMemcpy(L.hsrc, src.data(), n * 4, cudaMemcpyHostToDevice), "halo");
+            SCK(cudaMemcpy(L.hst, stv.data(), 3 * n * 4, cudaMemcpyHostToDevice), "halo");
+            SCK(cudaMemcpy(L.hw, w.data(), 3 * n * 8, cudaMemcpyHostToDevice), "halo");
+        }
+        SCK(sv->alloc(&L.z, (size_t)nb * L.d.npad * 4), "vectors");
+        SCK(sv->alloc(&L.r, (size_t)nb * L.d.nint * 4), "vectors");
+        SCK(sv->alloc(&L.res, (size_t)nb * L.d.nint * 4), "vectors");
+    }
+    const LevelDims& d0 = sv->lv[0].d;
+    SCK(sv->alloc(&sv->x, (size_t)nb * d0.npad * 8), "vectors");
+    SCK(sv->alloc(&sv->p, (size_t)nb * d0.npad * 8), "vectors");
+    SCK(sv->alloc(&sv->r, (size_t)nb * d0.nint * 8), "vectors");
+    SCK(sv->alloc(&sv->Ap, (size_t)nb * d0.nint * 8), "vectors");
+    SCK(sv->alloc(&sv->z, (size_t)nb * d0.nint * 8), "vectors");
+    SCK(sv->alloc(&sv->bvec, (size_t)nb * d0.nint * 8), "vectors");
+    SCK(sv->alloc(&sv->dots, (size_t)5 * S.nproblems * 8), "scalars");
+    SCK(sv->alloc(&sv->active, (size_t)S.nproblems * 4), "scalars");
+    SCK(sv->alloc(&sv->bprob, (size_t)nb * 4), "scalars");
+    SCK(cudaMemcpy(sv->bvec, S.b.data(), S.b.size() * 8, cudaMemcpyHostToDevice), "rhs");
+    SCK(cudaMemcpy(sv->bprob, S.block_problem.data(), (size_t)nb * 4, cudaMemcpyHostToDevice), "scalars");
+    SCK(cudaStreamSynchronize(sv->st), "setup");
+    return FALCON_OK;
+}
+
+// scatter an interior [b][nint] FP64 vector into the padded x
+__global__ void k_scatter_pad(LevelDims d, const double* v, double* x) {
+    const int b = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.nint) return;
+    int i, j, k;
+    cell_ijk(d, c, i, j, k);
+    x[pidx(d, b, i, j, k)] = v[(size_t)b * d.nint + c];
+}
+__global__ void k_gather_pad(LevelDims d, const double* x, double* v) {
+    const int b = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.nint) return;
+    int i, j, k;
+    cell_ijk(d, c, i, j, k);
+    v[(size_t)b * d.nint + c] = x[pidx(d, b, i, j, k)];
+}
+
+}  // namespace
+
+extern "C" {
+
+int falcon_solver_create(falcon_solver** out, const falcon_solver_spec* spec) {
+    if (!out || !spec) return FALCON_ERR_INVALID_ARG;
+    falcon_solver* sv = new falcon_solver();
+    *out = sv;
+    if (spec->nproblems < 1 || spec->nproblems > FALCON_MAX_PROBLEMS) return sv->fail(FALCON_ERR_INVALID_ARG, "nproblems out of range");
+    if (spec->block < 2 || spec->block > 32 || (spec->block & 1)) return sv->fail(FALCON_ERR_INVALID_ARG, "block must be even, 2..32");
+    sv->device = spec->device;
+    std::vector<falcon_config> cfgs(spec->nproblems);
+    const double kRsun = (double)6.955e10f;
+    for (int q = 0; q < spec->nproblems; ++q) {
+        falcon_config& c = cfgs[q];
+        std::memset(&c, 0, sizeof c);
+        falcon_tree_spec& t = c.tree;
+        t.ni = t.nj = t.nk = spec->block;
+        t.ng = 2;
+        const int B = spec->block;
+        if (spec->kind == FALCON_SOLVER_PFSS) {
+            // (nr, ntheta) -> per panel (nr, ntheta/2, 3 ntheta/2) rounded up to whole blocks
+            const int Nr = (spec->nr[q] + B - 1) / B;
+            const int Nt = (spec->nt[q] / 2 + B - 1) / B;
+            t.root_tiles[0] = Nr; t.root_tiles[1] = Nt; t.root_tiles[2] = 3 * Nt;
+            t.radial_levels = 0; t.radial_option = 2; t.n_amr = 0;
+        } else {
+            // conduction: per panel nr x nt x np cells, uniform radial blocks
+            const int Nr = spec->nr[q] / B, Nt = spec->nt[q] / B, Np = spec->np[q] / B;
+            if (Nr * B != spec->nr[q] || Nt * B != spec->nt[q] || Np * B != spec->np[q] || Np != 3 * Nt)
+                return sv->fail(FALCON_ERR_INVALID_ARG, "conduction grid must be whole blocks with np = 3 nt");
+            t.root_tiles[0] = Nr; t.root_tiles[1] = Nt; t.root_tiles[2] = Np;
+            t.radial_option = 2;
+        }
+        t.r_range_rsun[0] = spec->r_range_rsun[0];
+        t.r_range_rsun[1] = spec->r_range_rsun[1];
+        c.phys.cfl = 0.4;
+        c.bg.poly_n = 1.5; c.bg.density_contrast = 100.0; c.bg.mu = 0.6; c.bg.xi_mode = 1;
+        c.device = spec->device;
+    }
+    std::string e = build_solver_levels(sv->S, cfgs, spec->nlevels);
+    if (!e.empty()) return sv->fail(FALCON_ERR_INVALID_ARG, e);
+    SolverProblemSet& S = sv->S;
+    if (spec->kind == FALCON_SOLVER_PFSS) {
+        // magnetogram Br at the bottom face centres of bottom blocks (Yin frame)
+        const SolverLevel& L = S.L[0];
+        const int mj = L.m[1], mk = L.m[2];
+        std::vector<double> br((size_t)S.nblocks * mj * mk, 0.0);
+        for (int q = 0; q < S.nproblems; ++q) {
+            Magnetogram M;
+            M.init(spec->seed + (uint64_t)q, spec->r_range_rsun[0] * kRsun);
+            for (int gb = S.problem_first_block[q]; gb < S.problem_first_block[q + 1]; ++gb) {
+                if (!(S.block_flags[gb] & 4)) continue;
+                const bool yin = S.block_flags[gb] & 1;
+                const Grid& g = S.grids[q];
+                const int b = gb - S.problem_first_block[q];
+                const double r0 = g.ranges[(size_t)b * 6 + 0];
+                for (int k = 1; k <= mk; ++k)
+                    for (int j = 1; j <= mj; ++j) {
+                        double t = L.xj[(size_t)gb * (mj + 2) + j], ph = L.xk[(size_t)gb * (mk + 2) + k];
+                        if (!yin) {
+                            const double a[3] = {r0, t, ph};
+                            const double st_ = std::sin(a[1]), ct = std::cos(a[1]), sp = std::sin(a[2]), cp = std::cos(a[2]);
+                            t = std::acos(st_ * sp);
+                            ph = std::copysign(std::fabs(std::acos(-(st_ * cp) / std::sqrt(st_ * st_ * (cp * cp) + ct * ct))), ct);
+                        }
+                        br[((size_t)gb * mk + (k - 1)) * mj + (j - 1)] = M.br(r0, t, ph);
+                    }
+            }
+        }
+        assemble_pfss(S, br);
+    } else {
+        ConductionField F;
+        F.init(&S.grids[0].bg, spec->seed, S.grids[0].r_range[0]);
+        assemble_conduction(S, F, spec->dt_factor > 0 ? spec->dt_factor : 50.0, &sv->dt_conduction);
+    }
+    galerkin_coarsen(S);
+    if (spec->device < 0) return FALCON_OK;
+    return setup(sv);
+}
+
+void falcon_solver_destroy(falcon_solver* sv) {
+    if (!sv) return;
+    if (sv->st) {
+        cudaSetDevice(sv->device);
+        cudaStreamSynchronize(sv->st);
+        for (void* q : sv->allocs) cudaFree(q);
+        cudaStreamDestroy(sv->st);
+    }
+    delete sv;
+}
+
+int falcon_solver_last_error(const falcon_solver* sv, char* buf, size_t len) {
+    if (!sv || !buf || !len) return FALCON_ERR_INVALID_ARG;
+    snprintf(buf, len, "%s", sv->err.c_str());
+    return FALCON_OK;
+}
+
+int falcon_solver_info(const falcon_solver* sv, int32_t* info) {
+    if (!sv || !info) return FALCON_ERR_INVALID_ARG;
+    info[0] = sv->S.nblocks;
+    info[1] = sv->S.nproblems;
+    info[2] = sv->S.nlevels;
+    for (int d = 0; d < 3; ++d) info[3 + d] = sv->S.nlevels ? sv->S.L[0].m[d] : 0;
+    return FALCON_OK;
+}
+
+int falcon_solver_problem_blocks(const falcon_solver* sv, int32_t* first) {
+    if (!sv || !first) return FALCON_ERR_INVALID_ARG;
+    std::memcpy(first, sv->S.problem_first_block.data(), sv->S.problem_first_block.size() * 4);
+    return FALCON_OK;
+}
+
+int falcon_solver_rhs(const falcon_solver* sv, double* b) {
+    if (!sv || !b) return FALCON_ERR_INVALID_ARG;
+    std::memcpy(b, sv->S.b.data(), sv->S.b.size() * 8);
+    return FALCON_OK;
+}
+
+int falcon_solver_operator(const falcon_solver* sv, int32_t level, double* Aii, double* Ai, double* Aj, double* Ak) {
+    if (!sv || level < 0 || level >= sv->S.nlevels) return FALCON_ERR_INVALID_ARG;
+    const SolverLevel& L = sv->S.L[level];
+    if (Aii) std::memcpy(Aii, L.Aii.data(), L.Aii.size() * 8);
+    if (Ai) std::memcpy(Ai, L.Ai.data(), L.Ai.size() * 8);
+    if (Aj) std::memcpy(Aj, L.Aj.data(), L.Aj.size() * 8);
+    if (Ak) std::memcpy(Ak, L.Ak.data(), L.Ak.size() * 8);
+    return FALCON_OK;
+}
+
+int falcon_solver_halo_count(const falcon_solver* sv, int32_t level, int64_t* n) {
+    if (!sv || !n || level < 0 || level >= sv->S.nlevels) return FALCON_ERR_INVALID_ARG;
+    *n = (int64_t)sv->S.L[level].halo.size();
+    return FALCON_OK;
+}
+
+// entries: [n][8] int32 (tb,ti,tj,tk,sb,i0,j0,k0) and [n][6] double (w, src_x)
+int falcon_solver_halo_map(const falcon_solver* sv, int32_t level, int32_t* idx, double* wx) {
+    if (!sv || level < 0 || level >= sv->S.nlevels) return FALCON_ERR_INVALID_ARG;
+    const auto& H = sv->S.L[level].halo;
+    for (size_t q = 0; q < H.size(); ++q) {
+        const HaloEntry& h = H[q];
+        const int32_t v[8] = {h.tb, h.ti, h.tj, h.tk, h.sb, h.i0, h.j0, h.k0};
+        std::memcpy(idx + 8 * q, v, sizeof v);
+        for (int d = 0; d < 3; ++d) { wx[6 * q + d] = h.w[d]; wx[6 * q + 3 + d] = h.src_x[d]; }
+    }
+    return FALCON_OK;
+}
+
+// y = A x at level 0 on the GPU (x interior [b][nint]; halo filled on the device)
+int falcon_solver_apply(falcon_solver* sv, const double* x, double* y) {
+    if (!sv || !x || !y) return FALCON_ERR_INVALID_ARG;
+    if (!sv->st) return sv->fail(FALCON_ERR_NO_DEVICE, "solver created without a device");
+    cudaSetDevice(sv->device);
+    const LevelDims& d = sv->lv[0].d;
+    const int nb = sv->S.nblocks;
+    SCK(cudaMemcpyAsync(sv->z, x, (size_t)nb * d.nint * 8, cudaMemcpyHostToDevice, sv->st), "apply");
+    SCK(cudaMemsetAsync(sv->p, 0, (size_t)nb * d.npad * 8, sv->st), "apply");
+    k_scatter_pad<<<grid_cells(d, nb), 256, 0, sv->st>>>(d, sv->z, sv->p);
+    SCK(halo_fill<double>(sv, 0, sv->p), "apply halo");
+    SCK(cudaMemsetAsync(sv->dots, 0, (size_t)5 * sv->S.nproblems * 8, sv->st), "apply");
+    k_spmv_dots<<<grid_cells(d, nb), 256, 0, sv->st>>>(sv->lv[0].ops64(), d, sv->p, sv->Ap, sv->r, sv->D());
+    SCK(cudaGetLastError(), "apply");
+    SCK(cudaMemcpyAsync(y, sv->Ap, (size_t)nb * d.nint * 8, cudaMemcpyDeviceToHost, sv->st), "apply");
+    SCK(cudaStreamSynchronize(sv->st), "apply");
+    return FALCON_OK;
+}
+
+int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t precond, falcon_solve_report* rep) {
+    if (!sv || !rep) return FALCON_ERR_INVALID_ARG;
+    if (!sv->st) return sv->fail(FALCON_ERR_NO_DEVICE, "solver created without a device");
+    if (precond != FALCON_PRECOND_NONE && precond != FALCON_PRECOND_MG) return sv->fail(FALCON_ERR_INVALID_ARG, "unknown preconditioner");
+    cudaSetDevice(sv->device);
+    const SolverProblemSet& S = sv->S;
+    const int nb = S.nblocks, np = S.nproblems;
+    const LevelDims& d = sv->lv[0].d;
+    const dim3 g = grid_cells(d, nb);
+    std::memset(rep, 0, sizeof *rep);
+    cudaEvent_t t0, t1;
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    // x = x0, r = b - A x, bb = b.b
+    SCK(cudaMemsetAsync(sv->x, 0, (size_t)nb * d.npad * 8, sv->st), "init");
+    SCK(cudaMemcpyAsync(sv->z, S.x0.data(), (size_t)nb * d.nint * 8, cudaMemcpyHostToDevice, sv->st), "init");
+    SCK(cudaStreamSynchronize(sv->st), "init");
+    cudaEventRecord(t0, sv->st);
+    k_scatter_pad<<<g, 256, 0, sv->st>>>(d, sv->z, sv->x);
+    std::vector<int32_t> act(np, 1);
+    SCK(cudaMemcpyAsync(sv->active, act.data(), np * 4, cudaMemcpyHostToDevice, sv->st), "init");
+    SCK(cudaMemsetAsync(sv->dots, 0, (size_t)5 * np * 8, sv->st), "init");
+    SCK(halo_fill<double>(sv, 0, sv->x), "halo");
+    k_residual64<<<g, 256, 0, sv->st>>>(sv->lv[0].ops64(), d, sv->x, sv->bvec, sv->r, sv->lv[0].r, sv->D(), 1);
+    std::vector<double> rr(np), bb(np);
+    SCK(cudaMemcpyAsync(bb.data(), sv->dots + 4 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "bb");
+    SCK(cudaStreamSynchronize(sv->st), "bb");
+    for (int q = 0; q < np; ++q) if (bb[q] <= 0) bb[q] = 1.0;
+    auto precondition = [&](int want_zAp) -> cudaError_t {
+        cudaError_t e = cudaSuccess;
+        if (precond == FALCON_PRECOND_MG) { e = vcycle(sv); ++rep->vcycles; }
+        if (e != cudaSuccess) return e;
+        k_take_z<<<g, 256, 0, sv->st>>>(d, sv->lv[0].z, sv->r, precond == FALCON_PRECOND_NONE, sv->z, sv->Ap, sv->D(), want_zAp);
+        return cudaGetLastError();
+    };
+    // p = M r
+    SCK(precondition(0), "precondition");
+    k_update_p<<<g, 256, 0, sv->st>>>(d, sv->p, sv->z, sv->D(), 1);
+    SCK(halo_fill<double>(sv, 0, sv->p), "halo");
+    double worst = 0;
+    int it = 0;
+    bool done = false;
+    for (it = 1; it <= max_iter && !done; ++it) {
+        SCK(cudaMemsetAsync(sv->dots, 0, (size_t)4 * np * 8, sv->st), "dots");
+        k_spmv_dots<<<g, 256, 0, sv->st>>>(sv->lv[0].ops64(), d, sv->p, sv->Ap, sv->r, sv->D());
+        k_update_xr<<<g, 256, 0, sv->st>>>(d, sv->x, sv->p, sv->r, sv->Ap, sv->lv[0].r, sv->D());
+        SCK(cudaGetLastError(), "iterate");
+        SCK(cudaMemcpyAsync(rr.data(), sv->dots + 3 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "rr");
+        SCK(cudaStreamSynchronize(sv->st), "rr");
+        bool all = true;
+        for (int q = 0; q < np; ++q)
+            if (act[q] && std::sqrt(rr[q] / bb[q]) > tol) all = false;
+        if (all) {
+            // verify on the FP64 true residual; restart from it if the recurrence drifted
+            SCK(cudaMemsetAsync(sv->dots + 3 * np, 0, (size_t)np * 8, sv->st), "dots");
+            SCK(halo_fill<double>(sv, 0, sv->x), "halo");
+            k_residual64<<<g, 256, 0, sv->st>>>(sv->lv[0].ops64(), d, sv->x, sv->bvec, sv->r, sv->lv[0].r, sv->D(), 0);
+            SCK(cudaMemcpyAsync(rr.data(), sv->dots + 3 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "rr");
+            SCK(cudaStreamSynchronize(sv->st), "rr");
+            worst = 0;
+            bool ok = true;
+            for (int q = 0; q < np; ++q) {
+                const double rel = std::sqrt(rr[q] / bb[q]);
+                worst = std::max(worst, rel);
+                if (rel <= tol) act[q] = 0;
+                else ok = false;
+            }
+            SCK(cudaMemcpyAsync(sv->active, act.data(), np * 4, cudaMemcpyHostToDevice, sv->st), "active");
+            if (ok) { done = true; break; }
+            ++rep->refinements;
+            SCK(precondition(0), "precondition");
+            k_update_p<<<g, 256, 0, sv->st>>>(d, sv->p, sv->z, sv->D(), 1);
+            SCK(halo_fill<double>(sv, 0, sv->p), "halo");
+            continue;
+        }
+        SCK(precondition(1), "precondition");
+        k_update_p<<<g, 256, 0, sv->st>>>(d, sv->p, sv->z, sv->D(), 0);
+        SCK(halo_fill<double>(sv, 0, sv->p), "halo");
+    }
+    cudaEventRecord(t1, sv->st);
+    SCK(cudaEventSynchronize(t1), "solve");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, t0, t1);
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    if (!done) {
+        // report the true residual of the last iterate
+        SCK(cudaMemsetAsync(sv->dots + 3 * np, 0, (size_t)np * 8, sv->st), "dots");
+        SCK(halo_fill<double>(sv, 0, sv->x), "halo");
+        k_residual64<<<g, 256, 0, sv->st>>>(sv->lv[0].ops64(), d, sv->x, sv->bvec, sv->r, sv->lv[0].r, sv->D(), 0);
+        SCK(cudaMemcpyAsync(rr.data(), sv->dots + 3 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "rr");
+        SCK(cudaStreamSynchronize(sv->st), "rr");
+        worst = 0;
+        for (int q = 0; q < np; ++q) worst = std::max(worst, std::sqrt(rr[q] / bb[q]));
+    }
+    rep->iterations = std::min(it, max_iter);
+    rep->converged = done ? 1 : 0;
+    rep->rel_residual = worst;
+    rep->ms = ms;
+    if (!done) { sv->err = "not converged within max_iter"; return FALCON_ERR_NOT_CONVERGED; }
+    return FALCON_OK;
+}
+
+int falcon_solver_solution(falcon_solver* sv, double* x) {
+    if (!sv || !x) return FALCON_ERR_INVALID_ARG;
+    if (!sv->st) return sv->fail(FALCON_ERR_NO_DEVICE, "solver created without a device");
+    cudaSetDevice(sv->device);
+    const LevelDims& d = sv->lv[0].d;
+    const int nb = sv->S.nblocks;
+    k_gather_pad<<<grid_cells(d, nb), 256, 0, sv->st>>>(d, sv->x, sv->z);
+    SCK(cudaMemcpyAsync(x, sv->z, (size_t)nb * d.nint * 8, cudaMemcpyDeviceToHost, sv->st), "solution");
+    SCK(cudaStreamSynchronize(sv->st), "solution");
+    return FALCON_OK;
+}
+
+int falcon_solver_timestep(const falcon_solver* sv, double* dt) {
+    if (!sv || !dt) return FALCON_ERR_INVALID_ARG;
+    *dt = sv->dt_conduction;
+    return FALCON_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,164 @@
+"""Python face of the implicit-solver C ABI (include/falcon_gb300.h).
+
+    PFSS batch  : ModPFSS_setup + ModPFSS_solve (3_5/ModPFSS.f90:21-150)
+    Conduction  : the implicit step ModHeatConduction leaves empty
+                  (3_6/ModHeatConduction.f90), same operator format
+    solve       : ModLinearSolver_Multigrid_CG (3_5/ModLinearSolver.f90:313-427)
+                  as FP64 flexible CG with an FP32 V-cycle preconditioner
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import lib as _lib, FalconError, OK
+
+MAX_PROBLEMS = 256
+PFSS = 0
+CONDUCTION = 1
+PRECOND_NONE = 0
+PRECOND_MG = 1
+
+
+class SolverSpec(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32), ("nproblems", C.c_int32), ("block", C.c_int32), ("nlevels", C.c_int32),
+        ("device", C.c_int32), ("pad_", C.c_int32), ("seed", C.c_uint64),
+        ("r_range_rsun", C.c_double * 2), ("dt_factor", C.c_double),
+        ("nr", C.c_int32 * MAX_PROBLEMS), ("nt", C.c_int32 * MAX_PROBLEMS), ("np", C.c_int32 * MAX_PROBLEMS),
+    ]
+
+
+class SolveReport(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("converged", C.c_int32), ("vcycles", C.c_int32),
+                ("refinements", C.c_int32), ("rel_residual", C.c_double), ("ms", C.c_double)]
+
+
+_SYMS = ("falcon_solver_create", "falcon_solver_last_error", "falcon_solver_info", "falcon_solver_problem_blocks",
+         "falcon_solver_rhs", "falcon_solver_operator", "falcon_solver_halo_count", "falcon_solver_halo_map",
+         "falcon_solver_apply", "falcon_solver_solve", "falcon_solver_solution", "falcon_solver_timestep")
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def pfss_spec(sizes, seed=5000, block=8, nlevels=3, device=0, r_range=(1.0, 2.5)):
+    """sizes: list of (nr, ntheta) per problem (nphi = 2 ntheta)."""
+    s = SolverSpec()
+    s.kind, s.nproblems, s.block, s.nlevels, s.device, s.seed = PFSS, len(sizes), block, nlevels, device, seed
+    s.r_range_rsun[0], s.r_range_rsun[1] = r_range
+    for q, (nr, nt) in enumerate(sizes):
+        s.nr[q], s.nt[q] = nr, nt
+    return s
+
+
+def conduction_spec(nr=64, nt=128, np_=384, seed=3001, block=16, nlevels=3, device=0, dt_factor=50.0,
+                    r_range=(0.7, 1.0)):
+    s = SolverSpec()
+    s.kind, s.nproblems, s.block, s.nlevels, s.device, s.seed = CONDUCTION, 1, block, nlevels, device, seed
+    s.r_range_rsun[0], s.r_range_rsun[1] = r_range
+    s.dt_factor = dt_factor
+    s.nr[0], s.nt[0], s.np[0] = nr, nt, np_
+    return s
+
+
+def random_pfss_sizes(n=64, seed=5000):
+    """nr ~ U{24..64}, ntheta ~ U{45..180} per problem."""
+    rs = np.random.Generator(np.random.PCG64(seed))
+    return [(int(rs.integers(24, 65)), int(rs.integers(45, 181))) for _ in range(n)]
+
+
+class Solver:
+    def __init__(self, spec):
+        L = _lib()
+        for n in _SYMS:
+            getattr(L, n).restype = C.c_int
+        L.falcon_solver_destroy.restype = None
+        self.L = L
+        self.spec = spec
+        h = C.c_void_p()
+        rc = L.falcon_solver_create(C.byref(h), C.byref(spec))
+        self.h = h
+        if rc != OK:
+            msg = self.last_error()
+            L.falcon_solver_destroy(h)
+            self.h = None
+            raise FalconError(rc, msg)
+        info = (C.c_int32 * 6)()
+        L.falcon_solver_info(self.h, info)
+        self.nblocks, self.nproblems, self.nlevels = info[0], info[1], info[2]
+        self.m = (info[3], info[4], info[5])
+        self.nint = self.m[0] * self.m[1] * self.m[2]
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.falcon_solver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def last_error(self):
+        buf = C.create_string_buffer(512)
+        self.L.falcon_solver_last_error(self.h, buf, C.c_size_t(512))
+        return buf.value.decode()
+
+    def _ck(self, rc):
+        if rc != OK:
+            raise FalconError(rc, self.last_error())
+
+    def problem_blocks(self):
+        out = np.zeros(self.nproblems + 1, dtype=np.int32)
+        self._ck(self.L.falcon_solver_problem_blocks(self.h, _ptr(out)))
+        return out
+
+    def rhs(self):
+        out = np.zeros((self.nblocks, self.m[2], self.m[1], self.m[0]))
+        self._ck(self.L.falcon_solver_rhs(self.h, _ptr(out)))
+        return out
+
+    def level_shape(self, level):
+        return tuple(x >> level for x in self.m)
+
+    def operator(self, level=0):
+        mi, mj, mk = self.level_shape(level)
+        nb = self.nblocks
+        Aii = np.zeros((nb, mk, mj, mi)); Ai = np.zeros((nb, mk, mj, mi + 1))
+        Aj = np.zeros((nb, mk, mj + 1, mi)); Ak = np.zeros((nb, mk + 1, mj, mi))
+        self._ck(self.L.falcon_solver_operator(self.h, C.c_int32(level), _ptr(Aii), _ptr(Ai), _ptr(Aj), _ptr(Ak)))
+        return Aii, Ai, Aj, Ak
+
+    def halo_map(self, level=0):
+        n = C.c_int64()
+        self._ck(self.L.falcon_solver_halo_count(self.h, C.c_int32(level), C.byref(n)))
+        idx = np.zeros((n.value, 8), dtype=np.int32)
+        wx = np.zeros((n.value, 6))
+        self._ck(self.L.falcon_solver_halo_map(self.h, C.c_int32(level), _ptr(idx), _ptr(wx)))
+        return idx, wx
+
+    def apply(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros_like(x)
+        self._ck(self.L.falcon_solver_apply(self.h, _ptr(x), _ptr(y)))
+        return y
+
+    def solve(self, tol=1e-8, max_iter=500, precond=PRECOND_MG, check=True):
+        rep = SolveReport()
+        rc = self.L.falcon_solver_solve(self.h, C.c_double(tol), C.c_int32(max_iter), C.c_int32(precond),
+                                        C.byref(rep))
+        if check:
+            self._ck(rc)
+        return {k: getattr(rep, k) for k, _ in SolveReport._fields_}
+
+    def solution(self):
+        out = np.zeros((self.nblocks, self.m[2], self.m[1], self.m[0]))
+        self._ck(self.L.falcon_solver_solution(self.h, _ptr(out)))
+        return out
+
+    def timestep(self):
+        d = C.c_double()
+        self._ck(self.L.falcon_solver_timestep(self.h, C.byref(d)))
+        return d.value

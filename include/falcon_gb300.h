@@ -188,8 +188,74 @@ int  falcon_reset_kernel_stats(falcon_ctx* ctx);
 /* device-side event timing of the context stream */
 int  falcon_timer_start(falcon_ctx* ctx);
 int  falcon_timer_stop(falcon_ctx* ctx, double* ms);
+/* k-chunk depth (planes per CTA step) chosen for the stage and diffusion
+ * kernels. The autotuner runs once per context, before the first step: it
+ * times every compiled variant on this grid, on the stage buffer only. */
+int  falcon_tuning(falcon_ctx* ctx, int32_t* kpar_stage, int32_t* kpar_diffusion);
+/* device ghost-fill lists: counts[0] exact copies, [1] 1-D blends, [2] trilinear/rotated */
+int  falcon_ghost_list_sizes(const falcon_ctx* ctx, int64_t* counts);
 /* bytes of device memory held by the context */
 int  falcon_device_bytes(const falcon_ctx* ctx, int64_t* bytes);
+
+/* ======================================================================
+ * Implicit solvers: multigrid-preconditioned flexible CG on the Yin-Yang
+ * grid (replaces ModPFSS_setup/ModPFSS_solve, 3_5/ModPFSS.f90:21-150, and
+ * ModLinearSolver_Multigrid_CG, 3_5/ModLinearSolver.f90:313-427; the
+ * conduction operator fills the empty ModHeatConduction, 3_6/ModHeatConduction.f90).
+ * ====================================================================== */
+#define FALCON_MAX_PROBLEMS 256
+#define FALCON_SOLVER_PFSS        0   /* Laplace solve, source surface at r_range[1] */
+#define FALCON_SOLVER_CONDUCTION  1   /* backward-Euler anisotropic heat conduction */
+#define FALCON_PRECOND_NONE 0
+#define FALCON_PRECOND_MG   1         /* one FP32 V-cycle (red-black Gauss-Seidel) */
+
+typedef struct falcon_solver_spec {
+    int32_t  kind;                     /* FALCON_SOLVER_* */
+    int32_t  nproblems;                /* independent problems solved in one batch */
+    int32_t  block;                    /* cells per block edge (even) */
+    int32_t  nlevels;                  /* multigrid levels (capped by the block size) */
+    int32_t  device;                   /* CUDA device; < 0 builds the host side only */
+    int32_t  pad_;
+    uint64_t seed;                     /* problem q uses seed + q */
+    double   r_range_rsun[2];          /* PFSS: [1.0, 2.5]; conduction: [0.7, 1.0] */
+    double   dt_factor;                /* conduction: dt in units of the explicit limit */
+    /* PFSS: nr[q], nt[q] (ntheta; nphi = 2 ntheta), mapped to per-panel
+     * (nr, nt/2, 3 nt/2) rounded up to whole blocks. Conduction: per-panel
+     * cells nr[0] x nt[0] x np[0] (np = 3 nt). */
+    int32_t  nr[FALCON_MAX_PROBLEMS];
+    int32_t  nt[FALCON_MAX_PROBLEMS];
+    int32_t  np[FALCON_MAX_PROBLEMS];
+} falcon_solver_spec;
+
+typedef struct falcon_solve_report {
+    int32_t iterations, converged, vcycles, refinements;
+    double  rel_residual;              /* max over problems of the FP64 ||b-Ax||/||b|| */
+    double  ms;                        /* device time of the solve */
+} falcon_solve_report;
+
+typedef struct falcon_solver falcon_solver;
+
+int  falcon_solver_create(falcon_solver** out, const falcon_solver_spec* spec);
+void falcon_solver_destroy(falcon_solver* sv);
+int  falcon_solver_last_error(const falcon_solver* sv, char* buf, size_t len);
+/* info: nblocks, nproblems, nlevels, m_i, m_j, m_k (level-0 cells per block) */
+int  falcon_solver_info(const falcon_solver* sv, int32_t* info);
+/* first[q] = first global block of problem q, q = 0..nproblems */
+int  falcon_solver_problem_blocks(const falcon_solver* sv, int32_t* first);
+/* level-0 right-hand side [block][k][j][i] */
+int  falcon_solver_rhs(const falcon_solver* sv, double* b);
+/* face-coefficient operator of a level (3_5/ModBlock.f90:39-44 layout, C order
+ * [block][k][j][i]; Ai has m_i+1 faces along i, Aj m_j+1 along j, Ak m_k+1 along k) */
+int  falcon_solver_operator(const falcon_solver* sv, int32_t level, double* Aii, double* Ai, double* Aj, double* Ak);
+int  falcon_solver_halo_count(const falcon_solver* sv, int32_t level, int64_t* n);
+/* idx[n][8] = tb,ti,tj,tk,sb,i0,j0,k0 ; wx[n][6] = weights (3), source-frame centre (3) */
+int  falcon_solver_halo_map(const falcon_solver* sv, int32_t level, int32_t* idx, double* wx);
+/* y = A x on the GPU (level 0, halo filled on the device) */
+int  falcon_solver_apply(falcon_solver* sv, const double* x, double* y);
+int  falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t precond, falcon_solve_report* rep);
+int  falcon_solver_solution(falcon_solver* sv, double* x);
+/* conduction time step dt (dt_factor x the explicit stability limit) */
+int  falcon_solver_timestep(const falcon_solver* sv, double* dt);
 
 #ifdef __cplusplus
 }

@@ -17,8 +17,9 @@ _lib = None
 
 def build(force=False):
     """Compile the oracle with its Makefile (gcc, -ffp-contract=off)."""
-    if force or not os.path.exists(LIB_PATH) or (
-            os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "falcon_oracle.cpp"))):
+    srcs = [os.path.join(HERE, f) for f in ("falcon_oracle.cpp", "solver_oracle.cpp", "Makefile")]
+    if force or not os.path.exists(LIB_PATH) or any(
+            os.path.getmtime(LIB_PATH) < os.path.getmtime(f) for f in srcs):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB_PATH
 
@@ -44,6 +45,9 @@ def lib():
         L.orc_num_threads.restype = C.c_int
         L.orc_dt.restype = C.c_double
         L.orc_dt.argtypes = [vp]
+        L.orc_hc_halo.restype = C.c_int64
+        for name in ("orc_pfss_operator", "orc_spmv", "orc_halo_fill", "orc_find_leaf"):
+            getattr(L, name).restype = C.c_int
         _lib = L
     return _lib
 
@@ -158,6 +162,43 @@ class Oracle:
         d = np.zeros(3)
         self.L.orc_block_grid(self.hp, C.c_int32(b), _ptr(xi), _ptr(xj), _ptr(xk), _ptr(d))
         return xi, xj, xk, d
+
+
+def pfss_operator(o, m):
+    """Level-1 PFSS operator of the oracle's tree (3_5/ModPFSS.f90:57-86)."""
+    nb = o.nblocks
+    Aii = np.zeros((nb, m, m, m)); Ai = np.zeros((nb, m, m, m + 1))
+    Aj = np.zeros((nb, m, m + 1, m)); Ak = np.zeros((nb, m + 1, m, m))
+    lib().orc_pfss_operator(o.hp, C.c_int32(m), _ptr(Aii), _ptr(Ai), _ptr(Aj), _ptr(Ak))
+    return Aii, Ai, Aj, Ak
+
+
+def hc_halo(o, m):
+    """1-layer halo map in the reference's order: idx[n][8], wx[n][6], clamped[n]."""
+    L = lib()
+    n = L.orc_hc_halo(o.hp, C.c_int32(m), None, None, None, C.c_int64(1 << 40))
+    idx = np.zeros((n, 8), dtype=np.int32)
+    wx = np.zeros((n, 6))
+    cl = np.zeros(n, dtype=np.int32)
+    L.orc_hc_halo(o.hp, C.c_int32(m), _ptr(idx), _ptr(wx), _ptr(cl), C.c_int64(n))
+    return idx, wx, cl
+
+
+def spmv(m, A, xp):
+    """y = A x (3_5/ModLinearSolver.f90:43-50) on a padded vector."""
+    Aii, Ai, Aj, Ak = [np.ascontiguousarray(a, dtype=np.float64) for a in A]
+    nb = Aii.shape[0]
+    xp = np.ascontiguousarray(xp, dtype=np.float64)
+    y = np.zeros_like(Aii)
+    lib().orc_spmv(C.c_int32(nb), C.c_int32(m), _ptr(Aii), _ptr(Ai), _ptr(Aj), _ptr(Ak), _ptr(xp), _ptr(y))
+    return y
+
+
+def halo_fill(m, idx, wx, xp):
+    idx = np.ascontiguousarray(idx, dtype=np.int32)
+    wx = np.ascontiguousarray(wx, dtype=np.float64)
+    lib().orc_halo_fill(C.c_int32(m), _ptr(idx), _ptr(wx), C.c_int64(len(idx)), _ptr(xp))
+    return xp
 
 
 def ghost_entries_to_numpy(arr, n):

@@ -1130,6 +1130,11 @@ int orc_block_diffusion(void* h, int32_t b, const double* p, double* R) {
     std::memcpy(R, B.R.data(), B.R.size() * sizeof(double));
     return 0;
 }
+// leaf (0-based block) owning a point given in the frame of panel `yin`, or -1
+int orc_find_leaf(void* h, const double* rtp, int32_t yin) {
+    const orc::Node* nd = ((Oracle*)h)->tree.find(rtp, yin != 0);
+    return nd ? nd->leaf_id - 1 : -1;
+}
 // known-answer helpers
 void orc_coord_conv(const double* in, double* out) { orc::coord_conv(in, out); }
 void orc_vec_conv(const double* rtp, const double* v, double* out) { orc::vec_conv(rtp, v, out); }
