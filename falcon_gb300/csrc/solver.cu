@@ -11,7 +11,7 @@
 //     Galerkin coarse operators;
 //   - every problem of a batch is advanced by the same launches: kernels index
 //     block -> problem, scalars are per problem, converged problems freeze.
-// Kernels are launched with one CTA row per block (grid.y = block), so a CTA
+// Kernels are launched with one CTA column per block (grid.x = block), so a CTA
 // never mixes problems and its reductions go to one per-problem slot.
 #include <cuda_runtime.h>
 
@@ -105,7 +105,7 @@ struct Dots {
 
 // Ap = A p; pAp += p.Ap; pr += p.r (per problem)
 __global__ void k_spmv_dots(Ops64 A, LevelDims d, const double* p, double* Ap, const double* r, Dots D) {
-    const int b = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
     double pa = 0, pr = 0;
     if (c < d.nint) {
         int i, j, k;
@@ -124,7 +124,7 @@ __global__ void k_spmv_dots(Ops64 A, LevelDims d, const double* p, double* Ap, c
 
 // alpha = p.r / p.Ap; x += alpha p; r -= alpha Ap; rr += r.r; rf = (float)r
 __global__ void k_update_xr(LevelDims d, double* x, const double* p, double* r, const double* Ap, float* rf, Dots D) {
-    const int b = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
     const int pb = D.bprob[b];
     const double alpha = D.active[pb] ? D.pr[pb] / D.pAp[pb] : 0.0;
     double rr = 0;
@@ -144,7 +144,7 @@ __global__ void k_update_xr(LevelDims d, double* x, const double* p, double* r, 
 // r = b - A x (FP64 true residual); rr += r.r; rf = (float)r
 __global__ void k_residual64(Ops64 A, LevelDims d, const double* x, const double* bvec, double* r, float* rf, Dots D,
                              int want_bb) {
-    const int b = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
     double rr = 0, bb = 0;
     if (c < d.nint) {
         int i, j, k;
@@ -165,7 +165,7 @@ __global__ void k_residual64(Ops64 A, LevelDims d, const double* x, const double
 // zAp += z.Ap
 __global__ void k_take_z(LevelDims d, const float* zf, const double* r, int use_r, double* z, const double* Ap, Dots D,
                          int want_zAp) {
-    const int b = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
     double za = 0;
     if (c < d.nint) {
         int i, j, k;
@@ -181,7 +181,7 @@ __global__ void k_take_z(LevelDims d, const float* zf, const double* r, int use_
 // p = z + beta p, beta = -z.Ap / p.Ap (flexible CG, one-term A-orthogonalisation);
 // restart (beta = 0) when `restart`
 __global__ void k_update_p(LevelDims d, double* p, const double* z, Dots D, int restart) {
-    const int b = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
     if (c >= d.nint) return;
     const int pb = D.bprob[b];
     if (!D.active[pb]) return;
@@ -199,7 +199,7 @@ __global__ void k_zero_f(float* v, size_t n) {
 
 // red-black Gauss-Seidel half sweep: z = (r - sum_nb A z_nb) / Aii on cells of one colour
 __global__ void k_rbgs(Ops32 A, LevelDims d, const float* r, float* z, int colour) {
-    const int b = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
     if (c >= d.nint) return;
     int i, j, k;
     cell_ijk(d, c, i, j, k);
@@ -216,7 +216,7 @@ __global__ void k_rbgs(Ops32 A, LevelDims d, const float* r, float* z, int colou
 
 // res = r - A z
 __global__ void k_resid32(Ops32 A, LevelDims d, const float* r, const float* z, float* res) {
-    const int b = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
     if (c >= d.nint) return;
     int i, j, k;
     cell_ijk(d, c, i, j, k);
@@ -226,7 +226,7 @@ __global__ void k_resid32(Ops32 A, LevelDims d, const float* r, const float* z, 
 
 // r_coarse(I) = sum of the 8 children of res_fine (R = P^T)
 __global__ void k_restrict(LevelDims f, LevelDims cd, const float* res, float* rc) {
-    const int b = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
     if (c >= cd.nint) return;
     const int I = c % cd.m0, J = (c / cd.m0) % cd.m1, K = c / (cd.m0 * cd.m1);
     const float* R = res + (size_t)b * f.nint;
@@ -241,7 +241,7 @@ __global__ void k_restrict(LevelDims f, LevelDims cd, const float* res, float* r
 
 // z_fine(child) += z_coarse(I) (injection)
 __global__ void k_prolong_add(LevelDims f, LevelDims cd, const float* zc, float* zf) {
-    const int b = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
     if (c >= f.nint) return;
     int i, j, k;
     cell_ijk(f, c, i, j, k);
@@ -300,7 +300,8 @@ struct falcon_solver {
 
 namespace {
 
-dim3 grid_cells(const LevelDims& d, int nblocks) { return dim3((unsigned)((d.nint + 255) / 256), (unsigned)nblocks); }
+// grid.x = block (up to 2^31-1 blocks), grid.y = 256-cell chunk of the block
+dim3 grid_cells(const LevelDims& d, int nblocks) { return dim3((unsigned)nblocks, (unsigned)((d.nint + 255) / 256)); }
 
 template <class T> cudaError_t halo_fill(falcon_solver* sv, int l, T* v) {
     const SvLevel& L = sv->lv[l];
@@ -428,14 +429,14 @@ int setup(falcon_solver* sv) {
 
 // scatter an interior [b][nint] FP64 vector into the padded x
 __global__ void k_scatter_pad(LevelDims d, const double* v, double* x) {
-    const int b = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
     if (c >= d.nint) return;
     int i, j, k;
     cell_ijk(d, c, i, j, k);
     x[pidx(d, b, i, j, k)] = v[(size_t)b * d.nint + c];
 }
 __global__ void k_gather_pad(LevelDims d, const double* x, double* v) {
-    const int b = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
     if (c >= d.nint) return;
     int i, j, k;
     cell_ijk(d, c, i, j, k);
