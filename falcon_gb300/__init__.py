@@ -46,8 +46,11 @@ EXPORTS = (
     "falcon_solver_create", "falcon_solver_destroy", "falcon_solver_last_error", "falcon_solver_info",
     "falcon_solver_problem_blocks", "falcon_solver_rhs", "falcon_solver_operator", "falcon_solver_halo_count",
     "falcon_solver_halo_map", "falcon_solver_apply", "falcon_solver_solve", "falcon_solver_solution",
-    "falcon_solver_timestep",
+    "falcon_solver_timestep", "falcon_download_state_range",
 )
+
+# size of the static device array behind falcon_download_state_range
+STATIC_SCRATCH_BYTES = 16 << 20
 
 _lib = None
 

@@ -26,6 +26,7 @@ UNITS = [
     ("mhd_mixed.cu", []),
     ("synth.cu", []),
     ("capi.cu", []),
+    ("state_range.cu", []),
     ("host_setup.cpp", []),
     ("solver.cu", ["-fmad=false"]),
     ("solver_host.cpp", []),

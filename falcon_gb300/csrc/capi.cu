@@ -16,6 +16,13 @@
 #include "kernels.cuh"
 #include "synth.cuh"
 
+namespace falcon {
+// state_range.cu: range download through the library's static device array
+size_t static_scratch_elems();
+std::string download_range_static(int dev, cudaStream_t st, const void* U, bool mixed, size_t first, size_t count,
+                                  double* u);
+}  // namespace falcon
+
 using namespace falcon;
 
 namespace {
@@ -498,6 +505,26 @@ int falcon_download_state(falcon_ctx* ctx, double* u) {
         CK(cudaMemcpyAsync(u, ctx->U, n * 8, cudaMemcpyDeviceToHost, ctx->st), "download");
     }
     CK(cudaStreamSynchronize(ctx->st), "download");
+    return FALCON_OK;
+}
+
+int falcon_download_state_range(falcon_ctx* ctx, size_t first, size_t count, double* u) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    if (!u && count) return ctx->fail(FALCON_ERR_INVALID_ARG, "null state");
+    const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
+    const size_t cap = static_scratch_elems();
+    if (count > cap)
+        return ctx->fail(FALCON_ERR_INVALID_ARG,
+                         "falcon_download_state_range: count " + std::to_string(count) +
+                             " exceeds the static scratch limit of " + std::to_string(cap) + " elements (" +
+                             std::to_string(FALCON_STATIC_SCRATCH_BYTES >> 20) + " MiB); download in smaller ranges");
+    if (first > n || count > n - first)
+        return ctx->fail(FALCON_ERR_INVALID_ARG, "falcon_download_state_range: first " + std::to_string(first) +
+                                                     " + count " + std::to_string(count) + " exceeds the state size " +
+                                                     std::to_string(n));
+    const std::string e = download_range_static(ctx->device, ctx->st, ctx->U, ctx->mixed(), first, count, u);
+    if (!e.empty()) return ctx->fail(FALCON_ERR_CUDA, e);
     return FALCON_OK;
 }
 

@@ -1,0 +1,72 @@
+// state_range.cu -- download a range of the state without allocating.
+//
+// falcon_download_state widens a MIXED (FP32) state through an FP64 device
+// staging buffer of the whole state, allocated on first use. The range
+// download here stages through one fixed array compiled into the library
+// instead, so it needs no cudaMalloc, no cudaFree and no host allocation.
+//
+// The array is shared by every context on a device and keeps what the last
+// call wrote into it. Each call overwrites the part it reads back (the first
+// `count` elements), so no part of it has to start at zero. A call finishes
+// with a stream synchronise, so calls made one after another never overlap;
+// calls that overlap on the GPU (several host threads, several contexts on one
+// device) race on the array and must be serialised by the caller.
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+
+#include "../../include/falcon_gb300.h"
+#include "kernels.cuh"
+
+// FALCON_STATIC_SCRATCH_BYTES (16 MiB) of FP64 staging, 256-byte aligned.
+static __device__ __align__(256) double g_range_scratch[FALCON_STATIC_SCRATCH_BYTES / sizeof(double)];
+
+namespace falcon {
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+double* g_scratch_ptr[kMaxDevices] = {};
+
+// The array's device address on device `dev`, which must be current. Resolved
+// once per device (the first call may also load the library's device code on
+// that device) and cached.
+cudaError_t scratch_on_device(int dev, double** out) {
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+        double* ptr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_range_scratch);
+        if (e != cudaSuccess) return e;
+        g_scratch_ptr[dev] = ptr;
+    }
+    *out = g_scratch_ptr[dev];
+    return cudaSuccess;
+}
+}  // namespace
+
+size_t static_scratch_elems() { return FALCON_STATIC_SCRATCH_BYTES / sizeof(double); }
+
+// Copy U[first, first + count) (FP32 if mixed, else FP64) to host u as FP64.
+// The caller has checked the range and count <= static_scratch_elems(), and
+// made `dev` current. Returns "" or the failing step.
+std::string download_range_static(int dev, cudaStream_t st, const void* U, bool mixed, size_t first, size_t count,
+                                  double* u) {
+    if (count == 0) return "";
+    cudaError_t e;
+    if (mixed) {
+        double* ptr = nullptr;
+        e = scratch_on_device(dev, &ptr);
+        if (e != cudaSuccess) return std::string("static scratch address: ") + cudaGetErrorString(e);
+        e = launch_widen_state((const float*)U + first, ptr, (int64_t)count, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(u, ptr, count * sizeof(double), cudaMemcpyDeviceToHost, st);
+    } else {
+        e = cudaMemcpyAsync(u, (const double*)U + first, count * sizeof(double), cudaMemcpyDeviceToHost, st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return std::string("range download: ") + cudaGetErrorString(e);
+    return "";
+}
+
+}  // namespace falcon

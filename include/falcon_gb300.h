@@ -152,6 +152,31 @@ int  falcon_ghost_map(const falcon_ctx* ctx, falcon_ghost_entry* out, int64_t ca
  * FP64<->FP32 conversion runs on the GPU through a device staging buffer. */
 int  falcon_upload_state(falcon_ctx* ctx, const double* u);
 int  falcon_download_state(falcon_ctx* ctx, double* u);
+/* Download elements [first, first + count) of the falcon_download_state
+ * layout into u (FP64), allocating nothing on the device or the host. It has
+ * no counterpart in the reference, whose state is resident in host memory.
+ *
+ * Who needs it: in MIXED mode falcon_download_state stages through an FP64
+ * device buffer of the whole state (twice the FP32 state), allocated on its
+ * first call. A caller whose state fills most of HBM has no room for that
+ * buffer, and a caller that fixes its device footprint before the run (a
+ * memory pool sized at start-up, a job that must not let a library grow its
+ * memory mid-run, where cudaMalloc/cudaFree would also synchronise the whole
+ * device) cannot let it be allocated. This call stages through one static
+ * device array of FALCON_STATIC_SCRATCH_BYTES (16 MiB) compiled into the
+ * library instead, so count is limited to FALCON_STATIC_SCRATCH_BYTES / 8
+ * elements; larger counts, or a range past the end of the state, return
+ * FALCON_ERR_INVALID_ARG without touching u. Download a whole state as a
+ * sequence of ranges. In FP64 mode the range is copied directly.
+ *
+ * The first MIXED-mode call on each device sets up the array's address
+ * (cudaGetSymbolAddress; it may load the library's device code): make that
+ * first call before any stream capture on the device. Every context on a
+ * device shares the one array, which keeps the last call's data; each call
+ * synchronises the context stream before returning, but calls that overlap on
+ * the GPU (from several host threads) race on the array: serialise them. */
+#define FALCON_STATIC_SCRATCH_BYTES (16u << 20)
+int  falcon_download_state_range(falcon_ctx* ctx, size_t first, size_t count, double* u);
 /* Page-lock a host buffer so that state transfers run at full link speed
  * (cudaHostRegister); unpin before freeing it. */
 int  falcon_pin_host(falcon_ctx* ctx, void* p, size_t bytes);
