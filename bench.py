@@ -36,13 +36,17 @@ sys.path.insert(0, ROOT)
 METRIC = "MHD cell-updates/s per RK4 step"
 UNIT = "cell-updates/s"
 STATE_BYTES_PER_VAR = 4          # FP32 stored state
+CORR_BYTES_PER_VAR = 1           # 8-bit correction of u^n
 NVAR = 8
 # algorithmic bytes per interior cell per RK4 step: 4 stages x (read u_s,
 # read u^n, write u_s+1) + diffusion (read, write) = 14 state passes of 8
-# variables, plus the CFL pass reading 6 variables
-BYTES_PER_CELL_STEP = NVAR * STATE_BYTES_PER_VAR * 14 + 6 * STATE_BYTES_PER_VAR   # 472
-STAGE_BYTES_PER_CELL = NVAR * STATE_BYTES_PER_VAR * 3                            # 96 per stage launch
-DIFF_BYTES_PER_CELL = NVAR * STATE_BYTES_PER_VAR * 2                             # 64
+# variables, plus the CFL pass reading 6 variables, plus the u^n correction
+# read and written by stage 4 and by the diffusion pass (4 passes of 8 bytes)
+BYTES_PER_CELL_STEP = (NVAR * STATE_BYTES_PER_VAR * 14 + 6 * STATE_BYTES_PER_VAR
+                       + NVAR * CORR_BYTES_PER_VAR * 4)                           # 504
+# per launch, averaged over the 4 stage launches (stage 4 adds 16 bytes)
+STAGE_BYTES_PER_CELL = NVAR * STATE_BYTES_PER_VAR * 3 + NVAR * CORR_BYTES_PER_VAR * 2 / 4   # 100
+DIFF_BYTES_PER_CELL = NVAR * STATE_BYTES_PER_VAR * 2 + NVAR * CORR_BYTES_PER_VAR * 2       # 80
 WORKLOAD = "yinyang_shell_mhd_21M_mixed"
 
 

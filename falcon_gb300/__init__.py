@@ -46,7 +46,7 @@ EXPORTS = (
     "falcon_solver_create", "falcon_solver_destroy", "falcon_solver_last_error", "falcon_solver_info",
     "falcon_solver_problem_blocks", "falcon_solver_rhs", "falcon_solver_operator", "falcon_solver_halo_count",
     "falcon_solver_halo_map", "falcon_solver_apply", "falcon_solver_solve", "falcon_solver_solution",
-    "falcon_solver_timestep", "falcon_download_state_range",
+    "falcon_solver_timestep", "falcon_download_state_range", "falcon_exchange_stats",
 )
 
 # size of the static device array behind falcon_download_state_range
@@ -248,6 +248,12 @@ class Falcon:
         c = (C.c_int64 * 3)()
         self._ck(self.L.falcon_ghost_list_sizes(self.h, c))
         return {"copy": c[0], "linear": c[1], "trilinear": c[2]}
+
+    def exchange_stats(self):
+        c = np.zeros(5, dtype=np.int64)
+        self._ck(self.L.falcon_exchange_stats(self.h, _ptr(c)))
+        return {"stage_copy": int(c[0]), "stage_linear": int(c[1]), "stage_trilinear": int(c[2]),
+                "pushed_faces": int(c[3]), "pushed_cells": int(c[4])}
 
     def device_bytes(self):
         b = C.c_int64()

@@ -19,8 +19,8 @@
 namespace falcon {
 // state_range.cu: range download through the library's static device array
 size_t static_scratch_elems();
-std::string download_range_static(int dev, cudaStream_t st, const void* U, bool mixed, size_t first, size_t count,
-                                  double* u);
+std::string download_range_static(int dev, cudaStream_t st, const void* U, const int8_t* Ulo, bool mixed,
+                                  size_t first, size_t count, double* u);
 }  // namespace falcon
 
 using namespace falcon;
@@ -41,13 +41,19 @@ struct falcon_ctx {
     size_t elem = 8;            // bytes per state element
     void* U = nullptr;          // u^n (primitive_IV)
     void* RK = nullptr;         // stage state (primitive_rk_IV)
+    int8_t* Ulo = nullptr;      // mixed mode: 8-bit correction of u^n (interior cells)
     double* stage64 = nullptr;  // FP64 staging buffer for mixed-mode transfers (lazy)
     double *gi = nullptr, *gj = nullptr, *gs = nullptr;
     float *gi_f = nullptr, *gj_f = nullptr, *gs_f = nullptr;
     int32_t* flags = nullptr;
     StepScalars* sc = nullptr;
-    GhostLists gl{};
+    GhostLists gl{};          // every ghost cell (the exchange after the diffusion pass)
+    GhostLists gl_stage{};    // face ghosts not pushed by the stage kernel (exchanges after stages)
+    PushTable push{};         // mixed path: faces the stage kernel writes into its output
+    void* R2 = nullptr;       // mixed path: second stage buffer (pushing needs out != in)
     int64_t ghost_counts[3] = {0, 0, 0};   // copy, 1-D, general entries on the device
+    int64_t stage_counts[3] = {0, 0, 0};   // the same for the stage exchanges
+    int64_t pushed_faces = 0, pushed_cells = 0;
     int kpar_stage = 0, kpar_diff = 0;      // chosen by the autotuner (0 = not tuned yet)
     cudaGraphExec_t graph = nullptr;
     int64_t steps_done = 0;
@@ -112,10 +118,22 @@ void collect(falcon_ctx* ctx) {
     ctx->pending.clear();
 }
 
+// Ghost fill of every ghost cell (faces, edges and corners), as the reference's
+// exchange does.
 cudaError_t ghost(falcon_ctx* ctx, void* u) {
     return timed(ctx, KN_GHOST, [&] {
         return ctx->mixed() ? launch_ghost_mixed(ctx->dims, ctx->gl, (float*)u, ctx->st)
                             : launch_ghost_fp64(ctx->dims, ctx->gl, (double*)u, ctx->st);
+    });
+}
+
+// Ghost fill between RK stages: face ghosts only (every stencil of the step
+// is axis-aligned, so edge and corner ghosts are never read before the full
+// exchange that ends the step), minus the faces the stage kernel pushed.
+cudaError_t ghost_stage(falcon_ctx* ctx, void* u) {
+    return timed(ctx, KN_GHOST, [&] {
+        return ctx->mixed() ? launch_ghost_mixed(ctx->dims, ctx->gl_stage, (float*)u, ctx->st)
+                            : launch_ghost_fp64(ctx->dims, ctx->gl_stage, (double*)u, ctx->st);
     });
 }
 
@@ -129,25 +147,38 @@ cudaError_t cfl(falcon_ctx* ctx) {
 }
 
 // One ModAdvance_rk4 (3_6/ModAdvance.f90:18-112) as a kernel sequence.
+// FP64: stages 2-4 read and write the stage buffer in place. Mixed: the stage
+// kernels push ghost faces into their output, so input and output differ:
+// U -> RK -> R2 -> RK -> U (stage 4 writes u^{n+1} over u^n cell by cell).
 cudaError_t enqueue_step(falcon_ctx* ctx) {
     cudaError_t e = cfl(ctx);
     if (e != cudaSuccess) return e;
     for (int s = 1; s <= 4; ++s) {
-        void* in = (s == 1) ? ctx->U : ctx->RK;
-        void* out = (s < 4) ? ctx->RK : ctx->U;
+        void* in;
+        void* out;
+        if (ctx->mixed()) {
+            void* const seq[5] = {ctx->U, ctx->RK, ctx->R2, ctx->RK, ctx->U};
+            in = seq[s - 1];
+            out = seq[s];
+        } else {
+            in = (s == 1) ? ctx->U : ctx->RK;
+            out = (s < 4) ? ctx->RK : ctx->U;
+        }
         e = timed(ctx, KN_STAGE, [&] {
             return ctx->mixed()
                        ? launch_stage_mixed(ctx->dims, ctx->geom(), (const float*)in, (const float*)ctx->U,
-                                            (float*)out, s, 1, ctx->sc, 1, ctx->kpar_stage, ctx->st)
+                                            (float*)out, ctx->Ulo, ctx->push, s, 1, ctx->sc, 1, ctx->kpar_stage,
+                                            ctx->st)
                        : launch_stage_fp64(ctx->dims, ctx->geom(), (const double*)in, (const double*)ctx->U,
                                            (double*)out, s, 1, ctx->sc, 1, ctx->kpar_stage, ctx->st);
         });
         if (e != cudaSuccess) return e;
-        e = ghost(ctx, out);
+        e = ghost_stage(ctx, out);
         if (e != cudaSuccess) return e;
     }
     e = timed(ctx, KN_DIFF, [&] {
-        return ctx->mixed() ? launch_diffusion_mixed(ctx->dims, ctx->geom(), (float*)ctx->U, ctx->sc, ctx->kpar_diff, ctx->st)
+        return ctx->mixed() ? launch_diffusion_mixed(ctx->dims, ctx->geom(), (float*)ctx->U, ctx->Ulo, ctx->sc,
+                                                     ctx->kpar_diff, ctx->st)
                             : launch_diffusion_fp64(ctx->dims, ctx->geom(), (double*)ctx->U, ctx->sc, ctx->kpar_diff, ctx->st);
     });
     if (e != cudaSuccess) return e;
@@ -175,11 +206,12 @@ int autotune(falcon_ctx* ctx) {
                 cudaError_t e;
                 if (which == 0)
                     e = ctx->mixed() ? launch_stage_mixed(ctx->dims, ctx->geom(), (const float*)ctx->RK, (const float*)ctx->U,
-                                                          (float*)ctx->RK, 2, 1, ctx->sc, 1, kp, ctx->st)
+                                                          (float*)ctx->R2, nullptr, ctx->push, 2, 1, ctx->sc, 1, kp, ctx->st)
                                      : launch_stage_fp64(ctx->dims, ctx->geom(), (const double*)ctx->RK, (const double*)ctx->U,
                                                          (double*)ctx->RK, 2, 1, ctx->sc, 1, kp, ctx->st);
                 else
-                    e = ctx->mixed() ? launch_diffusion_mixed(ctx->dims, ctx->geom(), (float*)ctx->RK, ctx->sc, kp, ctx->st)
+                    e = ctx->mixed() ? launch_diffusion_mixed(ctx->dims, ctx->geom(), (float*)ctx->RK, nullptr, ctx->sc, kp,
+                                                              ctx->st)
                                      : launch_diffusion_fp64(ctx->dims, ctx->geom(), (double*)ctx->RK, ctx->sc, kp, ctx->st);
                 cudaEventRecord(b, ctx->st);
                 if (e != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess) { ok = false; cudaGetLastError(); break; }
@@ -246,6 +278,10 @@ int setup_device(falcon_ctx* ctx) {
     CK(ctx->alloc(&ctx->RK, sbytes), "alloc RK");
     CK(cudaMemsetAsync(ctx->U, 0, sbytes, ctx->st), "memset");
     CK(cudaMemsetAsync(ctx->RK, 0, sbytes, ctx->st), "memset");
+    if (ctx->mixed()) {
+        CK(ctx->alloc(&ctx->Ulo, (size_t)nb * NV * g.ncell), "alloc U correction");
+        CK(cudaMemsetAsync(ctx->Ulo, 0, (size_t)nb * NV * g.ncell, ctx->st), "memset");
+    }
 
     // geometry and background tables (3_6/ModBlock.f90:188-265, 288-438)
     std::vector<double> gi((size_t)nb * GI_COUNT * g.nip), gj((size_t)nb * GJ_COUNT * g.njp), gs((size_t)nb * GS_COUNT);
@@ -309,73 +345,176 @@ int setup_device(falcon_ctx* ctx) {
     // weights within 1e-6 of 0 or 1 (an error of 1e-6*|du|, far below FP32
     // resolution of the stencil inputs' differences) so aligned neighbours
     // become plain copies and radial neighbours of other spacing 1-D blends.
-    // Copies and blends are sorted by target for coalesced writes.
+    // Two sets: every ghost cell (the exchange that ends a step) and the face
+    // ghosts the stage kernel does not push (the exchanges between stages).
     const bool snap = ctx->mixed();
-    std::vector<std::pair<int32_t, int32_t>> copies;
-    struct Lin { int32_t d, s, st; float w; };
-    std::vector<Lin> lins;
-    std::vector<int32_t> idst, isrc;
-    std::vector<double> iw, irot;
-    std::vector<uint8_t> ikind;
-    const int32_t strides[3] = {1, g.nip, g.nip * g.njp};
+    const int n3[3] = {g.ni, g.nj, g.nk};
+    struct GE {
+        int32_t d, src;
+        double w[3];
+        int nz, face;             // face: 2*axis + side of the target, -1 for edges and corners
+        int32_t tb, sb, t[3], base[3];
+        bool rotate;
+        double rot[2];
+    };
+    std::vector<GE> ges;
+    ges.reserve(g.ghosts.size());
     for (const auto& e : g.ghosts) {
-        int base[3] = {e.i0, e.j0, e.k0};
-        double w[3] = {e.w[0], e.w[1], e.w[2]};
+        GE q{};
+        q.base[0] = e.i0; q.base[1] = e.j0; q.base[2] = e.k0;
+        q.w[0] = e.w[0]; q.w[1] = e.w[1]; q.w[2] = e.w[2];
         if (snap)
-            for (int q = 0; q < 3; ++q) {
-                if (w[q] < 1e-6) w[q] = 0.0;
-                else if (w[q] > 1.0 - 1e-6) { w[q] = 0.0; base[q] += 1; }
+            for (int a = 0; a < 3; ++a) {
+                if (q.w[a] < 1e-6) q.w[a] = 0.0;
+                else if (q.w[a] > 1.0 - 1e-6) { q.w[a] = 0.0; q.base[a] += 1; }
             }
-        const int nz = (w[0] != 0.0) + (w[1] != 0.0) + (w[2] != 0.0);
-        const int32_t d = (int32_t)cell_off(g, e.e.tblock, e.e.ti, e.e.tj, e.e.tk);
-        const int32_t src = (int32_t)cell_off(g, e.e.sblock, base[0], base[1], base[2]);
-        if (!e.rotate && nz == 0) { copies.push_back({d, src}); continue; }
-        if (snap && !e.rotate && nz == 1) {
-            const int q = w[0] != 0.0 ? 0 : (w[1] != 0.0 ? 1 : 2);
-            lins.push_back({d, src, strides[q], (float)w[q]});
-            continue;
-        }
-        idst.push_back(d);
-        isrc.push_back(src);
-        iw.insert(iw.end(), {w[0], w[1], w[2]});
-        irot.insert(irot.end(), {e.rotate ? e.rot[0] : 0.0, e.rotate ? e.rot[1] : 0.0});
-        ikind.push_back((uint8_t)((nz ? 1 : 0) | (e.rotate ? 2 : 0)));
+        q.nz = (q.w[0] != 0.0) + (q.w[1] != 0.0) + (q.w[2] != 0.0);
+        q.tb = e.e.tblock; q.sb = e.e.sblock;
+        q.t[0] = e.e.ti; q.t[1] = e.e.tj; q.t[2] = e.e.tk;
+        q.d = (int32_t)cell_off(g, q.tb, q.t[0], q.t[1], q.t[2]);
+        q.src = (int32_t)cell_off(g, q.sb, q.base[0], q.base[1], q.base[2]);
+        q.rotate = e.rotate;
+        q.rot[0] = e.rotate ? e.rot[0] : 0.0;
+        q.rot[1] = e.rotate ? e.rot[1] : 0.0;
+        int nghost = 0, axis = -1, side = 0;
+        for (int a = 0; a < 3; ++a)
+            if (q.t[a] < 1 || q.t[a] > n3[a]) { ++nghost; axis = a; side = q.t[a] > n3[a]; }
+        q.face = nghost == 1 ? 2 * axis + side : -1;
+        ges.push_back(q);
     }
-    std::sort(copies.begin(), copies.end());
-    std::sort(lins.begin(), lins.end(), [](const Lin& a, const Lin& b) { return a.d < b.d; });
-    std::vector<int32_t> cdst(copies.size()), csrc(copies.size());
-    for (size_t q = 0; q < copies.size(); ++q) { cdst[q] = copies[q].first; csrc[q] = copies[q].second; }
-    std::vector<int32_t> ldst(lins.size()), lsrc(lins.size()), lst(lins.size());
-    std::vector<float> lw(lins.size());
-    for (size_t q = 0; q < lins.size(); ++q) { ldst[q] = lins[q].d; lsrc[q] = lins[q].s; lst[q] = lins[q].st; lw[q] = lins[q].w; }
-    auto up = [&](auto** dptr, const auto& vec, const char* what) -> cudaError_t {
+
+    // Faces pushed by the stage kernel (mixed path): every ghost cell of the
+    // target face from one source block, no rotation; theta/phi: plain copies
+    // shifted by the block extent; radial: same (j,k), one blend per layer.
+    std::vector<int32_t> ptgt((size_t)nb * 6, -1), prsrc((size_t)nb * 4, 0), prdst((size_t)nb * 4, 0);
+    std::vector<float> prw((size_t)nb * 4, 0.f);
+    std::vector<uint8_t> pushed(ges.size(), 0);
+    if (snap) {
+        struct FaceState { int32_t sb = -1; bool ok = true; int64_t count = 0; int32_t rsrc[2] = {-1, -1}; double rw[2] = {0, 0}; };
+        std::vector<FaceState> fs((size_t)nb * 6);
+        for (const GE& q : ges) {
+            if (q.face < 0) continue;
+            FaceState& f = fs[(size_t)q.tb * 6 + q.face];
+            if (!f.ok) continue;
+            const int a = q.face / 2, side = q.face % 2;
+            bool ok = !q.rotate && (f.sb < 0 || f.sb == q.sb) && q.sb != q.tb;
+            for (int c = 0; c < 3 && ok; ++c) {
+                if (c == a) continue;
+                ok = q.base[c] == q.t[c] && q.w[c] == 0.0;
+            }
+            if (ok && a != 0) ok = q.nz == 0 && q.base[a] - q.t[a] == (side == 0 ? n3[a] : -n3[a]);
+            if (ok && a == 0) {
+                const int layer = (q.t[0] == (side == 0 ? -1 : n3[0] + 1)) ? 0 : 1;
+                const int32_t sp = q.base[0] + 1;   // padded
+                const bool inb = q.w[0] == 0.0 ? (sp >= 2 && sp <= n3[0] + 1) : (sp >= 2 && sp <= n3[0]);
+                if (!inb) ok = false;
+                else if (f.rsrc[layer] < 0) { f.rsrc[layer] = sp; f.rw[layer] = q.w[0]; }
+                else ok = f.rsrc[layer] == sp && f.rw[layer] == q.w[0];
+            }
+            if (!ok) { f.ok = false; continue; }
+            f.sb = q.sb;
+            ++f.count;
+        }
+        for (int tb = 0; tb < nb; ++tb)
+            for (int face = 0; face < 6; ++face) {
+                FaceState& f = fs[(size_t)tb * 6 + face];
+                const int a = face / 2, side = face % 2;
+                const int64_t full = 2LL * (a == 0 ? n3[1] * n3[2] : a == 1 ? n3[0] * n3[2] : n3[0] * n3[1]);
+                if (!f.ok || f.sb < 0 || f.count != full) { f.ok = false; continue; }
+                const size_t slot = (size_t)f.sb * 6 + 2 * a + (1 - side);   // the source's side facing the target
+                if (ptgt[slot] >= 0) { f.ok = false; continue; }
+                ptgt[slot] = tb;
+                if (a == 0)
+                    for (int layer = 0; layer < 2; ++layer) {
+                        const size_t r = ((size_t)f.sb * 2 + (1 - side)) * 2 + layer;
+                        prsrc[r] = f.rsrc[layer];
+                        prw[r] = (float)f.rw[layer];
+                        // padded target index of the layer: side 0 -> Fortran -1, 0; side 1 -> n+1, n+2
+                        prdst[r] = side == 0 ? (layer == 0 ? 0 : 1) : (layer == 0 ? n3[0] + 2 : n3[0] + 3);
+                    }
+                ++ctx->pushed_faces;
+            }
+        for (size_t k = 0; k < ges.size(); ++k) {
+            const GE& q = ges[k];
+            if (q.face >= 0 && fs[(size_t)q.tb * 6 + q.face].ok) { pushed[k] = 1; ++ctx->pushed_cells; }
+        }
+    }
+
+    auto up = [&](auto** dptr, const auto& vec) -> cudaError_t {
         using E = typename std::remove_reference<decltype(vec)>::type::value_type;
         cudaError_t e = ctx->alloc(dptr, vec.size() * sizeof(E));
         if (e == cudaSuccess && !vec.empty()) e = cudaMemcpy(*dptr, vec.data(), vec.size() * sizeof(E), cudaMemcpyHostToDevice);
-        (void)what;
         return e;
     };
-    int32_t *cp_dst, *cp_src, *ln_dst, *ln_src, *ln_st, *ip_dst, *ip_src;
-    float* ln_w;
-    double *ip_w, *ip_rot;
-    uint8_t* ip_kind;
-    CK(up(&cp_dst, cdst, "ghosts"), "upload ghosts");
-    CK(up(&cp_src, csrc, "ghosts"), "upload ghosts");
-    CK(up(&ln_dst, ldst, "ghosts"), "upload ghosts");
-    CK(up(&ln_src, lsrc, "ghosts"), "upload ghosts");
-    CK(up(&ln_st, lst, "ghosts"), "upload ghosts");
-    CK(up(&ln_w, lw, "ghosts"), "upload ghosts");
-    CK(up(&ip_dst, idst, "ghosts"), "upload ghosts");
-    CK(up(&ip_src, isrc, "ghosts"), "upload ghosts");
-    CK(up(&ip_w, iw, "ghosts"), "upload ghosts");
-    CK(up(&ip_rot, irot, "ghosts"), "upload ghosts");
-    CK(up(&ip_kind, ikind, "ghosts"), "upload ghosts");
-    ctx->gl.cp = GhostCopyList{(int64_t)cdst.size(), cp_dst, cp_src};
-    ctx->gl.ln = GhostLinList{(int64_t)ldst.size(), ln_dst, ln_src, ln_st, ln_w};
-    ctx->gl.ip = GhostInterpList{(int64_t)idst.size(), ip_dst, ip_src, ip_w, ip_rot, ip_kind};
-    ctx->ghost_counts[0] = (int64_t)cdst.size();
-    ctx->ghost_counts[1] = (int64_t)ldst.size();
-    ctx->ghost_counts[2] = (int64_t)idst.size();
+    const int32_t strides[3] = {1, g.nip, g.nip * g.njp};
+    // build and upload one set of lists over the entries `keep` selects
+    auto build_lists = [&](auto keep, GhostLists& out, int64_t* counts) -> cudaError_t {
+        std::vector<std::pair<int32_t, int32_t>> copies;
+        struct Lin { int32_t d, s, st; float w; };
+        std::vector<Lin> lins;
+        std::vector<int32_t> idst, isrc;
+        std::vector<double> iw, irot;
+        std::vector<uint8_t> ikind;
+        for (size_t k = 0; k < ges.size(); ++k) {
+            if (!keep(k)) continue;
+            const GE& q = ges[k];
+            if (!q.rotate && q.nz == 0) { copies.push_back({q.d, q.src}); continue; }
+            if (snap && !q.rotate && q.nz == 1) {
+                const int a = q.w[0] != 0.0 ? 0 : (q.w[1] != 0.0 ? 1 : 2);
+                lins.push_back({q.d, q.src, strides[a], (float)q.w[a]});
+                continue;
+            }
+            idst.push_back(q.d);
+            isrc.push_back(q.src);
+            iw.insert(iw.end(), {q.w[0], q.w[1], q.w[2]});
+            irot.insert(irot.end(), {q.rot[0], q.rot[1]});
+            ikind.push_back((uint8_t)((q.nz ? 1 : 0) | (q.rotate ? 2 : 0)));
+        }
+        std::sort(copies.begin(), copies.end());
+        std::sort(lins.begin(), lins.end(), [](const Lin& a, const Lin& b) { return a.d < b.d; });
+        std::vector<int32_t> cdst(copies.size()), csrc(copies.size());
+        for (size_t q = 0; q < copies.size(); ++q) { cdst[q] = copies[q].first; csrc[q] = copies[q].second; }
+        std::vector<int32_t> ldst(lins.size()), lsrc(lins.size()), lst(lins.size());
+        std::vector<float> lw(lins.size());
+        for (size_t q = 0; q < lins.size(); ++q) { ldst[q] = lins[q].d; lsrc[q] = lins[q].s; lst[q] = lins[q].st; lw[q] = lins[q].w; }
+        int32_t *cp_dst, *cp_src, *ln_dst, *ln_src, *ln_st, *ip_dst, *ip_src;
+        float* ln_w;
+        double *ip_w, *ip_rot;
+        uint8_t* ip_kind;
+        cudaError_t e = up(&cp_dst, cdst);
+        if (e == cudaSuccess) e = up(&cp_src, csrc);
+        if (e == cudaSuccess) e = up(&ln_dst, ldst);
+        if (e == cudaSuccess) e = up(&ln_src, lsrc);
+        if (e == cudaSuccess) e = up(&ln_st, lst);
+        if (e == cudaSuccess) e = up(&ln_w, lw);
+        if (e == cudaSuccess) e = up(&ip_dst, idst);
+        if (e == cudaSuccess) e = up(&ip_src, isrc);
+        if (e == cudaSuccess) e = up(&ip_w, iw);
+        if (e == cudaSuccess) e = up(&ip_rot, irot);
+        if (e == cudaSuccess) e = up(&ip_kind, ikind);
+        if (e != cudaSuccess) return e;
+        out.cp = GhostCopyList{(int64_t)cdst.size(), cp_dst, cp_src};
+        out.ln = GhostLinList{(int64_t)ldst.size(), ln_dst, ln_src, ln_st, ln_w};
+        out.ip = GhostInterpList{(int64_t)idst.size(), ip_dst, ip_src, ip_w, ip_rot, ip_kind};
+        counts[0] = (int64_t)cdst.size();
+        counts[1] = (int64_t)ldst.size();
+        counts[2] = (int64_t)idst.size();
+        return cudaSuccess;
+    };
+    CK(build_lists([&](size_t) { return true; }, ctx->gl, ctx->ghost_counts), "upload ghosts");
+    CK(build_lists([&](size_t k) { return ges[k].face >= 0 && !pushed[k]; }, ctx->gl_stage, ctx->stage_counts),
+       "upload stage ghosts");
+    if (snap) {
+        int32_t *d_tgt, *d_rsrc, *d_rdst;
+        float* d_rw;
+        CK(up(&d_tgt, ptgt), "upload push table");
+        CK(up(&d_rsrc, prsrc), "upload push table");
+        CK(up(&d_rdst, prdst), "upload push table");
+        CK(up(&d_rw, prw), "upload push table");
+        ctx->push = PushTable{d_tgt, d_rsrc, d_rdst, d_rw};
+        CK(ctx->alloc(&ctx->R2, sbytes), "alloc R2");
+        CK(cudaMemsetAsync(ctx->R2, 0, sbytes, ctx->st), "memset");
+    }
 
     StepScalars s0{};
     s0.min_ratio_bits = 0x7FF0000000000000ull;
@@ -482,7 +621,8 @@ int falcon_upload_state(falcon_ctx* ctx, const double* u) {
         // FP64 host array -> device staging -> FP32 state (conversion on the GPU)
         if (!ctx->stage64) CK(ctx->alloc(&ctx->stage64, n * 8), "alloc staging");
         CK(cudaMemcpyAsync(ctx->stage64, u, n * 8, cudaMemcpyHostToDevice, ctx->st), "upload");
-        CK(launch_convert_state(ctx->stage64, (float*)ctx->U, (int64_t)n, ctx->st), "upload convert");
+        CK(launch_convert_state(ctx->stage64, (float*)ctx->U, ctx->Ulo, (int64_t)n, ctx->dims, ctx->st),
+           "upload convert");
     } else {
         CK(cudaMemcpyAsync(ctx->U, u, n * 8, cudaMemcpyHostToDevice, ctx->st), "upload");
     }
@@ -499,7 +639,7 @@ int falcon_download_state(falcon_ctx* ctx, double* u) {
     const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
     if (ctx->mixed()) {
         if (!ctx->stage64) CK(ctx->alloc(&ctx->stage64, n * 8), "alloc staging");
-        CK(launch_widen_state((const float*)ctx->U, ctx->stage64, (int64_t)n, ctx->st), "download convert");
+        CK(launch_widen_state((const float*)ctx->U, ctx->Ulo, ctx->stage64, (int64_t)n, ctx->st), "download convert");
         CK(cudaMemcpyAsync(u, ctx->stage64, n * 8, cudaMemcpyDeviceToHost, ctx->st), "download");
     } else {
         CK(cudaMemcpyAsync(u, ctx->U, n * 8, cudaMemcpyDeviceToHost, ctx->st), "download");
@@ -523,7 +663,7 @@ int falcon_download_state_range(falcon_ctx* ctx, size_t first, size_t count, dou
         return ctx->fail(FALCON_ERR_INVALID_ARG, "falcon_download_state_range: first " + std::to_string(first) +
                                                      " + count " + std::to_string(count) + " exceeds the state size " +
                                                      std::to_string(n));
-    const std::string e = download_range_static(ctx->device, ctx->st, ctx->U, ctx->mixed(), first, count, u);
+    const std::string e = download_range_static(ctx->device, ctx->st, ctx->U, ctx->Ulo, ctx->mixed(), first, count, u);
     if (!e.empty()) return ctx->fail(FALCON_ERR_CUDA, e);
     return FALCON_OK;
 }
@@ -549,6 +689,7 @@ int falcon_init_synthetic(falcon_ctx* ctx, int32_t kind, uint64_t seed, double m
     if (kind < 0 || kind > 1) return ctx->fail(FALCON_ERR_INVALID_ARG, "unknown synthetic kind");
     std::string e = synth_initial_state(ctx->grid, ctx->geom(), ctx->U, ctx->mixed(), kind, seed, mach, ctx->st);
     if (!e.empty()) return ctx->fail(FALCON_ERR_CUDA, e);
+    if (ctx->Ulo) CK(cudaMemsetAsync(ctx->Ulo, 0, (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell, ctx->st), "init");
     const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
     CK(cudaMemcpyAsync(ctx->RK, ctx->U, n * ctx->elem, cudaMemcpyDeviceToDevice, ctx->st), "init");
     CK(cudaStreamSynchronize(ctx->st), "init");
@@ -638,12 +779,14 @@ int falcon_step_phase(falcon_ctx* ctx, int32_t phase) {
         void* in = (s == 1) ? ctx->U : ctx->RK;
         void* out = (s < 4) ? ctx->RK : ctx->U;
         e = ctx->mixed() ? launch_stage_mixed(ctx->dims, ctx->geom(), (const float*)in, (const float*)ctx->U,
-                                              (float*)out, s, 1, ctx->sc, 1, ctx->kpar_stage, ctx->st)
+                                              (float*)out, ctx->Ulo, PushTable{}, s, 1, ctx->sc, 1, ctx->kpar_stage,
+                                              ctx->st)
                          : launch_stage_fp64(ctx->dims, ctx->geom(), (const double*)in, (const double*)ctx->U,
                                              (double*)out, s, 1, ctx->sc, 1, ctx->kpar_stage, ctx->st);
         if (e == cudaSuccess) e = ghost(ctx, out);
     } else {
-        e = ctx->mixed() ? launch_diffusion_mixed(ctx->dims, ctx->geom(), (float*)ctx->U, ctx->sc, ctx->kpar_diff, ctx->st)
+        e = ctx->mixed() ? launch_diffusion_mixed(ctx->dims, ctx->geom(), (float*)ctx->U, ctx->Ulo, ctx->sc,
+                                                  ctx->kpar_diff, ctx->st)
                          : launch_diffusion_fp64(ctx->dims, ctx->geom(), (double*)ctx->U, ctx->sc, ctx->kpar_diff, ctx->st);
         if (e == cudaSuccess) e = ghost(ctx, ctx->U);
         if (e == cudaSuccess) ++ctx->steps_done;
@@ -661,7 +804,7 @@ int falcon_download_stage_state(falcon_ctx* ctx, double* u) {
     const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
     if (ctx->mixed()) {
         if (!ctx->stage64) CK(ctx->alloc(&ctx->stage64, n * 8), "alloc staging");
-        CK(launch_widen_state((const float*)ctx->RK, ctx->stage64, (int64_t)n, ctx->st), "download convert");
+        CK(launch_widen_state((const float*)ctx->RK, nullptr, ctx->stage64, (int64_t)n, ctx->st), "download convert");
         CK(cudaMemcpyAsync(u, ctx->stage64, n * 8, cudaMemcpyDeviceToHost, ctx->st), "download");
     } else {
         CK(cudaMemcpyAsync(u, ctx->RK, n * 8, cudaMemcpyDeviceToHost, ctx->st), "download");
@@ -736,6 +879,14 @@ int falcon_tuning(falcon_ctx* ctx, int32_t* kpar_stage, int32_t* kpar_diffusion)
     if (rc) return rc;
     if (kpar_stage) *kpar_stage = ctx->kpar_stage;
     if (kpar_diffusion) *kpar_diffusion = ctx->kpar_diff;
+    return FALCON_OK;
+}
+
+int falcon_exchange_stats(const falcon_ctx* ctx, int64_t* out) {
+    if (!ctx || !out) return FALCON_ERR_INVALID_ARG;
+    for (int q = 0; q < 3; ++q) out[q] = ctx->stage_counts[q];
+    out[3] = ctx->pushed_faces;
+    out[4] = ctx->pushed_cells;
     return FALCON_OK;
 }
 

@@ -23,6 +23,47 @@ namespace falcon {
 
 enum { V_RHO1 = 0, V_VR = 1, V_VT = 2, V_VP = 3, V_BR = 4, V_BT = 5, V_BP = 6, V_S1 = 7, NV = 8 };
 
+// ---- compensated FP32 state of the mixed path --------------------------------
+// u^n is held as an FP32 value hi plus an 8-bit correction q (a second array
+// with the state's layout): u = hi + q * unit(hi), unit(hi) = ulp(hi)/256 =
+// 2^(e-158) for hi's biased exponent e. Rounding u^n to plain FP32 once a step
+// is the dominant error of an FP32 state against FP64 (the stage buffers are
+// transient and stay plain FP32); the correction keeps 8 more bits of u^n.
+// Only interior cells carry a correction; ghost cells keep q = 0.
+#ifdef __CUDACC__
+__device__ __forceinline__ float lo_unit(float hi) {
+    const int e = (__float_as_int(hi) >> 23) & 0xff;
+    return e >= 32 ? __int_as_float((e - 31) << 23) : 0.f;
+}
+__device__ __forceinline__ float lo_inv_unit(float hi) {   // 1/unit(hi) = 2^(158-e)
+    const int e = (__float_as_int(hi) >> 23) & 0xff;
+    return e >= 32 ? __int_as_float((285 - e) << 23) : 0.f;
+}
+// q for the residual r = u - hi (|r| <= ulp(hi)/2); NaN residuals give -127
+__device__ __forceinline__ int8_t lo_encode(float hi, float r) {
+    const float q = rintf(__fmul_rn(r, lo_inv_unit(hi)));
+    return (int8_t)(int)fminf(fmaxf(q, -127.f), 127.f);
+}
+__device__ __forceinline__ int8_t lo_encode64(float hi, double r) {
+    const double q = rint(r * (double)lo_inv_unit(hi));
+    return (int8_t)(int)fmin(fmax(q, -127.0), 127.0);
+}
+// (hi + q*unit(hi)) + d, rounded to the nearest (hi', q') pair: two error-free
+// FP32 sums (Knuth's TwoSum), no contraction (explicit _rn intrinsics)
+__device__ __forceinline__ float ff_add(float hi, int8_t q, float d, int8_t& q_out) {
+    const float l = __fmul_rn((float)q, lo_unit(hi));   // exact
+    const float s = __fadd_rn(hi, d);
+    const float bs = __fsub_rn(s, hi);
+    const float es = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bs)), __fsub_rn(d, bs));
+    const float t = __fadd_rn(es, l);
+    const float h = __fadd_rn(s, t);
+    const float bh = __fsub_rn(h, s);
+    const float r = __fadd_rn(__fsub_rn(s, __fsub_rn(h, bh)), __fsub_rn(t, bh));
+    q_out = lo_encode(h, r);
+    return h;
+}
+#endif
+
 // per-block radial (i) tables, padded length nip
 enum {
     GI_R = 0,      // r (cell centres incl. ghosts)
@@ -96,6 +137,20 @@ struct GhostLists {
     GhostInterpList ip;
 };
 
+// Ghost faces written by the stage kernel of the SOURCE block (mixed path).
+// A face of a target block is pushed when all its ghost cells (2 layers x the
+// full face) come from one source block of the same panel without rotation:
+// theta/phi faces as a translation by the block extent (plain copies), radial
+// faces as a 1-D blend per ghost layer of two adjacent source cells along i.
+// Indexed by the source block and its side: face = 2*axis + side (side 0: the
+// low side of the source, whose target lies below it on that axis).
+struct PushTable {
+    const int32_t* tgt;      // [b][6] target block, -1 = not pushed
+    const int32_t* rad_src;  // [b][2 sides][2 layers] padded i of the first source cell
+    const int32_t* rad_dst;  // [b][2][2] padded i of the target ghost cell
+    const float* rad_w;      // [b][2][2] weight of the second source cell (0: copy)
+};
+
 struct StepDims {
     int nblocks, ni, nj, nk, nip, njp, nkp, ncell;
 };
@@ -114,10 +169,14 @@ cudaError_t launch_cfl_fp64(const StepDims& d, const Geometry& g, const double* 
                             cudaStream_t st);
 cudaError_t launch_ghost_fp64(const StepDims& d, const GhostLists& gl, double* u, cudaStream_t st);
 
+// lo: the correction array of u^n (see lo_unit); the stage kernel updates it
+// at stage 4 only, the diffusion pass always; nullptr leaves u^n plain FP32.
+// push: faces written into `out` by the stage kernel (tgt == nullptr: none);
+// pushing needs out != in, since a target block may still be reading `in`.
 cudaError_t launch_stage_mixed(const StepDims& d, const Geometry& g, const float* in, const float* un,
-                               float* out, int stage, int bc_writeback, StepScalars* sc,
-                               int heat_on, int kpar, cudaStream_t st);
-cudaError_t launch_diffusion_mixed(const StepDims& d, const Geometry& g, float* u, StepScalars* sc,
+                               float* out, int8_t* lo, const PushTable& push, int stage, int bc_writeback,
+                               StepScalars* sc, int heat_on, int kpar, cudaStream_t st);
+cudaError_t launch_diffusion_mixed(const StepDims& d, const Geometry& g, float* u, int8_t* lo, StepScalars* sc,
                                    int kpar, cudaStream_t st);
 cudaError_t launch_cfl_mixed(const StepDims& d, const Geometry& g, const float* u, StepScalars* sc,
                              cudaStream_t st);
@@ -127,8 +186,10 @@ cudaError_t launch_finalize_dt(StepScalars* sc, cudaStream_t st);
 // k-chunk depths instantiated for this block size (returns the count)
 int kpar_candidates_fp64(const StepDims& d, int* out);
 int kpar_candidates_mixed(const StepDims& d, int* out);
-cudaError_t launch_convert_state(const double* src, float* dst, int64_t n, cudaStream_t st);
-cudaError_t launch_widen_state(const float* src, double* dst, int64_t n, cudaStream_t st);
+// FP64 <-> compensated FP32 state (lo may be nullptr: plain FP32)
+cudaError_t launch_convert_state(const double* src, float* dst, int8_t* lo, int64_t n, const StepDims& dm,
+                                 cudaStream_t st);
+cudaError_t launch_widen_state(const float* src, const int8_t* lo, double* dst, int64_t n, cudaStream_t st);
 
 // names of the kernels as they appear in profiles
 const char* const* kernel_names();

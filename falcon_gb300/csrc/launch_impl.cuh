@@ -22,8 +22,8 @@ template <> struct Cand<float> {
 };
 
 template <class T, int N, int KP>
-cudaError_t stage_n(const StepDims& d, const Geometry& g, const T* in, const T* un, T* out, int stage,
-                    int bcw, StepScalars* sc, int heat, cudaStream_t st) {
+cudaError_t stage_n(const StepDims& d, const Geometry& g, const T* in, const T* un, T* out, int8_t* lo,
+                    const PushTable& push, int stage, int bcw, StepScalars* sc, int heat, cudaStream_t st) {
     using S = Shape<T, N, N, N, KP>;
     static bool attr = false;
     if (!attr) {
@@ -32,12 +32,12 @@ cudaError_t stage_n(const StepDims& d, const Geometry& g, const T* in, const T* 
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    k_stage<T, N, N, N, KP><<<d.nblocks, S::NT, S::smem_stage, st>>>(in, un, out, g, sc, stage, bcw, heat);
+    k_stage<T, N, N, N, KP><<<d.nblocks, S::NT, S::smem_stage, st>>>(in, un, out, lo, push, g, sc, stage, bcw, heat);
     return cudaGetLastError();
 }
 
 template <class T, int N, int KP>
-cudaError_t diff_n(const StepDims& d, const Geometry& g, T* u, StepScalars* sc, cudaStream_t st) {
+cudaError_t diff_n(const StepDims& d, const Geometry& g, T* u, int8_t* lo, StepScalars* sc, cudaStream_t st) {
     using S = Shape<T, N, N, N, KP>;
     static bool attr = false;
     if (!attr) {
@@ -46,15 +46,15 @@ cudaError_t diff_n(const StepDims& d, const Geometry& g, T* u, StepScalars* sc, 
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    k_diffusion<T, N, N, N, KP><<<d.nblocks, S::NT, S::smem_diff, st>>>(u, g, sc);
+    k_diffusion<T, N, N, N, KP><<<d.nblocks, S::NT, S::smem_diff, st>>>(u, lo, g, sc);
     return cudaGetLastError();
 }
 
 template <class T>
-cudaError_t stage_any(const StepDims& d, const Geometry& g, const T* in, const T* un, T* out, int stage, int bcw,
-                      StepScalars* sc, int heat, int kpar, cudaStream_t st) {
+cudaError_t stage_any(const StepDims& d, const Geometry& g, const T* in, const T* un, T* out, int8_t* lo,
+                      const PushTable& push, int stage, int bcw, StepScalars* sc, int heat, int kpar, cudaStream_t st) {
 #define FALCON_STAGE_CASE(N, K) \
-    if (d.ni == N && kpar == K) return stage_n<T, N, K>(d, g, in, un, out, stage, bcw, sc, heat, st);
+    if (d.ni == N && kpar == K) return stage_n<T, N, K>(d, g, in, un, out, lo, push, stage, bcw, sc, heat, st);
     if (d.ni != d.nj || d.ni != d.nk) return cudaErrorInvalidValue;
     FALCON_STAGE_CASE(8, 2) FALCON_STAGE_CASE(8, 4)
     FALCON_STAGE_CASE(16, 1)
@@ -64,9 +64,10 @@ cudaError_t stage_any(const StepDims& d, const Geometry& g, const T* in, const T
 }
 
 template <class T>
-cudaError_t diff_any(const StepDims& d, const Geometry& g, T* u, StepScalars* sc, int kpar, cudaStream_t st) {
+cudaError_t diff_any(const StepDims& d, const Geometry& g, T* u, int8_t* lo, StepScalars* sc, int kpar,
+                     cudaStream_t st) {
 #define FALCON_DIFF_CASE(N, K) \
-    if (d.ni == N && kpar == K) return diff_n<T, N, K>(d, g, u, sc, st);
+    if (d.ni == N && kpar == K) return diff_n<T, N, K>(d, g, u, lo, sc, st);
     if (d.ni != d.nj || d.ni != d.nk) return cudaErrorInvalidValue;
     FALCON_DIFF_CASE(8, 2) FALCON_DIFF_CASE(8, 4)
     FALCON_DIFF_CASE(16, 1)

@@ -11,11 +11,11 @@ using impl::ghost_any;
 
 cudaError_t launch_stage_fp64(const StepDims& d, const Geometry& g, const double* in, const double* un, double* out,
                               int stage, int bcw, StepScalars* sc, int heat, int kpar, cudaStream_t st) {
-    return stage_any<double>(d, g, in, un, out, stage, bcw, sc, heat, kpar, st);
+    return stage_any<double>(d, g, in, un, out, nullptr, PushTable{}, stage, bcw, sc, heat, kpar, st);
 }
 cudaError_t launch_diffusion_fp64(const StepDims& d, const Geometry& g, double* u, StepScalars* sc,
                                   int kpar, cudaStream_t st) {
-    return diff_any<double>(d, g, u, sc, kpar, st);
+    return diff_any<double>(d, g, u, nullptr, sc, kpar, st);
 }
 cudaError_t launch_cfl_fp64(const StepDims& d, const Geometry& g, const double* u, StepScalars* sc, cudaStream_t st) {
     return cfl_any<double>(d, g, u, sc, st);
@@ -41,20 +41,34 @@ cudaError_t launch_finalize_dt(StepScalars* sc, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-__global__ void k_narrow(const double* s, float* d, int64_t n) {
-    for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x)
-        d[x] = (float)s[x];
+// FP64 -> compensated FP32: hi = RN(u); interior cells get the correction of
+// u - hi, ghost cells q = 0 (x counts from the start of the state)
+__global__ void k_narrow(const double* s, float* d, int8_t* lo, int64_t n, StepDims dm) {
+    for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+        const double u = s[x];
+        const float hi = (float)u;
+        d[x] = hi;
+        if (lo) {
+            const int c = (int)(x % dm.ncell);
+            const int ip = c % dm.nip, jp = (c / dm.nip) % dm.njp, kp = c / (dm.nip * dm.njp);
+            const bool interior = ip >= 2 && ip < dm.nip - 2 && jp >= 2 && jp < dm.njp - 2 && kp >= 2 && kp < dm.nkp - 2;
+            lo[x] = interior ? lo_encode64(hi, u - (double)hi) : (int8_t)0;
+        }
+    }
 }
-__global__ void k_widen(const float* s, double* d, int64_t n) {
-    for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x)
-        d[x] = (double)s[x];
+__global__ void k_widen(const float* s, const int8_t* lo, double* d, int64_t n) {
+    for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+        const float hi = s[x];
+        d[x] = lo ? (double)hi + (double)lo[x] * (double)lo_unit(hi) : (double)hi;
+    }
 }
-cudaError_t launch_convert_state(const double* src, float* dst, int64_t n, cudaStream_t st) {
-    k_narrow<<<1216, 256, 0, st>>>(src, dst, n);
+cudaError_t launch_convert_state(const double* src, float* dst, int8_t* lo, int64_t n, const StepDims& dm,
+                                 cudaStream_t st) {
+    k_narrow<<<1216, 256, 0, st>>>(src, dst, lo, n, dm);
     return cudaGetLastError();
 }
-cudaError_t launch_widen_state(const float* src, double* dst, int64_t n, cudaStream_t st) {
-    k_widen<<<1216, 256, 0, st>>>(src, dst, n);
+cudaError_t launch_widen_state(const float* src, const int8_t* lo, double* dst, int64_t n, cudaStream_t st) {
+    k_widen<<<1216, 256, 0, st>>>(src, lo, dst, n);
     return cudaGetLastError();
 }
 

@@ -177,13 +177,62 @@ __device__ __forceinline__ void apply_bc(T* tile, int lo, int hi, int fl, T* wb)
     }
 }
 
+// 1-D blend a*(1-w) + b*w with one fixed rounding sequence, so the ghost
+// fill and the stage kernel's pushed faces give identical values
+__device__ __forceinline__ float blend(float a, float b, float uw, float w) { return __fmaf_rn(a, uw, __fmul_rn(b, w)); }
+__device__ __forceinline__ double blend(double a, double b, double uw, double w) { return a * uw + b * w; }
+
+// Write this cell's new values into the ghost cells of the neighbours whose
+// faces are pushed (PushTable). (ii, jj, kp): padded indices of the cell; o:
+// its 8 new values. Theta/phi faces: the two interior layers next to the side
+// are copied to the target's opposite ghost layers (a shift of one block
+// extent). Radial faces: the thread at the first source cell of a ghost layer
+// blends it with the next cell along i, taken from the next lane (i is the
+// fastest thread index, and the second cell is never beyond the row). Every
+// thread of the CTA calls this (the shuffle needs the full warp).
+template <class T, class S>
+__device__ __forceinline__ void push_faces(T* out, const PushTable& P, int b, int ii, int jj, int kp,
+                                           const T (&o)[NV]) {
+    constexpr int NI = S::NIP - 4, NJ = S::NJP - 4, NK = S::NKP - 4;
+    const int32_t* tg = P.tgt + 6 * b;
+    auto put = [&](int tb, int kt, int jt, int it, const T (&val)[NV]) {
+        T* dst = out + (size_t)tb * NV * S::NCELL + ((size_t)kt * S::NJP + jt) * S::NIP + it;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) dst[(size_t)v * S::NCELL] = val[v];
+    };
+    if (jj <= 3 && tg[2] >= 0) put(tg[2], kp, jj + NJ, ii, o);
+    if (jj >= NJ && tg[3] >= 0) put(tg[3], kp, jj - NJ, ii, o);
+    if (kp <= 3 && tg[4] >= 0) put(tg[4], kp + NK, jj, ii, o);
+    if (kp >= NK && tg[5] >= 0) put(tg[5], kp - NK, jj, ii, o);
+    if (tg[0] >= 0 || tg[1] >= 0) {   // uniform over the CTA
+        T nx[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) nx[v] = __shfl_down_sync(0xffffffffu, o[v], 1);
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+            if (tg[side] < 0) continue;
+#pragma unroll
+            for (int layer = 0; layer < 2; ++layer) {
+                const int q = (b * 2 + side) * 2 + layer;
+                if (ii != P.rad_src[q]) continue;
+                const T w = (T)P.rad_w[q], uw = T(1) - w;
+                T val[NV];
+#pragma unroll
+                for (int v = 0; v < NV; ++v) val[v] = w == T(0) ? o[v] : blend(o[v], nx[v], uw, w);
+                put(tg[side], kp, jj, P.rad_dst[q], val);
+            }
+        }
+    }
+    (void)NI;
+}
+
 // ---------------------------------------------------------------------------
 // One RK stage of one block: boundary -> RHS (3_6/ModEquation.f90:24-162) ->
 // u_out = u^n + dt*R/(5-s) (3_6/ModAdvance.f90:87-93).
 template <class T, int NI, int NJ, int NK, int KPAR>
 __global__ void __launch_bounds__(NI* NJ* KPAR)
-k_stage(const T* in, const T* un, T* out, Geometry g, StepScalars* sc, int stage, int bc_writeback,
-        int heat_on) {
+k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, Geometry g, StepScalars* sc, int stage,
+        int bc_writeback, int heat_on) {
     using S = Shape<T, NI, NJ, NK, KPAR>;
     constexpr int NIP = S::NIP, PL = S::PL, W = S::W, WP = S::WP, NCELL = S::NCELL;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -368,13 +417,29 @@ k_stage(const T* in, const T* un, T* out, Geometry g, StepScalars* sc, int stage
 
         // stage update
         const T R[NV] = {Rrho, Rvr, Rvt, Rvp, RBr, RBt, RBp, Rs};
+        T o[NV];
+        if constexpr (Pol<T>::exact) {
 #pragma unroll
-        for (int v = 0; v < NV; ++v) {
-            const T u0 = u0s[v];
-            T o;
-            if (Pol<T>::exact) o = (T)((double)u0 + (dt * (double)R[v]) / divs);
-            else o = fmaf((float)dtk, (float)R[v], (float)u0);
-            out[base + (size_t)v * NCELL] = o;
+            for (int v = 0; v < NV; ++v) o[v] = (T)((double)u0s[v] + (dt * (double)R[v]) / divs);
+        } else if (ulo != nullptr && stage == 4) {
+            // u^{n+1} = u^n + dt*R with u^n and u^{n+1} compensated
+            int8_t q0[NV];
+#pragma unroll
+            for (int v = 0; v < NV; ++v) q0[v] = ulo[base + (size_t)v * NCELL];
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+                int8_t q1;
+                o[v] = ff_add((float)u0s[v], q0[v], __fmul_rn(dtk, (float)R[v]), q1);
+                ulo[base + (size_t)v * NCELL] = q1;
+            }
+        } else {
+#pragma unroll
+            for (int v = 0; v < NV; ++v) o[v] = fmaf((float)dtk, (float)R[v], (float)u0s[v]);
+        }
+#pragma unroll
+        for (int v = 0; v < NV; ++v) out[base + (size_t)v * NCELL] = o[v];
+        if constexpr (!Pol<T>::exact) {
+            if (push.tgt != nullptr) push_faces<T, S>(out, push, b, ii, jj, kp, o);
         }
     }
 }
@@ -384,7 +449,7 @@ k_stage(const T* in, const T* un, T* out, Geometry g, StepScalars* sc, int stage
 // u += 0.5*dt*R (3_6/ModAdvance.f90:101-108), in place.
 template <class T, int NI, int NJ, int NK, int KPAR>
 __global__ void __launch_bounds__(NI* NJ* KPAR)
-k_diffusion(T* u, Geometry g, StepScalars* sc) {
+k_diffusion(T* u, int8_t* ulo, Geometry g, StepScalars* sc) {
     using S = Shape<T, NI, NJ, NK, KPAR>;
     constexpr int NIP = S::NIP, PL = S::PL, W = S::W, NCELL = S::NCELL;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -463,6 +528,21 @@ k_diffusion(T* u, Geometry g, StepScalars* sc) {
             }
         }
         const size_t base = (size_t)kp * PL + jj * NIP + ii;
+        if constexpr (!Pol<T>::exact) {
+            if (ulo != nullptr) {
+                int8_t* blo = ulo + (size_t)b * NV * NCELL;
+                int8_t q0[NV];
+#pragma unroll
+                for (int v = 0; v < NV; ++v) q0[v] = blo[(size_t)v * NCELL + base];
+#pragma unroll
+                for (int v = 0; v < NV; ++v) {
+                    int8_t q1;
+                    blk[(size_t)v * NCELL + base] = ff_add((float)A(v, 0, 0, 0), q0[v], __fmul_rn(hdt_f, (float)R[v]), q1);
+                    blo[(size_t)v * NCELL + base] = q1;
+                }
+                continue;
+            }
+        }
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
             const T u0 = A(v, 0, 0, 0);
@@ -556,7 +636,7 @@ __global__ void __launch_bounds__(256) k_ghost_lin(T* u, GhostLinList L, int nce
 #pragma unroll
     for (int q = 0; q < NV; ++q) {
         const T* f = u + s + (size_t)q * ncell;
-        v[q] = f[0] * uw + f[st] * w;
+        v[q] = blend(f[0], f[st], uw, w);
     }
 #pragma unroll
     for (int q = 0; q < NV; ++q) u[d + (size_t)q * ncell] = v[q];

@@ -1,15 +1,17 @@
 // mhd_mixed.cu -- mixed-precision instantiation of the step kernels: FP32
-// state and stencil RHS; p1 assembled in FP64; FP64 CFL reduction and dt.
+// state (u^n compensated by an 8-bit correction) and stencil RHS; p1 assembled
+// in FP64; FP64 CFL reduction and dt.
 #include "launch_impl.cuh"
 
 namespace falcon {
 cudaError_t launch_stage_mixed(const StepDims& d, const Geometry& g, const float* in, const float* un, float* out,
-                               int stage, int bcw, StepScalars* sc, int heat, int kpar, cudaStream_t st) {
-    return impl::stage_any<float>(d, g, in, un, out, stage, bcw, sc, heat, kpar, st);
+                               int8_t* lo, const PushTable& push, int stage, int bcw, StepScalars* sc, int heat, int kpar,
+                               cudaStream_t st) {
+    return impl::stage_any<float>(d, g, in, un, out, lo, push, stage, bcw, sc, heat, kpar, st);
 }
-cudaError_t launch_diffusion_mixed(const StepDims& d, const Geometry& g, float* u, StepScalars* sc,
+cudaError_t launch_diffusion_mixed(const StepDims& d, const Geometry& g, float* u, int8_t* lo, StepScalars* sc,
                                    int kpar, cudaStream_t st) {
-    return impl::diff_any<float>(d, g, u, sc, kpar, st);
+    return impl::diff_any<float>(d, g, u, lo, sc, kpar, st);
 }
 cudaError_t launch_cfl_mixed(const StepDims& d, const Geometry& g, const float* u, StepScalars* sc, cudaStream_t st) {
     return impl::cfl_any<float>(d, g, u, sc, st);

@@ -48,18 +48,19 @@ cudaError_t scratch_on_device(int dev, double** out) {
 
 size_t static_scratch_elems() { return FALCON_STATIC_SCRATCH_BYTES / sizeof(double); }
 
-// Copy U[first, first + count) (FP32 if mixed, else FP64) to host u as FP64.
+// Copy U[first, first + count) (FP32 with its correction Ulo if mixed, else
+// FP64) to host u as FP64.
 // The caller has checked the range and count <= static_scratch_elems(), and
 // made `dev` current. Returns "" or the failing step.
-std::string download_range_static(int dev, cudaStream_t st, const void* U, bool mixed, size_t first, size_t count,
-                                  double* u) {
+std::string download_range_static(int dev, cudaStream_t st, const void* U, const int8_t* Ulo, bool mixed,
+                                  size_t first, size_t count, double* u) {
     if (count == 0) return "";
     cudaError_t e;
     if (mixed) {
         double* ptr = nullptr;
         e = scratch_on_device(dev, &ptr);
         if (e != cudaSuccess) return std::string("static scratch address: ") + cudaGetErrorString(e);
-        e = launch_widen_state((const float*)U + first, ptr, (int64_t)count, st);
+        e = launch_widen_state((const float*)U + first, Ulo ? Ulo + first : nullptr, ptr, (int64_t)count, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(u, ptr, count * sizeof(double), cudaMemcpyDeviceToHost, st);
     } else {
         e = cudaMemcpyAsync(u, (const double*)U + first, count * sizeof(double), cudaMemcpyDeviceToHost, st);

@@ -55,9 +55,11 @@ extern "C" {
 /* ---- precision modes ---------------------------------------------------- */
 /* FP64: every operation in IEEE double, no FMA contraction, same operation
  *       order as the reference; bit-comparable with the CPU oracle.
- * MIXED: state stored in FP32; stencil RHS and stage updates in FP32; the
- *       linearised-EOS pressure p1 (where the background terms cancel) is
- *       assembled in FP64; the CFL ratio, its min-reduction and dt are FP64. */
+ * MIXED: state stored in FP32, u^n with an 8-bit correction of its FP32
+ *       rounding that the end-of-step updates carry (error-free FP32 sums);
+ *       stencil RHS and stage updates in FP32; the linearised-EOS pressure p1
+ *       (where the background terms cancel) is assembled in FP64; the CFL
+ *       ratio, its min-reduction and dt are FP64. */
 #define FALCON_PREC_FP64   0
 #define FALCON_PREC_MIXED  1
 
@@ -219,6 +221,11 @@ int  falcon_timer_stop(falcon_ctx* ctx, double* ms);
 int  falcon_tuning(falcon_ctx* ctx, int32_t* kpar_stage, int32_t* kpar_diffusion);
 /* device ghost-fill lists: counts[0] exact copies, [1] 1-D blends, [2] trilinear/rotated */
 int  falcon_ghost_list_sizes(const falcon_ctx* ctx, int64_t* counts);
+/* the exchanges between RK stages (face ghosts only; every stencil of a step
+ * is axis-aligned, the exchange that ends the step fills edges and corners):
+ * out[0..2] list sizes as above, out[3] block faces whose ghosts the stage
+ * kernel writes directly (mixed mode), out[4] ghost cells on those faces */
+int  falcon_exchange_stats(const falcon_ctx* ctx, int64_t* out5);
 /* bytes of device memory held by the context */
 int  falcon_device_bytes(const falcon_ctx* ctx, int64_t* bytes);
 
