@@ -47,6 +47,11 @@ EXPORTS = (
     "falcon_solver_problem_blocks", "falcon_solver_rhs", "falcon_solver_operator", "falcon_solver_halo_count",
     "falcon_solver_halo_map", "falcon_solver_apply", "falcon_solver_solve", "falcon_solver_solution",
     "falcon_solver_timestep", "falcon_download_state_range", "falcon_exchange_stats",
+    "falcon_solver_set_rhs", "falcon_solver_coarse_shape", "falcon_solver_attach_lcc", "falcon_solver_record",
+    "falcon_solver_set_smoothing",
+    "falcon_lcc_create", "falcon_lcc_destroy", "falcon_lcc_last_error", "falcon_lcc_num_params",
+    "falcon_lcc_get_params", "falcon_lcc_set_params", "falcon_lcc_forward", "falcon_lcc_loss_grad",
+    "falcon_lcc_train",
 )
 
 # size of the static device array behind falcon_download_state_range
@@ -77,6 +82,7 @@ def lib():
         for n in EXPORTS:
             getattr(L, n).restype = C.c_int
         L.falcon_destroy.restype = None
+        L.falcon_lcc_destroy.restype = None
         L.falcon_create.argtypes = [C.POINTER(vp), C.POINTER(Config)]
         _lib = L
     return _lib

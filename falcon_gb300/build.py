@@ -30,6 +30,7 @@ UNITS = [
     ("host_setup.cpp", []),
     ("solver.cu", ["-fmad=false"]),
     ("solver_host.cpp", []),
+    ("lcc.cu", []),
 ]
 
 

@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "../../include/falcon_gb300.h"
+#include "lcc.h"
 #include "solver.h"
 
 namespace falcon {
@@ -249,6 +250,132 @@ __global__ void k_prolong_add(LevelDims f, LevelDims cd, const float* zc, float*
     zf[pidx(f, b, i, j, k)] += zc[pidx(cd, b, I, J, K)];
 }
 
+// ---- learned coarse correction: coarsest level <-> dense panel grids ---------
+// gmap[b][c]: panel-grid voxel of coarse cell c of block b
+
+// static input channels 1..7: the six face couplings / diag, (diag + sum)/diag
+__global__ void k_lcc_static(Ops64 A, LevelDims d, const int32_t* gmap, float* feat) {
+    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
+    if (c >= d.nint) return;
+    int i, j, k;
+    cell_ijk(d, c, i, j, k);
+    const size_t fi = ((size_t)b * d.m2 * d.m1 + (size_t)(k - 1) * d.m1 + (j - 1)) * (d.m0 + 1) + (i - 1);
+    const size_t fj = ((size_t)b * d.m2 * (d.m1 + 1) + (size_t)(k - 1) * (d.m1 + 1) + (j - 1)) * d.m0 + (i - 1);
+    const size_t fk = ((size_t)b * (d.m2 + 1) * d.m1 + (size_t)(k - 1) * d.m1 + (j - 1)) * d.m0 + (i - 1);
+    const double dg = A.Aii[(size_t)b * d.nint + c];
+    const double cpl[6] = {A.Ai[fi], A.Ai[fi + 1], A.Aj[fj], A.Aj[fj + d.m0], A.Ak[fk], A.Ak[fk + (size_t)d.m0 * d.m1]};
+    float* f = feat + (size_t)gmap[(size_t)b * d.nint + c] * 8;
+    double sum = dg;
+    for (int q = 0; q < 6; ++q) { f[1 + q] = (float)(cpl[q] / dg); sum += cpl[q]; }
+    f[7] = (float)(sum / dg);
+}
+
+// sum over coarse cells of (r/diag)^2
+__global__ void k_lcc_sumsq(LevelDims d, const float* r, const float* Aii, double* sum) {
+    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
+    double v = 0.0;
+    if (c < d.nint) {
+        const size_t q = (size_t)b * d.nint + c;
+        const double x = (double)r[q] / (double)Aii[q];
+        v = x * x;
+    }
+    block_sum_atomic(v, sum);
+}
+
+__device__ __forceinline__ double lcc_scale(const double* sum, int64_t n) {
+    const double s = sqrt(*sum / (double)n);
+    return s > 0.0 ? s : 1.0;
+}
+
+// input channel 0: (r/diag)/s, s = RMS of r/diag
+__global__ void k_lcc_feat(LevelDims d, const float* r, const float* Aii, const int32_t* gmap, const double* sum,
+                           int64_t n, float* feat) {
+    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
+    if (c >= d.nint) return;
+    const size_t q = (size_t)b * d.nint + c;
+    feat[(size_t)gmap[q] * 8] = (float)((double)r[q] / (double)Aii[q] / lcc_scale(sum, n));
+}
+
+// coarse correction z = s * y (padded coarse layout)
+__global__ void k_lcc_scatter(LevelDims d, const float* y, const int32_t* gmap, const double* sum, int64_t n, float* z) {
+    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
+    if (c >= d.nint) return;
+    int i, j, k;
+    cell_ijk(d, c, i, j, k);
+    z[pidx(d, b, i, j, k)] = (float)(lcc_scale(sum, n) * (double)y[gmap[(size_t)b * d.nint + c]]);
+}
+
+// training target: t = e/s (e: padded FP64 coarse solution)
+__global__ void k_lcc_target(LevelDims d, const double* e, const int32_t* gmap, const double* sum, int64_t n, float* t) {
+    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
+    if (c >= d.nint) return;
+    int i, j, k;
+    cell_ijk(d, c, i, j, k);
+    t[gmap[(size_t)b * d.nint + c]] = (float)(e[pidx(d, b, i, j, k)] / lcc_scale(sum, n));
+}
+
+// ---- Jacobi-preconditioned CG on one level (FP64): exact coarse errors -------
+// dots: [0] r.z  [1] p.Ap  [2] r.r (current); nd: the same for the next iterate
+__global__ void k_ccg_init(Ops64 A, LevelDims d, const float* rc, double* r, double* z, double* p, double* dots) {
+    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
+    double rz = 0, rr = 0;
+    if (c < d.nint) {
+        int i, j, k;
+        cell_ijk(d, c, i, j, k);
+        const size_t q = (size_t)b * d.nint + c;
+        const double rv = (double)rc[q], zv = rv / A.Aii[q];
+        r[q] = rv;
+        z[q] = zv;
+        p[pidx(d, b, i, j, k)] = zv;
+        rz = rv * zv;
+        rr = rv * rv;
+    }
+    block_sum_atomic(rz, &dots[0]);
+    block_sum_atomic(rr, &dots[2]);
+}
+
+__global__ void k_ccg_spmv(Ops64 A, LevelDims d, const double* p, double* Ap, double* dots) {
+    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
+    double pa = 0;
+    if (c < d.nint) {
+        int i, j, k;
+        cell_ijk(d, c, i, j, k);
+        const double y = apply_A<double>(A, d, p, b, c, i, j, k);
+        Ap[(size_t)b * d.nint + c] = y;
+        pa = p[pidx(d, b, i, j, k)] * y;
+    }
+    block_sum_atomic(pa, &dots[1]);
+}
+
+__global__ void k_ccg_update(Ops64 A, LevelDims d, double* x, const double* p, double* r, const double* Ap, double* z,
+                             const double* dots, double* nd) {
+    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
+    const double alpha = dots[0] / dots[1];
+    double rz = 0, rr = 0;
+    if (c < d.nint) {
+        int i, j, k;
+        cell_ijk(d, c, i, j, k);
+        const size_t P = pidx(d, b, i, j, k), q = (size_t)b * d.nint + c;
+        x[P] += alpha * p[P];
+        const double rv = r[q] - alpha * Ap[q], zv = rv / A.Aii[q];
+        r[q] = rv;
+        z[q] = zv;
+        rz = rv * zv;
+        rr = rv * rv;
+    }
+    block_sum_atomic(rz, &nd[0]);
+    block_sum_atomic(rr, &nd[2]);
+}
+
+__global__ void k_ccg_p(LevelDims d, double* p, const double* z, const double* dots, const double* nd) {
+    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
+    if (c >= d.nint) return;
+    int i, j, k;
+    cell_ijk(d, c, i, j, k);
+    const size_t P = pidx(d, b, i, j, k);
+    p[P] = z[(size_t)b * d.nint + c] + (nd[0] / dots[0]) * p[P];
+}
+
 }  // namespace sv
 }  // namespace falcon
 
@@ -280,6 +407,19 @@ struct falcon_solver {
     std::vector<void*> allocs;
     int nu_pre = 2, nu_post = 2, nu_coarse = 16;
     double dt_conduction = 0;
+    // learned coarse correction
+    falcon_lcc* net = nullptr;
+    int net_sweeps = 2;
+    bool use_net = false;                 // set per V-cycle by the solve
+    bool cmap_ok = false;
+    int cD = 0, cH = 0, cW = 0;           // dense panel grid of the coarsest level
+    int32_t* gmap = nullptr;              // [b][nint_c] -> panel-grid voxel
+    float *feat = nullptr, *yout = nullptr;
+    double* csum = nullptr;
+    double* cdots = nullptr;              // [6] scalars of the coarse CG
+    // recording of coarsest-level residuals (falcon_solver_record)
+    float* rec = nullptr;
+    int rec_max = 0, rec_n = 0;
     int fail(int c, const std::string& m) { err = m; return c; }
     template <class P> cudaError_t alloc(P** ptr, size_t bytes) {
         cudaError_t e = cudaMalloc((void**)ptr, bytes ? bytes : 16);
@@ -328,7 +468,27 @@ cudaError_t vcycle(falcon_solver* sv) {
         SvLevel& L = sv->lv[l];
         k_zero_f<<<1216, 256, 0, sv->st>>>(L.z, (size_t)nb * L.d.npad);
         e = cudaGetLastError();
-        smooth(l, l == nl - 1 ? sv->nu_coarse : sv->nu_pre, false);
+        const bool coarsest = l == nl - 1 && nl > 1;
+        if (coarsest && sv->rec && sv->rec_n < sv->rec_max && e == cudaSuccess)
+            e = cudaMemcpyAsync(sv->rec + (size_t)sv->rec_n++ * nb * L.d.nint, L.r, (size_t)nb * L.d.nint * 4,
+                                cudaMemcpyDeviceToDevice, sv->st);
+        if (coarsest && sv->use_net && e == cudaSuccess) {
+            // z_c = s * net(r_c / diag / s, operator) then a few sweeps
+            const int64_t N = (int64_t)nb * L.d.nint;
+            e = cudaMemsetAsync(sv->csum, 0, 8, sv->st);
+            if (e == cudaSuccess) {
+                k_lcc_sumsq<<<grid_cells(L.d, nb), 256, 0, sv->st>>>(L.d, L.r, L.fAii, sv->csum);
+                k_lcc_feat<<<grid_cells(L.d, nb), 256, 0, sv->st>>>(L.d, L.r, L.fAii, sv->gmap, sv->csum, N, sv->feat);
+                e = lcc::forward_device(sv->net, sv->feat, 2, sv->cD, sv->cH, sv->cW, sv->yout, sv->st);
+            }
+            if (e == cudaSuccess) {
+                k_lcc_scatter<<<grid_cells(L.d, nb), 256, 0, sv->st>>>(L.d, sv->yout, sv->gmap, sv->csum, N, L.z);
+                e = cudaGetLastError();
+            }
+            smooth(l, sv->net_sweeps, false);
+        } else {
+            smooth(l, l == nl - 1 ? sv->nu_coarse : sv->nu_pre, false);
+        }
         if (l + 1 < nl && e == cudaSuccess) {
             e = halo_fill<float>(sv, l, L.z);
             if (e != cudaSuccess) break;
@@ -441,6 +601,115 @@ __global__ void k_gather_pad(LevelDims d, const double* x, double* v) {
     int i, j, k;
     cell_ijk(d, c, i, j, k);
     v[(size_t)b * d.nint + c] = x[pidx(d, b, i, j, k)];
+}
+
+// Map the coarsest level onto one dense grid per panel (single problem,
+// whole uniform blocks); builds gmap and the static input channels.
+int ensure_coarse_map(falcon_solver* sv) {
+    if (sv->cmap_ok) return FALCON_OK;
+    const SolverProblemSet& S = sv->S;
+    if (!sv->st) return sv->fail(FALCON_ERR_NO_DEVICE, "solver created without a device");
+    if (S.nproblems != 1) return sv->fail(FALCON_ERR_INVALID_ARG, "learned coarse correction: single-problem solvers only");
+    if (S.nlevels < 2) return sv->fail(FALCON_ERR_INVALID_ARG, "learned coarse correction: needs at least 2 levels");
+    const int lc = S.nlevels - 1, nb = S.nblocks;
+    const SolverLevel& C = S.L[lc];
+    const Grid& g = S.grids[0];
+    int tiles[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    std::vector<int32_t> bt((size_t)nb * 3), bpan(nb);
+    for (int pnl = 0; pnl < 2; ++pnl) {
+        int count = 0;
+        for (int ax = 0; ax < 3; ++ax) {
+            std::vector<double> starts;
+            for (int b = 0; b < nb; ++b)
+                if (((S.block_flags[b] & 1) != 0) == (pnl == 0)) starts.push_back(g.ranges[(size_t)b * 6 + ax * 2]);
+            std::sort(starts.begin(), starts.end());
+            std::vector<double> uniq;
+            for (double v : starts)
+                if (uniq.empty() || std::fabs(v - uniq.back()) > 1e-12 * std::max(1.0, std::fabs(v))) uniq.push_back(v);
+            tiles[pnl][ax] = (int)uniq.size();
+            for (int b = 0; b < nb; ++b) {
+                if (((S.block_flags[b] & 1) != 0) != (pnl == 0)) continue;
+                const double v = g.ranges[(size_t)b * 6 + ax * 2];
+                int idx = 0;
+                while (idx + 1 < (int)uniq.size() && v > uniq[idx] + 1e-12 * std::max(1.0, std::fabs(v))) ++idx;
+                bt[(size_t)b * 3 + ax] = idx;
+                bpan[b] = pnl;
+            }
+        }
+        for (int b = 0; b < nb; ++b) count += ((S.block_flags[b] & 1) != 0) == (pnl == 0);
+        if (count != tiles[pnl][0] * tiles[pnl][1] * tiles[pnl][2])
+            return sv->fail(FALCON_ERR_INVALID_ARG, "learned coarse correction: blocks do not tile the panels uniformly");
+    }
+    for (int ax = 0; ax < 3; ++ax)
+        if (tiles[0][ax] != tiles[1][ax]) return sv->fail(FALCON_ERR_INVALID_ARG, "learned coarse correction: panels differ");
+    const int D = tiles[0][0] * C.m[0], H = tiles[0][1] * C.m[1], W = tiles[0][2] * C.m[2];
+    if (D % 8 || H % 8 || W % 8)
+        return sv->fail(FALCON_ERR_INVALID_ARG, "learned coarse correction: coarse panel grid " + std::to_string(D) + "x" +
+                                                    std::to_string(H) + "x" + std::to_string(W) + " is not a multiple of 8");
+    const int nint = C.nint();
+    std::vector<int32_t> gm((size_t)nb * nint);
+    for (int b = 0; b < nb; ++b)
+        for (int c = 0; c < nint; ++c) {
+            const int i = c % C.m[0], j = (c / C.m[0]) % C.m[1], k = c / (C.m[0] * C.m[1]);
+            const int64_t vox = (int64_t)bpan[b] * D * H * W +
+                                ((int64_t)(bt[(size_t)b * 3] * C.m[0] + i) * H + bt[(size_t)b * 3 + 1] * C.m[1] + j) * W +
+                                bt[(size_t)b * 3 + 2] * C.m[2] + k;
+            gm[(size_t)b * nint + c] = (int32_t)vox;
+        }
+    // every coarse cell lands on its own voxel of the two panel grids
+    {
+        std::vector<uint8_t> seen((size_t)2 * D * H * W, 0);
+        for (int32_t v : gm) {
+            if (v < 0 || (size_t)v >= seen.size() || seen[v])
+                return sv->fail(FALCON_ERR_INVALID_ARG, "learned coarse correction: block tiling is not a bijection");
+            seen[v] = 1;
+        }
+    }
+    SCK(sv->alloc(&sv->gmap, gm.size() * 4), "coarse map");
+    SCK(cudaMemcpy(sv->gmap, gm.data(), gm.size() * 4, cudaMemcpyHostToDevice), "coarse map");
+    SCK(sv->alloc(&sv->feat, (size_t)2 * D * H * W * 8 * 4), "coarse features");
+    SCK(sv->alloc(&sv->yout, (size_t)2 * D * H * W * 4), "coarse features");
+    SCK(sv->alloc(&sv->csum, 8), "coarse features");
+    SCK(sv->alloc(&sv->cdots, 6 * 8), "coarse features");
+    SvLevel& L = sv->lv[lc];
+    k_lcc_static<<<grid_cells(L.d, nb), 256, 0, sv->st>>>(L.ops64(), L.d, sv->gmap, sv->feat);
+    SCK(cudaGetLastError(), "coarse features");
+    SCK(cudaStreamSynchronize(sv->st), "coarse features");
+    sv->cD = D; sv->cH = H; sv->cW = W;
+    sv->cmap_ok = true;
+    return FALCON_OK;
+}
+
+// e = A_c^{-1} r_c on the coarsest level (r_c: FP32 [b][nint]) by Jacobi-PCG
+// to ||r|| <= 1e-10 ||r_c||; the solution stays in sv->x (padded FP64)
+int coarse_solve(falcon_solver* sv, const float* rc) {
+    const int lc = sv->S.nlevels - 1, nb = sv->S.nblocks;
+    SvLevel& L = sv->lv[lc];
+    const dim3 g = grid_cells(L.d, nb);
+    double* dots = sv->cdots;      // [0..2] current, [3..5] next
+    SCK(cudaMemsetAsync(sv->x, 0, (size_t)nb * L.d.npad * 8, sv->st), "coarse cg");
+    SCK(cudaMemsetAsync(sv->p, 0, (size_t)nb * L.d.npad * 8, sv->st), "coarse cg");
+    SCK(cudaMemsetAsync(dots, 0, 6 * 8, sv->st), "coarse cg");
+    k_ccg_init<<<g, 256, 0, sv->st>>>(L.ops64(), L.d, rc, sv->r, sv->z, sv->p, dots);
+    double h[6];
+    SCK(cudaMemcpyAsync(h, dots, 6 * 8, cudaMemcpyDeviceToHost, sv->st), "coarse cg");
+    SCK(cudaStreamSynchronize(sv->st), "coarse cg");
+    const double rr0 = h[2];
+    if (!(rr0 > 0)) return FALCON_OK;
+    for (int it = 0; it < 5000; ++it) {
+        SCK(halo_fill<double>(sv, lc, sv->p), "coarse cg");
+        SCK(cudaMemsetAsync(dots + 1, 0, 8, sv->st), "coarse cg");
+        SCK(cudaMemsetAsync(dots + 3, 0, 3 * 8, sv->st), "coarse cg");
+        k_ccg_spmv<<<g, 256, 0, sv->st>>>(L.ops64(), L.d, sv->p, sv->Ap, dots);
+        k_ccg_update<<<g, 256, 0, sv->st>>>(L.ops64(), L.d, sv->x, sv->p, sv->r, sv->Ap, sv->z, dots, dots + 3);
+        k_ccg_p<<<g, 256, 0, sv->st>>>(L.d, sv->p, sv->z, dots, dots + 3);
+        SCK(cudaGetLastError(), "coarse cg");
+        SCK(cudaMemcpyAsync(dots, dots + 3, 3 * 8, cudaMemcpyDeviceToDevice, sv->st), "coarse cg");
+        SCK(cudaMemcpyAsync(h, dots + 3, 3 * 8, cudaMemcpyDeviceToHost, sv->st), "coarse cg");
+        SCK(cudaStreamSynchronize(sv->st), "coarse cg");
+        if (h[2] <= 1e-20 * rr0) return FALCON_OK;
+    }
+    return sv->fail(FALCON_ERR_NOT_CONVERGED, "coarse solve did not reach 1e-10");
 }
 
 }  // namespace
@@ -613,7 +882,10 @@ int falcon_solver_apply(falcon_solver* sv, const double* x, double* y) {
 int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t precond, falcon_solve_report* rep) {
     if (!sv || !rep) return FALCON_ERR_INVALID_ARG;
     if (!sv->st) return sv->fail(FALCON_ERR_NO_DEVICE, "solver created without a device");
-    if (precond != FALCON_PRECOND_NONE && precond != FALCON_PRECOND_MG) return sv->fail(FALCON_ERR_INVALID_ARG, "unknown preconditioner");
+    if (precond != FALCON_PRECOND_NONE && precond != FALCON_PRECOND_MG && precond != FALCON_PRECOND_MG_LCC)
+        return sv->fail(FALCON_ERR_INVALID_ARG, "unknown preconditioner");
+    if (precond == FALCON_PRECOND_MG_LCC && (!sv->net || !sv->cmap_ok))
+        return sv->fail(FALCON_ERR_INVALID_ARG, "FALCON_PRECOND_MG_LCC needs falcon_solver_attach_lcc first");
     cudaSetDevice(sv->device);
     const SolverProblemSet& S = sv->S;
     const int nb = S.nblocks, np = S.nproblems;
@@ -638,13 +910,20 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
     SCK(cudaMemcpyAsync(bb.data(), sv->dots + 4 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "bb");
     SCK(cudaStreamSynchronize(sv->st), "bb");
     for (int q = 0; q < np; ++q) if (bb[q] <= 0) bb[q] = 1.0;
+    int pc = precond;   // FALCON_PRECOND_MG_LCC falls back to FALCON_PRECOND_MG on stagnation
     auto precondition = [&](int want_zAp) -> cudaError_t {
         cudaError_t e = cudaSuccess;
-        if (precond == FALCON_PRECOND_MG) { e = vcycle(sv); ++rep->vcycles; }
+        if (pc != FALCON_PRECOND_NONE) {
+            sv->use_net = pc == FALCON_PRECOND_MG_LCC;
+            e = vcycle(sv);
+            sv->use_net = false;
+            ++rep->vcycles;
+        }
         if (e != cudaSuccess) return e;
-        k_take_z<<<g, 256, 0, sv->st>>>(d, sv->lv[0].z, sv->r, precond == FALCON_PRECOND_NONE, sv->z, sv->Ap, sv->D(), want_zAp);
+        k_take_z<<<g, 256, 0, sv->st>>>(d, sv->lv[0].z, sv->r, pc == FALCON_PRECOND_NONE, sv->z, sv->Ap, sv->D(), want_zAp);
         return cudaGetLastError();
     };
+    std::vector<double> hist;   // max over active problems of the recursive relative residual
     // p = M r
     SCK(precondition(0), "precondition");
     k_update_p<<<g, 256, 0, sv->st>>>(d, sv->p, sv->z, sv->D(), 1);
@@ -660,8 +939,23 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
         SCK(cudaMemcpyAsync(rr.data(), sv->dots + 3 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "rr");
         SCK(cudaStreamSynchronize(sv->st), "rr");
         bool all = true;
+        double hmax = 0;
         for (int q = 0; q < np; ++q)
-            if (act[q] && std::sqrt(rr[q] / bb[q]) > tol) all = false;
+            if (act[q]) {
+                hmax = std::max(hmax, std::sqrt(rr[q] / bb[q]));
+                if (std::sqrt(rr[q] / bb[q]) > tol) all = false;
+            }
+        hist.push_back(hmax);
+        const size_t nh = hist.size();
+        if (!all && pc == FALCON_PRECOND_MG_LCC && nh > 8 && hist[nh - 1] > 0.5 * hist[nh - 5]) {
+            // stagnation: less than 2x in 4 iterations; plain MG for the rest, restarted
+            pc = FALCON_PRECOND_MG;
+            ++rep->fallbacks;
+            SCK(precondition(0), "precondition");
+            k_update_p<<<g, 256, 0, sv->st>>>(d, sv->p, sv->z, sv->D(), 1);
+            SCK(halo_fill<double>(sv, 0, sv->p), "halo");
+            continue;
+        }
         if (all) {
             // verify on the FP64 true residual; restart from it if the recurrence drifted
             SCK(cudaMemsetAsync(sv->dots + 3 * np, 0, (size_t)np * 8, sv->st), "dots");
@@ -729,6 +1023,95 @@ int falcon_solver_timestep(const falcon_solver* sv, double* dt) {
     if (!sv || !dt) return FALCON_ERR_INVALID_ARG;
     *dt = sv->dt_conduction;
     return FALCON_OK;
+}
+
+int falcon_solver_set_smoothing(falcon_solver* sv, int32_t nu_pre, int32_t nu_post, int32_t nu_coarse) {
+    if (!sv || nu_pre < 0 || nu_post < 0 || nu_coarse < 0 || nu_pre > 64 || nu_post > 64 || nu_coarse > 4096)
+        return FALCON_ERR_INVALID_ARG;
+    sv->nu_pre = nu_pre;
+    sv->nu_post = nu_post;
+    sv->nu_coarse = nu_coarse;
+    return FALCON_OK;
+}
+
+int falcon_solver_set_rhs(falcon_solver* sv, const double* b) {
+    if (!sv || !b) return FALCON_ERR_INVALID_ARG;
+    std::memcpy(sv->S.b.data(), b, sv->S.b.size() * 8);
+    if (sv->st) {
+        cudaSetDevice(sv->device);
+        SCK(cudaMemcpy(sv->bvec, b, sv->S.b.size() * 8, cudaMemcpyHostToDevice), "rhs");
+    }
+    return FALCON_OK;
+}
+
+int falcon_solver_coarse_shape(falcon_solver* sv, int32_t* shape) {
+    if (!sv || !shape) return FALCON_ERR_INVALID_ARG;
+    if (sv->st) cudaSetDevice(sv->device);
+    const int rc = ensure_coarse_map(sv);
+    if (rc) return rc;
+    shape[0] = 2; shape[1] = sv->cD; shape[2] = sv->cH; shape[3] = sv->cW;
+    return FALCON_OK;
+}
+
+int falcon_solver_attach_lcc(falcon_solver* sv, falcon_lcc* net, int32_t sweeps) {
+    if (!sv || !net || sweeps < 0 || sweeps > 64) return FALCON_ERR_INVALID_ARG;
+    if (sv->st) cudaSetDevice(sv->device);
+    const int rc = ensure_coarse_map(sv);
+    if (rc) return rc;
+    sv->net = net;
+    sv->net_sweeps = sweeps;
+    // size the network's buffers for this grid now, not inside a timed solve
+    SCK(lcc::forward_device(net, sv->feat, 2, sv->cD, sv->cH, sv->cW, sv->yout, sv->st), "lcc");
+    SCK(cudaStreamSynchronize(sv->st), "lcc");
+    return FALCON_OK;
+}
+
+int falcon_solver_record(falcon_solver* sv, double tol, int32_t max_iter, int32_t max_records, float* x, float* t,
+                         int32_t* nrecords) {
+    if (!sv || !x || !t || !nrecords || max_records < 1) return FALCON_ERR_INVALID_ARG;
+    if (sv->st) cudaSetDevice(sv->device);
+    int rc = ensure_coarse_map(sv);
+    if (rc) return rc;
+    const int lc = sv->S.nlevels - 1, nb = sv->S.nblocks;
+    SvLevel& L = sv->lv[lc];
+    const size_t per = (size_t)nb * L.d.nint;
+    float* rec = nullptr;
+    SCK(cudaMalloc(&rec, (size_t)max_records * per * 4), "record buffer");
+    sv->rec = rec;
+    sv->rec_max = max_records;
+    sv->rec_n = 0;
+    falcon_solve_report rep;
+    rc = falcon_solver_solve(sv, tol, max_iter, FALCON_PRECOND_MG, &rep);
+    sv->rec = nullptr;
+    const int n = sv->rec_n;
+    *nrecords = 0;
+    if (rc == FALCON_OK || rc == FALCON_ERR_NOT_CONVERGED) {
+        rc = FALCON_OK;
+        const size_t vox = (size_t)2 * sv->cD * sv->cH * sv->cW;
+        float* tdev = nullptr;
+        cudaError_t e = cudaMalloc(&tdev, vox * 4);
+        for (int q = 0; q < n && rc == FALCON_OK && e == cudaSuccess; ++q) {
+            const float* rq = rec + (size_t)q * per;
+            rc = coarse_solve(sv, rq);
+            if (rc) break;
+            const int64_t N = (int64_t)per;
+            e = cudaMemsetAsync(sv->csum, 0, 8, sv->st);
+            if (e != cudaSuccess) break;
+            k_lcc_sumsq<<<grid_cells(L.d, nb), 256, 0, sv->st>>>(L.d, rq, L.fAii, sv->csum);
+            k_lcc_feat<<<grid_cells(L.d, nb), 256, 0, sv->st>>>(L.d, rq, L.fAii, sv->gmap, sv->csum, N, sv->feat);
+            k_lcc_target<<<grid_cells(L.d, nb), 256, 0, sv->st>>>(L.d, sv->x, sv->gmap, sv->csum, N, tdev);
+            e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaMemcpyAsync(x + (size_t)q * vox * 8, sv->feat, vox * 8 * 4, cudaMemcpyDeviceToHost, sv->st);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(t + (size_t)q * vox, tdev, vox * 4, cudaMemcpyDeviceToHost, sv->st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(sv->st);
+            if (e == cudaSuccess) *nrecords = q + 1;
+        }
+        cudaFree(tdev);
+        if (e != cudaSuccess && rc == FALCON_OK) rc = sv->fail(FALCON_ERR_CUDA, std::string("record: ") + cudaGetErrorString(e));
+    }
+    cudaStreamSynchronize(sv->st);
+    cudaFree(rec);
+    return rc;
 }
 
 }  // extern "C"

@@ -1,0 +1,95 @@
+"""ctypes binding of the learned coarse-correction network (falcon_lcc_* in
+include/falcon_gb300.h)."""
+import ctypes as C
+
+import numpy as np
+
+from . import FalconError, OK, lib
+
+CIN = 8
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class LCC:
+    """The network on one GPU; parameters as one float32 vector."""
+
+    def __init__(self, device=0, seed=7):
+        self.L = lib()
+        h = C.c_void_p()
+        rc = self.L.falcon_lcc_create(C.byref(h), C.c_int32(device), C.c_uint64(seed))
+        self.h = h
+        if rc != OK:
+            msg = self.last_error()
+            self.L.falcon_lcc_destroy(h)
+            self.h = None
+            raise FalconError(rc, msg)
+        n = C.c_int64()
+        self._ck(self.L.falcon_lcc_num_params(self.h, C.byref(n)))
+        self.nparams = n.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.falcon_lcc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def last_error(self):
+        buf = C.create_string_buffer(512)
+        self.L.falcon_lcc_last_error(self.h, buf, C.c_size_t(512))
+        return buf.value.decode()
+
+    def _ck(self, rc):
+        if rc != OK:
+            raise FalconError(rc, self.last_error())
+
+    def params(self):
+        p = np.zeros(self.nparams, dtype=np.float32)
+        self._ck(self.L.falcon_lcc_get_params(self.h, _ptr(p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.nparams
+        self._ck(self.L.falcon_lcc_set_params(self.h, _ptr(p)))
+
+    @staticmethod
+    def _shape(x):
+        n, D, H, W, c = x.shape
+        assert c == CIN
+        return n, D, H, W
+
+    def forward(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        n, D, H, W = self._shape(x)
+        y = np.zeros((n, D, H, W), dtype=np.float32)
+        self._ck(self.L.falcon_lcc_forward(self.h, _ptr(x), C.c_int32(n), C.c_int32(D), C.c_int32(H), C.c_int32(W),
+                                           _ptr(y)))
+        return y
+
+    def loss_grad(self, x, t):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        n, D, H, W = self._shape(x)
+        g = np.zeros(self.nparams, dtype=np.float32)
+        loss = C.c_double()
+        self._ck(self.L.falcon_lcc_loss_grad(self.h, _ptr(x), _ptr(t), C.c_int32(n), C.c_int32(D), C.c_int32(H),
+                                             C.c_int32(W), C.byref(loss), _ptr(g)))
+        return loss.value, g
+
+    def train(self, x, t, epochs=10, batch=8, lr=1e-3, seed=1):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        n, D, H, W = self._shape(x)
+        losses = np.zeros(epochs, dtype=np.float32)
+        self._ck(self.L.falcon_lcc_train(self.h, _ptr(x), _ptr(t), C.c_int32(n), C.c_int32(D), C.c_int32(H),
+                                         C.c_int32(W), C.c_int32(epochs), C.c_int32(batch), C.c_float(lr),
+                                         C.c_uint64(seed), _ptr(losses)))
+        return losses

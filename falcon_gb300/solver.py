@@ -17,6 +17,7 @@ PFSS = 0
 CONDUCTION = 1
 PRECOND_NONE = 0
 PRECOND_MG = 1
+PRECOND_MG_LCC = 2
 
 
 class SolverSpec(C.Structure):
@@ -30,12 +31,15 @@ class SolverSpec(C.Structure):
 
 class SolveReport(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("converged", C.c_int32), ("vcycles", C.c_int32),
-                ("refinements", C.c_int32), ("rel_residual", C.c_double), ("ms", C.c_double)]
+                ("refinements", C.c_int32), ("rel_residual", C.c_double), ("ms", C.c_double),
+                ("fallbacks", C.c_int32), ("pad_", C.c_int32)]
 
 
 _SYMS = ("falcon_solver_create", "falcon_solver_last_error", "falcon_solver_info", "falcon_solver_problem_blocks",
          "falcon_solver_rhs", "falcon_solver_operator", "falcon_solver_halo_count", "falcon_solver_halo_map",
-         "falcon_solver_apply", "falcon_solver_solve", "falcon_solver_solution", "falcon_solver_timestep")
+         "falcon_solver_apply", "falcon_solver_solve", "falcon_solver_solution", "falcon_solver_timestep",
+         "falcon_solver_set_rhs", "falcon_solver_coarse_shape", "falcon_solver_attach_lcc", "falcon_solver_record",
+         "falcon_solver_set_smoothing")
 
 
 def _ptr(a):
@@ -151,7 +155,34 @@ class Solver:
                                         C.byref(rep))
         if check:
             self._ck(rc)
-        return {k: getattr(rep, k) for k, _ in SolveReport._fields_}
+        return {k: getattr(rep, k) for k, _ in SolveReport._fields_ if k != "pad_"}
+
+    def set_smoothing(self, nu_pre=2, nu_post=2, nu_coarse=16):
+        self._ck(self.L.falcon_solver_set_smoothing(self.h, C.c_int32(nu_pre), C.c_int32(nu_post),
+                                                    C.c_int32(nu_coarse)))
+
+    def set_rhs(self, b):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        assert b.size == self.nblocks * self.nint
+        self._ck(self.L.falcon_solver_set_rhs(self.h, _ptr(b)))
+
+    def coarse_shape(self):
+        s = (C.c_int32 * 4)()
+        self._ck(self.L.falcon_solver_coarse_shape(self.h, s))
+        return tuple(s)
+
+    def attach_lcc(self, net, sweeps=2):
+        self._ck(self.L.falcon_solver_attach_lcc(self.h, net.h, C.c_int32(sweeps)))
+        self._net = net   # keep the network alive while attached
+
+    def record(self, tol=1e-8, max_iter=100, max_records=16):
+        n, D, H, W = self.coarse_shape()
+        x = np.zeros((max_records * n, D, H, W, 8), dtype=np.float32)
+        t = np.zeros((max_records * n, D, H, W), dtype=np.float32)
+        nr = C.c_int32()
+        self._ck(self.L.falcon_solver_record(self.h, C.c_double(tol), C.c_int32(max_iter), C.c_int32(max_records),
+                                             _ptr(x), _ptr(t), C.byref(nr)))
+        return x[:nr.value * n], t[:nr.value * n]
 
     def solution(self):
         out = np.zeros((self.nblocks, self.m[2], self.m[1], self.m[0]))

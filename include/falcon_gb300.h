@@ -240,6 +240,10 @@ int  falcon_device_bytes(const falcon_ctx* ctx, int64_t* bytes);
 #define FALCON_SOLVER_CONDUCTION  1   /* backward-Euler anisotropic heat conduction */
 #define FALCON_PRECOND_NONE 0
 #define FALCON_PRECOND_MG   1         /* one FP32 V-cycle (red-black Gauss-Seidel) */
+/* one V-cycle whose coarsest-level smoothing is replaced by the learned
+ * coarse correction (falcon_solver_attach_lcc) followed by a few sweeps;
+ * falls back to FALCON_PRECOND_MG for the rest of a solve that stagnates */
+#define FALCON_PRECOND_MG_LCC 2
 
 typedef struct falcon_solver_spec {
     int32_t  kind;                     /* FALCON_SOLVER_* */
@@ -263,9 +267,12 @@ typedef struct falcon_solve_report {
     int32_t iterations, converged, vcycles, refinements;
     double  rel_residual;              /* max over problems of the FP64 ||b-Ax||/||b|| */
     double  ms;                        /* device time of the solve */
+    int32_t fallbacks;                 /* FALCON_PRECOND_MG_LCC: switches to plain MG */
+    int32_t pad_;
 } falcon_solve_report;
 
 typedef struct falcon_solver falcon_solver;
+typedef struct falcon_lcc falcon_lcc;   /* learned coarse correction (below) */
 
 int  falcon_solver_create(falcon_solver** out, const falcon_solver_spec* spec);
 void falcon_solver_destroy(falcon_solver* sv);
@@ -288,6 +295,57 @@ int  falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_
 int  falcon_solver_solution(falcon_solver* sv, double* x);
 /* conduction time step dt (dt_factor x the explicit stability limit) */
 int  falcon_solver_timestep(const falcon_solver* sv, double* dt);
+/* red-black Gauss-Seidel sweeps of the V-cycle: before and after the coarse
+ * correction on every level but the coarsest, and on the coarsest level
+ * (defaults 2, 2, 16) */
+int  falcon_solver_set_smoothing(falcon_solver* sv, int32_t nu_pre, int32_t nu_post, int32_t nu_coarse);
+/* replace the level-0 right-hand side [block][k][j][i] */
+int  falcon_solver_set_rhs(falcon_solver* sv, const double* b);
+/* Learned coarse correction (single-problem solvers of whole uniform blocks):
+ * the coarsest level gathered into one dense grid per Yin-Yang panel,
+ * shape4 = {2, D, H, W} (D radial, H theta, W phi cells; multiples of 8). */
+int  falcon_solver_coarse_shape(falcon_solver* sv, int32_t* shape4);
+/* use `net` in FALCON_PRECOND_MG_LCC solves, followed by `sweeps` red-black
+ * Gauss-Seidel sweeps at the coarsest level (the network stays owned by the
+ * caller and must outlive its use) */
+int  falcon_solver_attach_lcc(falcon_solver* sv, falcon_lcc* net, int32_t sweeps);
+/* Training pairs from a real solve: runs an MG-preconditioned FCG solve and
+ * records the coarsest-level residual r_c of each V-cycle (up to
+ * max_records); for each, solves A_c e_c = r_c to 1e-10 (Jacobi-PCG, FP64)
+ * and writes the network input x[2 r][D][H][W][8] (r_c/diag scaled by its RMS
+ * s, then the six face couplings / diag and the diagonal surplus / diag) and
+ * the target t[2 r][D][H][W] = e_c / s. nrecords receives r. */
+int  falcon_solver_record(falcon_solver* sv, double tol, int32_t max_iter, int32_t max_records, float* x, float* t,
+                          int32_t* nrecords);
+
+/* ---- learned coarse correction (no counterpart in the reference) --------
+ * A 4-level 3D convolutional U-Net that predicts the coarsest-level error of
+ * the conduction V-cycle from the coarsest-level residual and operator, used
+ * as a preconditioner stage inside the flexible CG (ModLinearSolver_
+ * Multigrid_CG, 3_5/ModLinearSolver.f90:313-427, is the method it extends).
+ * Input x[n][D][H][W][FALCON_LCC_CIN] (FP32, channels last; D, H, W multiples
+ * of 8), output y[n][D][H][W]. Layers (3x3x3 convolutions, zero padding,
+ * ReLU on all but the last): 8->16, 16->16 | pool | 16->32, 32->32 | pool |
+ * 32->64 | pool | 64->64 | up + skip | 64->32 | up + skip | 32->16 | up + skip
+ * | 16->16, 16->1. Parameters: per layer W[co][ci][27] (tap = (kd*3+kh)*3+kw)
+ * then b[co], concatenated. BF16 weights and activations on tensor cores with
+ * FP32 accumulation; FP32 master weights trained with Adam on a mean-square
+ * loss. */
+#define FALCON_LCC_CIN 8
+int  falcon_lcc_create(falcon_lcc** out, int32_t device, uint64_t seed);
+void falcon_lcc_destroy(falcon_lcc* net);
+int  falcon_lcc_last_error(const falcon_lcc* net, char* buf, size_t len);
+int  falcon_lcc_num_params(const falcon_lcc* net, int64_t* n);
+int  falcon_lcc_get_params(falcon_lcc* net, float* params);
+int  falcon_lcc_set_params(falcon_lcc* net, const float* params);  /* also resets Adam */
+int  falcon_lcc_forward(falcon_lcc* net, const float* x, int32_t n, int32_t D, int32_t H, int32_t W, float* y);
+/* mean-square loss against t[n][D][H][W] and its gradient for every parameter */
+int  falcon_lcc_loss_grad(falcon_lcc* net, const float* x, const float* t, int32_t n, int32_t D, int32_t H, int32_t W,
+                          double* loss, float* grad);
+/* epochs of Adam over nsamples (x, t) pairs in shuffled minibatches of `batch`;
+ * epoch_loss[epochs] receives the mean training loss of each epoch */
+int  falcon_lcc_train(falcon_lcc* net, const float* x, const float* t, int32_t nsamples, int32_t D, int32_t H,
+                      int32_t W, int32_t epochs, int32_t batch, float lr, uint64_t seed, float* epoch_loss);
 
 #ifdef __cplusplus
 }

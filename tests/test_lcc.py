@@ -1,0 +1,84 @@
+"""Learned coarse-correction network: the numpy oracle's backward pass against
+finite differences (CPU), and the GPU forward pass, loss and parameter
+gradients against the oracle (GPU).
+
+Tolerances: the GPU stores activations and activation gradients in BF16 and
+accumulates in FP32; the oracle rounds the same tensors to BF16 and
+accumulates in FP64, so the remaining differences are accumulation order and
+the BF16 roundings that it flips: relative L2 error <= 1e-2 for outputs and
+the loss, <= 3e-2 per layer for gradients.
+"""
+import numpy as np
+import pytest
+
+from oracle import lcc_oracle as O
+
+
+def _inputs(n, D, H, W, seed):
+    rs = np.random.default_rng(seed)
+    x = rs.normal(size=(n, D, H, W, 8))
+    # smooth along every axis so the convolutions see correlated data
+    for ax in (1, 2, 3):
+        x = (x + np.roll(x, 1, axis=ax) + np.roll(x, -1, axis=ax)) / 3.0
+    t = x[..., 0] * 0.5 + 0.25 * np.roll(x[..., 1], 1, axis=2)
+    return x.astype(np.float32), t.astype(np.float32)
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def test_oracle_gradients_match_finite_differences():
+    rs = np.random.default_rng(11)
+    p = O.init_params(3).astype(np.float64)
+    p += rs.normal(0, 0.01, p.size)          # nonzero biases
+    x, t = _inputs(1, 8, 8, 8, 5)
+    x, t = x.astype(np.float64), t.astype(np.float64)
+    loss, g = O.loss_and_grads(p, x, t, bf16_acts=False)
+    offs = np.cumsum([0] + [co * ci * 27 + co for ci, co in O.LAYERS])
+    idx = [int(offs[l] + rs.integers(0, offs[l + 1] - offs[l])) for l in range(len(O.LAYERS)) for _ in range(2)]
+    h = 1e-6
+    for i in idx:
+        pp, pm = p.copy(), p.copy()
+        pp[i] += h
+        pm[i] -= h
+        fd = (O.loss_and_grads(pp, x, t, False)[0] - O.loss_and_grads(pm, x, t, False)[0]) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-5 * max(abs(fd), 1e-3 * np.abs(g).max()), (i, fd, g[i])
+
+
+def test_oracle_param_count():
+    # 27 ci co + co per layer over the fixed layer table: about 0.29M parameters
+    assert O.num_params() == sum(co * ci * 27 + co for ci, co in O.LAYERS) == 294481
+
+
+@pytest.mark.gpu
+def test_gpu_forward_and_gradients_match_oracle(built_lib):
+    from falcon_gb300.lcc import LCC
+    net = LCC(device=0, seed=1)
+    assert net.nparams == O.num_params()
+    rs = np.random.default_rng(2)
+    p = O.init_params(4)
+    p = p + rs.normal(0, 0.01, p.size).astype(np.float32)
+    net.set_params(p)
+    assert np.array_equal(net.params(), p)
+    x, t = _inputs(2, 8, 16, 16, 9)
+    y = net.forward(x)
+    yo = np.stack([O.forward(p.astype(np.float64), x[s])[0] for s in range(2)])
+    assert _rel(y, yo) <= 1e-2, _rel(y, yo)
+    loss, g = net.loss_grad(x, t)
+    lo, go = O.loss_and_grads(p.astype(np.float64), x, t)
+    assert abs(loss - lo) <= 1e-2 * lo, (loss, lo)
+    offs = np.cumsum([0] + [co * ci * 27 + co for ci, co in O.LAYERS])
+    for l in range(len(O.LAYERS)):
+        sl = slice(offs[l], offs[l + 1])
+        assert _rel(g[sl], go[sl]) <= 3e-2, (l, _rel(g[sl], go[sl]))
+
+
+@pytest.mark.gpu
+def test_gpu_training_reduces_loss(built_lib):
+    from falcon_gb300.lcc import LCC
+    net = LCC(device=0, seed=3)
+    x, t = _inputs(16, 8, 16, 16, 21)
+    losses = net.train(x, t, epochs=30, batch=4, lr=2e-3, seed=5)
+    assert np.isfinite(losses).all()
+    assert losses[-1] < 0.2 * losses[0], losses
