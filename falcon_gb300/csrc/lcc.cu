@@ -53,6 +53,26 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
+// grid coordinates of voxel v (computed once per row, outside the tap loop)
+struct Vox { int64_t base; int d, h, w; bool ok; };   // base: first voxel of v's sample
+__device__ __forceinline__ Vox decompose(const Grid3& g, int64_t v, int64_t total) {
+    Vox x{0, 0, 0, 0, v >= 0 && v < total};
+    if (!x.ok) return x;
+    const int64_t plane = (int64_t)g.H * g.W, vol = plane * g.D;
+    const int64_t s = v / vol, r = v - s * vol;
+    x.base = s * vol;
+    x.d = (int)(r / plane);
+    const int r2 = (int)(r - (int64_t)x.d * plane);
+    x.h = r2 / g.W;
+    x.w = r2 - x.h * g.W;
+    return x;
+}
+__device__ __forceinline__ int64_t shifted(const Grid3& g, const Vox& x, int dd, int dh, int dw) {
+    const int d2 = x.d + dd, h2 = x.h + dh, w2 = x.w + dw;
+    if (!x.ok || d2 < 0 || d2 >= g.D || h2 < 0 || h2 >= g.H || w2 < 0 || w2 >= g.W) return -1;
+    return x.base + ((int64_t)d2 * g.H + h2) * g.W + w2;
+}
+
 // neighbour of voxel v at tap offset (dd, dh, dw) in {-1,0,1}^3, -1 if outside
 __device__ __forceinline__ int64_t neighbour(const Grid3& g, int64_t v, int dd, int dh, int dw) {
     if (v < 0) return -1;
@@ -85,11 +105,12 @@ __global__ void __launch_bounds__(128) k_conv(const __nv_bfloat16* __restrict__ 
     float acc[NT][4];
 #pragma unroll
     for (int j = 0; j < NT; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+    const Vox x0 = decompose(g, v0, total), x1 = decompose(g, v1, total);
     for (int tap = 0; tap < 27; ++tap) {
         const int sgn = MODE == 2 ? -1 : 1;
         const int dd = sgn * (tap / 9 - 1), dh = sgn * ((tap / 3) % 3 - 1), dw = sgn * (tap % 3 - 1);
-        const int64_t n0 = v0 < total ? neighbour(g, v0, dd, dh, dw) : -1;
-        const int64_t n1 = v1 < total ? neighbour(g, v1, dd, dh, dw) : -1;
+        const int64_t n0 = shifted(g, x0, dd, dh, dw);
+        const int64_t n1 = shifted(g, x1, dd, dh, dw);
         const __nv_bfloat16* wt = w + (size_t)tap * NC * KC;
 #pragma unroll
         for (int kc = 0; kc < KC; kc += 16) {

@@ -32,7 +32,7 @@ class SolverSpec(C.Structure):
 class SolveReport(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("converged", C.c_int32), ("vcycles", C.c_int32),
                 ("refinements", C.c_int32), ("rel_residual", C.c_double), ("ms", C.c_double),
-                ("fallbacks", C.c_int32), ("pad_", C.c_int32)]
+                ("fallbacks", C.c_int32), ("pad_", C.c_int32), ("floor_residual", C.c_double)]
 
 
 _SYMS = ("falcon_solver_create", "falcon_solver_last_error", "falcon_solver_info", "falcon_solver_problem_blocks",

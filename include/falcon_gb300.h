@@ -269,6 +269,10 @@ typedef struct falcon_solve_report {
     double  ms;                        /* device time of the solve */
     int32_t fallbacks;                 /* FALCON_PRECOND_MG_LCC: switches to plain MG */
     int32_t pad_;
+    /* > 0 when a problem stopped above tol at the accuracy FP64 attains for
+     * it: below 4 x 8 eps (|b| + |A||x|) / ||b||, or within 10 x tol and no
+     * longer improving between two true-residual checks (the largest such) */
+    double  floor_residual;
 } falcon_solve_report;
 
 typedef struct falcon_solver falcon_solver;
@@ -311,7 +315,7 @@ int  falcon_solver_coarse_shape(falcon_solver* sv, int32_t* shape4);
 int  falcon_solver_attach_lcc(falcon_solver* sv, falcon_lcc* net, int32_t sweeps);
 /* Training pairs from a real solve: runs an MG-preconditioned FCG solve and
  * records the coarsest-level residual r_c of each V-cycle (up to
- * max_records); for each, solves A_c e_c = r_c to 1e-10 (Jacobi-PCG, FP64)
+ * max_records); for each, solves A_c e_c = r_c to 1e-6 (Jacobi-PCG, FP64)
  * and writes the network input x[2 r][D][H][W][8] (r_c/diag scaled by its RMS
  * s, then the six face couplings / diag and the diagonal surplus / diag) and
  * the target t[2 r][D][H][W] = e_c / s. nrecords receives r. */
