@@ -327,7 +327,7 @@ def run_ours(args, rank, world, local, dist):
             "step_roofline": {"achieved": step_ach, "peak": hbm, "unit": "GB/s", "frac": step_ach / hbm,
                               "algorithmic_bytes_per_cell_step": BYTES_PER_CELL_STEP},
             "kernel_time_share": shares,
-            "tuning": f.tuning(), "ghost_lists": lists,
+            "tuning": f.tuning(), "ghost_lists": lists, "stage_exchange": f.exchange_stats(),
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                     "mode": "state uploaded and downloaded (FP64, pinned) every step"},
@@ -335,8 +335,70 @@ def run_ours(args, rank, world, local, dist):
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clk,
         }
+        if world == 1 and not args.no_solvers and args.workload == "full":
+            line["solvers"] = solver_bench(local)
         print(json.dumps(line))
     f.close()
+
+
+def _smooth_field(shape, rs):
+    x = rs.normal(size=shape)
+    for ax in (1, 2, 3):
+        for _ in range(3):
+            x = (x + np.roll(x, 1, axis=ax) + np.roll(x, -1, axis=ax)) / 3.0
+    return x
+
+
+def solver_bench(device):
+    """The implicit-solver workloads, each solved once after a warm-up solve:
+    conduction MG-PCG at 64x128x384 cells per panel, the learned coarse
+    correction against MG-PCG at 96x192x576 (trained on records of 64x128x384
+    solves with other seeds and right-hand sides), and the batch of 64 PFSS
+    problems. Times are CUDA-event times of the solve on the device."""
+    from falcon_gb300 import solver as S
+    from falcon_gb300.lcc import LCC
+    out = {}
+    t0 = time.time()
+    sv = S.Solver(S.conduction_spec(seed=3001, device=device))
+    sv.solve(tol=1e-8, max_iter=300, precond=S.PRECOND_MG, check=False)
+    mg = sv.solve(tol=1e-8, max_iter=300, precond=S.PRECOND_MG, check=False)
+    cg = sv.solve(tol=1e-8, max_iter=3000, precond=S.PRECOND_NONE, check=False)
+    out["conduction_64x128x384"] = {"cells": sv.nblocks * sv.nint, "tol": 1e-8, "mg_pcg": mg, "plain_cg": cg}
+    sv.close()
+    # training pairs from real solves: 3 systems x 4 right-hand sides
+    X, T = [], []
+    for s in range(3):
+        sv = S.Solver(S.conduction_spec(seed=3101 + 17 * s, device=device))
+        rs = np.random.default_rng(200 + s)
+        for r in range(4):
+            sv.set_rhs(sv.apply(_smooth_field((sv.nblocks,) + sv.m[::-1], rs)))
+            x, t = sv.record(tol=1e-8, max_iter=100, max_records=16)
+            X.append(x)
+            T.append(t)
+        sv.close()
+    X, T = np.concatenate(X), np.concatenate(T)
+    net = LCC(device=device, seed=11)
+    t1 = time.time()
+    losses = net.train(X, T, epochs=20, batch=8, lr=1e-3, seed=3)
+    train_s = time.time() - t1
+    sv = S.Solver(S.conduction_spec(nr=96, nt=192, np_=576, seed=9999, device=device))
+    sv.attach_lcc(net, sweeps=2)
+    res = {}
+    for pc, name in ((S.PRECOND_MG, "mg_pcg"), (S.PRECOND_MG_LCC, "learned_fcg")):
+        sv.solve(tol=1e-8, max_iter=600, precond=pc, check=False)
+        res[name] = sv.solve(tol=1e-8, max_iter=600, precond=pc, check=False)
+    out["learned_vs_mg_96x192x576"] = {
+        "cells": sv.nblocks * sv.nint, "tol": 1e-8, "training_pairs": int(len(X)), "train_s": round(train_s, 2),
+        "epoch_loss_first_last": [float(losses[0]), float(losses[-1])], **res,
+        "time_ratio_learned_over_mg": res["learned_fcg"]["ms"] / res["mg_pcg"]["ms"]}
+    sv.close()
+    sizes = S.random_pfss_sizes(64, seed=5000)
+    sv = S.Solver(S.pfss_spec(sizes, device=device))
+    rep = sv.solve(tol=1e-10, max_iter=3000, precond=S.PRECOND_MG, check=False)
+    out["pfss_batch64"] = {"problems": 64, "cells": sv.nblocks * sv.nint, "tol": 1e-10, "mg_pcg": rep}
+    sv.close()
+    out["wall_s"] = round(time.time() - t0, 1)
+    return out
 
 
 def main():
@@ -347,6 +409,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-solvers", action="store_true",
+                    help="skip the implicit-solver workloads reported under 'solvers'")
     ap.add_argument("--workload", default="full", choices=["full", "small"],
                     help="small: the 1,296-block profiling case (not a bench line)")
     args = ap.parse_args()

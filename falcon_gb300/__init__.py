@@ -48,7 +48,7 @@ EXPORTS = (
     "falcon_solver_halo_map", "falcon_solver_apply", "falcon_solver_solve", "falcon_solver_solution",
     "falcon_solver_timestep", "falcon_download_state_range", "falcon_exchange_stats",
     "falcon_solver_set_rhs", "falcon_solver_coarse_shape", "falcon_solver_attach_lcc", "falcon_solver_record",
-    "falcon_solver_set_smoothing",
+    "falcon_solver_set_smoothing", "falcon_solver_problem_residuals",
     "falcon_lcc_create", "falcon_lcc_destroy", "falcon_lcc_last_error", "falcon_lcc_num_params",
     "falcon_lcc_get_params", "falcon_lcc_set_params", "falcon_lcc_forward", "falcon_lcc_loss_grad",
     "falcon_lcc_train",

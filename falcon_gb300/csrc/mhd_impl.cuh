@@ -226,6 +226,26 @@ __device__ __forceinline__ void push_faces(T* out, const PushTable& P, int b, in
     (void)NI;
 }
 
+// Cell (i, j, kq) of a thread in a k-chunk. With 16-wide rows and an even
+// chunk depth a warp takes one row of two adjacent planes (lanes 0-15 plane
+// kq, 16-31 plane kq+1): a plane is 400 floats, 16 banks apart, so every
+// shared-memory access of the stencil is free of bank conflicts (two rows of
+// one plane, 20 floats apart, share 4 banks). Otherwise rows of one plane.
+// i stays the fastest index within 16 or 8 lanes either way.
+template <int NI, int NJ, int KPAR>
+__device__ __forceinline__ void cell_of_thread(int tid, int& i, int& j, int& kq) {
+    if constexpr (NI == 16 && KPAR % 2 == 0) {
+        i = tid % NI;
+        const int pair = (tid / NI) % 2;
+        j = (tid / (2 * NI)) % NJ;
+        kq = 2 * (tid / (2 * NI * NJ)) + pair;
+    } else {
+        i = tid % NI;
+        j = (tid / NI) % NJ;
+        kq = tid / (NI * NJ);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // One RK stage of one block: boundary -> RHS (3_6/ModEquation.f90:24-162) ->
 // u_out = u^n + dt*R/(5-s) (3_6/ModAdvance.f90:87-93).
@@ -259,7 +279,8 @@ k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, Geometry 
     __syncthreads();   // the geometry tables are read by every thread below
 
     const int tid = threadIdx.x;
-    const int i = tid % NI, j = (tid / NI) % NJ, kq = tid / (NI * NJ);
+    int i, j, kq;
+    cell_of_thread<NI, NJ, KPAR>(tid, i, j, kq);
     const int ii = i + 2, jj = j + 2;
     const T c1 = gs[GS_C1], c2 = gs[GS_C2], c3 = gs[GS_C3];
     const T* GR = gi + GI_R * NIP;
@@ -470,7 +491,8 @@ k_diffusion(T* u, int8_t* ulo, Geometry g, StepScalars* sc) {
     load_geometry<T, S>(g, b, gi, gj, gs, nullptr);
     __syncthreads();   // the geometry tables are read by every thread below
     const int tid = threadIdx.x;
-    const int i = tid % NI, j = (tid / NI) % NJ, kq = tid / (NI * NJ);
+    int i, j, kq;
+    cell_of_thread<NI, NJ, KPAR>(tid, i, j, kq);
     const int ii = i + 2, jj = j + 2;
     const T* GCS = gi + GI_CS * NIP;
     const T rc = gi[GI_R * NIP + ii];

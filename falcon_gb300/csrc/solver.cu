@@ -21,6 +21,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <map>
 #include <vector>
 
 #include "../../include/falcon_gb300.h"
@@ -436,6 +437,12 @@ struct falcon_solver {
     // recording of coarsest-level residuals (falcon_solver_record)
     float* rec = nullptr;
     int rec_max = 0, rec_n = 0;
+    // one instantiated CUDA graph per V-cycle shape (smoothing sweeps, network on/off)
+    std::map<int64_t, cudaGraphExec_t> vgraphs;
+    void clear_graphs() {
+        for (auto& kv : vgraphs) cudaGraphExecDestroy(kv.second);
+        vgraphs.clear();
+    }
     int fail(int c, const std::string& m) { err = m; return c; }
     template <class P> cudaError_t alloc(P** ptr, size_t bytes) {
         cudaError_t e = cudaMalloc((void**)ptr, bytes ? bytes : 16);
@@ -467,7 +474,7 @@ template <class T> cudaError_t halo_fill(falcon_solver* sv, int l, T* v) {
 }
 
 // z_0 = M r_0: one V-cycle on the FP32 residual stored in lv[0].r
-cudaError_t vcycle(falcon_solver* sv) {
+cudaError_t vcycle_body(falcon_solver* sv) {
     const int nl = (int)sv->lv.size(), nb = sv->S.nblocks;
     cudaError_t e = cudaSuccess;
     auto smooth = [&](int l, int sweeps, bool reverse) {
@@ -522,6 +529,31 @@ cudaError_t vcycle(falcon_solver* sv) {
         smooth(l, sv->nu_post, true);
     }
     return e;
+}
+
+// z_0 = M r_0 as one CUDA graph launch: the V-cycle's ~100 launches are
+// captured once per shape and replayed (recording calls run eagerly: their
+// destination changes from call to call)
+cudaError_t vcycle(falcon_solver* sv) {
+    if (sv->rec) return vcycle_body(sv);
+    const int64_t key = (int64_t)(sv->use_net ? 1 : 0) | ((int64_t)sv->nu_pre << 1) | ((int64_t)sv->nu_post << 8) |
+                        ((int64_t)sv->nu_coarse << 15) | ((int64_t)sv->net_sweeps << 28);
+    auto it = sv->vgraphs.find(key);
+    if (it == sv->vgraphs.end()) {
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(sv->st, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return e;
+        const cudaError_t eb = vcycle_body(sv);
+        e = cudaStreamEndCapture(sv->st, &g);
+        if (eb != cudaSuccess) { if (g) cudaGraphDestroy(g); return eb; }
+        if (e != cudaSuccess) return e;
+        cudaGraphExec_t x = nullptr;
+        e = cudaGraphInstantiate(&x, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return e;
+        it = sv->vgraphs.emplace(key, x).first;
+    }
+    return cudaGraphLaunch(it->second, sv->st);
 }
 
 int setup(falcon_solver* sv) {
@@ -815,6 +847,7 @@ void falcon_solver_destroy(falcon_solver* sv) {
     if (sv->st) {
         cudaSetDevice(sv->device);
         cudaStreamSynchronize(sv->st);
+        sv->clear_graphs();
         for (void* q : sv->allocs) cudaFree(q);
         cudaStreamDestroy(sv->st);
     }
@@ -1071,6 +1104,24 @@ int falcon_solver_set_smoothing(falcon_solver* sv, int32_t nu_pre, int32_t nu_po
     return FALCON_OK;
 }
 
+int falcon_solver_problem_residuals(falcon_solver* sv, double* rel) {
+    if (!sv || !rel) return FALCON_ERR_INVALID_ARG;
+    if (!sv->st) return sv->fail(FALCON_ERR_NO_DEVICE, "solver created without a device");
+    cudaSetDevice(sv->device);
+    const int np = sv->S.nproblems, nb = sv->S.nblocks;
+    const LevelDims& d = sv->lv[0].d;
+    SCK(cudaMemsetAsync(sv->dots, 0, (size_t)6 * np * 8, sv->st), "residuals");
+    SCK(halo_fill<double>(sv, 0, sv->x), "residuals");
+    k_residual64<<<grid_cells(d, nb), 256, 0, sv->st>>>(sv->lv[0].ops64(), d, sv->x, sv->bvec, sv->r, sv->lv[0].r,
+                                                        sv->D(), 1);
+    std::vector<double> rr(np), bb(np);
+    SCK(cudaMemcpyAsync(rr.data(), sv->dots + 3 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "residuals");
+    SCK(cudaMemcpyAsync(bb.data(), sv->dots + 4 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "residuals");
+    SCK(cudaStreamSynchronize(sv->st), "residuals");
+    for (int q = 0; q < np; ++q) rel[q] = bb[q] > 0 ? std::sqrt(rr[q] / bb[q]) : std::sqrt(rr[q]);
+    return FALCON_OK;
+}
+
 int falcon_solver_set_rhs(falcon_solver* sv, const double* b) {
     if (!sv || !b) return FALCON_ERR_INVALID_ARG;
     std::memcpy(sv->S.b.data(), b, sv->S.b.size() * 8);
@@ -1096,6 +1147,7 @@ int falcon_solver_attach_lcc(falcon_solver* sv, falcon_lcc* net, int32_t sweeps)
     const int rc = ensure_coarse_map(sv);
     if (rc) return rc;
     sv->net = net;
+    sv->clear_graphs();
     sv->net_sweeps = sweeps;
     // size the network's buffers for this grid now, not inside a timed solve
     SCK(lcc::forward_device(net, sv->feat, 2, sv->cD, sv->cH, sv->cW, sv->yout, sv->st), "lcc");

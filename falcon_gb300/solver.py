@@ -39,7 +39,7 @@ _SYMS = ("falcon_solver_create", "falcon_solver_last_error", "falcon_solver_info
          "falcon_solver_rhs", "falcon_solver_operator", "falcon_solver_halo_count", "falcon_solver_halo_map",
          "falcon_solver_apply", "falcon_solver_solve", "falcon_solver_solution", "falcon_solver_timestep",
          "falcon_solver_set_rhs", "falcon_solver_coarse_shape", "falcon_solver_attach_lcc", "falcon_solver_record",
-         "falcon_solver_set_smoothing")
+         "falcon_solver_set_smoothing", "falcon_solver_problem_residuals")
 
 
 def _ptr(a):
@@ -160,6 +160,11 @@ class Solver:
     def set_smoothing(self, nu_pre=2, nu_post=2, nu_coarse=16):
         self._ck(self.L.falcon_solver_set_smoothing(self.h, C.c_int32(nu_pre), C.c_int32(nu_post),
                                                     C.c_int32(nu_coarse)))
+
+    def problem_residuals(self):
+        out = np.zeros(self.nproblems)
+        self._ck(self.L.falcon_solver_problem_residuals(self.h, _ptr(out)))
+        return out
 
     def set_rhs(self, b):
         b = np.ascontiguousarray(b, dtype=np.float64)

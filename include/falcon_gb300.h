@@ -303,6 +303,9 @@ int  falcon_solver_timestep(const falcon_solver* sv, double* dt);
  * correction on every level but the coarsest, and on the coarsest level
  * (defaults 2, 2, 16) */
 int  falcon_solver_set_smoothing(falcon_solver* sv, int32_t nu_pre, int32_t nu_post, int32_t nu_coarse);
+/* FP64 true relative residual ||b - A x|| / ||b|| of every problem for the
+ * current solution (rel[nproblems]) */
+int  falcon_solver_problem_residuals(falcon_solver* sv, double* rel);
 /* replace the level-0 right-hand side [block][k][j][i] */
 int  falcon_solver_set_rhs(falcon_solver* sv, const double* b);
 /* Learned coarse correction (single-problem solvers of whole uniform blocks):
