@@ -495,7 +495,14 @@ int setup_device(falcon_ctx* ctx) {
         if (e != cudaSuccess) return e;
         out.cp = GhostCopyList{(int64_t)cdst.size(), cp_dst, cp_src};
         out.ln = GhostLinList{(int64_t)ldst.size(), ln_dst, ln_src, ln_st, ln_w};
-        out.ip = GhostInterpList{(int64_t)idst.size(), ip_dst, ip_src, ip_w, ip_rot, ip_kind};
+        float *ip_wf = nullptr, *ip_rotf = nullptr;
+        if (snap) {
+            std::vector<float> wf(iw.begin(), iw.end()), rf(irot.begin(), irot.end());
+            e = up(&ip_wf, wf);
+            if (e == cudaSuccess) e = up(&ip_rotf, rf);
+            if (e != cudaSuccess) return e;
+        }
+        out.ip = GhostInterpList{(int64_t)idst.size(), ip_dst, ip_src, ip_w, ip_rot, ip_kind, ip_wf, ip_rotf};
         counts[0] = (int64_t)cdst.size();
         counts[1] = (int64_t)ldst.size();
         counts[2] = (int64_t)idst.size();

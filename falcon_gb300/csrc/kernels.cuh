@@ -121,6 +121,8 @@ struct GhostInterpList {  // trilinear (and/or Yin-Yang rotated) ghost cells
     const double* w;        // [n][3] weights wi, wj, wk
     const double* rot;      // [n][2] rotation coefficients (0 if not rotated)
     const uint8_t* kind;    // bit0: interpolate, bit1: rotate
+    const float* wf;        // mixed path: FP32 copies of w and rot
+    const float* rotf;
 };
 
 struct GhostLinList {     // 1-D linear ghost cells (mixed path)

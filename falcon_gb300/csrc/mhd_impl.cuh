@@ -671,6 +671,43 @@ __global__ void __launch_bounds__(128) k_ghost_interp(T* u, GhostInterpList L, i
     const int kind = L.kind[e];
     const size_t s = (size_t)L.src[e];
     T val[NV];
+    if constexpr (!Pol<T>::exact) {
+        // FP32 weights; the Yin-Yang seam is aligned in r (wi == 0 after
+        // snapping), so most entries are bilinear in (j, k): 4 source points
+        const float wi = L.wf[3 * e], wj = L.wf[3 * e + 1], wk = L.wf[3 * e + 2];
+        const float ui = 1.f - wi, uj = 1.f - wj, uk = 1.f - wk;
+        if (!(kind & 1)) {
+#pragma unroll
+            for (int v = 0; v < NV; ++v) val[v] = u[s + (size_t)v * ncell];
+        } else if (wi == 0.f) {
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+                const T* f = u + s + (size_t)v * ncell;
+                val[v] = f[0] * uj * uk + f[nip] * wj * uk + f[pl] * uj * wk + f[nip + pl] * wj * wk;
+            }
+        } else {
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+                const T* f = u + s + (size_t)v * ncell;
+                val[v] = f[0] * ui * uj * uk + f[1] * wi * uj * uk + f[nip] * ui * wj * uk + f[pl] * ui * uj * wk +
+                         f[1 + nip] * wi * wj * uk + f[nip + pl] * ui * wj * wk + f[1 + pl] * wi * uj * wk +
+                         f[1 + nip + pl] * wi * wj * wk;
+            }
+        }
+        if (kind & 2) {
+            const float a = L.rotf[2 * e], c = L.rotf[2 * e + 1];
+            T x2 = val[V_BT], x3 = val[V_BP];
+            val[V_BT] = -(a * x2) - c * x3;
+            val[V_BP] = -(a * x3) + c * x2;
+            x2 = val[V_VT]; x3 = val[V_VP];
+            val[V_VT] = -(a * x2) - c * x3;
+            val[V_VP] = -(a * x3) + c * x2;
+        }
+        const size_t dd = (size_t)L.dst[e];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) u[dd + (size_t)v * ncell] = val[v];
+        return;
+    }
     if (kind & 1) {
         const T wi = (T)L.w[3 * e], wj = (T)L.w[3 * e + 1], wk = (T)L.w[3 * e + 2];
         const T ui = T(1) - wi, uj = T(1) - wj, uk = T(1) - wk;

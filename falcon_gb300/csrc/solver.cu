@@ -128,7 +128,8 @@ __global__ void k_spmv_dots(Ops64 A, LevelDims d, const double* p, double* Ap, c
 __global__ void k_update_xr(LevelDims d, double* x, const double* p, double* r, const double* Ap, float* rf, Dots D) {
     const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
     const int pb = D.bprob[b];
-    const double alpha = D.active[pb] ? D.pr[pb] / D.pAp[pb] : 0.0;
+    // a problem whose direction vanished (p.Ap == 0) takes no step instead of 0/0
+    const double alpha = (D.active[pb] && D.pAp[pb] != 0.0) ? D.pr[pb] / D.pAp[pb] : 0.0;
     double rr = 0;
     if (c < d.nint) {
         int i, j, k;
@@ -203,7 +204,7 @@ __global__ void k_update_p(LevelDims d, double* p, const double* z, Dots D, int 
     if (c >= d.nint) return;
     const int pb = D.bprob[b];
     if (!D.active[pb]) return;
-    const double beta = restart ? 0.0 : -D.zAp[pb] / D.pAp[pb];
+    const double beta = (restart || D.pAp[pb] == 0.0) ? 0.0 : -D.zAp[pb] / D.pAp[pb];
     int i, j, k;
     cell_ijk(d, c, i, j, k);
     const size_t P = pidx(d, b, i, j, k);
@@ -993,6 +994,9 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
         bool all = true;
         double hmax = 0;
         for (int q = 0; q < np; ++q)
+            if (act[q] && !std::isfinite(rr[q]))
+                return sv->fail(FALCON_ERR_NAN_DETECTED, "solver: non-finite residual in problem " + std::to_string(q));
+        for (int q = 0; q < np; ++q)
             if (act[q]) {
                 hmax = std::max(hmax, std::sqrt(rr[q] / bb[q]));
                 if (std::sqrt(rr[q] / bb[q]) > tol) all = false;
@@ -1026,6 +1030,8 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
             for (int q = 0; q < np; ++q) {
                 if (!act[q]) continue;
                 const double rel = std::sqrt(rr[q] / bb[q]);
+                if (!std::isfinite(rel))
+                    return sv->fail(FALCON_ERR_NAN_DETECTED, "solver: non-finite true residual in problem " + std::to_string(q));
                 const double floor_q = 4.0 * 8.0 * 2.220446049250313e-16 * std::sqrt(ab[q] / bb[q]);
                 // a true residual within 10x of tol that no longer improves between
                 // two verifications has reached what FP64 attains for this problem
@@ -1067,7 +1073,10 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
         SCK(cudaMemcpyAsync(rr.data(), sv->dots + 3 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "rr");
         SCK(cudaStreamSynchronize(sv->st), "rr");
         worst = 0;
-        for (int q = 0; q < np; ++q) worst = std::max(worst, std::sqrt(rr[q] / bb[q]));
+        for (int q = 0; q < np; ++q) {
+            const double rel = std::sqrt(rr[q] / bb[q]);
+            if (!(rel <= worst)) worst = rel;   // NaN propagates
+        }
     }
     rep->iterations = std::min(it, max_iter);
     rep->converged = done ? 1 : 0;
