@@ -11,8 +11,9 @@
 //     Galerkin coarse operators;
 //   - every problem of a batch is advanced by the same launches: kernels index
 //     block -> problem, scalars are per problem, converged problems freeze.
-// Kernels are launched with one CTA column per block (grid.x = block), so a CTA
-// never mixes problems and its reductions go to one per-problem slot.
+// Kernels are launched with one CTA per block (grid.x = block) looping over the
+// block's cells, so a CTA never mixes problems and its reductions go to one
+// per-problem slot with one atomic.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -107,17 +108,17 @@ struct Dots {
 
 // Ap = A p; pAp += p.Ap; pr += p.r (per problem)
 __global__ void k_spmv_dots(Ops64 A, LevelDims d, const double* p, double* Ap, const double* r, Dots D) {
-    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
+    const int b = blockIdx.x;
     double pa = 0, pr = 0;
-    if (c < d.nint) {
+    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
         const double y = apply_A<double>(A, d, p, b, c, i, j, k);
         const size_t q = (size_t)b * d.nint + c;
         Ap[q] = y;
         const double pv = p[pidx(d, b, i, j, k)];
-        pa = pv * y;
-        pr = pv * r[q];
+        pa += pv * y;
+        pr += pv * r[q];
     }
     const int pb = D.bprob[b];
     block_sum_atomic(pa, &D.pAp[pb]);
@@ -126,12 +127,12 @@ __global__ void k_spmv_dots(Ops64 A, LevelDims d, const double* p, double* Ap, c
 
 // alpha = p.r / p.Ap; x += alpha p; r -= alpha Ap; rr += r.r; rf = (float)r
 __global__ void k_update_xr(LevelDims d, double* x, const double* p, double* r, const double* Ap, float* rf, Dots D) {
-    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
+    const int b = blockIdx.x;
     const int pb = D.bprob[b];
     // a problem whose direction vanished (p.Ap == 0) takes no step instead of 0/0
     const double alpha = (D.active[pb] && D.pAp[pb] != 0.0) ? D.pr[pb] / D.pAp[pb] : 0.0;
     double rr = 0;
-    if (c < d.nint) {
+    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
         const size_t P = pidx(d, b, i, j, k), q = (size_t)b * d.nint + c;
@@ -139,7 +140,7 @@ __global__ void k_update_xr(LevelDims d, double* x, const double* p, double* r, 
         const double rv = r[q] - alpha * Ap[q];
         r[q] = rv;
         rf[q] = (float)rv;
-        rr = rv * rv;
+        rr += rv * rv;
     }
     block_sum_atomic(rr, &D.rr[pb]);
 }
@@ -160,19 +161,19 @@ __device__ __forceinline__ double abs_row(const Ops64& A, const LevelDims& d, co
 // r = b - A x (FP64 true residual); rr += r.r; ab += (|b| + sum|A x|)^2; rf = (float)r
 __global__ void k_residual64(Ops64 A, LevelDims d, const double* x, const double* bvec, double* r, float* rf, Dots D,
                              int want_bb) {
-    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
+    const int b = blockIdx.x;
     double rr = 0, bb = 0, ab = 0;
-    if (c < d.nint) {
+    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
         const size_t q = (size_t)b * d.nint + c;
         const double rv = bvec[q] - apply_A<double>(A, d, x, b, c, i, j, k);
         r[q] = rv;
         rf[q] = (float)rv;
-        rr = rv * rv;
-        bb = bvec[q] * bvec[q];
+        rr += rv * rv;
+        bb += bvec[q] * bvec[q];
         const double s = fabs(bvec[q]) + abs_row(A, d, x, b, c, i, j, k);
-        ab = s * s;
+        ab += s * s;
     }
     const int pb = D.bprob[b];
     block_sum_atomic(rr, &D.rr[pb]);
@@ -184,15 +185,15 @@ __global__ void k_residual64(Ops64 A, LevelDims d, const double* x, const double
 // zAp += z.Ap
 __global__ void k_take_z(LevelDims d, const float* zf, const double* r, int use_r, double* z, const double* Ap, Dots D,
                          int want_zAp) {
-    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
+    const int b = blockIdx.x;
     double za = 0;
-    if (c < d.nint) {
+    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
         const size_t q = (size_t)b * d.nint + c;
         const double zv = use_r ? r[q] : (double)zf[pidx(d, b, i, j, k)];
         z[q] = zv;
-        if (want_zAp) za = zv * Ap[q];
+        if (want_zAp) za += zv * Ap[q];
     }
     if (want_zAp) block_sum_atomic(za, &D.zAp[D.bprob[b]]);
 }
@@ -200,15 +201,16 @@ __global__ void k_take_z(LevelDims d, const float* zf, const double* r, int use_
 // p = z + beta p, beta = -z.Ap / p.Ap (flexible CG, one-term A-orthogonalisation);
 // restart (beta = 0) when `restart`
 __global__ void k_update_p(LevelDims d, double* p, const double* z, Dots D, int restart) {
-    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
-    if (c >= d.nint) return;
-    const int pb = D.bprob[b];
-    if (!D.active[pb]) return;
-    const double beta = (restart || D.pAp[pb] == 0.0) ? 0.0 : -D.zAp[pb] / D.pAp[pb];
-    int i, j, k;
-    cell_ijk(d, c, i, j, k);
-    const size_t P = pidx(d, b, i, j, k);
-    p[P] = z[(size_t)b * d.nint + c] + beta * p[P];
+    const int b = blockIdx.x;
+    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+        const int pb = D.bprob[b];
+        if (!D.active[pb]) continue;
+        const double beta = (restart || D.pAp[pb] == 0.0) ? 0.0 : -D.zAp[pb] / D.pAp[pb];
+        int i, j, k;
+        cell_ijk(d, c, i, j, k);
+        const size_t P = pidx(d, b, i, j, k);
+        p[P] = z[(size_t)b * d.nint + c] + beta * p[P];
+    }
 }
 
 // ---- FP32 V-cycle ------------------------------------------------------------
@@ -218,54 +220,58 @@ __global__ void k_zero_f(float* v, size_t n) {
 
 // red-black Gauss-Seidel half sweep: z = (r - sum_nb A z_nb) / Aii on cells of one colour
 __global__ void k_rbgs(Ops32 A, LevelDims d, const float* r, float* z, int colour) {
-    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
-    if (c >= d.nint) return;
-    int i, j, k;
-    cell_ijk(d, c, i, j, k);
-    if (((i + j + k) & 1) != colour) return;
-    const size_t P = pidx(d, b, i, j, k);
-    const size_t sj = d.p0, sk = (size_t)d.p0 * d.p1;
-    const size_t fi = ((size_t)b * d.m2 * d.m1 + (size_t)(k - 1) * d.m1 + (j - 1)) * (d.m0 + 1) + (i - 1);
-    const size_t fj = ((size_t)b * d.m2 * (d.m1 + 1) + (size_t)(k - 1) * (d.m1 + 1) + (j - 1)) * d.m0 + (i - 1);
-    const size_t fk = ((size_t)b * (d.m2 + 1) * d.m1 + (size_t)(k - 1) * d.m1 + (j - 1)) * d.m0 + (i - 1);
-    const float off = A.Ai[fi] * z[P - 1] + A.Ai[fi + 1] * z[P + 1] + A.Aj[fj] * z[P - sj] + A.Aj[fj + d.m0] * z[P + sj] +
-                      A.Ak[fk] * z[P - sk] + A.Ak[fk + (size_t)d.m0 * d.m1] * z[P + sk];
-    z[P] = (r[(size_t)b * d.nint + c] - off) / A.Aii[(size_t)b * d.nint + c];
+    const int b = blockIdx.x;
+    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+        int i, j, k;
+        cell_ijk(d, c, i, j, k);
+        if (((i + j + k) & 1) != colour) continue;
+        const size_t P = pidx(d, b, i, j, k);
+        const size_t sj = d.p0, sk = (size_t)d.p0 * d.p1;
+        const size_t fi = ((size_t)b * d.m2 * d.m1 + (size_t)(k - 1) * d.m1 + (j - 1)) * (d.m0 + 1) + (i - 1);
+        const size_t fj = ((size_t)b * d.m2 * (d.m1 + 1) + (size_t)(k - 1) * (d.m1 + 1) + (j - 1)) * d.m0 + (i - 1);
+        const size_t fk = ((size_t)b * (d.m2 + 1) * d.m1 + (size_t)(k - 1) * d.m1 + (j - 1)) * d.m0 + (i - 1);
+        const float off = A.Ai[fi] * z[P - 1] + A.Ai[fi + 1] * z[P + 1] + A.Aj[fj] * z[P - sj] + A.Aj[fj + d.m0] * z[P + sj] +
+                          A.Ak[fk] * z[P - sk] + A.Ak[fk + (size_t)d.m0 * d.m1] * z[P + sk];
+        z[P] = (r[(size_t)b * d.nint + c] - off) / A.Aii[(size_t)b * d.nint + c];
+    }
 }
 
 // res = r - A z
 __global__ void k_resid32(Ops32 A, LevelDims d, const float* r, const float* z, float* res) {
-    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
-    if (c >= d.nint) return;
-    int i, j, k;
-    cell_ijk(d, c, i, j, k);
-    const size_t q = (size_t)b * d.nint + c;
-    res[q] = r[q] - apply_A<float>(A, d, z, b, c, i, j, k);
+    const int b = blockIdx.x;
+    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+        int i, j, k;
+        cell_ijk(d, c, i, j, k);
+        const size_t q = (size_t)b * d.nint + c;
+        res[q] = r[q] - apply_A<float>(A, d, z, b, c, i, j, k);
+    }
 }
 
 // r_coarse(I) = sum of the 8 children of res_fine (R = P^T)
 __global__ void k_restrict(LevelDims f, LevelDims cd, const float* res, float* rc) {
-    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
-    if (c >= cd.nint) return;
-    const int I = c % cd.m0, J = (c / cd.m0) % cd.m1, K = c / (cd.m0 * cd.m1);
-    const float* R = res + (size_t)b * f.nint;
-    float s = 0.f;
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-        const int i = 2 * I + (q & 1), j = 2 * J + ((q >> 1) & 1), k = 2 * K + (q >> 2);
-        s += R[((size_t)k * f.m1 + j) * f.m0 + i];
+    const int b = blockIdx.x;
+    for (int c = threadIdx.x; c < cd.nint; c += blockDim.x) {
+        const int I = c % cd.m0, J = (c / cd.m0) % cd.m1, K = c / (cd.m0 * cd.m1);
+        const float* R = res + (size_t)b * f.nint;
+        float s = 0.f;
+    #pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int i = 2 * I + (q & 1), j = 2 * J + ((q >> 1) & 1), k = 2 * K + (q >> 2);
+            s += R[((size_t)k * f.m1 + j) * f.m0 + i];
+        }
+        rc[(size_t)b * cd.nint + c] = s;
     }
-    rc[(size_t)b * cd.nint + c] = s;
 }
 
 // z_fine(child) += z_coarse(I) (injection)
 __global__ void k_prolong_add(LevelDims f, LevelDims cd, const float* zc, float* zf) {
-    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
-    if (c >= f.nint) return;
-    int i, j, k;
-    cell_ijk(f, c, i, j, k);
-    const int I = (i - 1) / 2 + 1, J = (j - 1) / 2 + 1, K = (k - 1) / 2 + 1;
-    zf[pidx(f, b, i, j, k)] += zc[pidx(cd, b, I, J, K)];
+    const int b = blockIdx.x;
+    for (int c = threadIdx.x; c < f.nint; c += blockDim.x) {
+        int i, j, k;
+        cell_ijk(f, c, i, j, k);
+        const int I = (i - 1) / 2 + 1, J = (j - 1) / 2 + 1, K = (k - 1) / 2 + 1;
+        zf[pidx(f, b, i, j, k)] += zc[pidx(cd, b, I, J, K)];
+    }
 }
 
 // ---- learned coarse correction: coarsest level <-> dense panel grids ---------
@@ -273,29 +279,30 @@ __global__ void k_prolong_add(LevelDims f, LevelDims cd, const float* zc, float*
 
 // static input channels 1..7: the six face couplings / diag, (diag + sum)/diag
 __global__ void k_lcc_static(Ops64 A, LevelDims d, const int32_t* gmap, float* feat) {
-    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
-    if (c >= d.nint) return;
-    int i, j, k;
-    cell_ijk(d, c, i, j, k);
-    const size_t fi = ((size_t)b * d.m2 * d.m1 + (size_t)(k - 1) * d.m1 + (j - 1)) * (d.m0 + 1) + (i - 1);
-    const size_t fj = ((size_t)b * d.m2 * (d.m1 + 1) + (size_t)(k - 1) * (d.m1 + 1) + (j - 1)) * d.m0 + (i - 1);
-    const size_t fk = ((size_t)b * (d.m2 + 1) * d.m1 + (size_t)(k - 1) * d.m1 + (j - 1)) * d.m0 + (i - 1);
-    const double dg = A.Aii[(size_t)b * d.nint + c];
-    const double cpl[6] = {A.Ai[fi], A.Ai[fi + 1], A.Aj[fj], A.Aj[fj + d.m0], A.Ak[fk], A.Ak[fk + (size_t)d.m0 * d.m1]};
-    float* f = feat + (size_t)gmap[(size_t)b * d.nint + c] * 8;
-    double sum = dg;
-    for (int q = 0; q < 6; ++q) { f[1 + q] = (float)(cpl[q] / dg); sum += cpl[q]; }
-    f[7] = (float)(sum / dg);
+    const int b = blockIdx.x;
+    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+        int i, j, k;
+        cell_ijk(d, c, i, j, k);
+        const size_t fi = ((size_t)b * d.m2 * d.m1 + (size_t)(k - 1) * d.m1 + (j - 1)) * (d.m0 + 1) + (i - 1);
+        const size_t fj = ((size_t)b * d.m2 * (d.m1 + 1) + (size_t)(k - 1) * (d.m1 + 1) + (j - 1)) * d.m0 + (i - 1);
+        const size_t fk = ((size_t)b * (d.m2 + 1) * d.m1 + (size_t)(k - 1) * d.m1 + (j - 1)) * d.m0 + (i - 1);
+        const double dg = A.Aii[(size_t)b * d.nint + c];
+        const double cpl[6] = {A.Ai[fi], A.Ai[fi + 1], A.Aj[fj], A.Aj[fj + d.m0], A.Ak[fk], A.Ak[fk + (size_t)d.m0 * d.m1]};
+        float* f = feat + (size_t)gmap[(size_t)b * d.nint + c] * 8;
+        double sum = dg;
+        for (int q = 0; q < 6; ++q) { f[1 + q] = (float)(cpl[q] / dg); sum += cpl[q]; }
+        f[7] = (float)(sum / dg);
+    }
 }
 
 // sum over coarse cells of (r/diag)^2
 __global__ void k_lcc_sumsq(LevelDims d, const float* r, const float* Aii, double* sum) {
-    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
+    const int b = blockIdx.x;
     double v = 0.0;
-    if (c < d.nint) {
+    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
         const size_t q = (size_t)b * d.nint + c;
         const double x = (double)r[q] / (double)Aii[q];
-        v = x * x;
+        v += x * x;
     }
     block_sum_atomic(v, sum);
 }
@@ -308,36 +315,39 @@ __device__ __forceinline__ double lcc_scale(const double* sum, int64_t n) {
 // input channel 0: (r/diag)/s, s = RMS of r/diag
 __global__ void k_lcc_feat(LevelDims d, const float* r, const float* Aii, const int32_t* gmap, const double* sum,
                            int64_t n, float* feat) {
-    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
-    if (c >= d.nint) return;
-    const size_t q = (size_t)b * d.nint + c;
-    feat[(size_t)gmap[q] * 8] = (float)((double)r[q] / (double)Aii[q] / lcc_scale(sum, n));
+    const int b = blockIdx.x;
+    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+        const size_t q = (size_t)b * d.nint + c;
+        feat[(size_t)gmap[q] * 8] = (float)((double)r[q] / (double)Aii[q] / lcc_scale(sum, n));
+    }
 }
 
 // coarse correction z = s * y (padded coarse layout)
 __global__ void k_lcc_scatter(LevelDims d, const float* y, const int32_t* gmap, const double* sum, int64_t n, float* z) {
-    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
-    if (c >= d.nint) return;
-    int i, j, k;
-    cell_ijk(d, c, i, j, k);
-    z[pidx(d, b, i, j, k)] = (float)(lcc_scale(sum, n) * (double)y[gmap[(size_t)b * d.nint + c]]);
+    const int b = blockIdx.x;
+    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+        int i, j, k;
+        cell_ijk(d, c, i, j, k);
+        z[pidx(d, b, i, j, k)] = (float)(lcc_scale(sum, n) * (double)y[gmap[(size_t)b * d.nint + c]]);
+    }
 }
 
 // training target: t = e/s (e: padded FP64 coarse solution)
 __global__ void k_lcc_target(LevelDims d, const double* e, const int32_t* gmap, const double* sum, int64_t n, float* t) {
-    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
-    if (c >= d.nint) return;
-    int i, j, k;
-    cell_ijk(d, c, i, j, k);
-    t[gmap[(size_t)b * d.nint + c]] = (float)(e[pidx(d, b, i, j, k)] / lcc_scale(sum, n));
+    const int b = blockIdx.x;
+    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+        int i, j, k;
+        cell_ijk(d, c, i, j, k);
+        t[gmap[(size_t)b * d.nint + c]] = (float)(e[pidx(d, b, i, j, k)] / lcc_scale(sum, n));
+    }
 }
 
 // ---- Jacobi-preconditioned CG on one level (FP64): exact coarse errors -------
 // dots: [0] r.z  [1] p.Ap  [2] r.r (current); nd: the same for the next iterate
 __global__ void k_ccg_init(Ops64 A, LevelDims d, const float* rc, double* r, double* z, double* p, double* dots) {
-    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
+    const int b = blockIdx.x;
     double rz = 0, rr = 0;
-    if (c < d.nint) {
+    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
         const size_t q = (size_t)b * d.nint + c;
@@ -345,32 +355,32 @@ __global__ void k_ccg_init(Ops64 A, LevelDims d, const float* rc, double* r, dou
         r[q] = rv;
         z[q] = zv;
         p[pidx(d, b, i, j, k)] = zv;
-        rz = rv * zv;
-        rr = rv * rv;
+        rz += rv * zv;
+        rr += rv * rv;
     }
     block_sum_atomic(rz, &dots[0]);
     block_sum_atomic(rr, &dots[2]);
 }
 
 __global__ void k_ccg_spmv(Ops64 A, LevelDims d, const double* p, double* Ap, double* dots) {
-    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
+    const int b = blockIdx.x;
     double pa = 0;
-    if (c < d.nint) {
+    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
         const double y = apply_A<double>(A, d, p, b, c, i, j, k);
         Ap[(size_t)b * d.nint + c] = y;
-        pa = p[pidx(d, b, i, j, k)] * y;
+        pa += p[pidx(d, b, i, j, k)] * y;
     }
     block_sum_atomic(pa, &dots[1]);
 }
 
 __global__ void k_ccg_update(Ops64 A, LevelDims d, double* x, const double* p, double* r, const double* Ap, double* z,
                              const double* dots, double* nd) {
-    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
+    const int b = blockIdx.x;
     const double alpha = dots[0] / dots[1];
     double rz = 0, rr = 0;
-    if (c < d.nint) {
+    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
         const size_t P = pidx(d, b, i, j, k), q = (size_t)b * d.nint + c;
@@ -378,20 +388,21 @@ __global__ void k_ccg_update(Ops64 A, LevelDims d, double* x, const double* p, d
         const double rv = r[q] - alpha * Ap[q], zv = rv / A.Aii[q];
         r[q] = rv;
         z[q] = zv;
-        rz = rv * zv;
-        rr = rv * rv;
+        rz += rv * zv;
+        rr += rv * rv;
     }
     block_sum_atomic(rz, &nd[0]);
     block_sum_atomic(rr, &nd[2]);
 }
 
 __global__ void k_ccg_p(LevelDims d, double* p, const double* z, const double* dots, const double* nd) {
-    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
-    if (c >= d.nint) return;
-    int i, j, k;
-    cell_ijk(d, c, i, j, k);
-    const size_t P = pidx(d, b, i, j, k);
-    p[P] = z[(size_t)b * d.nint + c] + (nd[0] / dots[0]) * p[P];
+    const int b = blockIdx.x;
+    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+        int i, j, k;
+        cell_ijk(d, c, i, j, k);
+        const size_t P = pidx(d, b, i, j, k);
+        p[P] = z[(size_t)b * d.nint + c] + (nd[0] / dots[0]) * p[P];
+    }
 }
 
 }  // namespace sv
@@ -465,7 +476,11 @@ struct falcon_solver {
 namespace {
 
 // grid.x = block (up to 2^31-1 blocks), grid.y = 256-cell chunk of the block
-dim3 grid_cells(const LevelDims& d, int nblocks) { return dim3((unsigned)nblocks, (unsigned)((d.nint + 255) / 256)); }
+// One CTA per block looping over its cells: consecutive CTAs stream
+// consecutive blocks, and each per-problem reduction takes one atomic per
+// block (up to 2^31-1 blocks).
+dim3 grid_cells(const LevelDims& d, int nblocks) { (void)d; return dim3((unsigned)nblocks); }
+unsigned tpb(const LevelDims& d) { return (unsigned)std::min(256, (d.nint + 31) / 32 * 32); }
 
 template <class T> cudaError_t halo_fill(falcon_solver* sv, int l, T* v) {
     const SvLevel& L = sv->lv[l];
@@ -484,7 +499,7 @@ cudaError_t vcycle_body(falcon_solver* sv) {
             for (int h = 0; h < 2 && e == cudaSuccess; ++h) {
                 e = halo_fill<float>(sv, l, L.z);
                 if (e != cudaSuccess) break;
-                k_rbgs<<<grid_cells(L.d, nb), 256, 0, sv->st>>>(L.ops32(), L.d, L.r, L.z, reverse ? 1 - h : h);
+                k_rbgs<<<grid_cells(L.d, nb), tpb(L.d), 0, sv->st>>>(L.ops32(), L.d, L.r, L.z, reverse ? 1 - h : h);
                 e = cudaGetLastError();
             }
     };
@@ -501,12 +516,12 @@ cudaError_t vcycle_body(falcon_solver* sv) {
             const int64_t N = (int64_t)nb * L.d.nint;
             e = cudaMemsetAsync(sv->csum, 0, 8, sv->st);
             if (e == cudaSuccess) {
-                k_lcc_sumsq<<<grid_cells(L.d, nb), 256, 0, sv->st>>>(L.d, L.r, L.fAii, sv->csum);
-                k_lcc_feat<<<grid_cells(L.d, nb), 256, 0, sv->st>>>(L.d, L.r, L.fAii, sv->gmap, sv->csum, N, sv->feat);
+                k_lcc_sumsq<<<grid_cells(L.d, nb), tpb(L.d), 0, sv->st>>>(L.d, L.r, L.fAii, sv->csum);
+                k_lcc_feat<<<grid_cells(L.d, nb), tpb(L.d), 0, sv->st>>>(L.d, L.r, L.fAii, sv->gmap, sv->csum, N, sv->feat);
                 e = lcc::forward_device(sv->net, sv->feat, 2, sv->cD, sv->cH, sv->cW, sv->yout, sv->st);
             }
             if (e == cudaSuccess) {
-                k_lcc_scatter<<<grid_cells(L.d, nb), 256, 0, sv->st>>>(L.d, sv->yout, sv->gmap, sv->csum, N, L.z);
+                k_lcc_scatter<<<grid_cells(L.d, nb), tpb(L.d), 0, sv->st>>>(L.d, sv->yout, sv->gmap, sv->csum, N, L.z);
                 e = cudaGetLastError();
             }
             smooth(l, sv->net_sweeps, false);
@@ -516,16 +531,16 @@ cudaError_t vcycle_body(falcon_solver* sv) {
         if (l + 1 < nl && e == cudaSuccess) {
             e = halo_fill<float>(sv, l, L.z);
             if (e != cudaSuccess) break;
-            k_resid32<<<grid_cells(L.d, nb), 256, 0, sv->st>>>(L.ops32(), L.d, L.r, L.z, L.res);
+            k_resid32<<<grid_cells(L.d, nb), tpb(L.d), 0, sv->st>>>(L.ops32(), L.d, L.r, L.z, L.res);
             SvLevel& C = sv->lv[l + 1];
-            k_restrict<<<grid_cells(C.d, nb), 256, 0, sv->st>>>(L.d, C.d, L.res, C.r);
+            k_restrict<<<grid_cells(C.d, nb), tpb(C.d), 0, sv->st>>>(L.d, C.d, L.res, C.r);
             e = cudaGetLastError();
         }
     }
     for (int l = nl - 2; l >= 0 && e == cudaSuccess; --l) {
         SvLevel& L = sv->lv[l];
         SvLevel& C = sv->lv[l + 1];
-        k_prolong_add<<<grid_cells(L.d, nb), 256, 0, sv->st>>>(L.d, C.d, C.z, L.z);
+        k_prolong_add<<<grid_cells(L.d, nb), tpb(L.d), 0, sv->st>>>(L.d, C.d, C.z, L.z);
         e = cudaGetLastError();
         smooth(l, sv->nu_post, true);
     }
@@ -638,18 +653,20 @@ int setup(falcon_solver* sv) {
 
 // scatter an interior [b][nint] FP64 vector into the padded x
 __global__ void k_scatter_pad(LevelDims d, const double* v, double* x) {
-    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
-    if (c >= d.nint) return;
-    int i, j, k;
-    cell_ijk(d, c, i, j, k);
-    x[pidx(d, b, i, j, k)] = v[(size_t)b * d.nint + c];
+    const int b = blockIdx.x;
+    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+        int i, j, k;
+        cell_ijk(d, c, i, j, k);
+        x[pidx(d, b, i, j, k)] = v[(size_t)b * d.nint + c];
+    }
 }
 __global__ void k_gather_pad(LevelDims d, const double* x, double* v) {
-    const int b = blockIdx.x, c = blockIdx.y * blockDim.x + threadIdx.x;
-    if (c >= d.nint) return;
-    int i, j, k;
-    cell_ijk(d, c, i, j, k);
-    v[(size_t)b * d.nint + c] = x[pidx(d, b, i, j, k)];
+    const int b = blockIdx.x;
+    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+        int i, j, k;
+        cell_ijk(d, c, i, j, k);
+        v[(size_t)b * d.nint + c] = x[pidx(d, b, i, j, k)];
+    }
 }
 
 // Map the coarsest level onto one dense grid per panel (single problem,
@@ -721,7 +738,7 @@ int ensure_coarse_map(falcon_solver* sv) {
     SCK(sv->alloc(&sv->csum, 8), "coarse features");
     SCK(sv->alloc(&sv->cdots, 6 * 8), "coarse features");
     SvLevel& L = sv->lv[lc];
-    k_lcc_static<<<grid_cells(L.d, nb), 256, 0, sv->st>>>(L.ops64(), L.d, sv->gmap, sv->feat);
+    k_lcc_static<<<grid_cells(L.d, nb), tpb(L.d), 0, sv->st>>>(L.ops64(), L.d, sv->gmap, sv->feat);
     SCK(cudaGetLastError(), "coarse features");
     SCK(cudaStreamSynchronize(sv->st), "coarse features");
     sv->cD = D; sv->cH = H; sv->cW = W;
@@ -740,7 +757,7 @@ int coarse_solve(falcon_solver* sv, const float* rc) {
     SCK(cudaMemsetAsync(sv->x, 0, (size_t)nb * L.d.npad * 8, sv->st), "coarse cg");
     SCK(cudaMemsetAsync(sv->p, 0, (size_t)nb * L.d.npad * 8, sv->st), "coarse cg");
     SCK(cudaMemsetAsync(dots, 0, 6 * 8, sv->st), "coarse cg");
-    k_ccg_init<<<g, 256, 0, sv->st>>>(L.ops64(), L.d, rc, sv->r, sv->z, sv->p, dots);
+    k_ccg_init<<<g, tpb(L.d), 0, sv->st>>>(L.ops64(), L.d, rc, sv->r, sv->z, sv->p, dots);
     double h[6];
     SCK(cudaMemcpyAsync(h, dots, 6 * 8, cudaMemcpyDeviceToHost, sv->st), "coarse cg");
     SCK(cudaStreamSynchronize(sv->st), "coarse cg");
@@ -750,9 +767,9 @@ int coarse_solve(falcon_solver* sv, const float* rc) {
         SCK(halo_fill<double>(sv, lc, sv->p), "coarse cg");
         SCK(cudaMemsetAsync(dots + 1, 0, 8, sv->st), "coarse cg");
         SCK(cudaMemsetAsync(dots + 3, 0, 3 * 8, sv->st), "coarse cg");
-        k_ccg_spmv<<<g, 256, 0, sv->st>>>(L.ops64(), L.d, sv->p, sv->Ap, dots);
-        k_ccg_update<<<g, 256, 0, sv->st>>>(L.ops64(), L.d, sv->x, sv->p, sv->r, sv->Ap, sv->z, dots, dots + 3);
-        k_ccg_p<<<g, 256, 0, sv->st>>>(L.d, sv->p, sv->z, dots, dots + 3);
+        k_ccg_spmv<<<g, tpb(L.d), 0, sv->st>>>(L.ops64(), L.d, sv->p, sv->Ap, dots);
+        k_ccg_update<<<g, tpb(L.d), 0, sv->st>>>(L.ops64(), L.d, sv->x, sv->p, sv->r, sv->Ap, sv->z, dots, dots + 3);
+        k_ccg_p<<<g, tpb(L.d), 0, sv->st>>>(L.d, sv->p, sv->z, dots, dots + 3);
         SCK(cudaGetLastError(), "coarse cg");
         SCK(cudaMemcpyAsync(dots, dots + 3, 3 * 8, cudaMemcpyDeviceToDevice, sv->st), "coarse cg");
         SCK(cudaMemcpyAsync(h, dots + 3, 3 * 8, cudaMemcpyDeviceToHost, sv->st), "coarse cg");
@@ -920,10 +937,10 @@ int falcon_solver_apply(falcon_solver* sv, const double* x, double* y) {
     const int nb = sv->S.nblocks;
     SCK(cudaMemcpyAsync(sv->z, x, (size_t)nb * d.nint * 8, cudaMemcpyHostToDevice, sv->st), "apply");
     SCK(cudaMemsetAsync(sv->p, 0, (size_t)nb * d.npad * 8, sv->st), "apply");
-    k_scatter_pad<<<grid_cells(d, nb), 256, 0, sv->st>>>(d, sv->z, sv->p);
+    k_scatter_pad<<<grid_cells(d, nb), tpb(d), 0, sv->st>>>(d, sv->z, sv->p);
     SCK(halo_fill<double>(sv, 0, sv->p), "apply halo");
     SCK(cudaMemsetAsync(sv->dots, 0, (size_t)6 * sv->S.nproblems * 8, sv->st), "apply");
-    k_spmv_dots<<<grid_cells(d, nb), 256, 0, sv->st>>>(sv->lv[0].ops64(), d, sv->p, sv->Ap, sv->r, sv->D());
+    k_spmv_dots<<<grid_cells(d, nb), tpb(d), 0, sv->st>>>(sv->lv[0].ops64(), d, sv->p, sv->Ap, sv->r, sv->D());
     SCK(cudaGetLastError(), "apply");
     SCK(cudaMemcpyAsync(y, sv->Ap, (size_t)nb * d.nint * 8, cudaMemcpyDeviceToHost, sv->st), "apply");
     SCK(cudaStreamSynchronize(sv->st), "apply");
@@ -951,12 +968,12 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
     SCK(cudaMemcpyAsync(sv->z, S.x0.data(), (size_t)nb * d.nint * 8, cudaMemcpyHostToDevice, sv->st), "init");
     SCK(cudaStreamSynchronize(sv->st), "init");
     cudaEventRecord(t0, sv->st);
-    k_scatter_pad<<<g, 256, 0, sv->st>>>(d, sv->z, sv->x);
+    k_scatter_pad<<<g, tpb(d), 0, sv->st>>>(d, sv->z, sv->x);
     std::vector<int32_t> act(np, 1);
     SCK(cudaMemcpyAsync(sv->active, act.data(), np * 4, cudaMemcpyHostToDevice, sv->st), "init");
     SCK(cudaMemsetAsync(sv->dots, 0, (size_t)6 * np * 8, sv->st), "init");
     SCK(halo_fill<double>(sv, 0, sv->x), "halo");
-    k_residual64<<<g, 256, 0, sv->st>>>(sv->lv[0].ops64(), d, sv->x, sv->bvec, sv->r, sv->lv[0].r, sv->D(), 1);
+    k_residual64<<<g, tpb(d), 0, sv->st>>>(sv->lv[0].ops64(), d, sv->x, sv->bvec, sv->r, sv->lv[0].r, sv->D(), 1);
     std::vector<double> rr(np), bb(np);
     SCK(cudaMemcpyAsync(bb.data(), sv->dots + 4 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "bb");
     SCK(cudaStreamSynchronize(sv->st), "bb");
@@ -971,7 +988,7 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
             ++rep->vcycles;
         }
         if (e != cudaSuccess) return e;
-        k_take_z<<<g, 256, 0, sv->st>>>(d, sv->lv[0].z, sv->r, pc == FALCON_PRECOND_NONE, sv->z, sv->Ap, sv->D(), want_zAp);
+        k_take_z<<<g, tpb(d), 0, sv->st>>>(d, sv->lv[0].z, sv->r, pc == FALCON_PRECOND_NONE, sv->z, sv->Ap, sv->D(), want_zAp);
         return cudaGetLastError();
     };
     std::vector<double> hist;   // max over active problems of the recursive relative residual
@@ -979,15 +996,15 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
     std::vector<double> prev_true(np, 1e300); // true residual at the previous verification
     // p = M r
     SCK(precondition(0), "precondition");
-    k_update_p<<<g, 256, 0, sv->st>>>(d, sv->p, sv->z, sv->D(), 1);
+    k_update_p<<<g, tpb(d), 0, sv->st>>>(d, sv->p, sv->z, sv->D(), 1);
     SCK(halo_fill<double>(sv, 0, sv->p), "halo");
     double worst = 0;
     int it = 0;
     bool done = false;
     for (it = 1; it <= max_iter && !done; ++it) {
         SCK(cudaMemsetAsync(sv->dots, 0, (size_t)4 * np * 8, sv->st), "dots");
-        k_spmv_dots<<<g, 256, 0, sv->st>>>(sv->lv[0].ops64(), d, sv->p, sv->Ap, sv->r, sv->D());
-        k_update_xr<<<g, 256, 0, sv->st>>>(d, sv->x, sv->p, sv->r, sv->Ap, sv->lv[0].r, sv->D());
+        k_spmv_dots<<<g, tpb(d), 0, sv->st>>>(sv->lv[0].ops64(), d, sv->p, sv->Ap, sv->r, sv->D());
+        k_update_xr<<<g, tpb(d), 0, sv->st>>>(d, sv->x, sv->p, sv->r, sv->Ap, sv->lv[0].r, sv->D());
         SCK(cudaGetLastError(), "iterate");
         SCK(cudaMemcpyAsync(rr.data(), sv->dots + 3 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "rr");
         SCK(cudaStreamSynchronize(sv->st), "rr");
@@ -1008,7 +1025,7 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
             pc = FALCON_PRECOND_MG;
             ++rep->fallbacks;
             SCK(precondition(0), "precondition");
-            k_update_p<<<g, 256, 0, sv->st>>>(d, sv->p, sv->z, sv->D(), 1);
+            k_update_p<<<g, tpb(d), 0, sv->st>>>(d, sv->p, sv->z, sv->D(), 1);
             SCK(halo_fill<double>(sv, 0, sv->p), "halo");
             continue;
         }
@@ -1020,7 +1037,7 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
             SCK(cudaMemsetAsync(sv->dots + 3 * np, 0, (size_t)np * 8, sv->st), "dots");
             SCK(cudaMemsetAsync(sv->dots + 5 * np, 0, (size_t)np * 8, sv->st), "dots");
             SCK(halo_fill<double>(sv, 0, sv->x), "halo");
-            k_residual64<<<g, 256, 0, sv->st>>>(sv->lv[0].ops64(), d, sv->x, sv->bvec, sv->r, sv->lv[0].r, sv->D(), 0);
+            k_residual64<<<g, tpb(d), 0, sv->st>>>(sv->lv[0].ops64(), d, sv->x, sv->bvec, sv->r, sv->lv[0].r, sv->D(), 0);
             std::vector<double> ab(np);
             SCK(cudaMemcpyAsync(rr.data(), sv->dots + 3 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "rr");
             SCK(cudaMemcpyAsync(ab.data(), sv->dots + 5 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "rr");
@@ -1051,12 +1068,12 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
             if (ok) { done = true; break; }
             ++rep->refinements;
             SCK(precondition(0), "precondition");
-            k_update_p<<<g, 256, 0, sv->st>>>(d, sv->p, sv->z, sv->D(), 1);
+            k_update_p<<<g, tpb(d), 0, sv->st>>>(d, sv->p, sv->z, sv->D(), 1);
             SCK(halo_fill<double>(sv, 0, sv->p), "halo");
             continue;
         }
         SCK(precondition(1), "precondition");
-        k_update_p<<<g, 256, 0, sv->st>>>(d, sv->p, sv->z, sv->D(), 0);
+        k_update_p<<<g, tpb(d), 0, sv->st>>>(d, sv->p, sv->z, sv->D(), 0);
         SCK(halo_fill<double>(sv, 0, sv->p), "halo");
     }
     cudaEventRecord(t1, sv->st);
@@ -1069,7 +1086,7 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
         // report the true residual of the last iterate
         SCK(cudaMemsetAsync(sv->dots + 3 * np, 0, (size_t)np * 8, sv->st), "dots");
         SCK(halo_fill<double>(sv, 0, sv->x), "halo");
-        k_residual64<<<g, 256, 0, sv->st>>>(sv->lv[0].ops64(), d, sv->x, sv->bvec, sv->r, sv->lv[0].r, sv->D(), 0);
+        k_residual64<<<g, tpb(d), 0, sv->st>>>(sv->lv[0].ops64(), d, sv->x, sv->bvec, sv->r, sv->lv[0].r, sv->D(), 0);
         SCK(cudaMemcpyAsync(rr.data(), sv->dots + 3 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "rr");
         SCK(cudaStreamSynchronize(sv->st), "rr");
         worst = 0;
@@ -1092,7 +1109,7 @@ int falcon_solver_solution(falcon_solver* sv, double* x) {
     cudaSetDevice(sv->device);
     const LevelDims& d = sv->lv[0].d;
     const int nb = sv->S.nblocks;
-    k_gather_pad<<<grid_cells(d, nb), 256, 0, sv->st>>>(d, sv->x, sv->z);
+    k_gather_pad<<<grid_cells(d, nb), tpb(d), 0, sv->st>>>(d, sv->x, sv->z);
     SCK(cudaMemcpyAsync(x, sv->z, (size_t)nb * d.nint * 8, cudaMemcpyDeviceToHost, sv->st), "solution");
     SCK(cudaStreamSynchronize(sv->st), "solution");
     return FALCON_OK;
@@ -1121,7 +1138,7 @@ int falcon_solver_problem_residuals(falcon_solver* sv, double* rel) {
     const LevelDims& d = sv->lv[0].d;
     SCK(cudaMemsetAsync(sv->dots, 0, (size_t)6 * np * 8, sv->st), "residuals");
     SCK(halo_fill<double>(sv, 0, sv->x), "residuals");
-    k_residual64<<<grid_cells(d, nb), 256, 0, sv->st>>>(sv->lv[0].ops64(), d, sv->x, sv->bvec, sv->r, sv->lv[0].r,
+    k_residual64<<<grid_cells(d, nb), tpb(d), 0, sv->st>>>(sv->lv[0].ops64(), d, sv->x, sv->bvec, sv->r, sv->lv[0].r,
                                                         sv->D(), 1);
     std::vector<double> rr(np), bb(np);
     SCK(cudaMemcpyAsync(rr.data(), sv->dots + 3 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "residuals");
@@ -1195,9 +1212,9 @@ int falcon_solver_record(falcon_solver* sv, double tol, int32_t max_iter, int32_
             const int64_t N = (int64_t)per;
             e = cudaMemsetAsync(sv->csum, 0, 8, sv->st);
             if (e != cudaSuccess) break;
-            k_lcc_sumsq<<<grid_cells(L.d, nb), 256, 0, sv->st>>>(L.d, rq, L.fAii, sv->csum);
-            k_lcc_feat<<<grid_cells(L.d, nb), 256, 0, sv->st>>>(L.d, rq, L.fAii, sv->gmap, sv->csum, N, sv->feat);
-            k_lcc_target<<<grid_cells(L.d, nb), 256, 0, sv->st>>>(L.d, sv->x, sv->gmap, sv->csum, N, tdev);
+            k_lcc_sumsq<<<grid_cells(L.d, nb), tpb(L.d), 0, sv->st>>>(L.d, rq, L.fAii, sv->csum);
+            k_lcc_feat<<<grid_cells(L.d, nb), tpb(L.d), 0, sv->st>>>(L.d, rq, L.fAii, sv->gmap, sv->csum, N, sv->feat);
+            k_lcc_target<<<grid_cells(L.d, nb), tpb(L.d), 0, sv->st>>>(L.d, sv->x, sv->gmap, sv->csum, N, tdev);
             e = cudaGetLastError();
             if (e == cudaSuccess) e = cudaMemcpyAsync(x + (size_t)q * vox * 8, sv->feat, vox * 8 * 4, cudaMemcpyDeviceToHost, sv->st);
             if (e == cudaSuccess) e = cudaMemcpyAsync(t + (size_t)q * vox, tdev, vox * 4, cudaMemcpyDeviceToHost, sv->st);
