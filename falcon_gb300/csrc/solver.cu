@@ -49,6 +49,17 @@ struct HaloList {
 struct Ops64 { const double *Aii, *Ai, *Aj, *Ak; };
 struct Ops32 { const float *Aii, *Ai, *Aj, *Ak; };
 
+// Launch geometry of the cell kernels: CTAs take chunks of kCellChunk cells,
+// block-major (consecutive CTAs stream consecutive memory); a chunk never
+// spans two blocks, so a CTA's reductions go to one problem.
+constexpr int kCellChunk = 1024;
+__device__ __forceinline__ int cell_chunks(const LevelDims& d) { return (d.nint + kCellChunk - 1) / kCellChunk; }
+__device__ __forceinline__ int cell_block(const LevelDims& d) { return (int)(blockIdx.x / (unsigned)cell_chunks(d)); }
+__device__ __forceinline__ int cell_first(const LevelDims& d) {
+    return (int)(blockIdx.x % (unsigned)cell_chunks(d)) * kCellChunk;
+}
+__device__ __forceinline__ int cell_end(const LevelDims& d) { return min(cell_first(d) + kCellChunk, d.nint); }
+
 __device__ __forceinline__ void cell_ijk(const LevelDims& d, int c, int& i, int& j, int& k) {
     i = c % d.m0 + 1;
     j = (c / d.m0) % d.m1 + 1;
@@ -86,6 +97,14 @@ __device__ __forceinline__ void block_sum_atomic(T v, double* slot) {
 }
 
 // ---- halo fill (trilinear from the source interior) ------------------------
+// entries whose three weights are exactly zero: the trilinear sum is the base
+// cell's value, copied
+template <class T>
+__global__ void k_halo_copy(T* v, const int32_t* dst, const int32_t* src, int64_t n) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < n) v[dst[e]] = v[src[e]];
+}
+
 template <class T>
 __global__ void k_halo(T* v, HaloList H) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -108,9 +127,9 @@ struct Dots {
 
 // Ap = A p; pAp += p.Ap; pr += p.r (per problem)
 __global__ void k_spmv_dots(Ops64 A, LevelDims d, const double* p, double* Ap, const double* r, Dots D) {
-    const int b = blockIdx.x;
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
     double pa = 0, pr = 0;
-    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
         const double y = apply_A<double>(A, d, p, b, c, i, j, k);
@@ -127,12 +146,12 @@ __global__ void k_spmv_dots(Ops64 A, LevelDims d, const double* p, double* Ap, c
 
 // alpha = p.r / p.Ap; x += alpha p; r -= alpha Ap; rr += r.r; rf = (float)r
 __global__ void k_update_xr(LevelDims d, double* x, const double* p, double* r, const double* Ap, float* rf, Dots D) {
-    const int b = blockIdx.x;
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
     const int pb = D.bprob[b];
     // a problem whose direction vanished (p.Ap == 0) takes no step instead of 0/0
     const double alpha = (D.active[pb] && D.pAp[pb] != 0.0) ? D.pr[pb] / D.pAp[pb] : 0.0;
     double rr = 0;
-    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
         const size_t P = pidx(d, b, i, j, k), q = (size_t)b * d.nint + c;
@@ -161,9 +180,9 @@ __device__ __forceinline__ double abs_row(const Ops64& A, const LevelDims& d, co
 // r = b - A x (FP64 true residual); rr += r.r; ab += (|b| + sum|A x|)^2; rf = (float)r
 __global__ void k_residual64(Ops64 A, LevelDims d, const double* x, const double* bvec, double* r, float* rf, Dots D,
                              int want_bb) {
-    const int b = blockIdx.x;
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
     double rr = 0, bb = 0, ab = 0;
-    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
         const size_t q = (size_t)b * d.nint + c;
@@ -185,9 +204,9 @@ __global__ void k_residual64(Ops64 A, LevelDims d, const double* x, const double
 // zAp += z.Ap
 __global__ void k_take_z(LevelDims d, const float* zf, const double* r, int use_r, double* z, const double* Ap, Dots D,
                          int want_zAp) {
-    const int b = blockIdx.x;
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
     double za = 0;
-    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
         const size_t q = (size_t)b * d.nint + c;
@@ -201,8 +220,8 @@ __global__ void k_take_z(LevelDims d, const float* zf, const double* r, int use_
 // p = z + beta p, beta = -z.Ap / p.Ap (flexible CG, one-term A-orthogonalisation);
 // restart (beta = 0) when `restart`
 __global__ void k_update_p(LevelDims d, double* p, const double* z, Dots D, int restart) {
-    const int b = blockIdx.x;
-    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         const int pb = D.bprob[b];
         if (!D.active[pb]) continue;
         const double beta = (restart || D.pAp[pb] == 0.0) ? 0.0 : -D.zAp[pb] / D.pAp[pb];
@@ -220,8 +239,8 @@ __global__ void k_zero_f(float* v, size_t n) {
 
 // red-black Gauss-Seidel half sweep: z = (r - sum_nb A z_nb) / Aii on cells of one colour
 __global__ void k_rbgs(Ops32 A, LevelDims d, const float* r, float* z, int colour) {
-    const int b = blockIdx.x;
-    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
         if (((i + j + k) & 1) != colour) continue;
@@ -238,8 +257,8 @@ __global__ void k_rbgs(Ops32 A, LevelDims d, const float* r, float* z, int colou
 
 // res = r - A z
 __global__ void k_resid32(Ops32 A, LevelDims d, const float* r, const float* z, float* res) {
-    const int b = blockIdx.x;
-    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
         const size_t q = (size_t)b * d.nint + c;
@@ -249,8 +268,8 @@ __global__ void k_resid32(Ops32 A, LevelDims d, const float* r, const float* z, 
 
 // r_coarse(I) = sum of the 8 children of res_fine (R = P^T)
 __global__ void k_restrict(LevelDims f, LevelDims cd, const float* res, float* rc) {
-    const int b = blockIdx.x;
-    for (int c = threadIdx.x; c < cd.nint; c += blockDim.x) {
+    const int b = cell_block(cd), c0 = cell_first(cd), c1 = cell_end(cd);
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         const int I = c % cd.m0, J = (c / cd.m0) % cd.m1, K = c / (cd.m0 * cd.m1);
         const float* R = res + (size_t)b * f.nint;
         float s = 0.f;
@@ -265,8 +284,8 @@ __global__ void k_restrict(LevelDims f, LevelDims cd, const float* res, float* r
 
 // z_fine(child) += z_coarse(I) (injection)
 __global__ void k_prolong_add(LevelDims f, LevelDims cd, const float* zc, float* zf) {
-    const int b = blockIdx.x;
-    for (int c = threadIdx.x; c < f.nint; c += blockDim.x) {
+    const int b = cell_block(f), c0 = cell_first(f), c1 = cell_end(f);
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         int i, j, k;
         cell_ijk(f, c, i, j, k);
         const int I = (i - 1) / 2 + 1, J = (j - 1) / 2 + 1, K = (k - 1) / 2 + 1;
@@ -279,8 +298,8 @@ __global__ void k_prolong_add(LevelDims f, LevelDims cd, const float* zc, float*
 
 // static input channels 1..7: the six face couplings / diag, (diag + sum)/diag
 __global__ void k_lcc_static(Ops64 A, LevelDims d, const int32_t* gmap, float* feat) {
-    const int b = blockIdx.x;
-    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
         const size_t fi = ((size_t)b * d.m2 * d.m1 + (size_t)(k - 1) * d.m1 + (j - 1)) * (d.m0 + 1) + (i - 1);
@@ -297,9 +316,9 @@ __global__ void k_lcc_static(Ops64 A, LevelDims d, const int32_t* gmap, float* f
 
 // sum over coarse cells of (r/diag)^2
 __global__ void k_lcc_sumsq(LevelDims d, const float* r, const float* Aii, double* sum) {
-    const int b = blockIdx.x;
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
     double v = 0.0;
-    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         const size_t q = (size_t)b * d.nint + c;
         const double x = (double)r[q] / (double)Aii[q];
         v += x * x;
@@ -315,8 +334,8 @@ __device__ __forceinline__ double lcc_scale(const double* sum, int64_t n) {
 // input channel 0: (r/diag)/s, s = RMS of r/diag
 __global__ void k_lcc_feat(LevelDims d, const float* r, const float* Aii, const int32_t* gmap, const double* sum,
                            int64_t n, float* feat) {
-    const int b = blockIdx.x;
-    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         const size_t q = (size_t)b * d.nint + c;
         feat[(size_t)gmap[q] * 8] = (float)((double)r[q] / (double)Aii[q] / lcc_scale(sum, n));
     }
@@ -324,8 +343,8 @@ __global__ void k_lcc_feat(LevelDims d, const float* r, const float* Aii, const 
 
 // coarse correction z = s * y (padded coarse layout)
 __global__ void k_lcc_scatter(LevelDims d, const float* y, const int32_t* gmap, const double* sum, int64_t n, float* z) {
-    const int b = blockIdx.x;
-    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
         z[pidx(d, b, i, j, k)] = (float)(lcc_scale(sum, n) * (double)y[gmap[(size_t)b * d.nint + c]]);
@@ -334,8 +353,8 @@ __global__ void k_lcc_scatter(LevelDims d, const float* y, const int32_t* gmap, 
 
 // training target: t = e/s (e: padded FP64 coarse solution)
 __global__ void k_lcc_target(LevelDims d, const double* e, const int32_t* gmap, const double* sum, int64_t n, float* t) {
-    const int b = blockIdx.x;
-    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
         t[gmap[(size_t)b * d.nint + c]] = (float)(e[pidx(d, b, i, j, k)] / lcc_scale(sum, n));
@@ -345,9 +364,9 @@ __global__ void k_lcc_target(LevelDims d, const double* e, const int32_t* gmap, 
 // ---- Jacobi-preconditioned CG on one level (FP64): exact coarse errors -------
 // dots: [0] r.z  [1] p.Ap  [2] r.r (current); nd: the same for the next iterate
 __global__ void k_ccg_init(Ops64 A, LevelDims d, const float* rc, double* r, double* z, double* p, double* dots) {
-    const int b = blockIdx.x;
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
     double rz = 0, rr = 0;
-    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
         const size_t q = (size_t)b * d.nint + c;
@@ -363,9 +382,9 @@ __global__ void k_ccg_init(Ops64 A, LevelDims d, const float* rc, double* r, dou
 }
 
 __global__ void k_ccg_spmv(Ops64 A, LevelDims d, const double* p, double* Ap, double* dots) {
-    const int b = blockIdx.x;
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
     double pa = 0;
-    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
         const double y = apply_A<double>(A, d, p, b, c, i, j, k);
@@ -377,10 +396,10 @@ __global__ void k_ccg_spmv(Ops64 A, LevelDims d, const double* p, double* Ap, do
 
 __global__ void k_ccg_update(Ops64 A, LevelDims d, double* x, const double* p, double* r, const double* Ap, double* z,
                              const double* dots, double* nd) {
-    const int b = blockIdx.x;
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
     const double alpha = dots[0] / dots[1];
     double rz = 0, rr = 0;
-    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
         const size_t P = pidx(d, b, i, j, k), q = (size_t)b * d.nint + c;
@@ -396,8 +415,8 @@ __global__ void k_ccg_update(Ops64 A, LevelDims d, double* x, const double* p, d
 }
 
 __global__ void k_ccg_p(LevelDims d, double* p, const double* z, const double* dots, const double* nd) {
-    const int b = blockIdx.x;
-    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
         const size_t P = pidx(d, b, i, j, k);
@@ -418,6 +437,8 @@ struct SvLevel {
     int32_t *hdst = nullptr, *hsrc = nullptr, *hst = nullptr;
     double* hw = nullptr;
     int64_t nh = 0;
+    int32_t *hcdst = nullptr, *hcsrc = nullptr;   // halo entries that are plain copies
+    int64_t nhc = 0;
     float *z = nullptr, *r = nullptr, *res = nullptr;
     HaloList halo() const { return HaloList{nh, hdst, hsrc, hst, hw}; }
     Ops64 ops64() const { return Ops64{Aii, Ai, Aj, Ak}; }
@@ -476,16 +497,18 @@ struct falcon_solver {
 namespace {
 
 // grid.x = block (up to 2^31-1 blocks), grid.y = 256-cell chunk of the block
-// One CTA per block looping over its cells: consecutive CTAs stream
-// consecutive blocks, and each per-problem reduction takes one atomic per
-// block (up to 2^31-1 blocks).
-dim3 grid_cells(const LevelDims& d, int nblocks) { (void)d; return dim3((unsigned)nblocks); }
+// CTAs over (block, chunk of kCellChunk cells), block-major: consecutive CTAs
+// stream consecutive memory, and each per-problem reduction takes one atomic
+// per chunk.
+dim3 grid_cells(const LevelDims& d, int nblocks) {
+    return dim3((unsigned)nblocks * (unsigned)((d.nint + kCellChunk - 1) / kCellChunk));
+}
 unsigned tpb(const LevelDims& d) { return (unsigned)std::min(256, (d.nint + 31) / 32 * 32); }
 
 template <class T> cudaError_t halo_fill(falcon_solver* sv, int l, T* v) {
     const SvLevel& L = sv->lv[l];
-    if (L.nh == 0) return cudaSuccess;
-    k_halo<T><<<(unsigned)((L.nh + 255) / 256), 256, 0, sv->st>>>(v, L.halo());
+    if (L.nhc > 0) k_halo_copy<T><<<(unsigned)((L.nhc + 255) / 256), 256, 0, sv->st>>>(v, L.hcdst, L.hcsrc, L.nhc);
+    if (L.nh > 0) k_halo<T><<<(unsigned)((L.nh + 255) / 256), 256, 0, sv->st>>>(v, L.halo());
     return cudaGetLastError();
 }
 
@@ -607,29 +630,44 @@ int setup(falcon_solver* sv) {
         SCK(up32(&L.fAj, H.Aj), "operator");
         SCK(up32(&L.fAk, H.Ak), "operator");
         // halo entries -> padded offsets and strides
-        const size_t n = H.halo.size();
-        std::vector<int32_t> dst(n), src(n), stv(3 * n);
-        std::vector<double> w(3 * n);
+        // halo entries -> padded offsets; entries with all weights zero are
+        // plain copies (a separate list: 8 bytes of index per entry)
+        std::vector<int32_t> dst, src, stv, cdst, csrc;
+        std::vector<double> w;
         const int32_t strides[3] = {1, L.d.p0, L.d.p0 * L.d.p1};
-        for (size_t q = 0; q < n; ++q) {
-            const HaloEntry& h = H.halo[q];
-            dst[q] = (int32_t)(h.tb * (int64_t)L.d.npad + ((int64_t)h.tk * L.d.p1 + h.tj) * L.d.p0 + h.ti);
-            src[q] = (int32_t)(h.sb * (int64_t)L.d.npad + ((int64_t)h.k0 * L.d.p1 + h.j0) * L.d.p0 + h.i0);
+        for (const HaloEntry& h : H.halo) {
+            const int32_t t = (int32_t)(h.tb * (int64_t)L.d.npad + ((int64_t)h.tk * L.d.p1 + h.tj) * L.d.p0 + h.ti);
+            const int32_t f = (int32_t)(h.sb * (int64_t)L.d.npad + ((int64_t)h.k0 * L.d.p1 + h.j0) * L.d.p0 + h.i0);
+            if (h.w[0] == 0.0 && h.w[1] == 0.0 && h.w[2] == 0.0) {
+                cdst.push_back(t);
+                csrc.push_back(f);
+                continue;
+            }
+            dst.push_back(t);
+            src.push_back(f);
             for (int dd = 0; dd < 3; ++dd) {
-                w[3 * q + dd] = h.w[dd];
-                stv[3 * q + dd] = h.w[dd] != 0.0 ? strides[dd] : 0;
+                w.push_back(h.w[dd]);
+                stv.push_back(h.w[dd] != 0.0 ? strides[dd] : 0);
             }
         }
+        const size_t n = dst.size(), nc = cdst.size();
         L.nh = (int64_t)n;
+        L.nhc = (int64_t)nc;
         SCK(sv->alloc(&L.hdst, n * 4), "halo");
         SCK(sv->alloc(&L.hsrc, n * 4), "halo");
         SCK(sv->alloc(&L.hst, 3 * n * 4), "halo");
         SCK(sv->alloc(&L.hw, 3 * n * 8), "halo");
+        SCK(sv->alloc(&L.hcdst, nc * 4), "halo");
+        SCK(sv->alloc(&L.hcsrc, nc * 4), "halo");
         if (n) {
             SCK(cudaMemcpy(L.hdst, dst.data(), n * 4, cudaMemcpyHostToDevice), "halo");
             SCK(cudaMemcpy(L.hsrc, src.data(), n * 4, cudaMemcpyHostToDevice), "halo");
             SCK(cudaMemcpy(L.hst, stv.data(), 3 * n * 4, cudaMemcpyHostToDevice), "halo");
             SCK(cudaMemcpy(L.hw, w.data(), 3 * n * 8, cudaMemcpyHostToDevice), "halo");
+        }
+        if (nc) {
+            SCK(cudaMemcpy(L.hcdst, cdst.data(), nc * 4, cudaMemcpyHostToDevice), "halo");
+            SCK(cudaMemcpy(L.hcsrc, csrc.data(), nc * 4, cudaMemcpyHostToDevice), "halo");
         }
         SCK(sv->alloc(&L.z, (size_t)nb * L.d.npad * 4), "vectors");
         SCK(sv->alloc(&L.r, (size_t)nb * L.d.nint * 4), "vectors");
@@ -653,16 +691,16 @@ int setup(falcon_solver* sv) {
 
 // scatter an interior [b][nint] FP64 vector into the padded x
 __global__ void k_scatter_pad(LevelDims d, const double* v, double* x) {
-    const int b = blockIdx.x;
-    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
         x[pidx(d, b, i, j, k)] = v[(size_t)b * d.nint + c];
     }
 }
 __global__ void k_gather_pad(LevelDims d, const double* x, double* v) {
-    const int b = blockIdx.x;
-    for (int c = threadIdx.x; c < d.nint; c += blockDim.x) {
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
         v[(size_t)b * d.nint + c] = x[pidx(d, b, i, j, k)];
