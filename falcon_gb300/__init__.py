@@ -67,7 +67,7 @@ class FalconError(RuntimeError):
 
 
 def build(force=False):
-    from .build import build as _b
+    from ._build import build as _b
     return _b(force=force)
 
 

@@ -10,13 +10,14 @@ import ctypes as C
 import math
 
 MAX_AMR = 16
-NVAR = 8
+NVAR = 9          # variables of the host block arrays (the reference's Dynamo MHD block)
+NVAR_EVOLVED = 8  # rho1 .. s1; psi (index 8) is evolved only with divb_option = 1
 NPROF = 9
 PREC_FP64 = 0
 PREC_MIXED = 1
 
-# variable order of the Dynamo MHD block (3_6/ModBlock.f90:153-162), psi omitted
-VAR_NAMES = ("rho1", "vr", "vt", "vp", "br", "bt", "bp", "s1")
+# variable order of the Dynamo MHD block (3_6/ModBlock.f90:153-163)
+VAR_NAMES = ("rho1", "vr", "vt", "vp", "br", "bt", "bp", "s1", "psi")
 
 
 class TreeSpec(C.Structure):
@@ -73,7 +74,7 @@ class GhostEntry(C.Structure):
 def make_config(block=(8, 8, 8), ng=2, root_tiles=(1, 3, 9), radial_levels=2,
                 radial_option=1, amr=((0, 1, 1),), r_range=(0.7, 1.0), cfl=0.4,
                 precision=PREC_FP64, device=0, if_involve_B=1, heating_ratio=1.0,
-                poly_n=1.5, density_contrast=100.0, mu=0.6, xi_mode=1):
+                poly_n=1.5, density_contrast=100.0, mu=0.6, xi_mode=1, divb_option=0):
     """Build a Config. amr is a sequence of (r, theta, phi) divide flags; each level
     is global over the whole radial range, like `#AMR ... T rmin rmax`."""
     cfg = Config()
@@ -97,7 +98,7 @@ def make_config(block=(8, 8, 8), ng=2, root_tiles=(1, 3, 9), radial_levels=2,
         t.amr_range[l][2][1] = math.pi
     t.r_range_rsun[0], t.r_range_rsun[1] = r_range
     cfg.phys.if_involve_B = if_involve_B
-    cfg.phys.divb_option = 0
+    cfg.phys.divb_option = divb_option   # 1: GLM cleaning, psi evolved
     cfg.phys.cfl = cfl
     cfg.phys.heating_ratio = heating_ratio
     cfg.bg.poly_n = poly_n

@@ -19,8 +19,8 @@
 namespace falcon {
 // state_range.cu: range download through the library's static device array
 size_t static_scratch_elems();
-std::string download_range_static(int dev, cudaStream_t st, const void* U, const int8_t* Ulo, bool mixed,
-                                  size_t first, size_t count, double* u);
+std::string download_range_static(int dev, cudaStream_t st, const void* U, const int8_t* Ulo, const void* P,
+                                  bool mixed, size_t first, size_t count, size_t ncell, double* u);
 }  // namespace falcon
 
 using namespace falcon;
@@ -42,6 +42,7 @@ struct falcon_ctx {
     void* U = nullptr;          // u^n (primitive_IV)
     void* RK = nullptr;         // stage state (primitive_rk_IV)
     int8_t* Ulo = nullptr;      // mixed mode: 8-bit correction of u^n (interior cells)
+    void *P = nullptr, *Prk = nullptr, *P2 = nullptr;   // psi of U, RK, R2 (GLM only) [b][cell]
     double* stage64 = nullptr;  // FP64 staging buffer for mixed-mode transfers (lazy)
     double *gi = nullptr, *gj = nullptr, *gs = nullptr;
     float *gi_f = nullptr, *gj_f = nullptr, *gs_f = nullptr;
@@ -146,6 +147,69 @@ cudaError_t cfl(falcon_ctx* ctx) {
     return timed(ctx, KN_FIN, [&] { return launch_finalize_dt(ctx->sc, ctx->st); });
 }
 
+// GLM psi through a stage: read psi_in (global memory, so never the array
+// being written), write P2, then copy to the stage array (RK's psi) for
+// stages 1-3; stage 4 writes u^{n+1}'s psi in place of u^n's cell by cell.
+PsiArgs psi_args(const falcon_ctx* ctx, int s) {
+    if (!ctx->P) return PsiArgs{nullptr, nullptr, nullptr};
+    return PsiArgs{s == 1 ? ctx->P : ctx->Prk, ctx->P, s == 4 ? ctx->P : ctx->P2};
+}
+cudaError_t psi_after_stage(falcon_ctx* ctx, int s) {
+    if (!ctx->P) return cudaSuccess;
+    void* tgt = s == 4 ? ctx->P : ctx->Prk;
+    if (s < 4) {
+        cudaError_t e = cudaMemcpyAsync(ctx->Prk, ctx->P2, (size_t)ctx->dims.nblocks * ctx->dims.ncell * ctx->elem,
+                                        cudaMemcpyDeviceToDevice, ctx->st);
+        if (e != cudaSuccess) return e;
+    }
+    return timed(ctx, KN_GHOST, [&] {
+        return ctx->mixed() ? launch_psi_ghost_mixed(ctx->dims, ctx->gl, (float*)tgt, ctx->st)
+                            : launch_psi_ghost_fp64(ctx->dims, ctx->gl, (double*)tgt, ctx->st);
+    });
+}
+
+// Stage s from `in` into `out` (ModAdvance.f90:59-97), GLM terms included.
+cudaError_t stage(falcon_ctx* ctx, int s, void* in, void* out, const PushTable& push) {
+    const PsiArgs ps = psi_args(ctx, s);
+    cudaError_t e = timed(ctx, KN_STAGE, [&] {
+        return ctx->mixed()
+                   ? launch_stage_mixed(ctx->dims, ctx->geom(), (const float*)in, (const float*)ctx->U, (float*)out,
+                                        ctx->Ulo, push, ps, s, 1, ctx->sc, 1, ctx->kpar_stage, ctx->st)
+                   : launch_stage_fp64(ctx->dims, ctx->geom(), (const double*)in, (const double*)ctx->U, (double*)out,
+                                       ps, s, 1, ctx->sc, 1, ctx->kpar_stage, ctx->st);
+    });
+    if (e != cudaSuccess) return e;
+    return psi_after_stage(ctx, s);
+}
+
+// Artificial diffusion of every variable (ModAdvance.f90:101-109); psi's runs
+// first, from the same pre-diffusion state, into P2.
+cudaError_t diffusion(falcon_ctx* ctx) {
+    cudaError_t e = cudaSuccess;
+    if (ctx->P) {
+        e = timed(ctx, KN_DIFF, [&] {
+            return ctx->mixed() ? launch_psi_diffusion_mixed(ctx->dims, ctx->geom(), (const float*)ctx->U,
+                                                             (const float*)ctx->P, (float*)ctx->P2, ctx->sc, ctx->st)
+                                : launch_psi_diffusion_fp64(ctx->dims, ctx->geom(), (const double*)ctx->U,
+                                                            (const double*)ctx->P, (double*)ctx->P2, ctx->sc, ctx->st);
+        });
+        if (e != cudaSuccess) return e;
+    }
+    e = timed(ctx, KN_DIFF, [&] {
+        return ctx->mixed() ? launch_diffusion_mixed(ctx->dims, ctx->geom(), (float*)ctx->U, ctx->Ulo, ctx->sc,
+                                                     ctx->kpar_diff, ctx->st)
+                            : launch_diffusion_fp64(ctx->dims, ctx->geom(), (double*)ctx->U, ctx->sc, ctx->kpar_diff, ctx->st);
+    });
+    if (e != cudaSuccess || !ctx->P) return e;
+    e = cudaMemcpyAsync(ctx->P, ctx->P2, (size_t)ctx->dims.nblocks * ctx->dims.ncell * ctx->elem,
+                        cudaMemcpyDeviceToDevice, ctx->st);
+    if (e != cudaSuccess) return e;
+    return timed(ctx, KN_GHOST, [&] {
+        return ctx->mixed() ? launch_psi_ghost_mixed(ctx->dims, ctx->gl, (float*)ctx->P, ctx->st)
+                            : launch_psi_ghost_fp64(ctx->dims, ctx->gl, (double*)ctx->P, ctx->st);
+    });
+}
+
 // One ModAdvance_rk4 (3_6/ModAdvance.f90:18-112) as a kernel sequence.
 // FP64: stages 2-4 read and write the stage buffer in place. Mixed: the stage
 // kernels push ghost faces into their output, so input and output differ:
@@ -164,23 +228,12 @@ cudaError_t enqueue_step(falcon_ctx* ctx) {
             in = (s == 1) ? ctx->U : ctx->RK;
             out = (s < 4) ? ctx->RK : ctx->U;
         }
-        e = timed(ctx, KN_STAGE, [&] {
-            return ctx->mixed()
-                       ? launch_stage_mixed(ctx->dims, ctx->geom(), (const float*)in, (const float*)ctx->U,
-                                            (float*)out, ctx->Ulo, ctx->push, s, 1, ctx->sc, 1, ctx->kpar_stage,
-                                            ctx->st)
-                       : launch_stage_fp64(ctx->dims, ctx->geom(), (const double*)in, (const double*)ctx->U,
-                                           (double*)out, s, 1, ctx->sc, 1, ctx->kpar_stage, ctx->st);
-        });
+        e = stage(ctx, s, in, out, ctx->mixed() ? ctx->push : PushTable{});
         if (e != cudaSuccess) return e;
         e = ghost_stage(ctx, out);
         if (e != cudaSuccess) return e;
     }
-    e = timed(ctx, KN_DIFF, [&] {
-        return ctx->mixed() ? launch_diffusion_mixed(ctx->dims, ctx->geom(), (float*)ctx->U, ctx->Ulo, ctx->sc,
-                                                     ctx->kpar_diff, ctx->st)
-                            : launch_diffusion_fp64(ctx->dims, ctx->geom(), (double*)ctx->U, ctx->sc, ctx->kpar_diff, ctx->st);
-    });
+    e = diffusion(ctx);
     if (e != cudaSuccess) return e;
     return ghost(ctx, ctx->U);
 }
@@ -206,9 +259,11 @@ int autotune(falcon_ctx* ctx) {
                 cudaError_t e;
                 if (which == 0)
                     e = ctx->mixed() ? launch_stage_mixed(ctx->dims, ctx->geom(), (const float*)ctx->RK, (const float*)ctx->U,
-                                                          (float*)ctx->R2, nullptr, ctx->push, 2, 1, ctx->sc, 1, kp, ctx->st)
+                                                          (float*)ctx->R2, nullptr, ctx->push, PsiArgs{nullptr, nullptr, nullptr},
+                                                          2, 1, ctx->sc, 1, kp, ctx->st)
                                      : launch_stage_fp64(ctx->dims, ctx->geom(), (const double*)ctx->RK, (const double*)ctx->U,
-                                                         (double*)ctx->RK, 2, 1, ctx->sc, 1, kp, ctx->st);
+                                                         (double*)ctx->RK, PsiArgs{nullptr, nullptr, nullptr}, 2, 1,
+                                                         ctx->sc, 1, kp, ctx->st);
                 else
                     e = ctx->mixed() ? launch_diffusion_mixed(ctx->dims, ctx->geom(), (float*)ctx->RK, nullptr, ctx->sc, kp,
                                                               ctx->st)
@@ -278,6 +333,13 @@ int setup_device(falcon_ctx* ctx) {
     CK(ctx->alloc(&ctx->RK, sbytes), "alloc RK");
     CK(cudaMemsetAsync(ctx->U, 0, sbytes, ctx->st), "memset");
     CK(cudaMemsetAsync(ctx->RK, 0, sbytes, ctx->st), "memset");
+    if (ctx->cfg.phys.divb_option == 1) {
+        const size_t pbytes = (size_t)nb * g.ncell * ctx->elem;
+        for (void** q : {&ctx->P, &ctx->Prk, &ctx->P2}) {
+            CK(ctx->alloc(q, pbytes), "alloc psi");
+            CK(cudaMemsetAsync(*q, 0, pbytes, ctx->st), "memset");
+        }
+    }
     if (ctx->mixed()) {
         CK(ctx->alloc(&ctx->Ulo, (size_t)nb * NV * g.ncell), "alloc U correction");
         CK(cudaMemsetAsync(ctx->Ulo, 0, (size_t)nb * NV * g.ncell, ctx->st), "memset");
@@ -619,22 +681,75 @@ int falcon_ghost_map(const falcon_ctx* ctx, falcon_ghost_entry* out, int64_t cap
     return FALCON_OK;
 }
 
+// Host block arrays are [b][FALCON_NVAR = 9][cell] (psi last, as the
+// reference's MHD block); the device keeps the 8 evolved variables as
+// [b][8][cell] and psi in an array of its own when GLM is on.
+namespace {
+size_t host_elems(const falcon_ctx* ctx) { return (size_t)ctx->dims.nblocks * FALCON_NVAR * ctx->dims.ncell; }
+
+int put_state(falcon_ctx* ctx, const double* u, void* U, int8_t* lo, void* P) {
+    const size_t nb = (size_t)ctx->dims.nblocks, nc = (size_t)ctx->dims.ncell;
+    if (!P) {   // psi is not evolved: it must be 0, as it then stays in the reference
+        for (size_t b = 0; b < nb; ++b) {
+            const double* q = u + (b * FALCON_NVAR + NV) * nc;
+            for (size_t c = 0; c < nc; ++c)
+                if (q[c] != 0.0) return ctx->fail(FALCON_ERR_INVALID_ARG, "psi must be 0 when divb_option = 0");
+        }
+    }
+    if (ctx->mixed()) {
+        const size_t n9 = host_elems(ctx);
+        if (!ctx->stage64) CK(ctx->alloc(&ctx->stage64, n9 * 8), "alloc staging");
+        CK(cudaMemcpyAsync(ctx->stage64, u, n9 * 8, cudaMemcpyHostToDevice, ctx->st), "upload");
+        CK(launch_convert_state(ctx->stage64, (float*)U, lo, (int64_t)(nb * NV * nc), ctx->dims, ctx->st), "upload convert");
+        if (P) CK(launch_convert_psi(ctx->stage64, (float*)P, (int64_t)nb, (int64_t)nc, ctx->st), "upload convert");
+    } else {
+        CK(cudaMemcpy2DAsync(U, NV * nc * 8, u, FALCON_NVAR * nc * 8, NV * nc * 8, nb, cudaMemcpyHostToDevice, ctx->st),
+           "upload");
+        if (P)
+            CK(cudaMemcpy2DAsync(P, nc * 8, u + NV * nc, FALCON_NVAR * nc * 8, nc * 8, nb, cudaMemcpyHostToDevice, ctx->st),
+               "upload");
+    }
+    return FALCON_OK;
+}
+
+int get_state(falcon_ctx* ctx, const void* U, const int8_t* lo, const void* P, double* u) {
+    const size_t nb = (size_t)ctx->dims.nblocks, nc = (size_t)ctx->dims.ncell;
+    if (ctx->mixed()) {
+        const size_t n9 = host_elems(ctx);
+        if (!ctx->stage64) CK(ctx->alloc(&ctx->stage64, n9 * 8), "alloc staging");
+        CK(launch_gather_host(U, lo, P, true, 0, (int64_t)n9, (int64_t)nc, ctx->stage64, ctx->st), "download convert");
+        CK(cudaMemcpyAsync(u, ctx->stage64, n9 * 8, cudaMemcpyDeviceToHost, ctx->st), "download");
+        CK(cudaStreamSynchronize(ctx->st), "download");
+    } else {
+        CK(cudaMemcpy2DAsync(u, FALCON_NVAR * nc * 8, U, NV * nc * 8, NV * nc * 8, nb, cudaMemcpyDeviceToHost, ctx->st),
+           "download");
+        if (P)
+            CK(cudaMemcpy2DAsync(u + NV * nc, FALCON_NVAR * nc * 8, P, nc * 8, nc * 8, nb, cudaMemcpyDeviceToHost, ctx->st),
+               "download");
+        CK(cudaStreamSynchronize(ctx->st), "download");
+        if (!P)
+            for (size_t b = 0; b < nb; ++b) std::memset(u + (b * FALCON_NVAR + NV) * nc, 0, nc * 8);
+    }
+    return FALCON_OK;
+}
+}  // namespace
+
 int falcon_upload_state(falcon_ctx* ctx, const double* u) {
     int rc = need_device(ctx);
     if (rc) return rc;
     if (!u) return ctx->fail(FALCON_ERR_INVALID_ARG, "null state");
-    const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
-    if (ctx->mixed()) {
-        // FP64 host array -> device staging -> FP32 state (conversion on the GPU)
-        if (!ctx->stage64) CK(ctx->alloc(&ctx->stage64, n * 8), "alloc staging");
-        CK(cudaMemcpyAsync(ctx->stage64, u, n * 8, cudaMemcpyHostToDevice, ctx->st), "upload");
-        CK(launch_convert_state(ctx->stage64, (float*)ctx->U, ctx->Ulo, (int64_t)n, ctx->dims, ctx->st),
-           "upload convert");
-    } else {
-        CK(cudaMemcpyAsync(ctx->U, u, n * 8, cudaMemcpyHostToDevice, ctx->st), "upload");
-    }
+    rc = put_state(ctx, u, ctx->U, ctx->Ulo, ctx->P);
+    if (rc) return rc;
     // primitive_rk_IV = primitive_IV, as the reference's initialisation leaves it
+    const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
     CK(cudaMemcpyAsync(ctx->RK, ctx->U, n * ctx->elem, cudaMemcpyDeviceToDevice, ctx->st), "upload");
+    // psi's stage array and the scratch it is copied from start equal too:
+    // their ghost cells that no exchange writes (the radial boundary planes)
+    // then stay at the uploaded values, as the reference's arrays do.
+    if (ctx->P)
+        for (void* q : {ctx->Prk, ctx->P2})
+            CK(cudaMemcpyAsync(q, ctx->P, (size_t)ctx->dims.nblocks * ctx->dims.ncell * ctx->elem,
+                               cudaMemcpyDeviceToDevice, ctx->st), "upload");
     CK(cudaStreamSynchronize(ctx->st), "upload");
     return FALCON_OK;
 }
@@ -643,23 +758,14 @@ int falcon_download_state(falcon_ctx* ctx, double* u) {
     int rc = need_device(ctx);
     if (rc) return rc;
     if (!u) return ctx->fail(FALCON_ERR_INVALID_ARG, "null state");
-    const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
-    if (ctx->mixed()) {
-        if (!ctx->stage64) CK(ctx->alloc(&ctx->stage64, n * 8), "alloc staging");
-        CK(launch_widen_state((const float*)ctx->U, ctx->Ulo, ctx->stage64, (int64_t)n, ctx->st), "download convert");
-        CK(cudaMemcpyAsync(u, ctx->stage64, n * 8, cudaMemcpyDeviceToHost, ctx->st), "download");
-    } else {
-        CK(cudaMemcpyAsync(u, ctx->U, n * 8, cudaMemcpyDeviceToHost, ctx->st), "download");
-    }
-    CK(cudaStreamSynchronize(ctx->st), "download");
-    return FALCON_OK;
+    return get_state(ctx, ctx->U, ctx->Ulo, ctx->P, u);
 }
 
 int falcon_download_state_range(falcon_ctx* ctx, size_t first, size_t count, double* u) {
     int rc = need_device(ctx);
     if (rc) return rc;
     if (!u && count) return ctx->fail(FALCON_ERR_INVALID_ARG, "null state");
-    const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
+    const size_t n = host_elems(ctx);
     const size_t cap = static_scratch_elems();
     if (count > cap)
         return ctx->fail(FALCON_ERR_INVALID_ARG,
@@ -670,7 +776,8 @@ int falcon_download_state_range(falcon_ctx* ctx, size_t first, size_t count, dou
         return ctx->fail(FALCON_ERR_INVALID_ARG, "falcon_download_state_range: first " + std::to_string(first) +
                                                      " + count " + std::to_string(count) + " exceeds the state size " +
                                                      std::to_string(n));
-    const std::string e = download_range_static(ctx->device, ctx->st, ctx->U, ctx->Ulo, ctx->mixed(), first, count, u);
+    const std::string e = download_range_static(ctx->device, ctx->st, ctx->U, ctx->Ulo, ctx->P, ctx->mixed(), first,
+                                                count, (size_t)ctx->dims.ncell, u);
     if (!e.empty()) return ctx->fail(FALCON_ERR_CUDA, e);
     return FALCON_OK;
 }
@@ -707,6 +814,10 @@ int falcon_exchange(falcon_ctx* ctx) {
     int rc = need_device(ctx);
     if (rc) return rc;
     CK(ghost(ctx, ctx->U), "ghost fill");
+    if (ctx->P)
+        CK(ctx->mixed() ? launch_psi_ghost_mixed(ctx->dims, ctx->gl, (float*)ctx->P, ctx->st)
+                        : launch_psi_ghost_fp64(ctx->dims, ctx->gl, (double*)ctx->P, ctx->st),
+           "ghost fill");
     CK(cudaStreamSynchronize(ctx->st), "ghost fill");
     collect(ctx);
     return FALCON_OK;
@@ -785,16 +896,10 @@ int falcon_step_phase(falcon_ctx* ctx, int32_t phase) {
         const int s = phase;
         void* in = (s == 1) ? ctx->U : ctx->RK;
         void* out = (s < 4) ? ctx->RK : ctx->U;
-        e = ctx->mixed() ? launch_stage_mixed(ctx->dims, ctx->geom(), (const float*)in, (const float*)ctx->U,
-                                              (float*)out, ctx->Ulo, PushTable{}, s, 1, ctx->sc, 1, ctx->kpar_stage,
-                                              ctx->st)
-                         : launch_stage_fp64(ctx->dims, ctx->geom(), (const double*)in, (const double*)ctx->U,
-                                             (double*)out, s, 1, ctx->sc, 1, ctx->kpar_stage, ctx->st);
+        e = stage(ctx, s, in, out, PushTable{});
         if (e == cudaSuccess) e = ghost(ctx, out);
     } else {
-        e = ctx->mixed() ? launch_diffusion_mixed(ctx->dims, ctx->geom(), (float*)ctx->U, ctx->Ulo, ctx->sc,
-                                                  ctx->kpar_diff, ctx->st)
-                         : launch_diffusion_fp64(ctx->dims, ctx->geom(), (double*)ctx->U, ctx->sc, ctx->kpar_diff, ctx->st);
+        e = diffusion(ctx);
         if (e == cudaSuccess) e = ghost(ctx, ctx->U);
         if (e == cudaSuccess) ++ctx->steps_done;
     }
@@ -808,16 +913,7 @@ int falcon_download_stage_state(falcon_ctx* ctx, double* u) {
     int rc = need_device(ctx);
     if (rc) return rc;
     if (!u) return ctx->fail(FALCON_ERR_INVALID_ARG, "null state");
-    const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
-    if (ctx->mixed()) {
-        if (!ctx->stage64) CK(ctx->alloc(&ctx->stage64, n * 8), "alloc staging");
-        CK(launch_widen_state((const float*)ctx->RK, nullptr, ctx->stage64, (int64_t)n, ctx->st), "download convert");
-        CK(cudaMemcpyAsync(u, ctx->stage64, n * 8, cudaMemcpyDeviceToHost, ctx->st), "download");
-    } else {
-        CK(cudaMemcpyAsync(u, ctx->RK, n * 8, cudaMemcpyDeviceToHost, ctx->st), "download");
-    }
-    CK(cudaStreamSynchronize(ctx->st), "download");
-    return FALCON_OK;
+    return get_state(ctx, ctx->RK, nullptr, ctx->Prk, u);
 }
 
 int falcon_synchronize(falcon_ctx* ctx) {

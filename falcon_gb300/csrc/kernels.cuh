@@ -157,14 +157,27 @@ struct StepDims {
     int nblocks, ni, nj, nk, nip, njp, nkp, ncell;
 };
 
+// GLM divergence cleaning (3_6/ModDivB.f90:13-38): psi arrays [b][cell] of the
+// stage input, of u^n and of the stage output (in == nullptr: GLM off). psi is
+// read from global memory (not the shared-memory ring), so out != in.
+struct PsiArgs {
+    const void* in;
+    const void* un;
+    void* out;
+};
+
 // ---- launchers (defined in mhd_fp64.cu / mhd_mixed.cu) --------------------
 // stage s = 1..4; in: u_s, un: u^n, out: u_{s+1}; bc_writeback: 1 writes the
 // mirrored radial ghosts back into `in`, as ModBoundary does in place
 // (3_6/ModBoundary.f90:10-55); the diffusion pass later reads those of u^n
 // (3_6/ModAdvance.f90:101-108)
 cudaError_t launch_stage_fp64(const StepDims& d, const Geometry& g, const double* in, const double* un,
-                              double* out, int stage, int bc_writeback, StepScalars* sc,
+                              double* out, const PsiArgs& psi, int stage, int bc_writeback, StepScalars* sc,
                               int heat_on, int kpar, cudaStream_t st);
+// GLM: psi's artificial diffusion (into psi_out) and psi's ghost fill
+cudaError_t launch_psi_diffusion_fp64(const StepDims& d, const Geometry& g, const double* u, const double* psi,
+                                      double* psi_out, StepScalars* sc, cudaStream_t st);
+cudaError_t launch_psi_ghost_fp64(const StepDims& d, const GhostLists& gl, double* psi, cudaStream_t st);
 cudaError_t launch_diffusion_fp64(const StepDims& d, const Geometry& g, double* u, StepScalars* sc,
                                   int kpar, cudaStream_t st);
 cudaError_t launch_cfl_fp64(const StepDims& d, const Geometry& g, const double* u, StepScalars* sc,
@@ -176,8 +189,11 @@ cudaError_t launch_ghost_fp64(const StepDims& d, const GhostLists& gl, double* u
 // push: faces written into `out` by the stage kernel (tgt == nullptr: none);
 // pushing needs out != in, since a target block may still be reading `in`.
 cudaError_t launch_stage_mixed(const StepDims& d, const Geometry& g, const float* in, const float* un,
-                               float* out, int8_t* lo, const PushTable& push, int stage, int bc_writeback,
-                               StepScalars* sc, int heat_on, int kpar, cudaStream_t st);
+                               float* out, int8_t* lo, const PushTable& push, const PsiArgs& psi, int stage,
+                               int bc_writeback, StepScalars* sc, int heat_on, int kpar, cudaStream_t st);
+cudaError_t launch_psi_diffusion_mixed(const StepDims& d, const Geometry& g, const float* u, const float* psi,
+                                       float* psi_out, StepScalars* sc, cudaStream_t st);
+cudaError_t launch_psi_ghost_mixed(const StepDims& d, const GhostLists& gl, float* psi, cudaStream_t st);
 cudaError_t launch_diffusion_mixed(const StepDims& d, const Geometry& g, float* u, int8_t* lo, StepScalars* sc,
                                    int kpar, cudaStream_t st);
 cudaError_t launch_cfl_mixed(const StepDims& d, const Geometry& g, const float* u, StepScalars* sc,
@@ -188,10 +204,14 @@ cudaError_t launch_finalize_dt(StepScalars* sc, cudaStream_t st);
 // k-chunk depths instantiated for this block size (returns the count)
 int kpar_candidates_fp64(const StepDims& d, int* out);
 int kpar_candidates_mixed(const StepDims& d, int* out);
-// FP64 <-> compensated FP32 state (lo may be nullptr: plain FP32)
+// Host block arrays ([b][FALCON_NVAR = 9][cell] FP64) <-> device state
+// ([b][8][cell], FP32 compensated or FP64) and the optional psi array.
+// convert: n = device state elements; gather: host elements [first, first+count)
 cudaError_t launch_convert_state(const double* src, float* dst, int8_t* lo, int64_t n, const StepDims& dm,
                                  cudaStream_t st);
-cudaError_t launch_widen_state(const float* src, const int8_t* lo, double* dst, int64_t n, cudaStream_t st);
+cudaError_t launch_convert_psi(const double* src, float* psi, int64_t nb, int64_t ncell, cudaStream_t st);
+cudaError_t launch_gather_host(const void* U, const int8_t* lo, const void* psi, bool fp32, int64_t first, int64_t count,
+                               int64_t ncell, double* out, cudaStream_t st);
 
 // names of the kernels as they appear in profiles
 const char* const* kernel_names();

@@ -23,7 +23,8 @@ template <> struct Cand<float> {
 
 template <class T, int N, int KP>
 cudaError_t stage_n(const StepDims& d, const Geometry& g, const T* in, const T* un, T* out, int8_t* lo,
-                    const PushTable& push, int stage, int bcw, StepScalars* sc, int heat, cudaStream_t st) {
+                    const PushTable& push, const PsiArgs& psi, int stage, int bcw, StepScalars* sc, int heat,
+                    cudaStream_t st) {
     using S = Shape<T, N, N, N, KP>;
     static bool attr = false;
     if (!attr) {
@@ -32,7 +33,7 @@ cudaError_t stage_n(const StepDims& d, const Geometry& g, const T* in, const T* 
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    k_stage<T, N, N, N, KP><<<d.nblocks, S::NT, S::smem_stage, st>>>(in, un, out, lo, push, g, sc, stage, bcw, heat);
+    k_stage<T, N, N, N, KP><<<d.nblocks, S::NT, S::smem_stage, st>>>(in, un, out, lo, push, psi, g, sc, stage, bcw, heat);
     return cudaGetLastError();
 }
 
@@ -52,9 +53,10 @@ cudaError_t diff_n(const StepDims& d, const Geometry& g, T* u, int8_t* lo, StepS
 
 template <class T>
 cudaError_t stage_any(const StepDims& d, const Geometry& g, const T* in, const T* un, T* out, int8_t* lo,
-                      const PushTable& push, int stage, int bcw, StepScalars* sc, int heat, int kpar, cudaStream_t st) {
+                      const PushTable& push, const PsiArgs& psi, int stage, int bcw, StepScalars* sc, int heat, int kpar,
+                      cudaStream_t st) {
 #define FALCON_STAGE_CASE(N, K) \
-    if (d.ni == N && kpar == K) return stage_n<T, N, K>(d, g, in, un, out, lo, push, stage, bcw, sc, heat, st);
+    if (d.ni == N && kpar == K) return stage_n<T, N, K>(d, g, in, un, out, lo, push, psi, stage, bcw, sc, heat, st);
     if (d.ni != d.nj || d.ni != d.nk) return cudaErrorInvalidValue;
     FALCON_STAGE_CASE(8, 2) FALCON_STAGE_CASE(8, 4)
     FALCON_STAGE_CASE(16, 1)
@@ -74,6 +76,22 @@ cudaError_t diff_any(const StepDims& d, const Geometry& g, T* u, int8_t* lo, Ste
     if constexpr (!Pol<T>::exact) { FALCON_DIFF_CASE(8, 8) FALCON_DIFF_CASE(16, 2) FALCON_DIFF_CASE(16, 4) }
 #undef FALCON_DIFF_CASE
     return cudaErrorInvalidValue;
+}
+
+template <class T>
+cudaError_t psi_diffusion_any(const StepDims& d, const Geometry& g, const T* u, const T* psi, T* psi_out,
+                              StepScalars* sc, cudaStream_t st) {
+    const int nint = d.ni * d.nj * d.nk;
+    k_psi_diffusion<T><<<dim3((nint + 255) / 256, d.nblocks), 256, 0, st>>>(u, psi, psi_out, g, sc, d);
+    return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t psi_ghost_any(const StepDims& d, const GhostLists& gl, T* psi, cudaStream_t st) {
+    const int64_t n = gl.cp.n + gl.ln.n + gl.ip.n;
+    if (n == 0) return cudaSuccess;
+    k_psi_ghost<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(psi, gl, d.ncell, d.nip, d.nip * d.njp);
+    return cudaGetLastError();
 }
 
 template <class T>

@@ -10,8 +10,16 @@ using impl::cfl_any;
 using impl::ghost_any;
 
 cudaError_t launch_stage_fp64(const StepDims& d, const Geometry& g, const double* in, const double* un, double* out,
-                              int stage, int bcw, StepScalars* sc, int heat, int kpar, cudaStream_t st) {
-    return stage_any<double>(d, g, in, un, out, nullptr, PushTable{}, stage, bcw, sc, heat, kpar, st);
+                              const PsiArgs& psi, int stage, int bcw, StepScalars* sc, int heat, int kpar,
+                              cudaStream_t st) {
+    return stage_any<double>(d, g, in, un, out, nullptr, PushTable{}, psi, stage, bcw, sc, heat, kpar, st);
+}
+cudaError_t launch_psi_diffusion_fp64(const StepDims& d, const Geometry& g, const double* u, const double* psi,
+                                      double* psi_out, StepScalars* sc, cudaStream_t st) {
+    return impl::psi_diffusion_any<double>(d, g, u, psi, psi_out, sc, st);
+}
+cudaError_t launch_psi_ghost_fp64(const StepDims& d, const GhostLists& gl, double* psi, cudaStream_t st) {
+    return impl::psi_ghost_any<double>(d, gl, psi, st);
 }
 cudaError_t launch_diffusion_fp64(const StepDims& d, const Geometry& g, double* u, StepScalars* sc,
                                   int kpar, cudaStream_t st) {
@@ -41,11 +49,19 @@ cudaError_t launch_finalize_dt(StepScalars* sc, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-// FP64 -> compensated FP32: hi = RN(u); interior cells get the correction of
-// u - hi, ghost cells q = 0 (x counts from the start of the state)
+// Host block arrays carry FALCON_NVAR = 9 variables ([b][9][cell], psi last);
+// the device state carries the 8 evolved ones ([b][8][cell]) and, with GLM,
+// psi in an array of its own ([b][cell]).
+__device__ __forceinline__ int64_t host_index(int64_t x, int64_t ncell) {   // device state element -> host element
+    const int64_t b = x / (NV * ncell);
+    return x + b * ncell;
+}
+
+// FP64 host array -> compensated FP32 state: hi = RN(u); interior cells get
+// the correction of u - hi, ghost cells q = 0
 __global__ void k_narrow(const double* s, float* d, int8_t* lo, int64_t n, StepDims dm) {
     for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
-        const double u = s[x];
+        const double u = s[host_index(x, dm.ncell)];
         const float hi = (float)u;
         d[x] = hi;
         if (lo) {
@@ -56,10 +72,33 @@ __global__ void k_narrow(const double* s, float* d, int8_t* lo, int64_t n, StepD
         }
     }
 }
-__global__ void k_widen(const float* s, const int8_t* lo, double* d, int64_t n) {
-    for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
-        const float hi = s[x];
-        d[x] = lo ? (double)hi + (double)lo[x] * (double)lo_unit(hi) : (double)hi;
+// psi plane of the host array -> FP32 psi array (mixed GLM)
+__global__ void k_narrow_psi(const double* s, float* psi, int64_t nb, int64_t ncell) {
+    for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < nb * ncell; x += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b = x / ncell;
+        psi[x] = (float)s[(b * (NV + 1) + NV) * ncell + (x - b * ncell)];
+    }
+}
+// host elements [first, first + count) as FP64 from the device state (FP32
+// with its correction, or FP64) and psi (nullptr: psi = 0)
+template <class T>
+__global__ void k_gather_host(const T* U, const int8_t* lo, const T* psi, int64_t first, int64_t count, int64_t ncell,
+                              double* out) {
+    for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < count; x += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t h = first + x;
+        const int64_t b = h / ((NV + 1) * ncell), r = h - b * (NV + 1) * ncell;
+        double v;
+        if (r < NV * ncell) {
+            const int64_t e = b * NV * ncell + r;
+            const T hi = U[e];
+            v = (double)hi;
+            if constexpr (sizeof(T) == 4) {
+                if (lo) v += (double)lo[e] * (double)lo_unit((float)hi);
+            }
+        } else {
+            v = psi ? (double)psi[b * ncell + (r - NV * ncell)] : 0.0;
+        }
+        out[x] = v;
     }
 }
 cudaError_t launch_convert_state(const double* src, float* dst, int8_t* lo, int64_t n, const StepDims& dm,
@@ -67,8 +106,14 @@ cudaError_t launch_convert_state(const double* src, float* dst, int8_t* lo, int6
     k_narrow<<<1216, 256, 0, st>>>(src, dst, lo, n, dm);
     return cudaGetLastError();
 }
-cudaError_t launch_widen_state(const float* src, const int8_t* lo, double* dst, int64_t n, cudaStream_t st) {
-    k_widen<<<1216, 256, 0, st>>>(src, lo, dst, n);
+cudaError_t launch_convert_psi(const double* src, float* psi, int64_t nb, int64_t ncell, cudaStream_t st) {
+    k_narrow_psi<<<1216, 256, 0, st>>>(src, psi, nb, ncell);
+    return cudaGetLastError();
+}
+cudaError_t launch_gather_host(const void* U, const int8_t* lo, const void* psi, bool fp32, int64_t first, int64_t count,
+                               int64_t ncell, double* out, cudaStream_t st) {
+    if (fp32) k_gather_host<float><<<1216, 256, 0, st>>>((const float*)U, lo, (const float*)psi, first, count, ncell, out);
+    else k_gather_host<double><<<1216, 256, 0, st>>>((const double*)U, nullptr, (const double*)psi, first, count, ncell, out);
     return cudaGetLastError();
 }
 

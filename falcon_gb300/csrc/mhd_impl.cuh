@@ -251,8 +251,8 @@ __device__ __forceinline__ void cell_of_thread(int tid, int& i, int& j, int& kq)
 // u_out = u^n + dt*R/(5-s) (3_6/ModAdvance.f90:87-93).
 template <class T, int NI, int NJ, int NK, int KPAR>
 __global__ void __launch_bounds__(NI* NJ* KPAR)
-k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, Geometry g, StepScalars* sc, int stage,
-        int bc_writeback, int heat_on) {
+k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, PsiArgs psi, Geometry g, StepScalars* sc,
+        int stage, int bc_writeback, int heat_on) {
     using S = Shape<T, NI, NJ, NK, KPAR>;
     constexpr int NIP = S::NIP, PL = S::PL, W = S::W, WP = S::WP, NCELL = S::NCELL;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -434,6 +434,46 @@ k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, Geometry 
             q1 = q1 * rinv; q2 = q2 * rinv; q3 = q3 * rinv;
             q1 = q1 * sinv;
             RBr = q1; RBt = q2; RBp = q3;
+        }
+
+        // GLM divergence cleaning (3_6/ModDivB.f90:13-38), after the equation
+        // terms as 3_6/ModAdvance.f90:82-84 orders it: dB += -grad(psi);
+        // dpsi = -v_wave^2 div(B) - v_wave/h_LLL psi, v_wave from u^n
+        if (psi.in != nullptr) {
+            const T* P = static_cast<const T*>(psi.in) + (size_t)b * NCELL + (size_t)kp * PL + jj * NIP + ii;
+            auto Q = [&](int di, int dj, int dk) -> T { return P[(size_t)dk * PL + dj * NIP + di]; };
+            // ModSpherical_Grad_f (3_6/ModSpherical.f90:201-239)
+            const T g1 = D(c1, [&](int m) { return Q(m, 0, 0); });
+            T g2 = D(c2, [&](int m) { return Q(0, m, 0); });
+            g2 = g2 * rinv;
+            T g3 = D(c3, [&](int m) { return Q(0, 0, m); });
+            g3 = g3 * rinv;
+            g3 = g3 * sinv;
+            RBr = RBr - g1;
+            RBt = RBt - g2;
+            RBp = RBp - g3;
+            // ModSpherical_div of B (3_6/ModSpherical.f90:104-159)
+            T dB = D(c1, [&](int m) { return A(V_BR, m, 0, 0) * GR2[ii + m]; });
+            dB = dB * r2inv;
+            T e23 = D(c2, [&](int m) { return A(V_BT, 0, m, 0) * GSIN[jj + m]; });
+            e23 = e23 + D(c3, [&](int m) { return A(V_BP, 0, 0, m); });
+            e23 = e23 * sinv;
+            e23 = e23 * rinv;
+            const T divB = dB + e23;
+            // ModWaveSpeed_Dynamo (3_6/ModWaveSpeed.f90:8-27) and h_LLL
+            // (3_6/ModBlock.f90:416-425) at this cell, as the CFL pass forms them
+            T w = gi[GI_CS * NIP + ii] +
+                  sqrt(u0s[V_VR] * u0s[V_VR] + u0s[V_VT] * u0s[V_VT] + u0s[V_VP] * u0s[V_VP]);
+            w = w + sqrt(u0s[V_BR] * u0s[V_BR] + u0s[V_BT] * u0s[V_BT] + u0s[V_BP] * u0s[V_BP]) / sqrt(rho0c);
+            const T rcell = GR[ii];
+            const T h = fmin(fmin(gs[GS_DXI], rcell * gs[GS_DXJ]), rcell * sin_c * gs[GS_DXK]);
+            const T Rpsi = -(w * w * divB) - w / h * Q(0, 0, 0);
+            const size_t pc = (size_t)b * NCELL + (size_t)kp * PL + jj * NIP + ii;
+            const T pn = static_cast<const T*>(psi.un)[pc];
+            T po;
+            if constexpr (Pol<T>::exact) po = (T)((double)pn + (dt * (double)Rpsi) / divs);
+            else po = fmaf((float)dtk, (float)Rpsi, (float)pn);
+            static_cast<T*>(psi.out)[pc] = po;
         }
 
         // stage update
@@ -734,6 +774,95 @@ __global__ void __launch_bounds__(128) k_ghost_interp(T* u, GhostInterpList L, i
     const size_t dd = (size_t)L.dst[e];
 #pragma unroll
     for (int v = 0; v < NV; ++v) u[dd + (size_t)v * ncell] = val[v];
+}
+
+// ---------------------------------------------------------------------------
+// GLM psi: artificial diffusion (3_6/ModDiffusion.f90:9-150 applies to every
+// variable, psi included) into psi_out = psi + dt/2 R_psi, the same formulas
+// as k_diffusion with psi read from global memory; wave speeds from u.
+template <class T>
+__global__ void __launch_bounds__(256) k_psi_diffusion(const T* u, const T* psi, T* psi_out, Geometry g,
+                                                       StepScalars* sc, StepDims d) {
+    const int nint = d.ni * d.nj * d.nk;
+    const int b = blockIdx.y;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nint) return;
+    const int ii = q % d.ni + 2, jj = (q / d.ni) % d.nj + 2, kp = q / (d.ni * d.nj) + 2;
+    const size_t pl = (size_t)d.nip * d.njp;
+    const size_t c0 = (size_t)b * d.ncell + (size_t)kp * pl + (size_t)jj * d.nip + ii;
+    const T* Gi = gi_ptr<T>(g) + (size_t)b * GI_COUNT * d.nip;
+    const T* Gj = gj_ptr<T>(g) + (size_t)b * GJ_COUNT * d.njp;
+    const T* Gs = gs_ptr<T>(g) + (size_t)b * GS_COUNT;
+    const T* GCS = Gi + GI_CS * d.nip;
+    const T rc = Gi[GI_R * d.nip + ii];
+    const T den[3] = {Gs[GS_DXI], Gs[GS_DXJ] * rc, Gs[GS_DXK] * rc * Gj[GJ_SIN * d.njp + jj]};
+    const size_t strides[3] = {1, (size_t)d.nip, pl};
+    T R = T(0);
+#pragma unroll
+    for (int dir = 0; dir < 3; ++dir) {
+        const size_t s = strides[dir];
+        const T* vd = u + (size_t)b * NV * d.ncell + (size_t)(V_VR + dir) * d.ncell + (c0 - (size_t)b * d.ncell);
+        auto at = [&](int m) -> T { return psi[(ptrdiff_t)c0 + (ptrdiff_t)m * (ptrdiff_t)s]; };
+        const T csm = dir == 0 ? GCS[ii - 1] : GCS[ii];
+        const T cs0 = GCS[ii];
+        const T csp = dir == 0 ? GCS[ii + 1] : GCS[ii];
+        const T cm = fabs(vd[-(ptrdiff_t)s]) + csm, cz = fabs(vd[0]) + cs0, cp = fabs(vd[s]) + csp;
+        const T fm2 = at(-2), fm1 = at(-1), f0 = at(0), fp1 = at(1), fp2 = at(2);
+        const T dm1 = minmod(fm2, fm1, f0);
+        const T d0 = minmod(fm1, f0, fp1);
+        const T dp1 = minmod(f0, fp1, fp2);
+        T num = ((f0 - d0 * T(0.5)) - fm1) - dm1 * T(0.5);
+        T phi = fmax(T(0), T(1) + T(2) * (Pol<T>::ratio(num, f0 - fm1) - T(1)));
+        T fL = -(T(0.5) * phi * num);
+        fL = fL * (cz + cm) * T(0.5);
+        num = ((fp1 - dp1 * T(0.5)) - f0) - d0 * T(0.5);
+        phi = fmax(T(0), T(1) + T(2) * (Pol<T>::ratio(num, fp1 - f0) - T(1)));
+        T fR = -(T(0.5) * phi * num);
+        fR = fR * (cp + cz) * T(0.5);
+        R = R + (fL - fR) / den[dir];
+    }
+    const T p0 = psi[c0];
+    T o;
+    if constexpr (Pol<T>::exact) o = (T)((double)p0 + (0.5 * sc->dt) * (double)R);
+    else o = fmaf(sc->dt_half_f, (float)R, (float)p0);
+    psi_out[c0] = o;
+}
+
+// GLM psi ghost fill with the state's ghost lists (psi is a scalar: no
+// rotation). List offsets address var 0 of the [b][NV][cell] state; psi's
+// array is [b][cell].
+__device__ __forceinline__ size_t psi_off(size_t off, int ncell) {
+    const size_t b = off / ((size_t)NV * ncell);
+    return off - b * (size_t)(NV - 1) * ncell;
+}
+template <class T>
+__global__ void __launch_bounds__(256) k_psi_ghost(T* psi, GhostLists L, int ncell, int nip, int pl) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t ncp = L.cp.n, nln = L.ln.n, nip_ = L.ip.n;
+    if (e < ncp) {
+        psi[psi_off(L.cp.dst[e], ncell)] = psi[psi_off(L.cp.src[e], ncell)];
+    } else if (e < ncp + nln) {
+        const int64_t q = e - ncp;
+        const T* f = psi + psi_off(L.ln.src[q], ncell);
+        const T w = (T)L.ln.w[q];
+        psi[psi_off(L.ln.dst[q], ncell)] = blend(f[0], f[L.ln.stride[q]], T(1) - w, w);
+    } else if (e < ncp + nln + nip_) {
+        const int64_t q = e - ncp - nln;
+        const T* f = psi + psi_off(L.ip.src[q], ncell);
+        T val;
+        if (!(L.ip.kind[q] & 1)) {
+            val = f[0];
+        } else {
+            T wi, wj, wk;
+            if constexpr (Pol<T>::exact) { wi = L.ip.w[3 * q]; wj = L.ip.w[3 * q + 1]; wk = L.ip.w[3 * q + 2]; }
+            else { wi = L.ip.wf[3 * q]; wj = L.ip.wf[3 * q + 1]; wk = L.ip.wf[3 * q + 2]; }
+            const T ui = T(1) - wi, uj = T(1) - wj, uk = T(1) - wk;
+            val = f[0] * ui * uj * uk + f[1] * wi * uj * uk + f[nip] * ui * wj * uk + f[pl] * ui * uj * wk +
+                  f[1 + nip] * wi * wj * uk + f[nip + pl] * ui * wj * wk + f[1 + pl] * wi * uj * wk +
+                  f[1 + nip + pl] * wi * wj * wk;
+        }
+        psi[psi_off(L.ip.dst[q], ncell)] = val;
+    }
 }
 
 }  // namespace impl

@@ -5,9 +5,16 @@
 
 namespace falcon {
 cudaError_t launch_stage_mixed(const StepDims& d, const Geometry& g, const float* in, const float* un, float* out,
-                               int8_t* lo, const PushTable& push, int stage, int bcw, StepScalars* sc, int heat, int kpar,
-                               cudaStream_t st) {
-    return impl::stage_any<float>(d, g, in, un, out, lo, push, stage, bcw, sc, heat, kpar, st);
+                               int8_t* lo, const PushTable& push, const PsiArgs& psi, int stage, int bcw, StepScalars* sc,
+                               int heat, int kpar, cudaStream_t st) {
+    return impl::stage_any<float>(d, g, in, un, out, lo, push, psi, stage, bcw, sc, heat, kpar, st);
+}
+cudaError_t launch_psi_diffusion_mixed(const StepDims& d, const Geometry& g, const float* u, const float* psi,
+                                       float* psi_out, StepScalars* sc, cudaStream_t st) {
+    return impl::psi_diffusion_any<float>(d, g, u, psi, psi_out, sc, st);
+}
+cudaError_t launch_psi_ghost_mixed(const StepDims& d, const GhostLists& gl, float* psi, cudaStream_t st) {
+    return impl::psi_ghost_any<float>(d, gl, psi, st);
 }
 cudaError_t launch_diffusion_mixed(const StepDims& d, const Geometry& g, float* u, int8_t* lo, StepScalars* sc,
                                    int kpar, cudaStream_t st) {

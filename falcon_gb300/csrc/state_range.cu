@@ -1,9 +1,10 @@
 // state_range.cu -- download a range of the state without allocating.
 //
-// falcon_download_state widens a MIXED (FP32) state through an FP64 device
-// staging buffer of the whole state, allocated on first use. The range
-// download here stages through one fixed array compiled into the library
-// instead, so it needs no cudaMalloc, no cudaFree and no host allocation.
+// falcon_download_state converts the device state (FP32 in MIXED mode, and
+// always without psi's plane when GLM is off) through an FP64 device staging
+// buffer of the whole host array, allocated on first use. The range download
+// here gathers through one fixed array compiled into the library instead, so
+// it needs no cudaMalloc, no cudaFree and no host allocation.
 //
 // The array is shared by every context on a device and keeps what the last
 // call wrote into it. Each call overwrites the part it reads back (the first
@@ -48,23 +49,19 @@ cudaError_t scratch_on_device(int dev, double** out) {
 
 size_t static_scratch_elems() { return FALCON_STATIC_SCRATCH_BYTES / sizeof(double); }
 
-// Copy U[first, first + count) (FP32 with its correction Ulo if mixed, else
-// FP64) to host u as FP64.
-// The caller has checked the range and count <= static_scratch_elems(), and
-// made `dev` current. Returns "" or the failing step.
-std::string download_range_static(int dev, cudaStream_t st, const void* U, const int8_t* Ulo, bool mixed,
-                                  size_t first, size_t count, double* u) {
+// Copy host-layout elements [first, first + count) ([b][9][cell], psi last)
+// of the device state (FP32 with its correction Ulo if mixed, else FP64) and
+// psi (P, nullptr: 0) to host u as FP64, through the static array. The caller
+// has checked the range and count <= static_scratch_elems(), and made `dev`
+// current. Returns "" or the failing step.
+std::string download_range_static(int dev, cudaStream_t st, const void* U, const int8_t* Ulo, const void* P,
+                                  bool mixed, size_t first, size_t count, size_t ncell, double* u) {
     if (count == 0) return "";
-    cudaError_t e;
-    if (mixed) {
-        double* ptr = nullptr;
-        e = scratch_on_device(dev, &ptr);
-        if (e != cudaSuccess) return std::string("static scratch address: ") + cudaGetErrorString(e);
-        e = launch_widen_state((const float*)U + first, Ulo ? Ulo + first : nullptr, ptr, (int64_t)count, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(u, ptr, count * sizeof(double), cudaMemcpyDeviceToHost, st);
-    } else {
-        e = cudaMemcpyAsync(u, (const double*)U + first, count * sizeof(double), cudaMemcpyDeviceToHost, st);
-    }
+    double* ptr = nullptr;
+    cudaError_t e = scratch_on_device(dev, &ptr);
+    if (e != cudaSuccess) return std::string("static scratch address: ") + cudaGetErrorString(e);
+    e = launch_gather_host(U, mixed ? Ulo : nullptr, P, mixed, (int64_t)first, (int64_t)count, (int64_t)ncell, ptr, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(u, ptr, count * sizeof(double), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return std::string("range download: ") + cudaGetErrorString(e);
     return "";

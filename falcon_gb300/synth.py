@@ -56,8 +56,12 @@ def polytrope_constants(r_lo, r_hi, poly_n=1.5, contrast=100.0, mu=0.6):
                 c_b=np.sqrt(GAMMA * p_b / rho_b))
 
 
-def initial_state(cfg, ranges, flags, seed=1001, amp=1e-4, b_frac=1e-3):
-    """State array (nblocks, 8, nkp, njp, nip) float64 for the shell workloads."""
+def initial_state(cfg, ranges, flags, seed=1001, amp=1e-4, b_frac=1e-3, psi_amp=0.0):
+    """State array (nblocks, 9, nkp, njp, nip) float64 for the shell workloads.
+
+    psi (index 8) is 0 unless psi_amp > 0, which puts a Gaussian of peak
+    psi_amp * B0 * c_b (B0 the base field, c_b the base sound speed) at the
+    entropy blob's centre, for runs with GLM cleaning."""
     t = cfg.tree
     ng = t.ng
     nb = ranges.shape[0]
@@ -72,7 +76,7 @@ def initial_state(cfg, ranges, flags, seed=1001, amp=1e-4, b_frac=1e-3):
     xc = np.array([rc * np.sin(tc) * np.cos(pcen), rc * np.sin(tc) * np.sin(pcen), rc * np.cos(tc)])
     cp_ = 2.5 * pc["R_gas"]
     B0 = b_frac * np.sqrt(pc["rho_b"]) * pc["c_b"]
-    u = np.zeros((nb, 8, t.nk + 2 * ng, t.nj + 2 * ng, t.ni + 2 * ng))
+    u = np.zeros((nb, 9, t.nk + 2 * ng, t.nj + 2 * ng, t.ni + 2 * ng))   # psi (index 8) starts at 0
     for b in range(nb):
         xi = cell_centres(ranges[b, 0], t.ni, ng)
         xj = cell_centres(ranges[b, 1], t.nj, ng)
@@ -91,4 +95,6 @@ def initial_state(cfg, ranges, flags, seed=1001, amp=1e-4, b_frac=1e-3):
         if not yin:
             br, bt, bp = vec_conv(Ry, Ty, Py, br, bt, bp)
         u[b, 4], u[b, 5], u[b, 6] = br, bt, bp
+        if psi_amp:
+            u[b, 8] = psi_amp * B0 * pc["c_b"] * np.exp(-d2 / (2 * sig * sig))
     return u

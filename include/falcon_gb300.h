@@ -15,8 +15,11 @@
  *     of a context runs on one CUDA stream owned by the context.
  *   - Block arrays use the reference's Fortran layout: primitive(i,j,k,var)
  *     with bounds (-ng+1:ni+ng, -ng+1:nj+ng, -ng+1:nk+ng, 1:nvar), i fastest
- *     (3_6/ModBlock.f90:275-277). Variables are rho1, vr, vt, vp, br, bt, bp, s1
- *     (3_6/ModBlock.f90:153-162; psi is not stored, see falcon_physics).
+ *     (3_6/ModBlock.f90:275-277). Variables are rho1, vr, vt, vp, br, bt, bp, s1,
+ *     psi (3_6/ModBlock.f90:153-163): FALCON_NVAR = 9, as the reference's MHD
+ *     block. psi is evolved only with divb_option = 1 (GLM cleaning); with 0 it
+ *     is not stored on the device, must be 0 on upload and downloads as 0,
+ *     which is what the reference keeps for a psi that starts at 0.
  *
  * The entry points replace these reference interfaces:
  *   falcon_create ........... YinYangTree_InitTree/ModAMR_set_grid/YinYangTree_SetAll
@@ -64,7 +67,7 @@ extern "C" {
 #define FALCON_PREC_MIXED  1
 
 #define FALCON_MAX_AMR 16
-#define FALCON_NVAR 8
+#define FALCON_NVAR 9
 /* number of 1D radial background profiles per block (see falcon_get_background) */
 #define FALCON_NPROF 9
 
@@ -88,7 +91,9 @@ typedef struct falcon_tree_spec {
 /* Physics switches of the Dynamo equations (3_6/ModEquation.f90:24-37). */
 typedef struct falcon_physics {
     int32_t if_involve_B;            /* iEquation=1 with if_involve_B */
-    int32_t divb_option;             /* only 0 is supported (psi is not stored) */
+    int32_t divb_option;             /* 0: none; 1: GLM cleaning (3_6/ModDivB.f90:13-38); 2: the
+                                        reference's 'DivBSource', parsed (3_6/ModReadParameters.f90:
+                                        250-258) but never acted on, so it steps as 0 */
     double  cfl;                     /* #TIMESTEPPING CFL */
     double  heating_ratio;           /* Artificial_heating_ratio */
 } falcon_physics;
@@ -159,8 +164,8 @@ int  falcon_download_state(falcon_ctx* ctx, double* u);
  * no counterpart in the reference, whose state is resident in host memory.
  *
  * Who needs it: in MIXED mode falcon_download_state stages through an FP64
- * device buffer of the whole state (twice the FP32 state), allocated on its
- * first call. A caller whose state fills most of HBM has no room for that
+ * device buffer of the whole host array (2.25x the FP32 state), allocated on
+ * its first call. A caller whose state fills most of HBM has no room for that
  * buffer, and a caller that fixes its device footprint before the run (a
  * memory pool sized at start-up, a job that must not let a library grow its
  * memory mid-run, where cudaMalloc/cudaFree would also synchronise the whole
@@ -169,9 +174,10 @@ int  falcon_download_state(falcon_ctx* ctx, double* u);
  * library instead, so count is limited to FALCON_STATIC_SCRATCH_BYTES / 8
  * elements; larger counts, or a range past the end of the state, return
  * FALCON_ERR_INVALID_ARG without touching u. Download a whole state as a
- * sequence of ranges. In FP64 mode the range is copied directly.
+ * sequence of ranges; ranges count elements of the host layout
+ * ([block][FALCON_NVAR][cell]), gathered from the device state on the GPU.
  *
- * The first MIXED-mode call on each device sets up the array's address
+ * The first call on each device sets up the array's address
  * (cudaGetSymbolAddress; it may load the library's device code): make that
  * first call before any stream capture on the device. Every context on a
  * device shares the one array, which keeps the last call's data; each call

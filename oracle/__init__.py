@@ -10,6 +10,8 @@ import subprocess
 
 import numpy as np
 
+NVAR = 9   # variables of a block array (rho1 .. s1, psi), as FALCON_NVAR
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "build", "liboracle.so")
 _lib = None
@@ -67,7 +69,7 @@ class Oracle:
         self.L.orc_num_blocks(C.c_void_p(self.h), C.byref(nb), C.byref(ny))
         self.nblocks, self.nblocks_yin = nb.value, ny.value
         t = cfg.tree
-        self.shape = (self.nblocks, 8, t.nk + 2 * t.ng, t.nj + 2 * t.ng, t.ni + 2 * t.ng)
+        self.shape = (self.nblocks, NVAR, t.nk + 2 * t.ng, t.nj + 2 * t.ng, t.ni + 2 * t.ng)
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -143,14 +145,14 @@ class Oracle:
     def block_rhs(self, b, p):
         t = self.cfg.tree
         p = np.ascontiguousarray(p, dtype=np.float64)
-        R = np.zeros((8, t.nk, t.nj, t.ni))
+        R = np.zeros((NVAR, t.nk, t.nj, t.ni))
         self.L.orc_block_rhs(self.hp, C.c_int32(b), _ptr(p), _ptr(R))
         return R
 
     def block_diffusion(self, b, p):
         t = self.cfg.tree
         p = np.ascontiguousarray(p, dtype=np.float64)
-        R = np.zeros((8, t.nk, t.nj, t.ni))
+        R = np.zeros((NVAR, t.nk, t.nj, t.ni))
         self.L.orc_block_diffusion(self.hp, C.c_int32(b), _ptr(p), _ptr(R))
         return R
 

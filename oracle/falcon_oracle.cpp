@@ -25,8 +25,10 @@
 //     children with YinYangTree_Divide's own formula, N not limited to 2;
 //   - the background is a polytrope served through the get_vars interface
 //     (3_6/ModStratification_new.f90:352-384) instead of the FreeEOS tables;
-//   - psi (variable 9) is not stored: with DivB_option=0 and psi=0 initially
-//     it stays exactly 0 (its RHS is only ever the diffusion of a zero field).
+//   - psi (variable 9) is stored as in the reference's MHD block; with
+//     DivB_option=0 its RHS is set to 0 each stage (the reference leaves the
+//     previous diffusion pass's value there, which is 0 for a psi that starts
+//     at 0, the only psi the GPU accepts with DivB_option=0).
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -51,7 +53,7 @@ static const double m_p = (double)1.67262192369e-24f;
 static const double gamma_ideal_gas = (double)(5.0f / 3.0f);
 
 static const int NPROF = FALCON_NPROF;
-enum { RHO1 = 0, VR = 1, VT = 2, VP = 3, BR = 4, BT = 5, BP = 6, S1 = 7 };
+enum { RHO1 = 0, VR = 1, VT = 2, VP = 3, BR = 4, BT = 5, BP = 6, S1 = 7, PSI = 8 };
 
 // ---- background: polytrope through the get_vars interface ----------------
 struct Background {
@@ -310,6 +312,7 @@ struct Oracle {
     void exchange(bool rk);
     void boundary(Block& b, std::vector<double>& p);
     void equation(Block& b, const std::vector<double>& p);
+    void glm(Block& b, const std::vector<double>& p);
     void diffusion(Block& b, const std::vector<double>& p);
     void wave_speed(Block& b);
     double timestep();
@@ -811,6 +814,34 @@ void Oracle::equation(Block& b, const std::vector<double>& p) {
         op.curl(e1, e2, e3, c1, c2, c3);
         for (int q = 0; q < nint; ++q) { Rv(BR, q) = c1[q]; Rv(BT, q) = c2[q]; Rv(BP, q) = c3[q]; }
     }
+    for (int q = 0; q < nint; ++q) Rv(PSI, q) = 0.0;
+    if (withB && cfg.phys.divb_option == 1) glm(b, p);
+}
+
+void Oracle::glm(Block& b, const std::vector<double>& p) {
+    // ModDivB_GLM (3_6/ModDivB.f90:13-38): dB/dt += -grad(psi);
+    // dpsi/dt = -v_wave^2 div(B) - v_wave/h_LLL psi, v_wave from the step start
+    Ops op(*this, b);
+    const int nint = ni * nj * nk;
+    auto Rv = [&](int v, int q) -> double& { return b.R[(size_t)v * nint + q]; };
+    Arr br = op.comp(p, BR), bt = op.comp(p, BT), bp = op.comp(p, BP), psi = op.comp(p, PSI);
+    Arr dvb = op.div(br, bt, bp);
+    // ModSpherical_Grad_f (3_6/ModSpherical.f90:201-239)
+    Arr g1 = op.D(psi, 1), g2 = op.D(psi, 2), g3 = op.D(psi, 3);
+    for (int k = 1; k <= nk; ++k)
+        for (int j = 1; j <= nj; ++j)
+            for (int i = 1; i <= ni; ++i) {
+                const int q = iidx(i, j, k);
+                const double rinv = 1. / op.rr(i), sinv = 1. / std::sin(op.tt(j));
+                double G2 = g2[q] * rinv;
+                double G3 = g3[q] * rinv;
+                G3 = G3 * sinv;
+                Rv(BR, q) = Rv(BR, q) - g1[q];
+                Rv(BT, q) = Rv(BT, q) - G2;
+                Rv(BP, q) = Rv(BP, q) - G3;
+                const double w = b.vwave[q];
+                Rv(PSI, q) = -(w * w * dvb[q]) - w / b.h[q] * psi[idx(i, j, k)];
+            }
 }
 
 // ModLinReconstruct_minmod one value (3_6/ModLinReconstruct.f90:5-49)

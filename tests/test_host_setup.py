@@ -77,6 +77,12 @@ def test_invalid_configs_fail_loudly():
         fg.Falcon(config.tiny(device=-1, cfl=-1.0))
     with pytest.raises(fg.FalconError):
         fg.Falcon(config.tiny(device=-1, if_involve_B=0))
+    with pytest.raises(fg.FalconError):
+        fg.Falcon(config.tiny(device=-1, divb_option=3))
+    with pytest.raises(fg.FalconError):
+        fg.Falcon(config.tiny(device=-1, divb_option=1, if_involve_B=0))
+    for d in (1, 2):
+        fg.Falcon(config.tiny(device=-1, divb_option=d)).close()
 
 
 def test_device_calls_without_device_are_errors():

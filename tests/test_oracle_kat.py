@@ -164,3 +164,36 @@ def test_step_is_deterministic_and_finite():
     a, b = o1.get_state(), o2.get_state()
     assert np.isfinite(a).all()
     assert np.array_equal(a, b)
+
+
+def test_glm_stage_is_linear_damping_of_psi():
+    """GLM (3_6/ModDivB.f90:13-38) with v = B = 0: the first RK stage gives
+    psi_rk = psi (1 - dt v_wave / (4 h_LLL)) cell by cell (0 < factor < 1),
+    B_rk = -dt grad(psi) / 4, and the whole stage is linear in psi: doubling
+    psi doubles psi_rk and B_rk bit for bit. With divb_option = 0 psi and B
+    stay 0."""
+    def run(divb, scale):
+        cfg = config.tiny(divb_option=divb)
+        o = oracle.Oracle(cfg)
+        u = synth.initial_state(cfg, o.block_ranges(), o.block_flags(), seed=7, psi_amp=1e-3)
+        u[:, 1:7] = 0.0          # v = B = 0
+        psi = u[:, 8]
+        psi[np.abs(psi) < 1e-30 * np.abs(psi).max()] = 0.0   # no underflow in the tails
+        u[:, 8] = psi * scale
+        o.set_state(u)
+        o.exchange()
+        o.phase(0)
+        o.phase(1)
+        return u, o.get_stage_state()
+    u1, r1 = run(1, 1.0)
+    u2, r2 = run(1, 2.0)
+    inner = (slice(None), slice(None), slice(2, -2), slice(2, -2), slice(2, -2))
+    p0, p1 = u1[inner][:, 8], r1[inner][:, 8]
+    assert np.abs(p0).max() > 0
+    f = p1[p0 != 0] / p0[p0 != 0]
+    assert (f > 0).all() and (f < 1).all()
+    assert np.abs(r1[inner][:, 4:7]).max() > 0
+    assert np.array_equal(2 * r1[:, 4:7], r2[:, 4:7])
+    assert np.array_equal(2 * r1[:, 8], r2[:, 8])
+    _, r0 = run(0, 1.0)
+    assert not np.abs(r0[inner][:, 4:7]).any()
