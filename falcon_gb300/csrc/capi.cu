@@ -150,9 +150,9 @@ cudaError_t cfl(falcon_ctx* ctx) {
 // GLM psi through a stage: read psi_in (global memory, so never the array
 // being written), write P2, then copy to the stage array (RK's psi) for
 // stages 1-3; stage 4 writes u^{n+1}'s psi in place of u^n's cell by cell.
-PsiArgs psi_args(const falcon_ctx* ctx, int s) {
-    if (!ctx->P) return PsiArgs{nullptr, nullptr, nullptr};
-    return PsiArgs{s == 1 ? ctx->P : ctx->Prk, ctx->P, s == 4 ? ctx->P : ctx->P2};
+DivBArgs psi_args(const falcon_ctx* ctx, int s) {
+    if (!ctx->P) return DivBArgs{nullptr, nullptr, nullptr, ctx->cfg.phys.divb_option == 2 ? 2 : 0};
+    return DivBArgs{s == 1 ? ctx->P : ctx->Prk, ctx->P, s == 4 ? ctx->P : ctx->P2, 1};
 }
 cudaError_t psi_after_stage(falcon_ctx* ctx, int s) {
     if (!ctx->P) return cudaSuccess;
@@ -170,7 +170,7 @@ cudaError_t psi_after_stage(falcon_ctx* ctx, int s) {
 
 // Stage s from `in` into `out` (ModAdvance.f90:59-97), GLM terms included.
 cudaError_t stage(falcon_ctx* ctx, int s, void* in, void* out, const PushTable& push) {
-    const PsiArgs ps = psi_args(ctx, s);
+    const DivBArgs ps = psi_args(ctx, s);
     cudaError_t e = timed(ctx, KN_STAGE, [&] {
         return ctx->mixed()
                    ? launch_stage_mixed(ctx->dims, ctx->geom(), (const float*)in, (const float*)ctx->U, (float*)out,
@@ -259,10 +259,10 @@ int autotune(falcon_ctx* ctx) {
                 cudaError_t e;
                 if (which == 0)
                     e = ctx->mixed() ? launch_stage_mixed(ctx->dims, ctx->geom(), (const float*)ctx->RK, (const float*)ctx->U,
-                                                          (float*)ctx->R2, nullptr, ctx->push, PsiArgs{nullptr, nullptr, nullptr},
+                                                          (float*)ctx->R2, nullptr, ctx->push, psi_args(ctx, 2),
                                                           2, 1, ctx->sc, 1, kp, ctx->st)
                                      : launch_stage_fp64(ctx->dims, ctx->geom(), (const double*)ctx->RK, (const double*)ctx->U,
-                                                         (double*)ctx->RK, PsiArgs{nullptr, nullptr, nullptr}, 2, 1,
+                                                         (double*)ctx->RK, psi_args(ctx, 2), 2, 1,
                                                          ctx->sc, 1, kp, ctx->st);
                 else
                     e = ctx->mixed() ? launch_diffusion_mixed(ctx->dims, ctx->geom(), (float*)ctx->RK, nullptr, ctx->sc, kp,

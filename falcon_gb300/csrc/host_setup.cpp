@@ -204,9 +204,9 @@ std::string Grid::build(const falcon_config& c, bool with_ghosts) {
         return "block sizes must be >= 4 and ng must be 2 (fourth-order stencils)";
     (void)with_ghosts;
     if (t.ni > 32 || t.nj > 32 || t.nk > 32) return "block sizes above 32 are not supported";
-    // 2 (DivBSource) is parsed by the reference but acted on nowhere: it runs as 0
-    if (c.phys.divb_option < 0 || c.phys.divb_option > 2) return "divb_option must be 0 (none), 1 (GLM) or 2";
-    if (c.phys.divb_option == 1 && !c.phys.if_involve_B) return "divb_option 1 (GLM) needs if_involve_B = 1";
+    if (c.phys.divb_option < 0 || c.phys.divb_option > 2)
+        return "divb_option must be 0 (none), 1 (GLM) or 2 (Powell source term)";
+    if (c.phys.divb_option != 0 && !c.phys.if_involve_B) return "divb_option 1 or 2 needs if_involve_B = 1";
     if (with_ghosts && !c.phys.if_involve_B) return "if_involve_B must be 1 (the MHD block layout with B active)";
     if (t.radial_option < 1 || t.radial_option > 3) return "radial_option must be 1, 2 or 3";
     if (t.n_amr < 0 || t.n_amr > FALCON_MAX_AMR) return "n_amr out of range";

@@ -157,13 +157,16 @@ struct StepDims {
     int nblocks, ni, nj, nk, nip, njp, nkp, ncell;
 };
 
-// GLM divergence cleaning (3_6/ModDivB.f90:13-38): psi arrays [b][cell] of the
-// stage input, of u^n and of the stage output (in == nullptr: GLM off). psi is
-// read from global memory (not the shared-memory ring), so out != in.
-struct PsiArgs {
+// div-B control of a stage (DivB_option): mode 0 none; 1 GLM cleaning
+// (3_6/ModDivB.f90:13-38) with psi arrays [b][cell] of the stage input, of u^n
+// and of the stage output -- psi is read from global memory (not the
+// shared-memory ring), so out != in; 2 the Powell source term -(div B) v on
+// the induction equation (3_5/ModEquation.f90:169-176), no psi.
+struct DivBArgs {
     const void* in;
     const void* un;
     void* out;
+    int mode;
 };
 
 // ---- launchers (defined in mhd_fp64.cu / mhd_mixed.cu) --------------------
@@ -172,7 +175,7 @@ struct PsiArgs {
 // (3_6/ModBoundary.f90:10-55); the diffusion pass later reads those of u^n
 // (3_6/ModAdvance.f90:101-108)
 cudaError_t launch_stage_fp64(const StepDims& d, const Geometry& g, const double* in, const double* un,
-                              double* out, const PsiArgs& psi, int stage, int bc_writeback, StepScalars* sc,
+                              double* out, const DivBArgs& psi, int stage, int bc_writeback, StepScalars* sc,
                               int heat_on, int kpar, cudaStream_t st);
 // GLM: psi's artificial diffusion (into psi_out) and psi's ghost fill
 cudaError_t launch_psi_diffusion_fp64(const StepDims& d, const Geometry& g, const double* u, const double* psi,
@@ -189,7 +192,7 @@ cudaError_t launch_ghost_fp64(const StepDims& d, const GhostLists& gl, double* u
 // push: faces written into `out` by the stage kernel (tgt == nullptr: none);
 // pushing needs out != in, since a target block may still be reading `in`.
 cudaError_t launch_stage_mixed(const StepDims& d, const Geometry& g, const float* in, const float* un,
-                               float* out, int8_t* lo, const PushTable& push, const PsiArgs& psi, int stage,
+                               float* out, int8_t* lo, const PushTable& push, const DivBArgs& psi, int stage,
                                int bc_writeback, StepScalars* sc, int heat_on, int kpar, cudaStream_t st);
 cudaError_t launch_psi_diffusion_mixed(const StepDims& d, const Geometry& g, const float* u, const float* psi,
                                        float* psi_out, StepScalars* sc, cudaStream_t st);

@@ -21,20 +21,37 @@ template <> struct Cand<float> {
     static constexpr int k16[3] = {1, 2, 4};
 };
 
-template <class T, int N, int KP>
-cudaError_t stage_n(const StepDims& d, const Geometry& g, const T* in, const T* un, T* out, int8_t* lo,
-                    const PushTable& push, const PsiArgs& psi, int stage, int bcw, StepScalars* sc, int heat,
-                    cudaStream_t st) {
+template <class T, int N, int KP, int DIVB>
+cudaError_t stage_nd(const StepDims& d, const Geometry& g, const T* in, const T* un, T* out, int8_t* lo,
+                     const PushTable& push, const DivBArgs& psi, int stage, int bcw, StepScalars* sc, int heat,
+                     cudaStream_t st) {
     using S = Shape<T, N, N, N, KP>;
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_stage<T, N, N, N, KP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)S::smem_stage);
+        cudaError_t e = cudaFuncSetAttribute(k_stage<T, N, N, N, KP, DIVB>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::smem_stage);
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    k_stage<T, N, N, N, KP><<<d.nblocks, S::NT, S::smem_stage, st>>>(in, un, out, lo, push, psi, g, sc, stage, bcw, heat);
+    k_stage<T, N, N, N, KP, DIVB>
+        <<<d.nblocks, S::NT, S::smem_stage, st>>>(in, un, out, lo, push, psi, g, sc, stage, bcw, heat);
     return cudaGetLastError();
+}
+
+// The div-B mode is a template parameter: the plain stage keeps its register
+// allocation free of the GLM/Powell terms.
+template <class T, int N, int KP>
+cudaError_t stage_n(const StepDims& d, const Geometry& g, const T* in, const T* un, T* out, int8_t* lo,
+                    const PushTable& push, const DivBArgs& psi, int stage, int bcw, StepScalars* sc, int heat,
+                    cudaStream_t st) {
+    switch (psi.mode) {
+    case 0: return stage_nd<T, N, KP, 0>(d, g, in, un, out, lo, push, psi, stage, bcw, sc, heat, st);
+    case 1:
+        if (!psi.in || !psi.un || !psi.out) return cudaErrorInvalidValue;
+        return stage_nd<T, N, KP, 1>(d, g, in, un, out, lo, push, psi, stage, bcw, sc, heat, st);
+    case 2: return stage_nd<T, N, KP, 2>(d, g, in, un, out, lo, push, psi, stage, bcw, sc, heat, st);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 template <class T, int N, int KP>
@@ -53,7 +70,7 @@ cudaError_t diff_n(const StepDims& d, const Geometry& g, T* u, int8_t* lo, StepS
 
 template <class T>
 cudaError_t stage_any(const StepDims& d, const Geometry& g, const T* in, const T* un, T* out, int8_t* lo,
-                      const PushTable& push, const PsiArgs& psi, int stage, int bcw, StepScalars* sc, int heat, int kpar,
+                      const PushTable& push, const DivBArgs& psi, int stage, int bcw, StepScalars* sc, int heat, int kpar,
                       cudaStream_t st) {
 #define FALCON_STAGE_CASE(N, K) \
     if (d.ni == N && kpar == K) return stage_n<T, N, K>(d, g, in, un, out, lo, push, psi, stage, bcw, sc, heat, st);

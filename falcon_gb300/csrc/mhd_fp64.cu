@@ -10,7 +10,7 @@ using impl::cfl_any;
 using impl::ghost_any;
 
 cudaError_t launch_stage_fp64(const StepDims& d, const Geometry& g, const double* in, const double* un, double* out,
-                              const PsiArgs& psi, int stage, int bcw, StepScalars* sc, int heat, int kpar,
+                              const DivBArgs& psi, int stage, int bcw, StepScalars* sc, int heat, int kpar,
                               cudaStream_t st) {
     return stage_any<double>(d, g, in, un, out, nullptr, PushTable{}, psi, stage, bcw, sc, heat, kpar, st);
 }

@@ -111,6 +111,13 @@ struct Shape {
     static constexpr size_t off_gs = off_gj + (size_t)GJ_COUNT * NJP * sizeof(T);
     static constexpr size_t smem_stage = off_gs + GS_COUNT * sizeof(T);
     static constexpr size_t smem_diff = smem_stage;
+    // FP32 stage: as many CTAs per SM as the shared memory holds (228 KB per
+    // SM, 1 KB reserved per CTA), so the register allocation must fit them
+    // too (at least 32 registers a thread). FP64 keeps the compiler's choice.
+    static constexpr int by_smem = (int)(233472 / (smem_stage + 1024));
+    static constexpr int reg_cap = 2048 / NT;
+    static constexpr int min_blocks =
+        sizeof(T) != 4 || by_smem < 2 ? 1 : (by_smem < reg_cap ? by_smem : (reg_cap < 1 ? 1 : reg_cap));
 };
 
 // Thread 0: bulk-copy planes kp in [lo,hi) of all variables of the block into
@@ -249,9 +256,9 @@ __device__ __forceinline__ void cell_of_thread(int tid, int& i, int& j, int& kq)
 // ---------------------------------------------------------------------------
 // One RK stage of one block: boundary -> RHS (3_6/ModEquation.f90:24-162) ->
 // u_out = u^n + dt*R/(5-s) (3_6/ModAdvance.f90:87-93).
-template <class T, int NI, int NJ, int NK, int KPAR>
-__global__ void __launch_bounds__(NI* NJ* KPAR)
-k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, PsiArgs psi, Geometry g, StepScalars* sc,
+template <class T, int NI, int NJ, int NK, int KPAR, int DIVB>
+__global__ void __launch_bounds__(NI* NJ* KPAR, (Shape<T, NI, NJ, NK, KPAR>::min_blocks))
+k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, DivBArgs psi, Geometry g, StepScalars* sc,
         int stage, int bc_writeback, int heat_on) {
     using S = Shape<T, NI, NJ, NK, KPAR>;
     constexpr int NIP = S::NIP, PL = S::PL, W = S::W, WP = S::WP, NCELL = S::NCELL;
@@ -436,10 +443,27 @@ k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, PsiArgs p
             RBr = q1; RBt = q2; RBp = q3;
         }
 
-        // GLM divergence cleaning (3_6/ModDivB.f90:13-38), after the equation
-        // terms as 3_6/ModAdvance.f90:82-84 orders it: dB += -grad(psi);
-        // dpsi = -v_wave^2 div(B) - v_wave/h_LLL psi, v_wave from u^n
-        if (psi.in != nullptr) {
+        // div-B control. GLM cleaning (3_6/ModDivB.f90:13-38), after the
+        // equation terms as 3_6/ModAdvance.f90:82-84 orders it: dB += -grad(psi);
+        // dpsi = -v_wave^2 div(B) - v_wave/h_LLL psi, v_wave from u^n. Powell
+        // (3_5/ModEquation.f90:169-176): dB += -(div B) v.
+        T divB = T(0);
+        if constexpr (DIVB != 0) {
+            // ModSpherical_div of B (3_6/ModSpherical.f90:104-159)
+            T dB = D(c1, [&](int m) { return A(V_BR, m, 0, 0) * GR2[ii + m]; });
+            dB = dB * r2inv;
+            T e23 = D(c2, [&](int m) { return A(V_BT, 0, m, 0) * GSIN[jj + m]; });
+            e23 = e23 + D(c3, [&](int m) { return A(V_BP, 0, 0, m); });
+            e23 = e23 * sinv;
+            e23 = e23 * rinv;
+            divB = dB + e23;
+        }
+        if constexpr (DIVB == 2) {
+            RBr = RBr - divB * vr;
+            RBt = RBt - divB * vt;
+            RBp = RBp - divB * vp;
+        }
+        if constexpr (DIVB == 1) {
             const T* P = static_cast<const T*>(psi.in) + (size_t)b * NCELL + (size_t)kp * PL + jj * NIP + ii;
             auto Q = [&](int di, int dj, int dk) -> T { return P[(size_t)dk * PL + dj * NIP + di]; };
             // ModSpherical_Grad_f (3_6/ModSpherical.f90:201-239)
@@ -452,14 +476,6 @@ k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, PsiArgs p
             RBr = RBr - g1;
             RBt = RBt - g2;
             RBp = RBp - g3;
-            // ModSpherical_div of B (3_6/ModSpherical.f90:104-159)
-            T dB = D(c1, [&](int m) { return A(V_BR, m, 0, 0) * GR2[ii + m]; });
-            dB = dB * r2inv;
-            T e23 = D(c2, [&](int m) { return A(V_BT, 0, m, 0) * GSIN[jj + m]; });
-            e23 = e23 + D(c3, [&](int m) { return A(V_BP, 0, 0, m); });
-            e23 = e23 * sinv;
-            e23 = e23 * rinv;
-            const T divB = dB + e23;
             // ModWaveSpeed_Dynamo (3_6/ModWaveSpeed.f90:8-27) and h_LLL
             // (3_6/ModBlock.f90:416-425) at this cell, as the CFL pass forms them
             T w = gi[GI_CS * NIP + ii] +

@@ -5,7 +5,7 @@
 
 namespace falcon {
 cudaError_t launch_stage_mixed(const StepDims& d, const Geometry& g, const float* in, const float* un, float* out,
-                               int8_t* lo, const PushTable& push, const PsiArgs& psi, int stage, int bcw, StepScalars* sc,
+                               int8_t* lo, const PushTable& push, const DivBArgs& psi, int stage, int bcw, StepScalars* sc,
                                int heat, int kpar, cudaStream_t st) {
     return impl::stage_any<float>(d, g, in, un, out, lo, push, psi, stage, bcw, sc, heat, kpar, st);
 }

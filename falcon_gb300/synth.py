@@ -56,12 +56,14 @@ def polytrope_constants(r_lo, r_hi, poly_n=1.5, contrast=100.0, mu=0.6):
                 c_b=np.sqrt(GAMMA * p_b / rho_b))
 
 
-def initial_state(cfg, ranges, flags, seed=1001, amp=1e-4, b_frac=1e-3, psi_amp=0.0):
+def initial_state(cfg, ranges, flags, seed=1001, amp=1e-4, b_frac=1e-3, psi_amp=0.0, b_div_amp=0.0):
     """State array (nblocks, 9, nkp, njp, nip) float64 for the shell workloads.
 
     psi (index 8) is 0 unless psi_amp > 0, which puts a Gaussian of peak
     psi_amp * B0 * c_b (B0 the base field, c_b the base sound speed) at the
-    entropy blob's centre, for runs with GLM cleaning."""
+    entropy blob's centre, for runs with GLM cleaning. b_div_amp > 0 adds a
+    Gaussian of peak b_div_amp * B0 there to B_r alone, a field with
+    divergence (B_r is the same in both panels' coordinates)."""
     t = cfg.tree
     ng = t.ng
     nb = ranges.shape[0]
@@ -95,6 +97,8 @@ def initial_state(cfg, ranges, flags, seed=1001, amp=1e-4, b_frac=1e-3, psi_amp=
         if not yin:
             br, bt, bp = vec_conv(Ry, Ty, Py, br, bt, bp)
         u[b, 4], u[b, 5], u[b, 6] = br, bt, bp
+        if b_div_amp:
+            u[b, 4] += b_div_amp * B0 * np.exp(-d2 / (2 * sig * sig))
         if psi_amp:
             u[b, 8] = psi_amp * B0 * pc["c_b"] * np.exp(-d2 / (2 * sig * sig))
     return u

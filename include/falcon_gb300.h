@@ -91,9 +91,10 @@ typedef struct falcon_tree_spec {
 /* Physics switches of the Dynamo equations (3_6/ModEquation.f90:24-37). */
 typedef struct falcon_physics {
     int32_t if_involve_B;            /* iEquation=1 with if_involve_B */
-    int32_t divb_option;             /* 0: none; 1: GLM cleaning (3_6/ModDivB.f90:13-38); 2: the
-                                        reference's 'DivBSource', parsed (3_6/ModReadParameters.f90:
-                                        250-258) but never acted on, so it steps as 0 */
+    int32_t divb_option;             /* DivB_option: 0 none; 1 GLM cleaning (3_6/ModDivB.f90:13-38);
+                                        2 Powell source term -(div B) v (3_5/ModEquation.f90:169-176;
+                                        3_6 declares 2 as Powell's term, ModParameters.f90:70, but its
+                                        ModAdvance applies only 1, so a 3_6 run with 2 steps as 0) */
     double  cfl;                     /* #TIMESTEPPING CFL */
     double  heating_ratio;           /* Artificial_heating_ratio */
 } falcon_physics;

@@ -313,6 +313,7 @@ struct Oracle {
     void boundary(Block& b, std::vector<double>& p);
     void equation(Block& b, const std::vector<double>& p);
     void glm(Block& b, const std::vector<double>& p);
+    void powell(Block& b, const std::vector<double>& p);
     void diffusion(Block& b, const std::vector<double>& p);
     void wave_speed(Block& b);
     double timestep();
@@ -816,6 +817,7 @@ void Oracle::equation(Block& b, const std::vector<double>& p) {
     }
     for (int q = 0; q < nint; ++q) Rv(PSI, q) = 0.0;
     if (withB && cfg.phys.divb_option == 1) glm(b, p);
+    if (withB && cfg.phys.divb_option == 2) powell(b, p);
 }
 
 void Oracle::glm(Block& b, const std::vector<double>& p) {
@@ -841,6 +843,22 @@ void Oracle::glm(Block& b, const std::vector<double>& p) {
                 Rv(BP, q) = Rv(BP, q) - G3;
                 const double w = b.vwave[q];
                 Rv(PSI, q) = -(w * w * dvb[q]) - w / b.h[q] * psi[idx(i, j, k)];
+            }
+}
+
+void Oracle::powell(Block& b, const std::vector<double>& p) {
+    // Powell source term of 3_5/ModEquation.f90:169-176: dB_i/dt += -(div B) v_i,
+    // with 3_6's ModSpherical_div; applied after the induction term
+    Ops op(*this, b);
+    const int nint = ni * nj * nk;
+    Arr dvb = op.div(op.comp(p, BR), op.comp(p, BT), op.comp(p, BP));
+    for (int k = 1; k <= nk; ++k)
+        for (int j = 1; j <= nj; ++j)
+            for (int i = 1; i <= ni; ++i) {
+                const int q = iidx(i, j, k), m = idx(i, j, k);
+                for (int c = 0; c < 3; ++c)
+                    b.R[(size_t)(BR + c) * nint + q] =
+                        b.R[(size_t)(BR + c) * nint + q] - dvb[q] * p[(size_t)(VR + c) * ncell + m];
             }
 }
 

@@ -191,12 +191,19 @@ def test_nan_in_state_is_reported_not_trapped():
     assert e.value.code == fg.ERR_NAN_DETECTED
 
 
-# ---- GLM divergence cleaning (divb_option = 1: psi evolved) ---------------
-def _glm_pair(mk, seed=1004):
-    cfg = mk(divb_option=1)
+# ---- div-B control: GLM cleaning (divb_option 1, psi evolved) and the ----
+# ---- Powell source term (divb_option 2) --------------------------------
+def _init_divb(cfg, ranges, flags, divb, seed):
+    if divb == 1:
+        return synth.initial_state(cfg, ranges, flags, seed=seed, psi_amp=1e-3)
+    return synth.initial_state(cfg, ranges, flags, seed=seed, b_div_amp=0.3)
+
+
+def _divb_pair(mk, divb, seed=1004):
+    cfg = mk(divb_option=divb)
     f = fg.Falcon(cfg)
-    o = oracle.Oracle(mk(divb_option=1))
-    u0 = synth.initial_state(cfg, o.block_ranges(), o.block_flags(), seed=seed, psi_amp=1e-3)
+    o = oracle.Oracle(mk(divb_option=divb))
+    u0 = _init_divb(cfg, o.block_ranges(), o.block_flags(), divb, seed)
     f.upload_state(u0)
     o.set_state(u0)
     for x in (f, o):
@@ -205,25 +212,28 @@ def _glm_pair(mk, seed=1004):
     return f, o
 
 
-def test_glm_phase_by_phase_bit_identical():
-    """GLM terms in each RK stage (-grad psi on B, the psi equation with the
-    step-start wave speed and h_LLL), psi's diffusion and psi's exchange: both
-    state buffers, psi included, identical to the oracle after every phase."""
-    f, o = _glm_pair(config.tiny)
+@pytest.mark.parametrize("divb", [1, 2])
+def test_divb_phase_by_phase_bit_identical(divb):
+    """GLM: the terms in each RK stage (-grad psi on B, the psi equation with
+    the step-start wave speed and h_LLL), psi's diffusion and exchange.
+    Powell: -(div B) v on B. Both state buffers, psi included, identical to
+    the oracle after every phase."""
+    f, o = _divb_pair(config.tiny, divb)
     names = ["cfl", "stage1", "stage2", "stage3", "stage4", "diffusion"]
     for ph in range(6):
         f.step_phase(ph)
         o.phase(ph)
         a, b = f.download_state(), o.get_state()
-        assert np.abs(b[:, 8]).max() > 0
+        assert (np.abs(b[:, 8]).max() > 0) == (divb == 1)
         assert np.array_equal(a, b), (names[ph], "u", relerr(a, b))
         if 1 <= ph <= 3:
             a, b = f.download_stage_state(), o.get_stage_state()
             assert np.array_equal(a, b), (names[ph], "u_rk", relerr(a, b))
 
 
-def test_glm_fp64_steps_bit_identical():
-    f, o = _glm_pair(config.tiny)
+@pytest.mark.parametrize("divb", [1, 2])
+def test_divb_fp64_steps_bit_identical(divb):
+    f, o = _divb_pair(config.tiny, divb)
     for _ in range(3):
         assert f.advance_rk4() == o.step()
         a, b = f.download_state(), o.get_state()
@@ -231,8 +241,9 @@ def test_glm_fp64_steps_bit_identical():
         assert np.array_equal(a, b), relerr(a, b)
 
 
-def test_glm_fp64_ten_steps_cfg1_within_1e12():
-    f, o = _glm_pair(config.shell_fp64_cpu)
+@pytest.mark.parametrize("divb", [1, 2])
+def test_divb_fp64_ten_steps_cfg1_within_1e12(divb):
+    f, o = _divb_pair(config.shell_fp64_cpu, divb)
     for s in range(10):
         dtf, dto = f.advance_rk4(), o.step()
         assert abs(dtf - dto) <= TOL_FP64 * dto
@@ -240,14 +251,15 @@ def test_glm_fp64_ten_steps_cfg1_within_1e12():
         assert (e <= TOL_FP64).all(), (s, dict(zip(config.VAR_NAMES, e)))
 
 
-def test_glm_mixed_vs_fp64_gpu_100_steps():
-    """The mixed path with GLM against the FP64 GPU path after 100 steps:
-    relative L2 <= 1e-6 for every variable, psi included (psi is driven by
-    the divergence of B formed from FP32 values)."""
-    mk64 = lambda: config.shell_fp64_cpu(divb_option=1)
-    mkmx = lambda: config.shell_fp64_cpu(divb_option=1, precision=config.PREC_MIXED)
+@pytest.mark.parametrize("divb", [1, 2])
+def test_divb_mixed_vs_fp64_gpu_100_steps(divb):
+    """The mixed path with GLM or Powell against the FP64 GPU path after 100
+    steps: relative L2 <= 1e-6 for every variable, psi included (psi is
+    driven by the divergence of B formed from FP32 values)."""
+    mk64 = lambda: config.shell_fp64_cpu(divb_option=divb)
+    mkmx = lambda: config.shell_fp64_cpu(divb_option=divb, precision=config.PREC_MIXED)
     a, b = fg.Falcon(mk64()), fg.Falcon(mkmx())
-    u0 = synth.initial_state(mk64(), a.block_ranges(), a.block_flags(), seed=1005, psi_amp=1e-3)
+    u0 = _init_divb(mk64(), a.block_ranges(), a.block_flags(), divb, 1005)
     for x in (a, b):
         x.upload_state(u0)
         x.exchange()
@@ -263,16 +275,17 @@ def test_glm_mixed_vs_fp64_gpu_100_steps():
     da = (ib - ia).transpose(1, 0, 2, 3, 4).reshape(nv, -1)
     ra = ia.transpose(1, 0, 2, 3, 4).reshape(nv, -1)
     l2 = np.sqrt((da ** 2).sum(1)) / np.sqrt((ra ** 2).sum(1)).clip(1e-300)
-    print("GLM mixed vs fp64 relative L2:", dict(zip(config.VAR_NAMES, l2)))
+    print("divb_option %d mixed vs fp64 relative L2:" % divb, dict(zip(config.VAR_NAMES, l2)))
     active = np.abs(ra).max(1) > 0
-    assert active[8]
+    assert active[8] == (divb == 1)
     assert (l2[active] <= TOL_MIXED).all(), dict(zip(config.VAR_NAMES, l2))
 
 
-def test_glm_mixed_step_matches_phase_sequence():
-    mk = lambda: config.shell_fp64_cpu(divb_option=1, precision=config.PREC_MIXED)
+@pytest.mark.parametrize("divb", [1, 2])
+def test_divb_mixed_step_matches_phase_sequence(divb):
+    mk = lambda: config.shell_fp64_cpu(divb_option=divb, precision=config.PREC_MIXED)
     a, b = fg.Falcon(mk()), fg.Falcon(mk())
-    u0 = synth.initial_state(mk(), a.block_ranges(), a.block_flags(), seed=1006, psi_amp=1e-3)
+    u0 = _init_divb(mk(), a.block_ranges(), a.block_flags(), divb, 1006)
     for x in (a, b):
         x.upload_state(u0)
         x.exchange()

@@ -197,3 +197,45 @@ def test_glm_stage_is_linear_damping_of_psi():
     assert np.array_equal(2 * r1[:, 8], r2[:, 8])
     _, r0 = run(0, 1.0)
     assert not np.abs(r0[inner][:, 4:7]).any()
+
+
+def test_powell_source_term_against_numpy():
+    """divb_option 2 adds -(div B) v to the induction equation
+    (3_5/ModEquation.f90:169-176) and nothing else: the oracle's block RHS with
+    and without it differ by that term, restated here in numpy with the
+    spherical divergence of 3_6/ModSpherical.f90:104-159 (FP32 1/12 stencil)."""
+    o0 = oracle.Oracle(config.tiny())
+    o2 = oracle.Oracle(config.tiny(divb_option=2))
+    cfg = config.tiny()
+    u = synth.initial_state(cfg, o0.block_ranges(), o0.block_flags(), seed=11)
+    rs = np.random.default_rng(3)
+    b = 7
+    p = u[b].copy()
+    bscale = np.abs(p[4:7]).max()
+    vscale = 1e-3 * bscale
+    p[4:7] += 0.1 * bscale * rs.standard_normal(p[4:7].shape)   # a field with divergence
+    p[1:4] = vscale * rs.standard_normal(p[1:4].shape)
+    R0, R2 = o0.block_rhs(b, p), o2.block_rhs(b, p)
+    others = [0, 1, 2, 3, 7, 8]
+    assert np.array_equal(R0[others], R2[others])
+    xi, xj, xk, d = o2.block_grid(b)
+    c = float(np.float32(1.0) / np.float32(12.0))
+    I = slice(2, -2)
+
+    def D(f, axis, dx):
+        n = f.shape[axis]
+        s = lambda o: np.take(f, np.arange(2 + o, n - 2 + o), axis=axis)
+        return (c / dx) * (((-s(2) + 8.0 * s(1)) - 8.0 * s(-1)) + s(-2))
+
+    r = xi[None, None, :]
+    st = np.sin(xj)[None, :, None]
+    br, bt, bp = p[4], p[5], p[6]
+    d1 = D(br * r * r, 2, d[0])[I, I, :] / (xi[2:-2] ** 2)[None, None, :]
+    d2 = D(bt * st, 1, d[1])[I, :, I]
+    d3 = D(bp, 0, d[2])[:, I, I]
+    divb = d1 + ((d2 + d3) / np.sin(xj[2:-2])[None, :, None]) / xi[2:-2][None, None, :]
+    v = p[1:4][:, I, I, I]
+    want = -divb[None] * v
+    got = R2[4:7] - R0[4:7]
+    assert np.abs(want).max() > 0
+    assert np.abs(got - want).max() <= 1e-9 * np.abs(want).max()
