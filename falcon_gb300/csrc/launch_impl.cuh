@@ -56,15 +56,15 @@ cudaError_t stage_n(const StepDims& d, const Geometry& g, const T* in, const T* 
 
 template <class T, int N, int KP>
 cudaError_t diff_n(const StepDims& d, const Geometry& g, T* u, int8_t* lo, StepScalars* sc, cudaStream_t st) {
-    using S = Shape<T, N, N, N, KP>;
+    using S = DShape<T, N, N, N, KP>;
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(k_diffusion<T, N, N, N, KP>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::smem_diff);
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::smem);
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    k_diffusion<T, N, N, N, KP><<<d.nblocks, S::NT, S::smem_diff, st>>>(u, lo, g, sc);
+    k_diffusion<T, N, N, N, KP><<<d.nblocks, S::NT, S::smem, st>>>(u, lo, g, sc);
     return cudaGetLastError();
 }
 
@@ -90,7 +90,8 @@ cudaError_t diff_any(const StepDims& d, const Geometry& g, T* u, int8_t* lo, Ste
     if (d.ni != d.nj || d.ni != d.nk) return cudaErrorInvalidValue;
     FALCON_DIFF_CASE(8, 2) FALCON_DIFF_CASE(8, 4)
     FALCON_DIFF_CASE(16, 1)
-    if constexpr (!Pol<T>::exact) { FALCON_DIFF_CASE(8, 8) FALCON_DIFF_CASE(16, 2) FALCON_DIFF_CASE(16, 4) }
+    // (16, 4) would need more than 227 KB of shared memory for its face arrays
+    if constexpr (!Pol<T>::exact) { FALCON_DIFF_CASE(8, 8) FALCON_DIFF_CASE(16, 2) }
 #undef FALCON_DIFF_CASE
     return cudaErrorInvalidValue;
 }

@@ -524,14 +524,67 @@ k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, DivBArgs 
 // ---------------------------------------------------------------------------
 // Artificial diffusion with h=2 (3_6/ModDiffusion.f90:9-150) and the update
 // u += 0.5*dt*R (3_6/ModAdvance.f90:101-108), in place.
+//
+// The reference evaluates, for every cell and direction, the limited fluxes
+// through its two faces, so every face flux (and the minmod slopes under it)
+// is formed twice. Here each face flux is formed once per chunk of KPAR
+// planes into shared memory: i and j faces of the chunk's planes, and the k
+// faces in a ring of KPAR+1 face planes (the last face of a chunk is the
+// first of the next). A flux is the same function of the same four values as
+// the reference's, so sharing it changes no bit. Then each cell sums
+// (F_left - F_right)/den over the three directions, in the reference's order.
 template <class T, int NI, int NJ, int NK, int KPAR>
-__global__ void __launch_bounds__(NI* NJ* KPAR)
+struct DShape : Shape<T, NI, NJ, NK, KPAR> {
+    using B = Shape<T, NI, NJ, NK, KPAR>;
+    static constexpr int NCELLS = NI * NJ * KPAR;        // interior cells of a chunk
+    static constexpr int TPC = NCELLS >= 512 ? 1 : 2;    // threads per cell in the sum (variables split)
+    static constexpr int NT = NCELLS * TPC;
+    static constexpr int VPT = NV / TPC;
+    static constexpr int KS = KPAR + 1;                  // k-face ring slots
+    static constexpr int NFI = NV * KPAR * NJ * (NI + 1);
+    static constexpr int NFJ = NV * KPAR * (NJ + 1) * NI;
+    static constexpr int NFK = KS * NV * NJ * NI;
+    // shared memory: mbarriers | tile[NV][W][PL] | FI | FJ | FK | gi | gj | gs
+    static constexpr size_t off_tile = 16;
+    static constexpr size_t off_fi = off_tile + (size_t)NV * B::W * B::PL * sizeof(T);
+    static constexpr size_t off_fj = off_fi + (size_t)NFI * sizeof(T);
+    static constexpr size_t off_fk = off_fj + (size_t)NFJ * sizeof(T);
+    static constexpr size_t off_gi = off_fk + (size_t)NFK * sizeof(T);
+    static constexpr size_t off_gj = off_gi + (size_t)GI_COUNT * B::NIP * sizeof(T);
+    static constexpr size_t off_gs = off_gj + (size_t)GJ_COUNT * B::NJP * sizeof(T);
+    static constexpr size_t smem = off_gs + GS_COUNT * sizeof(T);
+    static constexpr bool fits = smem <= 232448;         // 227 KB of opt-in shared memory per CTA
+    static constexpr int by_smem = (int)(233472 / (smem + 1024));
+    static constexpr int reg_cap = 2048 / NT;
+    static constexpr int min_blocks =
+        sizeof(T) != 4 || by_smem < 2 ? 1 : (by_smem < reg_cap ? by_smem : (reg_cap < 1 ? 1 : reg_cap));
+};
+
+// Limited flux through the face between cells L and R along one direction
+// (3_6/ModDiffusion.f90:40-60 for one side): values at L-1, L, R, R+1 and
+// the speeds |v_dir| + c_s at L and R.
+template <class T>
+__device__ __forceinline__ T face_flux(T fm, T fl, T fr, T fp, T cL, T cR) {
+    const T dL = minmod(fm, fl, fr);
+    const T dR = minmod(fl, fr, fp);
+    const T num = ((fr - dR * T(0.5)) - fl) - dL * T(0.5);
+    const T phi = fmax(T(0), T(1) + T(2) * (Pol<T>::ratio(num, fr - fl) - T(1)));
+    const T f = -(T(0.5) * phi * num);
+    return f * (cR + cL) * T(0.5);
+}
+
+template <class T, int NI, int NJ, int NK, int KPAR>
+__global__ void __launch_bounds__(DShape<T, NI, NJ, NK, KPAR>::NT, (DShape<T, NI, NJ, NK, KPAR>::min_blocks))
 k_diffusion(T* u, int8_t* ulo, Geometry g, StepScalars* sc) {
-    using S = Shape<T, NI, NJ, NK, KPAR>;
-    constexpr int NIP = S::NIP, PL = S::PL, W = S::W, NCELL = S::NCELL;
+    using S = DShape<T, NI, NJ, NK, KPAR>;
+    static_assert(S::fits, "diffusion shared memory above 227 KB");
+    constexpr int NIP = S::NIP, PL = S::PL, W = S::W, NCELL = S::NCELL, KS = S::KS;
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
     T* tile = reinterpret_cast<T*>(smem + S::off_tile);
+    T* FI = reinterpret_cast<T*>(smem + S::off_fi);
+    T* FJ = reinterpret_cast<T*>(smem + S::off_fj);
+    T* FK = reinterpret_cast<T*>(smem + S::off_fk);
     T* gi = reinterpret_cast<T*>(smem + S::off_gi);
     T* gj = reinterpret_cast<T*>(smem + S::off_gj);
     T* gs = reinterpret_cast<T*>(smem + S::off_gs);
@@ -547,86 +600,95 @@ k_diffusion(T* u, int8_t* ulo, Geometry g, StepScalars* sc) {
     load_geometry<T, S>(g, b, gi, gj, gs, nullptr);
     __syncthreads();   // the geometry tables are read by every thread below
     const int tid = threadIdx.x;
-    int i, j, kq;
-    cell_of_thread<NI, NJ, KPAR>(tid, i, j, kq);
-    const int ii = i + 2, jj = j + 2;
     const T* GCS = gi + GI_CS * NIP;
+    // the cell and variables this thread sums and updates
+    const int c = tid % S::NCELLS, v0 = (tid / S::NCELLS) * S::VPT;
+    const int i = c % NI, j = (c / NI) % NJ, kq = c / (NI * NJ);
+    const int ii = i + 2, jj = j + 2;
     const T rc = gi[GI_R * NIP + ii];
     const T den[3] = {gs[GS_DXI], gs[GS_DXJ] * rc, gs[GS_DXK] * rc * gj[GJ_SIN * S::NJP + jj]};
+    const T dinv[3] = {T(1) / den[0], T(1) / den[1], T(1) / den[2]};
     const double hdt = 0.5 * sc->dt;
     const float hdt_f = sc->dt_half_f;
+    // tile value of variable v at padded (x, y) of padded plane z
+    auto F = [&](int v, int x, int y, int z) -> T { return tile[(v * W + z % W) * PL + y * NIP + x]; };
     constexpr int nchunk = NK / KPAR;
     for (int ch = 0; ch < nchunk; ++ch) {
         const int k0 = 1 + ch * KPAR;
         const int hi = k0 + KPAR + 3;
-        __syncthreads();
+        __syncthreads();   // ring slots and face arrays of the previous chunk are free
         if (threadIdx.x == 0 && ch + 1 < nchunk) issue_planes<T, S>(blk, tile, hi, hi + KPAR, &bars[(ch + 1) & 1]);
         if (!mbar_wait(&bars[ch & 1], (uint32_t)((ch >> 1) & 1), kWaitPolls)) {
             atomicOr(&sc->nan_flag, 2);
             mbar_wait(&bars[(ch + 1) & 1], (uint32_t)(((ch + 1) >> 1) & 1), kWaitPolls);
             return;
         }
-        const int kp = k0 + kq + 1;
-        int sl[5];
-#pragma unroll
-        for (int d = 0; d < 5; ++d) sl[d] = (kp + d - 2) % W;
-        auto A = [&](int v, int di, int dj, int dk) -> T {
-            return tile[(v * W + sl[dk + 2]) * PL + (jj + dj) * NIP + ii + di];
-        };
-        T R[NV];
-#pragma unroll
-        for (int v = 0; v < NV; ++v) R[v] = T(0);
-#pragma unroll
-        for (int dir = 0; dir < 3; ++dir) {
-            const int vd = V_VR + dir;   // velocity component along the direction
-            auto at = [&](int v, int m) -> T {
-                return dir == 0 ? A(v, m, 0, 0) : dir == 1 ? A(v, 0, m, 0) : A(v, 0, 0, m);
-            };
-            const T csm = dir == 0 ? GCS[ii - 1] : GCS[ii];
-            const T cs0 = GCS[ii];
-            const T csp = dir == 0 ? GCS[ii + 1] : GCS[ii];
-            const T cm = fabs(at(vd, -1)) + csm, c0 = fabs(at(vd, 0)) + cs0, cp = fabs(at(vd, 1)) + csp;
-#pragma unroll 1
-            for (int v = 0; v < NV; ++v) {
-                const T fm2 = at(v, -2), fm1 = at(v, -1), f0 = at(v, 0), fp1 = at(v, 1), fp2 = at(v, 2);
-                const T dm1 = minmod(fm2, fm1, f0);
-                const T d0 = minmod(fm1, f0, fp1);
-                const T dp1 = minmod(f0, fp1, fp2);
-                // face between cells -1 and 0
-                T num = ((f0 - d0 * T(0.5)) - fm1) - dm1 * T(0.5);
-                T phi = fmax(T(0), T(1) + T(2) * (Pol<T>::ratio(num, f0 - fm1) - T(1)));
-                T fL = -(T(0.5) * phi * num);
-                fL = fL * (c0 + cm) * T(0.5);
-                // face between cells 0 and +1
-                num = ((fp1 - dp1 * T(0.5)) - f0) - d0 * T(0.5);
-                phi = fmax(T(0), T(1) + T(2) * (Pol<T>::ratio(num, fp1 - f0) - T(1)));
-                T fR = -(T(0.5) * phi * num);
-                fR = fR * (cp + c0) * T(0.5);
-                R[v] = R[v] + (fL - fR) / den[dir];
-            }
+        const int kp0 = k0 + 1;   // padded index of the chunk's first plane
+        // i faces: face f between padded cells f+1 and f+2 of a row
+        for (int x = tid; x < S::NFI; x += S::NT) {
+            const int f = x % (NI + 1);
+            int r = x / (NI + 1);
+            const int y = r % NJ + 2;
+            r /= NJ;
+            const int z = kp0 + r % KPAR, v = r / KPAR;
+            const T cL = fabs(F(V_VR, f + 1, y, z)) + GCS[f + 1];
+            const T cR = fabs(F(V_VR, f + 2, y, z)) + GCS[f + 2];
+            FI[x] = face_flux(F(v, f, y, z), F(v, f + 1, y, z), F(v, f + 2, y, z), F(v, f + 3, y, z), cL, cR);
         }
+        // j faces
+        for (int x = tid; x < S::NFJ; x += S::NT) {
+            const int xx = x % NI + 2;
+            int r = x / NI;
+            const int f = r % (NJ + 1);
+            r /= NJ + 1;
+            const int z = kp0 + r % KPAR, v = r / KPAR;
+            const T cs = GCS[xx];
+            const T cL = fabs(F(V_VT, xx, f + 1, z)) + cs;
+            const T cR = fabs(F(V_VT, xx, f + 2, z)) + cs;
+            FJ[x] = face_flux(F(v, xx, f, z), F(v, xx, f + 1, z), F(v, xx, f + 2, z), F(v, xx, f + 3, z), cL, cR);
+        }
+        // k faces not yet in the ring: face f between padded planes f+1 and f+2
+        const int kf_lo = ch == 0 ? kp0 - 2 : kp0 - 1;
+        const int nk_items = (kp0 + KPAR - 1 - kf_lo) * NV * NJ * NI;
+        for (int x = tid; x < nk_items; x += S::NT) {
+            const int xx = x % NI + 2;
+            int r = x / NI;
+            const int y = r % NJ + 2;
+            r /= NJ;
+            const int v = r % NV, f = kf_lo + r / NV;
+            const T cs = GCS[xx];
+            const T cL = fabs(F(V_VP, xx, y, f + 1)) + cs;
+            const T cR = fabs(F(V_VP, xx, y, f + 2)) + cs;
+            FK[(((f % KS) * NV + v) * NJ + (y - 2)) * NI + (xx - 2)] =
+                face_flux(F(v, xx, y, f), F(v, xx, y, f + 1), F(v, xx, y, f + 2), F(v, xx, y, f + 3), cL, cR);
+        }
+        __syncthreads();
+        const int kp = kp0 + kq;
         const size_t base = (size_t)kp * PL + jj * NIP + ii;
-        if constexpr (!Pol<T>::exact) {
-            if (ulo != nullptr) {
-                int8_t* blo = ulo + (size_t)b * NV * NCELL;
-                int8_t q0[NV];
+        const T* fk_l = FK + ((size_t)((kp - 2) % KS) * NV) * NJ * NI + j * NI + i;
+        const T* fk_r = FK + ((size_t)((kp - 1) % KS) * NV) * NJ * NI + j * NI + i;
 #pragma unroll
-                for (int v = 0; v < NV; ++v) q0[v] = blo[(size_t)v * NCELL + base];
-#pragma unroll
-                for (int v = 0; v < NV; ++v) {
+        for (int t = 0; t < S::VPT; ++t) {
+            const int v = v0 + t;
+            const T* fi = FI + ((v * KPAR + kq) * NJ + j) * (NI + 1) + i;
+            const T* fj = FJ + ((v * KPAR + kq) * (NJ + 1) + j) * NI + i;
+            T R = T(0);
+            R = R + Pol<T>::dv(fi[0] - fi[1], den[0], dinv[0]);
+            R = R + Pol<T>::dv(fj[0] - fj[NI], den[1], dinv[1]);
+            R = R + Pol<T>::dv(fk_l[v * NJ * NI] - fk_r[v * NJ * NI], den[2], dinv[2]);
+            const T u0 = F(v, ii, jj, kp);
+            if constexpr (!Pol<T>::exact) {
+                if (ulo != nullptr) {
+                    int8_t* q = ulo + (size_t)b * NV * NCELL + (size_t)v * NCELL + base;
                     int8_t q1;
-                    blk[(size_t)v * NCELL + base] = ff_add((float)A(v, 0, 0, 0), q0[v], __fmul_rn(hdt_f, (float)R[v]), q1);
-                    blo[(size_t)v * NCELL + base] = q1;
+                    blk[(size_t)v * NCELL + base] = ff_add((float)u0, *q, __fmul_rn(hdt_f, (float)R), q1);
+                    *q = q1;
+                    continue;
                 }
-                continue;
             }
-        }
-#pragma unroll
-        for (int v = 0; v < NV; ++v) {
-            const T u0 = A(v, 0, 0, 0);
             T o;
-            if (Pol<T>::exact) o = (T)((double)u0 + hdt * (double)R[v]);
-            else o = fmaf(hdt_f, (float)R[v], (float)u0);
+            if constexpr (Pol<T>::exact) o = (T)((double)u0 + hdt * (double)R);
+            else o = fmaf(hdt_f, (float)R, (float)u0);
             blk[(size_t)v * NCELL + base] = o;
         }
     }
