@@ -610,8 +610,6 @@ k_diffusion(T* u, int8_t* ulo, Geometry g, StepScalars* sc) {
     const T dinv[3] = {T(1) / den[0], T(1) / den[1], T(1) / den[2]};
     const double hdt = 0.5 * sc->dt;
     const float hdt_f = sc->dt_half_f;
-    // tile value of variable v at padded (x, y) of padded plane z
-    auto F = [&](int v, int x, int y, int z) -> T { return tile[(v * W + z % W) * PL + y * NIP + x]; };
     constexpr int nchunk = NK / KPAR;
     for (int ch = 0; ch < nchunk; ++ch) {
         const int k0 = 1 + ch * KPAR;
@@ -624,46 +622,65 @@ k_diffusion(T* u, int8_t* ulo, Geometry g, StepScalars* sc) {
             return;
         }
         const int kp0 = k0 + 1;   // padded index of the chunk's first plane
-        // i faces: face f between padded cells f+1 and f+2 of a row
-        for (int x = tid; x < S::NFI; x += S::NT) {
-            const int f = x % (NI + 1);
-            int r = x / (NI + 1);
-            const int y = r % NJ + 2;
-            r /= NJ;
-            const int z = kp0 + r % KPAR, v = r / KPAR;
-            const T cL = fabs(F(V_VR, f + 1, y, z)) + GCS[f + 1];
-            const T cR = fabs(F(V_VR, f + 2, y, z)) + GCS[f + 2];
-            FI[x] = face_flux(F(v, f, y, z), F(v, f + 1, y, z), F(v, f + 2, y, z), F(v, f + 3, y, z), cL, cR);
+        const int kp = kp0 + kq;
+        // ring offsets of planes kp-2 .. kp+2
+        int so[5];
+        so[0] = ((kp - 2) % W) * PL;
+#pragma unroll
+        for (int d = 1; d < 5; ++d) so[d] = so[d - 1] + PL >= W * PL ? so[d - 1] + PL - W * PL : so[d - 1] + PL;
+        const T* t0 = tile + jj * NIP + ii;   // this cell's column in every plane
+        // this cell's left i and j faces and right k face, for its variables
+        {
+            const T* tc = t0 + so[2];
+            const T cLi = fabs(tc[V_VR * W * PL - 1]) + GCS[ii - 1], cRi = fabs(tc[V_VR * W * PL]) + GCS[ii];
+            const T cs = GCS[ii];
+            const T cLj = fabs(tc[V_VT * W * PL - NIP]) + cs, cRj = fabs(tc[V_VT * W * PL]) + cs;
+            const T cLk = fabs(t0[V_VP * W * PL + so[2]]) + cs, cRk = fabs(t0[V_VP * W * PL + so[3]]) + cs;
+            T* fkw = FK + ((size_t)((kp - 1) % KS) * NV) * NJ * NI + j * NI + i;
+#pragma unroll
+            for (int t = 0; t < S::VPT; ++t) {
+                const int v = v0 + t;
+                const T* a = tc + v * W * PL;
+                FI[((v * KPAR + kq) * NJ + j) * (NI + 1) + i] = face_flux(a[-2], a[-1], a[0], a[1], cLi, cRi);
+                FJ[((v * KPAR + kq) * (NJ + 1) + j) * NI + i] =
+                    face_flux(a[-2 * NIP], a[-NIP], a[0], a[NIP], cLj, cRj);
+                const T* ak = t0 + v * W * PL;
+                fkw[v * NJ * NI] = face_flux(ak[so[1]], ak[so[2]], ak[so[3]], ak[so[4]], cLk, cRk);
+            }
         }
-        // j faces
-        for (int x = tid; x < S::NFJ; x += S::NT) {
-            const int xx = x % NI + 2;
-            int r = x / NI;
-            const int f = r % (NJ + 1);
-            r /= NJ + 1;
-            const int z = kp0 + r % KPAR, v = r / KPAR;
-            const T cs = GCS[xx];
-            const T cL = fabs(F(V_VT, xx, f + 1, z)) + cs;
-            const T cR = fabs(F(V_VT, xx, f + 2, z)) + cs;
-            FJ[x] = face_flux(F(v, xx, f, z), F(v, xx, f + 1, z), F(v, xx, f + 2, z), F(v, xx, f + 3, z), cL, cR);
+        // the right faces of the last cells of i rows and j columns
+        constexpr int NXI = NV * KPAR * NJ, NXJ = NV * KPAR * NI;
+        for (int x = tid; x < NXI + NXJ; x += S::NT) {
+            if (x < NXI) {
+                const int y = x % NJ + 2, q = (x / NJ) % KPAR, v = x / (NJ * KPAR);
+                const T* a = tile + (v * W + (kp0 + q) % W) * PL + y * NIP + NI + 1;   // last interior cell
+                const T* vr = tile + (V_VR * W + (kp0 + q) % W) * PL + y * NIP + NI + 1;
+                const T cL = fabs(vr[0]) + GCS[NI + 1], cR = fabs(vr[1]) + GCS[NI + 2];
+                FI[((v * KPAR + q) * NJ + (y - 2)) * (NI + 1) + NI] = face_flux(a[-1], a[0], a[1], a[2], cL, cR);
+            } else {
+                const int z = x - NXI;
+                const int xx = z % NI + 2, q = (z / NI) % KPAR, v = z / (NI * KPAR);
+                const T* a = tile + (v * W + (kp0 + q) % W) * PL + (NJ + 1) * NIP + xx;
+                const T* vt = tile + (V_VT * W + (kp0 + q) % W) * PL + (NJ + 1) * NIP + xx;
+                const T cs = GCS[xx];
+                const T cL = fabs(vt[0]) + cs, cR = fabs(vt[NIP]) + cs;
+                FJ[((v * KPAR + q) * (NJ + 1) + NJ) * NI + (xx - 2)] =
+                    face_flux(a[-NIP], a[0], a[NIP], a[2 * NIP], cL, cR);
+            }
         }
-        // k faces not yet in the ring: face f between padded planes f+1 and f+2
-        const int kf_lo = ch == 0 ? kp0 - 2 : kp0 - 1;
-        const int nk_items = (kp0 + KPAR - 1 - kf_lo) * NV * NJ * NI;
-        for (int x = tid; x < nk_items; x += S::NT) {
-            const int xx = x % NI + 2;
-            int r = x / NI;
-            const int y = r % NJ + 2;
-            r /= NJ;
-            const int v = r % NV, f = kf_lo + r / NV;
-            const T cs = GCS[xx];
-            const T cL = fabs(F(V_VP, xx, y, f + 1)) + cs;
-            const T cR = fabs(F(V_VP, xx, y, f + 2)) + cs;
-            FK[(((f % KS) * NV + v) * NJ + (y - 2)) * NI + (xx - 2)] =
-                face_flux(F(v, xx, y, f), F(v, xx, y, f + 1), F(v, xx, y, f + 2), F(v, xx, y, f + 3), cL, cR);
+        // first chunk: the k faces below the first plane (between padded planes 1 and 2)
+        if (ch == 0) {
+            for (int x = tid; x < NV * NJ * NI; x += S::NT) {
+                const int xx = x % NI + 2, y = (x / NI) % NJ + 2, v = x / (NI * NJ);
+                const T* a = tile + (size_t)v * W * PL + y * NIP + xx;
+                const T* vp = tile + (size_t)V_VP * W * PL + y * NIP + xx;
+                const T cs = GCS[xx];
+                const T cL = fabs(vp[PL]) + cs, cR = fabs(vp[2 * PL]) + cs;
+                FK[((0 * NV + v) * NJ + (y - 2)) * NI + (xx - 2)] =
+                    face_flux(a[0], a[PL], a[2 * PL], a[3 * PL], cL, cR);
+            }
         }
         __syncthreads();
-        const int kp = kp0 + kq;
         const size_t base = (size_t)kp * PL + jj * NIP + ii;
         const T* fk_l = FK + ((size_t)((kp - 2) % KS) * NV) * NJ * NI + j * NI + i;
         const T* fk_r = FK + ((size_t)((kp - 1) % KS) * NV) * NJ * NI + j * NI + i;
@@ -676,7 +693,7 @@ k_diffusion(T* u, int8_t* ulo, Geometry g, StepScalars* sc) {
             R = R + Pol<T>::dv(fi[0] - fi[1], den[0], dinv[0]);
             R = R + Pol<T>::dv(fj[0] - fj[NI], den[1], dinv[1]);
             R = R + Pol<T>::dv(fk_l[v * NJ * NI] - fk_r[v * NJ * NI], den[2], dinv[2]);
-            const T u0 = F(v, ii, jj, kp);
+            const T u0 = t0[v * W * PL + so[2]];
             if constexpr (!Pol<T>::exact) {
                 if (ulo != nullptr) {
                     int8_t* q = ulo + (size_t)b * NV * NCELL + (size_t)v * NCELL + base;
