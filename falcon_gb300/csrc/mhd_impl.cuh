@@ -141,9 +141,39 @@ __device__ __forceinline__ void load_geometry(const Geometry& g, int b, T* gi, T
     for (int x = threadIdx.x; x < GS_COUNT; x += S::NT) gs[x] = Gs[x];
     if (a12) {
         const double* Gd = g.gi + (size_t)b * GI_COUNT * S::NIP;
-        for (int x = threadIdx.x; x < 2 * S::NIP; x += S::NT)
-            a12[x] = Gd[(x < S::NIP ? GI_A1 * S::NIP : GI_A2 * S::NIP - S::NIP) + x];
+        for (int x = threadIdx.x; x < 2 * S::NIP; x += S::NT) {
+            const double a = Gd[(x < S::NIP ? GI_A1 * S::NIP : GI_A2 * S::NIP - S::NIP) + x];
+            if constexpr (Pol<T>::exact) {
+                a12[x] = a;
+            } else {
+                // FP32 pairs (hi, lo) with hi + lo = a to about 2^-48:
+                // [a1 hi | a1 lo | a2 hi | a2 lo], NIP floats each
+                float* f = reinterpret_cast<float*>(a12);
+                const int c = x % S::NIP, which = x / S::NIP;
+                const float hi = (float)a;
+                f[(2 * which) * S::NIP + c] = hi;
+                f[(2 * which + 1) * S::NIP + c] = (float)(a - (double)hi);
+            }
+        }
     }
+}
+
+// p1 = a1*rho1 + a2*s1 for the mixed path in float-float arithmetic: the
+// two products are formed exactly with FMA (plus the coefficients' low
+// parts), summed with an error-free two-sum, and rounded once to FP32. The
+// terms nearly cancel, so a plain FP32 sum would lose digits; this keeps the
+// accuracy of an FP64 assembly on the FP32 pipe (GB300's FP64 rate is a
+// small fraction of its FP32 rate).
+__device__ __forceinline__ float p1_ff(float a1h, float a1l, float a2h, float a2l, float r1, float s1) {
+    const float ph = __fmul_rn(a1h, r1);
+    const float pl = __fmaf_rn(a1h, r1, -ph);
+    const float qh = __fmul_rn(a2h, s1);
+    const float ql = __fmaf_rn(a2h, s1, -qh);
+    const float sh = __fadd_rn(ph, qh);
+    const float bb = __fsub_rn(sh, ph);
+    const float se = __fadd_rn(__fsub_rn(ph, __fsub_rn(sh, bb)), __fsub_rn(qh, bb));
+    const float lo = __fmaf_rn(a1l, r1, __fmaf_rn(a2l, s1, __fadd_rn(pl, ql)));
+    return __fadd_rn(sh, __fadd_rn(se, lo));
 }
 
 // Radial mirror boundary (3_6/ModBoundary.f90:10-55) on planes [lo,hi) of the
@@ -324,9 +354,16 @@ k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, DivBArgs 
         for (int x = tid; x < (hi - lo) * PL; x += S::NT) {
             const int kp = lo + x / PL, c = x % PL, ic = c % NIP;
             const int slot = kp % W;
-            const double r1 = (double)tile[(V_RHO1 * W + slot) * PL + c];
-            const double s1v = (double)tile[(V_S1 * W + slot) * PL + c];
-            tp1[(kp % WP) * PL + c] = (T)(a12[ic] * r1 + a12[NIP + ic] * s1v);
+            if constexpr (Pol<T>::exact) {
+                const double r1 = (double)tile[(V_RHO1 * W + slot) * PL + c];
+                const double s1v = (double)tile[(V_S1 * W + slot) * PL + c];
+                tp1[(kp % WP) * PL + c] = (T)(a12[ic] * r1 + a12[NIP + ic] * s1v);
+            } else {
+                const float* f = reinterpret_cast<const float*>(a12);
+                tp1[(kp % WP) * PL + c] = p1_ff(f[ic], f[NIP + ic], f[2 * NIP + ic], f[3 * NIP + ic],
+                                                (float)tile[(V_RHO1 * W + slot) * PL + c],
+                                                (float)tile[(V_S1 * W + slot) * PL + c]);
+            }
         }
         __syncthreads();
 
