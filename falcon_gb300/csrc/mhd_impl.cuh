@@ -72,6 +72,11 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
 // 1-D bulk copy global -> shared, completion counted on `bar` (16-byte aligned, size % 16 == 0)
+// Hint: pull `bytes` (a multiple of 16, 16-byte aligned) of global memory into
+// L2 ahead of plain loads.
+__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ void tma_load_1d(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
                  ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
@@ -312,6 +317,17 @@ k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, DivBArgs 
     }
     __syncthreads();
     if (threadIdx.x == 0) issue_planes<T, S>(blk_in, tile, 0, KPAR + 4, &bars[0]);
+    // u^n (and its int8 correction at stage 4) is read with plain loads at
+    // stages 2-4: warm L2 with the planes of the first chunk, then one chunk ahead
+    const T* blk_un = un + (size_t)b * NV * NCELL;
+    const int8_t* blk_lo = ulo != nullptr ? ulo + (size_t)b * NV * NCELL : nullptr;
+    auto prefetch_un = [&](int kp_first) {
+        if (stage == 1 || threadIdx.x >= NV) return;
+        const int v = threadIdx.x;
+        prefetch_l2(blk_un + ((size_t)v * S::NKP + kp_first) * PL, KPAR * S::PLB);
+        if (blk_lo != nullptr && stage == 4) prefetch_l2(blk_lo + ((size_t)v * S::NKP + kp_first) * PL, KPAR * PL);
+    };
+    prefetch_un(2);
     load_geometry<T, S>(g, b, gi, gj, gs, a12);
     __syncthreads();   // the geometry tables are read by every thread below
 
@@ -341,6 +357,7 @@ k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, DivBArgs 
         __syncthreads();   // chunk ch-1 is done with the slots the prefetch below overwrites
         if (threadIdx.x == 0 && ch + 1 < nchunk)
             issue_planes<T, S>(blk_in, tile, hi, hi + KPAR, &bars[(ch + 1) & 1]);
+        if (ch + 1 < nchunk) prefetch_un(k0 + KPAR + 1);
         if (!mbar_wait(&bars[ch & 1], (uint32_t)((ch >> 1) & 1), kWaitPolls)) {
             atomicOr(&sc->nan_flag, 2);   // timed-out copy: reported as an error, no hang
             mbar_wait(&bars[(ch + 1) & 1], (uint32_t)(((ch + 1) >> 1) & 1), kWaitPolls);
