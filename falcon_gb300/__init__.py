@@ -51,7 +51,7 @@ EXPORTS = (
     "falcon_solver_set_smoothing", "falcon_solver_problem_residuals",
     "falcon_lcc_create", "falcon_lcc_destroy", "falcon_lcc_last_error", "falcon_lcc_num_params",
     "falcon_lcc_get_params", "falcon_lcc_set_params", "falcon_lcc_forward", "falcon_lcc_loss_grad",
-    "falcon_lcc_train",
+    "falcon_lcc_train", "falcon_save_allcells", "falcon_save_restart", "falcon_load_restart",
 )
 
 # size of the static device array behind falcon_download_state_range
@@ -220,6 +220,19 @@ class Falcon:
 
     def synchronize(self):
         self._ck(self.L.falcon_synchronize(self.h))
+
+    # ---- output and restart
+    def save_allcells(self, directory, step):
+        """Write directory/AllCells_<step>/ (info.dat, Block_*.dat) in the
+        reference's AllCells text format; returns that directory."""
+        self._ck(self.L.falcon_save_allcells(self.h, os.fsencode(directory), C.c_int32(step)))
+        return os.path.join(directory, "AllCells_" + str(int(step)).rjust(8).replace(" ", "0"))
+
+    def save_restart(self, path):
+        self._ck(self.L.falcon_save_restart(self.h, os.fsencode(path)))
+
+    def load_restart(self, path):
+        self._ck(self.L.falcon_load_restart(self.h, os.fsencode(path)))
 
     # ---- measurement
     def set_kernel_timing(self, on):

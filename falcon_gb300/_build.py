@@ -27,6 +27,7 @@ UNITS = [
     ("synth.cu", []),
     ("capi.cu", []),
     ("state_range.cu", []),
+    ("output.cu", ["-fmad=false"]),
     ("host_setup.cpp", []),
     ("solver.cu", ["-fmad=false"]),
     ("solver_host.cpp", []),

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <filesystem>
 #include <memory>
 #include <string>
 #include <type_traits>
@@ -914,6 +915,254 @@ int falcon_download_stage_state(falcon_ctx* ctx, double* u) {
     if (rc) return rc;
     if (!u) return ctx->fail(FALCON_ERR_INVALID_ARG, "null state");
     return get_state(ctx, ctx->RK, nullptr, ctx->Prk, u);
+}
+
+// ---- output and restart ----------------------------------------------------
+namespace {
+// Fortran ES16.8: d.ddddddddE+dd right-justified in 16 columns; with a
+// three-digit exponent Fortran drops the E (d.dddddddd+ddd).
+void es16_8(double x, char* o) {
+    char buf[48];
+    int n;
+    if (std::isnan(x)) {
+        n = snprintf(buf, sizeof buf, "NaN");
+    } else if (std::isinf(x)) {
+        n = snprintf(buf, sizeof buf, "%s", x > 0 ? "Infinity" : "-Infinity");
+    } else {
+        n = snprintf(buf, sizeof buf, "%.8E", x);
+        char* e = std::strchr(buf, 'E');
+        if (e && std::strlen(e + 2) == 3) {
+            std::memmove(e, e + 1, std::strlen(e + 1) + 1);
+            --n;
+        }
+    }
+    if (n > 16) {
+        std::memset(o, '*', 16);
+        return;
+    }
+    std::memset(o, ' ', (size_t)(16 - n));
+    std::memcpy(o + 16 - n, buf, (size_t)n);
+}
+// write(c,'(I8)') with the blanks turned into '0' (3_6/ModSavePlot.f90:536-539)
+std::string i8_zero(long v) {
+    char b[32];
+    snprintf(b, sizeof b, "%8ld", v);
+    for (char* c = b; *c; ++c)
+        if (*c == ' ') *c = '0';
+    return b;
+}
+
+struct RestartHeader {
+    char magic[8];
+    uint32_t version, precision;
+    int32_t ni, nj, nk, ng, nblocks, divb_option;
+    uint64_t grid_hash;
+    int64_t steps_done;
+    uint64_t bytes_state, bytes_lo, bytes_psi;
+};
+const char kRestartMagic[8] = {'F', 'A', 'L', 'C', 'R', 'S', 'T', '1'};
+
+uint64_t grid_hash(const Grid& g) {   // FNV-1a over the block ranges and flags
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](const void* p, size_t n) {
+        const unsigned char* c = (const unsigned char*)p;
+        for (size_t q = 0; q < n; ++q) { h ^= c[q]; h *= 1099511628211ull; }
+    };
+    mix(g.ranges.data(), g.ranges.size() * sizeof(double));
+    mix(g.flags.data(), g.flags.size() * sizeof(int32_t));
+    return h;
+}
+
+RestartHeader restart_header(const falcon_ctx* ctx) {
+    RestartHeader h{};
+    std::memcpy(h.magic, kRestartMagic, 8);
+    h.version = 1;
+    h.precision = (uint32_t)ctx->cfg.precision;
+    h.ni = ctx->dims.ni; h.nj = ctx->dims.nj; h.nk = ctx->dims.nk; h.ng = ctx->grid.ng;
+    h.nblocks = ctx->dims.nblocks;
+    h.divb_option = ctx->cfg.phys.divb_option;
+    h.grid_hash = grid_hash(ctx->grid);
+    h.steps_done = ctx->steps_done;
+    const size_t cells = (size_t)ctx->dims.nblocks * ctx->dims.ncell;
+    h.bytes_state = cells * NV * ctx->elem;
+    h.bytes_lo = ctx->Ulo ? cells * NV : 0;
+    h.bytes_psi = ctx->P ? cells * ctx->elem : 0;
+    return h;
+}
+constexpr size_t kIoChunk = 64u << 20;
+}  // namespace
+
+int falcon_save_allcells(falcon_ctx* ctx, const char* directory, int32_t step) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    if (!directory) return ctx->fail(FALCON_ERR_INVALID_ARG, "null directory");
+    const Grid& g = ctx->grid;
+    const StepDims& d = ctx->dims;
+    const std::string dir = std::string(directory) + "/AllCells_" + i8_zero(step);
+    std::error_code ec;
+    std::filesystem::create_directories(dir, ec);
+    if (ec) return ctx->fail(FALCON_ERR_INVALID_ARG, "cannot create " + dir + ": " + ec.message());
+    {
+        FILE* f = std::fopen((dir + "/info.dat").c_str(), "w");
+        if (!f) return ctx->fail(FALCON_ERR_INVALID_ARG, "cannot write " + dir + "/info.dat");
+        std::fprintf(f, "nBlocks = %d\nni = %d\nnj = %d\nnk = %d\nnVarsTotal = %d\n", g.nblocks, g.ni, g.nj, g.nk,
+                     FALCON_NVAR + 3);
+        std::fputs("VARIABLES = \"X [Rs]\", \"Y [Rs]\", \"Z [Rs]\", \"Rho1\", \"Vx\", \"Vy\", \"Vz\", "
+                   "\"Bx\", \"By\", \"Bz\", \"S1\", \"PHI\"\n", f);
+        if (std::fclose(f) != 0) return ctx->fail(FALCON_ERR_INVALID_ARG, "cannot write " + dir + "/info.dat");
+    }
+    // face coordinates (3_6/ModBlock.f90:320-322) and their sines and cosines
+    const int nci = g.ni + 1, ncj = g.nj + 1, nck = g.nk + 1;
+    const int ts = allcells_table_stride(d);
+    std::vector<double> tab((size_t)g.nblocks * ts);
+    for (int b = 0; b < g.nblocks; ++b) {
+        const double* r = &g.ranges[(size_t)b * 6];
+        double* t = &tab[(size_t)b * ts];
+        for (int i = 1; i <= nci; ++i) t[i - 1] = (r[0] * (g.ni + 1 - i) + r[1] * (i - 1)) / g.ni;
+        for (int j = 1; j <= ncj; ++j) {
+            const double th = (r[2] * (g.nj + 1 - j) + r[3] * (j - 1)) / g.nj;
+            t[nci + j - 1] = std::sin(th);
+            t[nci + ncj + j - 1] = std::cos(th);
+        }
+        for (int k = 1; k <= nck; ++k) {
+            const double ph = (r[4] * (g.nk + 1 - k) + r[5] * (k - 1)) / g.nk;
+            t[nci + 2 * ncj + k - 1] = std::sin(ph);
+            t[nci + 2 * ncj + nck + k - 1] = std::cos(ph);
+        }
+        t[nci + 2 * ncj + 2 * nck] = (g.flags[b] & 1) ? 1.0 : 0.0;
+    }
+    const size_t ncor = (size_t)nci * ncj * nck;
+    const int batch = (int)std::max<size_t>(1, std::min<size_t>(g.nblocks, (64u << 20) / (ncor * 12 * 8)));
+    double *dtab = nullptr, *dout = nullptr;
+    auto release = [&] {
+        if (dtab) cudaFree(dtab);
+        if (dout) cudaFree(dout);
+    };
+    cudaError_t e = cudaMalloc((void**)&dtab, tab.size() * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&dout, (size_t)batch * ncor * 12 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dtab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->st);
+    if (e != cudaSuccess) {
+        release();
+        return ctx->cuda_fail(e, "allcells buffers");
+    }
+    std::vector<double> host((size_t)batch * ncor * 12);
+    const size_t line = 12 * 16 + 1;
+    int bad = -1;
+    for (int b0 = 0; b0 < g.nblocks && bad < 0; b0 += batch) {
+        const int nbb = std::min(batch, g.nblocks - b0);
+        e = launch_allcells(d, ctx->U, ctx->Ulo, ctx->P, ctx->mixed(), dtab, b0, nbb, dout, ctx->st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(host.data(), dout, (size_t)nbb * ncor * 12 * sizeof(double), cudaMemcpyDeviceToHost,
+                                ctx->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+        if (e != cudaSuccess) {
+            release();
+            return ctx->cuda_fail(e, "allcells");
+        }
+#pragma omp parallel for schedule(dynamic)
+        for (int bb = 0; bb < nbb; ++bb) {
+            std::string text(ncor * line, ' ');
+            const double* v = &host[(size_t)bb * ncor * 12];
+            for (size_t c = 0; c < ncor; ++c) {
+                char* o = &text[c * line];
+                for (int q = 0; q < 12; ++q) es16_8(v[c * 12 + q], o + 16 * q);
+                o[line - 1] = '\n';
+            }
+            const std::string fn = dir + "/Block_" + i8_zero(b0 + bb + 1) + ".dat";
+            FILE* f = std::fopen(fn.c_str(), "w");
+            bool ok = f && std::fwrite(text.data(), 1, text.size(), f) == text.size();
+            if (f) ok = (std::fclose(f) == 0) && ok;
+            if (!ok) {
+#pragma omp critical
+                bad = b0 + bb;
+            }
+        }
+    }
+    release();
+    if (bad >= 0) return ctx->fail(FALCON_ERR_INVALID_ARG, "cannot write the file of block " + std::to_string(bad + 1));
+    return FALCON_OK;
+}
+
+int falcon_save_restart(falcon_ctx* ctx, const char* path) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    if (!path) return ctx->fail(FALCON_ERR_INVALID_ARG, "null path");
+    CK(cudaStreamSynchronize(ctx->st), "restart");
+    const RestartHeader h = restart_header(ctx);
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return ctx->fail(FALCON_ERR_INVALID_ARG, std::string("cannot write ") + path);
+    bool ok = std::fwrite(&h, sizeof h, 1, f) == 1;
+    std::vector<unsigned char> buf(kIoChunk);
+    const void* src[3] = {ctx->U, ctx->Ulo, ctx->P};
+    const uint64_t len[3] = {h.bytes_state, h.bytes_lo, h.bytes_psi};
+    cudaError_t e = cudaSuccess;
+    for (int a = 0; a < 3 && ok; ++a)
+        for (uint64_t off = 0; off < len[a] && ok; off += kIoChunk) {
+            const size_t n = (size_t)std::min<uint64_t>(kIoChunk, len[a] - off);
+            e = cudaMemcpy(buf.data(), (const unsigned char*)src[a] + off, n, cudaMemcpyDeviceToHost);
+            ok = e == cudaSuccess && std::fwrite(buf.data(), 1, n, f) == n;
+        }
+    ok = (std::fclose(f) == 0) && ok;
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "restart");
+    if (!ok) return ctx->fail(FALCON_ERR_INVALID_ARG, std::string("cannot write ") + path);
+    return FALCON_OK;
+}
+
+int falcon_load_restart(falcon_ctx* ctx, const char* path) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    if (!path) return ctx->fail(FALCON_ERR_INVALID_ARG, "null path");
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return ctx->fail(FALCON_ERR_INVALID_ARG, std::string("cannot read ") + path);
+    RestartHeader h{};
+    const RestartHeader want = restart_header(ctx);
+    std::string why;
+    if (std::fread(&h, sizeof h, 1, f) != 1 || std::memcmp(h.magic, kRestartMagic, 8) != 0 || h.version != 1)
+        why = "not a restart file of this library";
+    else if (h.precision != want.precision)
+        why = "precision differs";
+    else if (h.ni != want.ni || h.nj != want.nj || h.nk != want.nk || h.ng != want.ng || h.nblocks != want.nblocks ||
+             h.grid_hash != want.grid_hash)
+        why = "grid differs";
+    else if (h.divb_option != want.divb_option)
+        why = "divb_option differs";
+    else if (h.bytes_state != want.bytes_state || h.bytes_lo != want.bytes_lo || h.bytes_psi != want.bytes_psi)
+        why = "payload sizes differ";
+    if (why.empty()) {   // the whole payload must be there before the state is touched
+        const long here = std::ftell(f);
+        std::fseek(f, 0, SEEK_END);
+        const long end = std::ftell(f);
+        std::fseek(f, here, SEEK_SET);
+        if ((uint64_t)(end - here) != h.bytes_state + h.bytes_lo + h.bytes_psi) why = "file is truncated or too long";
+    }
+    if (!why.empty()) {
+        std::fclose(f);
+        return ctx->fail(FALCON_ERR_INVALID_ARG, std::string("restart ") + path + ": " + why);
+    }
+    CK(cudaStreamSynchronize(ctx->st), "restart");
+    std::vector<unsigned char> buf(kIoChunk);
+    void* dst[3] = {ctx->U, ctx->Ulo, ctx->P};
+    const uint64_t len[3] = {h.bytes_state, h.bytes_lo, h.bytes_psi};
+    cudaError_t e = cudaSuccess;
+    bool ok = true;
+    for (int a = 0; a < 3 && ok; ++a)
+        for (uint64_t off = 0; off < len[a] && ok; off += kIoChunk) {
+            const size_t n = (size_t)std::min<uint64_t>(kIoChunk, len[a] - off);
+            ok = std::fread(buf.data(), 1, n, f) == n;
+            if (ok) e = cudaMemcpy((unsigned char*)dst[a] + off, buf.data(), n, cudaMemcpyHostToDevice);
+            ok = ok && e == cudaSuccess;
+        }
+    std::fclose(f);
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "restart");
+    if (!ok) return ctx->fail(FALCON_ERR_INVALID_ARG, std::string("restart ") + path + ": short read");
+    // the stage arrays start equal to the state, as after falcon_upload_state
+    CK(cudaMemcpyAsync(ctx->RK, ctx->U, h.bytes_state, cudaMemcpyDeviceToDevice, ctx->st), "restart");
+    if (ctx->P)
+        for (void* q : {ctx->Prk, ctx->P2})
+            CK(cudaMemcpyAsync(q, ctx->P, h.bytes_psi, cudaMemcpyDeviceToDevice, ctx->st), "restart");
+    CK(cudaStreamSynchronize(ctx->st), "restart");
+    ctx->steps_done = h.steps_done;
+    return FALCON_OK;
 }
 
 int falcon_synchronize(falcon_ctx* ctx) {

@@ -213,6 +213,16 @@ int kpar_candidates_mixed(const StepDims& d, int* out);
 cudaError_t launch_convert_state(const double* src, float* dst, int8_t* lo, int64_t n, const StepDims& dm,
                                  cudaStream_t st);
 cudaError_t launch_convert_psi(const double* src, float* psi, int64_t nb, int64_t ncell, cudaStream_t st);
+// AllCells output (output.cu): per-block face table [r (ni+1) | sin theta,
+// cos theta (nj+1 each) | sin phi, cos phi (nk+1 each) | yin], and the
+// kernel writing 12 doubles per corner (x, y, z, then the 9 variables with
+// Cartesian vectors) for blocks [b0, b0 + nbb)
+__host__ __device__ inline int allcells_table_stride(const StepDims& d) {
+    return (d.ni + 1) + 2 * (d.nj + 1) + 2 * (d.nk + 1) + 1;
+}
+cudaError_t launch_allcells(const StepDims& d, const void* U, const int8_t* lo, const void* psi, bool fp32,
+                            const double* tab, int b0, int nbb, double* out, cudaStream_t st);
+
 cudaError_t launch_gather_host(const void* U, const int8_t* lo, const void* psi, bool fp32, int64_t first, int64_t count,
                                int64_t ncell, double* out, cudaStream_t st);
 

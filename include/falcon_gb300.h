@@ -195,6 +195,29 @@ int  falcon_unpin_host(falcon_ctx* ctx, void* p);
  * kind 1: kind 0 plus a random-phase Kolmogorov velocity field (rms Mach mach) */
 int  falcon_init_synthetic(falcon_ctx* ctx, int32_t kind, uint64_t seed, double mach);
 
+/* ---- output and restart ------------------------------------------------- */
+/* AllCells plot output from the device state, replacing ModSave_AllCells
+ * (3_6/ModSavePlot.f90:520-650, called from ModSave_DoAll :16-59): creates
+ * <directory>/AllCells_<step, 8 digits>/ with info.dat and one
+ * Block_<global block index, 8 digits>.dat per block, in the reference's text
+ * format -- per corner (i fastest, 1..n+1 in each direction) one line of 12
+ * ES16.8 values: x, y, z in solar radii, then the 9 variables averaged over the
+ * 8 cells around the corner, velocity and B in Cartesian components (Yang
+ * blocks mapped as (x, y, z) = (-x0, z0, y0)). The averaging and conversions
+ * run on the GPU in batches of blocks; the host writes the text. The state's
+ * ghost cells must be current (as after a step or falcon_exchange).
+ * 3_6/merge_AllCells.py merges the directory into one Tecplot file. */
+int  falcon_save_allcells(falcon_ctx* ctx, const char* directory, int32_t step);
+/* Binary restart dump of the device state, which the reference lacks: the
+ * raw device arrays (state, the mixed path's 8-bit corrections of u^n, psi
+ * with GLM) behind a header with the grid's shape, precision, div-B option, a
+ * hash of the block ranges and the step count. falcon_load_restart into a
+ * context of the same configuration continues bit for bit as the run that
+ * wrote the dump; a file of another configuration, or a short file, returns
+ * FALCON_ERR_INVALID_ARG and leaves the state unchanged. */
+int  falcon_save_restart(falcon_ctx* ctx, const char* path);
+int  falcon_load_restart(falcon_ctx* ctx, const char* path);
+
 /* ---- the hot path ------------------------------------------------------- */
 int  falcon_exchange(falcon_ctx* ctx);
 int  falcon_timestep(falcon_ctx* ctx, double* dt_out);

@@ -38,7 +38,7 @@ def lib():
         for name in ("orc_num_blocks", "orc_block_ranges", "orc_block_flags", "orc_get_background",
                      "orc_ghost_map", "orc_set_state", "orc_get_state", "orc_exchange",
                      "orc_timestep", "orc_step", "orc_block_rhs", "orc_block_diffusion",
-                     "orc_block_grid", "orc_phase", "orc_get_stage_state"):
+                     "orc_block_grid", "orc_phase", "orc_get_stage_state", "orc_save_allcells"):
             getattr(L, name).restype = C.c_int
         L.orc_ghost_count.restype = C.c_int64
         L.orc_ghost_count.argtypes = [vp]
@@ -136,6 +136,13 @@ class Oracle:
     def phase(self, ph):
         self.L.orc_phase(self.hp, C.c_int32(ph))
         return self.L.orc_dt(self.hp)
+
+    def save_allcells(self, directory, step):
+        """ModSave_AllCells of the oracle's state: directory/AllCells_<step>/."""
+        rc = self.L.orc_save_allcells(C.c_void_p(self.h), os.fsencode(directory), C.c_int32(step))
+        if rc != 0:
+            raise OSError("oracle could not write AllCells files under %s" % directory)
+        return os.path.join(directory, "AllCells_" + str(int(step)).rjust(8).replace(" ", "0"))
 
     def get_stage_state(self):
         u = np.zeros(self.shape)

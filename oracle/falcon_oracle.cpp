@@ -34,6 +34,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <filesystem>
 #include <string>
 #include <vector>
 #include <algorithm>
@@ -1038,6 +1039,102 @@ void Oracle::phase(int ph) {
 
 }  // namespace orc
 
+// ---- ModSave_AllCells (3_6/ModSavePlot.f90:520-650) ------------------------
+namespace orc {
+// Fortran ES16.8 (gfortran): d.ddddddddE+dd right-justified in 16 columns,
+// the E dropped before a three-digit exponent
+static std::string fortran_es16_8(double x) {
+    char b[64];
+    if (std::isnan(x)) std::snprintf(b, sizeof b, "NaN");
+    else if (std::isinf(x)) std::snprintf(b, sizeof b, "%s", x > 0 ? "Infinity" : "-Infinity");
+    else std::snprintf(b, sizeof b, "%.8E", x);
+    std::string t(b);
+    const size_t e = t.find('E');
+    if (e != std::string::npos && t.size() - e - 2 == 3) t.erase(e, 1);
+    if (t.size() > 16) return std::string(16, '*');
+    return std::string(16 - t.size(), ' ') + t;
+}
+static std::string fortran_i8_zero(long v) {
+    char b[32];
+    std::snprintf(b, sizeof b, "%8ld", v);
+    std::string t(b);
+    for (char& c : t)
+        if (c == ' ') c = '0';
+    return t;
+}
+}  // namespace orc
+
+static int orc_save_allcells_impl(orc::Oracle& o, const char* directory, int step) {
+    using namespace orc;
+    const std::string dir = std::string(directory) + "/AllCells_" + fortran_i8_zero(step);
+    std::filesystem::create_directories(dir);
+    FILE* f = std::fopen((dir + "/info.dat").c_str(), "w");
+    if (!f) return -1;
+    std::fprintf(f, "nBlocks = %d\n", (int)o.blk.size());
+    std::fprintf(f, "ni = %d\nnj = %d\nnk = %d\n", o.ni, o.nj, o.nk);
+    std::fprintf(f, "nVarsTotal = %d\n", o.nvar + 3);
+    std::fprintf(f, "VARIABLES = \"X [Rs]\", \"Y [Rs]\", \"Z [Rs]\", \"Rho1\", \"Vx\", \"Vy\", \"Vz\", \"Bx\", "
+                    "\"By\", \"Bz\", \"S1\", \"PHI\"\n");
+    std::fclose(f);
+    const double rsun = (double)6.955e10f;   // R_sun__CGS (3_6/ModConst.f90:5)
+    const int ni = o.ni, nj = o.nj, nk = o.nk, nv = o.nvar;
+    for (const Block& B : o.blk) {
+        // corner values (3_6/ModSavePlot.f90:572-582)
+        std::vector<double> cor((size_t)(ni + 1) * (nj + 1) * (nk + 1) * nv);
+        auto p = [&](int v, int i, int j, int k) { return B.u[(size_t)v * o.ncell + o.idx(i, j, k)]; };
+        size_t q = 0;
+        for (int k = 1; k <= nk + 1; ++k)
+            for (int j = 1; j <= nj + 1; ++j)
+                for (int i = 1; i <= ni + 1; ++i, ++q)
+                    for (int v = 0; v < nv; ++v)
+                        cor[q * nv + v] = 0.125 * (p(v, i - 1, j - 1, k - 1) + p(v, i, j - 1, k - 1) +
+                                                   p(v, i - 1, j, k - 1) + p(v, i, j, k - 1) +
+                                                   p(v, i - 1, j - 1, k) + p(v, i, j - 1, k) +
+                                                   p(v, i - 1, j, k) + p(v, i, j, k));
+        // face coordinates (3_6/ModBlock.f90:320-322)
+        std::vector<double> xf(ni + 1), yf(nj + 1), zf(nk + 1);
+        for (int i = 1; i <= ni + 1; ++i) xf[i - 1] = (B.rng[0][0] * (ni + 1 - i) + B.rng[0][1] * (i - 1)) / ni;
+        for (int j = 1; j <= nj + 1; ++j) yf[j - 1] = (B.rng[1][0] * (nj + 1 - j) + B.rng[1][1] * (j - 1)) / nj;
+        for (int k = 1; k <= nk + 1; ++k) zf[k - 1] = (B.rng[2][0] * (nk + 1 - k) + B.rng[2][1] * (k - 1)) / nk;
+        f = std::fopen((dir + "/Block_" + fortran_i8_zero(B.id) + ".dat").c_str(), "w");
+        if (!f) return -1;
+        q = 0;
+        for (int k = 1; k <= nk + 1; ++k)
+            for (int j = 1; j <= nj + 1; ++j)
+                for (int i = 1; i <= ni + 1; ++i, ++q) {
+                    const double r = xf[i - 1], th = yf[j - 1], ph = zf[k - 1];
+                    const double sth = std::sin(th), cth = std::cos(th), sph = std::sin(ph), cph = std::cos(ph);
+                    double xyz[3];
+                    if (B.yin) {
+                        xyz[0] = r * sth * cph;
+                        xyz[1] = r * sth * sph;
+                        xyz[2] = r * cth;
+                    } else {
+                        xyz[0] = -(r * sth * cph);
+                        xyz[1] = r * cth;
+                        xyz[2] = r * sth * sph;
+                    }
+                    for (double& c : xyz) c = c / rsun;
+                    double vo[FALCON_NVAR];
+                    for (int v = 0; v < nv; ++v) vo[v] = cor[q * nv + v];
+                    for (int a : {VR, BR}) {
+                        const double vx = vo[a] * sth * cph + vo[a + 1] * cth * cph - vo[a + 2] * sph;
+                        const double vy = vo[a] * sth * sph + vo[a + 1] * cth * sph + vo[a + 2] * cph;
+                        const double vz = vo[a] * cth - vo[a + 1] * sth;
+                        if (B.yin) { vo[a] = vx; vo[a + 1] = vy; vo[a + 2] = vz; }
+                        else { vo[a] = -vx; vo[a + 1] = vz; vo[a + 2] = vy; }
+                    }
+                    std::string line;
+                    for (double c : xyz) line += fortran_es16_8(c);
+                    for (int v = 0; v < nv; ++v) line += fortran_es16_8(vo[v]);
+                    line += '\n';
+                    std::fputs(line.c_str(), f);
+                }
+        std::fclose(f);
+    }
+    return 0;
+}
+
 // ---- C API used by the tests and by bench.py's CPU baseline -------------
 using orc::Oracle;
 
@@ -1147,6 +1244,9 @@ int orc_get_stage_state(void* h, double* u) {
     size_t n = (size_t)o->nvar * o->ncell;
     for (size_t b = 0; b < o->blk.size(); ++b) std::memcpy(u + n * b, o->blk[b].urk.data(), n * sizeof(double));
     return 0;
+}
+int orc_save_allcells(void* h, const char* directory, int32_t step) {
+    return orc_save_allcells_impl(*(Oracle*)h, directory, step);
 }
 int orc_exchange(void* h) { ((Oracle*)h)->exchange(false); return 0; }
 int orc_timestep(void* h, double* dt) {
