@@ -45,6 +45,8 @@ struct falcon_ctx {
     int8_t* Ulo = nullptr;      // mixed mode: 8-bit correction of u^n (interior cells)
     void *P = nullptr, *Prk = nullptr, *P2 = nullptr;   // psi of U, RK, R2 (GLM only) [b][cell]
     double* stage64 = nullptr;  // FP64 staging buffer for mixed-mode transfers (lazy)
+    int32_t* dflag = nullptr;   // device flag of the upload's psi check (lazy)
+    std::vector<std::pair<uintptr_t, size_t>> pinned;   // host ranges pinned through falcon_pin_host
     double *gi = nullptr, *gj = nullptr, *gs = nullptr;
     float *gi_f = nullptr, *gj_f = nullptr, *gs_f = nullptr;
     int32_t* flags = nullptr;
@@ -688,22 +690,57 @@ int falcon_ghost_map(const falcon_ctx* ctx, falcon_ghost_entry* out, int64_t cap
 namespace {
 size_t host_elems(const falcon_ctx* ctx) { return (size_t)ctx->dims.nblocks * FALCON_NVAR * ctx->dims.ncell; }
 
+// Device address of the host range [p, p + bytes) when it lies inside one
+// buffer pinned through falcon_pin_host: the GPU then reads or writes it in
+// place over the host link (NVLink-C2C on GB300), with no staging copy.
+// Any other host memory gives nullptr (staged through device memory).
+void* mapped_host(falcon_ctx* ctx, const void* p, size_t bytes) {
+    const uintptr_t a = (uintptr_t)p;
+    for (const auto& r : ctx->pinned)
+        if (a >= r.first && a + bytes <= r.first + r.second) {
+            void* d = nullptr;
+            if (cudaHostGetDevicePointer(&d, (void*)r.first, 0) != cudaSuccess || !d) {
+                cudaGetLastError();
+                return nullptr;
+            }
+            return (char*)d + (a - r.first);
+        }
+    return nullptr;
+}
+
 int put_state(falcon_ctx* ctx, const double* u, void* U, int8_t* lo, void* P) {
     const size_t nb = (size_t)ctx->dims.nblocks, nc = (size_t)ctx->dims.ncell;
-    if (!P) {   // psi is not evolved: it must be 0, as it then stays in the reference
-        for (size_t b = 0; b < nb; ++b) {
-            const double* q = u + (b * FALCON_NVAR + NV) * nc;
-            for (size_t c = 0; c < nc; ++c)
-                if (q[c] != 0.0) return ctx->fail(FALCON_ERR_INVALID_ARG, "psi must be 0 when divb_option = 0");
-        }
-    }
+    // psi is not evolved without GLM: it must be 0, as it then stays in the
+    // reference (checked before anything on the device changes)
+    const char* psi_msg = "psi must be 0 unless divb_option = 1";
     if (ctx->mixed()) {
         const size_t n9 = host_elems(ctx);
-        if (!ctx->stage64) CK(ctx->alloc(&ctx->stage64, n9 * 8), "alloc staging");
-        CK(cudaMemcpyAsync(ctx->stage64, u, n9 * 8, cudaMemcpyHostToDevice, ctx->st), "upload");
-        CK(launch_convert_state(ctx->stage64, (float*)U, lo, (int64_t)(nb * NV * nc), ctx->dims, ctx->st), "upload convert");
-        if (P) CK(launch_convert_psi(ctx->stage64, (float*)P, (int64_t)nb, (int64_t)nc, ctx->st), "upload convert");
+        if (!ctx->dflag) CK(ctx->alloc(&ctx->dflag, sizeof(int32_t)), "alloc flag");
+        const double* src = (const double*)mapped_host(ctx, u, n9 * 8);
+        if (!src) {
+            if (!ctx->stage64) CK(ctx->alloc(&ctx->stage64, n9 * 8), "alloc staging");
+            CK(cudaMemcpyAsync(ctx->stage64, u, n9 * 8, cudaMemcpyHostToDevice, ctx->st), "upload");
+            src = ctx->stage64;
+        }
+        if (!P) {
+            int32_t bad = 0;
+            CK(launch_psi_nonzero(src, (int64_t)nb, (int64_t)nc, ctx->dflag, ctx->st), "upload check");
+            CK(cudaMemcpyAsync(&bad, ctx->dflag, sizeof bad, cudaMemcpyDeviceToHost, ctx->st), "upload check");
+            CK(cudaStreamSynchronize(ctx->st), "upload check");
+            if (bad) return ctx->fail(FALCON_ERR_INVALID_ARG, psi_msg);
+        }
+        CK(launch_convert_state(src, (float*)U, lo, (int64_t)(nb * NV * nc), ctx->dims, ctx->st), "upload convert");
+        if (P) CK(launch_convert_psi(src, (float*)P, (int64_t)nb, (int64_t)nc, ctx->st), "upload convert");
     } else {
+        if (!P) {
+            int bad = 0;
+#pragma omp parallel for reduction(| : bad) schedule(static)
+            for (long b = 0; b < (long)nb; ++b) {
+                const double* q = u + ((size_t)b * FALCON_NVAR + NV) * nc;
+                for (size_t c = 0; c < nc; ++c) bad |= q[c] != 0.0;
+            }
+            if (bad) return ctx->fail(FALCON_ERR_INVALID_ARG, psi_msg);
+        }
         CK(cudaMemcpy2DAsync(U, NV * nc * 8, u, FALCON_NVAR * nc * 8, NV * nc * 8, nb, cudaMemcpyHostToDevice, ctx->st),
            "upload");
         if (P)
@@ -717,9 +754,14 @@ int get_state(falcon_ctx* ctx, const void* U, const int8_t* lo, const void* P, d
     const size_t nb = (size_t)ctx->dims.nblocks, nc = (size_t)ctx->dims.ncell;
     if (ctx->mixed()) {
         const size_t n9 = host_elems(ctx);
-        if (!ctx->stage64) CK(ctx->alloc(&ctx->stage64, n9 * 8), "alloc staging");
-        CK(launch_gather_host(U, lo, P, true, 0, (int64_t)n9, (int64_t)nc, ctx->stage64, ctx->st), "download convert");
-        CK(cudaMemcpyAsync(u, ctx->stage64, n9 * 8, cudaMemcpyDeviceToHost, ctx->st), "download");
+        double* dst = (double*)mapped_host(ctx, u, n9 * 8);
+        if (dst) {
+            CK(launch_gather_host(U, lo, P, true, 0, (int64_t)n9, (int64_t)nc, dst, ctx->st), "download convert");
+        } else {
+            if (!ctx->stage64) CK(ctx->alloc(&ctx->stage64, n9 * 8), "alloc staging");
+            CK(launch_gather_host(U, lo, P, true, 0, (int64_t)n9, (int64_t)nc, ctx->stage64, ctx->st), "download convert");
+            CK(cudaMemcpyAsync(u, ctx->stage64, n9 * 8, cudaMemcpyDeviceToHost, ctx->st), "download");
+        }
         CK(cudaStreamSynchronize(ctx->st), "download");
     } else {
         CK(cudaMemcpy2DAsync(u, FALCON_NVAR * nc * 8, U, NV * nc * 8, NV * nc * 8, nb, cudaMemcpyDeviceToHost, ctx->st),
@@ -787,7 +829,8 @@ int falcon_pin_host(falcon_ctx* ctx, void* p, size_t bytes) {
     int rc = need_device(ctx);
     if (rc) return rc;
     if (!p || !bytes) return ctx->fail(FALCON_ERR_INVALID_ARG, "null buffer");
-    CK(cudaHostRegister(p, bytes, cudaHostRegisterDefault), "cudaHostRegister");
+    CK(cudaHostRegister(p, bytes, cudaHostRegisterMapped), "cudaHostRegister");
+    ctx->pinned.push_back({(uintptr_t)p, bytes});
     return FALCON_OK;
 }
 
@@ -795,6 +838,11 @@ int falcon_unpin_host(falcon_ctx* ctx, void* p) {
     int rc = need_device(ctx);
     if (rc) return rc;
     CK(cudaHostUnregister(p), "cudaHostUnregister");
+    for (size_t q = 0; q < ctx->pinned.size(); ++q)
+        if (ctx->pinned[q].first == (uintptr_t)p) {
+            ctx->pinned.erase(ctx->pinned.begin() + (long)q);
+            break;
+        }
     return FALCON_OK;
 }
 

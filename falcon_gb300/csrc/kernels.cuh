@@ -213,6 +213,8 @@ int kpar_candidates_mixed(const StepDims& d, int* out);
 cudaError_t launch_convert_state(const double* src, float* dst, int8_t* lo, int64_t n, const StepDims& dm,
                                  cudaStream_t st);
 cudaError_t launch_convert_psi(const double* src, float* psi, int64_t nb, int64_t ncell, cudaStream_t st);
+// *flag = 1 if the psi planes of a host-layout FP64 array on the device hold a non-zero value
+cudaError_t launch_psi_nonzero(const double* src, int64_t nb, int64_t ncell, int32_t* flag, cudaStream_t st);
 // AllCells output (output.cu): per-block face table [r (ni+1) | sin theta,
 // cos theta (nj+1 each) | sin phi, cos phi (nk+1 each) | yin], and the
 // kernel writing 12 doubles per corner (x, y, z, then the 9 variables with

@@ -79,6 +79,16 @@ __global__ void k_narrow_psi(const double* s, float* psi, int64_t nb, int64_t nc
         psi[x] = (float)s[(b * (NV + 1) + NV) * ncell + (x - b * ncell)];
     }
 }
+// flag = 1 if any psi value of the host array (already on the device) is
+// not 0 (NaN counts as not 0)
+__global__ void k_psi_nonzero(const double* s, int64_t nb, int64_t ncell, int32_t* flag) {
+    int any = 0;
+    for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < nb * ncell; x += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b = x / ncell;
+        any |= s[(b * (NV + 1) + NV) * ncell + (x - b * ncell)] != 0.0;
+    }
+    if (__any_sync(0xffffffffu, any) && (threadIdx.x & 31) == 0) *flag = 1;
+}
 // host elements [first, first + count) as FP64 from the device state (FP32
 // with its correction, or FP64) and psi (nullptr: psi = 0)
 template <class T>
@@ -108,6 +118,12 @@ cudaError_t launch_convert_state(const double* src, float* dst, int8_t* lo, int6
 }
 cudaError_t launch_convert_psi(const double* src, float* psi, int64_t nb, int64_t ncell, cudaStream_t st) {
     k_narrow_psi<<<1216, 256, 0, st>>>(src, psi, nb, ncell);
+    return cudaGetLastError();
+}
+cudaError_t launch_psi_nonzero(const double* src, int64_t nb, int64_t ncell, int32_t* flag, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int32_t), st);
+    if (e != cudaSuccess) return e;
+    k_psi_nonzero<<<1216, 256, 0, st>>>(src, nb, ncell, flag);
     return cudaGetLastError();
 }
 cudaError_t launch_gather_host(const void* U, const int8_t* lo, const void* psi, bool fp32, int64_t first, int64_t count,

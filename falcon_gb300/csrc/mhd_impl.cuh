@@ -651,6 +651,14 @@ k_diffusion(T* u, int8_t* ulo, Geometry g, StepScalars* sc) {
     }
     __syncthreads();
     if (threadIdx.x == 0) issue_planes<T, S>(blk, tile, 0, KPAR + 4, &bars[0]);
+    // the int8 corrections of u^n are read with plain loads: warm L2 with the
+    // first chunk's planes, then one chunk ahead
+    const int8_t* blk_lo = ulo != nullptr ? ulo + (size_t)b * NV * NCELL : nullptr;
+    auto prefetch_lo = [&](int kp_first) {
+        if (blk_lo == nullptr || threadIdx.x >= NV) return;
+        prefetch_l2(blk_lo + ((size_t)threadIdx.x * S::NKP + kp_first) * PL, KPAR * PL);
+    };
+    prefetch_lo(2);
     load_geometry<T, S>(g, b, gi, gj, gs, nullptr);
     __syncthreads();   // the geometry tables are read by every thread below
     const int tid = threadIdx.x;
@@ -670,6 +678,7 @@ k_diffusion(T* u, int8_t* ulo, Geometry g, StepScalars* sc) {
         const int hi = k0 + KPAR + 3;
         __syncthreads();   // ring slots and face arrays of the previous chunk are free
         if (threadIdx.x == 0 && ch + 1 < nchunk) issue_planes<T, S>(blk, tile, hi, hi + KPAR, &bars[(ch + 1) & 1]);
+        if (ch + 1 < nchunk) prefetch_lo(k0 + KPAR + 1);
         if (!mbar_wait(&bars[ch & 1], (uint32_t)((ch >> 1) & 1), kWaitPolls)) {
             atomicOr(&sc->nan_flag, 2);
             mbar_wait(&bars[(ch + 1) & 1], (uint32_t)(((ch + 1) >> 1) & 1), kWaitPolls);

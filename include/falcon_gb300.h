@@ -186,8 +186,11 @@ int  falcon_download_state(falcon_ctx* ctx, double* u);
  * the GPU (from several host threads) race on the array: serialise them. */
 #define FALCON_STATIC_SCRATCH_BYTES (16u << 20)
 int  falcon_download_state_range(falcon_ctx* ctx, size_t first, size_t count, double* u);
-/* Page-lock a host buffer so that state transfers run at full link speed
- * (cudaHostRegister); unpin before freeing it. */
+/* Page-lock a host buffer (cudaHostRegister, mapped) and remember it: a MIXED
+ * falcon_upload_state / falcon_download_state whose whole array lies in such
+ * a buffer converts straight from / into host memory on the GPU over the host
+ * link (NVLink-C2C on GB300), with no device staging copy. Unpin before
+ * freeing the buffer. */
 int  falcon_pin_host(falcon_ctx* ctx, void* p, size_t bytes);
 int  falcon_unpin_host(falcon_ctx* ctx, void* p);
 /* synthetic initial condition generated on the device (seeded):

@@ -297,3 +297,54 @@ def test_divb_mixed_step_matches_phase_sequence(divb):
     ua, ub = a.download_state(), b.download_state()
     assert np.isfinite(ua).all()
     assert np.array_equal(ua, ub)
+
+
+@pytest.mark.parametrize("prec", [config.PREC_FP64, config.PREC_MIXED])
+def test_upload_rejects_nonzero_psi_without_glm(prec):
+    """Without GLM psi is not evolved (the reference leaves it 0): an upload
+    with a non-zero psi fails and leaves the device state as it was."""
+    f = fg.Falcon(config.tiny(precision=prec))
+    u0 = synth.initial_state(config.tiny(), f.block_ranges(), f.block_flags(), seed=1007)
+    f.upload_state(u0)
+    before = f.download_state()
+    u1 = u0.copy()
+    u1[3, 8, 4, 5, 6] = 1e-9
+    with pytest.raises(fg.FalconError) as e:
+        f.upload_state(u1)
+    assert e.value.code == fg.ERR_INVALID_ARG and "psi" in str(e.value)
+    assert np.array_equal(before, f.download_state())
+
+
+@pytest.mark.parametrize("divb", [0, 1])
+def test_mixed_transfers_through_pinned_buffers_match_staged(divb):
+    """A pinned host array is read and written in place by the GPU (no
+    staging copy); the device state and the downloads are bit-identical to
+    the staged path's, and the psi check still rejects before any change."""
+    mk = lambda: config.tiny(precision=config.PREC_MIXED, divb_option=divb)
+    a, b = fg.Falcon(mk()), fg.Falcon(mk())
+    u0 = synth.initial_state(mk(), a.block_ranges(), a.block_flags(), seed=1008, psi_amp=1e-3 if divb else 0.0)
+    pinned = np.ascontiguousarray(u0.copy())
+    a.pin_host(pinned)
+    try:
+        a.upload_state_raw(pinned)
+        b.upload_state(u0)
+        for x in (a, b):
+            x.exchange()
+            x.advance_rk4(want_dt=False)
+        out = np.zeros_like(pinned)
+        a.pin_host(out)
+        try:
+            a.download_state_into(out)
+            assert np.array_equal(out, b.download_state())
+            assert np.array_equal(a.download_state(), b.download_state())
+        finally:
+            a.unpin_host(out)
+        if divb == 0:
+            before = a.download_state()
+            pinned[2, 8, 3, 3, 3] = 5.0
+            with pytest.raises(fg.FalconError) as e:
+                a.upload_state_raw(pinned)
+            assert e.value.code == fg.ERR_INVALID_ARG
+            assert np.array_equal(before, a.download_state())
+    finally:
+        a.unpin_host(pinned)
