@@ -111,25 +111,142 @@ __global__ void k_gather_host(const T* U, const int8_t* lo, const T* psi, int64_
         out[x] = v;
     }
 }
+// Wide forms of the transfer kernels: each thread moves kWide elements per
+// pass as kWide/2 16-byte accesses, all issued before any is used (a warp's
+// access q covers 512 contiguous bytes), so that many bytes are in flight when
+// the FP64 side is host memory read or written in place over the host link. They need 16-byte-aligned FP64
+// arrays, an even cell count and even ranges (pairs never straddle a
+// variable); the launchers fall back to the one-element kernels otherwise.
+constexpr int kWide = 8;
+__device__ __forceinline__ void narrow_one(double u, int64_t x, float* d, int8_t* lo, const StepDims& dm) {
+    const float hi = (float)u;
+    d[x] = hi;
+    if (lo) {
+        const int c = (int)(x % dm.ncell);
+        const int ip = c % dm.nip, jp = (c / dm.nip) % dm.njp, kp = c / (dm.nip * dm.njp);
+        const bool interior = ip >= 2 && ip < dm.nip - 2 && jp >= 2 && jp < dm.njp - 2 && kp >= 2 && kp < dm.nkp - 2;
+        lo[x] = interior ? lo_encode64(hi, u - (double)hi) : (int8_t)0;
+    }
+}
+__global__ void k_narrow_wide(const double* s, float* d, int8_t* lo, int64_t n, StepDims dm) {
+    const int64_t lane2 = 2 * (threadIdx.x & 31);
+    for (int64_t w0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32 * kWide; w0 < n;
+         w0 += (((int64_t)gridDim.x * blockDim.x) >> 5) * 32 * kWide) {
+        double2 v[kWide / 2];
+#pragma unroll
+        for (int q = 0; q < kWide / 2; ++q)
+            if ((w0 + 64 * q + lane2) < n) v[q] = *reinterpret_cast<const double2*>(s + host_index((w0 + 64 * q + lane2), dm.ncell));
+#pragma unroll
+        for (int q = 0; q < kWide / 2; ++q)
+            if ((w0 + 64 * q + lane2) < n) {
+                narrow_one(v[q].x, (w0 + 64 * q + lane2), d, lo, dm);
+                narrow_one(v[q].y, (w0 + 64 * q + lane2) + 1, d, lo, dm);
+            }
+    }
+}
+__device__ __forceinline__ int64_t psi_host_index(int64_t x, int64_t ncell) {   // psi element -> host element
+    const int64_t b = x / ncell;
+    return (b * (NV + 1) + NV) * ncell + (x - b * ncell);
+}
+__global__ void k_narrow_psi_wide(const double* s, float* psi, int64_t nb, int64_t ncell) {
+    const int64_t n = nb * ncell;
+    const int64_t lane2 = 2 * (threadIdx.x & 31);
+    for (int64_t w0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32 * kWide; w0 < n;
+         w0 += (((int64_t)gridDim.x * blockDim.x) >> 5) * 32 * kWide) {
+        double2 v[kWide / 2];
+#pragma unroll
+        for (int q = 0; q < kWide / 2; ++q)
+            if ((w0 + 64 * q + lane2) < n) v[q] = *reinterpret_cast<const double2*>(s + psi_host_index((w0 + 64 * q + lane2), ncell));
+#pragma unroll
+        for (int q = 0; q < kWide / 2; ++q)
+            if ((w0 + 64 * q + lane2) < n) {
+                psi[(w0 + 64 * q + lane2)] = (float)v[q].x;
+                psi[(w0 + 64 * q + lane2) + 1] = (float)v[q].y;
+            }
+    }
+}
+__global__ void k_psi_nonzero_wide(const double* s, int64_t nb, int64_t ncell, int32_t* flag) {
+    const int64_t n = nb * ncell;
+    int any = 0;
+    const int64_t lane2 = 2 * (threadIdx.x & 31);
+    for (int64_t w0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32 * kWide; w0 < n;
+         w0 += (((int64_t)gridDim.x * blockDim.x) >> 5) * 32 * kWide) {
+        double2 v[kWide / 2];
+#pragma unroll
+        for (int q = 0; q < kWide / 2; ++q)
+            if ((w0 + 64 * q + lane2) < n) v[q] = *reinterpret_cast<const double2*>(s + psi_host_index((w0 + 64 * q + lane2), ncell));
+#pragma unroll
+        for (int q = 0; q < kWide / 2; ++q)
+            if ((w0 + 64 * q + lane2) < n) any |= (v[q].x != 0.0) | (v[q].y != 0.0);
+    }
+    if (__any_sync(0xffffffffu, any) && (threadIdx.x & 31) == 0) *flag = 1;
+}
+template <class T>
+__device__ __forceinline__ double gather_one(const T* U, const int8_t* lo, const T* psi, int64_t h, int64_t ncell) {
+    const int64_t b = h / ((NV + 1) * ncell), r = h - b * (NV + 1) * ncell;
+    if (r < NV * ncell) {
+        const int64_t e = b * NV * ncell + r;
+        const T hi = U[e];
+        double v = (double)hi;
+        if constexpr (sizeof(T) == 4) {
+            if (lo) v += (double)lo[e] * (double)lo_unit((float)hi);
+        }
+        return v;
+    }
+    return psi ? (double)psi[b * ncell + (r - NV * ncell)] : 0.0;
+}
+template <class T>
+__global__ void k_gather_host_wide(const T* U, const int8_t* lo, const T* psi, int64_t first, int64_t count,
+                                   int64_t ncell, double* out) {
+    const int64_t lane2 = 2 * (threadIdx.x & 31);
+    for (int64_t w0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32 * kWide; w0 < count;
+         w0 += (((int64_t)gridDim.x * blockDim.x) >> 5) * 32 * kWide) {
+        double2 v[kWide / 2];
+#pragma unroll
+        for (int q = 0; q < kWide / 2; ++q)
+            if ((w0 + 64 * q + lane2) < count) {
+                v[q].x = gather_one(U, lo, psi, first + (w0 + 64 * q + lane2), ncell);
+                v[q].y = gather_one(U, lo, psi, first + (w0 + 64 * q + lane2) + 1, ncell);
+            }
+#pragma unroll
+        for (int q = 0; q < kWide / 2; ++q)
+            if ((w0 + 64 * q + lane2) < count) *reinterpret_cast<double2*>(out + (w0 + 64 * q + lane2)) = v[q];
+    }
+}
+bool wide_ok(const void* p, int64_t ncell) { return ((uintptr_t)p % 16) == 0 && ncell % 2 == 0; }
+
 cudaError_t launch_convert_state(const double* src, float* dst, int8_t* lo, int64_t n, const StepDims& dm,
                                  cudaStream_t st) {
-    k_narrow<<<1216, 256, 0, st>>>(src, dst, lo, n, dm);
+    if (wide_ok(src, dm.ncell) && n % 2 == 0) k_narrow_wide<<<1216, 256, 0, st>>>(src, dst, lo, n, dm);
+    else k_narrow<<<1216, 256, 0, st>>>(src, dst, lo, n, dm);
     return cudaGetLastError();
 }
 cudaError_t launch_convert_psi(const double* src, float* psi, int64_t nb, int64_t ncell, cudaStream_t st) {
-    k_narrow_psi<<<1216, 256, 0, st>>>(src, psi, nb, ncell);
+    if (wide_ok(src, ncell)) k_narrow_psi_wide<<<1216, 256, 0, st>>>(src, psi, nb, ncell);
+    else k_narrow_psi<<<1216, 256, 0, st>>>(src, psi, nb, ncell);
     return cudaGetLastError();
 }
 cudaError_t launch_psi_nonzero(const double* src, int64_t nb, int64_t ncell, int32_t* flag, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int32_t), st);
     if (e != cudaSuccess) return e;
-    k_psi_nonzero<<<1216, 256, 0, st>>>(src, nb, ncell, flag);
+    if (wide_ok(src, ncell)) k_psi_nonzero_wide<<<1216, 256, 0, st>>>(src, nb, ncell, flag);
+    else k_psi_nonzero<<<1216, 256, 0, st>>>(src, nb, ncell, flag);
     return cudaGetLastError();
 }
 cudaError_t launch_gather_host(const void* U, const int8_t* lo, const void* psi, bool fp32, int64_t first, int64_t count,
                                int64_t ncell, double* out, cudaStream_t st) {
-    if (fp32) k_gather_host<float><<<1216, 256, 0, st>>>((const float*)U, lo, (const float*)psi, first, count, ncell, out);
-    else k_gather_host<double><<<1216, 256, 0, st>>>((const double*)U, nullptr, (const double*)psi, first, count, ncell, out);
+    const bool wide = wide_ok(out, ncell) && first % 2 == 0 && count % 2 == 0;
+    if (fp32) {
+        if (wide) k_gather_host_wide<float><<<1216, 256, 0, st>>>((const float*)U, lo, (const float*)psi, first, count, ncell, out);
+        else k_gather_host<float><<<1216, 256, 0, st>>>((const float*)U, lo, (const float*)psi, first, count, ncell, out);
+    } else {
+        if (wide)
+            k_gather_host_wide<double><<<1216, 256, 0, st>>>((const double*)U, nullptr, (const double*)psi, first, count,
+                                                             ncell, out);
+        else
+            k_gather_host<double><<<1216, 256, 0, st>>>((const double*)U, nullptr, (const double*)psi, first, count, ncell,
+                                                        out);
+    }
     return cudaGetLastError();
 }
 
