@@ -53,13 +53,19 @@ struct falcon_ctx {
     StepScalars* sc = nullptr;
     GhostLists gl{};          // every ghost cell (the exchange after the diffusion pass)
     GhostLists gl_stage{};    // face ghosts not pushed by the stage kernel (exchanges after stages)
+    GhostLists gl_final{};    // mixed: every ghost entry not pushed by the diffusion pass (end of a step)
     PushTable push{};         // mixed path: faces the stage kernel writes into its output
     void* R2 = nullptr;       // mixed path: second stage buffer (pushing needs out != in)
     int64_t ghost_counts[3] = {0, 0, 0};   // copy, 1-D, general entries on the device
     int64_t stage_counts[3] = {0, 0, 0};   // the same for the stage exchanges
+    int64_t final_counts[3] = {0, 0, 0};   // the same for the exchange ending a mixed step
     int64_t pushed_faces = 0, pushed_cells = 0;
     int kpar_stage = 0, kpar_diff = 0;      // chosen by the autotuner (0 = not tuned yet)
-    cudaGraphExec_t graph = nullptr;
+    // step graphs: the mixed step writes u^{n+1} into the second stage buffer
+    // and the two buffers swap roles, so one graph per assignment (index 0
+    // while U is the first allocation)
+    cudaGraphExec_t graphs[2] = {nullptr, nullptr};
+    void* bufA = nullptr;
     int64_t steps_done = 0;
     int64_t dev_bytes = 0;
     // timing
@@ -187,7 +193,7 @@ cudaError_t stage(falcon_ctx* ctx, int s, void* in, void* out, const PushTable& 
 
 // Artificial diffusion of every variable (ModAdvance.f90:101-109); psi's runs
 // first, from the same pre-diffusion state, into P2.
-cudaError_t diffusion(falcon_ctx* ctx) {
+cudaError_t diffusion(falcon_ctx* ctx, void* out, const PushTable& push) {
     cudaError_t e = cudaSuccess;
     if (ctx->P) {
         e = timed(ctx, KN_DIFF, [&] {
@@ -199,8 +205,8 @@ cudaError_t diffusion(falcon_ctx* ctx) {
         if (e != cudaSuccess) return e;
     }
     e = timed(ctx, KN_DIFF, [&] {
-        return ctx->mixed() ? launch_diffusion_mixed(ctx->dims, ctx->geom(), (float*)ctx->U, ctx->Ulo, ctx->sc,
-                                                     ctx->kpar_diff, ctx->st)
+        return ctx->mixed() ? launch_diffusion_mixed(ctx->dims, ctx->geom(), (const float*)ctx->U, (float*)out,
+                                                     ctx->Ulo, push, ctx->sc, ctx->kpar_diff, ctx->st)
                             : launch_diffusion_fp64(ctx->dims, ctx->geom(), (double*)ctx->U, ctx->sc, ctx->kpar_diff, ctx->st);
     });
     if (e != cudaSuccess || !ctx->P) return e;
@@ -236,9 +242,31 @@ cudaError_t enqueue_step(falcon_ctx* ctx) {
         e = ghost_stage(ctx, out);
         if (e != cudaSuccess) return e;
     }
-    e = diffusion(ctx);
+    if (ctx->mixed() && ctx->R2) {
+        // u^{n+1} into the second stage buffer, regular faces pushed by the
+        // diffusion pass, then the remaining ghost entries; end_step swaps
+        // the two buffers' roles
+        e = diffusion(ctx, ctx->R2, ctx->push);
+        if (e != cudaSuccess) return e;
+        return timed(ctx, KN_GHOST, [&] { return launch_ghost_mixed(ctx->dims, ctx->gl_final, (float*)ctx->R2, ctx->st); });
+    }
+    e = diffusion(ctx, ctx->U, PushTable{});
     if (e != cudaSuccess) return e;
     return ghost(ctx, ctx->U);
+}
+
+// After a step has been enqueued: the mixed step left u^{n+1} in R2.
+void end_step(falcon_ctx* ctx) {
+    if (ctx->mixed() && ctx->R2) std::swap(ctx->U, ctx->R2);
+}
+
+// The second stage buffer starts as a copy of the state: cells that no
+// kernel writes (ghost cells outside every exchange list) then agree in both
+// buffers whichever holds the state.
+cudaError_t mirror_state(falcon_ctx* ctx) {
+    if (!ctx->R2) return cudaSuccess;
+    return cudaMemcpyAsync(ctx->R2, ctx->U, (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell * ctx->elem,
+                           cudaMemcpyDeviceToDevice, ctx->st);
 }
 
 // Autotuner: time every instantiated k-chunk depth of the stage and diffusion
@@ -268,8 +296,8 @@ int autotune(falcon_ctx* ctx) {
                                                          (double*)ctx->RK, psi_args(ctx, 2), 2, 1,
                                                          ctx->sc, 1, kp, ctx->st);
                 else
-                    e = ctx->mixed() ? launch_diffusion_mixed(ctx->dims, ctx->geom(), (float*)ctx->RK, nullptr, ctx->sc, kp,
-                                                              ctx->st)
+                    e = ctx->mixed() ? launch_diffusion_mixed(ctx->dims, ctx->geom(), (const float*)ctx->RK,
+                                                              (float*)ctx->RK, nullptr, PushTable{}, ctx->sc, kp, ctx->st)
                                      : launch_diffusion_fp64(ctx->dims, ctx->geom(), (double*)ctx->RK, ctx->sc, kp, ctx->st);
                 cudaEventRecord(b, ctx->st);
                 if (e != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess) { ok = false; cudaGetLastError(); break; }
@@ -333,6 +361,7 @@ int setup_device(falcon_ctx* ctx) {
     ctx->elem = ctx->mixed() ? 4 : 8;
     const size_t sbytes = (size_t)nb * NV * g.ncell * ctx->elem;
     CK(ctx->alloc(&ctx->U, sbytes), "alloc U");
+    ctx->bufA = ctx->U;
     CK(ctx->alloc(&ctx->RK, sbytes), "alloc RK");
     CK(cudaMemsetAsync(ctx->U, 0, sbytes, ctx->st), "memset");
     CK(cudaMemsetAsync(ctx->RK, 0, sbytes, ctx->st), "memset");
@@ -574,6 +603,7 @@ int setup_device(falcon_ctx* ctx) {
         return cudaSuccess;
     };
     CK(build_lists([&](size_t) { return true; }, ctx->gl, ctx->ghost_counts), "upload ghosts");
+    if (snap) CK(build_lists([&](size_t k) { return !pushed[k]; }, ctx->gl_final, ctx->final_counts), "upload final ghosts");
     CK(build_lists([&](size_t k) { return ges[k].face >= 0 && !pushed[k]; }, ctx->gl_stage, ctx->stage_counts),
        "upload stage ghosts");
     if (snap) {
@@ -629,7 +659,8 @@ void falcon_destroy(falcon_ctx* ctx) {
     if (ctx->on_device) {
         cudaSetDevice(ctx->device);
         cudaStreamSynchronize(ctx->st);
-        if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+        for (cudaGraphExec_t& gx : ctx->graphs)
+            if (gx) cudaGraphExecDestroy(gx);
         for (auto& r : ctx->pending) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
         for (auto e : ctx->pool) cudaEventDestroy(e);
         for (void* p : ctx->allocs) cudaFree(p);
@@ -786,6 +817,7 @@ int falcon_upload_state(falcon_ctx* ctx, const double* u) {
     // primitive_rk_IV = primitive_IV, as the reference's initialisation leaves it
     const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
     CK(cudaMemcpyAsync(ctx->RK, ctx->U, n * ctx->elem, cudaMemcpyDeviceToDevice, ctx->st), "upload");
+    CK(mirror_state(ctx), "upload");
     // psi's stage array and the scratch it is copied from start equal too:
     // their ghost cells that no exchange writes (the radial boundary planes)
     // then stay at the uploaded values, as the reference's arrays do.
@@ -855,6 +887,7 @@ int falcon_init_synthetic(falcon_ctx* ctx, int32_t kind, uint64_t seed, double m
     if (ctx->Ulo) CK(cudaMemsetAsync(ctx->Ulo, 0, (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell, ctx->st), "init");
     const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
     CK(cudaMemcpyAsync(ctx->RK, ctx->U, n * ctx->elem, cudaMemcpyDeviceToDevice, ctx->st), "init");
+    CK(mirror_state(ctx), "init");
     CK(cudaStreamSynchronize(ctx->st), "init");
     return FALCON_OK;
 }
@@ -890,22 +923,25 @@ static int run(falcon_ctx* ctx, int32_t n) {
     if (ctx->ktiming) {
         for (int32_t s = 0; s < n; ++s) {
             CK(enqueue_step(ctx), "step");
+            end_step(ctx);
             ++ctx->steps_done;
         }
         return FALCON_OK;
     }
-    if (!ctx->graph) {
-        cudaGraph_t gr;
-        CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal), "capture");
-        cudaError_t e = enqueue_step(ctx);
-        cudaError_t e2 = cudaStreamEndCapture(ctx->st, &gr);
-        if (e != cudaSuccess) return ctx->cuda_fail(e, "capture step");
-        if (e2 != cudaSuccess) return ctx->cuda_fail(e2, "end capture");
-        CK(cudaGraphInstantiate(&ctx->graph, gr, 0), "instantiate");
-        cudaGraphDestroy(gr);
-    }
     for (int32_t s = 0; s < n; ++s) {
-        CK(cudaGraphLaunch(ctx->graph, ctx->st), "graph launch");
+        cudaGraphExec_t& gx = ctx->graphs[ctx->U == ctx->bufA ? 0 : 1];
+        if (!gx) {
+            cudaGraph_t gr;
+            CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal), "capture");
+            cudaError_t e = enqueue_step(ctx);
+            cudaError_t e2 = cudaStreamEndCapture(ctx->st, &gr);
+            if (e != cudaSuccess) return ctx->cuda_fail(e, "capture step");
+            if (e2 != cudaSuccess) return ctx->cuda_fail(e2, "end capture");
+            CK(cudaGraphInstantiate(&gx, gr, 0), "instantiate");
+            cudaGraphDestroy(gr);
+        }
+        CK(cudaGraphLaunch(gx, ctx->st), "graph launch");
+        end_step(ctx);
         ++ctx->steps_done;
     }
     return FALCON_OK;
@@ -948,7 +984,7 @@ int falcon_step_phase(falcon_ctx* ctx, int32_t phase) {
         e = stage(ctx, s, in, out, PushTable{});
         if (e == cudaSuccess) e = ghost(ctx, out);
     } else {
-        e = diffusion(ctx);
+        e = diffusion(ctx, ctx->U, PushTable{});
         if (e == cudaSuccess) e = ghost(ctx, ctx->U);
         if (e == cudaSuccess) ++ctx->steps_done;
     }
@@ -1205,6 +1241,7 @@ int falcon_load_restart(falcon_ctx* ctx, const char* path) {
     if (!ok) return ctx->fail(FALCON_ERR_INVALID_ARG, std::string("restart ") + path + ": short read");
     // the stage arrays start equal to the state, as after falcon_upload_state
     CK(cudaMemcpyAsync(ctx->RK, ctx->U, h.bytes_state, cudaMemcpyDeviceToDevice, ctx->st), "restart");
+    CK(mirror_state(ctx), "restart");
     if (ctx->P)
         for (void* q : {ctx->Prk, ctx->P2})
             CK(cudaMemcpyAsync(q, ctx->P, h.bytes_psi, cudaMemcpyDeviceToDevice, ctx->st), "restart");

@@ -197,8 +197,11 @@ cudaError_t launch_stage_mixed(const StepDims& d, const Geometry& g, const float
 cudaError_t launch_psi_diffusion_mixed(const StepDims& d, const Geometry& g, const float* u, const float* psi,
                                        float* psi_out, StepScalars* sc, cudaStream_t st);
 cudaError_t launch_psi_ghost_mixed(const StepDims& d, const GhostLists& gl, float* psi, cudaStream_t st);
-cudaError_t launch_diffusion_mixed(const StepDims& d, const Geometry& g, float* u, int8_t* lo, StepScalars* sc,
-                                   int kpar, cudaStream_t st);
+// diffusion of u into out: in place (out == u, push.tgt == nullptr) or out of
+// place with the regular faces pushed into out and the radial boundary ghost
+// columns copied (see k_diffusion)
+cudaError_t launch_diffusion_mixed(const StepDims& d, const Geometry& g, const float* u, float* out, int8_t* lo,
+                                   const PushTable& push, StepScalars* sc, int kpar, cudaStream_t st);
 cudaError_t launch_cfl_mixed(const StepDims& d, const Geometry& g, const float* u, StepScalars* sc,
                              cudaStream_t st);
 cudaError_t launch_ghost_mixed(const StepDims& d, const GhostLists& gl, float* u, cudaStream_t st);

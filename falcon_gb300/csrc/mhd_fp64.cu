@@ -23,7 +23,7 @@ cudaError_t launch_psi_ghost_fp64(const StepDims& d, const GhostLists& gl, doubl
 }
 cudaError_t launch_diffusion_fp64(const StepDims& d, const Geometry& g, double* u, StepScalars* sc,
                                   int kpar, cudaStream_t st) {
-    return diff_any<double>(d, g, u, nullptr, sc, kpar, st);
+    return diff_any<double>(d, g, u, u, nullptr, PushTable{}, sc, kpar, st);
 }
 cudaError_t launch_cfl_fp64(const StepDims& d, const Geometry& g, const double* u, StepScalars* sc, cudaStream_t st) {
     return cfl_any<double>(d, g, u, sc, st);

@@ -232,24 +232,24 @@ __device__ __forceinline__ double blend(double a, double b, double uw, double w)
 // blends it with the next cell along i, taken from the next lane (i is the
 // fastest thread index, and the second cell is never beyond the row). Every
 // thread of the CTA calls this (the shuffle needs the full warp).
-template <class T, class S>
-__device__ __forceinline__ void push_faces(T* out, const PushTable& P, int b, int ii, int jj, int kp,
-                                           const T (&o)[NV]) {
-    constexpr int NI = S::NIP - 4, NJ = S::NJP - 4, NK = S::NKP - 4;
+template <class T, class S, int VN>
+__device__ __forceinline__ void push_faces_part(T* out, const PushTable& P, int b, int ii, int jj, int kp,
+                                                const T (&o)[VN], int v0) {
+    constexpr int NJ = S::NJP - 4, NK = S::NKP - 4;
     const int32_t* tg = P.tgt + 6 * b;
-    auto put = [&](int tb, int kt, int jt, int it, const T (&val)[NV]) {
-        T* dst = out + (size_t)tb * NV * S::NCELL + ((size_t)kt * S::NJP + jt) * S::NIP + it;
+    auto put = [&](int tb, int kt, int jt, int it, const T (&val)[VN]) {
+        T* dst = out + ((size_t)tb * NV + v0) * S::NCELL + ((size_t)kt * S::NJP + jt) * S::NIP + it;
 #pragma unroll
-        for (int v = 0; v < NV; ++v) dst[(size_t)v * S::NCELL] = val[v];
+        for (int v = 0; v < VN; ++v) dst[(size_t)v * S::NCELL] = val[v];
     };
     if (jj <= 3 && tg[2] >= 0) put(tg[2], kp, jj + NJ, ii, o);
     if (jj >= NJ && tg[3] >= 0) put(tg[3], kp, jj - NJ, ii, o);
     if (kp <= 3 && tg[4] >= 0) put(tg[4], kp + NK, jj, ii, o);
     if (kp >= NK && tg[5] >= 0) put(tg[5], kp - NK, jj, ii, o);
     if (tg[0] >= 0 || tg[1] >= 0) {   // uniform over the CTA
-        T nx[NV];
+        T nx[VN];
 #pragma unroll
-        for (int v = 0; v < NV; ++v) nx[v] = __shfl_down_sync(0xffffffffu, o[v], 1);
+        for (int v = 0; v < VN; ++v) nx[v] = __shfl_down_sync(0xffffffffu, o[v], 1);
 #pragma unroll
         for (int side = 0; side < 2; ++side) {
             if (tg[side] < 0) continue;
@@ -258,14 +258,18 @@ __device__ __forceinline__ void push_faces(T* out, const PushTable& P, int b, in
                 const int q = (b * 2 + side) * 2 + layer;
                 if (ii != P.rad_src[q]) continue;
                 const T w = (T)P.rad_w[q], uw = T(1) - w;
-                T val[NV];
+                T val[VN];
 #pragma unroll
-                for (int v = 0; v < NV; ++v) val[v] = w == T(0) ? o[v] : blend(o[v], nx[v], uw, w);
+                for (int v = 0; v < VN; ++v) val[v] = w == T(0) ? o[v] : blend(o[v], nx[v], uw, w);
                 put(tg[side], kp, jj, P.rad_dst[q], val);
             }
         }
     }
-    (void)NI;
+}
+template <class T, class S>
+__device__ __forceinline__ void push_faces(T* out, const PushTable& P, int b, int ii, int jj, int kp,
+                                           const T (&o)[NV]) {
+    push_faces_part<T, S, NV>(out, P, b, ii, jj, kp, o, 0);
 }
 
 // Cell (i, j, kq) of a thread in a k-chunk. With 16-wide rows and an even
@@ -627,9 +631,16 @@ __device__ __forceinline__ T face_flux(T fm, T fl, T fr, T fp, T cL, T cR) {
     return f * (cR + cL) * T(0.5);
 }
 
+//
+// In place (out == u), or out of place into `out` (mixed step): then the
+// kernel also writes the regular ghost faces of its neighbours in `out`
+// (push, as the stage kernel does) and copies the radial physical-boundary
+// ghost columns (set by the boundary condition at stage 1) from u to out, so
+// that with an exchange of the remaining ghost entries `out` holds the whole
+// updated state.
 template <class T, int NI, int NJ, int NK, int KPAR>
 __global__ void __launch_bounds__(DShape<T, NI, NJ, NK, KPAR>::NT, (DShape<T, NI, NJ, NK, KPAR>::min_blocks))
-k_diffusion(T* u, int8_t* ulo, Geometry g, StepScalars* sc) {
+k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepScalars* sc) {
     using S = DShape<T, NI, NJ, NK, KPAR>;
     static_assert(S::fits, "diffusion shared memory above 227 KB");
     constexpr int NIP = S::NIP, PL = S::PL, W = S::W, NCELL = S::NCELL, KS = S::KS;
@@ -643,7 +654,9 @@ k_diffusion(T* u, int8_t* ulo, Geometry g, StepScalars* sc) {
     T* gj = reinterpret_cast<T*>(smem + S::off_gj);
     T* gs = reinterpret_cast<T*>(smem + S::off_gs);
     const int b = blockIdx.x;
-    T* blk = u + (size_t)b * NV * NCELL;
+    const T* blk = u + (size_t)b * NV * NCELL;
+    T* oblk = out + (size_t)b * NV * NCELL;
+    const bool copy_bc = out != u && (g.flags[b] & 6);
     if (threadIdx.x == 0) {
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
@@ -686,6 +699,18 @@ k_diffusion(T* u, int8_t* ulo, Geometry g, StepScalars* sc) {
         }
         const int kp0 = k0 + 1;   // padded index of the chunk's first plane
         const int kp = kp0 + kq;
+        if (copy_bc) {   // radial boundary ghost columns of the planes new to this chunk
+            const int plo = ch == 0 ? 0 : k0 + 3, phi = k0 + KPAR + 3, fl = g.flags[b];
+            const int total = (phi - plo) * S::NJP * NV * 4;
+            for (int x = tid; x < total; x += S::NT) {
+                const int c4 = x & 3, r = x >> 2;
+                const int v = r % NV, r2 = r / NV;
+                const int y = r2 % S::NJP, z = plo + r2 / S::NJP;
+                if (!((c4 < 2) ? (fl & 4) : (fl & 2))) continue;
+                const int xi = c4 < 2 ? c4 : NI + c4;   // 0, 1 (bottom) or NI+2, NI+3 (top)
+                oblk[((size_t)v * S::NKP + z) * PL + y * NIP + xi] = tile[(v * W + z % W) * PL + y * NIP + xi];
+            }
+        }
         // ring offsets of planes kp-2 .. kp+2
         int so[5];
         so[0] = ((kp - 2) % W) * PL;
@@ -747,6 +772,7 @@ k_diffusion(T* u, int8_t* ulo, Geometry g, StepScalars* sc) {
         const size_t base = (size_t)kp * PL + jj * NIP + ii;
         const T* fk_l = FK + ((size_t)((kp - 2) % KS) * NV) * NJ * NI + j * NI + i;
         const T* fk_r = FK + ((size_t)((kp - 1) % KS) * NV) * NJ * NI + j * NI + i;
+        T o[S::VPT];
 #pragma unroll
         for (int t = 0; t < S::VPT; ++t) {
             const int v = v0 + t;
@@ -757,19 +783,20 @@ k_diffusion(T* u, int8_t* ulo, Geometry g, StepScalars* sc) {
             R = R + Pol<T>::dv(fj[0] - fj[NI], den[1], dinv[1]);
             R = R + Pol<T>::dv(fk_l[v * NJ * NI] - fk_r[v * NJ * NI], den[2], dinv[2]);
             const T u0 = t0[v * W * PL + so[2]];
-            if constexpr (!Pol<T>::exact) {
-                if (ulo != nullptr) {
-                    int8_t* q = ulo + (size_t)b * NV * NCELL + (size_t)v * NCELL + base;
-                    int8_t q1;
-                    blk[(size_t)v * NCELL + base] = ff_add((float)u0, *q, __fmul_rn(hdt_f, (float)R), q1);
-                    *q = q1;
-                    continue;
-                }
+            if constexpr (Pol<T>::exact) {
+                o[t] = (T)((double)u0 + hdt * (double)R);
+            } else if (ulo != nullptr) {
+                int8_t* q = ulo + (size_t)b * NV * NCELL + (size_t)v * NCELL + base;
+                int8_t q1;
+                o[t] = ff_add((float)u0, *q, __fmul_rn(hdt_f, (float)R), q1);
+                *q = q1;
+            } else {
+                o[t] = fmaf(hdt_f, (float)R, (float)u0);
             }
-            T o;
-            if constexpr (Pol<T>::exact) o = (T)((double)u0 + hdt * (double)R);
-            else o = fmaf(hdt_f, (float)R, (float)u0);
-            blk[(size_t)v * NCELL + base] = o;
+            oblk[(size_t)v * NCELL + base] = o[t];
+        }
+        if constexpr (!Pol<T>::exact) {
+            if (push.tgt != nullptr) push_faces_part<T, S, S::VPT>(out, push, b, ii, jj, kp, o, v0);
         }
     }
 }
