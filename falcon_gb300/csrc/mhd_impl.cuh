@@ -325,9 +325,13 @@ k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, DivBArgs 
     // stages 2-4: warm L2 with the planes of the first chunk, then one chunk ahead
     const T* blk_un = un + (size_t)b * NV * NCELL;
     const int8_t* blk_lo = ulo != nullptr ? ulo + (size_t)b * NV * NCELL : nullptr;
+    T* blk_out = out + (size_t)b * NV * NCELL;
     auto prefetch_un = [&](int kp_first) {
-        if (stage == 1 || threadIdx.x >= NV) return;
+        if (threadIdx.x >= NV) return;
         const int v = threadIdx.x;
+        // the output rows are written in part (interior cells only): their lines into L2 first
+        if (out != un || stage == 1) prefetch_l2(blk_out + ((size_t)v * S::NKP + kp_first) * PL, KPAR * S::PLB);
+        if (stage == 1) return;
         prefetch_l2(blk_un + ((size_t)v * S::NKP + kp_first) * PL, KPAR * S::PLB);
         if (blk_lo != nullptr && stage == 4) prefetch_l2(blk_lo + ((size_t)v * S::NKP + kp_first) * PL, KPAR * PL);
     };
@@ -668,8 +672,11 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
     // first chunk's planes, then one chunk ahead
     const int8_t* blk_lo = ulo != nullptr ? ulo + (size_t)b * NV * NCELL : nullptr;
     auto prefetch_lo = [&](int kp_first) {
-        if (blk_lo == nullptr || threadIdx.x >= NV) return;
-        prefetch_l2(blk_lo + ((size_t)threadIdx.x * S::NKP + kp_first) * PL, KPAR * PL);
+        if (threadIdx.x >= NV) return;
+        if (blk_lo != nullptr) prefetch_l2(blk_lo + ((size_t)threadIdx.x * S::NKP + kp_first) * PL, KPAR * PL);
+        // out of place: the output rows are written in part (interior cells
+        // only), so bring their lines into L2 first
+        if (out != u) prefetch_l2(oblk + ((size_t)threadIdx.x * S::NKP + kp_first) * PL, KPAR * S::PLB);
     };
     prefetch_lo(2);
     load_geometry<T, S>(g, b, gi, gj, gs, nullptr);
