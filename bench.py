@@ -228,7 +228,9 @@ def run_ours(args, rank, world, local, dist):
     from falcon_gb300 import config
     fg.build()
     cfg = config.shell_mixed_21m(device=local) if args.workload == "full" else small_config(local)
-    f = fg.Falcon(cfg)
+    t_setup = time.perf_counter()
+    f = fg.Falcon(cfg)   # tree, block geometry, ghost map (host), device tables and lists
+    setup_s = time.perf_counter() - t_setup
     cells = f.interior_cells
     f.init_synthetic(kind=1, seed=1002, mach=0.01)
     f.exchange()
@@ -331,6 +333,7 @@ def run_ours(args, rank, world, local, dist):
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                     "mode": "state uploaded and downloaded (FP64, pinned) every step"},
+            "setup_s": round(setup_s, 3),
             "e2e_resident": {"value": res_val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 8},
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clk,
