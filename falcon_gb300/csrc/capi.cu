@@ -53,7 +53,8 @@ struct falcon_ctx {
     StepScalars* sc = nullptr;
     GhostLists gl{};          // every ghost cell (the exchange after the diffusion pass)
     GhostLists gl_stage{};    // face ghosts not pushed by the stage kernel (exchanges after stages)
-    GhostLists gl_final{};    // mixed: every ghost entry not pushed by the diffusion pass (end of a step)
+    GhostLists gl_final{};    // mixed: ghost entries the exchange ending a step fills (see setup_device)
+    bool stale_edges = false; // mixed: edge/corner ghosts not refreshed since the last step
     PushTable push{};         // mixed path: faces the stage kernel writes into its output
     void* R2 = nullptr;       // mixed path: second stage buffer (pushing needs out != in)
     int64_t ghost_counts[3] = {0, 0, 0};   // copy, 1-D, general entries on the device
@@ -255,9 +256,23 @@ cudaError_t enqueue_step(falcon_ctx* ctx) {
     return ghost(ctx, ctx->U);
 }
 
-// After a step has been enqueued: the mixed step left u^{n+1} in R2.
+// After a step has been enqueued: the mixed step left u^{n+1} in R2, with
+// edge and corner ghosts not refreshed.
 void end_step(falcon_ctx* ctx) {
-    if (ctx->mixed() && ctx->R2) std::swap(ctx->U, ctx->R2);
+    if (ctx->mixed() && ctx->R2) {
+        std::swap(ctx->U, ctx->R2);
+        ctx->stale_edges = true;
+    }
+}
+
+// Before the state is read from outside the step: complete its ghost cells.
+// Every ghost entry is a function of interior cells only, so this gives the
+// values the reference's exchange would have left.
+cudaError_t fresh_state(falcon_ctx* ctx) {
+    if (!ctx->stale_edges) return cudaSuccess;
+    cudaError_t e = ghost(ctx, ctx->U);
+    if (e == cudaSuccess) ctx->stale_edges = false;
+    return e;
 }
 
 // The second stage buffer starts as a copy of the state: cells that no
@@ -603,7 +618,22 @@ int setup_device(falcon_ctx* ctx) {
         return cudaSuccess;
     };
     CK(build_lists([&](size_t) { return true; }, ctx->gl, ctx->ghost_counts), "upload ghosts");
-    if (snap) CK(build_lists([&](size_t k) { return !pushed[k]; }, ctx->gl_final, ctx->final_counts), "upload final ghosts");
+    // The exchange ending a mixed step: every face entry not pushed by the
+    // diffusion pass, plus the theta-phi edge ghosts of the two planes next to
+    // a radial boundary (the boundary condition of the next stage 1 mirrors
+    // those planes whole). No kernel of a step reads the other edge and
+    // corner ghosts; they are filled before the state is read (fresh_state).
+    if (snap) {
+        auto bc_edge = [&](const GE& q) {
+            const int fl = g.flags[q.tb];
+            const bool jg = q.t[1] < 1 || q.t[1] > n3[1], kg = q.t[2] < 1 || q.t[2] > n3[2];
+            if (!jg || !kg) return false;
+            return ((fl & 4) && (q.t[0] == 1 || q.t[0] == 2)) || ((fl & 2) && (q.t[0] == n3[0] || q.t[0] == n3[0] - 1));
+        };
+        CK(build_lists([&](size_t k) { return !pushed[k] && (ges[k].face >= 0 || bc_edge(ges[k])); }, ctx->gl_final,
+                       ctx->final_counts),
+           "upload final ghosts");
+    }
     CK(build_lists([&](size_t k) { return ges[k].face >= 0 && !pushed[k]; }, ctx->gl_stage, ctx->stage_counts),
        "upload stage ghosts");
     if (snap) {
@@ -814,6 +844,7 @@ int falcon_upload_state(falcon_ctx* ctx, const double* u) {
     if (!u) return ctx->fail(FALCON_ERR_INVALID_ARG, "null state");
     rc = put_state(ctx, u, ctx->U, ctx->Ulo, ctx->P);
     if (rc) return rc;
+    ctx->stale_edges = false;   // the uploaded ghost cells are the state's
     // primitive_rk_IV = primitive_IV, as the reference's initialisation leaves it
     const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
     CK(cudaMemcpyAsync(ctx->RK, ctx->U, n * ctx->elem, cudaMemcpyDeviceToDevice, ctx->st), "upload");
@@ -833,6 +864,7 @@ int falcon_download_state(falcon_ctx* ctx, double* u) {
     int rc = need_device(ctx);
     if (rc) return rc;
     if (!u) return ctx->fail(FALCON_ERR_INVALID_ARG, "null state");
+    CK(fresh_state(ctx), "ghost fill");
     return get_state(ctx, ctx->U, ctx->Ulo, ctx->P, u);
 }
 
@@ -840,6 +872,7 @@ int falcon_download_state_range(falcon_ctx* ctx, size_t first, size_t count, dou
     int rc = need_device(ctx);
     if (rc) return rc;
     if (!u && count) return ctx->fail(FALCON_ERR_INVALID_ARG, "null state");
+    CK(fresh_state(ctx), "ghost fill");
     const size_t n = host_elems(ctx);
     const size_t cap = static_scratch_elems();
     if (count > cap)
@@ -888,6 +921,7 @@ int falcon_init_synthetic(falcon_ctx* ctx, int32_t kind, uint64_t seed, double m
     const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
     CK(cudaMemcpyAsync(ctx->RK, ctx->U, n * ctx->elem, cudaMemcpyDeviceToDevice, ctx->st), "init");
     CK(mirror_state(ctx), "init");
+    ctx->stale_edges = false;
     CK(cudaStreamSynchronize(ctx->st), "init");
     return FALCON_OK;
 }
@@ -896,6 +930,7 @@ int falcon_exchange(falcon_ctx* ctx) {
     int rc = need_device(ctx);
     if (rc) return rc;
     CK(ghost(ctx, ctx->U), "ghost fill");
+    ctx->stale_edges = false;
     if (ctx->P)
         CK(ctx->mixed() ? launch_psi_ghost_mixed(ctx->dims, ctx->gl, (float*)ctx->P, ctx->st)
                         : launch_psi_ghost_fp64(ctx->dims, ctx->gl, (double*)ctx->P, ctx->st),
@@ -986,7 +1021,10 @@ int falcon_step_phase(falcon_ctx* ctx, int32_t phase) {
     } else {
         e = diffusion(ctx, ctx->U, PushTable{});
         if (e == cudaSuccess) e = ghost(ctx, ctx->U);
-        if (e == cudaSuccess) ++ctx->steps_done;
+        if (e == cudaSuccess) {
+            ++ctx->steps_done;
+            ctx->stale_edges = false;
+        }
     }
     if (e != cudaSuccess) return ctx->cuda_fail(e, "phase");
     CK(cudaStreamSynchronize(ctx->st), "phase");
@@ -1080,6 +1118,7 @@ int falcon_save_allcells(falcon_ctx* ctx, const char* directory, int32_t step) {
     int rc = need_device(ctx);
     if (rc) return rc;
     if (!directory) return ctx->fail(FALCON_ERR_INVALID_ARG, "null directory");
+    CK(fresh_state(ctx), "ghost fill");
     const Grid& g = ctx->grid;
     const StepDims& d = ctx->dims;
     const std::string dir = std::string(directory) + "/AllCells_" + i8_zero(step);
@@ -1171,6 +1210,7 @@ int falcon_save_restart(falcon_ctx* ctx, const char* path) {
     int rc = need_device(ctx);
     if (rc) return rc;
     if (!path) return ctx->fail(FALCON_ERR_INVALID_ARG, "null path");
+    CK(fresh_state(ctx), "ghost fill");
     CK(cudaStreamSynchronize(ctx->st), "restart");
     const RestartHeader h = restart_header(ctx);
     FILE* f = std::fopen(path, "wb");
@@ -1242,6 +1282,7 @@ int falcon_load_restart(falcon_ctx* ctx, const char* path) {
     // the stage arrays start equal to the state, as after falcon_upload_state
     CK(cudaMemcpyAsync(ctx->RK, ctx->U, h.bytes_state, cudaMemcpyDeviceToDevice, ctx->st), "restart");
     CK(mirror_state(ctx), "restart");
+    ctx->stale_edges = false;
     if (ctx->P)
         for (void* q : {ctx->Prk, ctx->P2})
             CK(cudaMemcpyAsync(q, ctx->P, h.bytes_psi, cudaMemcpyDeviceToDevice, ctx->st), "restart");
