@@ -384,9 +384,20 @@ k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, DivBArgs 
             mbar_wait(&bars[(ch + 1) & 1], (uint32_t)(((ch + 1) >> 1) & 1), kWaitPolls);
             return;
         }
-        apply_bc<T, S>(tile, lo, hi, fl, wb);
-        fence_proxy_async();   // order these generic writes before later bulk copies into the slots
-        __syncthreads();
+        // u^n for the update (stages 2-4), loaded here so that the latency of
+        // these plain loads overlaps the boundary and p1 phases below
+        const int kp = k0 + kq + 1;
+        const size_t base = (size_t)b * NV * NCELL + (size_t)kp * PL + jj * NIP + ii;
+        T u0s[NV];
+        if (stage != 1) {
+#pragma unroll
+            for (int v = 0; v < NV; ++v) u0s[v] = un[base + (size_t)v * NCELL];
+        }
+        if (fl & 6) {   // radial boundary block (uniform over the CTA)
+            apply_bc<T, S>(tile, lo, hi, fl, wb);
+            fence_proxy_async();   // order these generic writes before later bulk copies into the slots
+            __syncthreads();
+        }
         // p1 = gamma1*(p0/rho0)*rho1 + (gamma3-1)*(rho0*T0)*s1, assembled in FP64
         // (3_6/ModEquation.f90:40-46)
         for (int x = tid; x < (hi - lo) * PL; x += S::NT) {
@@ -405,8 +416,6 @@ k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, DivBArgs 
         }
         __syncthreads();
 
-        const int k = k0 + kq;
-        const int kp = k + 1;
         int sl[5], sp[5];
 #pragma unroll
         for (int d = 0; d < 5; ++d) { sl[d] = (kp + d - 2) % W; sp[d] = (kp + d - 2) % WP; }
@@ -419,16 +428,10 @@ k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, DivBArgs 
         const T vr = A(V_VR, 0, 0, 0), vt = A(V_VT, 0, 0, 0), vp = A(V_VP, 0, 0, 0);
         const T br = A(V_BR, 0, 0, 0), bt = A(V_BT, 0, 0, 0), bp = A(V_BP, 0, 0, 0);
         const T rho1 = A(V_RHO1, 0, 0, 0);
-        // u^n for the update, fetched before the stencil arithmetic so its
-        // latency overlaps it; at stage 1 the input is u^n and sits in the ring
-        const size_t base = (size_t)b * NV * NCELL + (size_t)kp * PL + jj * NIP + ii;
-        T u0s[NV];
+        // at stage 1 the input is u^n and sits in the ring
         if (stage == 1) {
 #pragma unroll
             for (int v = 0; v < NV; ++v) u0s[v] = A(v, 0, 0, 0);
-        } else {
-#pragma unroll
-            for (int v = 0; v < NV; ++v) u0s[v] = un[base + (size_t)v * NCELL];
         }
 
         // Mass conservation: -div(rho0 v)/Xi^2 (3_6/ModEquation.f90:50-61, ModSpherical_div :104-159)
