@@ -198,3 +198,42 @@ class Solver:
         d = C.c_double()
         self._ck(self.L.falcon_solver_timestep(self.h, C.byref(d)))
         return d.value
+
+
+def _main(argv=None):
+    """Command line: one heat-conduction or PFSS solve on a GPU, report printed.
+
+    python -m falcon_gb300.solver conduction --size 64 128 384 --tol 1e-8
+    python -m falcon_gb300.solver pfss --problems 4 --size 64 96 --tol 1e-10
+    """
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(prog="python -m falcon_gb300.solver")
+    ap.add_argument("kind", choices=["conduction", "pfss"])
+    ap.add_argument("--size", type=int, nargs="+", default=None,
+                    help="conduction: nr ntheta nphi per panel; pfss: nr ntheta")
+    ap.add_argument("--problems", type=int, default=1)
+    ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--max-iter", type=int, default=300)
+    ap.add_argument("--precond", choices=["mg", "none"], default="mg")
+    ap.add_argument("--solves", type=int, default=2, help="solves of the same system (the first warms up)")
+    ap.add_argument("--device", type=int, default=0)
+    a = ap.parse_args(argv)
+    from . import build
+    build()
+    if a.kind == "conduction":
+        nr, nt, np_ = a.size or (64, 128, 384)
+        spec = conduction_spec(nr=nr, nt=nt, np_=np_, device=a.device)
+    else:
+        nr, nt = a.size or (64, 96)
+        spec = pfss_spec([(nr, nt)] * a.problems, device=a.device)
+    sv = Solver(spec)
+    pc = PRECOND_MG if a.precond == "mg" else PRECOND_NONE
+    for s in range(a.solves):
+        rep = sv.solve(tol=a.tol, max_iter=a.max_iter, precond=pc, check=False)
+        print(json.dumps({"solve": s, "cells": sv.nblocks * sv.nint, **rep}))
+    sv.close()
+
+
+if __name__ == "__main__":
+    _main()
