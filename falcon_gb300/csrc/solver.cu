@@ -4,8 +4,12 @@
 // (3_5/ModLinearSolver.f90:86-427) with the 7-point face-coefficient operator
 // (:15-84) and the 1-layer face-ghost halo (3_5/ModCommunication.f90:1497-1639).
 // GB300 form:
-//   - outer flexible CG in FP64 (dot products, residual norms and the true
-//     residual b-Ax in FP64), iterative refinement on the true residual;
+//   - outer flexible CG in float-float (FP32 pairs, about 48 bits; GB300's
+//     FP64 pipe is too slow for the per-cell work) on the system scaled by
+//     per-problem powers of two, per-problem dot products reduced into FP64,
+//     iterative refinement on the true residual; y = A x of
+//     falcon_solver_apply, the coarse training solve and the residual query
+//     stay FP64;
 //   - V-cycle preconditioner in FP32: red-black Gauss-Seidel smoothing,
 //     restriction R = P^T (sum of 8 children), injection prolongation,
 //     Galerkin coarse operators;
@@ -232,6 +236,219 @@ __global__ void k_update_p(LevelDims d, double* p, const double* z, Dots D, int 
     }
 }
 
+// ---- float-float outer iteration ------------------------------------------------
+// GB300 runs FP64 at a small fraction of its FP32 rate, and the FP64 outer
+// kernels above are bound by the FP64 pipe. The solve therefore runs the
+// flexible CG in float-float: every value an FP32 pair (hi, lo), hi + lo with
+// |lo| <= ulp(hi)/2, about 48 significant bits, formed with error-free FP32
+// transformations (this file is compiled without FMA contraction; the FMAs
+// below are explicit). FP32's exponent range is too narrow for the raw
+// system (b.b reaches 1e54 for conduction), so the solve works on
+// A' = A / sA, b' = b / sb, x' = x sA / sb per problem with sA, sb powers of
+// two (exact): every vector and dot product is then O(1).
+struct Ops2 { const float2 *Aii, *Ai, *Aj, *Ak; };
+constexpr double kEpsFF = 7.105427357601002e-15;   // 2^-47: unit roundoff of the FF pairs
+
+__device__ __forceinline__ float2 ff_quick(float s, float e) {
+    const float h = s + e;
+    return make_float2(h, e - (h - s));
+}
+__device__ __forceinline__ float2 ff_two_sum(float a, float b) {
+    const float s = a + b;
+    const float bb = s - a;
+    return make_float2(s, (a - (s - bb)) + (b - bb));
+}
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
+    float2 s = ff_two_sum(a.x, b.x);
+    const float2 t = ff_two_sum(a.y, b.y);
+    s.y += t.x;
+    s = ff_quick(s.x, s.y);
+    s.y += t.y;
+    return ff_quick(s.x, s.y);
+}
+__device__ __forceinline__ float2 ff_mul(float2 a, float2 b) {
+    const float p = a.x * b.x;
+    float e = fmaf(a.x, b.x, -p);
+    e = fmaf(a.x, b.y, e);
+    e = fmaf(a.y, b.x, e);
+    return ff_quick(p, e);
+}
+__device__ __forceinline__ float2 ff_neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 ff_from(double v) {   // a few FP64 operations: per thread, not per cell
+    const float h = (float)v;
+    return make_float2(h, (float)(v - (double)h));
+}
+__device__ __forceinline__ double ff_to(float2 a) { return (double)a.x + (double)a.y; }
+
+// per-problem FF sums -> one FP64 atomic per CTA (FP64 work once per warp)
+__device__ __forceinline__ void block_sum_atomic_ff(float2 v, double* slot) {
+    for (int o = 16; o > 0; o >>= 1)
+        v = ff_add(v, make_float2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o)));
+    __shared__ double ws[8];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = ff_to(v);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += ws[w];
+        atomicAdd(slot, t);
+    }
+    __syncthreads();
+}
+
+// y = A' x over the interior, the reference's operand order
+__device__ __forceinline__ float2 apply_A_ff(const Ops2& A, const LevelDims& d, const float2* x, int b, int c, int i,
+                                             int j, int k, float* absrow) {
+    const size_t P = pidx(d, b, i, j, k);
+    const size_t sj = d.p0, sk = (size_t)d.p0 * d.p1;
+    const size_t fi = ((size_t)b * d.m2 * d.m1 + (size_t)(k - 1) * d.m1 + (j - 1)) * (d.m0 + 1) + (i - 1);
+    const size_t fj = ((size_t)b * d.m2 * (d.m1 + 1) + (size_t)(k - 1) * (d.m1 + 1) + (j - 1)) * d.m0 + (i - 1);
+    const size_t fk = ((size_t)b * (d.m2 + 1) * d.m1 + (size_t)(k - 1) * d.m1 + (j - 1)) * d.m0 + (i - 1);
+    const float2 c7[7] = {A.Aii[(size_t)b * d.nint + c], A.Ai[fi], A.Ai[fi + 1], A.Aj[fj], A.Aj[fj + d.m0], A.Ak[fk],
+                          A.Ak[fk + (size_t)d.m0 * d.m1]};
+    const float2 x7[7] = {x[P], x[P - 1], x[P + 1], x[P - sj], x[P + sj], x[P - sk], x[P + sk]};
+    float2 y = ff_mul(c7[0], x7[0]);
+    float ar = fabsf(c7[0].x * x7[0].x);
+#pragma unroll
+    for (int t = 1; t < 7; ++t) {
+        y = ff_add(y, ff_mul(c7[t], x7[t]));
+        ar += fabsf(c7[t].x * x7[t].x);
+    }
+    if (absrow) *absrow = ar;
+    return y;
+}
+
+// Ap = A' p; pAp += p.Ap; pr += p.r
+__global__ void k_spmv_dots_ff(Ops2 A, LevelDims d, const float2* p, float2* Ap, const float2* r, Dots D) {
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
+    float2 pa = make_float2(0.f, 0.f), pr = make_float2(0.f, 0.f);
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
+        int i, j, k;
+        cell_ijk(d, c, i, j, k);
+        const float2 y = apply_A_ff(A, d, p, b, c, i, j, k, nullptr);
+        const size_t q = (size_t)b * d.nint + c;
+        Ap[q] = y;
+        const float2 pv = p[pidx(d, b, i, j, k)];
+        pa = ff_add(pa, ff_mul(pv, y));
+        pr = ff_add(pr, ff_mul(pv, r[q]));
+    }
+    const int pb = D.bprob[b];
+    block_sum_atomic_ff(pa, &D.pAp[pb]);
+    block_sum_atomic_ff(pr, &D.pr[pb]);
+}
+
+// alpha = p.r / p.Ap; x += alpha p; r -= alpha Ap; rr += r.r; rf = hi(r) (the V-cycle's input)
+__global__ void k_update_xr_ff(LevelDims d, float2* x, const float2* p, float2* r, const float2* Ap, float* rf, Dots D) {
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
+    const int pb = D.bprob[b];
+    const double alpha = (D.active[pb] && D.pAp[pb] != 0.0) ? D.pr[pb] / D.pAp[pb] : 0.0;
+    const float2 al = ff_from(alpha), nal = ff_neg(al);
+    float2 rr = make_float2(0.f, 0.f);
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
+        int i, j, k;
+        cell_ijk(d, c, i, j, k);
+        const size_t P = pidx(d, b, i, j, k), q = (size_t)b * d.nint + c;
+        x[P] = ff_add(x[P], ff_mul(al, p[P]));
+        const float2 rv = ff_add(r[q], ff_mul(nal, Ap[q]));
+        r[q] = rv;
+        rf[q] = rv.x;
+        rr = ff_add(rr, ff_mul(rv, rv));
+    }
+    block_sum_atomic_ff(rr, &D.rr[pb]);
+}
+
+// r = b' - A' x (true residual); rr += r.r; ab += (|b| + sum|A x|)^2 (the
+// scale of its rounding error); bb += b.b
+__global__ void k_residual_ff(Ops2 A, LevelDims d, const float2* x, const float2* bvec, float2* r, float* rf, Dots D,
+                              int want_bb) {
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
+    float2 rr = make_float2(0.f, 0.f), bb = make_float2(0.f, 0.f), ab = make_float2(0.f, 0.f);
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
+        int i, j, k;
+        cell_ijk(d, c, i, j, k);
+        const size_t q = (size_t)b * d.nint + c;
+        float ar;
+        const float2 bv = bvec[q];
+        const float2 rv = ff_add(bv, ff_neg(apply_A_ff(A, d, x, b, c, i, j, k, &ar)));
+        r[q] = rv;
+        rf[q] = rv.x;
+        rr = ff_add(rr, ff_mul(rv, rv));
+        bb = ff_add(bb, ff_mul(bv, bv));
+        const float sa = fabsf(bv.x) + ar;
+        ab = ff_add(ab, make_float2(sa * sa, 0.f));
+    }
+    const int pb = D.bprob[b];
+    block_sum_atomic_ff(rr, &D.rr[pb]);
+    block_sum_atomic_ff(ab, &D.ab[pb]);
+    if (want_bb) block_sum_atomic_ff(bb, &D.bb[pb]);
+}
+
+// z = the preconditioner's FP32 output scaled by sA (it inverts the unscaled
+// FP32 operator), or r; zAp += z.Ap
+__global__ void k_take_z_ff(LevelDims d, const float* zf, const float* sA, const float2* r, int use_r, float2* z,
+                            const float2* Ap, Dots D, int want_zAp) {
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
+    const float s = sA[D.bprob[b]];
+    float2 za = make_float2(0.f, 0.f);
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
+        int i, j, k;
+        cell_ijk(d, c, i, j, k);
+        const size_t q = (size_t)b * d.nint + c;
+        const float2 zv = use_r ? r[q] : make_float2(zf[pidx(d, b, i, j, k)] * s, 0.f);
+        z[q] = zv;
+        if (want_zAp) za = ff_add(za, ff_mul(zv, Ap[q]));
+    }
+    if (want_zAp) block_sum_atomic_ff(za, &D.zAp[D.bprob[b]]);
+}
+
+// p = z + beta p, beta = -z.Ap / p.Ap; restart (beta = 0) when `restart`
+__global__ void k_update_p_ff(LevelDims d, float2* p, const float2* z, Dots D, int restart) {
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
+    const int pb = D.bprob[b];
+    if (!D.active[pb]) return;
+    const double beta = (restart || D.pAp[pb] == 0.0) ? 0.0 : -D.zAp[pb] / D.pAp[pb];
+    const float2 be = ff_from(beta);
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
+        int i, j, k;
+        cell_ijk(d, c, i, j, k);
+        const size_t P = pidx(d, b, i, j, k);
+        p[P] = ff_add(z[(size_t)b * d.nint + c], ff_mul(be, p[P]));
+    }
+}
+
+// halo of an FF vector: the trilinear sum with the 8 corner weights
+// precomputed in FP64 on the host and stored as FF pairs
+struct HaloListFF {
+    int64_t n;
+    const int32_t* dst;
+    const int32_t* src;
+    const int32_t* st;     // [n][3]
+    const float2* w8;      // [n][8] corner weights
+};
+__global__ void k_halo_ff(float2* v, HaloListFF H) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= H.n) return;
+    const int a = H.st[3 * e], bq = H.st[3 * e + 1], c = H.st[3 * e + 2];
+    const int off[8] = {0, a, bq, c, a + bq, bq + c, a + c, a + bq + c};
+    const float2* f = v + H.src[e];
+    const float2* w = H.w8 + 8 * e;
+    float2 s = ff_mul(w[0], f[0]);
+#pragma unroll
+    for (int t = 1; t < 8; ++t) s = ff_add(s, ff_mul(w[t], f[off[t]]));
+    v[H.dst[e]] = s;
+}
+
+// x (FP64, interior of the padded array) = x' sb / sA per problem, after a solve
+__global__ void k_ff_unscale(LevelDims d, const float2* x2, const double* fac, const int32_t* bprob, double* x) {
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
+    const double f = fac[bprob[b]];
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
+        int i, j, k;
+        cell_ijk(d, c, i, j, k);
+        const size_t P = pidx(d, b, i, j, k);
+        x[P] = ff_to(x2[P]) * f;
+    }
+}
+
 // ---- FP32 V-cycle ------------------------------------------------------------
 __global__ void k_zero_f(float* v, size_t n) {
     for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (size_t)gridDim.x * blockDim.x) v[x] = 0.f;
@@ -440,7 +657,11 @@ struct SvLevel {
     int32_t *hcdst = nullptr, *hcsrc = nullptr;   // halo entries that are plain copies
     int64_t nhc = 0;
     float *z = nullptr, *r = nullptr, *res = nullptr;
+    // level 0: the scaled operator A / sA and the halo's corner weights as FF pairs
+    float2 *Aii2 = nullptr, *Ai2 = nullptr, *Aj2 = nullptr, *Ak2 = nullptr, *hw8 = nullptr;
     HaloList halo() const { return HaloList{nh, hdst, hsrc, hst, hw}; }
+    HaloListFF halo_ff() const { return HaloListFF{nh, hdst, hsrc, hst, hw8}; }
+    Ops2 ops2() const { return Ops2{Aii2, Ai2, Aj2, Ak2}; }
     Ops64 ops64() const { return Ops64{Aii, Ai, Aj, Ak}; }
     Ops32 ops32() const { return Ops32{fAii, fAi, fAj, fAk}; }
 };
@@ -452,6 +673,11 @@ struct falcon_solver {
     cudaStream_t st = nullptr;
     std::vector<SvLevel> lv;
     double *x = nullptr, *p = nullptr, *r = nullptr, *Ap = nullptr, *z = nullptr, *bvec = nullptr;
+    // the float-float solve (scaled system, see Ops2): padded x2, p2; interior r2, Ap2, z2, b2
+    float2 *x2 = nullptr, *p2 = nullptr, *r2 = nullptr, *Ap2 = nullptr, *z2 = nullptr, *b2 = nullptr;
+    std::vector<double> sA, sb;           // per-problem powers of two
+    float* dsA = nullptr;                 // sA on the device (FP32: powers of two are exact)
+    double* dunscale = nullptr;           // sb / sA per problem
     double* dots = nullptr;       // [5][nproblems]
     int32_t *active = nullptr, *bprob = nullptr;
     std::vector<void*> allocs;
@@ -510,6 +736,53 @@ template <class T> cudaError_t halo_fill(falcon_solver* sv, int l, T* v) {
     if (L.nhc > 0) k_halo_copy<T><<<(unsigned)((L.nhc + 255) / 256), 256, 0, sv->st>>>(v, L.hcdst, L.hcsrc, L.nhc);
     if (L.nh > 0) k_halo<T><<<(unsigned)((L.nh + 255) / 256), 256, 0, sv->st>>>(v, L.halo());
     return cudaGetLastError();
+}
+
+cudaError_t halo_fill_ff(falcon_solver* sv, float2* v) {
+    const SvLevel& L = sv->lv[0];
+    if (L.nhc > 0) k_halo_copy<float2><<<(unsigned)((L.nhc + 255) / 256), 256, 0, sv->st>>>(v, L.hcdst, L.hcsrc, L.nhc);
+    if (L.nh > 0) k_halo_ff<<<(unsigned)((L.nh + 255) / 256), 256, 0, sv->st>>>(v, L.halo_ff());
+    return cudaGetLastError();
+}
+
+// power of two at or above max |v| over each problem's blocks (1 if all zero)
+std::vector<double> problem_scale(const SolverProblemSet& S, const std::vector<double>& v, size_t per_block) {
+    std::vector<double> m(S.nproblems, 0.0);
+    for (int b = 0; b < S.nblocks; ++b) {
+        double& q = m[S.block_problem[b]];
+        for (size_t c = 0; c < per_block; ++c) q = std::max(q, std::fabs(v[(size_t)b * per_block + c]));
+    }
+    for (double& q : m) {
+        if (!(q > 0) || !std::isfinite(q)) { q = 1.0; continue; }
+        int e;
+        std::frexp(q, &e);
+        q = std::ldexp(1.0, e);
+    }
+    return m;
+}
+std::vector<float2> to_ff(const std::vector<double>& v, const std::vector<double>& scale_of_elem) {
+    std::vector<float2> o(v.size());
+    for (size_t q = 0; q < v.size(); ++q) {
+        const double x = v[q] / scale_of_elem[q];
+        const float h = (float)x;
+        o[q] = make_float2(h, (float)(x - (double)h));
+    }
+    return o;
+}
+
+// b2 = b / sb per problem (host b), and the unscale factors sb / sA
+int upload_rhs_ff(falcon_solver* sv) {
+    const SolverProblemSet& S = sv->S;
+    const size_t nint = (size_t)sv->lv[0].d.nint;
+    sv->sb = problem_scale(S, S.b, nint);
+    std::vector<double> sc(S.b.size()), un(S.nproblems);
+    for (int b = 0; b < S.nblocks; ++b)
+        for (size_t c = 0; c < nint; ++c) sc[(size_t)b * nint + c] = sv->sb[S.block_problem[b]];
+    for (int q = 0; q < S.nproblems; ++q) un[q] = sv->sb[q] / sv->sA[q];
+    const std::vector<float2> b2 = to_ff(S.b, sc);
+    SCK(cudaMemcpy(sv->b2, b2.data(), b2.size() * sizeof(float2), cudaMemcpyHostToDevice), "rhs");
+    SCK(cudaMemcpy(sv->dunscale, un.data(), un.size() * 8, cudaMemcpyHostToDevice), "rhs");
+    return FALCON_OK;
 }
 
 // z_0 = M r_0: one V-cycle on the FP32 residual stored in lv[0].r
@@ -669,6 +942,21 @@ int setup(falcon_solver* sv) {
             SCK(cudaMemcpy(L.hcdst, cdst.data(), nc * 4, cudaMemcpyHostToDevice), "halo");
             SCK(cudaMemcpy(L.hcsrc, csrc.data(), nc * 4, cudaMemcpyHostToDevice), "halo");
         }
+        if (l == 0) {   // the 8 corner weights of each interpolated halo entry, FF pairs
+            std::vector<float2> w8(8 * n);
+            for (size_t q = 0; q < n; ++q) {
+                const double wi = w[3 * q], wj = w[3 * q + 1], wk = w[3 * q + 2];
+                const double ui = 1.0 - wi, uj = 1.0 - wj, uk = 1.0 - wk;
+                const double c8[8] = {ui * uj * uk, wi * uj * uk, ui * wj * uk, ui * uj * wk,
+                                      wi * wj * uk, ui * wj * wk, wi * uj * wk, wi * wj * wk};
+                for (int t = 0; t < 8; ++t) {
+                    const float h = (float)c8[t];
+                    w8[8 * q + t] = make_float2(h, (float)(c8[t] - (double)h));
+                }
+            }
+            SCK(sv->alloc(&L.hw8, w8.size() * sizeof(float2)), "halo");
+            if (n) SCK(cudaMemcpy(L.hw8, w8.data(), w8.size() * sizeof(float2), cudaMemcpyHostToDevice), "halo");
+        }
         SCK(sv->alloc(&L.z, (size_t)nb * L.d.npad * 4), "vectors");
         SCK(sv->alloc(&L.r, (size_t)nb * L.d.nint * 4), "vectors");
         SCK(sv->alloc(&L.res, (size_t)nb * L.d.nint * 4), "vectors");
@@ -685,12 +973,43 @@ int setup(falcon_solver* sv) {
     SCK(sv->alloc(&sv->bprob, (size_t)nb * 4), "scalars");
     SCK(cudaMemcpy(sv->bvec, S.b.data(), S.b.size() * 8, cudaMemcpyHostToDevice), "rhs");
     SCK(cudaMemcpy(sv->bprob, S.block_problem.data(), (size_t)nb * 4, cudaMemcpyHostToDevice), "scalars");
+    // the float-float solve: A' = A / sA per problem (sA from the diagonal)
+    {
+        const SolverLevel& H = S.L[0];
+        const size_t nint = (size_t)d0.nint;
+        sv->sA = problem_scale(S, H.Aii, nint);
+        auto upff = [&](float2** dptr, const std::vector<double>& h) -> cudaError_t {
+            const size_t per = h.size() / (size_t)nb;   // entries per block
+            std::vector<double> sc(h.size());
+            for (int b = 0; b < nb; ++b)
+                for (size_t c = 0; c < per; ++c) sc[(size_t)b * per + c] = sv->sA[S.block_problem[b]];
+            const std::vector<float2> f = to_ff(h, sc);
+            cudaError_t e = sv->alloc(dptr, f.size() * sizeof(float2));
+            if (e == cudaSuccess) e = cudaMemcpy(*dptr, f.data(), f.size() * sizeof(float2), cudaMemcpyHostToDevice);
+            return e;
+        };
+        SvLevel& L0 = sv->lv[0];
+        SCK(upff(&L0.Aii2, H.Aii), "operator");
+        SCK(upff(&L0.Ai2, H.Ai), "operator");
+        SCK(upff(&L0.Aj2, H.Aj), "operator");
+        SCK(upff(&L0.Ak2, H.Ak), "operator");
+        for (float2** v : {&sv->x2, &sv->p2}) SCK(sv->alloc(v, (size_t)nb * d0.npad * sizeof(float2)), "vectors");
+        for (float2** v : {&sv->r2, &sv->Ap2, &sv->z2, &sv->b2})
+            SCK(sv->alloc(v, (size_t)nb * d0.nint * sizeof(float2)), "vectors");
+        std::vector<float> fa(sv->sA.begin(), sv->sA.end());
+        SCK(sv->alloc(&sv->dsA, fa.size() * 4), "scalars");
+        SCK(cudaMemcpy(sv->dsA, fa.data(), fa.size() * 4, cudaMemcpyHostToDevice), "scalars");
+        SCK(sv->alloc(&sv->dunscale, (size_t)S.nproblems * 8), "scalars");
+        const int rc = upload_rhs_ff(sv);
+        if (rc) return rc;
+    }
     SCK(cudaStreamSynchronize(sv->st), "setup");
     return FALCON_OK;
 }
 
-// scatter an interior [b][nint] FP64 vector into the padded x
-__global__ void k_scatter_pad(LevelDims d, const double* v, double* x) {
+// scatter an interior [b][nint] vector into the padded x
+template <class T>
+__global__ void k_scatter_pad(LevelDims d, const T* v, T* x) {
     const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
     for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         int i, j, k;
@@ -698,7 +1017,8 @@ __global__ void k_scatter_pad(LevelDims d, const double* v, double* x) {
         x[pidx(d, b, i, j, k)] = v[(size_t)b * d.nint + c];
     }
 }
-__global__ void k_gather_pad(LevelDims d, const double* x, double* v) {
+template <class T>
+__global__ void k_gather_pad(LevelDims d, const T* x, T* v) {
     const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
     for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         int i, j, k;
@@ -975,7 +1295,7 @@ int falcon_solver_apply(falcon_solver* sv, const double* x, double* y) {
     const int nb = sv->S.nblocks;
     SCK(cudaMemcpyAsync(sv->z, x, (size_t)nb * d.nint * 8, cudaMemcpyHostToDevice, sv->st), "apply");
     SCK(cudaMemsetAsync(sv->p, 0, (size_t)nb * d.npad * 8, sv->st), "apply");
-    k_scatter_pad<<<grid_cells(d, nb), tpb(d), 0, sv->st>>>(d, sv->z, sv->p);
+    k_scatter_pad<double><<<grid_cells(d, nb), tpb(d), 0, sv->st>>>(d, sv->z, sv->p);
     SCK(halo_fill<double>(sv, 0, sv->p), "apply halo");
     SCK(cudaMemsetAsync(sv->dots, 0, (size_t)6 * sv->S.nproblems * 8, sv->st), "apply");
     k_spmv_dots<<<grid_cells(d, nb), tpb(d), 0, sv->st>>>(sv->lv[0].ops64(), d, sv->p, sv->Ap, sv->r, sv->D());
@@ -1001,17 +1321,23 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
     cudaEvent_t t0, t1;
     cudaEventCreate(&t0);
     cudaEventCreate(&t1);
-    // x = x0, r = b - A x, bb = b.b
-    SCK(cudaMemsetAsync(sv->x, 0, (size_t)nb * d.npad * 8, sv->st), "init");
-    SCK(cudaMemcpyAsync(sv->z, S.x0.data(), (size_t)nb * d.nint * 8, cudaMemcpyHostToDevice, sv->st), "init");
-    SCK(cudaStreamSynchronize(sv->st), "init");
+    // x' = x0 sA / sb, r' = b' - A' x', bb = b'.b' (float-float, the scaled system)
+    {
+        std::vector<double> sc(S.x0.size());
+        for (int b = 0; b < nb; ++b)
+            for (int c = 0; c < d.nint; ++c) sc[(size_t)b * d.nint + c] = sv->sb[S.block_problem[b]] / sv->sA[S.block_problem[b]];
+        const std::vector<float2> x0 = to_ff(S.x0, sc);
+        SCK(cudaMemsetAsync(sv->x2, 0, (size_t)nb * d.npad * sizeof(float2), sv->st), "init");
+        SCK(cudaMemcpyAsync(sv->z2, x0.data(), x0.size() * sizeof(float2), cudaMemcpyHostToDevice, sv->st), "init");
+        SCK(cudaStreamSynchronize(sv->st), "init");
+    }
     cudaEventRecord(t0, sv->st);
-    k_scatter_pad<<<g, tpb(d), 0, sv->st>>>(d, sv->z, sv->x);
+    k_scatter_pad<float2><<<g, tpb(d), 0, sv->st>>>(d, sv->z2, sv->x2);
     std::vector<int32_t> act(np, 1);
     SCK(cudaMemcpyAsync(sv->active, act.data(), np * 4, cudaMemcpyHostToDevice, sv->st), "init");
     SCK(cudaMemsetAsync(sv->dots, 0, (size_t)6 * np * 8, sv->st), "init");
-    SCK(halo_fill<double>(sv, 0, sv->x), "halo");
-    k_residual64<<<g, tpb(d), 0, sv->st>>>(sv->lv[0].ops64(), d, sv->x, sv->bvec, sv->r, sv->lv[0].r, sv->D(), 1);
+    SCK(halo_fill_ff(sv, sv->x2), "halo");
+    k_residual_ff<<<g, tpb(d), 0, sv->st>>>(sv->lv[0].ops2(), d, sv->x2, sv->b2, sv->r2, sv->lv[0].r, sv->D(), 1);
     std::vector<double> rr(np), bb(np);
     SCK(cudaMemcpyAsync(bb.data(), sv->dots + 4 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "bb");
     SCK(cudaStreamSynchronize(sv->st), "bb");
@@ -1026,7 +1352,8 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
             ++rep->vcycles;
         }
         if (e != cudaSuccess) return e;
-        k_take_z<<<g, tpb(d), 0, sv->st>>>(d, sv->lv[0].z, sv->r, pc == FALCON_PRECOND_NONE, sv->z, sv->Ap, sv->D(), want_zAp);
+        k_take_z_ff<<<g, tpb(d), 0, sv->st>>>(d, sv->lv[0].z, sv->dsA, sv->r2, pc == FALCON_PRECOND_NONE, sv->z2, sv->Ap2,
+                                               sv->D(), want_zAp);
         return cudaGetLastError();
     };
     std::vector<double> hist;   // max over active problems of the recursive relative residual
@@ -1034,15 +1361,15 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
     std::vector<double> prev_true(np, 1e300); // true residual at the previous verification
     // p = M r
     SCK(precondition(0), "precondition");
-    k_update_p<<<g, tpb(d), 0, sv->st>>>(d, sv->p, sv->z, sv->D(), 1);
-    SCK(halo_fill<double>(sv, 0, sv->p), "halo");
+    k_update_p_ff<<<g, tpb(d), 0, sv->st>>>(d, sv->p2, sv->z2, sv->D(), 1);
+    SCK(halo_fill_ff(sv, sv->p2), "halo");
     double worst = 0;
     int it = 0;
     bool done = false;
     for (it = 1; it <= max_iter && !done; ++it) {
         SCK(cudaMemsetAsync(sv->dots, 0, (size_t)4 * np * 8, sv->st), "dots");
-        k_spmv_dots<<<g, tpb(d), 0, sv->st>>>(sv->lv[0].ops64(), d, sv->p, sv->Ap, sv->r, sv->D());
-        k_update_xr<<<g, tpb(d), 0, sv->st>>>(d, sv->x, sv->p, sv->r, sv->Ap, sv->lv[0].r, sv->D());
+        k_spmv_dots_ff<<<g, tpb(d), 0, sv->st>>>(sv->lv[0].ops2(), d, sv->p2, sv->Ap2, sv->r2, sv->D());
+        k_update_xr_ff<<<g, tpb(d), 0, sv->st>>>(d, sv->x2, sv->p2, sv->r2, sv->Ap2, sv->lv[0].r, sv->D());
         SCK(cudaGetLastError(), "iterate");
         SCK(cudaMemcpyAsync(rr.data(), sv->dots + 3 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "rr");
         SCK(cudaStreamSynchronize(sv->st), "rr");
@@ -1063,8 +1390,8 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
             pc = FALCON_PRECOND_MG;
             ++rep->fallbacks;
             SCK(precondition(0), "precondition");
-            k_update_p<<<g, tpb(d), 0, sv->st>>>(d, sv->p, sv->z, sv->D(), 1);
-            SCK(halo_fill<double>(sv, 0, sv->p), "halo");
+            k_update_p_ff<<<g, tpb(d), 0, sv->st>>>(d, sv->p2, sv->z2, sv->D(), 1);
+            SCK(halo_fill_ff(sv, sv->p2), "halo");
             continue;
         }
         if (all) {
@@ -1074,8 +1401,8 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
             // stops at that floor, which the report states.
             SCK(cudaMemsetAsync(sv->dots + 3 * np, 0, (size_t)np * 8, sv->st), "dots");
             SCK(cudaMemsetAsync(sv->dots + 5 * np, 0, (size_t)np * 8, sv->st), "dots");
-            SCK(halo_fill<double>(sv, 0, sv->x), "halo");
-            k_residual64<<<g, tpb(d), 0, sv->st>>>(sv->lv[0].ops64(), d, sv->x, sv->bvec, sv->r, sv->lv[0].r, sv->D(), 0);
+            SCK(halo_fill_ff(sv, sv->x2), "halo");
+            k_residual_ff<<<g, tpb(d), 0, sv->st>>>(sv->lv[0].ops2(), d, sv->x2, sv->b2, sv->r2, sv->lv[0].r, sv->D(), 0);
             std::vector<double> ab(np);
             SCK(cudaMemcpyAsync(rr.data(), sv->dots + 3 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "rr");
             SCK(cudaMemcpyAsync(ab.data(), sv->dots + 5 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "rr");
@@ -1087,7 +1414,7 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
                 const double rel = std::sqrt(rr[q] / bb[q]);
                 if (!std::isfinite(rel))
                     return sv->fail(FALCON_ERR_NAN_DETECTED, "solver: non-finite true residual in problem " + std::to_string(q));
-                const double floor_q = 4.0 * 8.0 * 2.220446049250313e-16 * std::sqrt(ab[q] / bb[q]);
+                const double floor_q = 4.0 * 8.0 * kEpsFF * std::sqrt(ab[q] / bb[q]);
                 // a true residual within 10x of tol that no longer improves between
                 // two verifications has reached what FP64 attains for this problem
                 const bool stalled = rel < 10.0 * tol && rel > 0.9 * prev_true[q];
@@ -1106,14 +1433,16 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
             if (ok) { done = true; break; }
             ++rep->refinements;
             SCK(precondition(0), "precondition");
-            k_update_p<<<g, tpb(d), 0, sv->st>>>(d, sv->p, sv->z, sv->D(), 1);
-            SCK(halo_fill<double>(sv, 0, sv->p), "halo");
+            k_update_p_ff<<<g, tpb(d), 0, sv->st>>>(d, sv->p2, sv->z2, sv->D(), 1);
+            SCK(halo_fill_ff(sv, sv->p2), "halo");
             continue;
         }
         SCK(precondition(1), "precondition");
-        k_update_p<<<g, tpb(d), 0, sv->st>>>(d, sv->p, sv->z, sv->D(), 0);
-        SCK(halo_fill<double>(sv, 0, sv->p), "halo");
+        k_update_p_ff<<<g, tpb(d), 0, sv->st>>>(d, sv->p2, sv->z2, sv->D(), 0);
+        SCK(halo_fill_ff(sv, sv->p2), "halo");
     }
+    // the solution in FP64, unscaled: x = x' sb / sA
+    k_ff_unscale<<<g, tpb(d), 0, sv->st>>>(d, sv->x2, sv->dunscale, sv->bprob, sv->x);
     cudaEventRecord(t1, sv->st);
     SCK(cudaEventSynchronize(t1), "solve");
     float ms = 0;
@@ -1123,8 +1452,8 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
     if (!done) {
         // report the true residual of the last iterate
         SCK(cudaMemsetAsync(sv->dots + 3 * np, 0, (size_t)np * 8, sv->st), "dots");
-        SCK(halo_fill<double>(sv, 0, sv->x), "halo");
-        k_residual64<<<g, tpb(d), 0, sv->st>>>(sv->lv[0].ops64(), d, sv->x, sv->bvec, sv->r, sv->lv[0].r, sv->D(), 0);
+        SCK(halo_fill_ff(sv, sv->x2), "halo");
+        k_residual_ff<<<g, tpb(d), 0, sv->st>>>(sv->lv[0].ops2(), d, sv->x2, sv->b2, sv->r2, sv->lv[0].r, sv->D(), 0);
         SCK(cudaMemcpyAsync(rr.data(), sv->dots + 3 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "rr");
         SCK(cudaStreamSynchronize(sv->st), "rr");
         worst = 0;
@@ -1147,7 +1476,7 @@ int falcon_solver_solution(falcon_solver* sv, double* x) {
     cudaSetDevice(sv->device);
     const LevelDims& d = sv->lv[0].d;
     const int nb = sv->S.nblocks;
-    k_gather_pad<<<grid_cells(d, nb), tpb(d), 0, sv->st>>>(d, sv->x, sv->z);
+    k_gather_pad<double><<<grid_cells(d, nb), tpb(d), 0, sv->st>>>(d, sv->x, sv->z);
     SCK(cudaMemcpyAsync(x, sv->z, (size_t)nb * d.nint * 8, cudaMemcpyDeviceToHost, sv->st), "solution");
     SCK(cudaStreamSynchronize(sv->st), "solution");
     return FALCON_OK;
@@ -1192,6 +1521,8 @@ int falcon_solver_set_rhs(falcon_solver* sv, const double* b) {
     if (sv->st) {
         cudaSetDevice(sv->device);
         SCK(cudaMemcpy(sv->bvec, b, sv->S.b.size() * 8, cudaMemcpyHostToDevice), "rhs");
+        const int rc = upload_rhs_ff(sv);
+        if (rc) return rc;
     }
     return FALCON_OK;
 }
