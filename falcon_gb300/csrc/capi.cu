@@ -581,6 +581,27 @@ int setup_device(falcon_ctx* ctx) {
         }
         std::sort(copies.begin(), copies.end());
         std::sort(lins.begin(), lins.end(), [](const Lin& a, const Lin& b) { return a.d < b.d; });
+        {   // interpolated entries in source order: a warp's gathers then read neighbouring source cells
+            std::vector<size_t> ord(idst.size());
+            for (size_t q = 0; q < ord.size(); ++q) ord[q] = q;
+            std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return isrc[a] < isrc[b]; });
+            std::vector<int32_t> d2(ord.size()), s2(ord.size());
+            std::vector<double> w2(3 * ord.size()), r2(2 * ord.size());
+            std::vector<uint8_t> k2(ord.size());
+            for (size_t q = 0; q < ord.size(); ++q) {
+                const size_t o = ord[q];
+                d2[q] = idst[o];
+                s2[q] = isrc[o];
+                for (int t = 0; t < 3; ++t) w2[3 * q + t] = iw[3 * o + t];
+                for (int t = 0; t < 2; ++t) r2[2 * q + t] = irot[2 * o + t];
+                k2[q] = ikind[o];
+            }
+            idst.swap(d2);
+            isrc.swap(s2);
+            iw.swap(w2);
+            irot.swap(r2);
+            ikind.swap(k2);
+        }
         std::vector<int32_t> cdst(copies.size()), csrc(copies.size());
         for (size_t q = 0; q < copies.size(); ++q) { cdst[q] = copies[q].first; csrc[q] = copies[q].second; }
         std::vector<int32_t> ldst(lins.size()), lsrc(lins.size()), lst(lins.size());
