@@ -923,6 +923,32 @@ int setup(falcon_solver* sv) {
                 stv.push_back(h.w[dd] != 0.0 ? strides[dd] : 0);
             }
         }
+        {   // source order: a warp's gathers read neighbouring source cells
+            std::vector<size_t> ord(dst.size());
+            for (size_t q = 0; q < ord.size(); ++q) ord[q] = q;
+            std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return src[a] < src[b]; });
+            std::vector<int32_t> d2(ord.size()), s2(ord.size()), st2(3 * ord.size());
+            std::vector<double> w2(3 * ord.size());
+            for (size_t q = 0; q < ord.size(); ++q) {
+                d2[q] = dst[ord[q]];
+                s2[q] = src[ord[q]];
+                for (int t = 0; t < 3; ++t) {
+                    st2[3 * q + t] = stv[3 * ord[q] + t];
+                    w2[3 * q + t] = w[3 * ord[q] + t];
+                }
+            }
+            dst.swap(d2);
+            src.swap(s2);
+            stv.swap(st2);
+            w.swap(w2);
+            std::vector<size_t> oc(cdst.size());
+            for (size_t q = 0; q < oc.size(); ++q) oc[q] = q;
+            std::stable_sort(oc.begin(), oc.end(), [&](size_t a, size_t b) { return csrc[a] < csrc[b]; });
+            std::vector<int32_t> cd2(oc.size()), cs2(oc.size());
+            for (size_t q = 0; q < oc.size(); ++q) { cd2[q] = cdst[oc[q]]; cs2[q] = csrc[oc[q]]; }
+            cdst.swap(cd2);
+            csrc.swap(cs2);
+        }
         const size_t n = dst.size(), nc = cdst.size();
         L.nh = (int64_t)n;
         L.nhc = (int64_t)nc;
