@@ -455,8 +455,38 @@ __global__ void k_zero_f(float* v, size_t n) {
 }
 
 // red-black Gauss-Seidel half sweep: z = (r - sum_nb A z_nb) / Aii on cells of one colour
+// (The smoother's rounding is free -- the outer CG is flexible -- so it uses
+// explicit FMAs and a fast division; this file is otherwise compiled without
+// contraction.) With an even row length that divides the chunk a thread takes
+// only cells of the colour: m0/2 cells of each colour per row.
+__device__ __forceinline__ void rbgs_cell(const Ops32& A, const LevelDims& d, const float* r, float* z, int b, int c,
+                                          int i, int j, int k) {
+    const size_t P = pidx(d, b, i, j, k);
+    const size_t sj = d.p0, sk = (size_t)d.p0 * d.p1;
+    const size_t fi = ((size_t)b * d.m2 * d.m1 + (size_t)(k - 1) * d.m1 + (j - 1)) * (d.m0 + 1) + (i - 1);
+    const size_t fj = ((size_t)b * d.m2 * (d.m1 + 1) + (size_t)(k - 1) * (d.m1 + 1) + (j - 1)) * d.m0 + (i - 1);
+    const size_t fk = ((size_t)b * (d.m2 + 1) * d.m1 + (size_t)(k - 1) * d.m1 + (j - 1)) * d.m0 + (i - 1);
+    float off = A.Ai[fi] * z[P - 1];
+    off = fmaf(A.Ai[fi + 1], z[P + 1], off);
+    off = fmaf(A.Aj[fj], z[P - sj], off);
+    off = fmaf(A.Aj[fj + d.m0], z[P + sj], off);
+    off = fmaf(A.Ak[fk], z[P - sk], off);
+    off = fmaf(A.Ak[fk + (size_t)d.m0 * d.m1], z[P + sk], off);
+    z[P] = __fdividef(r[(size_t)b * d.nint + c] - off, A.Aii[(size_t)b * d.nint + c]);
+}
+
 __global__ void k_rbgs(Ops32 A, LevelDims d, const float* r, float* z, int colour) {
     const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
+    if ((d.m0 & 1) == 0 && kCellChunk % d.m0 == 0) {   // rows whole within a chunk
+        const int half = d.m0 >> 1;
+        for (int h = (c0 >> 1) + threadIdx.x; h < (c1 >> 1); h += blockDim.x) {
+            const int row = h / half, ih = h - row * half;
+            const int j = row % d.m1 + 1, k = row / d.m1 + 1;
+            const int i = (((colour - j - k) & 1) ? 1 : 2) + 2 * ih;
+            rbgs_cell(A, d, r, z, b, row * d.m0 + (i - 1), i, j, k);
+        }
+        return;
+    }
     for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
