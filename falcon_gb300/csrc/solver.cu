@@ -101,17 +101,18 @@ __device__ __forceinline__ void block_sum_atomic(T v, double* slot) {
 }
 
 // ---- halo fill (trilinear from the source interior) ------------------------
-// entries whose three weights are exactly zero: the trilinear sum is the base
-// cell's value, copied
+// entries whose three weights are exactly zero are plain copies of the base
+// cell (a separate index list, no weights)
+// one launch for both lists: entries [0, nc) are the copies, the rest the
+// interpolated entries of H
 template <class T>
-__global__ void k_halo_copy(T* v, const int32_t* dst, const int32_t* src, int64_t n) {
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < n) v[dst[e]] = v[src[e]];
-}
-
-template <class T>
-__global__ void k_halo(T* v, HaloList H) {
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void k_halo(T* v, HaloList H, const int32_t* cdst, const int32_t* csrc, int64_t nc) {
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < nc) {
+        v[cdst[e]] = v[csrc[e]];
+        return;
+    }
+    e -= nc;
     if (e >= H.n) return;
     const size_t s = (size_t)H.src[e];
     const int a = H.st[3 * e], bq = H.st[3 * e + 1], c = H.st[3 * e + 2];
@@ -424,8 +425,13 @@ struct HaloListFF {
     const int32_t* st;     // [n][3]
     const float2* w8;      // [n][8] corner weights
 };
-__global__ void k_halo_ff(float2* v, HaloListFF H) {
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void k_halo_ff(float2* v, HaloListFF H, const int32_t* cdst, const int32_t* csrc, int64_t nc) {
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < nc) {
+        v[cdst[e]] = v[csrc[e]];
+        return;
+    }
+    e -= nc;
     if (e >= H.n) return;
     const int a = H.st[3 * e], bq = H.st[3 * e + 1], c = H.st[3 * e + 2];
     const int off[8] = {0, a, bq, c, a + bq, bq + c, a + c, a + bq + c};
@@ -763,15 +769,15 @@ unsigned tpb(const LevelDims& d) { return (unsigned)std::min(256, (d.nint + 31) 
 
 template <class T> cudaError_t halo_fill(falcon_solver* sv, int l, T* v) {
     const SvLevel& L = sv->lv[l];
-    if (L.nhc > 0) k_halo_copy<T><<<(unsigned)((L.nhc + 255) / 256), 256, 0, sv->st>>>(v, L.hcdst, L.hcsrc, L.nhc);
-    if (L.nh > 0) k_halo<T><<<(unsigned)((L.nh + 255) / 256), 256, 0, sv->st>>>(v, L.halo());
+    const int64_t n = L.nhc + L.nh;
+    if (n > 0) k_halo<T><<<(unsigned)((n + 255) / 256), 256, 0, sv->st>>>(v, L.halo(), L.hcdst, L.hcsrc, L.nhc);
     return cudaGetLastError();
 }
 
 cudaError_t halo_fill_ff(falcon_solver* sv, float2* v) {
     const SvLevel& L = sv->lv[0];
-    if (L.nhc > 0) k_halo_copy<float2><<<(unsigned)((L.nhc + 255) / 256), 256, 0, sv->st>>>(v, L.hcdst, L.hcsrc, L.nhc);
-    if (L.nh > 0) k_halo_ff<<<(unsigned)((L.nh + 255) / 256), 256, 0, sv->st>>>(v, L.halo_ff());
+    const int64_t n = L.nhc + L.nh;
+    if (n > 0) k_halo_ff<<<(unsigned)((n + 255) / 256), 256, 0, sv->st>>>(v, L.halo_ff(), L.hcdst, L.hcsrc, L.nhc);
     return cudaGetLastError();
 }
 
