@@ -739,9 +739,16 @@ struct falcon_solver {
         vgraphs.clear();
     }
     int fail(int c, const std::string& m) { err = m; return c; }
+    // zero-filled; the fill completes before returning: the uploads that follow
+    // an allocation are plain cudaMemcpy calls, which nothing orders after
+    // work on the solver's non-blocking stream
     template <class P> cudaError_t alloc(P** ptr, size_t bytes) {
         cudaError_t e = cudaMalloc((void**)ptr, bytes ? bytes : 16);
-        if (e == cudaSuccess) { allocs.push_back(*ptr); cudaMemsetAsync(*ptr, 0, bytes ? bytes : 16, st); }
+        if (e == cudaSuccess) {
+            allocs.push_back(*ptr);
+            e = cudaMemsetAsync(*ptr, 0, bytes ? bytes : 16, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        }
         return e;
     }
     Dots D() const {
@@ -1210,6 +1217,7 @@ int falcon_solver_create(falcon_solver** out, const falcon_solver_spec* spec) {
     if (spec->nproblems < 1 || spec->nproblems > FALCON_MAX_PROBLEMS) return sv->fail(FALCON_ERR_INVALID_ARG, "nproblems out of range");
     if (spec->block < 2 || spec->block > 32 || (spec->block & 1)) return sv->fail(FALCON_ERR_INVALID_ARG, "block must be even, 2..32");
     sv->device = spec->device;
+    if (spec->kind == FALCON_SOLVER_CONDUCTION) sv->nu_coarse = 4;
     std::vector<falcon_config> cfgs(spec->nproblems);
     const double kRsun = (double)6.955e10f;
     for (int q = 0; q < spec->nproblems; ++q) {

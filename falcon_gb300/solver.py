@@ -217,6 +217,8 @@ def _main(argv=None):
     ap.add_argument("--max-iter", type=int, default=300)
     ap.add_argument("--precond", choices=["mg", "none"], default="mg")
     ap.add_argument("--solves", type=int, default=2, help="solves of the same system (the first warms up)")
+    ap.add_argument("--smoothing", type=int, nargs=3, default=None, metavar=("PRE", "POST", "COARSE"),
+                    help="red-black Gauss-Seidel sweeps before/after the coarse correction and on the coarsest level")
     ap.add_argument("--device", type=int, default=0)
     a = ap.parse_args(argv)
     from . import build
@@ -228,6 +230,8 @@ def _main(argv=None):
         nr, nt = a.size or (64, 96)
         spec = pfss_spec([(nr, nt)] * a.problems, device=a.device)
     sv = Solver(spec)
+    if a.smoothing:
+        sv.set_smoothing(*a.smoothing)
     pc = PRECOND_MG if a.precond == "mg" else PRECOND_NONE
     for s in range(a.solves):
         rep = sv.solve(tol=a.tol, max_iter=a.max_iter, precond=pc, check=False)

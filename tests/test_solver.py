@@ -230,3 +230,19 @@ def test_gpu_pfss_solution_matches_cpu_direct_solve():
     err = np.linalg.norm(xg - x_ref) / np.linalg.norm(x_ref)
     print("pfss 16x24: GPU vs CPU direct solve relative error", err, rep)
     assert err <= 1e-6
+
+
+@pytest.mark.gpu
+def test_gpu_large_pfss_batch_converges_every_problem():
+    """32 PFSS problems of the benchmark's random sizes (72,744 blocks, 37M
+    cells): every problem reaches 1e-10 on its FP64 true residual. Large
+    arrays are where an upload not ordered after its buffer's zero-fill lost
+    the operator; this size failed before that was fixed."""
+    sizes = S.random_pfss_sizes(64, seed=5000)[:32]
+    sv = S.Solver(S.pfss_spec(sizes, device=0))
+    assert sv.nblocks > 65536
+    rep = sv.solve(tol=1e-10, max_iter=200, precond=S.PRECOND_MG, check=False)
+    rel = sv.problem_residuals()
+    print("32-problem PFSS batch:", rep, "max FP64 residual %.3e" % rel.max())
+    assert rep["converged"] == 1 and (rel <= 1.05e-10).all(), rel.max()
+    sv.close()
