@@ -327,14 +327,25 @@ std::string Grid::build(const falcon_config& c, bool with_ghosts) {
                     owner.push_back(o);
                     cell.push_back(((i + ng - 1) * 64 + (j + ng - 1)) * 64 + (k + ng - 1));
                 }
-        // stable grouping by first appearance of the owner
-        std::vector<int32_t> order;
-        std::vector<int32_t> seen;
-        for (size_t q = 0; q < owner.size(); ++q)
-            if (std::find(seen.begin(), seen.end(), owner[q]) == seen.end()) seen.push_back(owner[q]);
+        // stable grouping by first appearance of the owner: rank the owners in
+        // first-appearance order, then bucket the entries by rank (linear)
+        std::vector<int32_t> seen, rank(owner.size());
+        for (size_t q = 0; q < owner.size(); ++q) {
+            const auto it = std::find(seen.begin(), seen.end(), owner[q]);
+            rank[q] = (int32_t)(it - seen.begin());
+            if (it == seen.end()) seen.push_back(owner[q]);
+        }
+        std::vector<int32_t> start(seen.size() + 1, 0), order(owner.size());
+        for (size_t q = 0; q < owner.size(); ++q) ++start[rank[q] + 1];
+        for (size_t r = 0; r < seen.size(); ++r) start[r + 1] += start[r];
+        {
+            std::vector<int32_t> fill(start.begin(), start.end() - 1);
+            for (size_t q = 0; q < owner.size(); ++q) order[fill[rank[q]]++] = (int32_t)q;
+        }
         auto& out = per[b];
         out.reserve(owner.size());
-        for (int32_t s : seen) {
+        for (size_t r = 0; r < seen.size(); ++r) {
+            const int32_t s = seen[r];
             const bool syin = flags[s] & 1;
             const double* SX = &xi[(size_t)s * nip];
             const double* SY = &xj[(size_t)s * njp];
@@ -345,8 +356,8 @@ std::string Grid::build(const falcon_config& c, bool with_ghosts) {
             const double s0[3] = {SX[0], SY[0], SZ[0]};
             const double nmax[3] = {(double)((float)ni + 0.0f), (double)((float)nj + 0.0f), (double)((float)nk + 0.0f)};
             const double off = (double)((float)(-ng) + 1.0f);
-            for (size_t q = 0; q < owner.size(); ++q) {
-                if (owner[q] != s) continue;
+            for (int32_t oq = start[r]; oq < start[r + 1]; ++oq) {
+                const size_t q = (size_t)order[oq];
                 const int i = cell[q] / 4096 - ng + 1, j = (cell[q] / 64) % 64 - ng + 1, k = cell[q] % 64 - ng + 1;
                 GhostMapEntry g{};
                 g.e.tblock = b; g.e.ti = i; g.e.tj = j; g.e.tk = k;
@@ -376,11 +387,17 @@ std::string Grid::build(const falcon_config& c, bool with_ghosts) {
         }
     }
     uncovered = unc;
-    size_t total = 0;
-    for (auto& v : per) total += v.size();
+    // concatenate in block order, in parallel (the map of a 21M-cell shell is
+    // about 2 GB)
+    std::vector<size_t> offs((size_t)nblocks + 1, 0);
+    for (int b = 0; b < nblocks; ++b) offs[b + 1] = offs[b] + per[b].size();
     ghosts.clear();
-    ghosts.reserve(total);
-    for (auto& v : per) ghosts.insert(ghosts.end(), v.begin(), v.end());
+    ghosts.resize(offs[nblocks]);
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int b = 0; b < nblocks; ++b) {
+        std::copy(per[b].begin(), per[b].end(), ghosts.begin() + (long)offs[b]);
+        std::vector<GhostMapEntry>().swap(per[b]);
+    }
     if (uncovered > 0) return "ghost cells inside the radial range have no owner leaf";
     return "";
 }

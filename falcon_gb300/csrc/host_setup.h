@@ -8,6 +8,8 @@
 #pragma once
 #include <cstdint>
 #include <string>
+#include <memory>
+#include <utility>
 #include <vector>
 
 #include "../../include/falcon_gb300.h"
@@ -41,6 +43,18 @@ struct GhostMapEntry {          // falcon_ghost_entry plus derived interpolation
     double rot[2];              // sin(phi_s)*sin(phi_t), cos(phi_s)/sin(theta_t)
 };
 
+// std::allocator whose resize() leaves trivially constructible elements
+// uninitialised: the ghost map (about 2 GB for a 21M-cell shell) is then
+// written once, in parallel, instead of being zero-filled serially first
+template <class T>
+struct DefaultInitAlloc : std::allocator<T> {
+    template <class U> struct rebind { using other = DefaultInitAlloc<U>; };
+    DefaultInitAlloc() = default;
+    template <class U> DefaultInitAlloc(const DefaultInitAlloc<U>&) noexcept {}
+    template <class U> void construct(U* p) noexcept { ::new ((void*)p) U; }
+    template <class U, class... A> void construct(U* p, A&&... a) { ::new ((void*)p) U(std::forward<A>(a)...); }
+};
+
 struct Grid {
     falcon_config cfg;
     int ni, nj, nk, ng, nip, njp, nkp, ncell;
@@ -54,7 +68,7 @@ struct Grid {
     std::vector<double> xi, xj, xk;       // [b][nip], [b][njp], [b][nkp]
     std::vector<double> dx;               // [b][3]
     std::vector<double> prof;             // [b][FALCON_NPROF][nip]
-    std::vector<GhostMapEntry> ghosts;    // canonical (reference) order
+    std::vector<GhostMapEntry, DefaultInitAlloc<GhostMapEntry>> ghosts;   // canonical (reference) order
     int64_t uncovered = 0;                // non-radial ghosts without owner
 
     // returns empty string on success, else the error message; with_ghosts=false
