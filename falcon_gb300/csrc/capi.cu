@@ -466,9 +466,11 @@ int setup_device(falcon_ctx* ctx) {
         bool rotate;
         double rot[2];
     };
-    std::vector<GE> ges;
-    ges.reserve(g.ghosts.size());
-    for (const auto& e : g.ghosts) {
+    // one derived entry per ghost, in parallel into uninitialised storage
+    std::vector<GE, DefaultInitAlloc<GE>> ges(g.ghosts.size());
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < (long)g.ghosts.size(); ++k) {
+        const auto& e = g.ghosts[k];
         GE q{};
         q.base[0] = e.i0; q.base[1] = e.j0; q.base[2] = e.k0;
         q.w[0] = e.w[0]; q.w[1] = e.w[1]; q.w[2] = e.w[2];
@@ -489,8 +491,14 @@ int setup_device(falcon_ctx* ctx) {
         for (int a = 0; a < 3; ++a)
             if (q.t[a] < 1 || q.t[a] > n3[a]) { ++nghost; axis = a; side = q.t[a] > n3[a]; }
         q.face = nghost == 1 ? 2 * axis + side : -1;
-        ges.push_back(q);
+        ges[k] = q;
     }
+    // the entries of a target block are contiguous (canonical order): segments
+    std::vector<size_t> seg((size_t)nb + 1, 0);
+    for (size_t k = 0; k < ges.size(); ++k) ++seg[(size_t)ges[k].tb + 1];
+    for (int b = 0; b < nb; ++b) seg[b + 1] += seg[b];
+    for (size_t k = 1; k < ges.size(); ++k)
+        if (ges[k].tb < ges[k - 1].tb) return ctx->fail(FALCON_ERR_INVALID_ARG, "ghost map not in target-block order");
 
     // Faces pushed by the stage kernel (mixed path): every ghost cell of the
     // target face from one source block, no rotation; theta/phi: plain copies
@@ -501,7 +509,10 @@ int setup_device(falcon_ctx* ctx) {
     if (snap) {
         struct FaceState { int32_t sb = -1; bool ok = true; int64_t count = 0; int32_t rsrc[2] = {-1, -1}; double rw[2] = {0, 0}; };
         std::vector<FaceState> fs((size_t)nb * 6);
-        for (const GE& q : ges) {
+#pragma omp parallel for schedule(dynamic, 16)
+        for (int tb = 0; tb < nb; ++tb)
+          for (size_t k = seg[tb]; k < seg[tb + 1]; ++k) {
+            const GE& q = ges[k];
             if (q.face < 0) continue;
             FaceState& f = fs[(size_t)q.tb * 6 + q.face];
             if (!f.ok) continue;
@@ -543,10 +554,13 @@ int setup_device(falcon_ctx* ctx) {
                     }
                 ++ctx->pushed_faces;
             }
-        for (size_t k = 0; k < ges.size(); ++k) {
+        int64_t pc = 0;
+#pragma omp parallel for schedule(static) reduction(+ : pc)
+        for (long k = 0; k < (long)ges.size(); ++k) {
             const GE& q = ges[k];
-            if (q.face >= 0 && fs[(size_t)q.tb * 6 + q.face].ok) { pushed[k] = 1; ++ctx->pushed_cells; }
+            if (q.face >= 0 && fs[(size_t)q.tb * 6 + q.face].ok) { pushed[k] = 1; ++pc; }
         }
+        ctx->pushed_cells += pc;
     }
 
     auto up = [&](auto** dptr, const auto& vec) -> cudaError_t {
@@ -558,29 +572,50 @@ int setup_device(falcon_ctx* ctx) {
     const int32_t strides[3] = {1, g.nip, g.nip * g.njp};
     // build and upload one set of lists over the entries `keep` selects
     auto build_lists = [&](auto keep, GhostLists& out, int64_t* counts) -> cudaError_t {
-        std::vector<std::pair<int32_t, int32_t>> copies;
         struct Lin { int32_t d, s, st; float w; };
-        std::vector<Lin> lins;
-        std::vector<int32_t> idst, isrc;
-        std::vector<double> iw, irot;
-        std::vector<uint8_t> ikind;
-        for (size_t k = 0; k < ges.size(); ++k) {
-            if (!keep(k)) continue;
-            const GE& q = ges[k];
-            if (!q.rotate && q.nz == 0) { copies.push_back({q.d, q.src}); continue; }
-            if (snap && !q.rotate && q.nz == 1) {
-                const int a = q.w[0] != 0.0 ? 0 : (q.w[1] != 0.0 ? 1 : 2);
-                lins.push_back({q.d, q.src, strides[a], (float)q.w[a]});
-                continue;
-            }
-            idst.push_back(q.d);
-            isrc.push_back(q.src);
-            iw.insert(iw.end(), {q.w[0], q.w[1], q.w[2]});
-            irot.insert(irot.end(), {q.rot[0], q.rot[1]});
-            ikind.push_back((uint8_t)((q.nz ? 1 : 0) | (q.rotate ? 2 : 0)));
+        // kind of an entry: 0 copy, 1 one-direction blend (mixed), 2 general
+        auto kind = [&](const GE& q) { return (!q.rotate && q.nz == 0) ? 0 : (snap && !q.rotate && q.nz == 1) ? 1 : 2; };
+        // per target block counts, offsets, then a parallel fill (blocks are
+        // contiguous and their target offsets ascend with the block)
+        std::vector<size_t> oc((size_t)nb + 1, 0), ol((size_t)nb + 1, 0), oi((size_t)nb + 1, 0);
+#pragma omp parallel for schedule(dynamic, 16)
+        for (int b = 0; b < nb; ++b) {
+            size_t n3k[3] = {0, 0, 0};
+            for (size_t k = seg[b]; k < seg[b + 1]; ++k)
+                if (keep(k)) ++n3k[kind(ges[k])];
+            oc[b + 1] = n3k[0]; ol[b + 1] = n3k[1]; oi[b + 1] = n3k[2];
         }
-        std::sort(copies.begin(), copies.end());
-        std::sort(lins.begin(), lins.end(), [](const Lin& a, const Lin& b) { return a.d < b.d; });
+        for (int b = 0; b < nb; ++b) { oc[b + 1] += oc[b]; ol[b + 1] += ol[b]; oi[b + 1] += oi[b]; }
+        std::vector<std::pair<int32_t, int32_t>> copies(oc[nb]);
+        std::vector<Lin> lins(ol[nb]);
+        std::vector<int32_t> idst(oi[nb]), isrc(oi[nb]);
+        std::vector<double> iw(3 * oi[nb]), irot(2 * oi[nb]);
+        std::vector<uint8_t> ikind(oi[nb]);
+#pragma omp parallel for schedule(dynamic, 16)
+        for (int b = 0; b < nb; ++b) {
+            size_t c = oc[b], l = ol[b], i = oi[b];
+            for (size_t k = seg[b]; k < seg[b + 1]; ++k) {
+                if (!keep(k)) continue;
+                const GE& q = ges[k];
+                const int kd = kind(q);
+                if (kd == 0) { copies[c++] = {q.d, q.src}; continue; }
+                if (kd == 1) {
+                    const int a = q.w[0] != 0.0 ? 0 : (q.w[1] != 0.0 ? 1 : 2);
+                    lins[l++] = Lin{q.d, q.src, strides[a], (float)q.w[a]};
+                    continue;
+                }
+                idst[i] = q.d;
+                isrc[i] = q.src;
+                for (int t = 0; t < 3; ++t) iw[3 * i + t] = q.w[t];
+                irot[2 * i] = q.rot[0];
+                irot[2 * i + 1] = q.rot[1];
+                ikind[i] = (uint8_t)((q.nz ? 1 : 0) | (q.rotate ? 2 : 0));
+                ++i;
+            }
+            std::sort(copies.begin() + (long)oc[b], copies.begin() + (long)oc[b + 1]);
+            std::sort(lins.begin() + (long)ol[b], lins.begin() + (long)ol[b + 1],
+                      [](const Lin& x, const Lin& y) { return x.d < y.d; });
+        }
         {   // interpolated entries in source order: a warp's gathers then read neighbouring source cells
             std::vector<size_t> ord(idst.size());
             for (size_t q = 0; q < ord.size(); ++q) ord[q] = q;
