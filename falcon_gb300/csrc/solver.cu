@@ -46,8 +46,10 @@ struct HaloList {
     int64_t n;
     const int32_t* dst;    // padded global offset
     const int32_t* src;    // padded global offset of the base source cell
-    const int32_t* st;     // [n][3] element strides (0 where the weight is 0)
-    const double* w;       // [n][3]
+    const uint8_t* code;   // bit d set: the weight of direction d is not 0
+    const double* w;       // [n][3] (FP64 fills)
+    const float* wf;       // [n][3] (FP32 fills: the V-cycle)
+    int32_t sj, sk;        // padded strides of j and k
 };
 
 struct Ops64 { const double *Aii, *Ai, *Aj, *Ak; };
@@ -115,8 +117,14 @@ __global__ void k_halo(T* v, HaloList H, const int32_t* cdst, const int32_t* csr
     e -= nc;
     if (e >= H.n) return;
     const size_t s = (size_t)H.src[e];
-    const int a = H.st[3 * e], bq = H.st[3 * e + 1], c = H.st[3 * e + 2];
-    const T wi = (T)H.w[3 * e], wj = (T)H.w[3 * e + 1], wk = (T)H.w[3 * e + 2];
+    const int cd = H.code[e];
+    const int a = (cd & 1) ? 1 : 0, bq = (cd & 2) ? H.sj : 0, c = (cd & 4) ? H.sk : 0;
+    T wi, wj, wk;
+    if constexpr (sizeof(T) == 4) {
+        wi = H.wf[3 * e]; wj = H.wf[3 * e + 1]; wk = H.wf[3 * e + 2];
+    } else {
+        wi = H.w[3 * e]; wj = H.w[3 * e + 1]; wk = H.w[3 * e + 2];
+    }
     const T ui = T(1) - wi, uj = T(1) - wj, uk = T(1) - wk;
     const T* f = v + s;
     v[H.dst[e]] = f[0] * ui * uj * uk + f[a] * wi * uj * uk + f[bq] * ui * wj * uk + f[c] * ui * uj * wk +
@@ -422,8 +430,9 @@ struct HaloListFF {
     int64_t n;
     const int32_t* dst;
     const int32_t* src;
-    const int32_t* st;     // [n][3]
+    const uint8_t* code;   // as HaloList
     const float2* w8;      // [n][8] corner weights
+    int32_t sj, sk;
 };
 __global__ void k_halo_ff(float2* v, HaloListFF H, const int32_t* cdst, const int32_t* csrc, int64_t nc) {
     int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -433,7 +442,8 @@ __global__ void k_halo_ff(float2* v, HaloListFF H, const int32_t* cdst, const in
     }
     e -= nc;
     if (e >= H.n) return;
-    const int a = H.st[3 * e], bq = H.st[3 * e + 1], c = H.st[3 * e + 2];
+    const int cd = H.code[e];
+    const int a = (cd & 1) ? 1 : 0, bq = (cd & 2) ? H.sj : 0, c = (cd & 4) ? H.sk : 0;
     const int off[8] = {0, a, bq, c, a + bq, bq + c, a + c, a + bq + c};
     const float2* f = v + H.src[e];
     const float2* w = H.w8 + 8 * e;
@@ -687,7 +697,9 @@ struct SvLevel {
     LevelDims d{};
     double *Aii = nullptr, *Ai = nullptr, *Aj = nullptr, *Ak = nullptr;
     float *fAii = nullptr, *fAi = nullptr, *fAj = nullptr, *fAk = nullptr;
-    int32_t *hdst = nullptr, *hsrc = nullptr, *hst = nullptr;
+    int32_t *hdst = nullptr, *hsrc = nullptr;
+    uint8_t* hcode = nullptr;
+    float* hwf = nullptr;
     double* hw = nullptr;
     int64_t nh = 0;
     int32_t *hcdst = nullptr, *hcsrc = nullptr;   // halo entries that are plain copies
@@ -695,8 +707,8 @@ struct SvLevel {
     float *z = nullptr, *r = nullptr, *res = nullptr;
     // level 0: the scaled operator A / sA and the halo's corner weights as FF pairs
     float2 *Aii2 = nullptr, *Ai2 = nullptr, *Aj2 = nullptr, *Ak2 = nullptr, *hw8 = nullptr;
-    HaloList halo() const { return HaloList{nh, hdst, hsrc, hst, hw}; }
-    HaloListFF halo_ff() const { return HaloListFF{nh, hdst, hsrc, hst, hw8}; }
+    HaloList halo() const { return HaloList{nh, hdst, hsrc, hcode, hw, hwf, d.p0, d.p0 * d.p1}; }
+    HaloListFF halo_ff() const { return HaloListFF{nh, hdst, hsrc, hcode, hw8, d.p0, d.p0 * d.p1}; }
     Ops2 ops2() const { return Ops2{Aii2, Ai2, Aj2, Ak2}; }
     Ops64 ops64() const { return Ops64{Aii, Ai, Aj, Ak}; }
     Ops32 ops32() const { return Ops32{fAii, fAi, fAj, fAk}; }
@@ -997,14 +1009,22 @@ int setup(falcon_solver* sv) {
         L.nhc = (int64_t)nc;
         SCK(sv->alloc(&L.hdst, n * 4), "halo");
         SCK(sv->alloc(&L.hsrc, n * 4), "halo");
-        SCK(sv->alloc(&L.hst, 3 * n * 4), "halo");
+        std::vector<uint8_t> code(n);
+        std::vector<float> wf(3 * n);
+        for (size_t q = 0; q < n; ++q) {
+            code[q] = (uint8_t)((stv[3 * q] ? 1 : 0) | (stv[3 * q + 1] ? 2 : 0) | (stv[3 * q + 2] ? 4 : 0));
+            for (int t = 0; t < 3; ++t) wf[3 * q + t] = (float)w[3 * q + t];
+        }
+        SCK(sv->alloc(&L.hcode, n), "halo");
+        SCK(sv->alloc(&L.hwf, 3 * n * 4), "halo");
         SCK(sv->alloc(&L.hw, 3 * n * 8), "halo");
         SCK(sv->alloc(&L.hcdst, nc * 4), "halo");
         SCK(sv->alloc(&L.hcsrc, nc * 4), "halo");
         if (n) {
             SCK(cudaMemcpy(L.hdst, dst.data(), n * 4, cudaMemcpyHostToDevice), "halo");
             SCK(cudaMemcpy(L.hsrc, src.data(), n * 4, cudaMemcpyHostToDevice), "halo");
-            SCK(cudaMemcpy(L.hst, stv.data(), 3 * n * 4, cudaMemcpyHostToDevice), "halo");
+            SCK(cudaMemcpy(L.hcode, code.data(), n, cudaMemcpyHostToDevice), "halo");
+            SCK(cudaMemcpy(L.hwf, wf.data(), 3 * n * 4, cudaMemcpyHostToDevice), "halo");
             SCK(cudaMemcpy(L.hw, w.data(), 3 * n * 8, cudaMemcpyHostToDevice), "halo");
         }
         if (nc) {
