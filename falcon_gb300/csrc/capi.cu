@@ -55,6 +55,7 @@ struct falcon_ctx {
     GhostLists gl_stage{};    // face ghosts not pushed by the stage kernel (exchanges after stages)
     GhostLists gl_final{};    // mixed: ghost entries the exchange ending a step fills (see setup_device)
     bool stale_edges = false; // mixed: edge/corner ghosts not refreshed since the last step
+    bool cfl_ready = false;   // mixed: the last diffusion pass formed this state's CFL minimum
     PushTable push{};         // mixed path: faces the stage kernel writes into its output
     void* R2 = nullptr;       // mixed path: second stage buffer (pushing needs out != in)
     int64_t ghost_counts[3] = {0, 0, 0};   // copy, 1-D, general entries on the device
@@ -65,7 +66,8 @@ struct falcon_ctx {
     // step graphs: the mixed step writes u^{n+1} into the second stage buffer
     // and the two buffers swap roles, so one graph per assignment (index 0
     // while U is the first allocation)
-    cudaGraphExec_t graphs[2] = {nullptr, nullptr};
+    // [buffer assignment][CFL minimum already formed by the previous step]
+    cudaGraphExec_t graphs[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     void* bufA = nullptr;
     int64_t steps_done = 0;
     int64_t dev_bytes = 0;
@@ -149,6 +151,7 @@ cudaError_t ghost_stage(falcon_ctx* ctx, void* u) {
 }
 
 cudaError_t cfl(falcon_ctx* ctx) {
+    ctx->cfl_ready = false;   // the minimum formed by a diffusion pass is replaced and consumed here
     cudaError_t e = timed(ctx, KN_CFL, [&] {
         return ctx->mixed() ? launch_cfl_mixed(ctx->dims, ctx->geom(), (const float*)ctx->U, ctx->sc, ctx->st)
                             : launch_cfl_fp64(ctx->dims, ctx->geom(), (const double*)ctx->U, ctx->sc, ctx->st);
@@ -194,7 +197,7 @@ cudaError_t stage(falcon_ctx* ctx, int s, void* in, void* out, const PushTable& 
 
 // Artificial diffusion of every variable (ModAdvance.f90:101-109); psi's runs
 // first, from the same pre-diffusion state, into P2.
-cudaError_t diffusion(falcon_ctx* ctx, void* out, const PushTable& push) {
+cudaError_t diffusion(falcon_ctx* ctx, void* out, const PushTable& push, int cfl_next = 0) {
     cudaError_t e = cudaSuccess;
     if (ctx->P) {
         e = timed(ctx, KN_DIFF, [&] {
@@ -207,7 +210,7 @@ cudaError_t diffusion(falcon_ctx* ctx, void* out, const PushTable& push) {
     }
     e = timed(ctx, KN_DIFF, [&] {
         return ctx->mixed() ? launch_diffusion_mixed(ctx->dims, ctx->geom(), (const float*)ctx->U, (float*)out,
-                                                     ctx->Ulo, push, ctx->sc, ctx->kpar_diff, ctx->st)
+                                                     ctx->Ulo, push, ctx->sc, ctx->kpar_diff, ctx->st, cfl_next)
                             : launch_diffusion_fp64(ctx->dims, ctx->geom(), (double*)ctx->U, ctx->sc, ctx->kpar_diff, ctx->st);
     });
     if (e != cudaSuccess || !ctx->P) return e;
@@ -225,7 +228,9 @@ cudaError_t diffusion(falcon_ctx* ctx, void* out, const PushTable& push) {
 // kernels push ghost faces into their output, so input and output differ:
 // U -> RK -> R2 -> RK -> U (stage 4 writes u^{n+1} over u^n cell by cell).
 cudaError_t enqueue_step(falcon_ctx* ctx) {
-    cudaError_t e = cfl(ctx);
+    const bool fused_cfl = ctx->mixed() && ctx->R2;
+    cudaError_t e = (fused_cfl && ctx->cfl_ready) ? timed(ctx, KN_FIN, [&] { return launch_finalize_dt(ctx->sc, ctx->st); })
+                                                   : cfl(ctx);
     if (e != cudaSuccess) return e;
     for (int s = 1; s <= 4; ++s) {
         void* in;
@@ -247,7 +252,7 @@ cudaError_t enqueue_step(falcon_ctx* ctx) {
         // u^{n+1} into the second stage buffer, regular faces pushed by the
         // diffusion pass, then the remaining ghost entries; end_step swaps
         // the two buffers' roles
-        e = diffusion(ctx, ctx->R2, ctx->push);
+        e = diffusion(ctx, ctx->R2, ctx->push, 1);
         if (e != cudaSuccess) return e;
         return timed(ctx, KN_GHOST, [&] { return launch_ghost_mixed(ctx->dims, ctx->gl_final, (float*)ctx->R2, ctx->st); });
     }
@@ -262,6 +267,7 @@ void end_step(falcon_ctx* ctx) {
     if (ctx->mixed() && ctx->R2) {
         std::swap(ctx->U, ctx->R2);
         ctx->stale_edges = true;
+        ctx->cfl_ready = true;
     }
 }
 
@@ -745,8 +751,9 @@ void falcon_destroy(falcon_ctx* ctx) {
     if (ctx->on_device) {
         cudaSetDevice(ctx->device);
         cudaStreamSynchronize(ctx->st);
-        for (cudaGraphExec_t& gx : ctx->graphs)
-            if (gx) cudaGraphExecDestroy(gx);
+        for (auto& row : ctx->graphs)
+            for (cudaGraphExec_t& gx : row)
+                if (gx) cudaGraphExecDestroy(gx);
         for (auto& r : ctx->pending) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
         for (auto e : ctx->pool) cudaEventDestroy(e);
         for (void* p : ctx->allocs) cudaFree(p);
@@ -901,6 +908,7 @@ int falcon_upload_state(falcon_ctx* ctx, const double* u) {
     rc = put_state(ctx, u, ctx->U, ctx->Ulo, ctx->P);
     if (rc) return rc;
     ctx->stale_edges = false;   // the uploaded ghost cells are the state's
+    ctx->cfl_ready = false;
     // primitive_rk_IV = primitive_IV, as the reference's initialisation leaves it
     const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
     CK(cudaMemcpyAsync(ctx->RK, ctx->U, n * ctx->elem, cudaMemcpyDeviceToDevice, ctx->st), "upload");
@@ -978,6 +986,7 @@ int falcon_init_synthetic(falcon_ctx* ctx, int32_t kind, uint64_t seed, double m
     CK(cudaMemcpyAsync(ctx->RK, ctx->U, n * ctx->elem, cudaMemcpyDeviceToDevice, ctx->st), "init");
     CK(mirror_state(ctx), "init");
     ctx->stale_edges = false;
+    ctx->cfl_ready = false;
     CK(cudaStreamSynchronize(ctx->st), "init");
     return FALCON_OK;
 }
@@ -1020,7 +1029,7 @@ static int run(falcon_ctx* ctx, int32_t n) {
         return FALCON_OK;
     }
     for (int32_t s = 0; s < n; ++s) {
-        cudaGraphExec_t& gx = ctx->graphs[ctx->U == ctx->bufA ? 0 : 1];
+        cudaGraphExec_t& gx = ctx->graphs[ctx->U == ctx->bufA ? 0 : 1][ctx->cfl_ready ? 1 : 0];
         if (!gx) {
             cudaGraph_t gr;
             CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal), "capture");
@@ -1065,6 +1074,7 @@ int falcon_step_phase(falcon_ctx* ctx, int32_t phase) {
     if (phase < 0 || phase > 5) return ctx->fail(FALCON_ERR_INVALID_ARG, "phase must be 0..5");
     rc = autotune(ctx);
     if (rc) return rc;
+    ctx->cfl_ready = false;   // the phases change the state outside the fused step
     cudaError_t e = cudaSuccess;
     if (phase == 0) {
         e = cfl(ctx);
@@ -1339,6 +1349,7 @@ int falcon_load_restart(falcon_ctx* ctx, const char* path) {
     CK(cudaMemcpyAsync(ctx->RK, ctx->U, h.bytes_state, cudaMemcpyDeviceToDevice, ctx->st), "restart");
     CK(mirror_state(ctx), "restart");
     ctx->stale_edges = false;
+    ctx->cfl_ready = false;
     if (ctx->P)
         for (void* q : {ctx->Prk, ctx->P2})
             CK(cudaMemcpyAsync(q, ctx->P, h.bytes_psi, cudaMemcpyDeviceToDevice, ctx->st), "restart");

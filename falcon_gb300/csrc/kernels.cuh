@@ -201,7 +201,8 @@ cudaError_t launch_psi_ghost_mixed(const StepDims& d, const GhostLists& gl, floa
 // place with the regular faces pushed into out and the radial boundary ghost
 // columns copied (see k_diffusion)
 cudaError_t launch_diffusion_mixed(const StepDims& d, const Geometry& g, const float* u, float* out, int8_t* lo,
-                                   const PushTable& push, StepScalars* sc, int kpar, cudaStream_t st);
+                                   const PushTable& push, StepScalars* sc, int kpar, cudaStream_t st,
+                                   int cfl_next = 0);
 cudaError_t launch_cfl_mixed(const StepDims& d, const Geometry& g, const float* u, StepScalars* sc,
                              cudaStream_t st);
 cudaError_t launch_ghost_mixed(const StepDims& d, const GhostLists& gl, float* u, cudaStream_t st);

@@ -56,7 +56,7 @@ cudaError_t stage_n(const StepDims& d, const Geometry& g, const T* in, const T* 
 
 template <class T, int N, int KP>
 cudaError_t diff_n(const StepDims& d, const Geometry& g, const T* u, T* out, int8_t* lo, const PushTable& push,
-                   StepScalars* sc, cudaStream_t st) {
+                   StepScalars* sc, int cfl_next, cudaStream_t st) {
     using S = DShape<T, N, N, N, KP>;
     static bool attr = false;
     if (!attr) {
@@ -65,7 +65,7 @@ cudaError_t diff_n(const StepDims& d, const Geometry& g, const T* u, T* out, int
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    k_diffusion<T, N, N, N, KP><<<d.nblocks, S::NT, S::smem, st>>>(u, out, lo, push, g, sc);
+    k_diffusion<T, N, N, N, KP><<<d.nblocks, S::NT, S::smem, st>>>(u, out, lo, push, g, sc, cfl_next);
     return cudaGetLastError();
 }
 
@@ -85,10 +85,10 @@ cudaError_t stage_any(const StepDims& d, const Geometry& g, const T* in, const T
 
 template <class T>
 cudaError_t diff_any(const StepDims& d, const Geometry& g, const T* u, T* out, int8_t* lo, const PushTable& push,
-                     StepScalars* sc, int kpar, cudaStream_t st) {
+                     StepScalars* sc, int kpar, cudaStream_t st, int cfl_next = 0) {
     if (push.tgt != nullptr && out == u) return cudaErrorInvalidValue;   // pushing needs out != u
 #define FALCON_DIFF_CASE(N, K) \
-    if (d.ni == N && kpar == K) return diff_n<T, N, K>(d, g, u, out, lo, push, sc, st);
+    if (d.ni == N && kpar == K) return diff_n<T, N, K>(d, g, u, out, lo, push, sc, cfl_next, st);
     if (d.ni != d.nj || d.ni != d.nk) return cudaErrorInvalidValue;
     FALCON_DIFF_CASE(8, 2) FALCON_DIFF_CASE(8, 4)
     FALCON_DIFF_CASE(16, 1)

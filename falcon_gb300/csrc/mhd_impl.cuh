@@ -59,6 +59,41 @@ __device__ __forceinline__ float minmod_sel(float ul, float u, float ur) {
     return x >= 1.e-30f ? copysignf(m, a) : 0.f;
 }
 
+// The per-cell CFL ratio h_LLL / v_wave of the mixed path, shared by k_cfl and
+// the diffusion pass that forms it for the next step: explicitly rounded FP32
+// operations, so both give the same bits whatever the compiler contracts.
+__device__ __forceinline__ float cfl_sq3(float x, float y, float z) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z));
+}
+__device__ __forceinline__ float cfl_ratio_f(float v2, float b2, float cs, float rho0, float r, float sin_t,
+                                             float dxi, float dxj, float dxk) {
+    // h_LLL = min(dxi, r*dxj, r*sin(theta)*dxk) (3_6/ModBlock.f90:416-425)
+    const float h = fminf(fminf(dxi, __fmul_rn(r, dxj)), __fmul_rn(__fmul_rn(r, sin_t), dxk));
+    float w = __fadd_rn(cs, __fsqrt_rn(v2));
+    w = __fadd_rn(w, __fdiv_rn(__fsqrt_rn(b2), __fsqrt_rn(rho0)));
+    return __fdiv_rn(h, w);
+}
+// block minimum of the ratios (FP64 bit order for positive values) and NaN flag
+__device__ __forceinline__ void cfl_commit(float ratio, int nan, StepScalars* sc) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        ratio = fminf(ratio, __shfl_xor_sync(0xffffffffu, ratio, o));
+        nan |= __shfl_xor_sync(0xffffffffu, nan, o);
+    }
+    __shared__ float wmin[32];
+    __shared__ int wnan[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) { wmin[wid] = ratio; wnan[wid] = nan; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float m = wmin[0];
+        int n = wnan[0];
+        for (int w2 = 1; w2 < (int)(blockDim.x >> 5); ++w2) { m = fminf(m, wmin[w2]); n |= wnan[w2]; }
+        atomicMin(&sc->min_ratio_bits, (unsigned long long)__double_as_longlong((double)m));
+        if (n) atomicOr(&sc->nan_flag, 1);
+    }
+}
+
 template <class T> __device__ __forceinline__ const T* gi_ptr(const Geometry& g);
 template <> __device__ __forceinline__ const double* gi_ptr<double>(const Geometry& g) { return g.gi; }
 template <> __device__ __forceinline__ const float* gi_ptr<float>(const Geometry& g) { return g.gi_f; }
@@ -668,9 +703,13 @@ __device__ __forceinline__ T face_flux(T fm, T fl, T fr, T fp, T cL, T cR) {
 // ghost columns (set by the boundary condition at stage 1) from u to out, so
 // that with an exchange of the remaining ghost entries `out` holds the whole
 // updated state.
+//
+// cfl_next (mixed): the outputs are the next step's u^n, so the kernel also
+// forms the next step's CFL minimum and NaN flag from them (k_cfl's formula,
+// cfl_ratio_f), and that step skips k_cfl.
 template <class T, int NI, int NJ, int NK, int KPAR>
 __global__ void __launch_bounds__(DShape<T, NI, NJ, NK, KPAR>::NT, (DShape<T, NI, NJ, NK, KPAR>::min_blocks))
-k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepScalars* sc) {
+k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepScalars* sc, int cfl_next) {
     using S = DShape<T, NI, NJ, NK, KPAR>;
     static_assert(S::fits, "diffusion shared memory above 227 KB");
     constexpr int NIP = S::NIP, PL = S::PL, W = S::W, NCELL = S::NCELL, KS = S::KS;
@@ -715,6 +754,9 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
     const T dinv[3] = {T(1) / den[0], T(1) / den[1], T(1) / den[2]};
     const double hdt = 0.5 * sc->dt;
     const float hdt_f = sc->dt_half_f;
+    float cmin = INFINITY;   // next step's CFL ratio minimum over this thread's cells
+    int cnan = 0;
+    __shared__ float sb2[S::TPC == 2 ? S::NCELLS : 1];   // |B|^2 from the thread holding B
     constexpr int nchunk = NK / KPAR;
     for (int ch = 0; ch < nchunk; ++ch) {
         const int k0 = 1 + ch * KPAR;
@@ -827,7 +869,32 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
         }
         if constexpr (!Pol<T>::exact) {
             if (push.tgt != nullptr) push_faces_part<T, S, S::VPT>(out, push, b, ii, jj, kp, o, v0);
+            if (cfl_next) {   // uniform over the CTA
+#pragma unroll
+                for (int t = 0; t < S::VPT; ++t) cnan |= (o[t] != o[t]);
+                float v2 = 0.f, b2 = 0.f;
+                if constexpr (S::TPC == 1) {
+                    v2 = cfl_sq3(o[V_VR], o[V_VT], o[V_VP]);
+                    b2 = cfl_sq3(o[V_BR], o[V_BT], o[V_BP]);
+                } else {
+                    if (v0 != 0) sb2[c] = cfl_sq3(o[V_BR - 4], o[V_BT - 4], o[V_BP - 4]);
+                    __syncthreads();
+                    if (v0 == 0) {
+                        v2 = cfl_sq3(o[V_VR], o[V_VT], o[V_VP]);
+                        b2 = sb2[c];
+                    }
+                }
+                if (v0 == 0) {
+                    float ratio = cfl_ratio_f(v2, b2, GCS[ii], gi[GI_RHO0 * NIP + ii], rc, gj[GJ_SIN * S::NJP + jj],
+                                              gs[GS_DXI], gs[GS_DXJ], gs[GS_DXK]);
+                    if (ratio != ratio) { cnan = 1; ratio = INFINITY; }
+                    cmin = fminf(cmin, ratio);
+                }
+            }
         }
+    }
+    if constexpr (!Pol<T>::exact) {
+        if (cfl_next) cfl_commit(cmin, cnan, sc);
     }
 }
 
@@ -858,10 +925,16 @@ __global__ void __launch_bounds__(256) k_cfl(const T* u, Geometry g, StepScalars
         const T* Gs = gs_ptr<T>(g) + (size_t)b * GS_COUNT;
         // h_LLL = min(dxi, r*dxj, r*sin(theta)*dxk) (3_6/ModBlock.f90:416-425)
         const T r = Gi[GI_R * d.nip + i];
-        const T h = fmin(fmin(Gs[GS_DXI], r * Gs[GS_DXJ]), r * Gj[GJ_SIN * d.njp + j] * Gs[GS_DXK]);
-        T w = Gi[GI_CS * d.nip + i] + sqrt(x[V_VR] * x[V_VR] + x[V_VT] * x[V_VT] + x[V_VP] * x[V_VP]);
-        w = w + sqrt(x[V_BR] * x[V_BR] + x[V_BT] * x[V_BT] + x[V_BP] * x[V_BP]) / sqrt(Gi[GI_RHO0 * d.nip + i]);
-        ratio = h / w;                     // the reference's h_LLL/v_wave
+        if constexpr (Pol<T>::exact) {
+            const T h = fmin(fmin(Gs[GS_DXI], r * Gs[GS_DXJ]), r * Gj[GJ_SIN * d.njp + j] * Gs[GS_DXK]);
+            T w = Gi[GI_CS * d.nip + i] + sqrt(x[V_VR] * x[V_VR] + x[V_VT] * x[V_VT] + x[V_VP] * x[V_VP]);
+            w = w + sqrt(x[V_BR] * x[V_BR] + x[V_BT] * x[V_BT] + x[V_BP] * x[V_BP]) / sqrt(Gi[GI_RHO0 * d.nip + i]);
+            ratio = h / w;                 // the reference's h_LLL/v_wave
+        } else {
+            ratio = cfl_ratio_f(cfl_sq3(x[V_VR], x[V_VT], x[V_VP]), cfl_sq3(x[V_BR], x[V_BT], x[V_BP]),
+                                Gi[GI_CS * d.nip + i], Gi[GI_RHO0 * d.nip + i], r, Gj[GJ_SIN * d.njp + j],
+                                Gs[GS_DXI], Gs[GS_DXJ], Gs[GS_DXK]);
+        }
         if (ratio != ratio) { nan = 1; ratio = R(INFINITY); }
     }
 #pragma unroll

@@ -17,8 +17,8 @@ cudaError_t launch_psi_ghost_mixed(const StepDims& d, const GhostLists& gl, floa
     return impl::psi_ghost_any<float>(d, gl, psi, st);
 }
 cudaError_t launch_diffusion_mixed(const StepDims& d, const Geometry& g, const float* u, float* out, int8_t* lo,
-                                   const PushTable& push, StepScalars* sc, int kpar, cudaStream_t st) {
-    return impl::diff_any<float>(d, g, u, out, lo, push, sc, kpar, st);
+                                   const PushTable& push, StepScalars* sc, int kpar, cudaStream_t st, int cfl_next) {
+    return impl::diff_any<float>(d, g, u, out, lo, push, sc, kpar, st, cfl_next);
 }
 cudaError_t launch_cfl_mixed(const StepDims& d, const Geometry& g, const float* u, StepScalars* sc, cudaStream_t st) {
     return impl::cfl_any<float>(d, g, u, sc, st);
