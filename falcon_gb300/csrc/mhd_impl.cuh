@@ -280,11 +280,32 @@ __device__ __forceinline__ double blend(double a, double b, double uw, double w)
 // blends it with the next cell along i, taken from the next lane (i is the
 // fastest thread index, and the second cell is never beyond the row). Every
 // thread of the CTA calls this (the shuffle needs the full warp).
+// The push-table entries of one block, staged in shared memory before the
+// kernel's first barrier: they are read at the end of every k-chunk, and as
+// global loads their latency held every warp at the chunk's end.
+struct PushBlock {
+    int32_t tgt[6];
+    int32_t src[4], dst[4];   // [side][layer]
+    float w[4];
+};
+__device__ __forceinline__ void load_push_block(const PushTable& P, int b, PushBlock* s) {
+    const int t = threadIdx.x;
+    if (P.tgt == nullptr) return;
+    if (t < 6) {
+        s->tgt[t] = P.tgt[6 * b + t];
+    } else if (t < 10) {
+        const int q = t - 6;
+        s->src[q] = P.rad_src[4 * b + q];
+        s->dst[q] = P.rad_dst[4 * b + q];
+        s->w[q] = P.rad_w[4 * b + q];
+    }
+}
+
 template <class T, class S, int VN>
-__device__ __forceinline__ void push_faces_part(T* out, const PushTable& P, int b, int ii, int jj, int kp,
+__device__ __forceinline__ void push_faces_part(T* out, const PushBlock& P, int ii, int jj, int kp,
                                                 const T (&o)[VN], int v0) {
     constexpr int NJ = S::NJP - 4, NK = S::NKP - 4;
-    const int32_t* tg = P.tgt + 6 * b;
+    const int32_t* tg = P.tgt;
     auto put = [&](int tb, int kt, int jt, int it, const T (&val)[VN]) {
         T* dst = out + ((size_t)tb * NV + v0) * S::NCELL + ((size_t)kt * S::NJP + jt) * S::NIP + it;
 #pragma unroll
@@ -303,21 +324,20 @@ __device__ __forceinline__ void push_faces_part(T* out, const PushTable& P, int 
             if (tg[side] < 0) continue;
 #pragma unroll
             for (int layer = 0; layer < 2; ++layer) {
-                const int q = (b * 2 + side) * 2 + layer;
-                if (ii != P.rad_src[q]) continue;
-                const T w = (T)P.rad_w[q], uw = T(1) - w;
+                const int q = side * 2 + layer;
+                if (ii != P.src[q]) continue;
+                const T w = (T)P.w[q], uw = T(1) - w;
                 T val[VN];
 #pragma unroll
                 for (int v = 0; v < VN; ++v) val[v] = w == T(0) ? o[v] : blend(o[v], nx[v], uw, w);
-                put(tg[side], kp, jj, P.rad_dst[q], val);
+                put(tg[side], kp, jj, P.dst[q], val);
             }
         }
     }
 }
 template <class T, class S>
-__device__ __forceinline__ void push_faces(T* out, const PushTable& P, int b, int ii, int jj, int kp,
-                                           const T (&o)[NV]) {
-    push_faces_part<T, S, NV>(out, P, b, ii, jj, kp, o, 0);
+__device__ __forceinline__ void push_faces(T* out, const PushBlock& P, int ii, int jj, int kp, const T (&o)[NV]) {
+    push_faces_part<T, S, NV>(out, P, ii, jj, kp, o, 0);
 }
 
 // Cell (i, j, kq) of a thread in a k-chunk. With 16-wide rows and an even
@@ -362,6 +382,8 @@ k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, DivBArgs 
     const int fl = g.flags[b];
     const T* blk_in = in + (size_t)b * NV * NCELL;
     T* wb = bc_writeback ? const_cast<T*>(blk_in) : nullptr;
+    __shared__ PushBlock pb;
+    load_push_block(push, b, &pb);
     if (threadIdx.x == 0) {
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
@@ -629,7 +651,7 @@ k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, DivBArgs 
 #pragma unroll
         for (int v = 0; v < NV; ++v) out[base + (size_t)v * NCELL] = o[v];
         if constexpr (!Pol<T>::exact) {
-            if (push.tgt != nullptr) push_faces<T, S>(out, push, b, ii, jj, kp, o);
+            if (push.tgt != nullptr) push_faces<T, S>(out, pb, ii, jj, kp, o);
         }
     }
 }
@@ -726,6 +748,8 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
     const T* blk = u + (size_t)b * NV * NCELL;
     T* oblk = out + (size_t)b * NV * NCELL;
     const bool copy_bc = out != u && (g.flags[b] & 6);
+    __shared__ PushBlock pb;
+    load_push_block(push, b, &pb);
     if (threadIdx.x == 0) {
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
@@ -868,7 +892,7 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
             oblk[(size_t)v * NCELL + base] = o[t];
         }
         if constexpr (!Pol<T>::exact) {
-            if (push.tgt != nullptr) push_faces_part<T, S, S::VPT>(out, push, b, ii, jj, kp, o, v0);
+            if (push.tgt != nullptr) push_faces_part<T, S, S::VPT>(out, pb, ii, jj, kp, o, v0);
             if (cfl_next) {   // uniform over the CTA
 #pragma unroll
                 for (int t = 0; t < S::VPT; ++t) cnan |= (o[t] != o[t]);
