@@ -747,7 +747,8 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
     const int b = blockIdx.x;
     const T* blk = u + (size_t)b * NV * NCELL;
     T* oblk = out + (size_t)b * NV * NCELL;
-    const bool copy_bc = out != u && (g.flags[b] & 6);
+    const int flb = g.flags[b];
+    const bool copy_bc = out != u && (flb & 6);
     __shared__ PushBlock pb;
     load_push_block(push, b, &pb);
     if (threadIdx.x == 0) {
@@ -788,6 +789,17 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
         __syncthreads();   // ring slots and face arrays of the previous chunk are free
         if (threadIdx.x == 0 && ch + 1 < nchunk) issue_planes<T, S>(blk, tile, hi, hi + KPAR, &bars[(ch + 1) & 1]);
         if (ch + 1 < nchunk) prefetch_lo(k0 + KPAR + 1);
+        // this thread's int8 corrections, loaded now so that their latency
+        // overlaps the copy wait and the face phase
+        int8_t qlo[S::VPT];
+        if constexpr (!Pol<T>::exact) {
+            if (ulo != nullptr) {
+                const int8_t* q = ulo + (size_t)b * NV * NCELL + (size_t)v0 * NCELL +
+                                  (size_t)(k0 + 1 + kq) * PL + jj * NIP + ii;
+#pragma unroll
+                for (int t = 0; t < S::VPT; ++t) qlo[t] = q[(size_t)t * NCELL];
+            }
+        }
         if (!mbar_wait(&bars[ch & 1], (uint32_t)((ch >> 1) & 1), kWaitPolls)) {
             atomicOr(&sc->nan_flag, 2);
             mbar_wait(&bars[(ch + 1) & 1], (uint32_t)(((ch + 1) >> 1) & 1), kWaitPolls);
@@ -796,7 +808,7 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
         const int kp0 = k0 + 1;   // padded index of the chunk's first plane
         const int kp = kp0 + kq;
         if (copy_bc) {   // radial boundary ghost columns of the planes new to this chunk
-            const int plo = ch == 0 ? 0 : k0 + 3, phi = k0 + KPAR + 3, fl = g.flags[b];
+            const int plo = ch == 0 ? 0 : k0 + 3, phi = k0 + KPAR + 3, fl = flb;
             const int total = (phi - plo) * S::NJP * NV * 4;
             for (int x = tid; x < total; x += S::NT) {
                 const int c4 = x & 3, r = x >> 2;
@@ -882,10 +894,9 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
             if constexpr (Pol<T>::exact) {
                 o[t] = (T)((double)u0 + hdt * (double)R);
             } else if (ulo != nullptr) {
-                int8_t* q = ulo + (size_t)b * NV * NCELL + (size_t)v * NCELL + base;
                 int8_t q1;
-                o[t] = ff_add((float)u0, *q, __fmul_rn(hdt_f, (float)R), q1);
-                *q = q1;
+                o[t] = ff_add((float)u0, qlo[t], __fmul_rn(hdt_f, (float)R), q1);
+                ulo[(size_t)b * NV * NCELL + (size_t)v * NCELL + base] = q1;
             } else {
                 o[t] = fmaf(hdt_f, (float)R, (float)u0);
             }
