@@ -316,6 +316,35 @@ __device__ __forceinline__ void push_faces_part(T* out, const PushBlock& P, int 
     if (kp <= 3 && tg[4] >= 0) put(tg[4], kp + NK, jj, ii, o);
     if (kp >= NK && tg[5] >= 0) put(tg[5], kp - NK, jj, ii, o);
     if (tg[0] >= 0 || tg[1] >= 0) {   // uniform over the CTA
+        if constexpr (S::NIP == 20 && 2 * VN <= 16) {
+            // 16-wide rows: every half-warp holds one full row (i = lane % 16).
+            // Lane (v, layer) = (lh / 2, lh % 2) of the half gathers its value
+            // from the row's source lanes, so a side takes one store per row
+            // instead of a divergent store per variable and layer.
+            const int lane = threadIdx.x & 31, lh = lane & 15, hb = lane & 16;
+            const int v = lh >> 1, layer = lh & 1;
+#pragma unroll
+            for (int side = 0; side < 2; ++side) {
+                if (tg[side] < 0) continue;
+                const int q = side * 2 + layer;
+                const int s0 = hb + P.src[q] - 2;
+                const bool two = P.w[side * 2] != 0.f || P.w[side * 2 + 1] != 0.f;   // uniform
+                T a = T(0), c = T(0);
+#pragma unroll
+                for (int u = 0; u < VN; ++u) {
+                    const T x0 = __shfl_sync(0xffffffffu, o[u], s0);
+                    T x1 = T(0);
+                    if (two) x1 = __shfl_sync(0xffffffffu, o[u], s0 + 1);
+                    if (u == v) { a = x0; c = x1; }
+                }
+                if (v < VN) {
+                    const T w = (T)P.w[q];
+                    const T val = w == T(0) ? a : blend(a, c, T(1) - w, w);
+                    out[((size_t)tg[side] * NV + v0 + v) * S::NCELL + ((size_t)kp * S::NJP + jj) * S::NIP + P.dst[q]] = val;
+                }
+            }
+            return;
+        }
         T nx[VN];
 #pragma unroll
         for (int v = 0; v < VN; ++v) nx[v] = __shfl_down_sync(0xffffffffu, o[v], 1);

@@ -152,6 +152,31 @@ def test_mixed_step_matches_phase_sequence():
     assert np.array_equal(ua, ub)
 
 
+@pytest.mark.parametrize("radial_option", [1, 2])
+def test_mixed_step_matches_phase_sequence_16(radial_option):
+    """As above on 16^3 blocks (108 blocks), where the radial faces are pushed
+    by half-warp gathers: option 1 splits the shell radially at the density
+    scale-height midpoint (radial neighbours of different spacing, blended
+    pushes), option 2 at the arithmetic midpoint."""
+    mk = lambda: config.make_config(block=(16, 16, 16), root_tiles=(1, 3, 9), radial_levels=1,
+                                    radial_option=radial_option, amr=(), precision=config.PREC_MIXED)
+    a, b = fg.Falcon(mk()), fg.Falcon(mk())
+    st = a.exchange_stats()
+    assert st["pushed_faces"] > 0 and st["pushed_cells"] > 0
+    u0 = synth.initial_state(mk(), a.block_ranges(), a.block_flags(), seed=1004)
+    for x in (a, b):
+        x.upload_state(u0)
+        x.exchange()
+    for _ in range(3):
+        a.advance_rk4(want_dt=False)
+        for ph in range(6):
+            b.step_phase(ph)
+    a.synchronize()
+    ua, ub = a.download_state(), b.download_state()
+    assert np.isfinite(ua).all()
+    assert np.array_equal(ua, ub)
+
+
 def test_full_size_mixed_properties():
     """21M cells, 5,184 blocks of 16^3: steps stay finite, the exchange is
     idempotent (bit-exact), dt is positive and stable."""
