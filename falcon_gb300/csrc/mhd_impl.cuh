@@ -705,7 +705,29 @@ struct DShape : Shape<T, NI, NJ, NK, KPAR> {
     static constexpr int NT = NCELLS * TPC;
     static constexpr int VPT = NV / TPC;
     static constexpr int KS = KPAR + 1;                  // k-face ring slots
-    static constexpr int NFI = NV * KPAR * NJ * (NI + 1);
+    // FP32, 16-wide rows: a warp takes rows j and j+4 of a plane (80 floats,
+    // 16 banks apart) so that its two halves touch disjoint banks in every
+    // tile access (rows j and j+1, 20 floats apart, share 4 banks). The i-face
+    // rows get a pitch of 20 for the same reason, and the j- and k-face rows
+    // are stored in the order rpos() that puts the two rows of a warp side by side.
+    static constexpr bool R4 = sizeof(T) == 4 && NI == 16 && NJ % 8 == 0;
+    static constexpr int FIP = R4 ? 20 : NI + 1;         // i-face row pitch
+    __device__ static __forceinline__ void cell(int c, int& i, int& j, int& kq) {
+        kq = c / (NI * NJ);
+        const int cc = c % (NI * NJ);
+        i = cc % NI;
+        if constexpr (R4) {
+            const int w = cc / 32;
+            j = (w % 4) + 8 * (w / 4) + 4 * ((cc / 16) % 2);
+        } else {
+            j = cc / NI;
+        }
+    }
+    __device__ static __forceinline__ int rpos(int j) {   // j in [0, NJ]; NJ maps to itself
+        if constexpr (R4) return j >= NJ ? NJ : 2 * ((j % 4) + 4 * (j / 8)) + ((j / 4) % 2);
+        else return j;
+    }
+    static constexpr int NFI = NV * KPAR * NJ * FIP;
     static constexpr int NFJ = NV * KPAR * (NJ + 1) * NI;
     static constexpr int NFK = KS * NV * NJ * NI;
     // shared memory: mbarriers | tile[NV][W][PL] | FI | FJ | FK | gi | gj | gs
@@ -801,8 +823,9 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
     const T* GCS = gi + GI_CS * NIP;
     // the cell and variables this thread sums and updates
     const int c = tid % S::NCELLS, v0 = (tid / S::NCELLS) * S::VPT;
-    const int i = c % NI, j = (c / NI) % NJ, kq = c / (NI * NJ);
-    const int ii = i + 2, jj = j + 2;
+    int i, j, kq;
+    S::cell(c, i, j, kq);
+    const int ii = i + 2, jj = j + 2, jr = S::rpos(j), jr1 = S::rpos(j + 1);
     const T rc = gi[GI_R * NIP + ii];
     const T den[3] = {gs[GS_DXI], gs[GS_DXJ] * rc, gs[GS_DXK] * rc * gj[GJ_SIN * S::NJP + jj]};
     const T dinv[3] = {T(1) / den[0], T(1) / den[1], T(1) / den[2]};
@@ -861,13 +884,13 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
             const T cs = GCS[ii];
             const T cLj = fabs(tc[V_VT * W * PL - NIP]) + cs, cRj = fabs(tc[V_VT * W * PL]) + cs;
             const T cLk = fabs(t0[V_VP * W * PL + so[2]]) + cs, cRk = fabs(t0[V_VP * W * PL + so[3]]) + cs;
-            T* fkw = FK + ((size_t)((kp - 1) % KS) * NV) * NJ * NI + j * NI + i;
+            T* fkw = FK + ((size_t)((kp - 1) % KS) * NV) * NJ * NI + jr * NI + i;
 #pragma unroll
             for (int t = 0; t < S::VPT; ++t) {
                 const int v = v0 + t;
                 const T* a = tc + v * W * PL;
-                FI[((v * KPAR + kq) * NJ + j) * (NI + 1) + i] = face_flux(a[-2], a[-1], a[0], a[1], cLi, cRi);
-                FJ[((v * KPAR + kq) * (NJ + 1) + j) * NI + i] =
+                FI[((v * KPAR + kq) * NJ + j) * S::FIP + i] = face_flux(a[-2], a[-1], a[0], a[1], cLi, cRi);
+                FJ[((v * KPAR + kq) * (NJ + 1) + jr) * NI + i] =
                     face_flux(a[-2 * NIP], a[-NIP], a[0], a[NIP], cLj, cRj);
                 const T* ak = t0 + v * W * PL;
                 fkw[v * NJ * NI] = face_flux(ak[so[1]], ak[so[2]], ak[so[3]], ak[so[4]], cLk, cRk);
@@ -881,7 +904,7 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
                 const T* a = tile + (v * W + (kp0 + q) % W) * PL + y * NIP + NI + 1;   // last interior cell
                 const T* vr = tile + (V_VR * W + (kp0 + q) % W) * PL + y * NIP + NI + 1;
                 const T cL = fabs(vr[0]) + GCS[NI + 1], cR = fabs(vr[1]) + GCS[NI + 2];
-                FI[((v * KPAR + q) * NJ + (y - 2)) * (NI + 1) + NI] = face_flux(a[-1], a[0], a[1], a[2], cL, cR);
+                FI[((v * KPAR + q) * NJ + (y - 2)) * S::FIP + NI] = face_flux(a[-1], a[0], a[1], a[2], cL, cR);
             } else {
                 const int z = x - NXI;
                 const int xx = z % NI + 2, q = (z / NI) % KPAR, v = z / (NI * KPAR);
@@ -901,23 +924,23 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
                 const T* vp = tile + (size_t)V_VP * W * PL + y * NIP + xx;
                 const T cs = GCS[xx];
                 const T cL = fabs(vp[PL]) + cs, cR = fabs(vp[2 * PL]) + cs;
-                FK[((0 * NV + v) * NJ + (y - 2)) * NI + (xx - 2)] =
+                FK[((0 * NV + v) * NJ + S::rpos(y - 2)) * NI + (xx - 2)] =
                     face_flux(a[0], a[PL], a[2 * PL], a[3 * PL], cL, cR);
             }
         }
         __syncthreads();
         const size_t base = (size_t)kp * PL + jj * NIP + ii;
-        const T* fk_l = FK + ((size_t)((kp - 2) % KS) * NV) * NJ * NI + j * NI + i;
-        const T* fk_r = FK + ((size_t)((kp - 1) % KS) * NV) * NJ * NI + j * NI + i;
+        const T* fk_l = FK + ((size_t)((kp - 2) % KS) * NV) * NJ * NI + jr * NI + i;
+        const T* fk_r = FK + ((size_t)((kp - 1) % KS) * NV) * NJ * NI + jr * NI + i;
         T o[S::VPT];
 #pragma unroll
         for (int t = 0; t < S::VPT; ++t) {
             const int v = v0 + t;
-            const T* fi = FI + ((v * KPAR + kq) * NJ + j) * (NI + 1) + i;
-            const T* fj = FJ + ((v * KPAR + kq) * (NJ + 1) + j) * NI + i;
+            const T* fi = FI + ((v * KPAR + kq) * NJ + j) * S::FIP + i;
+            const T* fj = FJ + ((v * KPAR + kq) * (NJ + 1)) * NI + i;
             T R = T(0);
             R = R + Pol<T>::dv(fi[0] - fi[1], den[0], dinv[0]);
-            R = R + Pol<T>::dv(fj[0] - fj[NI], den[1], dinv[1]);
+            R = R + Pol<T>::dv(fj[jr * NI] - fj[jr1 * NI], den[1], dinv[1]);
             R = R + Pol<T>::dv(fk_l[v * NJ * NI] - fk_r[v * NJ * NI], den[2], dinv[2]);
             const T u0 = t0[v * W * PL + so[2]];
             if constexpr (Pol<T>::exact) {
