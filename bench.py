@@ -283,27 +283,34 @@ def run_ours(args, rank, world, local, dist):
 
     # ---- end to end through the C ABI with host buffers: every step uploads
     # the FP64 Fortran-layout state from pinned host memory, advances, and
-    # downloads the new state (the drop-in keeps Tree%LocalBlocks authoritative)
-    e2e_val = res_val = None
-    nbytes = 0
+    # downloads the new state (the drop-in keeps Tree%LocalBlocks authoritative).
+    # Headline: core transfers (interior planes x interior rows of every block
+    # and variable; theta/phi ghost layers recomputed on the device); also the
+    # whole padded array moved both ways.
+    e2e_val = res_val = full_val = None
+    nbytes = full_bytes = 0
     k_e2e = max(1, min(args.steps, 10))
     if not args.no_e2e:
         host = np.empty(f.shape, dtype=np.float64)
         f.pin_host(host)
         f.download_state_into(host)
         f.synchronize()
-        barrier(dist)
-        t0 = time.perf_counter()
-        for _ in range(k_e2e):
-            f.upload_state_raw(host)
-            f.advance_rk4(want_dt=True)
-            f.download_state_into(host)
-        e2e_s = time.perf_counter() - t0
-        barrier(dist)
-        e2e_s = reduce_max(dist, e2e_s)
-        e2e_val = reduce_sum(dist, float(cells * k_e2e)) / e2e_s
+
+        def e2e_loop(up, down):
+            barrier(dist)
+            t0 = time.perf_counter()
+            for _ in range(k_e2e):
+                up(host)
+                f.advance_rk4(want_dt=True)
+                down(host)
+            dt_s = reduce_max(dist, time.perf_counter() - t0)
+            return reduce_sum(dist, float(cells * k_e2e)) / dt_s
+
+        e2e_val = e2e_loop(f.upload_state_core, f.download_state_core)
+        full_val = e2e_loop(f.upload_state_raw, f.download_state_into)
         f.unpin_host(host)
-        nbytes = host.nbytes
+        full_bytes = host.nbytes
+        nbytes = host[:, :, 2:-2, 2:-2, :].size * 8
         # resident variant: the state stays on the GPU, dt comes back every step
         t0 = time.perf_counter()
         for _ in range(k_e2e):
@@ -332,7 +339,11 @@ def run_ours(args, rank, world, local, dist):
             "tuning": f.tuning(), "ghost_lists": lists, "stage_exchange": f.exchange_stats(),
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
-                    "mode": "state uploaded and downloaded (FP64, pinned) every step"},
+                    "mode": "core of the FP64 state (interior planes x interior rows, pinned) uploaded and "
+                            "downloaded every step; theta/phi ghost layers recomputed on the device"},
+            "e2e_full_array": {"value": full_val, "unit": UNIT, "h2d_bytes_per_step": full_bytes,
+                               "d2h_bytes_per_step": full_bytes,
+                               "mode": "whole padded FP64 state (pinned) uploaded and downloaded every step"},
             "setup_s": round(setup_s, 3),
             "e2e_resident": {"value": res_val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 8},
             "gpu_launches": launches_per_step * args.steps,

@@ -52,6 +52,7 @@ EXPORTS = (
     "falcon_lcc_create", "falcon_lcc_destroy", "falcon_lcc_last_error", "falcon_lcc_num_params",
     "falcon_lcc_get_params", "falcon_lcc_set_params", "falcon_lcc_forward", "falcon_lcc_loss_grad",
     "falcon_lcc_train", "falcon_save_allcells", "falcon_save_restart", "falcon_load_restart",
+    "falcon_upload_state_core", "falcon_download_state_core",
 )
 
 # size of the static device array behind falcon_download_state_range
@@ -182,6 +183,18 @@ class Falcon:
 
     def download_state_into(self, u):
         self._ck(self.L.falcon_download_state(self.h, _ptr(u)))
+        return u
+
+    def upload_state_core(self, u):
+        """Upload the core of u (interior planes x interior rows of every block
+        and variable, radial ghost columns included); the theta/phi ghost layers
+        are recomputed on the device. u: C-contiguous float64 of self.shape,
+        pinned with pin_host for the in-place path (else a full upload runs)."""
+        self._ck(self.L.falcon_upload_state_core(self.h, _ptr(u)))
+
+    def download_state_core(self, u):
+        """Write the core of the state into u; its other cells are left as they are."""
+        self._ck(self.L.falcon_download_state_core(self.h, _ptr(u)))
         return u
 
     def pin_host(self, a):

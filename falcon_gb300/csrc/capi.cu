@@ -954,6 +954,68 @@ int falcon_download_state_range(falcon_ctx* ctx, size_t first, size_t count, dou
     return FALCON_OK;
 }
 
+// Core transfers: only the interior planes x interior rows of the host array
+// move (64% of a 16^3 block's padded cells); the theta/phi ghost layers are
+// recomputed on the device by a full exchange (upload) or left as they are
+// in host memory (download). They need the array pinned with falcon_pin_host
+// (read and written in place over the host link); otherwise, and for an
+// upload into a context without a second state buffer (FP64 path), the full
+// transfer runs instead.
+int falcon_upload_state_core(falcon_ctx* ctx, const double* u) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    if (!u) return ctx->fail(FALCON_ERR_INVALID_ARG, "null state");
+    const double* src = (const double*)mapped_host(ctx, u, host_elems(ctx) * 8);
+    if (!src || !ctx->mixed() || !ctx->R2 || ((uintptr_t)src % 16) != 0) return falcon_upload_state(ctx, u);
+    // into the second state buffer (and the stage buffer as int8 scratch for
+    // the corrections), so that a rejected array (psi not 0) leaves the state
+    // as it was
+    if (!ctx->dflag) CK(ctx->alloc(&ctx->dflag, sizeof(int32_t)), "alloc flag");
+    int8_t* lo_tmp = (int8_t*)ctx->RK;
+    const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
+    CK(cudaMemsetAsync(lo_tmp, 0, n, ctx->st), "upload core");   // ghost cells carry no correction
+    CK(launch_core_up(src, ctx->R2, lo_tmp, ctx->P ? ctx->P2 : nullptr, ctx->P ? nullptr : ctx->dflag, true, ctx->dims,
+                      ctx->st),
+       "upload core");
+    int32_t bad = 0;
+    if (!ctx->P) CK(cudaMemcpyAsync(&bad, ctx->dflag, sizeof bad, cudaMemcpyDeviceToHost, ctx->st), "upload core");
+    CK(cudaStreamSynchronize(ctx->st), "upload core");
+    if (bad) {
+        CK(mirror_state(ctx), "upload core");
+        CK(cudaStreamSynchronize(ctx->st), "upload core");
+        return ctx->fail(FALCON_ERR_INVALID_ARG, "psi must be 0 unless divb_option = 1");
+    }
+    std::swap(ctx->U, ctx->R2);
+    CK(cudaMemcpyAsync(ctx->Ulo, lo_tmp, n, cudaMemcpyDeviceToDevice, ctx->st), "upload core");
+    CK(ghost(ctx, ctx->U), "upload core");
+    ctx->stale_edges = false;
+    ctx->cfl_ready = false;
+    CK(cudaMemcpyAsync(ctx->RK, ctx->U, n * ctx->elem, cudaMemcpyDeviceToDevice, ctx->st), "upload core");
+    CK(mirror_state(ctx), "upload core");
+    if (ctx->P) {
+        const size_t np = (size_t)ctx->dims.nblocks * ctx->dims.ncell * ctx->elem;
+        CK(cudaMemcpyAsync(ctx->P, ctx->P2, np, cudaMemcpyDeviceToDevice, ctx->st), "upload core");
+        CK(launch_psi_ghost_mixed(ctx->dims, ctx->gl, (float*)ctx->P, ctx->st), "upload core");
+        for (void* q : {ctx->Prk, ctx->P2}) CK(cudaMemcpyAsync(q, ctx->P, np, cudaMemcpyDeviceToDevice, ctx->st), "upload core");
+    }
+    CK(cudaStreamSynchronize(ctx->st), "upload core");
+    return FALCON_OK;
+}
+
+int falcon_download_state_core(falcon_ctx* ctx, double* u) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    if (!u) return ctx->fail(FALCON_ERR_INVALID_ARG, "null state");
+    double* dst = (double*)mapped_host(ctx, u, host_elems(ctx) * 8);
+    if (!dst || ((uintptr_t)dst % 16) != 0) return falcon_download_state(ctx, u);
+    // the core cells are current after a step (its last exchange and the
+    // radial boundary copy cover them); only edge ghosts are left stale
+    CK(launch_core_down(ctx->U, ctx->mixed() ? ctx->Ulo : nullptr, ctx->P, ctx->mixed(), dst, ctx->dims, ctx->st),
+       "download core");
+    CK(cudaStreamSynchronize(ctx->st), "download core");
+    return FALCON_OK;
+}
+
 int falcon_pin_host(falcon_ctx* ctx, void* p, size_t bytes) {
     int rc = need_device(ctx);
     if (rc) return rc;

@@ -229,6 +229,13 @@ __host__ __device__ inline int allcells_table_stride(const StepDims& d) {
 cudaError_t launch_allcells(const StepDims& d, const void* U, const int8_t* lo, const void* psi, bool fp32,
                             const double* tab, int b0, int nbb, double* out, cudaStream_t st);
 
+// Core transfers (interior planes x interior rows of every block and
+// variable of the host array, radial ghost columns included), host array
+// 16-byte aligned; U is FP32 (with its correction lo) or FP64.
+cudaError_t launch_core_up(const double* host, void* U, int8_t* lo, void* P, int32_t* flag, bool fp32, const StepDims& dm,
+                           cudaStream_t st);
+cudaError_t launch_core_down(const void* U, const int8_t* lo, const void* P, bool fp32, double* host, const StepDims& dm,
+                             cudaStream_t st);
 cudaError_t launch_gather_host(const void* U, const int8_t* lo, const void* psi, bool fp32, int64_t first, int64_t count,
                                int64_t ncell, double* out, cudaStream_t st);
 

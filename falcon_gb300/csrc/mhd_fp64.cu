@@ -215,6 +215,114 @@ __global__ void k_gather_host_wide(const T* U, const int8_t* lo, const T* psi, i
 }
 bool wide_ok(const void* p, int64_t ncell) { return ((uintptr_t)p % 16) == 0 && ncell % 2 == 0; }
 
+// Core transfers: of every block and variable of the host array (9 per block,
+// psi last), the interior planes and within them the interior rows, each
+// row whole (its radial ghost columns, which hold the radial boundary
+// condition, included). Element x of the core enumerates (block, var, plane,
+// offset in the plane's run of rows); runs are NJ*NIP long and even, so the
+// pairs of the wide loop never straddle a run.
+struct CoreIdx {
+    int64_t host, cell, b;   // host element, cell offset in the block, block
+    int v;                   // 0..NV-1 state, NV psi
+    bool interior;           // not a radial ghost column
+};
+__device__ __forceinline__ CoreIdx core_index(int64_t x, const StepDims& dm) {
+    const int64_t run = (int64_t)(dm.njp - 4) * dm.nip, per = (int64_t)(dm.nkp - 4) * run;
+    const int64_t bv = x / per, r = x - bv * per;
+    const int64_t kp = 2 + r / run, o = r % run;
+    CoreIdx c;
+    c.b = bv / (NV + 1);
+    c.v = (int)(bv - c.b * (NV + 1));
+    c.cell = kp * dm.nip * dm.njp + 2 * dm.nip + o;
+    c.host = bv * dm.ncell + c.cell;
+    const int ip = (int)(o % dm.nip);
+    c.interior = ip >= 2 && ip < dm.nip - 2;
+    return c;
+}
+// host core -> device: state cells narrowed (FP32 with its correction) or
+// copied (FP64); psi converted into P, or, without P, tested for 0 (flag)
+template <class T>
+__global__ void k_core_up(const double* s, T* U, int8_t* lo, T* P, int32_t* flag, int64_t n, StepDims dm) {
+    const int64_t lane2 = 2 * (threadIdx.x & 31);
+    int any = 0;
+    for (int64_t w0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32 * kWide; w0 < n;
+         w0 += (((int64_t)gridDim.x * blockDim.x) >> 5) * 32 * kWide) {
+        double2 v[kWide / 2];
+#pragma unroll
+        for (int q = 0; q < kWide / 2; ++q)
+            if (w0 + 64 * q + lane2 < n)
+                v[q] = *reinterpret_cast<const double2*>(s + core_index(w0 + 64 * q + lane2, dm).host);
+#pragma unroll
+        for (int q = 0; q < kWide / 2; ++q) {
+            if (w0 + 64 * q + lane2 >= n) continue;
+            const CoreIdx c = core_index(w0 + 64 * q + lane2, dm);
+            const double u2[2] = {v[q].x, v[q].y};
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int64_t cell = c.cell + h;
+                const bool in = h == 0 ? c.interior : (int)((cell % dm.nip)) >= 2 && (int)(cell % dm.nip) < dm.nip - 2;
+                if (c.v < NV) {
+                    const int64_t e = (c.b * NV + c.v) * dm.ncell + cell;
+                    if constexpr (sizeof(T) == 4) {
+                        const float hi = (float)u2[h];
+                        U[e] = hi;
+                        if (lo) lo[e] = in ? lo_encode64(hi, u2[h] - (double)hi) : (int8_t)0;
+                    } else {
+                        U[e] = (T)u2[h];
+                    }
+                } else if (P) {
+                    P[c.b * dm.ncell + cell] = (T)u2[h];
+                } else {
+                    any |= u2[h] != 0.0;
+                }
+            }
+        }
+    }
+    if (flag && __any_sync(0xffffffffu, any) && (threadIdx.x & 31) == 0) *flag = 1;
+}
+// device -> host core (psi 0 without P)
+template <class T>
+__global__ void k_core_down(const T* U, const int8_t* lo, const T* P, double* out, int64_t n, StepDims dm) {
+    const int64_t lane2 = 2 * (threadIdx.x & 31);
+    for (int64_t w0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32 * kWide; w0 < n;
+         w0 += (((int64_t)gridDim.x * blockDim.x) >> 5) * 32 * kWide) {
+        double2 v[kWide / 2];
+        int64_t hs[kWide / 2];
+#pragma unroll
+        for (int q = 0; q < kWide / 2; ++q) {
+            if (w0 + 64 * q + lane2 >= n) continue;
+            const CoreIdx c = core_index(w0 + 64 * q + lane2, dm);
+            hs[q] = c.host;
+            double u2[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int64_t cell = c.cell + h;
+                if (c.v < NV) {
+                    const int64_t e = (c.b * NV + c.v) * dm.ncell + cell;
+                    const T hi = U[e];
+                    double x = (double)hi;
+                    if constexpr (sizeof(T) == 4) {
+                        if (lo) x += (double)lo[e] * (double)lo_unit((float)hi);
+                    }
+                    u2[h] = x;
+                } else {
+                    u2[h] = P ? (double)P[c.b * dm.ncell + cell] : 0.0;
+                }
+            }
+            v[q] = make_double2(u2[0], u2[1]);
+        }
+#pragma unroll
+        for (int q = 0; q < kWide / 2; ++q)
+            if (w0 + 64 * q + lane2 < n) *reinterpret_cast<double2*>(out + hs[q]) = v[q];
+    }
+}
+int64_t core_elems(const StepDims& dm) {
+    return (int64_t)dm.nblocks * (NV + 1) * (dm.nkp - 4) * (dm.njp - 4) * dm.nip;
+}
+bool core_ok(const void* host, const StepDims& dm) {
+    return ((uintptr_t)host % 16) == 0 && dm.ncell % 2 == 0 && dm.nip % 2 == 0 && ((dm.njp - 4) * dm.nip) % 2 == 0;
+}
+
 cudaError_t launch_convert_state(const double* src, float* dst, int8_t* lo, int64_t n, const StepDims& dm,
                                  cudaStream_t st) {
     if (wide_ok(src, dm.ncell) && n % 2 == 0) k_narrow_wide<<<1216, 256, 0, st>>>(src, dst, lo, n, dm);
@@ -247,6 +355,27 @@ cudaError_t launch_gather_host(const void* U, const int8_t* lo, const void* psi,
             k_gather_host<double><<<1216, 256, 0, st>>>((const double*)U, nullptr, (const double*)psi, first, count, ncell,
                                                         out);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_core_up(const double* host, void* U, int8_t* lo, void* P, int32_t* flag, bool fp32, const StepDims& dm,
+                           cudaStream_t st) {
+    if (!core_ok(host, dm)) return cudaErrorInvalidValue;
+    const int64_t n = core_elems(dm);
+    if (flag) {
+        cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int32_t), st);
+        if (e != cudaSuccess) return e;
+    }
+    if (fp32) k_core_up<float><<<1216, 256, 0, st>>>(host, (float*)U, lo, (float*)P, flag, n, dm);
+    else k_core_up<double><<<1216, 256, 0, st>>>(host, (double*)U, nullptr, (double*)P, flag, n, dm);
+    return cudaGetLastError();
+}
+cudaError_t launch_core_down(const void* U, const int8_t* lo, const void* P, bool fp32, double* host, const StepDims& dm,
+                             cudaStream_t st) {
+    if (!core_ok(host, dm)) return cudaErrorInvalidValue;
+    const int64_t n = core_elems(dm);
+    if (fp32) k_core_down<float><<<1216, 256, 0, st>>>((const float*)U, lo, (const float*)P, host, n, dm);
+    else k_core_down<double><<<1216, 256, 0, st>>>((const double*)U, nullptr, (const double*)P, host, n, dm);
     return cudaGetLastError();
 }
 

@@ -701,7 +701,9 @@ template <class T, int NI, int NJ, int NK, int KPAR>
 struct DShape : Shape<T, NI, NJ, NK, KPAR> {
     using B = Shape<T, NI, NJ, NK, KPAR>;
     static constexpr int NCELLS = NI * NJ * KPAR;        // interior cells of a chunk
-    static constexpr int TPC = NCELLS >= 512 ? 1 : 2;    // threads per cell in the sum (variables split)
+    // threads per cell in the sum (variables split): one in FP32, two for a
+    // 256-cell FP64 chunk
+    static constexpr int TPC = (NCELLS >= 512 || sizeof(T) == 4) ? 1 : 2;
     static constexpr int NT = NCELLS * TPC;
     static constexpr int VPT = NV / TPC;
     static constexpr int KS = KPAR + 1;                  // k-face ring slots

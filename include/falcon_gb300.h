@@ -186,6 +186,19 @@ int  falcon_download_state(falcon_ctx* ctx, double* u);
  * the GPU (from several host threads) race on the array: serialise them. */
 #define FALCON_STATIC_SCRATCH_BYTES (16u << 20)
 int  falcon_download_state_range(falcon_ctx* ctx, size_t first, size_t count, double* u);
+/* Core transfers, for a driver that keeps the state on the host and moves it
+ * every step: of every block and variable, only the interior planes and,
+ * within them, the interior rows (whole, radial ghost columns included) move,
+ * 64% of a 16^3 block's padded cells. falcon_upload_state_core recomputes the
+ * theta/phi ghost layers on the device with a full exchange (the values the
+ * reference's ModCommunication_SendRecvGC leaves there) and rejects a non-zero
+ * psi without GLM, leaving the state unchanged; falcon_download_state_core
+ * leaves the array's other cells untouched. Same array layout as
+ * falcon_upload_state. The array must lie in a falcon_pin_host buffer and be
+ * 16-byte aligned; otherwise, and for a core upload into an FP64 context, the
+ * full transfer runs instead. */
+int  falcon_upload_state_core(falcon_ctx* ctx, const double* u);
+int  falcon_download_state_core(falcon_ctx* ctx, double* u);
 /* Page-lock a host buffer (cudaHostRegister, mapped) and remember it: a MIXED
  * falcon_upload_state / falcon_download_state whose whole array lies in such
  * a buffer converts straight from / into host memory on the GPU over the host

@@ -373,3 +373,59 @@ def test_mixed_transfers_through_pinned_buffers_match_staged(divb):
             assert np.array_equal(before, a.download_state())
     finally:
         a.unpin_host(pinned)
+
+
+def _core_mask(shape):
+    """Core cells of the state array: interior planes x interior rows (whole rows)."""
+    m = np.zeros(shape, dtype=bool)
+    m[:, :, 2:-2, 2:-2, :] = True
+    return m
+
+
+@pytest.mark.parametrize("divb", [0, 1])
+@pytest.mark.parametrize("grid", ["8cube", "16cube"])
+def test_core_transfers_match_full(divb, grid):
+    """Core upload (interior planes x interior rows moved, theta/phi ghost
+    layers recomputed on the device) leaves the state that a full upload and
+    an exchange leave: two steps later both agree bit for bit on every cell
+    that is core or a ghost-map target. The core download writes exactly the
+    core cells of the full download and no other; a non-zero psi without GLM
+    is rejected with the state unchanged."""
+    kw = dict(precision=config.PREC_MIXED, divb_option=divb)
+    if grid == "8cube":
+        mk = lambda: config.tiny(**kw)
+    else:
+        mk = lambda: config.make_config(block=(16, 16, 16), root_tiles=(1, 3, 9), radial_levels=1, amr=(), **kw)
+    a, b = fg.Falcon(mk()), fg.Falcon(mk())
+    u0 = synth.initial_state(mk(), a.block_ranges(), a.block_flags(), seed=1011, psi_amp=1e-3 if divb else 0.0)
+    host = np.ascontiguousarray(u0.copy())
+    a.pin_host(host)
+    try:
+        a.upload_state_core(host)
+        b.upload_state(u0)
+        b.exchange()
+        for x in (a, b):
+            for _ in range(2):
+                x.advance_rk4(want_dt=False)
+        full = b.download_state()
+        core = _core_mask(full.shape)
+        gm = a.ghost_map()
+        listed = np.zeros(full.shape, dtype=bool)
+        listed[gm["tblock"], :, gm["tk"] + 1, gm["tj"] + 1, gm["ti"] + 1] = True
+        ua = a.download_state()
+        assert np.isfinite(ua[core]).all()
+        assert np.array_equal(ua[core | listed], full[core | listed])
+        host[...] = np.nan
+        a.download_state_core(host)
+        assert np.array_equal(host[core], full[core])
+        assert np.isnan(host[~core]).all()
+        if divb == 0:
+            before = a.download_state()
+            host[...] = u0
+            host[2, 8, 3, 3, 3] = 5.0
+            with pytest.raises(fg.FalconError) as e:
+                a.upload_state_core(host)
+            assert e.value.code == fg.ERR_INVALID_ARG and "psi" in str(e.value)
+            assert np.array_equal(before, a.download_state())
+    finally:
+        a.unpin_host(host)
