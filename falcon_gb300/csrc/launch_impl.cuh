@@ -132,6 +132,13 @@ cudaError_t cfl_any(const StepDims& d, const Geometry& g, const T* u, StepScalar
 
 template <class T>
 cudaError_t ghost_any(const StepDims& d, const GhostLists& gl, T* u, cudaStream_t st) {
+    const int64_t nb_ip = (gl.ip.n + 127) / 128, nb_ln = (gl.ln.n + 127) / 128, nb_cp = (gl.cp.n + 127) / 128;
+    if (nb_ip + nb_ln + nb_cp == 0) return cudaSuccess;
+    if (nb_ip + nb_ln + nb_cp < (int64_t)INT32_MAX) {
+        k_ghost_all<T><<<(unsigned)(nb_ip + nb_ln + nb_cp), 128, 0, st>>>(u, gl, d.ncell, d.nip, d.nip * d.njp,
+                                                                          (int)nb_ip, (int)nb_ln);
+        return cudaGetLastError();
+    }
     if (gl.cp.n > 0) {
         k_ghost_copy<T><<<(unsigned)((gl.cp.n + 255) / 256), 256, 0, st>>>(u, gl.cp, d.ncell);
         cudaError_t e = cudaGetLastError();

@@ -1052,9 +1052,7 @@ __global__ void __launch_bounds__(256) k_cfl(const T* u, Geometry g, StepScalars
 // entries (3_6/ModMath.f90:283-291) with the Yin-Yang vector rotation
 // (3_6/ModYinYang.f90:58-60).
 template <class T>
-__global__ void __launch_bounds__(256) k_ghost_copy(T* u, GhostCopyList L, int ncell) {
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= L.n) return;
+__device__ __forceinline__ void ghost_copy_one(T* u, const GhostCopyList& L, int ncell, int64_t e) {
     const size_t d = (size_t)L.dst[e], s = (size_t)L.src[e];
     T v[NV];
 #pragma unroll
@@ -1066,9 +1064,7 @@ __global__ void __launch_bounds__(256) k_ghost_copy(T* u, GhostCopyList L, int n
 // one-dimensional linear interpolation (radial neighbours of different
 // spacing: the other two weights snapped to exactly 0), mixed path only
 template <class T>
-__global__ void __launch_bounds__(256) k_ghost_lin(T* u, GhostLinList L, int ncell) {
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= L.n) return;
+__device__ __forceinline__ void ghost_lin_one(T* u, const GhostLinList& L, int ncell, int64_t e) {
     const size_t d = (size_t)L.dst[e], s = (size_t)L.src[e], st = (size_t)L.stride[e];
     const T w = (T)L.w[e], uw = T(1) - w;
     T v[NV];
@@ -1082,9 +1078,7 @@ __global__ void __launch_bounds__(256) k_ghost_lin(T* u, GhostLinList L, int nce
 }
 
 template <class T>
-__global__ void __launch_bounds__(128) k_ghost_interp(T* u, GhostInterpList L, int ncell, int nip, int pl) {
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= L.n) return;
+__device__ __forceinline__ void ghost_interp_one(T* u, const GhostInterpList& L, int ncell, int nip, int pl, int64_t e) {
     const int kind = L.kind[e];
     const size_t s = (size_t)L.src[e];
     T val[NV];
@@ -1151,6 +1145,39 @@ __global__ void __launch_bounds__(128) k_ghost_interp(T* u, GhostInterpList L, i
     const size_t dd = (size_t)L.dst[e];
 #pragma unroll
     for (int v = 0; v < NV; ++v) u[dd + (size_t)v * ncell] = val[v];
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_ghost_copy(T* u, GhostCopyList L, int ncell) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < L.n) ghost_copy_one(u, L, ncell, e);
+}
+template <class T>
+__global__ void __launch_bounds__(256) k_ghost_lin(T* u, GhostLinList L, int ncell) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < L.n) ghost_lin_one(u, L, ncell, e);
+}
+template <class T>
+__global__ void __launch_bounds__(128) k_ghost_interp(T* u, GhostInterpList L, int ncell, int nip, int pl) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < L.n) ghost_interp_one(u, L, ncell, nip, pl, e);
+}
+// The three lists of one exchange in one launch: every entry reads interior
+// cells and writes a ghost cell that no other entry writes, so the lists are
+// independent. The interpolated entries (the longest) take the first CTAs.
+template <class T>
+__global__ void __launch_bounds__(128) k_ghost_all(T* u, GhostLists G, int ncell, int nip, int pl, int nb_ip, int nb_ln) {
+    const int bx = blockIdx.x;
+    if (bx < nb_ip) {
+        const int64_t e = (int64_t)bx * 128 + threadIdx.x;
+        if (e < G.ip.n) ghost_interp_one(u, G.ip, ncell, nip, pl, e);
+    } else if (bx < nb_ip + nb_ln) {
+        const int64_t e = (int64_t)(bx - nb_ip) * 128 + threadIdx.x;
+        if (e < G.ln.n) ghost_lin_one(u, G.ln, ncell, e);
+    } else {
+        const int64_t e = (int64_t)(bx - nb_ip - nb_ln) * 128 + threadIdx.x;
+        if (e < G.cp.n) ghost_copy_one(u, G.cp, ncell, e);
+    }
 }
 
 // ---------------------------------------------------------------------------
