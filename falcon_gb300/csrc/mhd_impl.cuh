@@ -751,24 +751,31 @@ struct DShape : Shape<T, NI, NJ, NK, KPAR> {
 // Limited flux through the face between cells L and R along one direction
 // (3_6/ModDiffusion.f90:40-60 for one side): values at L-1, L, R, R+1 and
 // the speeds |v_dir| + c_s at L and R.
+// The limited slope of a cell from its two neighbours along one direction.
 template <class T>
-__device__ __forceinline__ T face_flux(T fm, T fl, T fr, T fp, T cL, T cR) {
+__device__ __forceinline__ T face_slope(T ul, T u, T ur) {
+    if constexpr (Pol<T>::exact) return minmod(ul, u, ur);
+    else return minmod_sel(ul, u, ur);   // the minmod selector as a compare
+}
+// The flux from the face's two cell values and their slopes.
+template <class T>
+__device__ __forceinline__ T face_flux_s(T fl, T fr, T dL, T dR, T cL, T cR) {
     if constexpr (Pol<T>::exact) {
-        const T dL = minmod(fm, fl, fr);
-        const T dR = minmod(fl, fr, fp);
         const T num = ((fr - dR * T(0.5)) - fl) - dL * T(0.5);
         const T phi = fmax(T(0), T(1) + T(2) * (Pol<T>::ratio(num, fr - fl) - T(1)));
         const T f = -(T(0.5) * phi * num);
         return f * (cR + cL) * T(0.5);
     } else {
-        // the same limiter in fewer FP32 operations: the minmod selector as a
-        // compare (minmod_sel), 1 + 2(r - 1) as 2r - 1, the two halves folded
-        const float dL = minmod_sel(fm, fl, fr);
-        const float dR = minmod_sel(fl, fr, fp);
+        // the same limiter in fewer FP32 operations: 1 + 2(r - 1) as 2r - 1,
+        // the two halves folded
         const float num = fmaf(-0.5f, dL, fmaf(-0.5f, dR, fr) - fl);
         const float phi = fmaxf(0.f, fmaf(2.f, __fdividef(num, fr - fl), -1.f));
         return (-0.25f * phi) * num * (cR + cL);
     }
+}
+template <class T>
+__device__ __forceinline__ T face_flux(T fm, T fl, T fr, T fp, T cL, T cR) {
+    return face_flux_s(fl, fr, face_slope(fm, fl, fr), face_slope(fl, fr, fp), cL, cR);
 }
 
 //
@@ -833,6 +840,9 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
     const T dinv[3] = {T(1) / den[0], T(1) / den[1], T(1) / den[2]};
     const double hdt = 0.5 * sc->dt;
     const float hdt_f = sc->dt_half_f;
+    T sk[S::VPT];            // k slopes carried to the next chunk (one plane per chunk)
+#pragma unroll
+    for (int t = 0; t < S::VPT; ++t) sk[t] = T(0);
     float cmin = INFINITY;   // next step's CFL ratio minimum over this thread's cells
     int cnan = 0;
     __shared__ float sb2[S::TPC == 2 ? S::NCELLS : 1];   // |B|^2 from the thread holding B
@@ -894,8 +904,18 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
                 FI[((v * KPAR + kq) * NJ + j) * S::FIP + i] = face_flux(a[-2], a[-1], a[0], a[1], cLi, cRi);
                 FJ[((v * KPAR + kq) * (NJ + 1) + jr) * NI + i] =
                     face_flux(a[-2 * NIP], a[-NIP], a[0], a[NIP], cLj, cRj);
+                // the k face's slopes: with one plane per chunk the lower one
+                // is the upper one of the previous chunk (same values, same bits)
                 const T* ak = t0 + v * W * PL;
-                fkw[v * NJ * NI] = face_flux(ak[so[1]], ak[so[2]], ak[so[3]], ak[so[4]], cLk, cRk);
+                const T dRk = face_slope(ak[so[2]], ak[so[3]], ak[so[4]]);
+                T dLk;
+                if constexpr (KPAR == 1) {
+                    dLk = ch == 0 ? face_slope(ak[so[1]], ak[so[2]], ak[so[3]]) : sk[t];
+                    sk[t] = dRk;
+                } else {
+                    dLk = face_slope(ak[so[1]], ak[so[2]], ak[so[3]]);
+                }
+                fkw[v * NJ * NI] = face_flux_s(ak[so[2]], ak[so[3]], dLk, dRk, cLk, cRk);
             }
         }
         // the right faces of the last cells of i rows and j columns
