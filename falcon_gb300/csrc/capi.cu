@@ -21,7 +21,7 @@ namespace falcon {
 // state_range.cu: range download through the library's static device array
 size_t static_scratch_elems();
 std::string download_range_static(int dev, cudaStream_t st, const void* U, const int8_t* Ulo, const void* P,
-                                  bool mixed, size_t first, size_t count, size_t ncell, double* u);
+                                  bool mixed, const StepDims& dm, size_t first, size_t count, double* u);
 }  // namespace falcon
 
 using namespace falcon;
@@ -394,8 +394,8 @@ int setup_device(falcon_ctx* ctx) {
         }
     }
     if (ctx->mixed()) {
-        CK(ctx->alloc(&ctx->Ulo, (size_t)nb * NV * g.ncell), "alloc U correction");
-        CK(cudaMemsetAsync(ctx->Ulo, 0, (size_t)nb * NV * g.ncell, ctx->st), "memset");
+        CK(ctx->alloc(&ctx->Ulo, lo_elems(ctx->dims)), "alloc U correction");
+        CK(cudaMemsetAsync(ctx->Ulo, 0, lo_elems(ctx->dims), ctx->st), "memset");
     }
 
     // geometry and background tables (3_6/ModBlock.f90:188-265, 288-438)
@@ -880,10 +880,11 @@ int get_state(falcon_ctx* ctx, const void* U, const int8_t* lo, const void* P, d
         const size_t n9 = host_elems(ctx);
         double* dst = (double*)mapped_host(ctx, u, n9 * 8);
         if (dst) {
-            CK(launch_gather_host(U, lo, P, true, 0, (int64_t)n9, (int64_t)nc, dst, ctx->st), "download convert");
+            CK(launch_gather_host(U, lo, P, true, ctx->dims, 0, (int64_t)n9, (int64_t)nc, dst, ctx->st), "download convert");
         } else {
             if (!ctx->stage64) CK(ctx->alloc(&ctx->stage64, n9 * 8), "alloc staging");
-            CK(launch_gather_host(U, lo, P, true, 0, (int64_t)n9, (int64_t)nc, ctx->stage64, ctx->st), "download convert");
+            CK(launch_gather_host(U, lo, P, true, ctx->dims, 0, (int64_t)n9, (int64_t)nc, ctx->stage64, ctx->st),
+               "download convert");
             CK(cudaMemcpyAsync(u, ctx->stage64, n9 * 8, cudaMemcpyDeviceToHost, ctx->st), "download");
         }
         CK(cudaStreamSynchronize(ctx->st), "download");
@@ -948,8 +949,8 @@ int falcon_download_state_range(falcon_ctx* ctx, size_t first, size_t count, dou
         return ctx->fail(FALCON_ERR_INVALID_ARG, "falcon_download_state_range: first " + std::to_string(first) +
                                                      " + count " + std::to_string(count) + " exceeds the state size " +
                                                      std::to_string(n));
-    const std::string e = download_range_static(ctx->device, ctx->st, ctx->U, ctx->Ulo, ctx->P, ctx->mixed(), first,
-                                                count, (size_t)ctx->dims.ncell, u);
+    const std::string e = download_range_static(ctx->device, ctx->st, ctx->U, ctx->Ulo, ctx->P, ctx->mixed(), ctx->dims,
+                                                first, count, u);
     if (!e.empty()) return ctx->fail(FALCON_ERR_CUDA, e);
     return FALCON_OK;
 }
@@ -973,7 +974,7 @@ int falcon_upload_state_core(falcon_ctx* ctx, const double* u) {
     if (!ctx->dflag) CK(ctx->alloc(&ctx->dflag, sizeof(int32_t)), "alloc flag");
     int8_t* lo_tmp = (int8_t*)ctx->RK;
     const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
-    CK(cudaMemsetAsync(lo_tmp, 0, n, ctx->st), "upload core");   // ghost cells carry no correction
+
     CK(launch_core_up(src, ctx->R2, lo_tmp, ctx->P ? ctx->P2 : nullptr, ctx->P ? nullptr : ctx->dflag, true, ctx->dims,
                       ctx->st),
        "upload core");
@@ -986,7 +987,7 @@ int falcon_upload_state_core(falcon_ctx* ctx, const double* u) {
         return ctx->fail(FALCON_ERR_INVALID_ARG, "psi must be 0 unless divb_option = 1");
     }
     std::swap(ctx->U, ctx->R2);
-    CK(cudaMemcpyAsync(ctx->Ulo, lo_tmp, n, cudaMemcpyDeviceToDevice, ctx->st), "upload core");
+    CK(cudaMemcpyAsync(ctx->Ulo, lo_tmp, lo_elems(ctx->dims), cudaMemcpyDeviceToDevice, ctx->st), "upload core");
     CK(ghost(ctx, ctx->U), "upload core");
     ctx->stale_edges = false;
     ctx->cfl_ready = false;
@@ -1043,7 +1044,7 @@ int falcon_init_synthetic(falcon_ctx* ctx, int32_t kind, uint64_t seed, double m
     if (kind < 0 || kind > 1) return ctx->fail(FALCON_ERR_INVALID_ARG, "unknown synthetic kind");
     std::string e = synth_initial_state(ctx->grid, ctx->geom(), ctx->U, ctx->mixed(), kind, seed, mach, ctx->st);
     if (!e.empty()) return ctx->fail(FALCON_ERR_CUDA, e);
-    if (ctx->Ulo) CK(cudaMemsetAsync(ctx->Ulo, 0, (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell, ctx->st), "init");
+    if (ctx->Ulo) CK(cudaMemsetAsync(ctx->Ulo, 0, lo_elems(ctx->dims), ctx->st), "init");
     const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
     CK(cudaMemcpyAsync(ctx->RK, ctx->U, n * ctx->elem, cudaMemcpyDeviceToDevice, ctx->st), "init");
     CK(mirror_state(ctx), "init");
@@ -1226,7 +1227,7 @@ uint64_t grid_hash(const Grid& g) {   // FNV-1a over the block ranges and flags
 RestartHeader restart_header(const falcon_ctx* ctx) {
     RestartHeader h{};
     std::memcpy(h.magic, kRestartMagic, 8);
-    h.version = 1;
+    h.version = 2;   // 2: the u^n correction stored for interior cells only
     h.precision = (uint32_t)ctx->cfg.precision;
     h.ni = ctx->dims.ni; h.nj = ctx->dims.nj; h.nk = ctx->dims.nk; h.ng = ctx->grid.ng;
     h.nblocks = ctx->dims.nblocks;
@@ -1235,7 +1236,7 @@ RestartHeader restart_header(const falcon_ctx* ctx) {
     h.steps_done = ctx->steps_done;
     const size_t cells = (size_t)ctx->dims.nblocks * ctx->dims.ncell;
     h.bytes_state = cells * NV * ctx->elem;
-    h.bytes_lo = ctx->Ulo ? cells * NV : 0;
+    h.bytes_lo = ctx->Ulo ? lo_elems(ctx->dims) : 0;
     h.bytes_psi = ctx->P ? cells * ctx->elem : 0;
     return h;
 }
@@ -1369,7 +1370,7 @@ int falcon_load_restart(falcon_ctx* ctx, const char* path) {
     RestartHeader h{};
     const RestartHeader want = restart_header(ctx);
     std::string why;
-    if (std::fread(&h, sizeof h, 1, f) != 1 || std::memcmp(h.magic, kRestartMagic, 8) != 0 || h.version != 1)
+    if (std::fread(&h, sizeof h, 1, f) != 1 || std::memcmp(h.magic, kRestartMagic, 8) != 0 || h.version != 2)
         why = "not a restart file of this library";
     else if (h.precision != want.precision)
         why = "precision differs";

@@ -157,6 +157,19 @@ struct StepDims {
     int nblocks, ni, nj, nk, nip, njp, nkp, ncell;
 };
 
+// The u^n correction of the mixed path is stored for interior cells only,
+// [block][var][k][j][i] with the interior extents (1 byte per value, no
+// padding: its rows are whole 16-byte runs for 16^3 blocks). Index of state
+// element e (the state's padded layout), or -1 for a ghost cell.
+__host__ __device__ __forceinline__ int64_t lo_index(int64_t e, const StepDims& d) {
+    const int64_t bv = e / d.ncell;
+    const int c = (int)(e - bv * d.ncell);
+    const int ip = c % d.nip, jp = (c / d.nip) % d.njp, kp = c / (d.nip * d.njp);
+    if (ip < 2 || ip >= d.nip - 2 || jp < 2 || jp >= d.njp - 2 || kp < 2 || kp >= d.nkp - 2) return -1;
+    return ((bv * d.nk + (kp - 2)) * d.nj + (jp - 2)) * d.ni + (ip - 2);
+}
+inline size_t lo_elems(const StepDims& d) { return (size_t)d.nblocks * NV * d.ni * d.nj * d.nk; }
+
 // div-B control of a stage (DivB_option): mode 0 none; 1 GLM cleaning
 // (3_6/ModDivB.f90:13-38) with psi arrays [b][cell] of the stage input, of u^n
 // and of the stage output -- psi is read from global memory (not the
@@ -236,7 +249,8 @@ cudaError_t launch_core_up(const double* host, void* U, int8_t* lo, void* P, int
                            cudaStream_t st);
 cudaError_t launch_core_down(const void* U, const int8_t* lo, const void* P, bool fp32, double* host, const StepDims& dm,
                              cudaStream_t st);
-cudaError_t launch_gather_host(const void* U, const int8_t* lo, const void* psi, bool fp32, int64_t first, int64_t count,
+cudaError_t launch_gather_host(const void* U, const int8_t* lo, const void* psi, bool fp32, const StepDims& dm,
+                               int64_t first, int64_t count,
                                int64_t ncell, double* out, cudaStream_t st);
 
 // names of the kernels as they appear in profiles

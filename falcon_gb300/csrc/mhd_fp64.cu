@@ -65,10 +65,8 @@ __global__ void k_narrow(const double* s, float* d, int8_t* lo, int64_t n, StepD
         const float hi = (float)u;
         d[x] = hi;
         if (lo) {
-            const int c = (int)(x % dm.ncell);
-            const int ip = c % dm.nip, jp = (c / dm.nip) % dm.njp, kp = c / (dm.nip * dm.njp);
-            const bool interior = ip >= 2 && ip < dm.nip - 2 && jp >= 2 && jp < dm.njp - 2 && kp >= 2 && kp < dm.nkp - 2;
-            lo[x] = interior ? lo_encode64(hi, u - (double)hi) : (int8_t)0;
+            const int64_t q = lo_index(x, dm);
+            if (q >= 0) lo[q] = lo_encode64(hi, u - (double)hi);
         }
     }
 }
@@ -92,8 +90,8 @@ __global__ void k_psi_nonzero(const double* s, int64_t nb, int64_t ncell, int32_
 // host elements [first, first + count) as FP64 from the device state (FP32
 // with its correction, or FP64) and psi (nullptr: psi = 0)
 template <class T>
-__global__ void k_gather_host(const T* U, const int8_t* lo, const T* psi, int64_t first, int64_t count, int64_t ncell,
-                              double* out) {
+__global__ void k_gather_host(const T* U, const int8_t* lo, const T* psi, StepDims dm, int64_t first, int64_t count,
+                              int64_t ncell, double* out) {
     for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < count; x += (int64_t)gridDim.x * blockDim.x) {
         const int64_t h = first + x;
         const int64_t b = h / ((NV + 1) * ncell), r = h - b * (NV + 1) * ncell;
@@ -103,7 +101,8 @@ __global__ void k_gather_host(const T* U, const int8_t* lo, const T* psi, int64_
             const T hi = U[e];
             v = (double)hi;
             if constexpr (sizeof(T) == 4) {
-                if (lo) v += (double)lo[e] * (double)lo_unit((float)hi);
+                const int64_t q = lo ? lo_index(e, dm) : -1;
+                if (q >= 0) v += (double)lo[q] * (double)lo_unit((float)hi);
             }
         } else {
             v = psi ? (double)psi[b * ncell + (r - NV * ncell)] : 0.0;
@@ -122,10 +121,8 @@ __device__ __forceinline__ void narrow_one(double u, int64_t x, float* d, int8_t
     const float hi = (float)u;
     d[x] = hi;
     if (lo) {
-        const int c = (int)(x % dm.ncell);
-        const int ip = c % dm.nip, jp = (c / dm.nip) % dm.njp, kp = c / (dm.nip * dm.njp);
-        const bool interior = ip >= 2 && ip < dm.nip - 2 && jp >= 2 && jp < dm.njp - 2 && kp >= 2 && kp < dm.nkp - 2;
-        lo[x] = interior ? lo_encode64(hi, u - (double)hi) : (int8_t)0;
+        const int64_t q = lo_index(x, dm);
+        if (q >= 0) lo[q] = lo_encode64(hi, u - (double)hi);
     }
 }
 __global__ void k_narrow_wide(const double* s, float* d, int8_t* lo, int64_t n, StepDims dm) {
@@ -182,22 +179,24 @@ __global__ void k_psi_nonzero_wide(const double* s, int64_t nb, int64_t ncell, i
     if (__any_sync(0xffffffffu, any) && (threadIdx.x & 31) == 0) *flag = 1;
 }
 template <class T>
-__device__ __forceinline__ double gather_one(const T* U, const int8_t* lo, const T* psi, int64_t h, int64_t ncell) {
+__device__ __forceinline__ double gather_one(const T* U, const int8_t* lo, const T* psi, int64_t h, int64_t ncell,
+                                             const StepDims& dm) {
     const int64_t b = h / ((NV + 1) * ncell), r = h - b * (NV + 1) * ncell;
     if (r < NV * ncell) {
         const int64_t e = b * NV * ncell + r;
         const T hi = U[e];
         double v = (double)hi;
         if constexpr (sizeof(T) == 4) {
-            if (lo) v += (double)lo[e] * (double)lo_unit((float)hi);
+            const int64_t q = lo ? lo_index(e, dm) : -1;
+            if (q >= 0) v += (double)lo[q] * (double)lo_unit((float)hi);
         }
         return v;
     }
     return psi ? (double)psi[b * ncell + (r - NV * ncell)] : 0.0;
 }
 template <class T>
-__global__ void k_gather_host_wide(const T* U, const int8_t* lo, const T* psi, int64_t first, int64_t count,
-                                   int64_t ncell, double* out) {
+__global__ void k_gather_host_wide(const T* U, const int8_t* lo, const T* psi, StepDims dm, int64_t first,
+                                   int64_t count, int64_t ncell, double* out) {
     const int64_t lane2 = 2 * (threadIdx.x & 31);
     for (int64_t w0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32 * kWide; w0 < count;
          w0 += (((int64_t)gridDim.x * blockDim.x) >> 5) * 32 * kWide) {
@@ -205,8 +204,8 @@ __global__ void k_gather_host_wide(const T* U, const int8_t* lo, const T* psi, i
 #pragma unroll
         for (int q = 0; q < kWide / 2; ++q)
             if ((w0 + 64 * q + lane2) < count) {
-                v[q].x = gather_one(U, lo, psi, first + (w0 + 64 * q + lane2), ncell);
-                v[q].y = gather_one(U, lo, psi, first + (w0 + 64 * q + lane2) + 1, ncell);
+                v[q].x = gather_one(U, lo, psi, first + (w0 + 64 * q + lane2), ncell, dm);
+                v[q].y = gather_one(U, lo, psi, first + (w0 + 64 * q + lane2) + 1, ncell, dm);
             }
 #pragma unroll
         for (int q = 0; q < kWide / 2; ++q)
@@ -266,7 +265,7 @@ __global__ void k_core_up(const double* s, T* U, int8_t* lo, T* P, int32_t* flag
                     if constexpr (sizeof(T) == 4) {
                         const float hi = (float)u2[h];
                         U[e] = hi;
-                        if (lo) lo[e] = in ? lo_encode64(hi, u2[h] - (double)hi) : (int8_t)0;
+                        if (lo && in) lo[lo_index(e, dm)] = lo_encode64(hi, u2[h] - (double)hi);
                     } else {
                         U[e] = (T)u2[h];
                     }
@@ -302,7 +301,8 @@ __global__ void k_core_down(const T* U, const int8_t* lo, const T* P, double* ou
                     const T hi = U[e];
                     double x = (double)hi;
                     if constexpr (sizeof(T) == 4) {
-                        if (lo) x += (double)lo[e] * (double)lo_unit((float)hi);
+                        const int64_t q = lo ? lo_index(e, dm) : -1;
+                        if (q >= 0) x += (double)lo[q] * (double)lo_unit((float)hi);
                     }
                     u2[h] = x;
                 } else {
@@ -341,19 +341,21 @@ cudaError_t launch_psi_nonzero(const double* src, int64_t nb, int64_t ncell, int
     else k_psi_nonzero<<<1216, 256, 0, st>>>(src, nb, ncell, flag);
     return cudaGetLastError();
 }
-cudaError_t launch_gather_host(const void* U, const int8_t* lo, const void* psi, bool fp32, int64_t first, int64_t count,
-                               int64_t ncell, double* out, cudaStream_t st) {
+cudaError_t launch_gather_host(const void* U, const int8_t* lo, const void* psi, bool fp32, const StepDims& dm,
+                               int64_t first, int64_t count, int64_t ncell, double* out, cudaStream_t st) {
     const bool wide = wide_ok(out, ncell) && first % 2 == 0 && count % 2 == 0;
     if (fp32) {
-        if (wide) k_gather_host_wide<float><<<1216, 256, 0, st>>>((const float*)U, lo, (const float*)psi, first, count, ncell, out);
-        else k_gather_host<float><<<1216, 256, 0, st>>>((const float*)U, lo, (const float*)psi, first, count, ncell, out);
+        if (wide)
+            k_gather_host_wide<float><<<1216, 256, 0, st>>>((const float*)U, lo, (const float*)psi, dm, first, count, ncell,
+                                                            out);
+        else k_gather_host<float><<<1216, 256, 0, st>>>((const float*)U, lo, (const float*)psi, dm, first, count, ncell, out);
     } else {
         if (wide)
-            k_gather_host_wide<double><<<1216, 256, 0, st>>>((const double*)U, nullptr, (const double*)psi, first, count,
+            k_gather_host_wide<double><<<1216, 256, 0, st>>>((const double*)U, nullptr, (const double*)psi, dm, first, count,
                                                              ncell, out);
         else
-            k_gather_host<double><<<1216, 256, 0, st>>>((const double*)U, nullptr, (const double*)psi, first, count, ncell,
-                                                        out);
+            k_gather_host<double><<<1216, 256, 0, st>>>((const double*)U, nullptr, (const double*)psi, dm, first, count,
+                                                        ncell, out);
     }
     return cudaGetLastError();
 }

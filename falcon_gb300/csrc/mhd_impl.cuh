@@ -152,6 +152,7 @@ struct Shape {
     static constexpr int W = 2 * KPAR + 4;    // ring: current window (KPAR+4) + the prefetched KPAR planes
     static constexpr int WP = KPAR + 4;       // p1 window
     static constexpr int NCELL = PL * NKP;
+    static constexpr int PLI = NI * NJ, NINT = PLI * NK;   // the u^n correction's (interior-only) plane and block
     static constexpr uint32_t PLB = PL * (uint32_t)sizeof(T);   // bytes of one variable plane
     static_assert(PLB % 16 == 0, "plane must be a multiple of 16 bytes");
     static_assert(NK % KPAR == 0, "KPAR must divide NK");
@@ -423,7 +424,7 @@ k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, DivBArgs 
     // u^n (and its int8 correction at stage 4) is read with plain loads at
     // stages 2-4: warm L2 with the planes of the first chunk, then one chunk ahead
     const T* blk_un = un + (size_t)b * NV * NCELL;
-    const int8_t* blk_lo = ulo != nullptr ? ulo + (size_t)b * NV * NCELL : nullptr;
+    const int8_t* blk_lo = ulo != nullptr ? ulo + (size_t)b * NV * S::NINT : nullptr;
     T* blk_out = out + (size_t)b * NV * NCELL;
     auto prefetch_un = [&](int kp_first) {
         if (threadIdx.x >= NV) return;
@@ -432,7 +433,8 @@ k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, DivBArgs 
         if (out != un || stage == 1) prefetch_l2(blk_out + ((size_t)v * S::NKP + kp_first) * PL, KPAR * S::PLB);
         if (stage == 1) return;
         prefetch_l2(blk_un + ((size_t)v * S::NKP + kp_first) * PL, KPAR * S::PLB);
-        if (blk_lo != nullptr && stage == 4) prefetch_l2(blk_lo + ((size_t)v * S::NKP + kp_first) * PL, KPAR * PL);
+        if (blk_lo != nullptr && stage == 4)
+            prefetch_l2(blk_lo + ((size_t)v * NK + (kp_first - 2)) * S::PLI, KPAR * S::PLI);
     };
     prefetch_un(2);
     load_geometry<T, S>(g, b, gi, gj, gs, a12);
@@ -664,14 +666,15 @@ k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, DivBArgs 
             for (int v = 0; v < NV; ++v) o[v] = (T)((double)u0s[v] + (dt * (double)R[v]) / divs);
         } else if (ulo != nullptr && stage == 4) {
             // u^{n+1} = u^n + dt*R with u^n and u^{n+1} compensated
+            int8_t* ql = ulo + (size_t)b * NV * S::NINT + ((size_t)(kp - 2) * NJ + (jj - 2)) * NI + (ii - 2);
             int8_t q0[NV];
 #pragma unroll
-            for (int v = 0; v < NV; ++v) q0[v] = ulo[base + (size_t)v * NCELL];
+            for (int v = 0; v < NV; ++v) q0[v] = ql[(size_t)v * S::NINT];
 #pragma unroll
             for (int v = 0; v < NV; ++v) {
                 int8_t q1;
                 o[v] = ff_add((float)u0s[v], q0[v], __fmul_rn(dtk, (float)R[v]), q1);
-                ulo[base + (size_t)v * NCELL] = q1;
+                ql[(size_t)v * S::NINT] = q1;
             }
         } else {
 #pragma unroll
@@ -820,10 +823,10 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
     if (threadIdx.x == 0) issue_planes<T, S>(blk, tile, 0, KPAR + 4, &bars[0]);
     // the int8 corrections of u^n are read with plain loads: warm L2 with the
     // first chunk's planes, then one chunk ahead
-    const int8_t* blk_lo = ulo != nullptr ? ulo + (size_t)b * NV * NCELL : nullptr;
+    const int8_t* blk_lo = ulo != nullptr ? ulo + (size_t)b * NV * S::NINT : nullptr;
     auto prefetch_lo = [&](int kp_first) {
         if (threadIdx.x >= NV) return;
-        if (blk_lo != nullptr) prefetch_l2(blk_lo + ((size_t)threadIdx.x * S::NKP + kp_first) * PL, KPAR * PL);
+        if (blk_lo != nullptr) prefetch_l2(blk_lo + ((size_t)threadIdx.x * NK + (kp_first - 2)) * S::PLI, KPAR * S::PLI);
     };
     prefetch_lo(2);
     load_geometry<T, S>(g, b, gi, gj, gs, nullptr);
@@ -858,10 +861,10 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
         int8_t qlo[S::VPT];
         if constexpr (!Pol<T>::exact) {
             if (ulo != nullptr) {
-                const int8_t* q = ulo + (size_t)b * NV * NCELL + (size_t)v0 * NCELL +
-                                  (size_t)(k0 + 1 + kq) * PL + jj * NIP + ii;
+                const int8_t* q = ulo + ((size_t)b * NV + v0) * S::NINT +
+                                  ((size_t)(k0 - 1 + kq) * NJ + j) * NI + i;
 #pragma unroll
-                for (int t = 0; t < S::VPT; ++t) qlo[t] = q[(size_t)t * NCELL];
+                for (int t = 0; t < S::VPT; ++t) qlo[t] = q[(size_t)t * S::NINT];
             }
         }
         if (!mbar_wait(&bars[ch & 1], (uint32_t)((ch >> 1) & 1), kWaitPolls)) {
@@ -970,7 +973,7 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
             } else if (ulo != nullptr) {
                 int8_t q1;
                 o[t] = ff_add((float)u0, qlo[t], __fmul_rn(hdt_f, (float)R), q1);
-                ulo[(size_t)b * NV * NCELL + (size_t)v * NCELL + base] = q1;
+                ulo[((size_t)b * NV + v) * S::NINT + ((size_t)(kp - 2) * NJ + j) * NI + i] = q1;
             } else {
                 o[t] = fmaf(hdt_f, (float)R, (float)u0);
             }

@@ -15,13 +15,15 @@ namespace {
 // gives it (the mixed path adds the 8-bit correction of u^n)
 template <class T>
 __device__ __forceinline__ double cell_value(const T* U, const int8_t* lo, const T* psi, int64_t b, int v, int64_t c,
-                                             int64_t ncell) {
+                                             const StepDims& d) {
+    const int64_t ncell = d.ncell;
     if (v == NV) return psi ? (double)psi[b * ncell + c] : 0.0;
     const int64_t e = (b * NV + v) * ncell + c;
     const T hi = U[e];
     double x = (double)hi;
     if constexpr (sizeof(T) == 4) {
-        if (lo) x += (double)lo[e] * (double)lo_unit((float)hi);
+        const int64_t q = lo ? lo_index(e, d) : -1;
+        if (q >= 0) x += (double)lo[q] * (double)lo_unit((float)hi);
     }
     return x;
 }
@@ -46,7 +48,7 @@ __global__ void __launch_bounds__(256) k_allcells(const T* U, const int8_t* lo, 
         double val[NV + 1];
 #pragma unroll
         for (int v = 0; v <= NV; ++v) {
-            auto f = [&](int di, int dj, int dk) { return cell_value(U, lo, psi, b, v, cell(i + di, j + dj, k + dk), d.ncell); };
+            auto f = [&](int di, int dj, int dk) { return cell_value(U, lo, psi, b, v, cell(i + di, j + dj, k + dk), d); };
             // 0.125d0*(8 neighbours), summed left to right (3_6/ModSavePlot.f90:575-580)
             double s = f(0, 0, 0) + f(1, 0, 0);
             s = s + f(0, 1, 0);

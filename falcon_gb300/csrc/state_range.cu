@@ -55,12 +55,13 @@ size_t static_scratch_elems() { return FALCON_STATIC_SCRATCH_BYTES / sizeof(doub
 // has checked the range and count <= static_scratch_elems(), and made `dev`
 // current. Returns "" or the failing step.
 std::string download_range_static(int dev, cudaStream_t st, const void* U, const int8_t* Ulo, const void* P,
-                                  bool mixed, size_t first, size_t count, size_t ncell, double* u) {
+                                  bool mixed, const StepDims& dm, size_t first, size_t count, double* u) {
     if (count == 0) return "";
     double* ptr = nullptr;
     cudaError_t e = scratch_on_device(dev, &ptr);
     if (e != cudaSuccess) return std::string("static scratch address: ") + cudaGetErrorString(e);
-    e = launch_gather_host(U, mixed ? Ulo : nullptr, P, mixed, (int64_t)first, (int64_t)count, (int64_t)ncell, ptr, st);
+    e = launch_gather_host(U, mixed ? Ulo : nullptr, P, mixed, dm, (int64_t)first, (int64_t)count, (int64_t)dm.ncell, ptr,
+                           st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(u, ptr, count * sizeof(double), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return std::string("range download: ") + cudaGetErrorString(e);
