@@ -81,25 +81,39 @@ class ClockSampler:
     def __init__(self, device):
         self.device = device
         self.proc = None
-        self.lines = []
+        self.lines = []   # (arrival time, line)
+        self.window = None
 
     def start(self):
+        """Start sampling (every 50 ms) and wait for the first sample, so that
+        the window marked by begin()/end() is covered from its start."""
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.perf_counter()
+            while not self.lines and time.perf_counter() - t0 < 10.0 and self.proc.poll() is None:
+                time.sleep(0.01)
         except (OSError, FileNotFoundError):
             self.proc = None
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+
+    def begin(self):
+        self.window = [time.perf_counter(), None]
+
+    def end(self):
+        if self.window:
+            self.window[1] = time.perf_counter()
 
     def stop(self):
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.06)   # the sample that closes the window
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
@@ -107,7 +121,13 @@ class ClockSampler:
             self.proc.kill()
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        rows = self.lines
+        if self.window and self.window[1] is not None:
+            a, b = self.window
+            inside = [r for r in rows if a <= r[0] <= b]
+            after = [r for r in rows if r[0] > b][:1]   # a sample taken at the window's end
+            rows = inside + after if inside or after else rows
+        for _, ln in rows:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -242,10 +262,13 @@ def run_ours(args, rank, world, local, dist):
     f.synchronize()
     clocks = ClockSampler(local)
     clocks.start()
+    f.synchronize()
+    clocks.begin()
     f.timer_start()
     f.run_steps(args.steps)
     ms = f.timer_stop()
     f.synchronize()
+    clocks.end()
     clk = clocks.stop()
     barrier(dist)
     ms_max = reduce_max(dist, ms)
