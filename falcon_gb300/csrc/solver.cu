@@ -704,6 +704,9 @@ struct SvLevel {
     int64_t nh = 0;
     int32_t *hcdst = nullptr, *hcsrc = nullptr;   // halo entries that are plain copies
     int64_t nhc = 0;
+    // the copies in three runs: ghost and source both of parity 0 (nhc0), of
+    // differing parities (nhcm), both of parity 1 (the rest); parity of i+j+k
+    int64_t nhc0 = 0, nhcm = 0;
     float *z = nullptr, *r = nullptr, *res = nullptr;
     // level 0: the scaled operator A / sA and the halo's corner weights as FF pairs
     float2 *Aii2 = nullptr, *Ai2 = nullptr, *Aj2 = nullptr, *Ak2 = nullptr, *hw8 = nullptr;
@@ -793,6 +796,22 @@ template <class T> cudaError_t halo_fill(falcon_solver* sv, int l, T* v) {
     return cudaGetLastError();
 }
 
+// Before a red-black half sweep of `colour`: only the ghosts of the other
+// parity are read. Copies whose ghost and source share a parity go stale only
+// when that parity's cells change, so the fill refreshes the copies of the
+// other parity, the copies whose parities differ and every interpolated
+// entry; the copies of `colour`'s parity were refreshed after that colour's
+// last sweep (the sweeps alternate).
+template <class T> cudaError_t halo_fill_part(falcon_solver* sv, int l, T* v, int colour) {
+    const SvLevel& L = sv->lv[l];
+    const int p = 1 - colour;
+    const int64_t off = p == 0 ? 0 : L.nhc0;
+    const int64_t nc = p == 0 ? L.nhc0 + L.nhcm : L.nhc - L.nhc0;
+    const int64_t n = nc + L.nh;
+    if (n > 0) k_halo<T><<<(unsigned)((n + 255) / 256), 256, 0, sv->st>>>(v, L.halo(), L.hcdst + off, L.hcsrc + off, nc);
+    return cudaGetLastError();
+}
+
 cudaError_t halo_fill_ff(falcon_solver* sv, float2* v) {
     const SvLevel& L = sv->lv[0];
     const int64_t n = L.nhc + L.nh;
@@ -844,16 +863,25 @@ int upload_rhs_ff(falcon_solver* sv) {
 cudaError_t vcycle_body(falcon_solver* sv) {
     const int nl = (int)sv->lv.size(), nb = sv->S.nblocks;
     cudaError_t e = cudaSuccess;
-    auto smooth = [&](int l, int sweeps, bool reverse) {
+    // smooth(): `zero` when z (ghosts included) was just zeroed, so the first
+    // sweep needs no fill; otherwise z changed everywhere and the first fill is
+    // whole. Returns the colour of the last half sweep (-1 if none).
+    auto smooth = [&](int l, int sweeps, bool reverse, bool zero) -> int {
         SvLevel& L = sv->lv[l];
+        int last = -1;
         for (int s = 0; s < sweeps && e == cudaSuccess; ++s)
             for (int h = 0; h < 2 && e == cudaSuccess; ++h) {
-                e = halo_fill<float>(sv, l, L.z);
+                const int colour = reverse ? 1 - h : h;
+                if (last >= 0) e = halo_fill_part<float>(sv, l, L.z, colour);
+                else if (!zero) e = halo_fill<float>(sv, l, L.z);
                 if (e != cudaSuccess) break;
-                k_rbgs<<<grid_cells(L.d, nb), tpb(L.d), 0, sv->st>>>(L.ops32(), L.d, L.r, L.z, reverse ? 1 - h : h);
+                k_rbgs<<<grid_cells(L.d, nb), tpb(L.d), 0, sv->st>>>(L.ops32(), L.d, L.r, L.z, colour);
                 e = cudaGetLastError();
+                last = colour;
             }
+        return last;
     };
+    int last = -1;
     for (int l = 0; l < nl && e == cudaSuccess; ++l) {
         SvLevel& L = sv->lv[l];
         k_zero_f<<<1216, 256, 0, sv->st>>>(L.z, (size_t)nb * L.d.npad);
@@ -875,12 +903,13 @@ cudaError_t vcycle_body(falcon_solver* sv) {
                 k_lcc_scatter<<<grid_cells(L.d, nb), tpb(L.d), 0, sv->st>>>(L.d, sv->yout, sv->gmap, sv->csum, N, L.z);
                 e = cudaGetLastError();
             }
-            smooth(l, sv->net_sweeps, false);
+            last = smooth(l, sv->net_sweeps, false, false);
         } else {
-            smooth(l, l == nl - 1 ? sv->nu_coarse : sv->nu_pre, false);
+            last = smooth(l, l == nl - 1 ? sv->nu_coarse : sv->nu_pre, false, true);
         }
         if (l + 1 < nl && e == cudaSuccess) {
-            e = halo_fill<float>(sv, l, L.z);
+            // the residual reads every ghost: refresh those of the last sweep's parity
+            e = last >= 0 ? halo_fill_part<float>(sv, l, L.z, 1 - last) : halo_fill<float>(sv, l, L.z);
             if (e != cudaSuccess) break;
             k_resid32<<<grid_cells(L.d, nb), tpb(L.d), 0, sv->st>>>(L.ops32(), L.d, L.r, L.z, L.res);
             SvLevel& C = sv->lv[l + 1];
@@ -893,7 +922,7 @@ cudaError_t vcycle_body(falcon_solver* sv) {
         SvLevel& C = sv->lv[l + 1];
         k_prolong_add<<<grid_cells(L.d, nb), tpb(L.d), 0, sv->st>>>(L.d, C.d, C.z, L.z);
         e = cudaGetLastError();
-        smooth(l, sv->nu_post, true);
+        smooth(l, sv->nu_post, true, false);
     }
     return e;
 }
@@ -999,10 +1028,29 @@ int setup(falcon_solver* sv) {
             std::vector<size_t> oc(cdst.size());
             for (size_t q = 0; q < oc.size(); ++q) oc[q] = q;
             std::stable_sort(oc.begin(), oc.end(), [&](size_t a, size_t b) { return csrc[a] < csrc[b]; });
+            // runs by parity (each run keeps the source order), see SvLevel
+            auto par = [&](int32_t o) {
+                const int64_t r = (int64_t)o % L.d.npad;
+                return (int)((r % L.d.p0 + (r / L.d.p0) % L.d.p1 + r / ((int64_t)L.d.p0 * L.d.p1)) & 1);
+            };
+            auto run = [&](size_t q) {
+                const int a = par(cdst[q]), b2 = par(csrc[q]);
+                return a != b2 ? 1 : (a == 0 ? 0 : 2);
+            };
+            std::stable_sort(oc.begin(), oc.end(), [&](size_t a, size_t b) { return run(a) < run(b); });
             std::vector<int32_t> cd2(oc.size()), cs2(oc.size());
-            for (size_t q = 0; q < oc.size(); ++q) { cd2[q] = cdst[oc[q]]; cs2[q] = csrc[oc[q]]; }
+            int64_t n0 = 0, nm = 0;
+            for (size_t q = 0; q < oc.size(); ++q) {
+                cd2[q] = cdst[oc[q]];
+                cs2[q] = csrc[oc[q]];
+                const int rq = run(oc[q]);
+                n0 += rq == 0;
+                nm += rq == 1;
+            }
             cdst.swap(cd2);
             csrc.swap(cs2);
+            L.nhc0 = n0;
+            L.nhcm = nm;
         }
         const size_t n = dst.size(), nc = cdst.size();
         L.nh = (int64_t)n;
