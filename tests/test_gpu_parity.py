@@ -216,6 +216,23 @@ def test_nan_in_state_is_reported_not_trapped():
     assert e.value.code == fg.ERR_NAN_DETECTED
 
 
+def test_nan_formed_in_a_mixed_step_is_reported_by_the_next():
+    """A NaN that first appears inside a mixed step (here: FP32 products of a
+    huge but finite velocity overflow) is caught by the next step's CFL
+    minimum, which the diffusion pass forms from the values it writes, and
+    reported as FALCON_ERR_NAN_DETECTED rather than propagated."""
+    mk = lambda: config.make_config(block=(16, 16, 16), root_tiles=(1, 3, 9), radial_levels=1, amr=(),
+                                    precision=config.PREC_MIXED)
+    f = fg.Falcon(mk())
+    u0 = synth.initial_state(mk(), f.block_ranges(), f.block_flags(), seed=1012)
+    u0[5, 1, 8, 8, 8] = 1e30   # vr of one interior cell: finite, its square is not
+    f.upload_state(u0)
+    with pytest.raises(fg.FalconError) as e:
+        for _ in range(4):
+            f.advance_rk4()
+    assert e.value.code == fg.ERR_NAN_DETECTED
+
+
 # ---- div-B control: GLM cleaning (divb_option 1, psi evolved) and the ----
 # ---- Powell source term (divb_option 2) --------------------------------
 def _init_divb(cfg, ranges, flags, divb, seed):
