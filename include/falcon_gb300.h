@@ -226,10 +226,11 @@ int  falcon_init_synthetic(falcon_ctx* ctx, int32_t kind, uint64_t seed, double 
 int  falcon_save_allcells(falcon_ctx* ctx, const char* directory, int32_t step);
 /* Binary restart dump of the device state, which the reference lacks: the
  * raw device arrays (state, the mixed path's 8-bit corrections of u^n, psi
- * with GLM) behind a header with the grid's shape, precision, div-B option, a
- * hash of the block ranges and the step count. falcon_load_restart into a
- * context of the same configuration continues bit for bit as the run that
- * wrote the dump; a file of another configuration, or a short file, returns
+ * with GLM) behind a header with a format version (2: corrections stored for
+ * interior cells only), the grid's shape, precision, div-B option, a hash of
+ * the block ranges and the step count. falcon_load_restart into a context of
+ * the same configuration continues bit for bit as the run that wrote the
+ * dump; a file of another configuration or version, or a short file, returns
  * FALCON_ERR_INVALID_ARG and leaves the state unchanged. */
 int  falcon_save_restart(falcon_ctx* ctx, const char* path);
 int  falcon_load_restart(falcon_ctx* ctx, const char* path);
