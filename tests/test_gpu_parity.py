@@ -96,13 +96,18 @@ def test_fp64_ten_steps_cfg1_within_1e12():
     print("fp64 worst relative error per var:", dict(zip(config.VAR_NAMES, worst)))
 
 
-def test_mixed_vs_fp64_gpu_100_steps():
+@pytest.mark.parametrize("blocks", ["8cube", "16cube"])
+def test_mixed_vs_fp64_gpu_100_steps(blocks):
     """FP32 state/RHS with FP64 p1 assembly against the FP64 GPU path after
     100 steps. Gate: relative L2 error ||u_mixed-u_64||_2/||u_64||_2 <= 1e-6
     per variable; the norm-wise max error max|d|/max|u| is reported and held
-    below 1e-5 (FP32 storage alone puts it near 2e-6 for B after 100 steps)."""
-    mk64 = config.shell_fp64_cpu
-    mkmx = lambda **kw: config.shell_fp64_cpu(precision=config.PREC_MIXED, **kw)
+    below 1e-5 (FP32 storage alone puts it near 2e-6 for B after 100 steps).
+    The same shell in 16^3 blocks runs the production forms of the mixed
+    kernels (half-warp radial pushes, one thread per diffusion cell with the
+    k slope carried between chunks)."""
+    gk = {} if blocks == "8cube" else dict(block=(16, 16, 16), radial_levels=1, amr=())
+    mk64 = lambda **kw: config.shell_fp64_cpu(**gk, **kw)
+    mkmx = lambda **kw: config.shell_fp64_cpu(precision=config.PREC_MIXED, **gk, **kw)
     a = fg.Falcon(mk64())
     b = fg.Falcon(mkmx())
     u0 = synth.initial_state(mk64(), a.block_ranges(), a.block_flags(), seed=1002)
