@@ -298,13 +298,16 @@ def test_divb_fp64_ten_steps_cfg1_within_1e12(divb):
         assert (e <= TOL_FP64).all(), (s, dict(zip(config.VAR_NAMES, e)))
 
 
+@pytest.mark.parametrize("blocks", ["8cube", "16cube"])
 @pytest.mark.parametrize("divb", [1, 2])
-def test_divb_mixed_vs_fp64_gpu_100_steps(divb):
+def test_divb_mixed_vs_fp64_gpu_100_steps(divb, blocks):
     """The mixed path with GLM or Powell against the FP64 GPU path after 100
     steps: relative L2 <= 1e-6 for every variable, psi included (psi is
-    driven by the divergence of B formed from FP32 values)."""
-    mk64 = lambda: config.shell_fp64_cpu(divb_option=divb)
-    mkmx = lambda: config.shell_fp64_cpu(divb_option=divb, precision=config.PREC_MIXED)
+    driven by the divergence of B formed from FP32 values); also on the same
+    shell in 16^3 blocks."""
+    gk = {} if blocks == "8cube" else dict(block=(16, 16, 16), radial_levels=1, amr=())
+    mk64 = lambda: config.shell_fp64_cpu(divb_option=divb, **gk)
+    mkmx = lambda: config.shell_fp64_cpu(divb_option=divb, precision=config.PREC_MIXED, **gk)
     a, b = fg.Falcon(mk64()), fg.Falcon(mkmx())
     u0 = _init_divb(mk64(), a.block_ranges(), a.block_flags(), divb, 1005)
     for x in (a, b):
