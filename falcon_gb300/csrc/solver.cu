@@ -1007,10 +1007,11 @@ int setup(falcon_solver* sv) {
                 stv.push_back(h.w[dd] != 0.0 ? strides[dd] : 0);
             }
         }
-        {   // source order: a warp's gathers read neighbouring source cells
+        {   // target order: a warp's stores write neighbouring ghost cells
+            // (measured faster than source order, most for the PFSS batch)
             std::vector<size_t> ord(dst.size());
             for (size_t q = 0; q < ord.size(); ++q) ord[q] = q;
-            std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return src[a] < src[b]; });
+            std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return dst[a] < dst[b]; });
             std::vector<int32_t> d2(ord.size()), s2(ord.size()), st2(3 * ord.size());
             std::vector<double> w2(3 * ord.size());
             for (size_t q = 0; q < ord.size(); ++q) {
@@ -1027,8 +1028,8 @@ int setup(falcon_solver* sv) {
             w.swap(w2);
             std::vector<size_t> oc(cdst.size());
             for (size_t q = 0; q < oc.size(); ++q) oc[q] = q;
-            std::stable_sort(oc.begin(), oc.end(), [&](size_t a, size_t b) { return csrc[a] < csrc[b]; });
-            // runs by parity (each run keeps the source order), see SvLevel
+            std::stable_sort(oc.begin(), oc.end(), [&](size_t a, size_t b) { return cdst[a] < cdst[b]; });
+            // runs by parity (each run keeps the target order), see SvLevel
             auto par = [&](int32_t o) {
                 const int64_t r = (int64_t)o % L.d.npad;
                 return (int)((r % L.d.p0 + (r / L.d.p0) % L.d.p1 + r / ((int64_t)L.d.p0 * L.d.p1)) & 1);
