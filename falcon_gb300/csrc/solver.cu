@@ -1286,7 +1286,12 @@ int falcon_solver_create(falcon_solver** out, const falcon_solver_spec* spec) {
     if (spec->nproblems < 1 || spec->nproblems > FALCON_MAX_PROBLEMS) return sv->fail(FALCON_ERR_INVALID_ARG, "nproblems out of range");
     if (spec->block < 2 || spec->block > 32 || (spec->block & 1)) return sv->fail(FALCON_ERR_INVALID_ARG, "block must be even, 2..32");
     sv->device = spec->device;
-    if (spec->kind == FALCON_SOLVER_CONDUCTION) sv->nu_coarse = 4;
+    if (spec->kind == FALCON_SOLVER_CONDUCTION) {
+        sv->nu_coarse = 4;
+    } else {   // PFSS: one sweep each way, 32 on the coarsest level (measured fastest to 1e-10)
+        sv->nu_pre = sv->nu_post = 1;
+        sv->nu_coarse = 32;
+    }
     std::vector<falcon_config> cfgs(spec->nproblems);
     const double kRsun = (double)6.955e10f;
     for (int q = 0; q < spec->nproblems; ++q) {

@@ -348,7 +348,7 @@ int  falcon_solver_solution(falcon_solver* sv, double* x);
 int  falcon_solver_timestep(const falcon_solver* sv, double* dt);
 /* red-black Gauss-Seidel sweeps of the V-cycle: before and after the coarse
  * correction on every level but the coarsest, and on the coarsest level
- * (defaults 2, 2, 16 for PFSS; 2, 2, 4 for conduction, whose implicit step
+ * (defaults 1, 1, 32 for PFSS; 2, 2, 4 for conduction, whose implicit step
  * makes the coarse problem well conditioned: fewer coarse sweeps leave its
  * iteration count unchanged) */
 int  falcon_solver_set_smoothing(falcon_solver* sv, int32_t nu_pre, int32_t nu_post, int32_t nu_coarse);
