@@ -377,10 +377,78 @@ def run_ours(args, rank, world, local, dist):
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clk,
         }
+    f.close()
+    if rank == 0:
+        if world == 1 and not args.no_accuracy and args.workload == "full":
+            line["accuracy"] = accuracy_leg(local, steps=100)
+            line["fp64_path"] = fp64_path_bench(local, line["accuracy"])
         if world == 1 and not args.no_solvers and args.workload == "full":
             line["solvers"] = solver_bench(local)
         print(json.dumps(line))
+
+
+def accuracy_leg(device, steps=100):
+    """The workload's accuracy: the same 21,233,664-cell shell and seeded
+    initial state advanced `steps` RK4 steps in MIXED and in FP64 on the GPU
+    (each with its own dt), per-variable relative L2 and norm-wise max error
+    of the mixed state against the FP64 state over the interior cells
+    (falcon_gb300.compare). The FP64 run is timed too (CUDA events)."""
+    import falcon_gb300 as fg
+    from falcon_gb300 import config
+    from falcon_gb300.compare import state_errors, worst
+    states, ms = {}, {}
+    for name, prec in (("fp64", config.PREC_FP64), ("mixed", config.PREC_MIXED)):
+        f = fg.Falcon(config.shell_mixed_21m(precision=prec, device=device))
+        f.init_synthetic(kind=1, seed=1002, mach=0.01)
+        f.exchange()
+        f.exchange()
+        f.advance_rk4(want_dt=False)    # first step: autotuner and graph capture
+        f.synchronize()
+        f.init_synthetic(kind=1, seed=1002, mach=0.01)
+        f.exchange()
+        f.exchange()
+        f.synchronize()
+        f.timer_start()
+        f.run_steps(steps)
+        ms[name] = f.timer_stop()
+        f.synchronize()
+        states[name] = f.download_state()
+        cells = f.interior_cells
+        f.close()
+    e = state_errors(states["mixed"], states["fp64"])
+    del states
+    return {"workload": WORKLOAD, "cells": cells, "steps": steps, "seed": 1002, "init": "kind 1 (Kolmogorov, Mach 0.01)",
+            "reference": "FP64 GPU path, same initial state", "per_var": e,
+            "max_rel_l2": worst(e, "rel_l2"), "max_rel_max": worst(e, "rel_max"), "target_rel": 1e-6,
+            "ms_per_step": {k: v / steps for k, v in ms.items()}}
+
+
+def fp64_path_bench(device, acc):
+    """Throughput of the FP64 (bit-exact) path: the 21M-cell shell from the
+    accuracy run, and the 442,368-cell shell of 8^3 blocks (the CPU-runnable
+    workload, 10 steps after 3 warm-up steps)."""
+    import falcon_gb300 as fg
+    from falcon_gb300 import config
+    out = {}
+    ms = acc["ms_per_step"]["fp64"]
+    out["shell_21M_16cube"] = {"cells": acc["cells"], "ms_per_step": ms, "value": acc["cells"] / (ms / 1e3),
+                               "bytes_per_cell_step": 944,
+                               "achieved_GBs": acc["cells"] * 944 / (ms / 1e3) / 1e9}
+    f = fg.Falcon(config.shell_fp64_cpu(device=device))
+    f.init_synthetic(kind=0, seed=1001)
+    f.exchange()
+    f.exchange()
+    f.run_steps(3)
+    f.synchronize()
+    f.timer_start()
+    f.run_steps(10)
+    t = f.timer_stop() / 10
+    out["shell_442k_8cube"] = {"cells": f.interior_cells, "ms_per_step": t, "value": f.interior_cells / (t / 1e3),
+                               "bytes_per_cell_step": 944,
+                               "achieved_GBs": f.interior_cells * 944 / (t / 1e3) / 1e9}
     f.close()
+    out["unit"] = UNIT
+    return out
 
 
 def _smooth_field(shape, rs):
@@ -451,6 +519,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the 100-step mixed-vs-FP64 accuracy run reported under 'accuracy'")
     ap.add_argument("--no-solvers", action="store_true",
                     help="skip the implicit-solver workloads reported under 'solvers'")
     ap.add_argument("--workload", default="full", choices=["full", "small"],

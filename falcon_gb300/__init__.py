@@ -52,7 +52,9 @@ EXPORTS = (
     "falcon_lcc_create", "falcon_lcc_destroy", "falcon_lcc_last_error", "falcon_lcc_num_params",
     "falcon_lcc_get_params", "falcon_lcc_set_params", "falcon_lcc_forward", "falcon_lcc_loss_grad",
     "falcon_lcc_train", "falcon_save_allcells", "falcon_save_restart", "falcon_load_restart",
-    "falcon_upload_state_core", "falcon_download_state_core",
+    "falcon_upload_state_core", "falcon_download_state_core", "falcon_set_wait_limit",
+    "falcon_set_background", "falcon_solver_set_operator", "falcon_solver_set_magnetogram",
+    "falcon_solver_magnetogram", "falcon_solver_set_guess",
 )
 
 # size of the static device array behind falcon_download_state_range
@@ -151,6 +153,15 @@ class Falcon:
         self._ck(self.L.falcon_get_background(self.h, _ptr(out)))
         return out
 
+    def set_background(self, prof):
+        """Replace the background with the driver's radial profiles, in the
+        layout of background(): [block][NPROF][ni+2ng]."""
+        prof = np.ascontiguousarray(prof, dtype=np.float64)
+        t = self.cfg.tree
+        if prof.shape != (self.nblocks, config.NPROF, t.ni + 2 * t.ng):
+            raise ValueError("background shape %s" % (prof.shape,))
+        self._ck(self.L.falcon_set_background(self.h, _ptr(prof)))
+
     def ghost_count(self):
         n = C.c_int64()
         self._ck(self.L.falcon_ghost_count(self.h, C.byref(n)))
@@ -233,6 +244,10 @@ class Falcon:
 
     def synchronize(self):
         self._ck(self.L.falcon_synchronize(self.h))
+
+    def set_wait_limit(self, polls):
+        """Poll limit of the step kernels' bulk-copy waits (< 0: the default)."""
+        self._ck(self.L.falcon_set_wait_limit(self.h, C.c_int32(polls)))
 
     # ---- output and restart
     def save_allcells(self, directory, step):

@@ -284,6 +284,14 @@ cudaError_t fresh_state(falcon_ctx* ctx) {
 // The second stage buffer starts as a copy of the state: cells that no
 // kernel writes (ghost cells outside every exchange list) then agree in both
 // buffers whichever holds the state.
+// A new state (upload, synthetic initial condition, restart) starts with the
+// step flags clear: no NaN seen, no copy wait run out.
+cudaError_t clear_step_flags(falcon_ctx* ctx) {
+    cudaError_t e = cudaMemsetAsync(&ctx->sc->nan_flag, 0, sizeof(int32_t), ctx->st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(&ctx->sc->nan_step, 0xFF, sizeof(int32_t), ctx->st);   // -1
+    return e;
+}
+
 cudaError_t mirror_state(falcon_ctx* ctx) {
     if (!ctx->R2) return cudaSuccess;
     return cudaMemcpyAsync(ctx->R2, ctx->U, (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell * ctx->elem,
@@ -350,6 +358,17 @@ int check_nan(falcon_ctx* ctx) {
     cudaError_t e = cudaMemcpy(&flag, &ctx->sc->nan_flag, sizeof(int32_t), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return ctx->cuda_fail(e, "nan flag");
     cudaMemcpy(&stp, &ctx->sc->nan_step, sizeof(int32_t), cudaMemcpyDeviceToHost);
+    if (flag & 2) {
+        // a step kernel's wait for a bulk copy ran out: its CTAs left cleanly,
+        // the step's results are discarded (the state is undefined until the
+        // next upload, synthetic initial condition or restart)
+        int32_t polls = 0;
+        cudaMemcpy(&polls, &ctx->sc->wait_polls, sizeof(int32_t), cudaMemcpyDeviceToHost);
+        char buf[192];
+        snprintf(buf, sizeof buf, "a step kernel's bulk-copy wait ran out (poll limit %d); the state is undefined", polls);
+        ctx->err = buf;
+        return FALCON_ERR_TIMEOUT;
+    }
     if (flag) {
         char buf[128];
         snprintf(buf, sizeof buf, "NaN detected in the state at the start of step %d", stp);
@@ -364,41 +383,13 @@ inline int64_t cell_off(const Grid& g, int b, int i, int j, int k) {
     return (int64_t)b * NV * g.ncell + ((int64_t)(k + 1) * g.njp + (j + 1)) * g.nip + (i + 1);
 }
 
-int setup_device(falcon_ctx* ctx) {
+// Per-block 1-D geometry and background tables on the device, from the grid's
+// radial profiles g.prof (the outputs of ModStratification_new_get_vars at the
+// cell centres, 3_6/ModBlock.f90:232-264): built at set-up and again when a
+// driver supplies its own profiles (falcon_set_background).
+int upload_tables(falcon_ctx* ctx, bool first) {
     const Grid& g = ctx->grid;
     const int nb = g.nblocks;
-    if ((int64_t)nb * NV * g.ncell >= (int64_t)INT32_MAX) return ctx->fail(FALCON_ERR_INVALID_ARG, "grid too large for 32-bit offsets");
-    const bool sup = (g.ni == 8 && g.nj == 8 && g.nk == 8) || (g.ni == 16 && g.nj == 16 && g.nk == 16);
-    if (!sup) return ctx->fail(FALCON_ERR_INVALID_ARG, "device kernels are built for 8^3 and 16^3 blocks");
-    int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return ctx->fail(FALCON_ERR_NO_DEVICE, "no CUDA device");
-    if (ctx->cfg.device >= ndev) return ctx->fail(FALCON_ERR_INVALID_ARG, "device ordinal out of range");
-    CK(cudaSetDevice(ctx->cfg.device), "cudaSetDevice");
-    ctx->device = ctx->cfg.device;
-    CK(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking), "stream");
-    CK(cudaEventCreate(&ctx->t0), "event");
-    CK(cudaEventCreate(&ctx->t1), "event");
-    ctx->dims = StepDims{nb, g.ni, g.nj, g.nk, g.nip, g.njp, g.nkp, g.ncell};
-    ctx->elem = ctx->mixed() ? 4 : 8;
-    const size_t sbytes = (size_t)nb * NV * g.ncell * ctx->elem;
-    CK(ctx->alloc(&ctx->U, sbytes), "alloc U");
-    ctx->bufA = ctx->U;
-    CK(ctx->alloc(&ctx->RK, sbytes), "alloc RK");
-    CK(cudaMemsetAsync(ctx->U, 0, sbytes, ctx->st), "memset");
-    CK(cudaMemsetAsync(ctx->RK, 0, sbytes, ctx->st), "memset");
-    if (ctx->cfg.phys.divb_option == 1) {
-        const size_t pbytes = (size_t)nb * g.ncell * ctx->elem;
-        for (void** q : {&ctx->P, &ctx->Prk, &ctx->P2}) {
-            CK(ctx->alloc(q, pbytes), "alloc psi");
-            CK(cudaMemsetAsync(*q, 0, pbytes, ctx->st), "memset");
-        }
-    }
-    if (ctx->mixed()) {
-        CK(ctx->alloc(&ctx->Ulo, lo_elems(ctx->dims)), "alloc U correction");
-        CK(cudaMemsetAsync(ctx->Ulo, 0, lo_elems(ctx->dims), ctx->st), "memset");
-    }
-
-    // geometry and background tables (3_6/ModBlock.f90:188-265, 288-438)
     std::vector<double> gi((size_t)nb * GI_COUNT * g.nip), gj((size_t)nb * GJ_COUNT * g.njp), gs((size_t)nb * GS_COUNT);
     const double ratio = ctx->cfg.phys.heating_ratio;
     for (int b = 0; b < nb; ++b) {
@@ -440,19 +431,67 @@ int setup_device(falcon_ctx* ctx) {
         S[GS_DXK] = g.dx[3 * b + 2];
     }
     std::vector<float> gif(gi.begin(), gi.end()), gjf(gj.begin(), gj.end()), gsf(gs.begin(), gs.end());
-    CK(ctx->alloc(&ctx->gi, gi.size() * 8), "alloc gi");
-    CK(ctx->alloc(&ctx->gj, gj.size() * 8), "alloc gj");
-    CK(ctx->alloc(&ctx->gs, gs.size() * 8), "alloc gs");
-    CK(ctx->alloc(&ctx->gi_f, gif.size() * 4), "alloc gi_f");
-    CK(ctx->alloc(&ctx->gj_f, gjf.size() * 4), "alloc gj_f");
-    CK(ctx->alloc(&ctx->gs_f, gsf.size() * 4), "alloc gs_f");
-    CK(ctx->alloc(&ctx->flags, (size_t)nb * 4), "alloc flags");
+    if (first) {
+        CK(ctx->alloc(&ctx->gi, gi.size() * 8), "alloc gi");
+        CK(ctx->alloc(&ctx->gj, gj.size() * 8), "alloc gj");
+        CK(ctx->alloc(&ctx->gs, gs.size() * 8), "alloc gs");
+        CK(ctx->alloc(&ctx->gi_f, gif.size() * 4), "alloc gi_f");
+        CK(ctx->alloc(&ctx->gj_f, gjf.size() * 4), "alloc gj_f");
+        CK(ctx->alloc(&ctx->gs_f, gsf.size() * 4), "alloc gs_f");
+    }
+    // ordered after the context stream's earlier work (the tables are read
+    // by every step kernel): plain copies wait for nothing on a non-blocking stream
+    CK(cudaStreamSynchronize(ctx->st), "tables");
     CK(cudaMemcpy(ctx->gi, gi.data(), gi.size() * 8, cudaMemcpyHostToDevice), "upload gi");
     CK(cudaMemcpy(ctx->gj, gj.data(), gj.size() * 8, cudaMemcpyHostToDevice), "upload gj");
     CK(cudaMemcpy(ctx->gs, gs.data(), gs.size() * 8, cudaMemcpyHostToDevice), "upload gs");
     CK(cudaMemcpy(ctx->gi_f, gif.data(), gif.size() * 4, cudaMemcpyHostToDevice), "upload gi_f");
     CK(cudaMemcpy(ctx->gj_f, gjf.data(), gjf.size() * 4, cudaMemcpyHostToDevice), "upload gj_f");
     CK(cudaMemcpy(ctx->gs_f, gsf.data(), gsf.size() * 4, cudaMemcpyHostToDevice), "upload gs_f");
+
+    return FALCON_OK;
+}
+
+int setup_device(falcon_ctx* ctx) {
+    const Grid& g = ctx->grid;
+    const int nb = g.nblocks;
+    if ((int64_t)nb * NV * g.ncell >= (int64_t)INT32_MAX) return ctx->fail(FALCON_ERR_INVALID_ARG, "grid too large for 32-bit offsets");
+    const bool sup = (g.ni == 8 && g.nj == 8 && g.nk == 8) || (g.ni == 16 && g.nj == 16 && g.nk == 16);
+    if (!sup) return ctx->fail(FALCON_ERR_INVALID_ARG, "device kernels are built for 8^3 and 16^3 blocks");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return ctx->fail(FALCON_ERR_NO_DEVICE, "no CUDA device");
+    if (ctx->cfg.device >= ndev) return ctx->fail(FALCON_ERR_INVALID_ARG, "device ordinal out of range");
+    CK(cudaSetDevice(ctx->cfg.device), "cudaSetDevice");
+    ctx->device = ctx->cfg.device;
+    CK(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking), "stream");
+    CK(cudaEventCreate(&ctx->t0), "event");
+    CK(cudaEventCreate(&ctx->t1), "event");
+    ctx->dims = StepDims{nb, g.ni, g.nj, g.nk, g.nip, g.njp, g.nkp, g.ncell};
+    ctx->elem = ctx->mixed() ? 4 : 8;
+    const size_t sbytes = (size_t)nb * NV * g.ncell * ctx->elem;
+    CK(ctx->alloc(&ctx->U, sbytes), "alloc U");
+    ctx->bufA = ctx->U;
+    CK(ctx->alloc(&ctx->RK, sbytes), "alloc RK");
+    CK(cudaMemsetAsync(ctx->U, 0, sbytes, ctx->st), "memset");
+    CK(cudaMemsetAsync(ctx->RK, 0, sbytes, ctx->st), "memset");
+    if (ctx->cfg.phys.divb_option == 1) {
+        const size_t pbytes = (size_t)nb * g.ncell * ctx->elem;
+        for (void** q : {&ctx->P, &ctx->Prk, &ctx->P2}) {
+            CK(ctx->alloc(q, pbytes), "alloc psi");
+            CK(cudaMemsetAsync(*q, 0, pbytes, ctx->st), "memset");
+        }
+    }
+    if (ctx->mixed()) {
+        CK(ctx->alloc(&ctx->Ulo, lo_elems(ctx->dims)), "alloc U correction");
+        CK(cudaMemsetAsync(ctx->Ulo, 0, lo_elems(ctx->dims), ctx->st), "memset");
+    }
+
+    // geometry and background tables (3_6/ModBlock.f90:188-265, 288-438)
+    {
+        const int rc = upload_tables(ctx, true);
+        if (rc) return rc;
+    }
+    CK(ctx->alloc(&ctx->flags, (size_t)nb * 4), "alloc flags");
     CK(cudaMemcpy(ctx->flags, g.flags.data(), (size_t)nb * 4, cudaMemcpyHostToDevice), "upload flags");
 
     // Ghost lists. FP64 keeps the reference's weights exactly (trilinear for
@@ -716,6 +755,7 @@ int setup_device(falcon_ctx* ctx) {
     s0.min_ratio_bits = 0x7FF0000000000000ull;
     s0.cfl = ctx->cfg.phys.cfl;
     s0.nan_step = -1;
+    s0.wait_polls = kDefaultWaitPolls;
     CK(ctx->alloc(&ctx->sc, sizeof(StepScalars)), "alloc scalars");
     CK(cudaMemcpy(ctx->sc, &s0, sizeof s0, cudaMemcpyHostToDevice), "upload scalars");
     CK(cudaStreamSynchronize(ctx->st), "sync");
@@ -794,6 +834,31 @@ int falcon_block_flags(const falcon_ctx* ctx, int32_t* f) {
 int falcon_get_background(const falcon_ctx* ctx, double* p) {
     if (!ctx || !p) return FALCON_ERR_INVALID_ARG;
     std::memcpy(p, ctx->grid.prof.data(), ctx->grid.prof.size() * sizeof(double));
+    return FALCON_OK;
+}
+
+int falcon_set_background(falcon_ctx* ctx, const double* p) {
+    if (!ctx || !p) return FALCON_ERR_INVALID_ARG;
+    Grid& g = ctx->grid;
+    const size_t n = g.prof.size();
+    // the derived tables divide by rho0, rho0*T0 and Xi, and take sqrt(gamma1 p0/rho0)
+    for (int b = 0; b < g.nblocks; ++b)
+        for (int i = 0; i < g.nip; ++i) {
+            const double* P = p + (size_t)b * FALCON_NPROF * g.nip + i;
+            bool ok = true;
+            for (int q = 0; q < FALCON_NPROF; ++q) ok = ok && std::isfinite(P[(size_t)q * g.nip]);
+            ok = ok && P[1 * g.nip] > 0 && P[2 * g.nip] > 0 && P[3 * g.nip] > 0 && P[4 * g.nip] > 0 && P[8 * g.nip] > 0;
+            if (!ok)
+                return ctx->fail(FALCON_ERR_INVALID_ARG, "falcon_set_background: block " + std::to_string(b) + " cell " +
+                                                              std::to_string(i) +
+                                                              ": profiles must be finite with rho0, p0, T0, gamma1, Xi > 0");
+        }
+    std::memcpy(g.prof.data(), p, n * sizeof(double));
+    if (!ctx->on_device) return FALCON_OK;
+    cudaSetDevice(ctx->device);
+    const int rc = upload_tables(ctx, false);
+    if (rc) return rc;
+    ctx->cfl_ready = false;   // the wave speed changed with the background
     return FALCON_OK;
 }
 
@@ -912,6 +977,7 @@ int falcon_upload_state(falcon_ctx* ctx, const double* u) {
     if (rc) return rc;
     ctx->stale_edges = false;   // the uploaded ghost cells are the state's
     ctx->cfl_ready = false;
+    CK(clear_step_flags(ctx), "upload");
     // primitive_rk_IV = primitive_IV, as the reference's initialisation leaves it
     const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
     CK(cudaMemcpyAsync(ctx->RK, ctx->U, n * ctx->elem, cudaMemcpyDeviceToDevice, ctx->st), "upload");
@@ -939,7 +1005,7 @@ int falcon_download_state_range(falcon_ctx* ctx, size_t first, size_t count, dou
     int rc = need_device(ctx);
     if (rc) return rc;
     if (!u && count) return ctx->fail(FALCON_ERR_INVALID_ARG, "null state");
-    CK(fresh_state(ctx), "ghost fill");
+    // the size checks need only the host layout: a rejected call does no device work
     const size_t n = host_elems(ctx);
     const size_t cap = static_scratch_elems();
     if (count > cap)
@@ -951,6 +1017,7 @@ int falcon_download_state_range(falcon_ctx* ctx, size_t first, size_t count, dou
         return ctx->fail(FALCON_ERR_INVALID_ARG, "falcon_download_state_range: first " + std::to_string(first) +
                                                      " + count " + std::to_string(count) + " exceeds the state size " +
                                                      std::to_string(n));
+    CK(fresh_state(ctx), "ghost fill");
     const std::string e = download_range_static(ctx->device, ctx->st, ctx->U, ctx->Ulo, ctx->P, ctx->mixed(), ctx->dims,
                                                 first, count, u);
     if (!e.empty()) return ctx->fail(FALCON_ERR_CUDA, e);
@@ -993,6 +1060,7 @@ int falcon_upload_state_core(falcon_ctx* ctx, const double* u) {
     CK(ghost(ctx, ctx->U), "upload core");
     ctx->stale_edges = false;
     ctx->cfl_ready = false;
+    CK(clear_step_flags(ctx), "upload core");
     CK(cudaMemcpyAsync(ctx->RK, ctx->U, n * ctx->elem, cudaMemcpyDeviceToDevice, ctx->st), "upload core");
     CK(mirror_state(ctx), "upload core");
     if (ctx->P) {
@@ -1052,6 +1120,7 @@ int falcon_init_synthetic(falcon_ctx* ctx, int32_t kind, uint64_t seed, double m
     CK(mirror_state(ctx), "init");
     ctx->stale_edges = false;
     ctx->cfl_ready = false;
+    CK(clear_step_flags(ctx), "init");
     CK(cudaStreamSynchronize(ctx->st), "init");
     return FALCON_OK;
 }
@@ -1415,11 +1484,21 @@ int falcon_load_restart(falcon_ctx* ctx, const char* path) {
     CK(mirror_state(ctx), "restart");
     ctx->stale_edges = false;
     ctx->cfl_ready = false;
+    CK(clear_step_flags(ctx), "restart");
     if (ctx->P)
         for (void* q : {ctx->Prk, ctx->P2})
             CK(cudaMemcpyAsync(q, ctx->P, h.bytes_psi, cudaMemcpyDeviceToDevice, ctx->st), "restart");
     CK(cudaStreamSynchronize(ctx->st), "restart");
     ctx->steps_done = h.steps_done;
+    return FALCON_OK;
+}
+
+int falcon_set_wait_limit(falcon_ctx* ctx, int32_t polls) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    const int32_t v = polls < 0 ? kDefaultWaitPolls : polls;
+    CK(cudaMemcpyAsync(&ctx->sc->wait_polls, &v, sizeof v, cudaMemcpyHostToDevice, ctx->st), "wait limit");
+    CK(cudaStreamSynchronize(ctx->st), "wait limit");
     return FALCON_OK;
 }
 

@@ -106,8 +106,12 @@ struct StepScalars {
     int32_t nan_flag;                   // sticky: bit0 NaN seen in the state, bit1 a copy wait timed out
     int32_t nan_step;                   // step counter value when it was first seen
     int32_t step_counter;               // steps finalised so far (device side)
-    int32_t pad_;
+    int32_t wait_polls;                 // poll limit of the step kernels' bulk-copy waits
 };
+
+// Default poll limit of a bulk-copy wait (each poll may suspend briefly, so
+// the wait is bounded in time as well as in count).
+constexpr int32_t kDefaultWaitPolls = 1 << 22;
 
 struct GhostCopyList {   // ghost cells that are exact copies (all weights zero, same panel)
     int64_t n;

@@ -143,7 +143,19 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int ma
     }
     return false;
 }
-constexpr int kWaitPolls = 1 << 22;   // each poll may suspend briefly; bounded overall
+constexpr int kWaitPolls = kDefaultWaitPolls;
+
+// A CTA whose wait for a chunk's planes ran out leaves cleanly: every thread
+// learns it at the next chunk's leading barrier (__syncthreads_or, so the exit
+// is uniform over the CTA and no thread is left at a barrier), then thread 0
+// flags the step (bit 1 of nan_flag: the host returns FALCON_ERR_TIMEOUT) and
+// waits, with the default bound, for the bulk copies still in flight into
+// this CTA's shared memory -- chunks c0..c1 -- before the CTA exits.
+__device__ __forceinline__ void copy_wait_abort(StepScalars* sc, uint64_t* bars, int c0, int c1) {
+    if (threadIdx.x != 0) return;
+    atomicOr(&sc->nan_flag, 2);
+    for (int c = c0 < 0 ? 0 : c0; c <= c1; ++c) mbar_wait(&bars[c & 1], (uint32_t)((c >> 1) & 1), kWaitPolls);
+}
 
 template <class T, int NI, int NJ, int NK, int KPAR>
 struct Shape {
@@ -459,19 +471,26 @@ k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, DivBArgs 
     const float dtk = sc->dt_stage_f[stage - 1];
 
     constexpr int nchunk = NK / KPAR;
+    const int polls = sc->wait_polls;
+    int late = 0;   // a wait of this thread for a chunk's planes ran out
     for (int ch = 0; ch < nchunk; ++ch) {
         const int k0 = 1 + ch * KPAR;  // first Fortran k of the chunk
         const int lo = (ch == 0) ? 0 : k0 + 3;   // first padded plane new to this chunk
         const int hi = k0 + KPAR + 3;            // one past the last plane it needs
-        __syncthreads();   // chunk ch-1 is done with the slots the prefetch below overwrites
+        // chunk ch-1 is done with the slots the prefetch below overwrites; a
+        // wait of chunk ch-1 that ran out ends the CTA here (chunks ch-1 and ch
+        // are in flight)
+        if (__syncthreads_or(late)) {
+            copy_wait_abort(sc, bars, ch - 1, ch);
+            return;
+        }
         if (threadIdx.x == 0 && ch + 1 < nchunk)
             issue_planes<T, S>(blk_in, tile, hi, hi + KPAR, &bars[(ch + 1) & 1]);
         if (ch + 1 < nchunk) prefetch_un(k0 + KPAR + 1);
-        if (!mbar_wait(&bars[ch & 1], (uint32_t)((ch >> 1) & 1), kWaitPolls)) {
-            atomicOr(&sc->nan_flag, 2);   // timed-out copy: reported as an error, no hang
-            mbar_wait(&bars[(ch + 1) & 1], (uint32_t)(((ch + 1) >> 1) & 1), kWaitPolls);
-            return;
-        }
+        // a wait that runs out does not leave the chunk (its barriers must be
+        // reached by every thread): the chunk computes on whatever the slots
+        // hold, the step is flagged and its results are discarded
+        late |= mbar_wait(&bars[ch & 1], (uint32_t)((ch >> 1) & 1), polls) ? 0 : 1;
         // u^n for the update (stages 2-4), loaded here so that the latency of
         // these plain loads overlaps the boundary and p1 phases below
         const int kp = k0 + kq + 1;
@@ -686,6 +705,7 @@ k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, DivBArgs 
             if (push.tgt != nullptr) push_faces<T, S>(out, pb, ii, jj, kp, o);
         }
     }
+    if (__syncthreads_or(late)) copy_wait_abort(sc, bars, nchunk - 1, nchunk - 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -850,10 +870,17 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
     int cnan = 0;
     __shared__ float sb2[S::TPC == 2 ? S::NCELLS : 1];   // |B|^2 from the thread holding B
     constexpr int nchunk = NK / KPAR;
+    const int polls = sc->wait_polls;
+    int late = 0;   // a wait of this thread for a chunk's planes ran out
     for (int ch = 0; ch < nchunk; ++ch) {
         const int k0 = 1 + ch * KPAR;
         const int hi = k0 + KPAR + 3;
-        __syncthreads();   // ring slots and face arrays of the previous chunk are free
+        // ring slots and face arrays of the previous chunk are free; a wait of
+        // chunk ch-1 that ran out ends the CTA here (chunks ch-1 and ch in flight)
+        if (__syncthreads_or(late)) {
+            copy_wait_abort(sc, bars, ch - 1, ch);
+            return;
+        }
         if (threadIdx.x == 0 && ch + 1 < nchunk) issue_planes<T, S>(blk, tile, hi, hi + KPAR, &bars[(ch + 1) & 1]);
         if (ch + 1 < nchunk) prefetch_lo(k0 + KPAR + 1);
         // this thread's int8 corrections, loaded now so that their latency
@@ -867,11 +894,9 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
                 for (int t = 0; t < S::VPT; ++t) qlo[t] = q[(size_t)t * S::NINT];
             }
         }
-        if (!mbar_wait(&bars[ch & 1], (uint32_t)((ch >> 1) & 1), kWaitPolls)) {
-            atomicOr(&sc->nan_flag, 2);
-            mbar_wait(&bars[(ch + 1) & 1], (uint32_t)(((ch + 1) >> 1) & 1), kWaitPolls);
-            return;
-        }
+        // as in the stage kernel: a wait that runs out finishes the chunk on
+        // whatever the slots hold; the step is flagged and discarded
+        late |= mbar_wait(&bars[ch & 1], (uint32_t)((ch >> 1) & 1), polls) ? 0 : 1;
         const int kp0 = k0 + 1;   // padded index of the chunk's first plane
         const int kp = kp0 + kq;
         if (copy_bc) {   // radial boundary ghost columns of the planes new to this chunk
@@ -1004,6 +1029,10 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
                 }
             }
         }
+    }
+    if (__syncthreads_or(late)) {
+        copy_wait_abort(sc, bars, nchunk - 1, nchunk - 1);
+        return;
     }
     if constexpr (!Pol<T>::exact) {
         if (cfl_next) cfl_commit(cmin, cnan, sc);

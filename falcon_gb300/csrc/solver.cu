@@ -4,12 +4,14 @@
 // (3_5/ModLinearSolver.f90:86-427) with the 7-point face-coefficient operator
 // (:15-84) and the 1-layer face-ghost halo (3_5/ModCommunication.f90:1497-1639).
 // GB300 form:
-//   - outer flexible CG in float-float (FP32 pairs, about 48 bits; GB300's
-//     FP64 pipe is too slow for the per-cell work) on the system scaled by
-//     per-problem powers of two, per-problem dot products reduced into FP64,
-//     iterative refinement on the true residual; y = A x of
-//     falcon_solver_apply, the coarse training solve and the residual query
-//     stay FP64;
+//   - FP64 iterative refinement outside: the true residual r = b - A x, its
+//     norms and the update x += d are FP64, and convergence is judged only on
+//     the FP64 ||b - A x|| / ||b||;
+//   - inside, flexible CG in float-float (FP32 pairs, about 48 bits; GB300's
+//     FP64 pipe is too slow for the per-cell work of every iteration) on the
+//     correction equation scaled by per-problem powers of two, per-problem
+//     dot products reduced into FP64; y = A x of falcon_solver_apply and the
+//     coarse training solve stay FP64;
 //   - V-cycle preconditioner in FP32: red-black Gauss-Seidel smoothing,
 //     restriction R = P^T (sum of 8 children), injection prolongation,
 //     Galerkin coarse operators;
@@ -245,18 +247,17 @@ __global__ void k_update_p(LevelDims d, double* p, const double* z, Dots D, int 
     }
 }
 
-// ---- float-float outer iteration ------------------------------------------------
-// GB300 runs FP64 at a small fraction of its FP32 rate, and the FP64 outer
-// kernels above are bound by the FP64 pipe. The solve therefore runs the
-// flexible CG in float-float: every value an FP32 pair (hi, lo), hi + lo with
-// |lo| <= ulp(hi)/2, about 48 significant bits, formed with error-free FP32
-// transformations (this file is compiled without FMA contraction; the FMAs
-// below are explicit). FP32's exponent range is too narrow for the raw
-// system (b.b reaches 1e54 for conduction), so the solve works on
-// A' = A / sA, b' = b / sb, x' = x sA / sb per problem with sA, sb powers of
-// two (exact): every vector and dot product is then O(1).
+// ---- float-float inner iteration -------------------------------------------------
+// GB300 runs FP64 at a small fraction of its FP32 rate, and FP64 kernels run
+// every iteration are bound by the FP64 pipe. The inner solve of each
+// refinement pass therefore runs the flexible CG in float-float: every value
+// an FP32 pair (hi, lo), hi + lo with |lo| <= ulp(hi)/2, about 48 significant
+// bits, formed with error-free FP32 transformations (this file is compiled
+// without FMA contraction; the FMAs below are explicit). FP32's exponent range
+// is too narrow for the raw system (b.b reaches 1e54 for conduction), so the
+// inner solve works on A' = A / sA, r' = r / sr, d' = d sA / sr per problem
+// with sA, sr powers of two (exact): every vector and dot product is O(1).
 struct Ops2 { const float2 *Aii, *Ai, *Aj, *Ak; };
-constexpr double kEpsFF = 7.105427357601002e-15;   // 2^-47: unit roundoff of the FF pairs
 
 __device__ __forceinline__ float2 ff_quick(float s, float e) {
     const float h = s + e;
@@ -365,32 +366,6 @@ __global__ void k_update_xr_ff(LevelDims d, float2* x, const float2* p, float2* 
     block_sum_atomic_ff(rr, &D.rr[pb]);
 }
 
-// r = b' - A' x (true residual); rr += r.r; ab += (|b| + sum|A x|)^2 (the
-// scale of its rounding error); bb += b.b
-__global__ void k_residual_ff(Ops2 A, LevelDims d, const float2* x, const float2* bvec, float2* r, float* rf, Dots D,
-                              int want_bb) {
-    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
-    float2 rr = make_float2(0.f, 0.f), bb = make_float2(0.f, 0.f), ab = make_float2(0.f, 0.f);
-    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
-        int i, j, k;
-        cell_ijk(d, c, i, j, k);
-        const size_t q = (size_t)b * d.nint + c;
-        float ar;
-        const float2 bv = bvec[q];
-        const float2 rv = ff_add(bv, ff_neg(apply_A_ff(A, d, x, b, c, i, j, k, &ar)));
-        r[q] = rv;
-        rf[q] = rv.x;
-        rr = ff_add(rr, ff_mul(rv, rv));
-        bb = ff_add(bb, ff_mul(bv, bv));
-        const float sa = fabsf(bv.x) + ar;
-        ab = ff_add(ab, make_float2(sa * sa, 0.f));
-    }
-    const int pb = D.bprob[b];
-    block_sum_atomic_ff(rr, &D.rr[pb]);
-    block_sum_atomic_ff(ab, &D.ab[pb]);
-    if (want_bb) block_sum_atomic_ff(bb, &D.bb[pb]);
-}
-
 // z = the preconditioner's FP32 output scaled by sA (it inverts the unscaled
 // FP32 operator), or r; zAp += z.Ap
 __global__ void k_take_z_ff(LevelDims d, const float* zf, const float* sA, const float2* r, int use_r, float2* z,
@@ -453,15 +428,36 @@ __global__ void k_halo_ff(float2* v, HaloListFF H, const int32_t* cdst, const in
     v[H.dst[e]] = s;
 }
 
-// x (FP64, interior of the padded array) = x' sb / sA per problem, after a solve
-__global__ void k_ff_unscale(LevelDims d, const float2* x2, const double* fac, const int32_t* bprob, double* x) {
+// ---- FP64 iterative refinement around the float-float solve ------------------
+// r' = r / sr per problem as FF pairs (sr a power of two at or above ||r||_2:
+// exact, and |r'| <= 1), its FP32 part for the V-cycle, and rr += r'.r'
+__global__ void k_ir_start(LevelDims d, const double* r, const double* inv_sr, float2* r2, float* rf, Dots D) {
+    const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
+    const int pb = D.bprob[b];
+    const double s = inv_sr[pb];
+    float2 rr = make_float2(0.f, 0.f);
+    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
+        const size_t q = (size_t)b * d.nint + c;
+        const double v = r[q] * s;
+        const float h = (float)v;
+        const float2 x = make_float2(h, (float)(v - (double)h));
+        r2[q] = x;
+        rf[q] = h;
+        rr = ff_add(rr, ff_mul(x, x));
+    }
+    block_sum_atomic_ff(rr, &D.rr[pb]);
+}
+
+// x += d' * fac per problem (FP64): d' the float-float correction of the
+// scaled system, fac = sr / sA (a power of two, so the scaling is exact)
+__global__ void k_ir_accum(LevelDims d, const float2* x2, const double* fac, const int32_t* bprob, double* x) {
     const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
     const double f = fac[bprob[b]];
     for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         int i, j, k;
         cell_ijk(d, c, i, j, k);
         const size_t P = pidx(d, b, i, j, k);
-        x[P] = ff_to(x2[P]) * f;
+        x[P] = x[P] + ff_to(x2[P]) * f;
     }
 }
 
@@ -724,12 +720,12 @@ struct falcon_solver {
     cudaStream_t st = nullptr;
     std::vector<SvLevel> lv;
     double *x = nullptr, *p = nullptr, *r = nullptr, *Ap = nullptr, *z = nullptr, *bvec = nullptr;
-    // the float-float solve (scaled system, see Ops2): padded x2, p2; interior r2, Ap2, z2, b2
-    float2 *x2 = nullptr, *p2 = nullptr, *r2 = nullptr, *Ap2 = nullptr, *z2 = nullptr, *b2 = nullptr;
-    std::vector<double> sA, sb;           // per-problem powers of two
+    // the float-float inner solve (scaled system, see Ops2): padded x2, p2; interior r2, Ap2, z2
+    float2 *x2 = nullptr, *p2 = nullptr, *r2 = nullptr, *Ap2 = nullptr, *z2 = nullptr;
+    std::vector<double> sA;               // per-problem powers of two (the operator's scale)
     float* dsA = nullptr;                 // sA on the device (FP32: powers of two are exact)
-    double* dunscale = nullptr;           // sb / sA per problem
-    double* dots = nullptr;       // [5][nproblems]
+    double* dots = nullptr;       // [6][nproblems]: pAp, pr, zAp, rr, bb, ab
+    double* ir_par = nullptr;     // [2][nproblems]: 1/sr and sr/sA of the refinement pass
     int32_t *active = nullptr, *bprob = nullptr;
     std::vector<void*> allocs;
     int nu_pre = 2, nu_post = 2, nu_coarse = 16;
@@ -842,21 +838,6 @@ std::vector<float2> to_ff(const std::vector<double>& v, const std::vector<double
         o[q] = make_float2(h, (float)(x - (double)h));
     }
     return o;
-}
-
-// b2 = b / sb per problem (host b), and the unscale factors sb / sA
-int upload_rhs_ff(falcon_solver* sv) {
-    const SolverProblemSet& S = sv->S;
-    const size_t nint = (size_t)sv->lv[0].d.nint;
-    sv->sb = problem_scale(S, S.b, nint);
-    std::vector<double> sc(S.b.size()), un(S.nproblems);
-    for (int b = 0; b < S.nblocks; ++b)
-        for (size_t c = 0; c < nint; ++c) sc[(size_t)b * nint + c] = sv->sb[S.block_problem[b]];
-    for (int q = 0; q < S.nproblems; ++q) un[q] = sv->sb[q] / sv->sA[q];
-    const std::vector<float2> b2 = to_ff(S.b, sc);
-    SCK(cudaMemcpy(sv->b2, b2.data(), b2.size() * sizeof(float2), cudaMemcpyHostToDevice), "rhs");
-    SCK(cudaMemcpy(sv->dunscale, un.data(), un.size() * 8, cudaMemcpyHostToDevice), "rhs");
-    return FALCON_OK;
 }
 
 // z_0 = M r_0: one V-cycle on the FP32 residual stored in lv[0].r
@@ -1107,6 +1088,7 @@ int setup(falcon_solver* sv) {
     SCK(sv->alloc(&sv->z, (size_t)nb * d0.nint * 8), "vectors");
     SCK(sv->alloc(&sv->bvec, (size_t)nb * d0.nint * 8), "vectors");
     SCK(sv->alloc(&sv->dots, (size_t)6 * S.nproblems * 8), "scalars");
+    SCK(sv->alloc(&sv->ir_par, (size_t)2 * S.nproblems * 8), "scalars");
     SCK(sv->alloc(&sv->active, (size_t)S.nproblems * 4), "scalars");
     SCK(sv->alloc(&sv->bprob, (size_t)nb * 4), "scalars");
     SCK(cudaMemcpy(sv->bvec, S.b.data(), S.b.size() * 8, cudaMemcpyHostToDevice), "rhs");
@@ -1132,14 +1114,11 @@ int setup(falcon_solver* sv) {
         SCK(upff(&L0.Aj2, H.Aj), "operator");
         SCK(upff(&L0.Ak2, H.Ak), "operator");
         for (float2** v : {&sv->x2, &sv->p2}) SCK(sv->alloc(v, (size_t)nb * d0.npad * sizeof(float2)), "vectors");
-        for (float2** v : {&sv->r2, &sv->Ap2, &sv->z2, &sv->b2})
+        for (float2** v : {&sv->r2, &sv->Ap2, &sv->z2})
             SCK(sv->alloc(v, (size_t)nb * d0.nint * sizeof(float2)), "vectors");
         std::vector<float> fa(sv->sA.begin(), sv->sA.end());
         SCK(sv->alloc(&sv->dsA, fa.size() * 4), "scalars");
         SCK(cudaMemcpy(sv->dsA, fa.data(), fa.size() * 4, cudaMemcpyHostToDevice), "scalars");
-        SCK(sv->alloc(&sv->dunscale, (size_t)S.nproblems * 8), "scalars");
-        const int rc = upload_rhs_ff(sv);
-        if (rc) return rc;
     }
     SCK(cudaStreamSynchronize(sv->st), "setup");
     return FALCON_OK;
@@ -1275,9 +1254,111 @@ int coarse_solve(falcon_solver* sv, const float* rc) {
     return sv->fail(FALCON_ERR_NOT_CONVERGED, "coarse solve did not reach 1e-6");
 }
 
+// The operators of every level on the device again, after the level-0
+// operator changed on the host (falcon_solver_set_operator): FP64 and FP32
+// copies of each level, the scaled float-float level 0 with its new sA, and
+// the learned stage's static input channels. Same sizes, same buffers: the
+// captured V-cycle graphs stay valid.
+int reupload_operators(falcon_solver* sv) {
+    const SolverProblemSet& S = sv->S;
+    const int nb = S.nblocks;
+    SCK(cudaStreamSynchronize(sv->st), "operator");
+    for (int l = 0; l < S.nlevels; ++l) {
+        const SolverLevel& H = S.L[l];
+        SvLevel& L = sv->lv[l];
+        const std::vector<double>* src[4] = {&H.Aii, &H.Ai, &H.Aj, &H.Ak};
+        double* d64[4] = {L.Aii, L.Ai, L.Aj, L.Ak};
+        float* d32[4] = {L.fAii, L.fAi, L.fAj, L.fAk};
+        for (int a = 0; a < 4; ++a) {
+            const std::vector<double>& h = *src[a];
+            std::vector<float> f(h.begin(), h.end());
+            SCK(cudaMemcpy(d64[a], h.data(), h.size() * 8, cudaMemcpyHostToDevice), "operator");
+            SCK(cudaMemcpy(d32[a], f.data(), f.size() * 4, cudaMemcpyHostToDevice), "operator");
+        }
+    }
+    const SolverLevel& H = S.L[0];
+    const size_t nint = (size_t)sv->lv[0].d.nint;
+    sv->sA = problem_scale(S, H.Aii, nint);
+    SvLevel& L0 = sv->lv[0];
+    const std::vector<double>* src[4] = {&H.Aii, &H.Ai, &H.Aj, &H.Ak};
+    float2* dff[4] = {L0.Aii2, L0.Ai2, L0.Aj2, L0.Ak2};
+    for (int a = 0; a < 4; ++a) {
+        const std::vector<double>& h = *src[a];
+        const size_t per = h.size() / (size_t)nb;
+        std::vector<double> sc(h.size());
+        for (int b = 0; b < nb; ++b)
+            for (size_t c = 0; c < per; ++c) sc[(size_t)b * per + c] = sv->sA[S.block_problem[b]];
+        const std::vector<float2> f = to_ff(h, sc);
+        SCK(cudaMemcpy(dff[a], f.data(), f.size() * sizeof(float2), cudaMemcpyHostToDevice), "operator");
+    }
+    std::vector<float> fa(sv->sA.begin(), sv->sA.end());
+    SCK(cudaMemcpy(sv->dsA, fa.data(), fa.size() * 4, cudaMemcpyHostToDevice), "operator");
+    if (sv->cmap_ok) {
+        SvLevel& Lc = sv->lv[S.nlevels - 1];
+        k_lcc_static<<<grid_cells(Lc.d, nb), tpb(Lc.d), 0, sv->st>>>(Lc.ops64(), Lc.d, sv->gmap, sv->feat);
+        SCK(cudaGetLastError(), "coarse features");
+    }
+    SCK(cudaStreamSynchronize(sv->st), "operator");
+    return FALCON_OK;
+}
+
+bool all_finite(const double* v, size_t n) {
+    for (size_t q = 0; q < n; ++q)
+        if (!std::isfinite(v[q])) return false;
+    return true;
+}
+
 }  // namespace
 
 extern "C" {
+
+int falcon_solver_set_operator(falcon_solver* sv, const double* Aii, const double* Ai, const double* Aj, const double* Ak) {
+    if (!sv || !Aii || !Ai || !Aj || !Ak) return FALCON_ERR_INVALID_ARG;
+    SolverProblemSet& S = sv->S;
+    SolverLevel& L = S.L[0];
+    const double* in[4] = {Aii, Ai, Aj, Ak};
+    std::vector<double>* dst[4] = {&L.Aii, &L.Ai, &L.Aj, &L.Ak};
+    for (int a = 0; a < 4; ++a)
+        if (!all_finite(in[a], dst[a]->size())) return sv->fail(FALCON_ERR_INVALID_ARG, "falcon_solver_set_operator: non-finite coefficient");
+    for (size_t q = 0; q < L.Aii.size(); ++q)
+        if (!(Aii[q] > 0.0)) return sv->fail(FALCON_ERR_INVALID_ARG, "falcon_solver_set_operator: the diagonal Aii must be positive");
+    for (int a = 0; a < 4; ++a) std::memcpy(dst[a]->data(), in[a], dst[a]->size() * 8);
+    galerkin_coarsen(S);
+    if (!sv->st) return FALCON_OK;
+    cudaSetDevice(sv->device);
+    return reupload_operators(sv);
+}
+
+int falcon_solver_set_magnetogram(falcon_solver* sv, const double* br) {
+    if (!sv || !br) return FALCON_ERR_INVALID_ARG;
+    SolverProblemSet& S = sv->S;
+    if (S.br.empty()) return sv->fail(FALCON_ERR_INVALID_ARG, "falcon_solver_set_magnetogram: not a PFSS solver");
+    if (!all_finite(br, S.br.size())) return sv->fail(FALCON_ERR_INVALID_ARG, "falcon_solver_set_magnetogram: non-finite Br");
+    std::vector<double> b(br, br + S.br.size());
+    for (int gb = 0; gb < S.nblocks; ++gb)   // only bottom blocks carry a magnetogram
+        if (!(S.block_flags[gb] & 4)) std::fill(b.begin() + (size_t)gb * (S.br.size() / S.nblocks),
+                                                b.begin() + (size_t)(gb + 1) * (S.br.size() / S.nblocks), 0.0);
+    pfss_rhs(S, b);
+    if (!sv->st) return FALCON_OK;
+    cudaSetDevice(sv->device);
+    SCK(cudaStreamSynchronize(sv->st), "rhs");
+    SCK(cudaMemcpy(sv->bvec, S.b.data(), S.b.size() * 8, cudaMemcpyHostToDevice), "rhs");
+    return FALCON_OK;
+}
+
+int falcon_solver_magnetogram(const falcon_solver* sv, double* br) {
+    if (!sv || !br) return FALCON_ERR_INVALID_ARG;
+    if (sv->S.br.empty()) return FALCON_ERR_INVALID_ARG;
+    std::memcpy(br, sv->S.br.data(), sv->S.br.size() * 8);
+    return FALCON_OK;
+}
+
+int falcon_solver_set_guess(falcon_solver* sv, const double* x0) {
+    if (!sv || !x0) return FALCON_ERR_INVALID_ARG;
+    if (!all_finite(x0, sv->S.x0.size())) return sv->fail(FALCON_ERR_INVALID_ARG, "falcon_solver_set_guess: non-finite value");
+    std::memcpy(sv->S.x0.data(), x0, sv->S.x0.size() * 8);
+    return FALCON_OK;
+}
 
 int falcon_solver_create(falcon_solver** out, const falcon_solver_spec* spec) {
     if (!out || !spec) return FALCON_ERR_INVALID_ARG;
@@ -1456,36 +1537,42 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
         return sv->fail(FALCON_ERR_INVALID_ARG, "unknown preconditioner");
     if (precond == FALCON_PRECOND_MG_LCC && (!sv->net || !sv->cmap_ok))
         return sv->fail(FALCON_ERR_INVALID_ARG, "FALCON_PRECOND_MG_LCC needs falcon_solver_attach_lcc first");
+    if (!(tol > 0.0) || max_iter < 0) return sv->fail(FALCON_ERR_INVALID_ARG, "tol must be positive and max_iter >= 0");
     cudaSetDevice(sv->device);
     const SolverProblemSet& S = sv->S;
     const int nb = S.nblocks, np = S.nproblems;
     const LevelDims& d = sv->lv[0].d;
     const dim3 g = grid_cells(d, nb);
     std::memset(rep, 0, sizeof *rep);
+    // Structure (ModLinearSolver_Multigrid_CG, 3_5/ModLinearSolver.f90:313-427,
+    // made an FP64 iterative refinement):
+    //   outer, FP64: r = b - A x with FP64 dots; a problem is done when
+    //     ||r||/||b|| <= tol -- the only convergence test;
+    //   inner, float-float FCG + FP32 V-cycle: A' d' = r' on the correction
+    //     equation scaled per problem (A' = A / sA, r' = r / sr), to a relative
+    //     recursive residual of 0.5 tol ||b|| / ||r|| (at least 2^-40);
+    //   x += d' sr / sA in FP64.
+    // A problem whose FP64 residual is at the attainable accuracy of b - A x
+    // (4 x 8 eps64 (|b| + |A||x|) / ||b||) or that a refinement no longer
+    // halves stops unconverged; its residual is reported as floor_residual.
+    constexpr double kEps64 = 1.1102230246251565e-16;   // 2^-53
+    constexpr double kEtaMin = 9.094947017729282e-13;   // 2^-40: float-float recursive residual limit
+    constexpr int kMaxPasses = 30;
     cudaEvent_t t0, t1;
     cudaEventCreate(&t0);
     cudaEventCreate(&t1);
-    // x' = x0 sA / sb, r' = b' - A' x', bb = b'.b' (float-float, the scaled system)
-    {
-        std::vector<double> sc(S.x0.size());
-        for (int b = 0; b < nb; ++b)
-            for (int c = 0; c < d.nint; ++c) sc[(size_t)b * d.nint + c] = sv->sb[S.block_problem[b]] / sv->sA[S.block_problem[b]];
-        const std::vector<float2> x0 = to_ff(S.x0, sc);
-        SCK(cudaMemsetAsync(sv->x2, 0, (size_t)nb * d.npad * sizeof(float2), sv->st), "init");
-        SCK(cudaMemcpyAsync(sv->z2, x0.data(), x0.size() * sizeof(float2), cudaMemcpyHostToDevice, sv->st), "init");
-        SCK(cudaStreamSynchronize(sv->st), "init");
-    }
+    // x = x0 (FP64, padded; ghost cells 0 until the halo fill)
+    SCK(cudaMemcpyAsync(sv->z, S.x0.data(), S.x0.size() * 8, cudaMemcpyHostToDevice, sv->st), "init");
+    SCK(cudaMemsetAsync(sv->x, 0, (size_t)nb * d.npad * 8, sv->st), "init");
+    SCK(cudaStreamSynchronize(sv->st), "init");
     cudaEventRecord(t0, sv->st);
-    k_scatter_pad<float2><<<g, tpb(d), 0, sv->st>>>(d, sv->z2, sv->x2);
-    std::vector<int32_t> act(np, 1);
-    SCK(cudaMemcpyAsync(sv->active, act.data(), np * 4, cudaMemcpyHostToDevice, sv->st), "init");
-    SCK(cudaMemsetAsync(sv->dots, 0, (size_t)6 * np * 8, sv->st), "init");
-    SCK(halo_fill_ff(sv, sv->x2), "halo");
-    k_residual_ff<<<g, tpb(d), 0, sv->st>>>(sv->lv[0].ops2(), d, sv->x2, sv->b2, sv->r2, sv->lv[0].r, sv->D(), 1);
-    std::vector<double> rr(np), bb(np);
-    SCK(cudaMemcpyAsync(bb.data(), sv->dots + 4 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "bb");
-    SCK(cudaStreamSynchronize(sv->st), "bb");
-    for (int q = 0; q < np; ++q) if (bb[q] <= 0) bb[q] = 1.0;
+    k_scatter_pad<double><<<g, tpb(d), 0, sv->st>>>(d, sv->z, sv->x);
+    SCK(cudaGetLastError(), "init");
+    // per problem: 0 being solved, 1 converged (FP64 residual <= tol), 2 stopped at its floor
+    std::vector<int> state(np, 0);
+    std::vector<int32_t> act(np, 0);
+    std::vector<double> rr(np), bb(np), ab(np), rel(np, 0.0), prev(np, 0.0), rr0(np), eta(np);
+    std::vector<double> inv_sr(np, 1.0), fac(np, 1.0);
     int pc = precond;   // FALCON_PRECOND_MG_LCC falls back to FALCON_PRECOND_MG on stagnation
     auto precondition = [&](int want_zAp) -> cudaError_t {
         cudaError_t e = cudaSuccess;
@@ -1500,117 +1587,132 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
                                                sv->D(), want_zAp);
         return cudaGetLastError();
     };
-    std::vector<double> hist;   // max over active problems of the recursive relative residual
-    std::vector<double> final_rel(np, 0.0);   // true residual of each problem when it stopped
-    std::vector<double> prev_true(np, 1e300); // true residual at the previous verification
-    // p = M r
-    SCK(precondition(0), "precondition");
-    k_update_p_ff<<<g, tpb(d), 0, sv->st>>>(d, sv->p2, sv->z2, sv->D(), 1);
-    SCK(halo_fill_ff(sv, sv->p2), "halo");
-    double worst = 0;
-    int it = 0;
-    bool done = false;
-    for (it = 1; it <= max_iter && !done; ++it) {
-        SCK(cudaMemsetAsync(sv->dots, 0, (size_t)4 * np * 8, sv->st), "dots");
-        k_spmv_dots_ff<<<g, tpb(d), 0, sv->st>>>(sv->lv[0].ops2(), d, sv->p2, sv->Ap2, sv->r2, sv->D());
-        k_update_xr_ff<<<g, tpb(d), 0, sv->st>>>(d, sv->x2, sv->p2, sv->r2, sv->Ap2, sv->lv[0].r, sv->D());
-        SCK(cudaGetLastError(), "iterate");
+    int it = 0, passes = 0;
+    for (bool first = true;; first = false) {
+        // FP64 true residual of every problem
+        SCK(cudaMemsetAsync(sv->dots + 3 * np, 0, (size_t)(first ? 3 : 1) * np * 8, sv->st), "dots");
+        SCK(cudaMemsetAsync(sv->dots + 5 * np, 0, (size_t)np * 8, sv->st), "dots");
+        SCK(halo_fill<double>(sv, 0, sv->x), "halo");
+        k_residual64<<<g, tpb(d), 0, sv->st>>>(sv->lv[0].ops64(), d, sv->x, sv->bvec, sv->r, sv->lv[0].r, sv->D(),
+                                               first ? 1 : 0);
+        SCK(cudaGetLastError(), "residual");
         SCK(cudaMemcpyAsync(rr.data(), sv->dots + 3 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "rr");
+        SCK(cudaMemcpyAsync(ab.data(), sv->dots + 5 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "rr");
+        if (first) SCK(cudaMemcpyAsync(bb.data(), sv->dots + 4 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "bb");
         SCK(cudaStreamSynchronize(sv->st), "rr");
-        bool all = true;
-        double hmax = 0;
-        for (int q = 0; q < np; ++q)
-            if (act[q] && !std::isfinite(rr[q]))
-                return sv->fail(FALCON_ERR_NAN_DETECTED, "solver: non-finite residual in problem " + std::to_string(q));
-        for (int q = 0; q < np; ++q)
-            if (act[q]) {
-                hmax = std::max(hmax, std::sqrt(rr[q] / bb[q]));
-                if (std::sqrt(rr[q] / bb[q]) > tol) all = false;
+        if (first)
+            for (int q = 0; q < np; ++q) if (!(bb[q] > 0)) bb[q] = 1.0;   // b = 0: absolute residual
+        bool any = false;
+        for (int q = 0; q < np; ++q) {
+            if (state[q] != 0) continue;
+            const double r_q = std::sqrt(rr[q] / bb[q]);
+            if (!std::isfinite(r_q))
+                return sv->fail(FALCON_ERR_NAN_DETECTED, "solver: non-finite FP64 residual in problem " + std::to_string(q));
+            const double floor_q = 4.0 * 8.0 * kEps64 * std::sqrt(ab[q] / bb[q]);
+            rel[q] = r_q;
+            if (r_q <= tol) {
+                state[q] = 1;
+            } else if (r_q <= floor_q || (!first && r_q > 0.5 * prev[q])) {
+                state[q] = 2;
+                rep->floor_residual = std::max(rep->floor_residual, r_q);
+            } else {
+                any = true;
             }
-        hist.push_back(hmax);
-        const size_t nh = hist.size();
-        if (!all && pc == FALCON_PRECOND_MG_LCC && nh > 10 && hist[nh - 1] > 0.95 * hist[nh - 9]) {
-            // stagnation: less than 5% in 8 iterations; plain MG for the rest, restarted
-            pc = FALCON_PRECOND_MG;
-            ++rep->fallbacks;
-            SCK(precondition(0), "precondition");
-            k_update_p_ff<<<g, tpb(d), 0, sv->st>>>(d, sv->p2, sv->z2, sv->D(), 1);
-            SCK(halo_fill_ff(sv, sv->p2), "halo");
-            continue;
+            prev[q] = r_q;
         }
-        if (all) {
-            // verify on the FP64 true residual; restart from it if the recurrence
-            // drifted. A problem whose requested tolerance lies below the FP64
-            // attainable accuracy of b - A x (8 eps (|b| + |A||x|), 4x margin)
-            // stops at that floor, which the report states.
-            SCK(cudaMemsetAsync(sv->dots + 3 * np, 0, (size_t)np * 8, sv->st), "dots");
-            SCK(cudaMemsetAsync(sv->dots + 5 * np, 0, (size_t)np * 8, sv->st), "dots");
-            SCK(halo_fill_ff(sv, sv->x2), "halo");
-            k_residual_ff<<<g, tpb(d), 0, sv->st>>>(sv->lv[0].ops2(), d, sv->x2, sv->b2, sv->r2, sv->lv[0].r, sv->D(), 0);
-            std::vector<double> ab(np);
+        if (!any || it >= max_iter || passes >= kMaxPasses) break;
+        // inner solve of A' d' = r' for the problems still being solved
+        ++passes;
+        for (int q = 0; q < np; ++q) {
+            act[q] = state[q] == 0;
+            int e2 = 0;
+            std::frexp(std::sqrt(rr[q]), &e2);
+            const double sr = act[q] && rr[q] > 0 ? std::ldexp(1.0, e2) : 1.0;
+            inv_sr[q] = 1.0 / sr;
+            fac[q] = sr / sv->sA[q];
+            eta[q] = std::max(0.5 * tol / std::max(rel[q], tol), kEtaMin);
+        }
+        SCK(cudaMemcpyAsync(sv->active, act.data(), np * 4, cudaMemcpyHostToDevice, sv->st), "active");
+        SCK(cudaMemcpyAsync(sv->ir_par, inv_sr.data(), np * 8, cudaMemcpyHostToDevice, sv->st), "scale");
+        SCK(cudaMemcpyAsync(sv->ir_par + np, fac.data(), np * 8, cudaMemcpyHostToDevice, sv->st), "scale");
+        SCK(cudaMemsetAsync(sv->x2, 0, (size_t)nb * d.npad * sizeof(float2), sv->st), "init");
+        SCK(cudaMemsetAsync(sv->p2, 0, (size_t)nb * d.npad * sizeof(float2), sv->st), "init");
+        SCK(cudaMemsetAsync(sv->dots, 0, (size_t)5 * np * 8, sv->st), "dots");
+        k_ir_start<<<g, tpb(d), 0, sv->st>>>(d, sv->r, sv->ir_par, sv->r2, sv->lv[0].r, sv->D());
+        SCK(cudaGetLastError(), "inner start");
+        SCK(cudaMemcpyAsync(rr0.data(), sv->dots + 3 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "rr");
+        SCK(cudaStreamSynchronize(sv->st), "rr");
+        for (int q = 0; q < np; ++q) if (!(rr0[q] > 0)) { rr0[q] = 1.0; act[q] = 0; }
+        std::vector<double> hist;   // max over the inner-active problems of the relative recursive residual
+        SCK(precondition(0), "precondition");
+        k_update_p_ff<<<g, tpb(d), 0, sv->st>>>(d, sv->p2, sv->z2, sv->D(), 1);
+        SCK(halo_fill_ff(sv, sv->p2), "halo");
+        while (it < max_iter) {
+            ++it;
+            SCK(cudaMemsetAsync(sv->dots, 0, (size_t)4 * np * 8, sv->st), "dots");
+            k_spmv_dots_ff<<<g, tpb(d), 0, sv->st>>>(sv->lv[0].ops2(), d, sv->p2, sv->Ap2, sv->r2, sv->D());
+            k_update_xr_ff<<<g, tpb(d), 0, sv->st>>>(d, sv->x2, sv->p2, sv->r2, sv->Ap2, sv->lv[0].r, sv->D());
+            SCK(cudaGetLastError(), "iterate");
             SCK(cudaMemcpyAsync(rr.data(), sv->dots + 3 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "rr");
-            SCK(cudaMemcpyAsync(ab.data(), sv->dots + 5 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "rr");
             SCK(cudaStreamSynchronize(sv->st), "rr");
-            worst = 0;
-            bool ok = true;
+            bool all = true, changed = false;
+            double hmax = 0;
             for (int q = 0; q < np; ++q) {
                 if (!act[q]) continue;
-                const double rel = std::sqrt(rr[q] / bb[q]);
-                if (!std::isfinite(rel))
-                    return sv->fail(FALCON_ERR_NAN_DETECTED, "solver: non-finite true residual in problem " + std::to_string(q));
-                const double floor_q = 4.0 * 8.0 * kEpsFF * std::sqrt(ab[q] / bb[q]);
-                // a true residual within 10x of tol that no longer improves between
-                // two verifications has reached what FP64 attains for this problem
-                const bool stalled = rel < 10.0 * tol && rel > 0.9 * prev_true[q];
-                prev_true[q] = rel;
-                worst = std::max(worst, rel);
-                if (rel <= tol || rel <= floor_q || stalled) {
-                    act[q] = 0;
-                    final_rel[q] = rel;
-                    if (rel > tol) rep->floor_residual = std::max(rep->floor_residual, rel);
-                } else {
-                    ok = false;
-                }
+                if (!std::isfinite(rr[q]))
+                    return sv->fail(FALCON_ERR_NAN_DETECTED, "solver: non-finite residual in problem " + std::to_string(q));
+                const double h = std::sqrt(rr[q] / rr0[q]);
+                hmax = std::max(hmax, h);
+                if (h <= eta[q]) { act[q] = 0; changed = true; } else { all = false; }
             }
-            for (int q = 0; q < np; ++q) if (!act[q]) worst = std::max(worst, final_rel[q]);
-            SCK(cudaMemcpyAsync(sv->active, act.data(), np * 4, cudaMemcpyHostToDevice, sv->st), "active");
-            if (ok) { done = true; break; }
-            ++rep->refinements;
-            SCK(precondition(0), "precondition");
-            k_update_p_ff<<<g, tpb(d), 0, sv->st>>>(d, sv->p2, sv->z2, sv->D(), 1);
+            if (all) break;
+            if (changed) SCK(cudaMemcpyAsync(sv->active, act.data(), np * 4, cudaMemcpyHostToDevice, sv->st), "active");
+            hist.push_back(hmax);
+            const size_t nh = hist.size();
+            if (nh > 10 && hist[nh - 1] > 0.95 * hist[nh - 9]) {
+                // stagnation: less than 5% in 8 iterations
+                if (pc != FALCON_PRECOND_MG_LCC) break;   // the refinement restarts from the FP64 residual
+                pc = FALCON_PRECOND_MG;   // the learned stage stalls: plain MG for the rest, restarted
+                ++rep->fallbacks;
+                hist.clear();
+                SCK(precondition(0), "precondition");
+                k_update_p_ff<<<g, tpb(d), 0, sv->st>>>(d, sv->p2, sv->z2, sv->D(), 1);
+                SCK(halo_fill_ff(sv, sv->p2), "halo");
+                continue;
+            }
+            SCK(precondition(1), "precondition");
+            k_update_p_ff<<<g, tpb(d), 0, sv->st>>>(d, sv->p2, sv->z2, sv->D(), 0);
             SCK(halo_fill_ff(sv, sv->p2), "halo");
-            continue;
         }
-        SCK(precondition(1), "precondition");
-        k_update_p_ff<<<g, tpb(d), 0, sv->st>>>(d, sv->p2, sv->z2, sv->D(), 0);
-        SCK(halo_fill_ff(sv, sv->p2), "halo");
+        // x += d' sr / sA (inactive problems: d' = 0)
+        k_ir_accum<<<g, tpb(d), 0, sv->st>>>(d, sv->x2, sv->ir_par + np, sv->bprob, sv->x);
+        SCK(cudaGetLastError(), "refine");
     }
-    // the solution in FP64, unscaled: x = x' sb / sA
-    k_ff_unscale<<<g, tpb(d), 0, sv->st>>>(d, sv->x2, sv->dunscale, sv->bprob, sv->x);
     cudaEventRecord(t1, sv->st);
     SCK(cudaEventSynchronize(t1), "solve");
     float ms = 0;
     cudaEventElapsedTime(&ms, t0, t1);
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
-    if (!done) {
-        // report the true residual of the last iterate
-        SCK(cudaMemsetAsync(sv->dots + 3 * np, 0, (size_t)np * 8, sv->st), "dots");
-        SCK(halo_fill_ff(sv, sv->x2), "halo");
-        k_residual_ff<<<g, tpb(d), 0, sv->st>>>(sv->lv[0].ops2(), d, sv->x2, sv->b2, sv->r2, sv->lv[0].r, sv->D(), 0);
-        SCK(cudaMemcpyAsync(rr.data(), sv->dots + 3 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "rr");
-        SCK(cudaStreamSynchronize(sv->st), "rr");
-        worst = 0;
-        for (int q = 0; q < np; ++q) {
-            const double rel = std::sqrt(rr[q] / bb[q]);
-            if (!(rel <= worst)) worst = rel;   // NaN propagates
-        }
+    double worst = 0;
+    bool done = true;
+    for (int q = 0; q < np; ++q) {
+        worst = std::max(worst, rel[q]);
+        if (state[q] != 1) done = false;
     }
-    rep->iterations = std::min(it, max_iter);
+    rep->iterations = it;
+    rep->refinements = std::max(0, passes - 1);
     rep->converged = done ? 1 : 0;
     rep->rel_residual = worst;
     rep->ms = ms;
-    if (!done) { sv->err = "not converged within max_iter"; return FALCON_ERR_NOT_CONVERGED; }
+    if (!done) {
+        char buf[256];
+        snprintf(buf, sizeof buf,
+                 "not converged: FP64 relative residual %.3e above tol %.3e (%d inner iterations, %d refinement passes%s)",
+                 worst, tol, it, passes, rep->floor_residual > 0 ? "; stopped at the FP64 attainable accuracy" : "");
+        sv->err = buf;
+        return FALCON_ERR_NOT_CONVERGED;
+    }
     return FALCON_OK;
 }
 
@@ -1664,9 +1766,8 @@ int falcon_solver_set_rhs(falcon_solver* sv, const double* b) {
     std::memcpy(sv->S.b.data(), b, sv->S.b.size() * 8);
     if (sv->st) {
         cudaSetDevice(sv->device);
+        SCK(cudaStreamSynchronize(sv->st), "rhs");
         SCK(cudaMemcpy(sv->bvec, b, sv->S.b.size() * 8, cudaMemcpyHostToDevice), "rhs");
-        const int rc = upload_rhs_ff(sv);
-        if (rc) return rc;
     }
     return FALCON_OK;
 }

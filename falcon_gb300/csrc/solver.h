@@ -46,6 +46,7 @@ struct SolverProblemSet {
     std::vector<SolverLevel> L;            // [level]
     std::vector<double> b;                 // right-hand side, level 0, [b][nint]
     std::vector<double> x0;                // initial guess, level 0
+    std::vector<double> br;                // PFSS: Br at the bottom faces [b][k][j] (0 off the bottom blocks)
     std::vector<Grid> grids;               // one tree per problem
     std::string err;
 };
@@ -75,6 +76,9 @@ std::string build_solver_levels(SolverProblemSet& S, const std::vector<falcon_co
 // Br at the bottom faces of bottom blocks: br[b][k][j] per level-0 block (only
 // bottom blocks read).
 void assemble_pfss(SolverProblemSet& S, const std::vector<double>& br_bottom);
+// Only the PFSS right-hand side from a bottom-face Br (the operator does not
+// depend on it): S.b and S.br.
+void pfss_rhs(SolverProblemSet& S, const std::vector<double>& br_bottom);
 
 // Coarse operators A_c = P^T A P for levels 1.. from level 0 (P: injection).
 void galerkin_coarsen(SolverProblemSet& S);

@@ -220,11 +220,17 @@ void assemble_pfss(SolverProblemSet& S, const std::vector<double>& br_bottom) {
                     }
         }
     }
-    // right-hand side: b(1,:,:) = Br * Si(1,:,:) on bottom blocks (level 1)
+    pfss_rhs(S, br_bottom);
+    S.x0.assign(S.b.size(), 0.0);
+}
+
+// right-hand side: b(1,:,:) = Br * Si(1,:,:) on bottom blocks, 0 elsewhere
+// (3_5/ModPFSS.f90:45-48, level 1); keeps Br in S.br
+void pfss_rhs(SolverProblemSet& S, const std::vector<double>& br_bottom) {
     SolverLevel& L = S.L[0];
     const int mi = L.m[0], mj = L.m[1], mk = L.m[2];
+    S.br.assign((size_t)S.nblocks * mk * mj, 0.0);
     S.b.assign((size_t)S.nblocks * mi * mj * mk, 0.0);
-    S.x0.assign(S.b.size(), 0.0);
     for (int gb = 0; gb < S.nblocks; ++gb) {
         if (!(S.block_flags[gb] & 4)) continue;
         const int p = S.block_problem[gb];
@@ -235,9 +241,11 @@ void assemble_pfss(SolverProblemSet& S, const std::vector<double>& br_bottom) {
         LevelGeometry G;
         G.init(rng, L.m);
         for (int k = 1; k <= mk; ++k)
-            for (int j = 1; j <= mj; ++j)
-                S.b[(size_t)gb * mi * mj * mk + ((size_t)(k - 1) * mj + (j - 1)) * mi] =
-                    br_bottom[((size_t)gb * mk + (k - 1)) * mj + (j - 1)] * G.Si(1, j, k);
+            for (int j = 1; j <= mj; ++j) {
+                const size_t f = ((size_t)gb * mk + (k - 1)) * mj + (j - 1);
+                S.br[f] = br_bottom[f];
+                S.b[(size_t)gb * mi * mj * mk + ((size_t)(k - 1) * mj + (j - 1)) * mi] = br_bottom[f] * G.Si(1, j, k);
+            }
     }
 }
 

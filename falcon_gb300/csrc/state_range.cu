@@ -32,7 +32,11 @@ double* g_scratch_ptr[kMaxDevices] = {};
 
 // The array's device address on device `dev`, which must be current. Resolved
 // once per device (the first call may also load the library's device code on
-// that device) and cached.
+// that device) and cached for the life of the process: the cache assumes that
+// the device's primary context (which every context of this library uses)
+// lives as long as the process. After a cudaDeviceReset, or another reset of
+// the primary context in the same process, the cached address is stale; do not
+// call this entry point after one.
 cudaError_t scratch_on_device(int dev, double** out) {
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(g_scratch_mu);

@@ -39,7 +39,8 @@ _SYMS = ("falcon_solver_create", "falcon_solver_last_error", "falcon_solver_info
          "falcon_solver_rhs", "falcon_solver_operator", "falcon_solver_halo_count", "falcon_solver_halo_map",
          "falcon_solver_apply", "falcon_solver_solve", "falcon_solver_solution", "falcon_solver_timestep",
          "falcon_solver_set_rhs", "falcon_solver_coarse_shape", "falcon_solver_attach_lcc", "falcon_solver_record",
-         "falcon_solver_set_smoothing", "falcon_solver_problem_residuals")
+         "falcon_solver_set_smoothing", "falcon_solver_problem_residuals", "falcon_solver_set_operator",
+         "falcon_solver_set_magnetogram", "falcon_solver_magnetogram", "falcon_solver_set_guess")
 
 
 def _ptr(a):
@@ -170,6 +171,34 @@ class Solver:
         b = np.ascontiguousarray(b, dtype=np.float64)
         assert b.size == self.nblocks * self.nint
         self._ck(self.L.falcon_solver_set_rhs(self.h, _ptr(b)))
+
+    def set_operator(self, Aii, Ai, Aj, Ak):
+        """The driver's level-0 face coefficients (the layout of operator(0))."""
+        ref = self.operator(0)
+        arrs = []
+        for a, r in zip((Aii, Ai, Aj, Ak), ref):
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            if a.shape != r.shape:
+                raise ValueError("operator array shape %s != %s" % (a.shape, r.shape))
+            arrs.append(a)
+        self._ck(self.L.falcon_solver_set_operator(self.h, *(_ptr(a) for a in arrs)))
+
+    def magnetogram(self):
+        """PFSS: Br at the bottom faces, [block][k][j] (0 off the bottom blocks)."""
+        out = np.zeros((self.nblocks, self.m[2], self.m[1]))
+        self._ck(self.L.falcon_solver_magnetogram(self.h, _ptr(out)))
+        return out
+
+    def set_magnetogram(self, br):
+        br = np.ascontiguousarray(br, dtype=np.float64)
+        if br.shape != (self.nblocks, self.m[2], self.m[1]):
+            raise ValueError("magnetogram shape %s" % (br.shape,))
+        self._ck(self.L.falcon_solver_set_magnetogram(self.h, _ptr(br)))
+
+    def set_guess(self, x0):
+        x0 = np.ascontiguousarray(x0, dtype=np.float64)
+        assert x0.size == self.nblocks * self.nint
+        self._ck(self.L.falcon_solver_set_guess(self.h, _ptr(x0)))
 
     def coarse_shape(self):
         s = (C.c_int32 * 4)()

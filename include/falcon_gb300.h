@@ -33,6 +33,8 @@
  *                             (3_6/ModWaveSpeed.f90:8-27, 3_6/ModTimeStep.f90:10-30,
  *                             3_6/ModAdvance.f90:31-48)
  *   falcon_step_rk4 ......... ModAdvance_rk4 (3_6/ModAdvance.f90:18-112)
+ *   falcon_set_background ... ModBlock_InitSSM's profiles from ModStratification_new_get_vars
+ *                             (3_6/ModBlock.f90:233-264)
  */
 #ifndef FALCON_GB300_H
 #define FALCON_GB300_H
@@ -61,8 +63,13 @@ extern "C" {
  * MIXED: state stored in FP32, u^n with an 8-bit correction of its FP32
  *       rounding that the end-of-step updates carry (error-free FP32 sums);
  *       stencil RHS and stage updates in FP32; the linearised-EOS pressure p1
- *       (where the background terms cancel) is assembled in FP64; the CFL
- *       ratio, its min-reduction and dt are FP64. */
+ *       (where the background terms nearly cancel) is assembled in float-float
+ *       (exact FP32 products with the coefficients' (hi, lo) FP32 pairs and an
+ *       error-free sum, about as accurate as an FP64 assembly, with no FP64
+ *       instruction per cell); the per-cell CFL ratio h/v_wave is formed in
+ *       explicitly rounded FP32, each block's minimum is widened to FP64 for
+ *       the cross-block min-reduction (an atomic on FP64 bits), and dt =
+ *       CFL * min is FP64. */
 #define FALCON_PREC_FP64   0
 #define FALCON_PREC_MIXED  1
 
@@ -150,6 +157,18 @@ int  falcon_block_flags(const falcon_ctx* ctx, int32_t* flags);
  * cooling, Xi -- the outputs of ModStratification_new_get_vars at the cell
  * centres (3_6/ModBlock.f90:232-249) */
 int  falcon_get_background(const falcon_ctx* ctx, double* prof);
+/* Replace the background with the driver's own radial profiles, same layout
+ * as falcon_get_background: prof[b][FALCON_NPROF][ni+2ng] = g, rho0, p0, T0,
+ * gamma1, gamma3, diffusion, cooling, Xi at every block's cell centres (ghost
+ * layers included) -- what ModBlock_InitSSM stores from
+ * ModStratification_new_get_vars (3_6/ModBlock.f90:233-264,
+ * 3_6/ModStratification_new.f90:352-384), e.g. from the FreeEOS/opacity
+ * tables this library does not read. The device tables of every step kernel
+ * are rebuilt from them (the GPU keeps 1-D profiles only). Rejected with
+ * FALCON_ERR_INVALID_ARG, background unchanged, unless every value is finite
+ * and rho0, p0, T0, gamma1 and Xi are positive. The next step re-forms the
+ * CFL minimum. Valid on host-only contexts too (device < 0). */
+int  falcon_set_background(falcon_ctx* ctx, const double* prof);
 int  falcon_ghost_count(const falcon_ctx* ctx, int64_t* n);
 /* entries in the reference's order: target block ascending, then its
  * GC_targets (first-appearance order of source leaves), then i-j-k loop order */
@@ -180,7 +199,10 @@ int  falcon_download_state(falcon_ctx* ctx, double* u);
  *
  * The first call on each device sets up the array's address
  * (cudaGetSymbolAddress; it may load the library's device code): make that
- * first call before any stream capture on the device. Every context on a
+ * first call before any stream capture on the device. The address is cached
+ * per device for the life of the process, which assumes that the device's
+ * primary context is never reset (no cudaDeviceReset) while the library is
+ * in use. Every context on a
  * device shares the one array, which keeps the last call's data; each call
  * synchronises the context stream before returning, but calls that overlap on
  * the GPU (from several host threads) race on the array: serialise them. */
@@ -244,6 +266,18 @@ int  falcon_step_rk4(falcon_ctx* ctx, double* dt_out);
 /* nsteps back-to-back steps, captured as CUDA graphs after the first call. */
 int  falcon_run_steps(falcon_ctx* ctx, int32_t nsteps);
 int  falcon_synchronize(falcon_ctx* ctx);
+/* Poll limit of the step kernels' bounded waits (no counterpart in the
+ * reference, whose MPI calls block without a limit). Each stage and diffusion
+ * CTA streams its block's planes into shared memory with bulk copies and
+ * waits on an mbarrier for each chunk, polling it at most `polls` times
+ * (default 4,194,304; each poll may suspend briefly; 0 gives up at once).
+ * A wait that runs out ends the CTA cleanly -- uniformly over its threads,
+ * after the copies in flight have landed -- and the step returns
+ * FALCON_ERR_TIMEOUT (from falcon_step_rk4 with dt_out, falcon_synchronize
+ * or falcon_timestep); the state is then undefined until the next
+ * falcon_upload_state, falcon_init_synthetic or falcon_load_restart, which
+ * clear the flag. polls < 0 restores the default. */
+int  falcon_set_wait_limit(falcon_ctx* ctx, int32_t polls);
 /* Verification: run one phase of ModAdvance_rk4 eagerly and synchronously.
  * phase 0: wave speed + CFL dt (3_6/ModAdvance.f90:31-48); 1..4: RK stage s
  * with its ghost exchange (:59-97); 5: artificial diffusion + exchange
@@ -310,15 +344,25 @@ typedef struct falcon_solver_spec {
     int32_t  np[FALCON_MAX_PROBLEMS];
 } falcon_solver_spec;
 
+/* A solve is an FP64 iterative refinement: r = b - A x and its norms in FP64,
+ * an inner flexible-CG solve (float-float vectors, FP32 V-cycle) of the
+ * correction equation A d = r, x += d in FP64; a problem is converged only
+ * when its FP64 ||b - A x|| / ||b|| <= tol. falcon_solver_solve returns
+ * FALCON_OK only when every problem converged, FALCON_ERR_NOT_CONVERGED
+ * otherwise (the report is filled either way). */
 typedef struct falcon_solve_report {
-    int32_t iterations, converged, vcycles, refinements;
-    double  rel_residual;              /* max over problems of the FP64 ||b-Ax||/||b|| */
+    int32_t iterations;                /* inner iterations, all refinement passes */
+    int32_t converged;                 /* 1: every problem's FP64 relative residual <= tol */
+    int32_t vcycles;
+    int32_t refinements;               /* refinement passes after the first */
+    double  rel_residual;              /* max over problems of the FP64 ||b-Ax||/||b|| at exit */
     double  ms;                        /* device time of the solve */
     int32_t fallbacks;                 /* FALCON_PRECOND_MG_LCC: switches to plain MG */
     int32_t pad_;
-    /* > 0 when a problem stopped above tol at the accuracy FP64 attains for
-     * it: below 4 x 8 eps (|b| + |A||x|) / ||b||, or within 10 x tol and no
-     * longer improving between two true-residual checks (the largest such) */
+    /* > 0 when a problem stopped above tol because FP64 cannot take it lower:
+     * its residual is at the attainable accuracy of b - A x, 4 x 8 eps64
+     * (|b| + |A||x|) / ||b||, or a refinement pass no longer halved it (the
+     * largest such residual; converged is then 0) */
     double  floor_residual;
 } falcon_solve_report;
 
@@ -357,6 +401,31 @@ int  falcon_solver_set_smoothing(falcon_solver* sv, int32_t nu_pre, int32_t nu_p
 int  falcon_solver_problem_residuals(falcon_solver* sv, double* rel);
 /* replace the level-0 right-hand side [block][k][j][i] */
 int  falcon_solver_set_rhs(falcon_solver* sv, const double* b);
+/* ---- the driver's own data (a solver created from a spec is then only the
+ * grid: its seeded synthetic operator or magnetogram is replaced) ---- */
+/* Replace the level-0 operator with the driver's face coefficients, the
+ * layout of falcon_solver_operator (Aii[b][k][j][i], Ai[b][k][j][m_i+1],
+ * Aj[b][k][m_j+1][i], Ak[b][m_k+1][j][i]; 3_5/ModBlock.f90:39-44), e.g. the
+ * backward-Euler conduction operator a driver assembled from its own T and B
+ * (ModHeatConduction, 3_6/ModHeatConduction.f90, is empty in the reference).
+ * The coarse levels are rebuilt (Galerkin) and every device copy refreshed.
+ * Rejected, operator unchanged, unless every coefficient is finite and every
+ * Aii positive. */
+int  falcon_solver_set_operator(falcon_solver* sv, const double* Aii, const double* Ai, const double* Aj,
+                                const double* Ak);
+/* PFSS: the lower-boundary radial field Br at the bottom faces of the level-0
+ * bottom blocks, br[b][k][j] (m_k x m_j per block; entries of other blocks
+ * are ignored) -- the driver's magnetogram in place of the synthetic one
+ * (ModPFSS_setup's Block%magnetogram_LL, 3_5/ModPFSS.f90:21-100, filled by
+ * ModMagnetogram, 3_5/ModMagnetogram.f90:13-80). The right-hand side becomes
+ * b(1,:,:) = Br * S_i(1,:,:) (3_5/ModPFSS.f90:45-48). Rejected, unchanged,
+ * if any value is not finite or the solver is not a PFSS solver. */
+int  falcon_solver_set_magnetogram(falcon_solver* sv, const double* br);
+/* the current PFSS magnetogram in the same layout (0 off the bottom blocks) */
+int  falcon_solver_magnetogram(const falcon_solver* sv, double* br);
+/* initial guess x0 of the next solves, level 0 [block][k][j][i] (PFSS
+ * default 0; conduction default the current temperature) */
+int  falcon_solver_set_guess(falcon_solver* sv, const double* x0);
 /* Learned coarse correction (single-problem solvers of whole uniform blocks):
  * the coarsest level gathered into one dense grid per Yin-Yang panel,
  * shape4 = {2, D, H, W} (D radial, H theta, W phi cells; multiples of 8). */

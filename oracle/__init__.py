@@ -38,7 +38,8 @@ def lib():
         for name in ("orc_num_blocks", "orc_block_ranges", "orc_block_flags", "orc_get_background",
                      "orc_ghost_map", "orc_set_state", "orc_get_state", "orc_exchange",
                      "orc_timestep", "orc_step", "orc_block_rhs", "orc_block_diffusion",
-                     "orc_block_grid", "orc_phase", "orc_get_stage_state", "orc_save_allcells"):
+                     "orc_block_grid", "orc_phase", "orc_get_stage_state", "orc_save_allcells",
+                     "orc_set_background"):
             getattr(L, name).restype = C.c_int
         L.orc_ghost_count.restype = C.c_int64
         L.orc_ghost_count.argtypes = [vp]
@@ -95,6 +96,12 @@ class Oracle:
         out = np.zeros((self.nblocks, 9, t.ni + 2 * t.ng))
         self.L.orc_get_background(self.hp, _ptr(out))
         return out
+
+    def set_background(self, prof):
+        """The driver's own radial profiles [b][9][ni+2ng] in place of the polytrope's."""
+        prof = np.ascontiguousarray(prof, dtype=np.float64)
+        assert prof.shape == self.background().shape
+        self.L.orc_set_background(self.hp, _ptr(prof))
 
     def ghost_count(self):
         return int(self.L.orc_ghost_count(self.hp))

@@ -307,6 +307,7 @@ struct Oracle {
     void build();
     void init_grid(Block& b);
     void init_ssm(Block& b);
+    void derive_ssm(Block& b);
     void find_gc(Block& b);
     void gc_targets(Block& b);
     void gc_sources();
@@ -408,6 +409,11 @@ void Oracle::init_ssm(Block& b) {
         bg.get_vars(b.xi[i], o);
         for (int p = 0; p < NPROF; ++p) b.prof[(size_t)p * nip + i] = o[p];
     }
+    derive_ssm(b);
+}
+
+// the block's background arrays from its 1-D profiles (3_6/ModBlock.f90:233-264)
+void Oracle::derive_ssm(Block& b) {
     auto P = [&](int p, int i) { return b.prof[(size_t)p * nip + i]; };
     b.gamma1.resize(nip); b.g3m1.resize(nip); b.rho0.resize(nip); b.g_over_rho0.resize(nip);
     b.p0_over_rho0.resize(nip); b.rho0T0.resize(nip); b.heat.resize(nip); b.Xi.resize(nip);
@@ -1177,6 +1183,16 @@ int orc_get_background(void* h, double* out) {
     Oracle* o = (Oracle*)h;
     size_t n = (size_t)FALCON_NPROF * o->nip;
     for (size_t b = 0; b < o->blk.size(); ++b) std::memcpy(out + n * b, o->blk[b].prof.data(), n * sizeof(double));
+    return 0;
+}
+// the driver's own profiles [b][NPROF][nip] in place of the polytrope's
+int orc_set_background(void* h, const double* in) {
+    Oracle* o = (Oracle*)h;
+    size_t n = (size_t)FALCON_NPROF * o->nip;
+    for (size_t b = 0; b < o->blk.size(); ++b) {
+        std::memcpy(o->blk[b].prof.data(), in + n * b, n * sizeof(double));
+        o->derive_ssm(o->blk[b]);
+    }
     return 0;
 }
 int64_t orc_ghost_count(void* h) {

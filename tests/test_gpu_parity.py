@@ -199,6 +199,34 @@ def test_full_size_mixed_properties():
     assert np.array_equal(u1, u2)
 
 
+def test_mixed_vs_fp64_full_size_100_steps():
+    """The headline workload's accuracy on the headline workload itself: the
+    21,233,664-cell shell (5,184 blocks of 16^3) from the seeded random-phase
+    Kolmogorov velocity (rms Mach 0.01, seed 1002), 100 RK4 steps in MIXED
+    and in FP64 on the GPU (each with its own dt sequence). Gate per evolved
+    variable over the interior cells: relative L2 <= 1e-6 and norm-wise max
+    <= 1e-5."""
+    from falcon_gb300.compare import state_errors, worst
+    ctxs = []
+    for prec in (config.PREC_FP64, config.PREC_MIXED):
+        f = fg.Falcon(config.shell_mixed_21m(precision=prec))
+        f.init_synthetic(kind=1, seed=1002, mach=0.01)
+        f.exchange()
+        f.exchange()
+        f.run_steps(100)
+        f.synchronize()
+        ctxs.append(f)
+    u64 = ctxs[0].download_state()
+    ctxs[0].close()
+    umx = ctxs[1].download_state()
+    ctxs[1].close()
+    e = state_errors(umx, u64)
+    print("21M-cell mixed vs fp64 after 100 steps:", e)
+    assert np.isfinite(umx).all()
+    assert worst(e, "rel_l2") <= TOL_MIXED, e
+    assert worst(e, "rel_max") <= 10 * TOL_MIXED, e
+
+
 def test_fp64_full_size_block16_vs_oracle_one_step():
     """16^3 blocks in FP64: one step against the oracle on a reduced shell
     (per panel 32 x 48 x 144 cells, 2 x 3 x 9 blocks)."""
@@ -236,6 +264,37 @@ def test_nan_formed_in_a_mixed_step_is_reported_by_the_next():
         for _ in range(4):
             f.advance_rk4()
     assert e.value.code == fg.ERR_NAN_DETECTED
+
+
+@pytest.mark.parametrize("prec", [config.PREC_FP64, config.PREC_MIXED])
+def test_copy_wait_that_runs_out_returns_timeout(prec):
+    """The step kernels' waits for their bulk copies are bounded. With the
+    poll limit at 0 every wait runs out on a valid state: each CTA leaves
+    uniformly after its copies in flight have landed, the step returns
+    FALCON_ERR_TIMEOUT (not a hang, not a fault, not 'NaN detected'), and the
+    context stays usable: with the default limit restored and the state
+    uploaded again, the next step equals a fresh context's bit for bit."""
+    mk = lambda: config.make_config(block=(16, 16, 16), root_tiles=(1, 3, 9), radial_levels=1, amr=(),
+                                    precision=prec)
+    f, ref = fg.Falcon(mk()), fg.Falcon(mk())
+    u0 = synth.initial_state(mk(), f.block_ranges(), f.block_flags(), seed=1013)
+    for x in (f, ref):
+        x.upload_state(u0)
+        x.exchange()
+    f.advance_rk4()            # the autotuner runs before the first step: keep it out of the test
+    f.upload_state(u0)
+    f.exchange()
+    f.set_wait_limit(0)
+    with pytest.raises(fg.FalconError) as e:
+        f.advance_rk4()
+    assert e.value.code == fg.ERR_TIMEOUT, e.value
+    assert "wait ran out" in str(e.value)
+    f.set_wait_limit(-1)
+    f.upload_state(u0)
+    f.exchange()
+    dt_f, dt_r = f.advance_rk4(), ref.advance_rk4()
+    assert dt_f == dt_r
+    assert np.array_equal(f.download_state(), ref.download_state())
 
 
 # ---- div-B control: GLM cleaning (divb_option 1, psi evolved) and the ----

@@ -8,6 +8,8 @@ downloads in a row (checking that neither depends on what the previous call
 left there), and one more after the state has changed.
 """
 import ctypes as C
+import glob
+import os
 
 import numpy as np
 import pytest
@@ -23,6 +25,25 @@ MAX_ELEMS = fg.STATIC_SCRATCH_BYTES // 8
 @pytest.fixture(scope="module", autouse=True)
 def _built(built_lib):
     return built_lib
+
+
+def _cudart():
+    """The CUDA runtime as a shared library, for an independent reading of the
+    device's free memory (the library under test links its own runtime)."""
+    root = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    for p in sorted(glob.glob(os.path.join(root, "lib64", "libcudart.so*")) +
+                    glob.glob(os.path.join(root, "targets", "*", "lib", "libcudart.so*"))):
+        try:
+            return C.CDLL(p)
+        except OSError:
+            continue
+    return None
+
+
+def _free_bytes(rt):
+    free, total = C.c_size_t(), C.c_size_t()
+    assert rt.cudaMemGetInfo(C.byref(free), C.byref(total)) == 0
+    return free.value
 
 
 def _range_call(f, first, count, out):
@@ -51,8 +72,15 @@ def test_range_download_matches_download_state(prec):
     f.exchange()
     before = f.device_bytes()
     a = _download_by_ranges(f, MAX_ELEMS)
+    # free device memory read through the CUDA runtime after the first calls
+    # (which may load the library's device code): a cudaMalloc on any path of
+    # the range call, the context's allocator or not, would lower it
+    rt = _cudart()
+    free0 = _free_bytes(rt) if rt is not None else None
     b = _download_by_ranges(f, 1_000_003)          # ragged ranges, second call in a row
     assert f.device_bytes() == before              # the range call allocated nothing
+    if rt is not None:
+        assert _free_bytes(rt) == free0
     ref = f.download_state()
     assert np.array_equal(a, ref)
     assert np.array_equal(b, ref)
