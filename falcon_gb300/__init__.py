@@ -54,7 +54,8 @@ EXPORTS = (
     "falcon_lcc_train", "falcon_save_allcells", "falcon_save_restart", "falcon_load_restart",
     "falcon_upload_state_core", "falcon_download_state_core", "falcon_set_wait_limit",
     "falcon_set_background", "falcon_solver_set_operator", "falcon_solver_set_magnetogram",
-    "falcon_solver_magnetogram", "falcon_solver_set_guess",
+    "falcon_solver_magnetogram", "falcon_solver_set_guess", "falcon_solver_block_ranges",
+    "falcon_solver_block_flags", "falcon_solver_magnetogram_sources", "falcon_solver_vcycle_op",
 )
 
 # size of the static device array behind falcon_download_state_range

@@ -730,6 +730,8 @@ struct falcon_solver {
     std::vector<void*> allocs;
     int nu_pre = 2, nu_post = 2, nu_coarse = 16;
     double dt_conduction = 0;
+    uint64_t seed = 0;                    // the spec's seed (problem q: seed + q)
+    double r_surface = 0;                 // PFSS: lower boundary radius (cm) of the synthetic magnetogram
     // learned coarse correction
     falcon_lcc* net = nullptr;
     int net_sweeps = 2;
@@ -1353,6 +1355,95 @@ int falcon_solver_magnetogram(const falcon_solver* sv, double* br) {
     return FALCON_OK;
 }
 
+int falcon_solver_vcycle_op(falcon_solver* sv, int32_t op, int32_t level, const float* in0, const float* in1,
+                            float* out) {
+    if (!sv || !in0 || !out) return FALCON_ERR_INVALID_ARG;
+    if (!sv->st) return sv->fail(FALCON_ERR_NO_DEVICE, "solver created without a device");
+    const int nl = sv->S.nlevels, nb = sv->S.nblocks;
+    const bool needs_coarse = op == FALCON_VCYCLE_RESTRICT || op == FALCON_VCYCLE_PROLONG_ADD;
+    if (op < FALCON_VCYCLE_RESTRICT || op > FALCON_VCYCLE_RESIDUAL || level < 0 || level >= nl ||
+        (needs_coarse && level + 1 >= nl) || (op != FALCON_VCYCLE_RESTRICT && !in1))
+        return sv->fail(FALCON_ERR_INVALID_ARG, "falcon_solver_vcycle_op: bad operation, level or input");
+    cudaSetDevice(sv->device);
+    SvLevel& L = sv->lv[level];
+    const size_t nf = (size_t)nb * L.d.nint;
+    const dim3 gf = grid_cells(L.d, nb);
+    SCK(cudaStreamSynchronize(sv->st), "vcycle op");
+    if (op == FALCON_VCYCLE_RESTRICT) {
+        SvLevel& Cl = sv->lv[level + 1];
+        SCK(cudaMemcpyAsync(L.res, in0, nf * 4, cudaMemcpyHostToDevice, sv->st), "vcycle op");
+        k_restrict<<<grid_cells(Cl.d, nb), tpb(Cl.d), 0, sv->st>>>(L.d, Cl.d, L.res, Cl.r);
+        SCK(cudaGetLastError(), "vcycle op");
+        SCK(cudaMemcpyAsync(out, Cl.r, (size_t)nb * Cl.d.nint * 4, cudaMemcpyDeviceToHost, sv->st), "vcycle op");
+    } else if (op == FALCON_VCYCLE_PROLONG_ADD) {
+        SvLevel& Cl = sv->lv[level + 1];
+        const size_t nc = (size_t)nb * Cl.d.nint;
+        SCK(cudaMemsetAsync(Cl.z, 0, (size_t)nb * Cl.d.npad * 4, sv->st), "vcycle op");
+        SCK(cudaMemsetAsync(L.z, 0, (size_t)nb * L.d.npad * 4, sv->st), "vcycle op");
+        SCK(cudaMemcpyAsync(Cl.r, in0, nc * 4, cudaMemcpyHostToDevice, sv->st), "vcycle op");
+        SCK(cudaMemcpyAsync(L.res, in1, nf * 4, cudaMemcpyHostToDevice, sv->st), "vcycle op");
+        k_scatter_pad<float><<<grid_cells(Cl.d, nb), tpb(Cl.d), 0, sv->st>>>(Cl.d, Cl.r, Cl.z);
+        k_scatter_pad<float><<<gf, tpb(L.d), 0, sv->st>>>(L.d, L.res, L.z);
+        k_prolong_add<<<gf, tpb(L.d), 0, sv->st>>>(L.d, Cl.d, Cl.z, L.z);
+        k_gather_pad<float><<<gf, tpb(L.d), 0, sv->st>>>(L.d, L.z, L.res);
+        SCK(cudaGetLastError(), "vcycle op");
+        SCK(cudaMemcpyAsync(out, L.res, nf * 4, cudaMemcpyDeviceToHost, sv->st), "vcycle op");
+    } else {
+        // z (interior) into the padded z, its halo filled, then one red-black
+        // half sweep of a colour or the residual r - A z
+        SCK(cudaMemsetAsync(L.z, 0, (size_t)nb * L.d.npad * 4, sv->st), "vcycle op");
+        SCK(cudaMemcpyAsync(L.r, in0, nf * 4, cudaMemcpyHostToDevice, sv->st), "vcycle op");
+        SCK(cudaMemcpyAsync(L.res, in1, nf * 4, cudaMemcpyHostToDevice, sv->st), "vcycle op");
+        k_scatter_pad<float><<<gf, tpb(L.d), 0, sv->st>>>(L.d, L.res, L.z);
+        SCK(halo_fill<float>(sv, level, L.z), "vcycle op");
+        if (op == FALCON_VCYCLE_RESIDUAL) {
+            k_resid32<<<gf, tpb(L.d), 0, sv->st>>>(L.ops32(), L.d, L.r, L.z, L.res);
+        } else {
+            k_rbgs<<<gf, tpb(L.d), 0, sv->st>>>(L.ops32(), L.d, L.r, L.z, op == FALCON_VCYCLE_SMOOTH_RED ? 0 : 1);
+            k_gather_pad<float><<<gf, tpb(L.d), 0, sv->st>>>(L.d, L.z, L.res);
+        }
+        SCK(cudaGetLastError(), "vcycle op");
+        SCK(cudaMemcpyAsync(out, L.res, nf * 4, cudaMemcpyDeviceToHost, sv->st), "vcycle op");
+    }
+    SCK(cudaStreamSynchronize(sv->st), "vcycle op");
+    return FALCON_OK;
+}
+
+int falcon_solver_block_ranges(const falcon_solver* sv, double* ranges) {
+    if (!sv || !ranges) return FALCON_ERR_INVALID_ARG;
+    const SolverProblemSet& S = sv->S;
+    for (int gb = 0; gb < S.nblocks; ++gb) {
+        const int p = S.block_problem[gb];
+        const int b = gb - S.problem_first_block[p];
+        std::memcpy(ranges + (size_t)gb * 6, &S.grids[p].ranges[(size_t)b * 6], 6 * sizeof(double));
+    }
+    return FALCON_OK;
+}
+
+int falcon_solver_block_flags(const falcon_solver* sv, int32_t* flags) {
+    if (!sv || !flags) return FALCON_ERR_INVALID_ARG;
+    std::memcpy(flags, sv->S.block_flags.data(), sv->S.block_flags.size() * sizeof(int32_t));
+    return FALCON_OK;
+}
+
+int falcon_solver_magnetogram_sources(const falcon_solver* sv, int32_t problem, double* xyzq, int32_t cap,
+                                      int32_t* n) {
+    if (!sv || !n || problem < 0 || problem >= sv->S.nproblems) return FALCON_ERR_INVALID_ARG;
+    if (sv->S.br.empty()) return FALCON_ERR_INVALID_ARG;
+    Magnetogram M;
+    M.init(sv->seed + (uint64_t)problem, sv->r_surface);
+    *n = (int32_t)M.q.size();
+    if (!xyzq) return FALCON_OK;
+    if (cap < *n) return FALCON_ERR_BOUNDS;
+    for (size_t c = 0; c < M.q.size(); ++c) {
+        xyzq[4 * c] = M.px[c];
+        xyzq[4 * c + 1] = M.py[c];
+        xyzq[4 * c + 2] = M.pz[c];
+        xyzq[4 * c + 3] = M.q[c];
+    }
+    return FALCON_OK;
+}
+
 int falcon_solver_set_guess(falcon_solver* sv, const double* x0) {
     if (!sv || !x0) return FALCON_ERR_INVALID_ARG;
     if (!all_finite(x0, sv->S.x0.size())) return sv->fail(FALCON_ERR_INVALID_ARG, "falcon_solver_set_guess: non-finite value");
@@ -1367,6 +1458,7 @@ int falcon_solver_create(falcon_solver** out, const falcon_solver_spec* spec) {
     if (spec->nproblems < 1 || spec->nproblems > FALCON_MAX_PROBLEMS) return sv->fail(FALCON_ERR_INVALID_ARG, "nproblems out of range");
     if (spec->block < 2 || spec->block > 32 || (spec->block & 1)) return sv->fail(FALCON_ERR_INVALID_ARG, "block must be even, 2..32");
     sv->device = spec->device;
+    sv->seed = spec->seed;
     if (spec->kind == FALCON_SOLVER_CONDUCTION) {
         sv->nu_coarse = 4;
     } else {   // PFSS: one sweep each way, 32 on the coarsest level (measured fastest to 1e-10)
@@ -1412,7 +1504,8 @@ int falcon_solver_create(falcon_solver** out, const falcon_solver_spec* spec) {
         std::vector<double> br((size_t)S.nblocks * mj * mk, 0.0);
         for (int q = 0; q < S.nproblems; ++q) {
             Magnetogram M;
-            M.init(spec->seed + (uint64_t)q, spec->r_range_rsun[0] * kRsun);
+            sv->r_surface = spec->r_range_rsun[0] * kRsun;
+            M.init(spec->seed + (uint64_t)q, sv->r_surface);
             for (int gb = S.problem_first_block[q]; gb < S.problem_first_block[q + 1]; ++gb) {
                 if (!(S.block_flags[gb] & 4)) continue;
                 const bool yin = S.block_flags[gb] & 1;

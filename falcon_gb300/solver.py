@@ -18,6 +18,7 @@ CONDUCTION = 1
 PRECOND_NONE = 0
 PRECOND_MG = 1
 PRECOND_MG_LCC = 2
+VCYCLE_RESTRICT, VCYCLE_PROLONG_ADD, VCYCLE_SMOOTH_RED, VCYCLE_SMOOTH_BLACK, VCYCLE_RESIDUAL = range(5)
 
 
 class SolverSpec(C.Structure):
@@ -40,7 +41,9 @@ _SYMS = ("falcon_solver_create", "falcon_solver_last_error", "falcon_solver_info
          "falcon_solver_apply", "falcon_solver_solve", "falcon_solver_solution", "falcon_solver_timestep",
          "falcon_solver_set_rhs", "falcon_solver_coarse_shape", "falcon_solver_attach_lcc", "falcon_solver_record",
          "falcon_solver_set_smoothing", "falcon_solver_problem_residuals", "falcon_solver_set_operator",
-         "falcon_solver_set_magnetogram", "falcon_solver_magnetogram", "falcon_solver_set_guess")
+         "falcon_solver_set_magnetogram", "falcon_solver_magnetogram", "falcon_solver_set_guess",
+         "falcon_solver_block_ranges", "falcon_solver_block_flags", "falcon_solver_magnetogram_sources",
+         "falcon_solver_vcycle_op")
 
 
 def _ptr(a):
@@ -194,6 +197,35 @@ class Solver:
         if br.shape != (self.nblocks, self.m[2], self.m[1]):
             raise ValueError("magnetogram shape %s" % (br.shape,))
         self._ck(self.L.falcon_solver_set_magnetogram(self.h, _ptr(br)))
+
+    def vcycle_op(self, op, level, in0, in1=None):
+        """One V-cycle kernel on host FP32 arrays (see falcon_solver_vcycle_op)."""
+        shp = lambda l: (self.nblocks,) + self.level_shape(l)[::-1]
+        a = np.ascontiguousarray(in0, dtype=np.float32)
+        b = None if in1 is None else np.ascontiguousarray(in1, dtype=np.float32)
+        out = np.zeros(shp(level + 1) if op == VCYCLE_RESTRICT else shp(level), dtype=np.float32)
+        self._ck(self.L.falcon_solver_vcycle_op(self.h, C.c_int32(op), C.c_int32(level), _ptr(a),
+                                                None if b is None else _ptr(b), _ptr(out)))
+        return out
+
+    def block_ranges(self):
+        out = np.zeros((self.nblocks, 3, 2))
+        self._ck(self.L.falcon_solver_block_ranges(self.h, _ptr(out)))
+        return out
+
+    def block_flags(self):
+        out = np.zeros(self.nblocks, dtype=np.int32)
+        self._ck(self.L.falcon_solver_block_flags(self.h, _ptr(out)))
+        return out
+
+    def magnetogram_sources(self, problem):
+        """[n][4] x, y, z (cm, Yin frame), q of problem's synthetic magnetogram."""
+        n = C.c_int32()
+        self._ck(self.L.falcon_solver_magnetogram_sources(self.h, C.c_int32(problem), None, C.c_int32(0), C.byref(n)))
+        out = np.zeros((n.value, 4))
+        self._ck(self.L.falcon_solver_magnetogram_sources(self.h, C.c_int32(problem), _ptr(out), C.c_int32(n.value),
+                                                          C.byref(n)))
+        return out
 
     def set_guess(self, x0):
         x0 = np.ascontiguousarray(x0, dtype=np.float64)

@@ -423,6 +423,42 @@ int  falcon_solver_set_operator(falcon_solver* sv, const double* Aii, const doub
 int  falcon_solver_set_magnetogram(falcon_solver* sv, const double* br);
 /* the current PFSS magnetogram in the same layout (0 off the bottom blocks) */
 int  falcon_solver_magnetogram(const falcon_solver* sv, double* br);
+/* Verification: one kernel of the V-cycle on host arrays at `level`, eagerly
+ * and synchronously (as falcon_step_phase is for the step). Arrays are FP32,
+ * interior cells [block][k][j][i] of their level.
+ *   RESTRICT:   in0 = fine residual (level) -> out = coarse right-hand side
+ *               (level+1), the sum of each cell's 8 children in the order of
+ *               ModMath_rebin_3D_factor2 (3_6/ModMath.f90:353-368) without its
+ *               /8 (the operators are volume-integrated: R = P^T)
+ *   PROLONG_ADD: in0 = coarse correction (level+1), in1 = fine correction
+ *               (level) -> out = in1 + injection of in0
+ *               (ModMath_prolongate_3D_factor2, 3_6/ModMath.f90:370-384)
+ *   SMOOTH_RED / SMOOTH_BLACK: in0 = r, in1 = z -> out = z after one
+ *               red-black Gauss-Seidel half sweep of that colour (cells with
+ *               i+j+k even / odd) with the halo filled from z first; each
+ *               updated cell takes the Jacobi formula of
+ *               ModMultigrid_Jacobi_Mz_r (3_5/ModMultigrid.f90:316-324)
+ *   RESIDUAL:   in0 = r, in1 = z -> out = r - A z (halo filled from z) */
+#define FALCON_VCYCLE_RESTRICT     0
+#define FALCON_VCYCLE_PROLONG_ADD  1
+#define FALCON_VCYCLE_SMOOTH_RED   2
+#define FALCON_VCYCLE_SMOOTH_BLACK 3
+#define FALCON_VCYCLE_RESIDUAL     4
+int  falcon_solver_vcycle_op(falcon_solver* sv, int32_t op, int32_t level, const float* in0, const float* in1,
+                             float* out);
+/* level-0 block geometry, for a driver that evaluates its own fields on the
+ * grid: ranges[b][3][2] (r in cm, theta, phi in the block's panel frame) and
+ * flags[b] (bit0 Yin, bit1 top, bit2 bottom), blocks of all problems in order */
+int  falcon_solver_block_ranges(const falcon_solver* sv, double* ranges);
+int  falcon_solver_block_flags(const falcon_solver* sv, int32_t* flags);
+/* PFSS: the point charges of problem `problem`'s synthetic magnetogram,
+ * xyzq[n][4] = x, y, z (cm, Yin frame) and signed charge, in pole pairs
+ * (+q, -q) of the tilted bipoles; *n receives the count (xyzq may be NULL to
+ * query it). The synthetic Br at a bottom face centre (r, theta, phi), Yin
+ * frame, is the ModMagnetogram sum (3_5/ModMagnetogram.f90:43-74) over these
+ * charges plus a 1 G axial dipole, cos(theta). */
+int  falcon_solver_magnetogram_sources(const falcon_solver* sv, int32_t problem, double* xyzq, int32_t cap,
+                                       int32_t* n);
 /* initial guess x0 of the next solves, level 0 [block][k][j][i] (PFSS
  * default 0; conduction default the current temperature) */
 int  falcon_solver_set_guess(falcon_solver* sv, const double* x0);

@@ -49,7 +49,8 @@ def lib():
         L.orc_dt.restype = C.c_double
         L.orc_dt.argtypes = [vp]
         L.orc_hc_halo.restype = C.c_int64
-        for name in ("orc_pfss_operator", "orc_spmv", "orc_halo_fill", "orc_find_leaf"):
+        for name in ("orc_pfss_operator", "orc_spmv", "orc_halo_fill", "orc_find_leaf", "orc_mg_restrict",
+                     "orc_mg_prolong_add", "orc_mg_rbgs"):
             getattr(L, name).restype = C.c_int
         _lib = L
     return _lib
@@ -215,6 +216,66 @@ def halo_fill(m, idx, wx, xp):
     wx = np.ascontiguousarray(wx, dtype=np.float64)
     lib().orc_halo_fill(C.c_int32(m), _ptr(idx), _ptr(wx), C.c_int64(len(idx)), _ptr(xp))
     return xp
+
+
+def mg_restrict(res):
+    """Coarse right-hand side from a fine residual res[b][m][m][m] (FP32):
+    the 8 children summed in ModMath_rebin_3D_factor2's order, no /8."""
+    res = np.ascontiguousarray(res, dtype=np.float32)
+    nb, m = res.shape[0], res.shape[1]
+    out = np.zeros((nb, m // 2, m // 2, m // 2), dtype=np.float32)
+    lib().orc_mg_restrict(C.c_int32(nb), C.c_int32(m), _ptr(res), _ptr(out))
+    return out
+
+
+def mg_prolong_add(zc, zf):
+    """zf + injection of zc (FP32, interior arrays)."""
+    zc = np.ascontiguousarray(zc, dtype=np.float32)
+    out = np.array(zf, dtype=np.float32, copy=True)
+    lib().orc_mg_prolong_add(C.c_int32(out.shape[0]), C.c_int32(out.shape[1]), _ptr(zc), _ptr(out))
+    return out
+
+
+def mg_rbgs(A, r, zp, colour):
+    """One red-black half sweep (FP32) on the padded zp (halo filled)."""
+    A32 = [np.ascontiguousarray(a, dtype=np.float32) for a in A]
+    r = np.ascontiguousarray(r, dtype=np.float32)
+    out = np.array(zp, dtype=np.float32, copy=True)
+    nb, m = r.shape[0], r.shape[1]
+    lib().orc_mg_rbgs(C.c_int32(nb), C.c_int32(m), *(_ptr(a) for a in A32), _ptr(r), _ptr(out), C.c_int32(colour))
+    return out
+
+
+def mg_solve(ops, halos, bprob, nproblems, b, x0, tol, max_iter, smoothing):
+    """CPU FP64 MG-preconditioned flexible CG of a batch (see orc_mg_solve).
+    ops[l] = (Aii, Ai, Aj, Ak), halos[l] = (idx, wx); returns (x, iterations,
+    per-problem FP64 relative residuals)."""
+    nl = len(ops)
+    keep = []
+    op_ptrs = (C.c_void_p * (4 * nl))()
+    hi = (C.c_void_p * nl)()
+    hw = (C.c_void_p * nl)()
+    nh = (C.c_int64 * nl)()
+    for l in range(nl):
+        for a, arr in enumerate(ops[l]):
+            arr = np.ascontiguousarray(arr, dtype=np.float64)
+            keep.append(arr)
+            op_ptrs[4 * l + a] = arr.ctypes.data
+        idx = np.ascontiguousarray(halos[l][0], dtype=np.int32)
+        wx = np.ascontiguousarray(halos[l][1], dtype=np.float64)
+        keep += [idx, wx]
+        hi[l], hw[l], nh[l] = idx.ctypes.data, wx.ctypes.data, len(idx)
+    bprob = np.ascontiguousarray(bprob, dtype=np.int32)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.array(x0, dtype=np.float64, copy=True)
+    rel = np.zeros(nproblems)
+    m0 = ops[0][0].shape[1]
+    L = lib()
+    L.orc_mg_solve.restype = C.c_int
+    it = L.orc_mg_solve(C.c_int32(b.shape[0]), C.c_int32(nproblems), _ptr(bprob), C.c_int32(nl), C.c_int32(m0),
+                        op_ptrs, hi, hw, nh, C.c_int32(smoothing[0]), C.c_int32(smoothing[1]),
+                        C.c_int32(smoothing[2]), _ptr(b), _ptr(x), C.c_double(tol), C.c_int32(max_iter), _ptr(rel))
+    return x, it, rel
 
 
 def ghost_entries_to_numpy(arr, n):

@@ -7,8 +7,14 @@
 //                   in first-appearance order, i-j-k loop order) and the
 //                   interpolation of 3_5/ModMath.f90:208-248
 //   SpMV            3_5/ModLinearSolver.f90:34-51
-// The reference solver runs in default real (FP32); this restatement keeps the
-// operation order and evaluates in FP64, the precision of the GPU outer solve.
+//   V-cycle parts   restriction 3_6/ModMath.f90:353-368, prolongation
+//                   3_6/ModMath.f90:370-384, the smoother's cell update
+//                   3_5/ModMultigrid.f90:316-324 (FP32, for component parity)
+//   MG-PCG          3_5/ModLinearSolver.f90:201-427 as the GPU corrects it
+//                   (FP64 throughout: the CPU reference solve of a batch)
+// The reference solver runs in default real (FP32); the SpMV and the CPU
+// solve keep its operation order and evaluate in FP64, the precision in which
+// the GPU solve judges convergence.
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -179,6 +185,7 @@ int64_t orc_hc_halo(void* h, int32_t m, int32_t* idx, double* wx, int32_t* clamp
 int orc_spmv(int32_t nb, int32_t m, const double* Aii, const double* Ai, const double* Aj, const double* Ak,
              const double* xp, double* y) {
     const int p = m + 2;
+#pragma omp parallel for schedule(static)
     for (int b = 0; b < nb; ++b)
         for (int k = 1; k <= m; ++k)
             for (int j = 1; j <= m; ++j)
@@ -197,6 +204,8 @@ int orc_spmv(int32_t nb, int32_t m, const double* Aii, const double* Ai, const d
 // collapse onto the base cell (only the sign of an exact zero can differ).
 int orc_halo_fill(int32_t m, const int32_t* idx, const double* w6, int64_t n, double* xp) {
     const int p = m + 2;
+    // every entry writes its own ghost cell and reads interior cells only
+#pragma omp parallel for schedule(static)
     for (int64_t e = 0; e < n; ++e) {
         const int32_t* v = idx + 8 * e;
         const double* w = w6 + 6 * e;
@@ -211,6 +220,274 @@ int orc_halo_fill(int32_t m, const int32_t* idx, const double* w6, int64_t n, do
         xp[(((size_t)v[0] * p + v[3]) * p + v[2]) * p + v[1]] = val;
     }
     return 0;
+}
+
+// ---- V-cycle components (FP32, the GPU smoother's precision) -----------------
+// Restriction: coarse cell (I,J,K) = the sum of its 8 children in the order of
+// ModMath_rebin_3D_factor2 (3_6/ModMath.f90:360-367: (1,1,1), (2,1,1), (1,2,1),
+// (2,2,1), (1,1,2), (2,1,2), (1,2,2), (2,2,2)), summed left to right, without
+// the reference's /8: the operators are volume-integrated, so the coarse
+// right-hand side is R = P^T of the fine residual. res, rc interior [b][k][j][i].
+int orc_mg_restrict(int32_t nb, int32_t m, const float* res, float* rc) {
+    const int mc = m / 2;
+    for (int b = 0; b < nb; ++b)
+        for (int K = 1; K <= mc; ++K)
+            for (int J = 1; J <= mc; ++J)
+                for (int I = 1; I <= mc; ++I) {
+                    auto F = [&](int i, int j, int k) { return res[cidx(m, b, 2 * I - 2 + i, 2 * J - 2 + j, 2 * K - 2 + k)]; };
+                    rc[cidx(mc, b, I, J, K)] =
+                        F(1, 1, 1) + F(2, 1, 1) + F(1, 2, 1) + F(2, 2, 1) + F(1, 1, 2) + F(2, 1, 2) + F(1, 2, 2) + F(2, 2, 2);
+                }
+    return 0;
+}
+
+// Prolongation by injection (ModMath_prolongate_3D_factor2, 3_6/ModMath.f90:
+// 370-384: each coarse value to its 2x2x2 children), added to the fine
+// correction zf (interior [b][k][j][i] of the fine level, m cells per edge).
+int orc_mg_prolong_add(int32_t nb, int32_t m, const float* zc, float* zf) {
+    const int mc = m / 2;
+    for (int b = 0; b < nb; ++b)
+        for (int k = 1; k <= m; ++k)
+            for (int j = 1; j <= m; ++j)
+                for (int i = 1; i <= m; ++i)
+                    zf[cidx(m, b, i, j, k)] += zc[cidx(mc, b, (i + 1) / 2, (j + 1) / 2, (k + 1) / 2)];
+    return 0;
+}
+
+// One red-black Gauss-Seidel half sweep: every cell with (i+j+k) % 2 ==
+// colour takes the Jacobi update of ModMultigrid_Jacobi_Mz_r
+// (3_5/ModMultigrid.f90:316-324), z = (r - Ai z(i-1) - Ai z(i+1) - Aj z(j-1)
+// - Aj z(j+1) - Ak z(k-1) - Ak z(k+1)) / Aii, left to right in FP32; its
+// neighbours are of the other colour, so the order of cells is immaterial.
+// zp padded [b][m+2]^3 with its halo filled.
+int orc_mg_rbgs(int32_t nb, int32_t m, const float* Aii, const float* Ai, const float* Aj, const float* Ak,
+                const float* r, float* zp, int32_t colour) {
+    const int p = m + 2;
+    for (int b = 0; b < nb; ++b)
+        for (int k = 1; k <= m; ++k)
+            for (int j = 1; j <= m; ++j)
+                for (int i = 1; i <= m; ++i) {
+                    if (((i + j + k) & 1) != colour) continue;
+                    auto Z = [&](int ii, int jj, int kk) -> float& { return zp[(((size_t)b * p + kk) * p + jj) * p + ii]; };
+                    float v = r[cidx(m, b, i, j, k)] - Ai[fidx_i(m, b, i, j, k)] * Z(i - 1, j, k);
+                    v = v - Ai[fidx_i(m, b, i + 1, j, k)] * Z(i + 1, j, k);
+                    v = v - Aj[fidx_j(m, b, i, j, k)] * Z(i, j - 1, k);
+                    v = v - Aj[fidx_j(m, b, i, j + 1, k)] * Z(i, j + 1, k);
+                    v = v - Ak[fidx_k(m, b, i, j, k)] * Z(i, j, k - 1);
+                    v = v - Ak[fidx_k(m, b, i, j, k + 1)] * Z(i, j, k + 1);
+                    Z(i, j, k) = v / Aii[cidx(m, b, i, j, k)];
+                }
+    return 0;
+}
+
+}  // extern "C"
+
+// ---- CPU reference solve (FP64) ---------------------------------------------
+namespace {
+
+struct MgLevel {
+    int m = 0;
+    const double *Aii, *Ai, *Aj, *Ak;
+    const int32_t* idx;   // halo [n][8]
+    const double* w6;     // halo [n][6]
+    int64_t nh;
+    std::vector<double> z, r, res;   // z padded; r, res interior
+};
+
+struct MgSolver {
+    int nb, np, nl, nu_pre, nu_post, nu_coarse;
+    const int32_t* bprob;
+    std::vector<MgLevel> L;
+
+    size_t nint(int l) const { return (size_t)nb * L[l].m * L[l].m * L[l].m; }
+    size_t npad(int l) const { const size_t p = L[l].m + 2; return (size_t)nb * p * p * p; }
+    void halo(int l, double* xp) const { orc_halo_fill(L[l].m, L[l].idx, L[l].w6, L[l].nh, xp); }
+    double& P(int l, std::vector<double>& v, int b, int i, int j, int k) const {
+        const size_t p = L[l].m + 2;
+        return v[(((size_t)b * p + k) * p + j) * p + i];
+    }
+    // one red-black half sweep on level l, FP64
+    void sweep(int l, int colour) {
+        MgLevel& Q = L[l];
+        const int m = Q.m, p = m + 2;
+        halo(l, Q.z.data());
+#pragma omp parallel for schedule(static)
+        for (int b = 0; b < nb; ++b)
+            for (int k = 1; k <= m; ++k)
+                for (int j = 1; j <= m; ++j)
+                    for (int i = 1; i <= m; ++i) {
+                        if (((i + j + k) & 1) != colour) continue;
+                        auto Z = [&](int ii, int jj, int kk) -> double& { return Q.z[(((size_t)b * p + kk) * p + jj) * p + ii]; };
+                        double v = Q.r[cidx(m, b, i, j, k)] - Q.Ai[fidx_i(m, b, i, j, k)] * Z(i - 1, j, k);
+                        v = v - Q.Ai[fidx_i(m, b, i + 1, j, k)] * Z(i + 1, j, k);
+                        v = v - Q.Aj[fidx_j(m, b, i, j, k)] * Z(i, j - 1, k);
+                        v = v - Q.Aj[fidx_j(m, b, i, j + 1, k)] * Z(i, j + 1, k);
+                        v = v - Q.Ak[fidx_k(m, b, i, j, k)] * Z(i, j, k - 1);
+                        v = v - Q.Ak[fidx_k(m, b, i, j, k + 1)] * Z(i, j, k + 1);
+                        Z(i, j, k) = v / Q.Aii[cidx(m, b, i, j, k)];
+                    }
+    }
+    // z_0 = M r_0 (L[0].r): V-cycle with the GPU's structure and sweep counts
+    void vcycle() {
+        for (int l = 0; l < nl; ++l) {
+            MgLevel& Q = L[l];
+            std::fill(Q.z.begin(), Q.z.end(), 0.0);
+            const int sw = (l == nl - 1 && nl > 1) ? nu_coarse : nu_pre;
+            for (int s = 0; s < sw; ++s) { sweep(l, 0); sweep(l, 1); }
+            if (l + 1 < nl) {
+                halo(l, Q.z.data());
+                orc_spmv(nb, Q.m, Q.Aii, Q.Ai, Q.Aj, Q.Ak, Q.z.data(), Q.res.data());
+                for (size_t c = 0; c < Q.res.size(); ++c) Q.res[c] = Q.r[c] - Q.res[c];
+                MgLevel& C = L[l + 1];
+                const int m = Q.m, mc = C.m;
+#pragma omp parallel for schedule(static)
+                for (int b = 0; b < nb; ++b)
+                    for (int K = 1; K <= mc; ++K)
+                        for (int J = 1; J <= mc; ++J)
+                            for (int I = 1; I <= mc; ++I) {
+                                auto F = [&](int i, int j, int k) {
+                                    return Q.res[cidx(m, b, 2 * I - 2 + i, 2 * J - 2 + j, 2 * K - 2 + k)];
+                                };
+                                C.r[cidx(mc, b, I, J, K)] = F(1, 1, 1) + F(2, 1, 1) + F(1, 2, 1) + F(2, 2, 1) + F(1, 1, 2) +
+                                                            F(2, 1, 2) + F(1, 2, 2) + F(2, 2, 2);
+                            }
+            }
+        }
+        for (int l = nl - 2; l >= 0; --l) {
+            MgLevel& Q = L[l];
+            MgLevel& C = L[l + 1];
+            const int m = Q.m;
+#pragma omp parallel for schedule(static)
+            for (int b = 0; b < nb; ++b)
+                for (int k = 1; k <= m; ++k)
+                    for (int j = 1; j <= m; ++j)
+                        for (int i = 1; i <= m; ++i) P(l, Q.z, b, i, j, k) += P(l + 1, C.z, b, (i + 1) / 2, (j + 1) / 2, (k + 1) / 2);
+            for (int s = 0; s < nu_post; ++s) { sweep(l, 1); sweep(l, 0); }
+        }
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+// CPU FP64 MG-preconditioned flexible CG of a batch of problems (blocks of
+// problem q share its scalars), the GPU solve's algorithm entirely in FP64:
+// the same Galerkin levels, halo maps and red-black V-cycle. ops: per level
+// Aii, Ai, Aj, Ak (4 pointers per level); halo: per level idx [n][8] and w6
+// [n][6] with counts nh[l]; m0 cells per block edge at level 0. x (interior
+// [b][m0^3]) holds the initial guess and receives the solution; each problem
+// iterates until its true FP64 relative residual is <= tol (checked every
+// iteration on a recomputed b - A x) or max_iter. rel[np] receives the final
+// relative residuals; returns the iterations taken.
+int orc_mg_solve(int32_t nb, int32_t np, const int32_t* bprob, int32_t nl, int32_t m0, const double* const* ops,
+                 const int32_t* const* hidx, const double* const* hw6, const int64_t* nh, int32_t nu_pre, int32_t nu_post,
+                 int32_t nu_coarse, const double* bvec, double* x, double tol, int32_t max_iter, double* rel) {
+    MgSolver S;
+    S.nb = nb; S.np = np; S.nl = nl; S.bprob = bprob;
+    S.nu_pre = nu_pre; S.nu_post = nu_post; S.nu_coarse = nu_coarse;
+    S.L.resize(nl);
+    for (int l = 0; l < nl; ++l) {
+        MgLevel& Q = S.L[l];
+        Q.m = m0 >> l;
+        Q.Aii = ops[4 * l]; Q.Ai = ops[4 * l + 1]; Q.Aj = ops[4 * l + 2]; Q.Ak = ops[4 * l + 3];
+        Q.idx = hidx[l]; Q.w6 = hw6[l]; Q.nh = nh[l];
+        Q.z.assign(S.npad(l), 0.0);
+        Q.r.assign(S.nint(l), 0.0);
+        Q.res.assign(S.nint(l), 0.0);
+    }
+    const int m = m0;
+    const size_t per = (size_t)m * m * m, n = (size_t)nb * per;
+    MgLevel& Z = S.L[0];
+    std::vector<double> xp(S.npad(0), 0.0), pp(S.npad(0), 0.0), r(n), z(n), Ap(n);
+    auto scatter = [&](const std::vector<double>& v, std::vector<double>& vp, const double* src) {
+        (void)v;
+#pragma omp parallel for schedule(static)
+        for (int b = 0; b < nb; ++b)
+            for (int k = 1; k <= m; ++k)
+                for (int j = 1; j <= m; ++j)
+                    for (int i = 1; i <= m; ++i) S.P(0, vp, b, i, j, k) = src[cidx(m, b, i, j, k)];
+    };
+    std::vector<double> part(nb);
+    auto dots = [&](const double* a, const double* b2, std::vector<double>& out) {
+#pragma omp parallel for schedule(static)
+        for (int b = 0; b < nb; ++b) {
+            double s = 0;
+            for (size_t c = 0; c < per; ++c) s += a[(size_t)b * per + c] * b2[(size_t)b * per + c];
+            part[b] = s;
+        }
+        std::fill(out.begin(), out.end(), 0.0);
+        for (int b = 0; b < nb; ++b) out[bprob[b]] += part[b];
+    };
+    std::vector<double> bb(np), rr(np), pAp(np), pr(np), zAp(np);
+    dots(bvec, bvec, bb);
+    for (auto& v : bb) if (!(v > 0)) v = 1.0;
+    auto true_residual = [&]() {
+        scatter(r, xp, x);
+        S.halo(0, xp.data());
+        orc_spmv(nb, m, Z.Aii, Z.Ai, Z.Aj, Z.Ak, xp.data(), r.data());
+        for (size_t c = 0; c < n; ++c) r[c] = bvec[c] - r[c];
+        dots(r.data(), r.data(), rr);
+    };
+    std::vector<int> active(np, 1);
+    auto check = [&]() {
+        bool any = false;
+        for (int q = 0; q < np; ++q) {
+            rel[q] = std::sqrt(rr[q] / bb[q]);
+            active[q] = rel[q] > tol;
+            any = any || active[q];
+        }
+        return any;
+    };
+    auto precondition = [&]() {
+        std::copy(r.begin(), r.end(), Z.r.begin());
+        S.vcycle();
+#pragma omp parallel for schedule(static)
+        for (int b = 0; b < nb; ++b)
+            for (int k = 1; k <= m; ++k)
+                for (int j = 1; j <= m; ++j)
+                    for (int i = 1; i <= m; ++i) z[cidx(m, b, i, j, k)] = S.P(0, Z.z, b, i, j, k);
+    };
+    true_residual();
+    if (!check()) return 0;
+    precondition();
+    scatter(z, pp, z.data());
+    int it = 0;
+    while (it < max_iter) {
+        ++it;
+        S.halo(0, pp.data());
+        orc_spmv(nb, m, Z.Aii, Z.Ai, Z.Aj, Z.Ak, pp.data(), Ap.data());
+        std::vector<double> pint(n);
+#pragma omp parallel for schedule(static)
+        for (int b = 0; b < nb; ++b)
+            for (int k = 1; k <= m; ++k)
+                for (int j = 1; j <= m; ++j)
+                    for (int i = 1; i <= m; ++i) pint[cidx(m, b, i, j, k)] = S.P(0, pp, b, i, j, k);
+        dots(pint.data(), Ap.data(), pAp);
+        dots(pint.data(), r.data(), pr);
+        for (int b = 0; b < nb; ++b) {
+            const int q = bprob[b];
+            const double al = (active[q] && pAp[q] != 0.0) ? pr[q] / pAp[q] : 0.0;
+            for (size_t c = 0; c < per; ++c) x[(size_t)b * per + c] += al * pint[(size_t)b * per + c];
+        }
+        true_residual();
+        if (!check()) break;
+        precondition();
+        dots(z.data(), Ap.data(), zAp);
+#pragma omp parallel for schedule(static)
+        for (int b = 0; b < nb; ++b) {
+            const int q = bprob[b];
+            if (!active[q]) continue;
+            const double be = pAp[q] != 0.0 ? -zAp[q] / pAp[q] : 0.0;
+            for (int k = 1; k <= m; ++k)
+                for (int j = 1; j <= m; ++j)
+                    for (int i = 1; i <= m; ++i) {
+                        double& pv = S.P(0, pp, b, i, j, k);
+                        pv = z[cidx(m, b, i, j, k)] + be * pv;
+                    }
+        }
+    }
+    return it;
 }
 
 }  // extern "C"

@@ -246,3 +246,140 @@ def test_gpu_large_pfss_batch_converges_every_problem():
     print("32-problem PFSS batch:", rep, "max FP64 residual %.3e" % rel.max())
     assert rep["converged"] == 1 and (rel <= 1.05e-10).all(), rel.max()
     sv.close()
+
+
+@pytest.mark.gpu
+def test_gpu_solve_reports_not_converged_on_its_fp64_residual():
+    """Convergence is judged on the FP64 true residual only: a solve cut off
+    by max_iter, or asked for a tolerance below what FP64 attains, returns
+    FALCON_ERR_NOT_CONVERGED with converged = 0, and its reported residual is
+    the FP64 ||b - A x|| / ||b|| of the returned solution."""
+    import falcon_gb300 as fg
+    sv = S.Solver(S.pfss_spec([(24, 45), (32, 60)], device=0))
+    with pytest.raises(fg.FalconError) as e:
+        sv.solve(tol=1e-10, max_iter=3)
+    assert e.value.code == fg.ERR_NOT_CONVERGED
+    rep = sv.solve(tol=1e-10, max_iter=3, check=False)
+    rel = sv.problem_residuals()
+    assert rep["converged"] == 0 and rep["iterations"] == 3
+    assert rep["rel_residual"] > 1e-10
+    assert abs(rep["rel_residual"] - rel.max()) <= 1e-9 * rel.max()
+    # below FP64's attainable accuracy: stops at the floor, not converged
+    rep = sv.solve(tol=1e-19, max_iter=400, check=False)
+    rel = sv.problem_residuals()
+    print("tol 1e-19:", rep, rel)
+    assert rep["converged"] == 0 and rep["floor_residual"] > 0
+    assert rep["rel_residual"] < 1e-12 and rel.max() < 1e-12
+    # and a reachable tolerance converges, judged on the same FP64 residual
+    rep = sv.solve(tol=1e-11, max_iter=400)
+    assert rep["converged"] == 1 and (sv.problem_residuals() <= 1e-11).all()
+
+
+def test_cpu_reference_mg_solve_matches_direct_solve():
+    """The oracle's FP64 MG-PCG (the CPU reference solve for the batched PFSS
+    error check) agrees with a sparse direct solve of the same operator."""
+    import scipy.sparse.linalg as spl
+    sv = S.Solver(S.pfss_spec([(16, 24), (16, 30)], device=-1))
+    A = _assemble_csr(sv)
+    b = sv.rhs()
+    x_ref = spl.spsolve(A.tocsc(), b.reshape(-1)).reshape(b.shape)
+    ops = [sv.operator(l) for l in range(sv.nlevels)]
+    halos = [sv.halo_map(l) for l in range(sv.nlevels)]
+    first = sv.problem_blocks()
+    bprob = np.repeat(np.arange(sv.nproblems), np.diff(first))
+    x, it, rel = oracle.mg_solve(ops, halos, bprob, sv.nproblems, b, np.zeros_like(b), 1e-13, 300, (1, 1, 32))
+    print("cpu mg-pcg:", it, rel)
+    assert (rel <= 1e-13).all()
+    for q in range(sv.nproblems):
+        sl = slice(first[q], first[q + 1])
+        assert np.linalg.norm(x[sl] - x_ref[sl]) <= 1e-9 * np.linalg.norm(x_ref[sl])
+
+
+def _vcycle_solver():
+    return S.Solver(S.pfss_spec([(24, 45), (16, 30)], device=0))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("level", [0, 1])
+def test_gpu_restriction_and_prolongation_bit_identical_to_oracle(level):
+    """k_restrict and k_prolong_add against the restatements of
+    ModMath_rebin_3D_factor2 (sum order of 3_6/ModMath.f90:360-367, no /8)
+    and ModMath_prolongate_3D_factor2 (3_6/ModMath.f90:370-384): FP32, bit for bit."""
+    sv = _vcycle_solver()
+    rs = np.random.default_rng(40 + level)
+    shp = lambda l: (sv.nblocks,) + sv.level_shape(l)[::-1]
+    res = rs.normal(size=shp(level)).astype(np.float32)
+    assert np.array_equal(sv.vcycle_op(S.VCYCLE_RESTRICT, level, res), oracle.mg_restrict(res))
+    zc = rs.normal(size=shp(level + 1)).astype(np.float32)
+    zf = rs.normal(size=shp(level)).astype(np.float32)
+    assert np.array_equal(sv.vcycle_op(S.VCYCLE_PROLONG_ADD, level, zc, zf), oracle.mg_prolong_add(zc, zf))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("level", [0, 1, 2])
+def test_gpu_smoother_half_sweeps_and_residual_match_oracle(level):
+    """One red-black half sweep of each colour (k_rbgs) and the FP32 residual
+    (k_resid32) against the oracle's FP32 restatement of the Jacobi cell
+    update of ModMultigrid_Jacobi_Mz_r (3_5/ModMultigrid.f90:316-324). Cells
+    of the other colour are untouched bit for bit; updated cells agree to
+    FP32 rounding (the GPU sweep uses explicit FMAs and a fast division, its
+    halo is interpolated in FP32, the oracle's in FP64): tolerance 2e-5 of the
+    largest |z|."""
+    sv = _vcycle_solver()
+    rs = np.random.default_rng(50 + level)
+    shp = (sv.nblocks,) + sv.level_shape(level)[::-1]
+    m = shp[1]
+    A = sv.operator(level)
+    r = rs.normal(size=shp).astype(np.float32)
+    z = rs.normal(size=shp).astype(np.float32)
+    idx, wx = sv.halo_map(level)
+    zp = np.zeros((sv.nblocks, m + 2, m + 2, m + 2))
+    zp[:, 1:-1, 1:-1, 1:-1] = z
+    zp = oracle.halo_fill(m, idx, wx, zp).astype(np.float32)
+    kk, jj, ii = np.meshgrid(np.arange(1, m + 1), np.arange(1, m + 1), np.arange(1, m + 1), indexing="ij")
+    for colour, op in ((0, S.VCYCLE_SMOOTH_RED), (1, S.VCYCLE_SMOOTH_BLACK)):
+        g = sv.vcycle_op(op, level, r, z)
+        o = oracle.mg_rbgs(A, r, zp, colour)[:, 1:-1, 1:-1, 1:-1]
+        upd = ((ii + jj + kk) & 1) == colour
+        assert np.array_equal(g[:, ~upd], z[:, ~upd])
+        err = np.abs(g[:, upd] - o[:, upd]).max() / np.abs(o).max()
+        print("level %d colour %d: max rel diff %.2e" % (level, colour, err))
+        assert err <= 2e-5
+    y = oracle.spmv(m, A, zp.astype(np.float64))
+    g = sv.vcycle_op(S.VCYCLE_RESIDUAL, level, r, z)
+    ref = r.astype(np.float64) - y
+    assert np.abs(g - ref).max() <= 2e-5 * np.abs(ref).max()
+
+
+@pytest.mark.gpu
+def test_gpu_pfss_batch64_error_per_solve_against_cpu_fp64_solve():
+    """The batched PFSS workload: 64 problems of the seeded random sizes
+    (nr 24..64, ntheta 45..180; 70.8M cells) solved together on the GPU to
+    1e-10, then each problem's FP64 error against a CPU FP64 solve. The CPU
+    reference is the oracle's FP64 MG-PCG on the same operator, started from
+    the GPU solution and run until each problem's FP64 true residual is
+    <= 1e-13: its correction is A^-1 r_gpu, the GPU solution's error, computed
+    on the CPU in FP64. Per problem: ||x_gpu - x_cpu|| / ||x_cpu||."""
+    import time
+    sizes = S.random_pfss_sizes(64, seed=5000)
+    sv = S.Solver(S.pfss_spec(sizes, device=0))
+    rep = sv.solve(tol=1e-10, max_iter=300)
+    assert rep["converged"] == 1
+    x_gpu = sv.solution()
+    rel_gpu = sv.problem_residuals()
+    t0 = time.time()
+    ops = [sv.operator(l) for l in range(sv.nlevels)]
+    halos = [sv.halo_map(l) for l in range(sv.nlevels)]
+    first = sv.problem_blocks()
+    bprob = np.repeat(np.arange(sv.nproblems), np.diff(first))
+    x_cpu, it, rel_cpu = oracle.mg_solve(ops, halos, bprob, sv.nproblems, sv.rhs(), x_gpu, 1e-13, 100, (1, 1, 32))
+    err = np.array([np.linalg.norm(x_gpu[first[q]:first[q + 1]] - x_cpu[first[q]:first[q + 1]]) /
+                    np.linalg.norm(x_cpu[first[q]:first[q + 1]]) for q in range(sv.nproblems)])
+    print("pfss batch64: GPU %s; CPU reference %d iterations in %.1f s, max residual %.2e" %
+          (rep, it, time.time() - t0, rel_cpu.max()))
+    print("per-problem FP64 error vs the CPU solve: max %.3e median %.3e min %.3e" %
+          (err.max(), np.median(err), err.min()))
+    print("per-problem GPU FP64 residual: max %.3e median %.3e" % (rel_gpu.max(), np.median(rel_gpu)))
+    assert (rel_gpu <= 1e-10).all()
+    assert (rel_cpu <= 1e-13).all()
+    assert err.max() <= 1e-7, err
