@@ -15,9 +15,9 @@ GPU ("replicas only": the shell is not partitioned across GPUs); value is the
 sum of cell-updates over ranks divided by the max time over ranks.
 
 --impl reference times the CPU restatement of the reference algorithm (the
-oracle; the Fortran reference cannot be built here) on the host cores, on a
-bounded sample of the same workload (a shell of 16^3 blocks with the same
-physics, 108 blocks / 442,368 cells), and prints the same JSON line.
+oracle's -O3 timing build; the Fortran reference cannot be built here) on the
+host cores, on the same 21,233,664-cell workload (a few steps, median), plus a
+1-core run on a 442,368-cell shell, and prints the same JSON line.
 """
 import argparse
 import json
@@ -187,49 +187,97 @@ def reduce_sum(dist, x):
 
 
 def cpu_sample_config():
-    """Bounded CPU sample of the workload: same physics and 16^3 blocks, per
-    panel 32 x 48 x 144 cells (108 blocks, 442,368 cells)."""
+    """The 1-core CPU sample: the same physics in 16^3 blocks, per panel
+    32 x 48 x 144 cells (108 blocks, 442,368 cells)."""
     from falcon_gb300 import config
     return config.make_config(block=(16, 16, 16), root_tiles=(1, 3, 9), radial_levels=1, radial_option=1,
-                              amr=(), precision=config.PREC_FP64)
+                              amr=(), precision=config.PREC_FP64, device=-1)
 
 
-def time_oracle(steps, warmup, budget_s=25.0):
-    """Time the CPU oracle on the bounded sample with all host threads."""
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+def _time_oracle_steps(cfg, max_steps, budget_s, threads=None):
+    """Median seconds per step of the oracle's -O3 timing build on cfg (one
+    warm-up step first), with `threads` OpenMP threads (None: all)."""
     import oracle
     from falcon_gb300 import synth
-    cfg = cpu_sample_config()
-    o = oracle.Oracle(cfg)
-    u0 = synth.initial_state(cfg, o.block_ranges(), o.block_flags(), seed=1002)
-    o.set_state(u0)
-    o.exchange()
-    o.exchange()
-    for _ in range(warmup):
+    oracle.build()
+    if threads is not None:
+        oracle.set_threads(threads, timing=True)
+    try:
+        o = oracle.Oracle(cfg, timing=True)
+        u0 = synth.initial_state(cfg, o.block_ranges(), o.block_flags(), seed=1002)
+        o.set_state(u0)
+        del u0
+        o.exchange()
+        o.exchange()
         o.step()
-    cells = o.nblocks * 16 ** 3
-    done, t0 = 0, time.perf_counter()
-    while done < steps:
-        o.step()
-        done += 1
-        if time.perf_counter() - t0 > budget_s:
-            break
-    el = time.perf_counter() - t0
-    return cells * done / el, oracle.num_threads(), "%d steps of the %d-cell 16^3-block shell (%d blocks)" % (
-        done, cells, o.nblocks)
+        times, t_all = [], time.perf_counter()
+        while len(times) < max_steps:
+            t0 = time.perf_counter()
+            o.step()
+            times.append(time.perf_counter() - t0)
+            if time.perf_counter() - t_all > budget_s:
+                break
+        cores = oracle.num_threads(timing=True)
+        cells = o.nblocks * cfg.tree.ni * cfg.tree.nj * cfg.tree.nk
+        del o
+        return statistics.median(times), len(times), cores, cells
+    finally:
+        if threads is not None:
+            oracle.set_threads(os.cpu_count() or 1, timing=True)
+
+
+def time_cpu_reference(max_steps=5, budget_s=60.0):
+    """The CPU restatement of the reference step (the oracle; the Fortran
+    reference cannot be built here), timing build (-O3, OpenMP over blocks),
+    on the machine's host cores: the full 21,233,664-cell workload with every
+    thread, median of up to `max_steps` steps after one warm-up step; and on
+    one core, the 442,368-cell sample shell, median of 5 steps."""
+    from falcon_gb300 import config
+    full = config.shell_mixed_21m(precision=config.PREC_FP64, device=-1)
+    med, n, cores, cells = _time_oracle_steps(full, max_steps, budget_s)
+    med1, n1, _, cells1 = _time_oracle_steps(cpu_sample_config(), 5, 30.0, threads=1)
+    return {"value": cells / med, "unit": UNIT, "cores": cores, "kind": "port",
+            "build": "oracle -O3 timing build (oracle/build/liboracle_fast.so), OpenMP over blocks",
+            "sample": "full workload: %d cells (5,184 blocks of 16^3), median of %d steps after 1 warm-up step; "
+                      "initial state: entropy bump + dipole B (the step's cost does not depend on the values)"
+                      % (cells, n),
+            "s_per_step": med,
+            "cores_1": {"value": cells1 / med1, "unit": UNIT, "cores": 1, "s_per_step": med1,
+                        "sample": "%d-cell shell (108 blocks of 16^3), median of %d steps" % (cells1, n1)},
+            "cpu_model": cpu_model(), "nproc": os.cpu_count()}
 
 
 def run_reference(args, rank, world, dist):
     if rank != 0:
         return
-    value, cores, sample = time_oracle(max(args.steps, 1), min(args.warmup, 1))
+    cpu = time_cpu_reference(max_steps=max(min(args.steps, 5), 3))
+    value = cpu["value"]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "cells": 21233664, "blocks": 5184, "block": [16, 16, 16],
-                   "sample": "cpu sample shell, same physics"},
+                   "same_config": True, "timed": cpu["sample"]},
         "impl": "reference",
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "cpu_baseline": cpu,
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -347,8 +395,7 @@ def run_ours(args, rank, world, local, dist):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline and args.workload == "full":
-        v, cores, sample = time_oracle(3, 1, budget_s=20.0)
-        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        cpu = time_cpu_reference(max_steps=5, budget_s=40.0)
 
     if rank == 0:
         line = {

@@ -14,46 +14,60 @@ NVAR = 9   # variables of a block array (rho1 .. s1, psi), as FALCON_NVAR
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "build", "liboracle.so")
+# -O3 timing build of the same sources (the CPU baseline's clock), never used as the checker
+FAST_LIB_PATH = os.path.join(HERE, "build", "liboracle_fast.so")
 _lib = None
+_fast = None
 
 
 def build(force=False):
-    """Compile the oracle with its Makefile (gcc, -ffp-contract=off)."""
+    """Compile both oracle builds with the Makefile (parity: -O2
+    -ffp-contract=off; timing: -O3)."""
     srcs = [os.path.join(HERE, f) for f in ("falcon_oracle.cpp", "solver_oracle.cpp", "Makefile")]
-    if force or not os.path.exists(LIB_PATH) or any(
-            os.path.getmtime(LIB_PATH) < os.path.getmtime(f) for f in srcs):
+    if force or any(not os.path.exists(p) or any(os.path.getmtime(p) < os.path.getmtime(f) for f in srcs)
+                    for p in (LIB_PATH, FAST_LIB_PATH)):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB_PATH
 
 
-def lib():
-    global _lib
+def lib(timing=False):
+    """The parity build, or with timing=True the -O3 timing build."""
+    global _lib, _fast
+    if timing:
+        if _fast is None:
+            build()
+            _fast = _declare(C.CDLL(FAST_LIB_PATH))
+        return _fast
     if _lib is None:
         build()
-        L = C.CDLL(LIB_PATH)
-        vp = C.c_void_p
-        L.orc_create.restype = vp
-        L.orc_create.argtypes = [vp]
-        L.orc_destroy.argtypes = [vp]
-        for name in ("orc_num_blocks", "orc_block_ranges", "orc_block_flags", "orc_get_background",
-                     "orc_ghost_map", "orc_set_state", "orc_get_state", "orc_exchange",
-                     "orc_timestep", "orc_step", "orc_block_rhs", "orc_block_diffusion",
-                     "orc_block_grid", "orc_phase", "orc_get_stage_state", "orc_save_allcells",
-                     "orc_set_background"):
-            getattr(L, name).restype = C.c_int
-        L.orc_ghost_count.restype = C.c_int64
-        L.orc_ghost_count.argtypes = [vp]
-        L.orc_uncovered_ghosts.restype = C.c_int64
-        L.orc_uncovered_ghosts.argtypes = [vp]
-        L.orc_num_threads.restype = C.c_int
-        L.orc_dt.restype = C.c_double
-        L.orc_dt.argtypes = [vp]
-        L.orc_hc_halo.restype = C.c_int64
-        for name in ("orc_pfss_operator", "orc_spmv", "orc_halo_fill", "orc_find_leaf", "orc_mg_restrict",
-                     "orc_mg_prolong_add", "orc_mg_rbgs"):
-            getattr(L, name).restype = C.c_int
-        _lib = L
+        _lib = _declare(C.CDLL(LIB_PATH))
     return _lib
+
+
+def _declare(L):
+    """Return types of the exported functions."""
+    vp = C.c_void_p
+    L.orc_create.restype = vp
+    L.orc_create.argtypes = [vp]
+    L.orc_destroy.argtypes = [vp]
+    for name in ("orc_num_blocks", "orc_block_ranges", "orc_block_flags", "orc_get_background",
+                 "orc_ghost_map", "orc_set_state", "orc_get_state", "orc_exchange",
+                 "orc_timestep", "orc_step", "orc_block_rhs", "orc_block_diffusion",
+                 "orc_block_grid", "orc_phase", "orc_get_stage_state", "orc_save_allcells",
+                 "orc_set_background"):
+        getattr(L, name).restype = C.c_int
+    L.orc_ghost_count.restype = C.c_int64
+    L.orc_ghost_count.argtypes = [vp]
+    L.orc_uncovered_ghosts.restype = C.c_int64
+    L.orc_uncovered_ghosts.argtypes = [vp]
+    L.orc_num_threads.restype = C.c_int
+    L.orc_dt.restype = C.c_double
+    L.orc_dt.argtypes = [vp]
+    L.orc_hc_halo.restype = C.c_int64
+    for name in ("orc_pfss_operator", "orc_spmv", "orc_halo_fill", "orc_find_leaf", "orc_mg_restrict",
+                 "orc_mg_prolong_add", "orc_mg_rbgs"):
+        getattr(L, name).restype = C.c_int
+    return L
 
 
 def _ptr(a):
@@ -63,8 +77,8 @@ def _ptr(a):
 class Oracle:
     """The reference step restated on the CPU, one instance per grid."""
 
-    def __init__(self, cfg):
-        self.L = lib()
+    def __init__(self, cfg, timing=False):
+        self.L = lib(timing)
         self.cfg = cfg
         self.h = self.L.orc_create(C.byref(cfg))
         nb, ny = C.c_int32(), C.c_int32()
@@ -301,9 +315,9 @@ def vec_conv(rtp, v):
     return out
 
 
-def set_threads(n):
-    lib().orc_set_threads(C.c_int(n))
+def set_threads(n, timing=False):
+    lib(timing).orc_set_threads(C.c_int(n))
 
 
-def num_threads():
-    return int(lib().orc_num_threads())
+def num_threads(timing=False):
+    return int(lib(timing).orc_num_threads())

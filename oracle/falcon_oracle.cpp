@@ -495,8 +495,13 @@ void Oracle::gc_sources() {
 }
 
 void Oracle::exchange(bool rk) {
-    // 3_6/ModCommunication.f90:678-721 (single rank: every target is local)
-    for (auto& S : blk) {
+    // 3_6/ModCommunication.f90:678-721 (single rank: every target is local).
+    // Source blocks in parallel, as the reference's ranks run them: every
+    // ghost cell is written by exactly one entry, and the interpolation reads
+    // a source's own ghost cells only with a zero weight.
+#pragma omp parallel for schedule(dynamic, 4)
+    for (size_t sb = 0; sb < blk.size(); ++sb) {
+        Block& S = blk[sb];
         const std::vector<double>& f = rk ? S.urk : S.u;
         double dxi = S.xi[2 + ng - 1] - S.xi[1 + ng - 1];
         double dxj = S.xj[2 + ng - 1] - S.xj[1 + ng - 1];
