@@ -520,7 +520,8 @@ def solver_bench(device):
     sv.solve(tol=1e-8, max_iter=300, precond=S.PRECOND_MG, check=False)
     mg = sv.solve(tol=1e-8, max_iter=300, precond=S.PRECOND_MG, check=False)
     cg = sv.solve(tol=1e-8, max_iter=3000, precond=S.PRECOND_NONE, check=False)
-    out["conduction_64x128x384"] = {"cells": sv.nblocks * sv.nint, "tol": 1e-8, "mg_pcg": mg, "plain_cg": cg}
+    out["conduction_64x128x384"] = {"cells": sv.nblocks * sv.nint, "tol": 1e-8, "mg_pcg": mg, "plain_cg": cg,
+                                     "tile": sv.tuning()}
     sv.close()
     # training pairs from real solves: 3 systems x 4 right-hand sides
     X, T = [], []
@@ -554,7 +555,10 @@ def solver_bench(device):
     rep = sv.solve(tol=1e-10, max_iter=300, precond=S.PRECOND_MG, check=False)
     rel = sv.problem_residuals()
     out["pfss_batch64"] = {"problems": 64, "cells": sv.nblocks * sv.nint, "tol": 1e-10, "mg_pcg": rep,
-                           "fp64_residual_per_problem": {"max": float(rel.max()), "median": float(np.median(rel))}}
+                           "fp64_residual_per_problem": {"max": float(rel.max()), "median": float(np.median(rel))},
+                           "tile": sv.tuning(),
+                           "graph_launches": "one per inner solve (a device-side WHILE loop of FCG iterations, "
+                                             "V-cycle included), one FP64 residual check per refinement pass"}
     sv.close()
     out["wall_s"] = round(time.time() - t0, 1)
     return out

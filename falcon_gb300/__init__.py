@@ -56,6 +56,7 @@ EXPORTS = (
     "falcon_set_background", "falcon_solver_set_operator", "falcon_solver_set_magnetogram",
     "falcon_solver_magnetogram", "falcon_solver_set_guess", "falcon_solver_block_ranges",
     "falcon_solver_block_flags", "falcon_solver_magnetogram_sources", "falcon_solver_vcycle_op",
+    "falcon_solver_tuning", "falcon_solver_set_tile",
 )
 
 # size of the static device array behind falcon_download_state_range

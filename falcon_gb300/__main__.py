@@ -1,0 +1,60 @@
+"""Command line: advance a named Yin-Yang MHD workload on a GPU and print the
+device time per step.
+
+    python -m falcon_gb300 --workload shell_fp64_442k --steps 10 --warmup 3
+    python -m falcon_gb300 --workload shell_mixed_21m --steps 20
+
+Workloads:
+  shell_fp64_442k  plain FP64 shell, per panel 32 x 48 x 144 cells in 8^3
+                   blocks (864 blocks, 442,368 cells), bit-identical to the oracle
+  shell_fp64_21m   the 21,233,664-cell shell (16^3 blocks) in FP64
+  shell_mixed_21m  the same shell in the mixed precision of the benchmark
+  shell_mixed_5m   the same physics at 1/4 of the blocks (1,296 blocks of 16^3,
+                   5,308,416 cells): the profiling case
+Initial state: kind 1 of falcon_init_synthetic (entropy bump, dipole B and a
+random-phase Kolmogorov velocity at rms Mach 0.01, seed 1002).
+"""
+import argparse
+import json
+import sys
+
+from . import Falcon, build, config
+
+WORKLOADS = {
+    "shell_fp64_442k": lambda d: config.shell_fp64_cpu(device=d),
+    "shell_fp64_21m": lambda d: config.shell_mixed_21m(precision=config.PREC_FP64, device=d),
+    "shell_mixed_21m": lambda d: config.shell_mixed_21m(device=d),
+    "shell_mixed_5m": lambda d: config.make_config(block=(16, 16, 16), root_tiles=(3, 3, 9), radial_levels=1,
+                                                   radial_option=1, amr=((0, 1, 1),), precision=config.PREC_MIXED,
+                                                   device=d),
+}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(prog="python -m falcon_gb300")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="shell_fp64_442k")
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--device", type=int, default=0)
+    a = ap.parse_args(argv)
+    build()
+    f = Falcon(WORKLOADS[a.workload](a.device))
+    f.init_synthetic(kind=1, seed=1002, mach=0.01)
+    f.exchange()
+    f.exchange()
+    f.run_steps(a.warmup)
+    f.synchronize()
+    f.timer_start()
+    f.run_steps(a.steps)
+    ms = f.timer_stop()
+    f.synchronize()
+    print(json.dumps({"workload": a.workload, "cells": f.interior_cells, "steps": a.steps,
+                      "ms_per_step": ms / max(a.steps, 1),
+                      "cell_updates_per_s": f.interior_cells * a.steps / (ms / 1e3) if ms > 0 else None,
+                      "tuning": f.tuning()}))
+    f.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

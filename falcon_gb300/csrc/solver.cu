@@ -42,6 +42,8 @@ struct LevelDims {
     int m0, m1, m2;        // interior
     int p0, p1, p2;        // padded (m+2)
     int nint, npad;
+    int chunk;             // cells per CTA (a multiple of m0; the solver's tuned tile)
+    int tpb;               // threads per CTA (<= 1024, a multiple of 32)
 };
 
 struct HaloList {
@@ -57,16 +59,16 @@ struct HaloList {
 struct Ops64 { const double *Aii, *Ai, *Aj, *Ak; };
 struct Ops32 { const float *Aii, *Ai, *Aj, *Ak; };
 
-// Launch geometry of the cell kernels: CTAs take chunks of kCellChunk cells,
+// Launch geometry of the cell kernels: CTAs take chunks of d.chunk cells,
 // block-major (consecutive CTAs stream consecutive memory); a chunk never
-// spans two blocks, so a CTA's reductions go to one problem.
-constexpr int kCellChunk = 1024;
-__device__ __forceinline__ int cell_chunks(const LevelDims& d) { return (d.nint + kCellChunk - 1) / kCellChunk; }
+// spans two blocks, so a CTA's reductions go to one problem. The chunk and
+// the CTA size are the solver's tile shape, picked by its autotuner.
+__device__ __forceinline__ int cell_chunks(const LevelDims& d) { return (d.nint + d.chunk - 1) / d.chunk; }
 __device__ __forceinline__ int cell_block(const LevelDims& d) { return (int)(blockIdx.x / (unsigned)cell_chunks(d)); }
 __device__ __forceinline__ int cell_first(const LevelDims& d) {
-    return (int)(blockIdx.x % (unsigned)cell_chunks(d)) * kCellChunk;
+    return (int)(blockIdx.x % (unsigned)cell_chunks(d)) * d.chunk;
 }
-__device__ __forceinline__ int cell_end(const LevelDims& d) { return min(cell_first(d) + kCellChunk, d.nint); }
+__device__ __forceinline__ int cell_end(const LevelDims& d) { return min(cell_first(d) + d.chunk, d.nint); }
 
 __device__ __forceinline__ void cell_ijk(const LevelDims& d, int c, int& i, int& j, int& k) {
     i = c % d.m0 + 1;
@@ -93,7 +95,7 @@ template <class T>
 __device__ __forceinline__ void block_sum_atomic(T v, double* slot) {
     double s = (double)v;
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    __shared__ double ws[8];
+    __shared__ double ws[32];
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -294,7 +296,7 @@ __device__ __forceinline__ double ff_to(float2 a) { return (double)a.x + (double
 __device__ __forceinline__ void block_sum_atomic_ff(float2 v, double* slot) {
     for (int o = 16; o > 0; o >>= 1)
         v = ff_add(v, make_float2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o)));
-    __shared__ double ws[8];
+    __shared__ double ws[32];
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = ff_to(v);
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -428,6 +430,73 @@ __global__ void k_halo_ff(float2* v, HaloListFF H, const int32_t* cdst, const in
     v[H.dst[e]] = s;
 }
 
+// ---- the inner solve's loop control on the device -----------------------------
+// One inner solve (an FCG on the correction equation) runs as one graph launch:
+// a first iteration, then a WHILE node whose body is one more iteration; the
+// last kernel of every iteration decides, on the device, whether the loop goes
+// on. The loop is bounded: it counts its iterations and stops at max_it.
+struct InnerCtl {
+    int32_t it;        // iterations done by this inner solve
+    int32_t max_it;    // its iteration limit (<= kInnerCap)
+    int32_t stalled;   // the largest relative residual fell by < 5% over 8 iterations
+    int32_t nan;       // a non-finite residual
+    int32_t cont;      // the loop condition written by the last check
+    int32_t pad_;
+    double hist[16];   // ring of the largest relative residual per iteration
+};
+constexpr int32_t kInnerCap = 100000;
+
+// After an iteration's x/r update: each problem's relative recursive residual
+// h = sqrt(r.r / r0.r0); a problem at or below its eta leaves the iteration
+// (active = 0: no further update). One CTA of 256 threads, problem per thread
+// (nproblems <= 256). With `set_cond`, sets the WHILE node's condition.
+__global__ void __launch_bounds__(256) k_inner_check(int np, const double* rr, const double* rr0, const double* eta,
+                                                     int32_t* active, InnerCtl* ctl, cudaGraphConditionalHandle h,
+                                                     int set_cond) {
+    __shared__ double smax[256];
+    __shared__ int sany[256], snan[256];
+    const int q = threadIdx.x;
+    double hq = 0.0;
+    int still = 0, bad = 0;
+    if (q < np && active[q]) {
+        hq = sqrt(rr[q] / rr0[q]);
+        if (!(hq == hq) || hq > 1e300) {
+            bad = 1;
+        } else if (hq <= eta[q]) {
+            active[q] = 0;
+        } else {
+            still = 1;
+        }
+    }
+    smax[q] = hq;
+    sany[q] = still;
+    snan[q] = bad;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (q < o) {
+            smax[q] = fmax(smax[q], smax[q + o]);
+            sany[q] |= sany[q + o];
+            snan[q] |= snan[q + o];
+        }
+        __syncthreads();
+    }
+    if (q == 0) {
+        const int it = ctl->it + 1;
+        ctl->it = it;
+        if (snan[0]) ctl->nan = 1;
+        int stalled = ctl->stalled;
+        if (sany[0]) {
+            ctl->hist[it & 15] = smax[0];
+            if (it > 10 && smax[0] > 0.95 * ctl->hist[(it - 8) & 15]) stalled = 1;
+        }
+        ctl->stalled = stalled;
+        const int cap = ctl->max_it < kInnerCap ? ctl->max_it : kInnerCap;
+        const int cont = (sany[0] && !stalled && !snan[0] && it < cap) ? 1 : 0;
+        ctl->cont = cont;
+        if (set_cond) cudaGraphSetConditional(h, (unsigned)cont);
+    }
+}
+
 // ---- FP64 iterative refinement around the float-float solve ------------------
 // r' = r / sr per problem as FF pairs (sr a power of two at or above ||r||_2:
 // exact, and |r'| <= 1), its FP32 part for the V-cycle, and rr += r'.r'
@@ -489,7 +558,7 @@ __device__ __forceinline__ void rbgs_cell(const Ops32& A, const LevelDims& d, co
 
 __global__ void k_rbgs(Ops32 A, LevelDims d, const float* r, float* z, int colour) {
     const int b = cell_block(d), c0 = cell_first(d), c1 = cell_end(d);
-    if ((d.m0 & 1) == 0 && kCellChunk % d.m0 == 0) {   // rows whole within a chunk
+    if ((d.m0 & 1) == 0 && d.chunk % d.m0 == 0) {   // rows whole within a chunk
         const int half = d.m0 >> 1;
         for (int h = (c0 >> 1) + threadIdx.x; h < (c1 >> 1); h += blockDim.x) {
             const int row = h / half, ih = h - row * half;
@@ -747,9 +816,21 @@ struct falcon_solver {
     int rec_max = 0, rec_n = 0;
     // one instantiated CUDA graph per V-cycle shape (smoothing sweeps, network on/off)
     std::map<int64_t, cudaGraphExec_t> vgraphs;
+    // one instantiated graph per inner-solve shape: a first iteration and a
+    // device-controlled WHILE loop of iterations (the V-cycle inside it)
+    std::map<int64_t, cudaGraphExec_t> igraphs;
+    bool capturing = false;               // enqueueing into a graph: the V-cycle's kernels inline
+    InnerCtl* ictl = nullptr;             // device loop control
+    double *rr0 = nullptr, *eta = nullptr;   // device, per problem
+    // tile shape of the cell kernels (cells per CTA, threads per CTA), tuned at the first solve
+    int tile_chunk = 1024, tile_tpb = 256;
+    bool tuned = false;
+    double tuned_ms = 0;                  // time of one timed iteration with the chosen tile
     void clear_graphs() {
         for (auto& kv : vgraphs) cudaGraphExecDestroy(kv.second);
         vgraphs.clear();
+        for (auto& kv : igraphs) cudaGraphExecDestroy(kv.second);
+        igraphs.clear();
     }
     int fail(int c, const std::string& m) { err = m; return c; }
     // zero-filled; the fill completes before returning: the uploads that follow
@@ -778,14 +859,13 @@ struct falcon_solver {
 
 namespace {
 
-// grid.x = block (up to 2^31-1 blocks), grid.y = 256-cell chunk of the block
-// CTAs over (block, chunk of kCellChunk cells), block-major: consecutive CTAs
+// CTAs over (block, chunk of d.chunk cells), block-major: consecutive CTAs
 // stream consecutive memory, and each per-problem reduction takes one atomic
 // per chunk.
 dim3 grid_cells(const LevelDims& d, int nblocks) {
-    return dim3((unsigned)nblocks * (unsigned)((d.nint + kCellChunk - 1) / kCellChunk));
+    return dim3((unsigned)nblocks * (unsigned)((d.nint + d.chunk - 1) / d.chunk));
 }
-unsigned tpb(const LevelDims& d) { return (unsigned)std::min(256, (d.nint + 31) / 32 * 32); }
+unsigned tpb(const LevelDims& d) { return (unsigned)std::min(d.tpb, (std::min(d.nint, d.chunk) + 31) / 32 * 32); }
 
 template <class T> cudaError_t halo_fill(falcon_solver* sv, int l, T* v) {
     const SvLevel& L = sv->lv[l];
@@ -914,7 +994,7 @@ cudaError_t vcycle_body(falcon_solver* sv) {
 // captured once per shape and replayed (recording calls run eagerly: their
 // destination changes from call to call)
 cudaError_t vcycle(falcon_solver* sv) {
-    if (sv->rec) return vcycle_body(sv);
+    if (sv->rec || sv->capturing) return vcycle_body(sv);
     const int64_t key = (int64_t)(sv->use_net ? 1 : 0) | ((int64_t)sv->nu_pre << 1) | ((int64_t)sv->nu_post << 8) |
                         ((int64_t)sv->nu_coarse << 15) | ((int64_t)sv->net_sweeps << 28);
     auto it = sv->vgraphs.find(key);
@@ -950,6 +1030,8 @@ int setup(falcon_solver* sv) {
         L.d.p0 = H.m[0] + 2; L.d.p1 = H.m[1] + 2; L.d.p2 = H.m[2] + 2;
         L.d.nint = H.nint();
         L.d.npad = L.d.p0 * L.d.p1 * L.d.p2;
+        L.d.chunk = sv->tile_chunk;
+        L.d.tpb = sv->tile_tpb;
         auto up64 = [&](double** d, const std::vector<double>& h) -> cudaError_t {
             cudaError_t e = sv->alloc(d, h.size() * 8);
             if (e == cudaSuccess) e = cudaMemcpy(*d, h.data(), h.size() * 8, cudaMemcpyHostToDevice);
@@ -1091,6 +1173,9 @@ int setup(falcon_solver* sv) {
     SCK(sv->alloc(&sv->bvec, (size_t)nb * d0.nint * 8), "vectors");
     SCK(sv->alloc(&sv->dots, (size_t)6 * S.nproblems * 8), "scalars");
     SCK(sv->alloc(&sv->ir_par, (size_t)2 * S.nproblems * 8), "scalars");
+    SCK(sv->alloc(&sv->rr0, (size_t)S.nproblems * 8), "scalars");
+    SCK(sv->alloc(&sv->eta, (size_t)S.nproblems * 8), "scalars");
+    SCK(sv->alloc(&sv->ictl, sizeof(InnerCtl)), "scalars");
     SCK(sv->alloc(&sv->active, (size_t)S.nproblems * 4), "scalars");
     SCK(sv->alloc(&sv->bprob, (size_t)nb * 4), "scalars");
     SCK(cudaMemcpy(sv->bvec, S.b.data(), S.b.size() * 8, cudaMemcpyHostToDevice), "rhs");
@@ -1310,6 +1395,182 @@ bool all_finite(const double* v, size_t n) {
     return true;
 }
 
+// ---- the inner solve: one FCG iteration, as a graph or eagerly ----------------
+// One iteration unit on the stream. `first`: z = M r, p = z (restart); else
+// z = M r, beta = -z.Ap / p.Ap, p = z + beta p. Then the halo of p, q = A p
+// with p.q and p.r, alpha, x += alpha p, r -= alpha q with r.r, and the
+// device-side check (k_inner_check), which sets the WHILE condition when
+// `set_cond`. Inactive problems take no step.
+cudaError_t enqueue_iteration(falcon_solver* sv, int pc, bool first, cudaGraphConditionalHandle h, int set_cond) {
+    const int nb = sv->S.nblocks, np = sv->S.nproblems;
+    const LevelDims& d = sv->lv[0].d;
+    const dim3 g = grid_cells(d, nb);
+    cudaError_t e = cudaSuccess;
+    if (pc != FALCON_PRECOND_NONE) {
+        sv->use_net = pc == FALCON_PRECOND_MG_LCC;
+        e = vcycle(sv);
+        sv->use_net = false;
+        if (e != cudaSuccess) return e;
+    }
+    k_take_z_ff<<<g, tpb(d), 0, sv->st>>>(d, sv->lv[0].z, sv->dsA, sv->r2, pc == FALCON_PRECOND_NONE, sv->z2, sv->Ap2,
+                                          sv->D(), first ? 0 : 1);
+    k_update_p_ff<<<g, tpb(d), 0, sv->st>>>(d, sv->p2, sv->z2, sv->D(), first ? 1 : 0);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = halo_fill_ff(sv, sv->p2);
+    if (e == cudaSuccess) e = cudaMemsetAsync(sv->dots, 0, (size_t)4 * np * 8, sv->st);
+    if (e != cudaSuccess) return e;
+    k_spmv_dots_ff<<<g, tpb(d), 0, sv->st>>>(sv->lv[0].ops2(), d, sv->p2, sv->Ap2, sv->r2, sv->D());
+    k_update_xr_ff<<<g, tpb(d), 0, sv->st>>>(d, sv->x2, sv->p2, sv->r2, sv->Ap2, sv->lv[0].r, sv->D());
+    k_inner_check<<<1, 256, 0, sv->st>>>(np, sv->dots + 3 * np, sv->rr0, sv->eta, sv->active, sv->ictl, h, set_cond);
+    return cudaGetLastError();
+}
+
+// The inner solve as one graph: the first iteration, then a WHILE node whose
+// body is a continuing iteration; the loop runs on the device until every
+// problem reached its eta, the residual stalls, or max_it (k_inner_check).
+cudaError_t build_inner_graph(falcon_solver* sv, int pc, cudaGraphExec_t* out) {
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    if (e != cudaSuccess) return e;
+    cudaGraphConditionalHandle h;
+    e = cudaGraphConditionalHandleCreate(&h, g, 0, 0);
+    sv->capturing = true;
+    if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(sv->st, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        const cudaError_t eb = enqueue_iteration(sv, pc, true, h, 1);
+        e = cudaStreamEndCapture(sv->st, &g);
+        if (eb != cudaSuccess) e = eb;
+    }
+    // the captured chain's last node is the check; the WHILE node follows it
+    std::vector<cudaGraphNode_t> leaves;
+    if (e == cudaSuccess) {
+        size_t nn = 0, ne = 0;
+        e = cudaGraphGetNodes(g, nullptr, &nn);
+        std::vector<cudaGraphNode_t> nodes(nn);
+        if (e == cudaSuccess) e = cudaGraphGetNodes(g, nodes.data(), &nn);
+        if (e == cudaSuccess) e = cudaGraphGetEdges(g, nullptr, nullptr, nullptr, &ne);
+        std::vector<cudaGraphNode_t> from(ne), to(ne);
+        if (e == cudaSuccess && ne) e = cudaGraphGetEdges(g, from.data(), to.data(), nullptr, &ne);
+        for (cudaGraphNode_t n : nodes)
+            if (std::find(from.begin(), from.end(), n) == from.end()) leaves.push_back(n);
+    }
+    if (e == cudaSuccess) {
+        cudaGraphNodeParams p = {};
+        p.type = cudaGraphNodeTypeConditional;
+        p.conditional.handle = h;
+        p.conditional.type = cudaGraphCondTypeWhile;
+        p.conditional.size = 1;
+        cudaGraphNode_t wn;
+        e = cudaGraphAddNode(&wn, g, leaves.data(), nullptr, leaves.size(), &p);
+        if (e == cudaSuccess) {
+            cudaGraph_t body = p.conditional.phGraph_out[0];
+            e = cudaStreamBeginCaptureToGraph(sv->st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                const cudaError_t eb = enqueue_iteration(sv, pc, false, h, 1);
+                e = cudaStreamEndCapture(sv->st, &body);
+                if (eb != cudaSuccess) e = eb;
+            }
+        }
+    }
+    sv->capturing = false;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(out, g, 0);
+    if (g) cudaGraphDestroy(g);
+    return e;
+}
+
+// One inner solve from the current r2 (x2 = 0): the graph when the solve is
+// not recording coarse residuals, else the same iterations eagerly with the
+// host reading the loop control after each. Fills ctl (host copy).
+cudaError_t run_inner(falcon_solver* sv, int pc, int max_it, InnerCtl* ctl) {
+    InnerCtl c0;
+    std::memset(&c0, 0, sizeof c0);
+    c0.max_it = std::max(1, std::min(max_it, kInnerCap));
+    cudaError_t e = cudaMemcpyAsync(sv->ictl, &c0, sizeof c0, cudaMemcpyHostToDevice, sv->st);
+    if (e != cudaSuccess) return e;
+    if (!sv->rec) {
+        const int64_t key = (int64_t)pc | ((int64_t)sv->nu_pre << 4) | ((int64_t)sv->nu_post << 12) |
+                            ((int64_t)sv->nu_coarse << 20) | ((int64_t)sv->net_sweeps << 34);
+        auto it = sv->igraphs.find(key);
+        if (it == sv->igraphs.end()) {
+            cudaGraphExec_t x = nullptr;
+            e = build_inner_graph(sv, pc, &x);
+            if (e != cudaSuccess) return e;
+            it = sv->igraphs.emplace(key, x).first;
+        }
+        e = cudaGraphLaunch(it->second, sv->st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(ctl, sv->ictl, sizeof *ctl, cudaMemcpyDeviceToHost, sv->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(sv->st);
+        return e;
+    }
+    for (bool first = true;; first = false) {
+        e = enqueue_iteration(sv, pc, first, 0, 0);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(ctl, sv->ictl, sizeof *ctl, cudaMemcpyDeviceToHost, sv->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(sv->st);
+        if (e != cudaSuccess || !ctl->cont) return e;
+    }
+}
+
+// The tile shape of every cell kernel (all levels); launch shapes are baked
+// into the captured graphs, so they go.
+void apply_tile(falcon_solver* sv, int chunk, int tpb_) {
+    sv->tile_chunk = chunk;
+    sv->tile_tpb = tpb_;
+    for (SvLevel& L : sv->lv) {
+        L.d.chunk = chunk;
+        L.d.tpb = tpb_;
+    }
+    sv->clear_graphs();
+}
+
+// The solver's autotuner: times one eager FCG iteration (V-cycle with the
+// solver's smoothing, the float-float kernels, halo fills) for each candidate
+// tile -- cells per CTA in {512, 1024, 2048, 4096} (a multiple of the row
+// length, so the red-black sweep's colour-only form applies) x threads per
+// CTA in {128, 256, 512} -- on this solver's own grid, and keeps the fastest.
+// Runs once, at the first solve, on scratch vectors that the solve
+// initialises afterwards.
+int autotune_tile(falcon_solver* sv) {
+    if (sv->tuned) return FALCON_OK;
+    const int np = sv->S.nproblems;
+    const int m0 = sv->lv[0].d.m0;
+    std::vector<int32_t> act(np, 1);
+    std::vector<double> ones(np, 1.0), zeros(np, 0.0);
+    SCK(cudaMemcpyAsync(sv->active, act.data(), np * 4, cudaMemcpyHostToDevice, sv->st), "tune");
+    SCK(cudaMemcpyAsync(sv->rr0, ones.data(), np * 8, cudaMemcpyHostToDevice, sv->st), "tune");
+    SCK(cudaMemcpyAsync(sv->eta, zeros.data(), np * 8, cudaMemcpyHostToDevice, sv->st), "tune");
+    SCK(cudaStreamSynchronize(sv->st), "tune");
+    const int pc = sv->S.nlevels > 1 ? FALCON_PRECOND_MG : FALCON_PRECOND_NONE;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    float best = 1e30f;
+    int bc = sv->tile_chunk, bt = sv->tile_tpb;
+    for (int chunk : {512, 1024, 2048, 4096}) {
+        if (chunk % m0) continue;
+        for (int t : {128, 256, 512}) {
+            apply_tile(sv, chunk, t);
+            InnerCtl c0;
+            std::memset(&c0, 0, sizeof c0);
+            c0.max_it = kInnerCap;
+            SCK(cudaMemcpyAsync(sv->ictl, &c0, sizeof c0, cudaMemcpyHostToDevice, sv->st), "tune");
+            SCK(enqueue_iteration(sv, pc, false, 0, 0), "tune");   // warm-up
+            cudaEventRecord(a, sv->st);
+            for (int r = 0; r < 2; ++r) SCK(enqueue_iteration(sv, pc, false, 0, 0), "tune");
+            cudaEventRecord(b, sv->st);
+            SCK(cudaEventSynchronize(b), "tune");
+            float ms = 0;
+            cudaEventElapsedTime(&ms, a, b);
+            if (ms < best) { best = ms; bc = chunk; bt = t; }
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    apply_tile(sv, bc, bt);
+    sv->tuned = true;
+    sv->tuned_ms = best / 2.0;
+    return FALCON_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1406,6 +1667,32 @@ int falcon_solver_vcycle_op(falcon_solver* sv, int32_t op, int32_t level, const 
         SCK(cudaMemcpyAsync(out, L.res, nf * 4, cudaMemcpyDeviceToHost, sv->st), "vcycle op");
     }
     SCK(cudaStreamSynchronize(sv->st), "vcycle op");
+    return FALCON_OK;
+}
+
+int falcon_solver_tuning(const falcon_solver* sv, int32_t* tile, double* ms_per_iteration) {
+    if (!sv || !tile) return FALCON_ERR_INVALID_ARG;
+    tile[0] = sv->tile_chunk;
+    tile[1] = sv->tile_tpb;
+    tile[2] = sv->tuned ? 1 : 0;
+    if (ms_per_iteration) *ms_per_iteration = sv->tuned_ms;
+    return FALCON_OK;
+}
+
+int falcon_solver_set_tile(falcon_solver* sv, int32_t cells_per_cta, int32_t threads_per_cta) {
+    if (!sv) return FALCON_ERR_INVALID_ARG;
+    if (cells_per_cta < 32 || cells_per_cta > (1 << 16) || (cells_per_cta & 31) || threads_per_cta < 32 ||
+        threads_per_cta > 1024 || (threads_per_cta & 31))
+        return sv->fail(FALCON_ERR_INVALID_ARG,
+                        "falcon_solver_set_tile: cells per CTA in [32, 65536] and threads per CTA in [32, 1024], "
+                        "both multiples of 32");
+    if (sv->st) {
+        cudaSetDevice(sv->device);
+        SCK(cudaStreamSynchronize(sv->st), "tile");
+    }
+    apply_tile(sv, cells_per_cta, threads_per_cta);
+    sv->tuned = true;   // the caller's shape: no autotuning
+    sv->tuned_ms = 0;
     return FALCON_OK;
 }
 
@@ -1651,6 +1938,13 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
     constexpr double kEps64 = 1.1102230246251565e-16;   // 2^-53
     constexpr double kEtaMin = 9.094947017729282e-13;   // 2^-40: float-float recursive residual limit
     constexpr int kMaxPasses = 30;
+    {
+        float* rec = sv->rec;   // the tuning iterations record nothing
+        sv->rec = nullptr;
+        const int rc = autotune_tile(sv);
+        sv->rec = rec;
+        if (rc) return rc;
+    }
     cudaEvent_t t0, t1;
     cudaEventCreate(&t0);
     cudaEventCreate(&t1);
@@ -1667,19 +1961,6 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
     std::vector<double> rr(np), bb(np), ab(np), rel(np, 0.0), prev(np, 0.0), rr0(np), eta(np);
     std::vector<double> inv_sr(np, 1.0), fac(np, 1.0);
     int pc = precond;   // FALCON_PRECOND_MG_LCC falls back to FALCON_PRECOND_MG on stagnation
-    auto precondition = [&](int want_zAp) -> cudaError_t {
-        cudaError_t e = cudaSuccess;
-        if (pc != FALCON_PRECOND_NONE) {
-            sv->use_net = pc == FALCON_PRECOND_MG_LCC;
-            e = vcycle(sv);
-            sv->use_net = false;
-            ++rep->vcycles;
-        }
-        if (e != cudaSuccess) return e;
-        k_take_z_ff<<<g, tpb(d), 0, sv->st>>>(d, sv->lv[0].z, sv->dsA, sv->r2, pc == FALCON_PRECOND_NONE, sv->z2, sv->Ap2,
-                                               sv->D(), want_zAp);
-        return cudaGetLastError();
-    };
     int it = 0, passes = 0;
     for (bool first = true;; first = false) {
         // FP64 true residual of every problem
@@ -1736,46 +2017,23 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
         SCK(cudaMemcpyAsync(rr0.data(), sv->dots + 3 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "rr");
         SCK(cudaStreamSynchronize(sv->st), "rr");
         for (int q = 0; q < np; ++q) if (!(rr0[q] > 0)) { rr0[q] = 1.0; act[q] = 0; }
-        std::vector<double> hist;   // max over the inner-active problems of the relative recursive residual
-        SCK(precondition(0), "precondition");
-        k_update_p_ff<<<g, tpb(d), 0, sv->st>>>(d, sv->p2, sv->z2, sv->D(), 1);
-        SCK(halo_fill_ff(sv, sv->p2), "halo");
-        while (it < max_iter) {
-            ++it;
-            SCK(cudaMemsetAsync(sv->dots, 0, (size_t)4 * np * 8, sv->st), "dots");
-            k_spmv_dots_ff<<<g, tpb(d), 0, sv->st>>>(sv->lv[0].ops2(), d, sv->p2, sv->Ap2, sv->r2, sv->D());
-            k_update_xr_ff<<<g, tpb(d), 0, sv->st>>>(d, sv->x2, sv->p2, sv->r2, sv->Ap2, sv->lv[0].r, sv->D());
-            SCK(cudaGetLastError(), "iterate");
-            SCK(cudaMemcpyAsync(rr.data(), sv->dots + 3 * np, np * 8, cudaMemcpyDeviceToHost, sv->st), "rr");
-            SCK(cudaStreamSynchronize(sv->st), "rr");
-            bool all = true, changed = false;
-            double hmax = 0;
-            for (int q = 0; q < np; ++q) {
-                if (!act[q]) continue;
-                if (!std::isfinite(rr[q]))
-                    return sv->fail(FALCON_ERR_NAN_DETECTED, "solver: non-finite residual in problem " + std::to_string(q));
-                const double h = std::sqrt(rr[q] / rr0[q]);
-                hmax = std::max(hmax, h);
-                if (h <= eta[q]) { act[q] = 0; changed = true; } else { all = false; }
-            }
-            if (all) break;
-            if (changed) SCK(cudaMemcpyAsync(sv->active, act.data(), np * 4, cudaMemcpyHostToDevice, sv->st), "active");
-            hist.push_back(hmax);
-            const size_t nh = hist.size();
-            if (nh > 10 && hist[nh - 1] > 0.95 * hist[nh - 9]) {
-                // stagnation: less than 5% in 8 iterations
-                if (pc != FALCON_PRECOND_MG_LCC) break;   // the refinement restarts from the FP64 residual
-                pc = FALCON_PRECOND_MG;   // the learned stage stalls: plain MG for the rest, restarted
+        SCK(cudaMemcpyAsync(sv->active, act.data(), np * 4, cudaMemcpyHostToDevice, sv->st), "active");
+        SCK(cudaMemcpyAsync(sv->rr0, rr0.data(), np * 8, cudaMemcpyHostToDevice, sv->st), "inner start");
+        SCK(cudaMemcpyAsync(sv->eta, eta.data(), np * 8, cudaMemcpyHostToDevice, sv->st), "inner start");
+        // the inner FCG: one graph launch, its loop controlled on the device
+        for (;;) {
+            InnerCtl ctl;
+            SCK(run_inner(sv, pc, max_iter - it, &ctl), "inner solve");
+            it += ctl.it;
+            if (pc != FALCON_PRECOND_NONE) rep->vcycles += ctl.it;
+            if (ctl.nan) return sv->fail(FALCON_ERR_NAN_DETECTED, "solver: non-finite residual in the inner solve");
+            if (ctl.stalled && pc == FALCON_PRECOND_MG_LCC && it < max_iter) {
+                // the learned stage stalls: plain MG for the rest, restarted from the current iterate
+                pc = FALCON_PRECOND_MG;
                 ++rep->fallbacks;
-                hist.clear();
-                SCK(precondition(0), "precondition");
-                k_update_p_ff<<<g, tpb(d), 0, sv->st>>>(d, sv->p2, sv->z2, sv->D(), 1);
-                SCK(halo_fill_ff(sv, sv->p2), "halo");
                 continue;
             }
-            SCK(precondition(1), "precondition");
-            k_update_p_ff<<<g, tpb(d), 0, sv->st>>>(d, sv->p2, sv->z2, sv->D(), 0);
-            SCK(halo_fill_ff(sv, sv->p2), "halo");
+            break;   // done, stalled (the refinement restarts from the FP64 residual) or out of iterations
         }
         // x += d' sr / sA (inactive problems: d' = 0)
         k_ir_accum<<<g, tpb(d), 0, sv->st>>>(d, sv->x2, sv->ir_par + np, sv->bprob, sv->x);

@@ -43,7 +43,7 @@ _SYMS = ("falcon_solver_create", "falcon_solver_last_error", "falcon_solver_info
          "falcon_solver_set_smoothing", "falcon_solver_problem_residuals", "falcon_solver_set_operator",
          "falcon_solver_set_magnetogram", "falcon_solver_magnetogram", "falcon_solver_set_guess",
          "falcon_solver_block_ranges", "falcon_solver_block_flags", "falcon_solver_magnetogram_sources",
-         "falcon_solver_vcycle_op")
+         "falcon_solver_vcycle_op", "falcon_solver_tuning", "falcon_solver_set_tile")
 
 
 def _ptr(a):
@@ -207,6 +207,17 @@ class Solver:
         self._ck(self.L.falcon_solver_vcycle_op(self.h, C.c_int32(op), C.c_int32(level), _ptr(a),
                                                 None if b is None else _ptr(b), _ptr(out)))
         return out
+
+    def tuning(self):
+        """The tile shape of the cell kernels: cells and threads per CTA, whether
+        tuned (or set), and the tuner's time of one iteration with it."""
+        t = (C.c_int32 * 3)()
+        ms = C.c_double()
+        self._ck(self.L.falcon_solver_tuning(self.h, t, C.byref(ms)))
+        return {"cells_per_cta": t[0], "threads_per_cta": t[1], "tuned": bool(t[2]), "ms_per_iteration": ms.value}
+
+    def set_tile(self, cells_per_cta, threads_per_cta):
+        self._ck(self.L.falcon_solver_set_tile(self.h, C.c_int32(cells_per_cta), C.c_int32(threads_per_cta)))
 
     def block_ranges(self):
         out = np.zeros((self.nblocks, 3, 2))

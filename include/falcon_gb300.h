@@ -347,9 +347,14 @@ typedef struct falcon_solver_spec {
 /* A solve is an FP64 iterative refinement: r = b - A x and its norms in FP64,
  * an inner flexible-CG solve (float-float vectors, FP32 V-cycle) of the
  * correction equation A d = r, x += d in FP64; a problem is converged only
- * when its FP64 ||b - A x|| / ||b|| <= tol. falcon_solver_solve returns
- * FALCON_OK only when every problem converged, FALCON_ERR_NOT_CONVERGED
- * otherwise (the report is filled either way). */
+ * when its FP64 ||b - A x|| / ||b|| <= tol. Every problem of the batch is
+ * advanced by the same launches, and each inner solve is one CUDA-graph
+ * launch: a first iteration and a conditional WHILE node whose body is one
+ * iteration (V-cycle included), looping on the device until every problem
+ * reaches its inner tolerance, the residual stalls or the iteration budget
+ * runs out (bounded). falcon_solver_solve returns FALCON_OK only when every
+ * problem converged, FALCON_ERR_NOT_CONVERGED otherwise (the report is
+ * filled either way). */
 typedef struct falcon_solve_report {
     int32_t iterations;                /* inner iterations, all refinement passes */
     int32_t converged;                 /* 1: every problem's FP64 relative residual <= tol */
@@ -423,6 +428,16 @@ int  falcon_solver_set_operator(falcon_solver* sv, const double* Aii, const doub
 int  falcon_solver_set_magnetogram(falcon_solver* sv, const double* br);
 /* the current PFSS magnetogram in the same layout (0 off the bottom blocks) */
 int  falcon_solver_magnetogram(const falcon_solver* sv, double* br);
+/* Tile shape of the solver's cell kernels: each CTA takes a chunk of a
+ * block's cells (never two blocks, so its reductions go to one problem).
+ * Chosen by the solver's autotuner at its first solve -- every candidate
+ * (cells per CTA 512..4096 that are multiples of the row length, threads per
+ * CTA 128, 256 or 512) timed on one eager FCG iteration of this grid.
+ * tile[0] cells per CTA, tile[1] threads per CTA, tile[2] 1 once tuned or
+ * set; ms_per_iteration (may be NULL) the timed iteration of the choice.
+ * falcon_solver_set_tile fixes the shape instead (no autotuning). */
+int  falcon_solver_tuning(const falcon_solver* sv, int32_t* tile, double* ms_per_iteration);
+int  falcon_solver_set_tile(falcon_solver* sv, int32_t cells_per_cta, int32_t threads_per_cta);
 /* Verification: one kernel of the V-cycle on host arrays at `level`, eagerly
  * and synchronously (as falcon_step_phase is for the step). Arrays are FP32,
  * interior cells [block][k][j][i] of their level.

@@ -383,3 +383,26 @@ def test_gpu_pfss_batch64_error_per_solve_against_cpu_fp64_solve():
     assert (rel_gpu <= 1e-10).all()
     assert (rel_cpu <= 1e-13).all()
     assert err.max() <= 1e-7, err
+
+
+@pytest.mark.gpu
+def test_gpu_solver_tile_shapes_and_autotuner():
+    """The autotuner picks one of its candidate tiles at the first solve, and
+    every tile shape (cells and threads per CTA of the cell kernels) solves the
+    same batch to the same FP64 tolerance; each inner solve is one graph
+    launch with its loop on the device, so the iteration count does not
+    depend on the shape either."""
+    sv = S.Solver(S.pfss_spec([(24, 45), (40, 80)], device=0))
+    rep0 = sv.solve(tol=1e-10, max_iter=400)
+    t = sv.tuning()
+    print("tuned:", t, rep0)
+    assert t["tuned"] and t["cells_per_cta"] in (512, 1024, 2048, 4096) and t["threads_per_cta"] in (128, 256, 512)
+    x0 = sv.solution()
+    for chunk, tpb in ((512, 128), (4096, 512), (1024, 256)):
+        sv.set_tile(chunk, tpb)
+        rep = sv.solve(tol=1e-10, max_iter=400)
+        assert rep["converged"] == 1 and (sv.problem_residuals() <= 1e-10).all()
+        assert abs(rep["iterations"] - rep0["iterations"]) <= 2
+        assert np.abs(sv.solution() - x0).max() <= 1e-8 * np.abs(x0).max()
+    with pytest.raises(Exception):
+        sv.set_tile(100, 128)
