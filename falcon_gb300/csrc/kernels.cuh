@@ -203,6 +203,11 @@ cudaError_t launch_diffusion_fp64(const StepDims& d, const Geometry& g, double* 
 cudaError_t launch_cfl_fp64(const StepDims& d, const Geometry& g, const double* u, StepScalars* sc,
                             cudaStream_t st);
 cudaError_t launch_ghost_fp64(const StepDims& d, const GhostLists& gl, double* u, cudaStream_t st);
+// block sharding (FP64): outgoing entries of L into pack[n][8]; pack into the ghost cells dst[n]
+cudaError_t launch_shard_pack_fp64(const StepDims& d, const GhostInterpList& L, const double* u, double* pack,
+                                   cudaStream_t st);
+cudaError_t launch_shard_unpack_fp64(const StepDims& d, const int32_t* dst, int64_t n, const double* pack, double* u,
+                                     cudaStream_t st);
 
 // lo: the correction array of u^n (see lo_unit); the stage kernel updates it
 // at stage 4 only, the diffusion pass always; nullptr leaves u^n plain FP32.

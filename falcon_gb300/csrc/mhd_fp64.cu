@@ -31,6 +31,18 @@ cudaError_t launch_cfl_fp64(const StepDims& d, const Geometry& g, const double* 
 cudaError_t launch_ghost_fp64(const StepDims& d, const GhostLists& gl, double* u, cudaStream_t st) {
     return ghost_any<double>(d, gl, u, st);
 }
+cudaError_t launch_shard_pack_fp64(const StepDims& d, const GhostInterpList& L, const double* u, double* pack,
+                                   cudaStream_t st) {
+    if (L.n == 0) return cudaSuccess;
+    impl::k_shard_pack<double><<<(unsigned)((L.n + 127) / 128), 128, 0, st>>>(u, L, d.ncell, d.nip, d.nip * d.njp, pack);
+    return cudaGetLastError();
+}
+cudaError_t launch_shard_unpack_fp64(const StepDims& d, const int32_t* dst, int64_t n, const double* pack, double* u,
+                                     cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    impl::k_shard_unpack<double><<<(unsigned)((n + 127) / 128), 128, 0, st>>>(u, dst, n, d.ncell, pack);
+    return cudaGetLastError();
+}
 
 // dt = min(1.e20, CFL*min(h/v_wave)) (3_6/ModTimeStep.f90:20-29); also the
 // per-stage FP32 factors of the mixed path and the reset of the accumulator.

@@ -1129,11 +1129,26 @@ __device__ __forceinline__ void ghost_lin_one(T* u, const GhostLinList& L, int n
     for (int q = 0; q < NV; ++q) u[d + (size_t)q * ncell] = v[q];
 }
 
+// The values of one interpolated/rotated ghost entry (into val); the FP64
+// path is the reference's trilinear form and operand order.
+template <class T>
+__device__ __forceinline__ void ghost_interp_vals(const T* u, const GhostInterpList& L, int ncell, int nip, int pl,
+                                                  int64_t e, T* val);
+
 template <class T>
 __device__ __forceinline__ void ghost_interp_one(T* u, const GhostInterpList& L, int ncell, int nip, int pl, int64_t e) {
+    T val[NV];
+    ghost_interp_vals(u, L, ncell, nip, pl, e, val);
+    const size_t dd = (size_t)L.dst[e];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) u[dd + (size_t)v * ncell] = val[v];
+}
+
+template <class T>
+__device__ __forceinline__ void ghost_interp_vals(const T* u, const GhostInterpList& L, int ncell, int nip, int pl,
+                                                  int64_t e, T* val) {
     const int kind = L.kind[e];
     const size_t s = (size_t)L.src[e];
-    T val[NV];
     if constexpr (!Pol<T>::exact) {
         // FP32 weights; the Yin-Yang seam is aligned in r (wi == 0 after
         // snapping), so most entries are bilinear in (j, k): 4 source points
@@ -1166,9 +1181,6 @@ __device__ __forceinline__ void ghost_interp_one(T* u, const GhostInterpList& L,
             val[V_VT] = -(a * x2) - c * x3;
             val[V_VP] = -(a * x3) + c * x2;
         }
-        const size_t dd = (size_t)L.dst[e];
-#pragma unroll
-        for (int v = 0; v < NV; ++v) u[dd + (size_t)v * ncell] = val[v];
         return;
     }
     if (kind & 1) {
@@ -1194,9 +1206,30 @@ __device__ __forceinline__ void ghost_interp_one(T* u, const GhostInterpList& L,
         val[V_VT] = -(a * x2) - c * x3;
         val[V_VP] = -(a * x3) + c * x2;
     }
-    const size_t dd = (size_t)L.dst[e];
+}
+
+// ---- block sharding: the entries that cross ranks ---------------------------
+// The sender evaluates each outgoing ghost entry from its own blocks (the
+// same values as the single-GPU ghost fill) into a pack buffer pack[e][NV];
+// the receiver writes pack[e] into its ghost cells (dst[e], the entries in
+// the same order), as the reference's per-peer send/receive buffers
+// (3_6/ModCommunication.f90:725-765).
+template <class T>
+__global__ void __launch_bounds__(128) k_shard_pack(const T* u, GhostInterpList L, int ncell, int nip, int pl, T* pack) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= L.n) return;
+    T val[NV];
+    ghost_interp_vals(u, L, ncell, nip, pl, e, val);
 #pragma unroll
-    for (int v = 0; v < NV; ++v) u[dd + (size_t)v * ncell] = val[v];
+    for (int v = 0; v < NV; ++v) pack[e * NV + v] = val[v];
+}
+template <class T>
+__global__ void __launch_bounds__(128) k_shard_unpack(T* u, const int32_t* dst, int64_t n, int ncell, const T* pack) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const size_t d = (size_t)dst[e];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) u[d + (size_t)v * ncell] = pack[e * NV + v];
 }
 
 template <class T>

@@ -1922,7 +1922,6 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
     const SolverProblemSet& S = sv->S;
     const int nb = S.nblocks, np = S.nproblems;
     const LevelDims& d = sv->lv[0].d;
-    const dim3 g = grid_cells(d, nb);
     std::memset(rep, 0, sizeof *rep);
     // Structure (ModLinearSolver_Multigrid_CG, 3_5/ModLinearSolver.f90:313-427,
     // made an FP64 iterative refinement):
@@ -1945,6 +1944,8 @@ int falcon_solver_solve(falcon_solver* sv, double tol, int32_t max_iter, int32_t
         sv->rec = rec;
         if (rc) return rc;
     }
+    // the launch grid of the tuned tile (the autotuner may just have changed it)
+    const dim3 g = grid_cells(d, nb);
     cudaEvent_t t0, t1;
     cudaEventCreate(&t0);
     cudaEventCreate(&t1);

@@ -299,6 +299,11 @@ struct Oracle {
     Tree tree;
     std::vector<Block> blk;
     double dt = 0.0;
+    // a rank of a block-sharded run owns blocks [own_first, own_last): the
+    // phases, the time step and the exchange then cover owned blocks only
+    // (own_last < 0: every block)
+    int own_first = 0, own_last = -1;
+    bool owned(int b) const { return own_last < 0 || (b >= own_first && b < own_last); }
     std::string err;
 
     int idx(int i, int j, int k) const { return (i + ng - 1) + nip * ((j + ng - 1) + njp * (k + ng - 1)); }
@@ -312,6 +317,9 @@ struct Oracle {
     void gc_targets(Block& b);
     void gc_sources();
     void exchange(bool rk);
+    // one ghost entry's values from source block S (ModMath_1D3D_interpolate_1D1D
+    // and, across the Yin-Yang seam, ModYinYang_VecConv_1D)
+    void interp(const Block& S, bool rk, const double* x, bool rotate, double* val) const;
     void boundary(Block& b, std::vector<double>& p);
     void equation(Block& b, const std::vector<double>& p);
     void glm(Block& b, const std::vector<double>& p);
@@ -494,54 +502,61 @@ void Oracle::gc_sources() {
         }
 }
 
+void Oracle::interp(const Block& S, bool rk, const double* x, bool rotate, double* val) const {
+    const std::vector<double>& f = rk ? S.urk : S.u;
+    double dxi = S.xi[2 + ng - 1] - S.xi[1 + ng - 1];
+    double dxj = S.xj[2 + ng - 1] - S.xj[1 + ng - 1];
+    double dxk = S.xk[2 + ng - 1] - S.xk[1 + ng - 1];
+    // ModMath_1D3D_interpolate_1D1D (3_6/ModMath.f90:250-293)
+    double pi_ = (double)((float)(-ng) + 1.0f) + (x[0] - S.xi[0]) / dxi;
+    double pj = (double)((float)(-ng) + 1.0f) + (x[1] - S.xj[0]) / dxj;
+    double pk = (double)((float)(-ng) + 1.0f) + (x[2] - S.xk[0]) / dxk;
+    pi_ = std::max(std::min(pi_, (double)((float)ni + 0.0f)), 1.0);
+    pj = std::max(std::min(pj, (double)((float)nj + 0.0f)), 1.0);
+    pk = std::max(std::min(pk, (double)((float)nk + 0.0f)), 1.0);
+    int i0 = (int)std::floor(pi_), j0 = (int)std::floor(pj), k0 = (int)std::floor(pk);
+    double wi = pi_ - i0, wj = pj - j0, wk = pk - k0;
+    for (int v = 0; v < nvar; ++v) {
+        const double* fv = &f[(size_t)v * ncell];
+        val[v] = fv[idx(i0, j0, k0)] * (1. - wi) * (1. - wj) * (1. - wk) +
+                 fv[idx(i0 + 1, j0, k0)] * (wi) * (1. - wj) * (1. - wk) +
+                 fv[idx(i0, j0 + 1, k0)] * (1. - wi) * (wj) * (1. - wk) +
+                 fv[idx(i0, j0, k0 + 1)] * (1. - wi) * (1. - wj) * (wk) +
+                 fv[idx(i0 + 1, j0 + 1, k0)] * (wi) * (wj) * (1. - wk) +
+                 fv[idx(i0, j0 + 1, k0 + 1)] * (1. - wi) * (wj) * (wk) +
+                 fv[idx(i0 + 1, j0, k0 + 1)] * (wi) * (1. - wj) * (wk) +
+                 fv[idx(i0 + 1, j0 + 1, k0 + 1)] * (wi) * (wj) * (wk);
+    }
+    if (rotate) {
+        // ModYinYang_VecConv_1D for B then v (3_6/ModCommunication.f90:695-702)
+        // B is rotated whenever the layout has B (br_ > 0), as in the reference
+        double o[3];
+        vec_conv(x, &val[BR], o);
+        val[BR] = o[0]; val[BT] = o[1]; val[BP] = o[2];
+        vec_conv(x, &val[VR], o);
+        val[VR] = o[0]; val[VT] = o[1]; val[VP] = o[2];
+    }
+}
+
 void Oracle::exchange(bool rk) {
     // 3_6/ModCommunication.f90:678-721 (single rank: every target is local).
     // Source blocks in parallel, as the reference's ranks run them: every
     // ghost cell is written by exactly one entry, and the interpolation reads
-    // a source's own ghost cells only with a zero weight.
+    // a source's own ghost cells only with a zero weight. A rank of a sharded
+    // run fills the entries whose source and target it owns; the others
+    // travel between ranks (orc_interp_entries, orc_write_ghosts).
 #pragma omp parallel for schedule(dynamic, 4)
     for (size_t sb = 0; sb < blk.size(); ++sb) {
+        if (!owned((int)sb)) continue;
         Block& S = blk[sb];
-        const std::vector<double>& f = rk ? S.urk : S.u;
-        double dxi = S.xi[2 + ng - 1] - S.xi[1 + ng - 1];
-        double dxj = S.xj[2 + ng - 1] - S.xj[1 + ng - 1];
-        double dxk = S.xk[2 + ng - 1] - S.xk[1 + ng - 1];
         for (auto& s : S.sources) {
+            if (!owned(s.other - 1)) continue;
             Block& T = blk[s.other - 1];
             std::vector<double>& tgt = rk ? T.urk : T.u;
             size_t n = s.ijk.size() / 3;
             for (size_t g = 0; g < n; ++g) {
-                // ModMath_1D3D_interpolate_1D1D (3_6/ModMath.f90:250-293)
-                const double* x = &s.x[3 * g];
-                double pi_ = (double)((float)(-ng) + 1.0f) + (x[0] - S.xi[0]) / dxi;
-                double pj = (double)((float)(-ng) + 1.0f) + (x[1] - S.xj[0]) / dxj;
-                double pk = (double)((float)(-ng) + 1.0f) + (x[2] - S.xk[0]) / dxk;
-                pi_ = std::max(std::min(pi_, (double)((float)ni + 0.0f)), 1.0);
-                pj = std::max(std::min(pj, (double)((float)nj + 0.0f)), 1.0);
-                pk = std::max(std::min(pk, (double)((float)nk + 0.0f)), 1.0);
-                int i0 = (int)std::floor(pi_), j0 = (int)std::floor(pj), k0 = (int)std::floor(pk);
-                double wi = pi_ - i0, wj = pj - j0, wk = pk - k0;
                 double val[FALCON_NVAR];
-                for (int v = 0; v < nvar; ++v) {
-                    const double* fv = &f[(size_t)v * ncell];
-                    val[v] = fv[idx(i0, j0, k0)] * (1. - wi) * (1. - wj) * (1. - wk) +
-                             fv[idx(i0 + 1, j0, k0)] * (wi) * (1. - wj) * (1. - wk) +
-                             fv[idx(i0, j0 + 1, k0)] * (1. - wi) * (wj) * (1. - wk) +
-                             fv[idx(i0, j0, k0 + 1)] * (1. - wi) * (1. - wj) * (wk) +
-                             fv[idx(i0 + 1, j0 + 1, k0)] * (wi) * (wj) * (1. - wk) +
-                             fv[idx(i0, j0 + 1, k0 + 1)] * (1. - wi) * (wj) * (wk) +
-                             fv[idx(i0 + 1, j0, k0 + 1)] * (wi) * (1. - wj) * (wk) +
-                             fv[idx(i0 + 1, j0 + 1, k0 + 1)] * (wi) * (wj) * (wk);
-                }
-                if (s.other_yin != S.yin) {
-                    // ModYinYang_VecConv_1D for B then v (3_6/ModCommunication.f90:695-702)
-                    // B is rotated whenever the layout has B (br_ > 0), as in the reference
-                    double o[3];
-                    vec_conv(x, &val[BR], o);
-                    val[BR] = o[0]; val[BT] = o[1]; val[BP] = o[2];
-                    vec_conv(x, &val[VR], o);
-                    val[VR] = o[0]; val[VT] = o[1]; val[VP] = o[2];
-                }
+                interp(S, rk, &s.x[3 * g], s.other_yin != S.yin, val);
                 int ti = s.ijk[3 * g], tj = s.ijk[3 * g + 1], tk = s.ijk[3 * g + 2];
                 for (int v = 0; v < nvar; ++v) tgt[(size_t)v * ncell + idx(ti, tj, tk)] = val[v];
             }
@@ -950,7 +965,9 @@ void Oracle::wave_speed(Block& b) {
 double Oracle::timestep() {
     // 3_6/ModTimeStep.f90:10-30
     double d = (double)1.e20f;
-    for (auto& b : blk) {
+    for (size_t ib = 0; ib < blk.size(); ++ib) {
+        if (!owned((int)ib)) continue;
+        const Block& b = blk[ib];
         double m = INFINITY;
         for (int q = 0; q < ni * nj * nk; ++q) m = std::min(m, b.h[q] / b.vwave[q]);
         double d1 = cfg.phys.cfl * m;
@@ -1007,7 +1024,8 @@ void Oracle::phase(int ph) {
     const int nb = (int)blk.size();
     if (ph == 0) {
 #pragma omp parallel for schedule(dynamic)
-        for (int b = 0; b < nb; ++b) wave_speed(blk[b]);
+        for (int b = 0; b < nb; ++b)
+            if (owned(b)) wave_speed(blk[b]);
         dt = timestep();
         return;
     }
@@ -1015,6 +1033,7 @@ void Oracle::phase(int ph) {
         const int rk = ph;
 #pragma omp parallel for schedule(dynamic)
         for (int ib = 0; ib < nb; ++ib) {
+            if (!owned(ib)) continue;
             Block& b = blk[ib];
             std::vector<double>& p = rk > 1 ? b.urk : b.u;
             boundary(b, p);
@@ -1034,6 +1053,7 @@ void Oracle::phase(int ph) {
     }
 #pragma omp parallel for schedule(dynamic)
     for (int ib = 0; ib < nb; ++ib) {
+        if (!owned(ib)) continue;
         Block& b = blk[ib];
         std::fill(b.R.begin(), b.R.end(), 0.0);
         diffusion(b, b.u);
@@ -1260,6 +1280,39 @@ int orc_get_state(void* h, double* u) {
 }
 int orc_phase(void* h, int32_t ph) { ((Oracle*)h)->phase(ph); return 0; }
 double orc_dt(void* h) { return ((Oracle*)h)->dt; }
+// ---- block sharding (a rank of a multi-rank run) -----------------------------
+int orc_set_owned(void* h, int32_t first, int32_t last) {
+    Oracle* o = (Oracle*)h;
+    o->own_first = first;
+    o->own_last = last;
+    return 0;
+}
+// the step's dt after the MIN over ranks (3_6/ModAdvance.f90:48)
+int orc_set_dt(void* h, double dt) { ((Oracle*)h)->dt = dt; return 0; }
+// values of ghost entries ent[n][5] = (target block, ti, tj, tk, source block)
+// (0-based blocks, Fortran cell indices) with source-frame centres x[n][3],
+// from the sources' stage buffer (rk) or state: out[n][nvar]
+int orc_interp_entries(void* h, int32_t rk, const int32_t* ent, const double* x, int64_t n, double* out) {
+    Oracle* o = (Oracle*)h;
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < n; ++e) {
+        const orc::Block& S = o->blk[ent[5 * e + 4]];
+        const orc::Block& T = o->blk[ent[5 * e]];
+        o->interp(S, rk != 0, x + 3 * e, T.yin != S.yin, out + (size_t)o->nvar * e);
+    }
+    return 0;
+}
+// write ghost values vals[n][nvar] into the target cells of ent[n][5]
+int orc_write_ghosts(void* h, int32_t rk, const int32_t* ent, int64_t n, const double* vals) {
+    Oracle* o = (Oracle*)h;
+    for (int64_t e = 0; e < n; ++e) {
+        orc::Block& T = o->blk[ent[5 * e]];
+        std::vector<double>& tgt = rk ? T.urk : T.u;
+        const int c = o->idx(ent[5 * e + 1], ent[5 * e + 2], ent[5 * e + 3]);
+        for (int v = 0; v < o->nvar; ++v) tgt[(size_t)v * o->ncell + c] = vals[(size_t)o->nvar * e + v];
+    }
+    return 0;
+}
 int orc_get_stage_state(void* h, double* u) {
     Oracle* o = (Oracle*)h;
     size_t n = (size_t)o->nvar * o->ncell;
