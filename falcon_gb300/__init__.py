@@ -32,6 +32,8 @@ ERR_NOT_CONVERGED = -5
 ERR_BOUNDS = -6
 ERR_UNCOVERED_GHOST = -7
 ERR_NO_DEVICE = -8
+SHARD_SEND = 0
+SHARD_RECV = 1
 
 # every symbol declared in include/falcon_gb300.h
 EXPORTS = (
@@ -56,7 +58,9 @@ EXPORTS = (
     "falcon_set_background", "falcon_solver_set_operator", "falcon_solver_set_magnetogram",
     "falcon_solver_magnetogram", "falcon_solver_set_guess", "falcon_solver_block_ranges",
     "falcon_solver_block_flags", "falcon_solver_magnetogram_sources", "falcon_solver_vcycle_op",
-    "falcon_solver_tuning", "falcon_solver_set_tile",
+    "falcon_solver_tuning", "falcon_solver_set_tile", "falcon_shard_ranges", "falcon_shard_plan",
+    "falcon_set_shard", "falcon_shard_counts", "falcon_shard_pack", "falcon_shard_unpack",
+    "falcon_shard_min_ratio", "falcon_shard_set_min_ratio",
 )
 
 # size of the static device array behind falcon_download_state_range
@@ -246,6 +250,50 @@ class Falcon:
 
     def synchronize(self):
         self._ck(self.L.falcon_synchronize(self.h))
+
+    # ---- block sharding over ranks
+    def shard_ranges(self, nranks):
+        """first[r] .. first[r+1]-1: rank r's blocks (ModAllocation_Init's partition)."""
+        out = np.zeros(nranks + 1, dtype=np.int32)
+        self._ck(self.L.falcon_shard_ranges(self.h, C.c_int32(nranks), _ptr(out)))
+        return out
+
+    def shard_plan(self, nranks, rank, peer, direction):
+        """Ghost-map indices of the entries rank sends to peer (SHARD_SEND) or
+        receives from it (SHARD_RECV), in map order."""
+        n = C.c_int64()
+        self._ck(self.L.falcon_shard_plan(self.h, C.c_int32(nranks), C.c_int32(rank), C.c_int32(peer),
+                                          C.c_int32(direction), None, C.c_int64(0), C.byref(n)))
+        out = np.zeros(n.value, dtype=np.int64)
+        self._ck(self.L.falcon_shard_plan(self.h, C.c_int32(nranks), C.c_int32(rank), C.c_int32(peer),
+                                          C.c_int32(direction), _ptr(out), C.c_int64(n.value), C.byref(n)))
+        return out
+
+    def set_shard(self, nranks, rank):
+        self._ck(self.L.falcon_set_shard(self.h, C.c_int32(nranks), C.c_int32(rank)))
+
+    def shard_counts(self, peer):
+        a, b = C.c_int64(), C.c_int64()
+        self._ck(self.L.falcon_shard_counts(self.h, C.c_int32(peer), C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def shard_pack(self, peer):
+        n, _ = self.shard_counts(peer)
+        buf = np.zeros((n, 8))
+        self._ck(self.L.falcon_shard_pack(self.h, C.c_int32(peer), _ptr(buf)))
+        return buf
+
+    def shard_unpack(self, peer, buf):
+        buf = np.ascontiguousarray(buf, dtype=np.float64)
+        self._ck(self.L.falcon_shard_unpack(self.h, C.c_int32(peer), _ptr(buf)))
+
+    def shard_min_ratio(self):
+        m = C.c_double()
+        self._ck(self.L.falcon_shard_min_ratio(self.h, C.byref(m)))
+        return m.value
+
+    def shard_set_min_ratio(self, m):
+        self._ck(self.L.falcon_shard_set_min_ratio(self.h, C.c_double(m)))
 
     def set_wait_limit(self, polls):
         """Poll limit of the step kernels' bulk-copy waits (< 0: the default)."""

@@ -68,6 +68,20 @@ struct falcon_ctx {
     // while U is the first allocation)
     // [buffer assignment][CFL minimum already formed by the previous step]
     cudaGraphExec_t graphs[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    // block sharding (FP64 phases): this context computes blocks [first, last)
+    // of the global tree; ghost entries whose source and target it owns are
+    // filled on the device, the others travel through per-peer pack buffers
+    struct Shard {
+        bool on = false;
+        int nranks = 1, rank = 0, first = 0, last = 0;
+        GhostLists local{};
+        std::vector<GhostInterpList> send;     // [peer] outgoing entries (source owned, target on the peer)
+        std::vector<int32_t*> recv_dst;        // [peer] target offsets of the incoming entries
+        std::vector<int64_t> nrecv;
+        double* pack = nullptr;                // device staging for host pack buffers
+        size_t pack_elems = 0;
+        void* last_out = nullptr;              // the buffer the last shard phase or exchange filled
+    } shard;
     void* bufA = nullptr;
     int64_t steps_done = 0;
     int64_t dev_bytes = 0;
@@ -381,6 +395,80 @@ int check_nan(falcon_ctx* ctx) {
 // global element offset of var 0 of padded cell (i,j,k) (Fortran indices) of block b
 inline int64_t cell_off(const Grid& g, int b, int i, int j, int k) {
     return (int64_t)b * NV * g.ncell + ((int64_t)(k + 1) * g.njp + (j + 1)) * g.nip + (i + 1);
+}
+
+// ---- block sharding ------------------------------------------------------------
+// The reference's partition of leaves over ranks (ModAllocation_Init,
+// 3_6/ModAllocation.f90:25-39): contiguous ranges, the first nb % R ranks one
+// leaf longer. first[r] .. first[r+1]-1 are rank r's blocks (0-based).
+std::vector<int> shard_ranges(int nb, int R) {
+    std::vector<int> first(R + 1, 0);
+    for (int r = 0; r < R; ++r) first[r + 1] = first[r] + nb / R + (r < nb % R ? 1 : 0);
+    return first;
+}
+int rank_of(const std::vector<int>& first, int b) {
+    return (int)(std::upper_bound(first.begin(), first.end(), b) - first.begin()) - 1;
+}
+// Entries of the canonical ghost map (falcon_ghost_map order) from the
+// blocks of rank `src` to the blocks of rank `dst`: in map order on both
+// sides, so the sender's pack order is the receiver's scatter order (the
+// reference's per-peer send/receive lists, 3_6/ModCommunication.f90:375-634).
+std::vector<int64_t> shard_entries(const Grid& g, const std::vector<int>& first, int src, int dst) {
+    std::vector<int64_t> out;
+    for (size_t k = 0; k < g.ghosts.size(); ++k) {
+        const auto& e = g.ghosts[k].e;
+        if (rank_of(first, e.sblock) == src && rank_of(first, e.tblock) == dst) out.push_back((int64_t)k);
+    }
+    return out;
+}
+
+// FP64 device lists of the given map entries: the trilinear/rotated form of
+// the exchange for every entry (a copy is an entry of kind 0), target offsets
+// and source base offsets into the state.
+cudaError_t upload_interp_list(falcon_ctx* ctx, const std::vector<int64_t>& ks, GhostInterpList& out, int32_t** dst_out) {
+    const Grid& g = ctx->grid;
+    const size_t n = ks.size();
+    std::vector<int32_t> dst(n), src(n);
+    std::vector<double> w(3 * n), rot(2 * n);
+    std::vector<uint8_t> kind(n);
+    for (size_t q = 0; q < n; ++q) {
+        const GhostMapEntry& e = g.ghosts[ks[q]];
+        dst[q] = (int32_t)cell_off(g, e.e.tblock, e.e.ti, e.e.tj, e.e.tk);
+        src[q] = (int32_t)cell_off(g, e.e.sblock, e.i0, e.j0, e.k0);
+        const int nz = (e.w[0] != 0.0) + (e.w[1] != 0.0) + (e.w[2] != 0.0);
+        for (int t = 0; t < 3; ++t) w[3 * q + t] = e.w[t];
+        rot[2 * q] = e.rotate ? e.rot[0] : 0.0;
+        rot[2 * q + 1] = e.rotate ? e.rot[1] : 0.0;
+        kind[q] = (uint8_t)((nz ? 1 : 0) | (e.rotate ? 2 : 0));
+    }
+    auto up = [&](auto** dptr, const auto& vec) -> cudaError_t {
+        using E = typename std::decay_t<decltype(vec)>::value_type;
+        cudaError_t r = ctx->alloc(dptr, vec.size() * sizeof(E));
+        if (r == cudaSuccess && !vec.empty()) r = cudaMemcpy(*dptr, vec.data(), vec.size() * sizeof(E), cudaMemcpyHostToDevice);
+        return r;
+    };
+    int32_t *d_dst, *d_src;
+    double *d_w, *d_rot;
+    uint8_t* d_kind;
+    cudaError_t e = up(&d_dst, dst);
+    if (e == cudaSuccess) e = up(&d_src, src);
+    if (e == cudaSuccess) e = up(&d_w, w);
+    if (e == cudaSuccess) e = up(&d_rot, rot);
+    if (e == cudaSuccess) e = up(&d_kind, kind);
+    if (e != cudaSuccess) return e;
+    out = GhostInterpList{(int64_t)n, d_dst, d_src, d_w, d_rot, d_kind, nullptr, nullptr};
+    if (dst_out) *dst_out = d_dst;
+    return cudaSuccess;
+}
+
+// Geometry of blocks [first, ..): the per-block tables advanced, so a kernel
+// launched over nlocal blocks computes the owned ones with its own indexing.
+Geometry geom_from(const falcon_ctx* ctx, int first) {
+    const Grid& g = ctx->grid;
+    const size_t fi = (size_t)first * GI_COUNT * g.nip, fj = (size_t)first * GJ_COUNT * g.njp,
+                 fs = (size_t)first * GS_COUNT;
+    return Geometry{ctx->gi + fi, ctx->gj + fj, ctx->gs + fs, ctx->gi_f + fi, ctx->gj_f + fj, ctx->gs_f + fs,
+                    ctx->flags + first};
 }
 
 // Per-block 1-D geometry and background tables on the device, from the grid's
@@ -1128,6 +1216,12 @@ int falcon_init_synthetic(falcon_ctx* ctx, int32_t kind, uint64_t seed, double m
 int falcon_exchange(falcon_ctx* ctx) {
     int rc = need_device(ctx);
     if (rc) return rc;
+    if (ctx->shard.on) {   // the entries within this rank; the others through falcon_shard_pack/unpack
+        CK(launch_ghost_fp64(ctx->dims, ctx->shard.local, (double*)ctx->U, ctx->st), "ghost fill");
+        ctx->shard.last_out = ctx->U;
+        CK(cudaStreamSynchronize(ctx->st), "ghost fill");
+        return FALCON_OK;
+    }
     CK(ghost(ctx, ctx->U), "ghost fill");
     ctx->stale_edges = false;
     if (ctx->P)
@@ -1202,12 +1296,48 @@ int falcon_run_steps(falcon_ctx* ctx, int32_t nsteps) {
     return run(ctx, nsteps);
 }
 
+// One phase over the owned blocks of a sharded context, then the exchange of
+// the entries within the rank. Phase 0 only accumulates the owned blocks'
+// CFL minimum (falcon_shard_min_ratio / falcon_shard_set_min_ratio finish dt
+// after the MIN over ranks).
+int shard_phase(falcon_ctx* ctx, int phase) {
+    auto& S = ctx->shard;
+    StepDims dl = ctx->dims;
+    dl.nblocks = S.last - S.first;
+    const Geometry gl = geom_from(ctx, S.first);
+    const size_t off = (size_t)S.first * NV * ctx->dims.ncell;
+    double* U = (double*)ctx->U;
+    double* RK = (double*)ctx->RK;
+    const DivBArgs none{nullptr, nullptr, nullptr, 0};
+    cudaError_t e = cudaSuccess;
+    if (phase == 0) {
+        if (dl.nblocks > 0) e = launch_cfl_fp64(dl, gl, U + off, ctx->sc, ctx->st);
+    } else if (phase <= 4) {
+        const int s = phase;
+        double* in = s == 1 ? U : RK;
+        double* out = s < 4 ? RK : U;
+        if (dl.nblocks > 0)
+            e = launch_stage_fp64(dl, gl, in + off, U + off, out + off, none, s, 1, ctx->sc, 1, ctx->kpar_stage, ctx->st);
+        if (e == cudaSuccess) e = launch_ghost_fp64(ctx->dims, S.local, out, ctx->st);
+        S.last_out = out;
+    } else {
+        if (dl.nblocks > 0) e = launch_diffusion_fp64(dl, gl, U + off, ctx->sc, ctx->kpar_diff, ctx->st);
+        if (e == cudaSuccess) e = launch_ghost_fp64(ctx->dims, S.local, U, ctx->st);
+        S.last_out = U;
+        ++ctx->steps_done;
+    }
+    if (e != cudaSuccess) return ctx->cuda_fail(e, "shard phase");
+    CK(cudaStreamSynchronize(ctx->st), "shard phase");
+    return FALCON_OK;
+}
+
 int falcon_step_phase(falcon_ctx* ctx, int32_t phase) {
     int rc = need_device(ctx);
     if (rc) return rc;
     if (phase < 0 || phase > 5) return ctx->fail(FALCON_ERR_INVALID_ARG, "phase must be 0..5");
     rc = autotune(ctx);
     if (rc) return rc;
+    if (ctx->shard.on) return shard_phase(ctx, phase);
     ctx->cfl_ready = false;   // the phases change the state outside the fused step
     cudaError_t e = cudaSuccess;
     if (phase == 0) {
@@ -1490,6 +1620,142 @@ int falcon_load_restart(falcon_ctx* ctx, const char* path) {
             CK(cudaMemcpyAsync(q, ctx->P, h.bytes_psi, cudaMemcpyDeviceToDevice, ctx->st), "restart");
     CK(cudaStreamSynchronize(ctx->st), "restart");
     ctx->steps_done = h.steps_done;
+    return FALCON_OK;
+}
+
+int falcon_shard_ranges(const falcon_ctx* ctx, int32_t nranks, int32_t* first) {
+    if (!ctx || !first || nranks < 1 || nranks > ctx->grid.nblocks) return FALCON_ERR_INVALID_ARG;
+    const std::vector<int> f = shard_ranges(ctx->grid.nblocks, nranks);
+    for (int r = 0; r <= nranks; ++r) first[r] = f[r];
+    return FALCON_OK;
+}
+
+int falcon_shard_plan(const falcon_ctx* ctx, int32_t nranks, int32_t rank, int32_t peer, int32_t dir, int64_t* entries,
+                      int64_t cap, int64_t* n) {
+    if (!ctx || !n || nranks < 1 || nranks > ctx->grid.nblocks || rank < 0 || rank >= nranks || peer < 0 ||
+        peer >= nranks || (dir != FALCON_SHARD_SEND && dir != FALCON_SHARD_RECV))
+        return FALCON_ERR_INVALID_ARG;
+    const std::vector<int> f = shard_ranges(ctx->grid.nblocks, nranks);
+    const std::vector<int64_t> v = dir == FALCON_SHARD_SEND ? shard_entries(ctx->grid, f, rank, peer)
+                                                            : shard_entries(ctx->grid, f, peer, rank);
+    *n = (int64_t)v.size();
+    if (!entries) return FALCON_OK;
+    if (cap < *n) return FALCON_ERR_BOUNDS;
+    std::memcpy(entries, v.data(), v.size() * sizeof(int64_t));
+    return FALCON_OK;
+}
+
+int falcon_set_shard(falcon_ctx* ctx, int32_t nranks, int32_t rank) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    if (ctx->shard.on) return ctx->fail(FALCON_ERR_INVALID_ARG, "falcon_set_shard: the context is already sharded");
+    if (ctx->mixed() || ctx->cfg.phys.divb_option != 0)
+        return ctx->fail(FALCON_ERR_INVALID_ARG, "falcon_set_shard: FP64 precision and divb_option 0 only");
+    if (nranks < 1 || nranks > ctx->grid.nblocks || rank < 0 || rank >= nranks)
+        return ctx->fail(FALCON_ERR_INVALID_ARG, "falcon_set_shard: bad rank count or rank");
+    rc = autotune(ctx);
+    if (rc) return rc;
+    auto& S = ctx->shard;
+    const std::vector<int> f = shard_ranges(ctx->grid.nblocks, nranks);
+    S.nranks = nranks;
+    S.rank = rank;
+    S.first = f[rank];
+    S.last = f[rank + 1];
+    // entries within the rank: copies and interpolated/rotated entries as one list
+    GhostInterpList loc{};
+    CK(upload_interp_list(ctx, shard_entries(ctx->grid, f, rank, rank), loc, nullptr), "shard lists");
+    S.local = GhostLists{GhostCopyList{0, nullptr, nullptr}, GhostLinList{0, nullptr, nullptr, nullptr, nullptr}, loc};
+    S.send.assign(nranks, GhostInterpList{});
+    S.recv_dst.assign(nranks, nullptr);
+    S.nrecv.assign(nranks, 0);
+    size_t most = 0;
+    for (int p = 0; p < nranks; ++p) {
+        if (p == rank) continue;
+        CK(upload_interp_list(ctx, shard_entries(ctx->grid, f, rank, p), S.send[p], nullptr), "shard lists");
+        GhostInterpList in{};
+        CK(upload_interp_list(ctx, shard_entries(ctx->grid, f, p, rank), in, &S.recv_dst[p]), "shard lists");
+        S.nrecv[p] = in.n;
+        most = std::max(most, (size_t)std::max(S.send[p].n, in.n));
+    }
+    S.pack_elems = most * NV;
+    CK(ctx->alloc(&S.pack, std::max<size_t>(S.pack_elems, 1) * sizeof(double)), "shard pack");
+    S.last_out = ctx->U;
+    S.on = true;
+    CK(cudaStreamSynchronize(ctx->st), "shard");
+    return FALCON_OK;
+}
+
+int falcon_shard_counts(const falcon_ctx* ctx, int32_t peer, int64_t* nsend, int64_t* nrecv) {
+    if (!ctx || !ctx->shard.on || peer < 0 || peer >= ctx->shard.nranks || !nsend || !nrecv) return FALCON_ERR_INVALID_ARG;
+    *nsend = peer == ctx->shard.rank ? 0 : ctx->shard.send[peer].n;
+    *nrecv = peer == ctx->shard.rank ? 0 : ctx->shard.nrecv[peer];
+    return FALCON_OK;
+}
+
+namespace {
+bool is_device_ptr(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+}  // namespace
+
+int falcon_shard_pack(falcon_ctx* ctx, int32_t peer, double* buf) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    auto& S = ctx->shard;
+    if (!S.on || peer < 0 || peer >= S.nranks || peer == S.rank || !buf)
+        return ctx->fail(FALCON_ERR_INVALID_ARG, "falcon_shard_pack: not sharded, or bad peer or buffer");
+    const GhostInterpList& L = S.send[peer];
+    const bool dev = is_device_ptr(buf);
+    double* out = dev ? buf : S.pack;
+    CK(launch_shard_pack_fp64(ctx->dims, L, (const double*)S.last_out, out, ctx->st), "shard pack");
+    if (!dev && L.n) CK(cudaMemcpyAsync(buf, S.pack, (size_t)L.n * NV * sizeof(double), cudaMemcpyDeviceToHost, ctx->st), "shard pack");
+    CK(cudaStreamSynchronize(ctx->st), "shard pack");
+    return FALCON_OK;
+}
+
+int falcon_shard_unpack(falcon_ctx* ctx, int32_t peer, const double* buf) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    auto& S = ctx->shard;
+    if (!S.on || peer < 0 || peer >= S.nranks || peer == S.rank || !buf)
+        return ctx->fail(FALCON_ERR_INVALID_ARG, "falcon_shard_unpack: not sharded, or bad peer or buffer");
+    const int64_t n = S.nrecv[peer];
+    const bool dev = is_device_ptr(buf);
+    const double* in = buf;
+    if (!dev && n) {
+        CK(cudaMemcpyAsync(S.pack, buf, (size_t)n * NV * sizeof(double), cudaMemcpyHostToDevice, ctx->st), "shard unpack");
+        in = S.pack;
+    }
+    CK(launch_shard_unpack_fp64(ctx->dims, S.recv_dst[peer], n, in, (double*)S.last_out, ctx->st), "shard unpack");
+    CK(cudaStreamSynchronize(ctx->st), "shard unpack");
+    return FALCON_OK;
+}
+
+int falcon_shard_min_ratio(falcon_ctx* ctx, double* local_min) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    if (!ctx->shard.on || !local_min) return ctx->fail(FALCON_ERR_INVALID_ARG, "falcon_shard_min_ratio: not sharded");
+    unsigned long long bits = 0;
+    CK(cudaMemcpyAsync(&bits, &ctx->sc->min_ratio_bits, sizeof bits, cudaMemcpyDeviceToHost, ctx->st), "min ratio");
+    CK(cudaStreamSynchronize(ctx->st), "min ratio");
+    std::memcpy(local_min, &bits, sizeof bits);
+    return check_nan(ctx);
+}
+
+int falcon_shard_set_min_ratio(falcon_ctx* ctx, double global_min) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    if (!ctx->shard.on || !(global_min > 0.0)) return ctx->fail(FALCON_ERR_INVALID_ARG, "falcon_shard_set_min_ratio");
+    unsigned long long bits;
+    std::memcpy(&bits, &global_min, sizeof bits);
+    CK(cudaMemcpyAsync(&ctx->sc->min_ratio_bits, &bits, sizeof bits, cudaMemcpyHostToDevice, ctx->st), "min ratio");
+    CK(launch_finalize_dt(ctx->sc, ctx->st), "min ratio");
+    CK(cudaStreamSynchronize(ctx->st), "min ratio");
     return FALCON_OK;
 }
 

@@ -266,6 +266,54 @@ int  falcon_step_rk4(falcon_ctx* ctx, double* dt_out);
 /* nsteps back-to-back steps, captured as CUDA graphs after the first call. */
 int  falcon_run_steps(falcon_ctx* ctx, int32_t nsteps);
 int  falcon_synchronize(falcon_ctx* ctx);
+/* ---- block sharding over ranks (one GPU per rank) ------------------------
+ * The reference distributes leaf blocks over MPI ranks in contiguous ranges
+ * (ModAllocation_Init, 3_6/ModAllocation.f90:25-39) and moves the ghost
+ * entries that cross ranks through per-peer packed messages
+ * (ModCommunication_SetGC_Sender/Receiver and the exchange,
+ * 3_6/ModCommunication.f90:375-634, 725-765), with MIN and SUM allreduces for
+ * dt and the CG dot products. Here every rank builds the same tree and ghost
+ * map; these entry points give the partition, the per-peer entry lists and,
+ * on a sharded context, the pack/unpack of those entries. The transport
+ * (NCCL send/recv on GPUs, any message layer) and the MIN of dt are the
+ * caller's.
+ *
+ * falcon_shard_ranges: first[r] .. first[r+1]-1 are rank r's blocks
+ * (0-based), r = 0..nranks-1; the first nblocks % nranks ranks get one more.
+ * falcon_shard_plan: indices into the falcon_ghost_map order of the entries
+ * rank `rank` sends to `peer` (FALCON_SHARD_SEND: source block on rank,
+ * target block on peer) or receives from it (FALCON_SHARD_RECV); peer == rank
+ * gives the entries within the rank. Both sides list a message's entries in
+ * map order, so the sender's pack order is the receiver's. Host-only
+ * contexts too.
+ *
+ * falcon_set_shard (FP64 precision, divb_option 0): this context computes
+ * rank `rank`'s blocks. falcon_step_phase then runs over the owned blocks
+ * only and fills the ghost entries within the rank; phase 0 accumulates the
+ * owned blocks' CFL minimum h/v_wave without forming dt:
+ *   per step: phase 0; m = falcon_shard_min_ratio; MIN over ranks;
+ *             falcon_shard_set_min_ratio(global m) (dt = min(1e20, CFL m));
+ *             for phases 1..5: falcon_step_phase, then for every peer
+ *             falcon_shard_pack into the message, and falcon_shard_unpack of
+ *             the peer's message.
+ * falcon_exchange on a sharded context fills the entries within the rank (the
+ * remote ones follow with pack/unpack). Pack buffers hold 8 doubles per entry
+ * (falcon_shard_counts gives the entries per peer); a buffer may be host or
+ * device memory (a device buffer is written or read in place, ready for a
+ * device-side transport). The state's blocks outside the owned range are not
+ * updated. */
+#define FALCON_SHARD_SEND 0
+#define FALCON_SHARD_RECV 1
+int  falcon_shard_ranges(const falcon_ctx* ctx, int32_t nranks, int32_t* first);
+int  falcon_shard_plan(const falcon_ctx* ctx, int32_t nranks, int32_t rank, int32_t peer, int32_t dir,
+                       int64_t* entries, int64_t cap, int64_t* n);
+int  falcon_set_shard(falcon_ctx* ctx, int32_t nranks, int32_t rank);
+int  falcon_shard_counts(const falcon_ctx* ctx, int32_t peer, int64_t* nsend, int64_t* nrecv);
+int  falcon_shard_pack(falcon_ctx* ctx, int32_t peer, double* buf);
+int  falcon_shard_unpack(falcon_ctx* ctx, int32_t peer, const double* buf);
+int  falcon_shard_min_ratio(falcon_ctx* ctx, double* local_min);
+int  falcon_shard_set_min_ratio(falcon_ctx* ctx, double global_min);
+
 /* Poll limit of the step kernels' bounded waits (no counterpart in the
  * reference, whose MPI calls block without a limit). Each stage and diffusion
  * CTA streams its block's planes into shared memory with bulk copies and

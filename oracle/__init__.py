@@ -121,6 +121,32 @@ class Oracle:
     def ghost_count(self):
         return int(self.L.orc_ghost_count(self.hp))
 
+    # ---- a rank of a block-sharded run
+    def set_owned(self, first, last):
+        """Compute (phases, dt, exchange) only blocks [first, last)."""
+        self.L.orc_set_owned(self.hp, C.c_int32(first), C.c_int32(last))
+
+    def set_dt(self, dt):
+        self.L.orc_set_dt(self.hp, C.c_double(dt))
+
+    def dt(self):
+        """The current step's dt (after phase 0 or a step)."""
+        return float(self.L.orc_dt(self.hp))
+
+    def interp_entries(self, rk, ent, x):
+        """Values [n][9] of ghost entries ent[n][5] = (tblock, ti, tj, tk, sblock)
+        with source-frame centres x[n][3], from the stage buffer (rk) or state."""
+        ent = np.ascontiguousarray(ent, dtype=np.int32)
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = np.zeros((len(ent), NVAR))
+        self.L.orc_interp_entries(self.hp, C.c_int32(1 if rk else 0), _ptr(ent), _ptr(x), C.c_int64(len(ent)), _ptr(out))
+        return out
+
+    def write_ghosts(self, rk, ent, vals):
+        ent = np.ascontiguousarray(ent, dtype=np.int32)
+        vals = np.ascontiguousarray(vals, dtype=np.float64)
+        self.L.orc_write_ghosts(self.hp, C.c_int32(1 if rk else 0), _ptr(ent), C.c_int64(len(ent)), _ptr(vals))
+
     def uncovered_ghosts(self):
         return int(self.L.orc_uncovered_ghosts(self.hp))
 
