@@ -74,7 +74,19 @@ def test_learned_coarse_correction_trains_and_preconditions(built_lib, oracle_li
     rep_lcc = sv.solve(tol=1e-8, max_iter=300, precond=S.PRECOND_MG_LCC)
     res = _cpu_residual(sv, sv.solution())
     rep_mg = sv.solve(tol=1e-8, max_iter=300, precond=S.PRECOND_MG)
+    # the same V-cycle without the network: the 2 coarsest-level sweeps alone
+    sv.set_smoothing(2, 2, 2)
+    rep_two = sv.solve(tol=1e-8, max_iter=300, precond=S.PRECOND_MG)
     sv.set_smoothing(2, 2, 0)
     rep_none = sv.solve(tol=1e-8, max_iter=300, precond=S.PRECOND_MG)
-    print("MG+LCC:", rep_lcc, "MG:", rep_mg, "MG without coarse work:", rep_none)
+    print("MG+LCC:", rep_lcc, "MG:", rep_mg, "same V-cycle without the network:", rep_two,
+          "MG without coarse work:", rep_none)
     assert rep_lcc["converged"] == 1 and res <= 1.05e-8, res
+    # what the trained network gains over the method without it: the network
+    # plus 2 coarsest-level sweeps against the 2 sweeps alone. Measured: the
+    # same iteration count -- on this system (Delta t = 50 explicit limits)
+    # the coarse levels do not limit convergence (no coarse work at all costs
+    # the same), so the learned stage has nothing to win; the wall-time target
+    # of <= 0.5x MG-PCG is not met
+    assert rep_lcc["iterations"] <= rep_two["iterations"], (rep_lcc, rep_two)
+    assert rep_none["iterations"] <= rep_mg["iterations"] + 1, (rep_none, rep_mg)
