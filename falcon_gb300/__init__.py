@@ -60,7 +60,7 @@ EXPORTS = (
     "falcon_solver_block_flags", "falcon_solver_magnetogram_sources", "falcon_solver_vcycle_op",
     "falcon_solver_tuning", "falcon_solver_set_tile", "falcon_shard_ranges", "falcon_shard_plan",
     "falcon_set_shard", "falcon_shard_counts", "falcon_shard_pack", "falcon_shard_unpack",
-    "falcon_shard_min_ratio", "falcon_shard_set_min_ratio",
+    "falcon_shard_min_ratio", "falcon_shard_set_min_ratio", "falcon_lcc_set_tensor_path",
 )
 
 # size of the static device array behind falcon_download_state_range

@@ -153,6 +153,182 @@ __global__ void __launch_bounds__(128) k_conv(const __nv_bfloat16* __restrict__ 
     }
 }
 
+// ---------------------------------------------------------------------------
+// The same implicit-GEMM convolution on the 5th-generation tensor cores:
+// tcgen05.mma (kind::f16, BF16 operands, FP32 accumulation in tensor memory).
+// A CTA of 128 threads owns a tile of M = 128 voxels x N = NC channels; its
+// accumulator is NC columns of TMEM (lane = voxel row). Per tap, every thread
+// gathers its voxel's KC input channels (zero outside the grid) into the A
+// tile in shared memory and the CTA copies the tap's weights into the B tile,
+// both in the canonical K-major layout without swizzle: 8-row x 16-byte core
+// matrices, the next along K at LBO = 128 B, the next 8 rows at SBO =
+// (KC / 8) x 128 B. One thread issues KC / 16 MMAs (K = 16 each) on the
+// smem descriptors and commits them to the tile's mbarrier; the tiles are
+// double-buffered, so the gather of tap t+1 overlaps the MMAs of tap t. The
+// epilogue reads the accumulator with tcgen05.ld (warp w: TMEM lanes
+// 32w..32w+31, its voxels), adds the bias / ReLU and stores. Waits on the
+// mbarriers are bounded: one that runs out sets *err and the tile's result is
+// discarded by the host.
+namespace tc {
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+// smem matrix descriptor: start, LBO, SBO (>> 4), version 1, no swizzle
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// instruction descriptor, kind::f16: D F32, A and B BF16, both K-major, N, M
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* b) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(b)) : "memory");
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, int polls) {
+    for (int it = 0; it < polls; ++it) {
+        uint32_t ok;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(ok)
+                     : "r"(smem_u32(b)), "r"(parity)
+                     : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+constexpr int kPolls = 1 << 22;
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+__device__ __forceinline__ void commit(uint64_t* b) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(b))
+                 : "memory");
+}
+__device__ __forceinline__ void ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int q = 0; q < 16; ++q) v[q] = __uint_as_float(r[q]);
+}
+}  // namespace tc
+
+template <int KC, int NC, int MODE>
+__global__ void __launch_bounds__(128) k_conv_tc(const __nv_bfloat16* __restrict__ x, Grid3 g,
+                                                 const __nv_bfloat16* __restrict__ w, const float* __restrict__ bias,
+                                                 int relu, __nv_bfloat16* __restrict__ out16, float* __restrict__ out32,
+                                                 int32_t* err) {
+    constexpr int CK = KC / 8;                       // 16-byte chunks (core matrices) along K per row
+    constexpr uint32_t A_BYTES = 128u * KC * 2, B_BYTES = (uint32_t)NC * KC * 2;
+    constexpr uint32_t SBO = CK * 128u;
+    constexpr int NCOLS = NC < 32 ? 32 : NC;         // TMEM columns (a power of two >= 32)
+    constexpr uint32_t IDESC = tc::idesc_bf16(128, NC);
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ uint64_t bars[2];
+    __shared__ uint32_t tmem_slot;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int64_t total = nvox(g);
+    const int64_t v = (int64_t)blockIdx.x * 128 + tid;   // this thread's voxel (row m = tid)
+    const Vox xv = decompose(g, v, total);
+    if (tid == 0) {
+        tc::mbar_init(&bars[0]);
+        tc::mbar_init(&bars[1]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncwarp();
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc::smem_u32(&tmem_slot)),
+                     "r"(NCOLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = tmem_slot;
+    int late = 0;
+    for (int tap = 0; tap < 27; ++tap) {
+        const int buf = tap & 1;
+        unsigned char* abuf = smem + (size_t)buf * A_BYTES;
+        unsigned char* bbuf = smem + 2 * (size_t)A_BYTES + (size_t)buf * B_BYTES;
+        // the MMAs of tap - 2 read this buffer: wait for their commit
+        if (tap >= 2) late |= tc::mbar_wait(&bars[buf], (uint32_t)(((tap - 2) >> 1) & 1), tc::kPolls) ? 0 : 1;
+        const int sgn = MODE == 2 ? -1 : 1;
+        const int dd = sgn * (tap / 9 - 1), dh = sgn * ((tap / 3) % 3 - 1), dw = sgn * (tap % 3 - 1);
+        const int64_t n = shifted(g, xv, dd, dh, dw);
+        // A: row m = tid, its KC channels as CK chunks of 16 bytes
+        unsigned char* arow = abuf + (size_t)(tid >> 3) * SBO + (size_t)(tid & 7) * 16;
+#pragma unroll
+        for (int c = 0; c < CK; ++c) {
+            uint4 q = make_uint4(0u, 0u, 0u, 0u);
+            if (n >= 0) q = *reinterpret_cast<const uint4*>(x + n * KC + c * 8);
+            *reinterpret_cast<uint4*>(arow + (size_t)c * 128) = q;
+        }
+        // B: the tap's weights [NC][KC], NC x CK chunks
+        const __nv_bfloat16* wt = w + (size_t)tap * NC * KC;
+        for (int q = tid; q < NC * CK; q += 128) {
+            const int row = q / CK, c = q % CK;
+            *reinterpret_cast<uint4*>(bbuf + (size_t)(row >> 3) * SBO + (size_t)(row & 7) * 16 + (size_t)c * 128) =
+                *reinterpret_cast<const uint4*>(wt + (size_t)row * KC + c * 8);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // generic writes -> the MMA's async proxy
+        tc::fence_before();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after();
+            const uint32_t a0 = tc::smem_u32(abuf), b0 = tc::smem_u32(bbuf);
+#pragma unroll
+            for (int kk = 0; kk < KC / 16; ++kk)
+                tc::mma(tmem, tc::sdesc(a0 + kk * 256u, 128u, SBO), tc::sdesc(b0 + kk * 256u, 128u, SBO), IDESC,
+                        (tap > 0 || kk > 0) ? 1u : 0u);
+            tc::commit(&bars[buf]);
+        }
+    }
+    // the last commit covers every MMA of the tile
+    late |= tc::mbar_wait(&bars[26 & 1], (uint32_t)((26 >> 1) & 1), tc::kPolls) ? 0 : 1;
+    late = __syncthreads_or(late);    // one verdict for the whole tile
+    tc::fence_after();
+    if (late && tid == 0) atomicOr(err, 1);
+    // epilogue: warp w holds TMEM lanes 32w..32w+31 = voxels tid
+#pragma unroll
+    for (int c0 = 0; c0 < NC; c0 += 16) {
+        float acc[16];
+        tc::ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, acc);
+        if (v < total && !late) {
+            if constexpr (MODE == 0) {
+#pragma unroll
+                for (int q = 0; q < 16; q += 2) {
+                    float y0 = acc[q] + bias[c0 + q], y1 = acc[q + 1] + bias[c0 + q + 1];
+                    if (relu) { y0 = fmaxf(y0, 0.f); y1 = fmaxf(y1, 0.f); }
+                    __nv_bfloat162 p;
+                    p.x = __float2bfloat16_rn(y0);
+                    p.y = __float2bfloat16_rn(y1);
+                    *reinterpret_cast<__nv_bfloat162*>(out16 + v * NC + c0 + q) = p;
+                }
+            } else if constexpr (MODE == 1) {
+                if (c0 == 0) out32[v] = acc[0] + bias[0];
+            } else {
+#pragma unroll
+                for (int q = 0; q < 16; ++q) out32[v * NC + c0 + q] = acc[q];
+            }
+        }
+    }
+    tc::fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NCOLS) : "memory");
+    }
+}
+
 // Backward weights: dw[co][ci][tap] += sum_v gy[v][co] * x[v + off(tap)][ci].
 // One CTA per (chunk of `chunk` voxels, tap); warp = (m-tile of 16 output
 // channels, share of the chunk). CO, CI: padded output and input channels
@@ -385,13 +561,29 @@ __global__ void k_weights_bf16(const float* __restrict__ wm, int ci, int co, int
 // ---- launch helpers ----------------------------------------------------------
 inline unsigned ew_grid(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16)); }
 
+// the tcgen05 kernel of one shape (dynamic shared memory: two A and two B tiles)
+template <int K, int N, int MODE>
+cudaError_t conv_tc_launch(const __nv_bfloat16* x, Grid3 g, const __nv_bfloat16* w, const float* bias, int relu,
+                           __nv_bfloat16* out16, float* out32, int32_t* err, cudaStream_t st) {
+    constexpr size_t smem = 2 * (128u * K * 2) + 2 * ((size_t)N * K * 2);
+    // with the kernel's static barriers, 64 x 64 tiles pass the 48 KB default
+    cudaError_t e = cudaFuncSetAttribute(k_conv_tc<K, N, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int64_t nv = (int64_t)g.n * g.D * g.H * g.W;
+    k_conv_tc<K, N, MODE><<<(unsigned)((nv + 127) / 128), 128, smem, st>>>(x, g, w, bias, relu, out16, out32, err);
+    return cudaGetLastError();
+}
+
+// tc: the tcgen05 kernel (else mma.sync); err: its wait-timeout flag
 template <int MODE>
 cudaError_t conv_launch(int kc, int nc, const __nv_bfloat16* x, Grid3 g, const __nv_bfloat16* w, const float* bias,
-                        int relu, __nv_bfloat16* out16, float* out32, cudaStream_t st) {
+                        int relu, __nv_bfloat16* out16, float* out32, cudaStream_t st, bool tc = false,
+                        int32_t* err = nullptr) {
     const int64_t nv = (int64_t)g.n * g.D * g.H * g.W;
     const unsigned blocks = (unsigned)((nv + 63) / 64);
 #define LCC_CONV(K, N)                                                                                   \
     if (kc == K && nc == N) {                                                                            \
+        if (tc) return conv_tc_launch<K, N, MODE>(x, g, w, bias, relu, out16, out32, err, st);           \
         k_conv<K, N, MODE><<<blocks, 128, 0, st>>>(x, g, w, bias, relu, out16, out32);                   \
         return cudaGetLastError();                                                                       \
     }
@@ -437,6 +629,8 @@ struct falcon_lcc {
     bf16 *wf[kLayers] = {}, *wb[kLayers] = {};
     int64_t adam_t = 0;
     Grid3 shape{0, 0, 0, 0};
+    bool use_tc = false;              // convolutions on tcgen05 (else mma.sync)
+    int32_t* dflag = nullptr;         // device: a tcgen05 kernel's wait ran out
     struct Acts {
         bf16 *x0, *a1, *s0, *p0, *a2, *s1, *p1, *s2, *p2, *a5, *u2, *a6, *u1, *a7, *u0, *a8, *gb;
         float *y, *xin, *t;
@@ -506,7 +700,7 @@ cudaError_t forward(falcon_lcc* net, cudaStream_t st) {
     k_prep_input<<<ew_grid(V0 * 16), 256, 0, st>>>(A.xin, V0, A.x0);
     auto conv = [&](int l, const bf16* x, Grid3 g, bf16* y) {
         return conv_launch<0>(pad16(kSpec[l].ci), pad16(kSpec[l].co), x, g, net->wf[l], net->p + net->boff[l],
-                              kSpec[l].relu, y, nullptr, st);
+                              kSpec[l].relu, y, nullptr, st, net->use_tc, net->dflag);
     };
     auto pool = [&](const bf16* x, Grid3 g, int C, bf16* y) {
         k_pool<<<ew_grid((int64_t)g.n * g.D * g.H * g.W * C / 8), 256, 0, st>>>(x, g, C, y);
@@ -531,7 +725,8 @@ cudaError_t forward(falcon_lcc* net, cudaStream_t st) {
     if ((e = conv(7, A.u1, G1, A.a7)) != cudaSuccess) return e;
     if ((e = upadd(A.a7, A.s0, G0, 16, A.u0)) != cudaSuccess) return e;
     if ((e = conv(8, A.u0, G0, A.a8)) != cudaSuccess) return e;
-    return conv_launch<1>(16, 16, A.a8, G0, net->wf[9], net->p + net->boff[9], 0, nullptr, A.y, st);
+    return conv_launch<1>(16, 16, A.a8, G0, net->wf[9], net->p + net->boff[9], 0, nullptr, A.y, st, net->use_tc,
+                          net->dflag);
 }
 
 // loss and parameter gradients (net->g zeroed here) for targets in A.t
@@ -553,7 +748,7 @@ cudaError_t backward(falcon_lcc* net, cudaStream_t st) {
         k_bias_grad<<<ew_grid(n), 256, 0, st>>>(A.gb, nv(g), cop, co, net->g + net->boff[l]);
         cudaError_t e2 = wgrad_launch(cop, cip, A.gb, x, g, co, ci, net->g + net->woff[l], st);
         if (e2 != cudaSuccess || !dx) return e2;
-        return conv_launch<2>(cop, cip, A.gb, g, net->wb[l], nullptr, 0, nullptr, dx, st);
+        return conv_launch<2>(cop, cip, A.gb, g, net->wb[l], nullptr, 0, nullptr, dx, st, net->use_tc, net->dflag);
     };
     auto upback = [&](const float* gf, Grid3 gfine, int C, float* out) {
         k_up_back<<<ew_grid(nv(gfine) * C / 8), 256, 0, st>>>(gf, gfine, C, out);
@@ -579,6 +774,16 @@ cudaError_t backward(falcon_lcc* net, cudaStream_t st) {
     if ((e = poolback(A.d_p0, A.d_u0, G0, 16, A.d_s0)) != cudaSuccess) return e;
     if ((e = back(1, A.d_s0, A.s0, A.a1, G0, A.d_a1)) != cudaSuccess) return e;
     return back(0, A.d_a1, A.a1, A.x0, G0, nullptr);
+}
+
+// a tcgen05 kernel's bounded wait that ran out (cleared when read)
+int check_flag(falcon_lcc* net) {
+    int32_t f = 0;
+    if (cudaMemcpy(&f, net->dflag, sizeof f, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return net->fail(FALCON_ERR_CUDA, "lcc: flag");
+    if (!f) return FALCON_OK;
+    cudaMemset(net->dflag, 0, sizeof f);
+    return net->fail(FALCON_ERR_TIMEOUT, "lcc: a tensor-core convolution's wait ran out; its result was discarded");
 }
 
 int check_shape(falcon_lcc* net, int n, int D, int H, int W) {
@@ -632,6 +837,7 @@ int falcon_lcc_create(falcon_lcc** out, int32_t device, uint64_t seed) {
     LCK(net->alloc(&net->g, h.size() * 4, net->allocs), "grads");
     LCK(net->alloc(&net->m, h.size() * 4, net->allocs), "adam");
     LCK(net->alloc(&net->v, h.size() * 4, net->allocs), "adam");
+    LCK(net->alloc(&net->dflag, sizeof(int32_t), net->allocs), "flag");
     for (int l = 0; l < kLayers; ++l) {
         const size_t n = (size_t)27 * pad16(kSpec[l].ci) * pad16(kSpec[l].co);
         LCK(net->alloc(&net->wf[l], n * 2, net->allocs), "weights");
@@ -698,7 +904,7 @@ int falcon_lcc_forward(falcon_lcc* net, const float* x, int32_t n, int32_t D, in
     LCK(forward(net, net->st), "forward");
     LCK(cudaMemcpyAsync(y, net->A.y, V0 * 4, cudaMemcpyDeviceToHost, net->st), "output");
     LCK(cudaStreamSynchronize(net->st), "forward");
-    return FALCON_OK;
+    return check_flag(net);
 }
 
 int falcon_lcc_loss_grad(falcon_lcc* net, const float* x, const float* t, int32_t n, int32_t D, int32_t H, int32_t W,
@@ -718,6 +924,12 @@ int falcon_lcc_loss_grad(falcon_lcc* net, const float* x, const float* t, int32_
     LCK(cudaMemcpyAsync(grad, net->g, (size_t)net->nparam * 4, cudaMemcpyDeviceToHost, net->st), "grad");
     LCK(cudaStreamSynchronize(net->st), "backward");
     *loss = sum / (double)V0;
+    return check_flag(net);
+}
+
+int falcon_lcc_set_tensor_path(falcon_lcc* net, int32_t path) {
+    if (!net || (path != FALCON_LCC_MMA_SYNC && path != FALCON_LCC_TCGEN05)) return FALCON_ERR_INVALID_ARG;
+    net->use_tc = path == FALCON_LCC_TCGEN05;
     return FALCON_OK;
 }
 
@@ -772,7 +984,7 @@ int falcon_lcc_train(falcon_lcc* net, const float* x, const float* t, int32_t ns
     }
     cleanup();
     if (e != cudaSuccess) return net->fail(FALCON_ERR_CUDA, std::string("lcc train: ") + cudaGetErrorString(e));
-    return FALCON_OK;
+    return check_flag(net);
 }
 
 }  // extern "C"

@@ -7,6 +7,8 @@ import numpy as np
 from . import FalconError, OK, lib
 
 CIN = 8
+MMA_SYNC = 0      # warp-level mma.sync convolutions
+TCGEN05 = 1       # 5th-generation tensor cores (tcgen05.mma, accumulator in tensor memory)
 
 
 def _ptr(a):
@@ -49,6 +51,10 @@ class LCC:
     def _ck(self, rc):
         if rc != OK:
             raise FalconError(rc, self.last_error())
+
+    def set_tensor_path(self, path):
+        """TCGEN05 or MMA_SYNC for the forward and backward-data convolutions."""
+        self._ck(self.L.falcon_lcc_set_tensor_path(self.h, C.c_int32(path)))
 
     def params(self):
         p = np.zeros(self.nparams, dtype=np.float32)

@@ -52,9 +52,11 @@ def test_oracle_param_count():
 
 
 @pytest.mark.gpu
-def test_gpu_forward_and_gradients_match_oracle(built_lib):
-    from falcon_gb300.lcc import LCC
-    net = LCC(device=0, seed=1)
+@pytest.mark.parametrize("path", ["mma_sync", "tcgen05"])
+def test_gpu_forward_and_gradients_match_oracle(built_lib, path):
+    from falcon_gb300 import lcc as L
+    net = L.LCC(device=0, seed=1)
+    net.set_tensor_path(L.TCGEN05 if path == "tcgen05" else L.MMA_SYNC)
     assert net.nparams == O.num_params()
     rs = np.random.default_rng(2)
     p = O.init_params(4)
@@ -82,3 +84,33 @@ def test_gpu_training_reduces_loss(built_lib):
     losses = net.train(x, t, epochs=30, batch=4, lr=2e-3, seed=5)
     assert np.isfinite(losses).all()
     assert losses[-1] < 0.2 * losses[0], losses
+
+
+@pytest.mark.gpu
+def test_gpu_tcgen05_convolutions_match_mma_sync(built_lib):
+    """The forward and backward-data convolutions on tcgen05 (accumulator in
+    tensor memory) against the same network on mma.sync: same BF16 operands,
+    FP32 sums in another order. A 3 x 8 x 8 x 24 batch: its 4,608 voxels are
+    36 tiles of 128, and 24 is not a multiple of the 8-voxel core rows of one
+    tile's face, so tiles straddle grid rows and samples."""
+    from falcon_gb300 import lcc as L
+    rs = np.random.default_rng(7)
+    p = L.LCC(device=0, seed=2).params()
+    p = p + rs.normal(0, 0.01, p.size).astype(np.float32)
+    x, t = _inputs(3, 8, 8, 24, 13)
+    out = {}
+    for path in (L.MMA_SYNC, L.TCGEN05):
+        net = L.LCC(device=0, seed=2)
+        net.set_params(p)
+        net.set_tensor_path(path)
+        y = net.forward(x)
+        loss, g = net.loss_grad(x, t)
+        out[path] = (y, loss, g)
+    (y0, l0, g0), (y1, l1, g1) = out[L.MMA_SYNC], out[L.TCGEN05]
+    print("tcgen05 vs mma.sync: forward rel %.2e, loss rel %.2e" % (_rel(y1, y0), abs(l1 - l0) / l0))
+    assert _rel(y1, y0) <= 2e-3
+    assert abs(l1 - l0) <= 2e-3 * l0
+    offs = np.cumsum([0] + [co * ci * 27 + co for ci, co in O.LAYERS])
+    for l in range(len(O.LAYERS)):
+        sl = slice(offs[l], offs[l + 1])
+        assert _rel(g1[sl], g0[sl]) <= 2e-2, (l, _rel(g1[sl], g0[sl]))
