@@ -15,6 +15,8 @@
 // padding at the grid edge, the B fragments from a per-tap weight copy laid
 // out so each fragment register is one 32-bit load. Weights have FP32 master
 // copies updated by Adam; BF16 copies are regenerated after every update.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -154,37 +156,55 @@ __global__ void __launch_bounds__(128) k_conv(const __nv_bfloat16* __restrict__ 
 }
 
 // ---------------------------------------------------------------------------
-// The same implicit-GEMM convolution on the 5th-generation tensor cores:
-// tcgen05.mma (kind::f16, BF16 operands, FP32 accumulation in tensor memory).
-// A CTA of 128 threads owns a tile of M = 128 voxels x N = NC channels; its
-// accumulator is NC columns of TMEM (lane = voxel row). Per tap, every thread
-// gathers its voxel's KC input channels (zero outside the grid) into the A
-// tile in shared memory and the CTA copies the tap's weights into the B tile,
-// both in the canonical K-major layout without swizzle: 8-row x 16-byte core
-// matrices, the next along K at LBO = 128 B, the next 8 rows at SBO =
-// (KC / 8) x 128 B. One thread issues KC / 16 MMAs (K = 16 each) on the
-// smem descriptors and commits them to the tile's mbarrier; the tiles are
-// double-buffered, so the gather of tap t+1 overlaps the MMAs of tap t. The
-// epilogue reads the accumulator with tcgen05.ld (warp w: TMEM lanes
-// 32w..32w+31, its voxels), adds the bias / ReLU and stores. Waits on the
-// mbarriers are bounded: one that runs out sets *err and the tile's result is
-// discarded by the host.
+// The same convolutions on the 5th-generation tensor cores: tcgen05.mma
+// (kind::f16, BF16 operands, FP32 accumulation in tensor memory), with TMA
+// tensor copies (cp.async.bulk.tensor) feeding a ring of shared-memory stages.
+//
+// Roles in a CTA of 128 threads: lane 0 of warp 0 issues the copies, lane 0 of
+// warp 1 waits for each stage, issues its MMAs and commits them to the
+// stage's `empty` barrier (which frees the stage for the next copy); the
+// other lanes of those two warps wait at __syncwarp, so no polling lane
+// shares a warp with a role lane. All four warps then read the accumulator
+// (warp w: TMEM lanes 32w..32w+31) for the epilogue.
+//
+// Forward and backward data (k_conv_tc): the CTA's 128 voxels are one row
+// block; its halo is loaded once and every tap's A operand is a view of it
+// (see the kernel); only the tap's weight tile [N][K] is copied per tap.
+// Weight gradient (k_wgrad_tc): K runs over voxel bricks of 4 x 4 x 8; per
+// brick two 5-D box copies of [n][D][H][W][C] (gy, and x shifted by the tap;
+// the copy engine fills voxels outside the grid with zeros, the
+// convolution's padding). Copied rows are one voxel's C channels, C x 2 bytes
+// = the swizzle span (32, 64 or 128 B), so the copies write exactly the
+// canonical swizzled layouts that the MMA descriptors name.
+// Every wait is bounded; one that runs out sets *err, the CTA waits (bounded)
+// for its copies in flight, frees its tensor memory and discards its tile.
 namespace tc {
+constexpr int kStages = 4;                          // ring depth of the weight-gradient tiles
+constexpr int kConvStages = 8;                      // ring depth of the convolutions' weight tiles
+constexpr int kBW = 8, kBH = 4, kBD = 4;            // voxel brick (w, h, d) of a weight-gradient tile
+constexpr int kRowW = 8, kRowH = 16;                // row block (w, h; one d) of a convolution tile
+constexpr int kPolls = 1 << 22;
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-// smem matrix descriptor: start, LBO, SBO (>> 4), version 1, no swizzle
-__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+// UMMA layout code of a swizzle span (bytes): 32 -> 6, 64 -> 4, 128 -> 2
+__host__ __device__ constexpr uint32_t umma_layout(int span) { return span == 32 ? 6u : span == 64 ? 4u : 2u; }
+// shared-memory matrix descriptor: start, LBO, SBO (>> 4), version 1, layout
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo, uint32_t layout) {
     return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
-           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46) | ((uint64_t)layout << 61);
 }
-// instruction descriptor, kind::f16: D F32, A and B BF16, both K-major, N, M
-__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+// instruction descriptor, kind::f16: D F32, A and B BF16, majors (0 K, 1 MN), N, M
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N, int a_mn, int b_mn) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)a_mn << 15) | ((uint32_t)b_mn << 16) |
+           ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 __device__ __forceinline__ void mbar_init(uint64_t* b) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(b)) : "memory");
 }
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, int polls) {
-    for (int it = 0; it < polls; ++it) {
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
+    for (int it = 0; it < kPolls; ++it) {
         uint32_t ok;
         asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
                      : "=r"(ok)
@@ -194,7 +214,21 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, int poll
     }
     return false;
 }
-constexpr int kPolls = 1 << 22;
+__device__ __forceinline__ void tma_5d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2, int c3,
+                                       int c4) {
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5, %6, "
+        "%7}], [%2];" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4)
+        : "memory");
+}
+__device__ __forceinline__ void tma_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+            smem_u32(dst)),
+        "l"(map), "r"(smem_u32(bar)), "r"(c0), "r"(c1)
+        : "memory");
+}
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
@@ -219,114 +253,271 @@ __device__ __forceinline__ void ld16(uint32_t taddr, float (&v)[16]) {
 #pragma unroll
     for (int q = 0; q < 16; ++q) v[q] = __uint_as_float(r[q]);
 }
-}  // namespace tc
+__host__ __device__ constexpr uint32_t up1024(uint32_t b) { return (b + 1023u) / 1024u * 1024u; }
 
-template <int KC, int NC, int MODE>
-__global__ void __launch_bounds__(128) k_conv_tc(const __nv_bfloat16* __restrict__ x, Grid3 g,
-                                                 const __nv_bfloat16* __restrict__ w, const float* __restrict__ bias,
-                                                 int relu, __nv_bfloat16* __restrict__ out16, float* __restrict__ out32,
-                                                 int32_t* err) {
-    constexpr int CK = KC / 8;                       // 16-byte chunks (core matrices) along K per row
-    constexpr uint32_t A_BYTES = 128u * KC * 2, B_BYTES = (uint32_t)NC * KC * 2;
-    constexpr uint32_t SBO = CK * 128u;
-    constexpr int NCOLS = NC < 32 ? 32 : NC;         // TMEM columns (a power of two >= 32)
-    constexpr uint32_t IDESC = tc::idesc_bf16(128, NC);
-    extern __shared__ __align__(1024) unsigned char smem[];
-    __shared__ uint64_t bars[2];
-    __shared__ uint32_t tmem_slot;
-    const int tid = threadIdx.x, warp = tid >> 5;
-    const int64_t total = nvox(g);
-    const int64_t v = (int64_t)blockIdx.x * 128 + tid;   // this thread's voxel (row m = tid)
-    const Vox xv = decompose(g, v, total);
+// tensor memory of the tile (warp 0), barriers (thread 0); all threads synced
+template <int NCOLS, int STAGES>
+__device__ __forceinline__ uint32_t tile_setup(uint64_t* bars, uint32_t* slot) {
+    const int tid = threadIdx.x;
     if (tid == 0) {
-        tc::mbar_init(&bars[0]);
-        tc::mbar_init(&bars[1]);
+        for (int q = 0; q < 2 * STAGES + 1; ++q) mbar_init(&bars[q]);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncwarp();
-    if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc::smem_u32(&tmem_slot)),
+    if ((tid >> 5) == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
                      "r"(NCOLS)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    tc::fence_before();
+    fence_before();
     __syncthreads();
-    tc::fence_after();
-    const uint32_t tmem = tmem_slot;
-    int late = 0;
-    for (int tap = 0; tap < 27; ++tap) {
-        const int buf = tap & 1;
-        unsigned char* abuf = smem + (size_t)buf * A_BYTES;
-        unsigned char* bbuf = smem + 2 * (size_t)A_BYTES + (size_t)buf * B_BYTES;
-        // the MMAs of tap - 2 read this buffer: wait for their commit
-        if (tap >= 2) late |= tc::mbar_wait(&bars[buf], (uint32_t)(((tap - 2) >> 1) & 1), tc::kPolls) ? 0 : 1;
-        const int sgn = MODE == 2 ? -1 : 1;
-        const int dd = sgn * (tap / 9 - 1), dh = sgn * ((tap / 3) % 3 - 1), dw = sgn * (tap % 3 - 1);
-        const int64_t n = shifted(g, xv, dd, dh, dw);
-        // A: row m = tid, its KC channels as CK chunks of 16 bytes
-        unsigned char* arow = abuf + (size_t)(tid >> 3) * SBO + (size_t)(tid & 7) * 16;
-#pragma unroll
-        for (int c = 0; c < CK; ++c) {
-            uint4 q = make_uint4(0u, 0u, 0u, 0u);
-            if (n >= 0) q = *reinterpret_cast<const uint4*>(x + n * KC + c * 8);
-            *reinterpret_cast<uint4*>(arow + (size_t)c * 128) = q;
-        }
-        // B: the tap's weights [NC][KC], NC x CK chunks
-        const __nv_bfloat16* wt = w + (size_t)tap * NC * KC;
-        for (int q = tid; q < NC * CK; q += 128) {
-            const int row = q / CK, c = q % CK;
-            *reinterpret_cast<uint4*>(bbuf + (size_t)(row >> 3) * SBO + (size_t)(row & 7) * 16 + (size_t)c * 128) =
-                *reinterpret_cast<const uint4*>(wt + (size_t)row * KC + c * 8);
-        }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // generic writes -> the MMA's async proxy
-        tc::fence_before();
-        __syncthreads();
-        if (tid == 0) {
-            tc::fence_after();
-            const uint32_t a0 = tc::smem_u32(abuf), b0 = tc::smem_u32(bbuf);
-#pragma unroll
-            for (int kk = 0; kk < KC / 16; ++kk)
-                tc::mma(tmem, tc::sdesc(a0 + kk * 256u, 128u, SBO), tc::sdesc(b0 + kk * 256u, 128u, SBO), IDESC,
-                        (tap > 0 || kk > 0) ? 1u : 0u);
-            tc::commit(&bars[buf]);
-        }
-    }
-    // the last commit covers every MMA of the tile
-    late |= tc::mbar_wait(&bars[26 & 1], (uint32_t)((26 >> 1) & 1), tc::kPolls) ? 0 : 1;
-    late = __syncthreads_or(late);    // one verdict for the whole tile
-    tc::fence_after();
-    if (late && tid == 0) atomicOr(err, 1);
-    // epilogue: warp w holds TMEM lanes 32w..32w+31 = voxels tid
-#pragma unroll
-    for (int c0 = 0; c0 < NC; c0 += 16) {
-        float acc[16];
-        tc::ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, acc);
-        if (v < total && !late) {
-            if constexpr (MODE == 0) {
-#pragma unroll
-                for (int q = 0; q < 16; q += 2) {
-                    float y0 = acc[q] + bias[c0 + q], y1 = acc[q + 1] + bias[c0 + q + 1];
-                    if (relu) { y0 = fmaxf(y0, 0.f); y1 = fmaxf(y1, 0.f); }
-                    __nv_bfloat162 p;
-                    p.x = __float2bfloat16_rn(y0);
-                    p.y = __float2bfloat16_rn(y1);
-                    *reinterpret_cast<__nv_bfloat162*>(out16 + v * NC + c0 + q) = p;
-                }
-            } else if constexpr (MODE == 1) {
-                if (c0 == 0) out32[v] = acc[0] + bias[0];
-            } else {
-#pragma unroll
-                for (int q = 0; q < 16; ++q) out32[v * NC + c0 + q] = acc[q];
-            }
-        }
-    }
-    tc::fence_before();
+    fence_after();
+    return *slot;
+}
+template <int NCOLS>
+__device__ __forceinline__ void tile_release(uint32_t tmem) {
+    fence_before();
     __syncthreads();
-    if (warp == 0) {
-        tc::fence_after();
+    if ((threadIdx.x >> 5) == 0) {
+        fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NCOLS) : "memory");
     }
+}
+// after a wait ran out somewhere: thread 0 waits (bounded) for the copies it
+// issued into the last STAGES stages, so none lands after the CTA exits
+template <int STAGES>
+__device__ __forceinline__ void drain_copies(uint64_t* full, int issued) {
+    for (int t = issued - STAGES < 0 ? 0 : issued - STAGES; t < issued; ++t)
+        mbar_wait(&full[t % STAGES], (uint32_t)((t / STAGES) & 1));
+}
+// brick of tile index `t`: sample and first voxel (d0, h0, w0)
+struct Brick { int s, d0, h0, w0; };
+__device__ __forceinline__ Brick brick_of(const Grid3& g, int64_t t) {
+    const int tw = (g.W + kBW - 1) / kBW, th = (g.H + kBH - 1) / kBH, td = (g.D + kBD - 1) / kBD;
+    Brick b;
+    b.w0 = (int)(t % tw) * kBW;
+    t /= tw;
+    b.h0 = (int)(t % th) * kBH;
+    t /= th;
+    b.d0 = (int)(t % td) * kBD;
+    b.s = (int)(t / td);
+    return b;
+}
+}  // namespace tc
+
+// Forward / backward-data convolution: KC channels gathered (the K of each
+// tap), NC output channels, MODE as k_conv. A CTA owns a row block of 1 x 16 x
+// 8 voxels (d, h, w): M = 128, TMEM lane m = voxel (h0 + m / 8, w0 + m % 8).
+// Its 3 x 18 x 10 halo is loaded once, by all threads, into shared memory in
+// the no-swizzle K-major core-matrix layout: chunk c of 8 channels is a slab
+// [540 halo voxels][16 B] at c x 8640 B. For tap (dd, dh, dw) the A operand
+// is then a view of that slab: the 8 rows of core group j (h = j) start at
+// halo voxel ((dd + 1) x 18 + j + dh + 1) x 10 + dw + 1, i.e. a fixed start
+// and a group stride (SBO) of 10 voxels = 160 B; the next 8 channels are one
+// slab further (LBO). No data moves between taps. The tap's weight tile
+// [NC][KC] comes by TMA into a ring of kConvStages stages (swizzled K-major).
+// wmap: tensor map of the weights [27 * NC][KC].
+template <int KC, int NC, int MODE>
+__global__ void __launch_bounds__(128) k_conv_tc(const __nv_bfloat16* __restrict__ x,
+                                                 const __grid_constant__ CUtensorMap wmap, Grid3 g,
+                                                 const float* __restrict__ bias, int relu,
+                                                 __nv_bfloat16* __restrict__ out16, float* __restrict__ out32,
+                                                 int32_t* err) {
+    using namespace tc;
+    constexpr int ST = kConvStages;
+    constexpr int HD = 3, HH = kRowH + 2, HW = kRowW + 2, HROWS = HD * HH * HW;
+    constexpr uint32_t SLAB = HROWS * 16u;                               // one chunk of 8 channels
+    constexpr uint32_t SPAN = KC * 2, B_BYTES = (uint32_t)NC * SPAN, B_STRIDE = up1024(B_BYTES);
+    constexpr int NCOLS = NC < 32 ? 32 : NC;
+    constexpr uint32_t IDESC = idesc_bf16(128, NC, 0, 0);
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ uint64_t bars[2 * ST + 1];
+    __shared__ uint32_t tmem_slot;
+    unsigned char* bbase = smem + ((1024u - (smem_u32(smem) & 1023u)) & 1023u);   // swizzle atoms: 1 KB aligned
+    unsigned char* abase = bbase + ST * B_STRIDE;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    uint64_t *full = bars, *empty = bars + ST, *done = bars + 2 * ST;
+    // row block of this CTA
+    const int tw = (g.W + kRowW - 1) / kRowW, th = (g.H + kRowH - 1) / kRowH;
+    int64_t q = blockIdx.x;
+    const int w0 = (int)(q % tw) * kRowW;
+    q /= tw;
+    const int h0 = (int)(q % th) * kRowH;
+    q /= th;
+    const int d0 = (int)(q % g.D), smp = (int)(q / g.D);
+    const uint32_t tmem = tile_setup<NCOLS, ST>(bars, &tmem_slot);
+    int late = 0, issued = 0;
+    auto issue_b = [&](int t) {
+        const int s = t % ST;
+        mbar_expect_tx(&full[s], B_BYTES);
+        tma_2d(bbase + s * B_STRIDE, &wmap, &full[s], 0, t * NC);
+        issued = t + 1;
+    };
+    if (tid == 0)
+        for (int t = 0; t < ST; ++t) issue_b(t);
+    // halo: voxel (d0 - 1 + r / 180, h0 - 1 + (r / 10) % 18, w0 - 1 + r % 10), zero outside the grid
+    const int64_t plane = (int64_t)g.H * g.W, sbase = (int64_t)smp * g.D * plane;
+    constexpr int NITEM = HROWS * (KC / 8), UNR = 4;  // 16-B items; UNR loads in flight per thread
+    for (int i0 = 0; i0 < NITEM; i0 += 128 * UNR) {
+        uint4 val[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+            const int i = i0 + u * 128 + tid, c = i % (KC / 8), r = i / (KC / 8);
+            const int d = d0 - 1 + r / (HH * HW), h = h0 - 1 + (r / HW) % HH, w = w0 - 1 + r % HW;
+            val[u] = make_uint4(0u, 0u, 0u, 0u);
+            if (i < NITEM && d >= 0 && d < g.D && h >= 0 && h < g.H && w >= 0 && w < g.W)
+                val[u] = *reinterpret_cast<const uint4*>(x + (sbase + d * plane + (int64_t)h * g.W + w) * KC + c * 8);
+        }
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+            const int i = i0 + u * 128 + tid;
+            if (i < NITEM) *reinterpret_cast<uint4*>(abase + (i % (KC / 8)) * SLAB + (i / (KC / 8)) * 16u) = val[u];
+        }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");      // the halo -> the MMA's async proxy
+    __syncthreads();
+    // one lane of warp 0 copies, one of warp 1 issues the MMAs; the other lanes
+    // of those warps wait at __syncwarp, not in a polling loop beside them
+    if (tid == 0) {                                  // weight copies of the later taps
+        for (int t = ST; t < 27; ++t) {
+            if (!mbar_wait(&empty[t % ST], (uint32_t)((t / ST - 1) & 1))) { late = 1; break; }
+            issue_b(t);
+        }
+    } else if (tid == 32) {                          // MMAs
+        fence_after();
+        const uint32_t a0 = smem_u32(abase);
+        for (int t = 0; t < 27; ++t) {
+            const int s = t % ST;
+            if (!mbar_wait(&full[s], (uint32_t)((t / ST) & 1))) { late = 1; break; }
+            fence_after();
+            const int sgn = MODE == 2 ? -1 : 1;
+            const int dd = sgn * (t / 9 - 1), dh = sgn * ((t / 3) % 3 - 1), dw = sgn * (t % 3 - 1);
+            const uint32_t at = a0 + (uint32_t)((((dd + 1) * HH + dh + 1) * HW + dw + 1) * 16);
+            const uint32_t b0 = smem_u32(bbase + s * B_STRIDE);
+#pragma unroll
+            for (int kk = 0; kk < KC / 16; ++kk)
+                mma(tmem, sdesc(at + kk * 2 * SLAB, SLAB, HW * 16u, 0u),
+                    sdesc(b0 + kk * 32u, 16u, 8 * SPAN, umma_layout(SPAN)), IDESC, (t > 0 || kk > 0) ? 1u : 0u);
+            commit(&empty[s]);
+        }
+        commit(done);                                // completes when every MMA issued above has
+    }
+    if (warp < 2) __syncwarp();
+    if (!mbar_wait(done, 0u)) late = 1;
+    late = __syncthreads_or(late);
+    if (late && tid == 0) {
+        drain_copies<ST>(full, issued);
+        atomicOr(err, 1);
+    }
+    fence_after();
+    // epilogue: warp w reads TMEM lanes 32w..32w+31; row m = tid
+    const int h = h0 + tid / kRowW, w = w0 + tid % kRowW;
+    const bool ok = !late && h < g.H && w < g.W;
+    const int64_t v = sbase + d0 * plane + (int64_t)h * g.W + w;
+#pragma unroll
+    for (int c0 = 0; c0 < (MODE == 1 ? 16 : NC); c0 += 16) {
+        float acc[16];
+        ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, acc);
+        if (!ok) continue;
+        if constexpr (MODE == 0) {
+#pragma unroll
+            for (int k = 0; k < 16; k += 2) {
+                float y0 = acc[k] + bias[c0 + k], y1 = acc[k + 1] + bias[c0 + k + 1];
+                if (relu) { y0 = fmaxf(y0, 0.f); y1 = fmaxf(y1, 0.f); }
+                __nv_bfloat162 p;
+                p.x = __float2bfloat16_rn(y0);
+                p.y = __float2bfloat16_rn(y1);
+                *reinterpret_cast<__nv_bfloat162*>(out16 + v * NC + c0 + k) = p;
+            }
+        } else if constexpr (MODE == 1) {
+            out32[v] = acc[0] + bias[0];
+        } else {
+#pragma unroll
+            for (int k = 0; k < 16; k += 4)
+                *reinterpret_cast<float4*>(out32 + v * NC + c0 + k) = make_float4(acc[k], acc[k + 1], acc[k + 2], acc[k + 3]);
+        }
+    }
+    tile_release<NCOLS>(tmem);
+}
+
+// Weight gradient of one tap over a run of bricks: D[co][ci] (M = 128 rows,
+// co < CO real; N = CI) += sum over the bricks' voxels of gy[v][co] x[v +
+// off][ci]. Both tiles are [128 voxels][C] as copied, i.e. MN-major with the
+// voxels as K: 8 voxel rows form a swizzle atom (SBO = 8 rows), and the 16
+// voxels of one MMA are 16 rows further on. M = 128 covers CO with LBO = 0:
+// the rows past CO repeat the first ones and their accumulators are unused.
+// The sums of all bricks are added into dw[co][ci][tap] with FP32 atomics.
+template <int CO, int CI>
+__global__ void __launch_bounds__(128) k_wgrad_tc(const __grid_constant__ CUtensorMap gmap,
+                                                  const __grid_constant__ CUtensorMap xmap, Grid3 g, int64_t nbricks,
+                                                  int per_cta, int co_real, int ci_real, float* __restrict__ dw,
+                                                  int32_t* err) {
+    using namespace tc;
+    constexpr uint32_t SPAN_A = CO * 2, SPAN_B = CI * 2;
+    constexpr uint32_t A_BYTES = 128u * SPAN_A, B_BYTES = 128u * SPAN_B;
+    constexpr uint32_t A_STRIDE = up1024(A_BYTES), B_STRIDE = up1024(B_BYTES);
+    constexpr int NCOLS = CI < 32 ? 32 : CI;
+    constexpr uint32_t IDESC = idesc_bf16(128, CI, 1, 1);
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ uint64_t bars[2 * kStages + 1];
+    __shared__ uint32_t tmem_slot;
+    unsigned char* abase = smem + ((1024u - (smem_u32(smem) & 1023u)) & 1023u);   // swizzle atoms: 1 KB aligned
+    unsigned char* bbase = abase + kStages * A_STRIDE;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    uint64_t *full = bars, *empty = bars + kStages, *done = bars + 2 * kStages;
+    const int tap = blockIdx.y;
+    const int dd = tap / 9 - 1, dh = (tap / 3) % 3 - 1, dwo = tap % 3 - 1;
+    const int64_t b0 = (int64_t)blockIdx.x * per_cta;
+    const int nb = (int)((nbricks - b0) < per_cta ? (nbricks - b0) : per_cta);
+    const uint32_t tmem = tile_setup<NCOLS, kStages>(bars, &tmem_slot);
+    int late = 0, issued = 0;
+    if (tid == 0) {
+        for (int t = 0; t < nb; ++t) {
+            const int s = t % kStages;
+            if (t >= kStages && !mbar_wait(&empty[s], (uint32_t)((t / kStages - 1) & 1))) { late = 1; break; }
+            const Brick bk = brick_of(g, b0 + t);
+            mbar_expect_tx(&full[s], A_BYTES + B_BYTES);
+            tma_5d(abase + s * A_STRIDE, &gmap, &full[s], 0, bk.w0, bk.h0, bk.d0, bk.s);
+            tma_5d(bbase + s * B_STRIDE, &xmap, &full[s], 0, bk.w0 + dwo, bk.h0 + dh, bk.d0 + dd, bk.s);
+            issued = t + 1;
+        }
+    } else if (tid == 32) {
+        for (int t = 0; t < nb; ++t) {
+            const int s = t % kStages;
+            if (!mbar_wait(&full[s], (uint32_t)((t / kStages) & 1))) { late = 1; break; }
+            fence_after();
+            const uint32_t a0 = smem_u32(abase + s * A_STRIDE), bb = smem_u32(bbase + s * B_STRIDE);
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk)
+                mma(tmem, sdesc(a0 + kk * 16u * SPAN_A, 0u, 8 * SPAN_A, umma_layout(SPAN_A)),
+                    sdesc(bb + kk * 16u * SPAN_B, 0u, 8 * SPAN_B, umma_layout(SPAN_B)), IDESC,
+                    (t > 0 || kk > 0) ? 1u : 0u);
+            commit(&empty[s]);
+        }
+        commit(done);
+    }
+    if (warp < 2) __syncwarp();                      // the role lanes' warps reconverge before polling
+    if (!mbar_wait(done, 0u)) late = 1;
+    late = __syncthreads_or(late);
+    if (late && tid == 0) {
+        drain_copies<kStages>(full, issued);
+        atomicOr(err, 1);
+    }
+    fence_after();
+    if (warp * 32 < CO && nb > 0) {                  // warp-uniform: TMEM lanes 32w.. hold co = 32w..
+        const int co = tid;
+#pragma unroll
+        for (int c0 = 0; c0 < CI; c0 += 16) {
+            float acc[16];
+            ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, acc);
+            if (late || co >= co_real) continue;
+#pragma unroll
+            for (int q = 0; q < 16; ++q)
+                if (c0 + q < ci_real) atomicAdd(&dw[((size_t)co * ci_real + c0 + q) * 27 + tap], acc[q]);
+        }
+    }
+    tile_release<NCOLS>(tmem);
 }
 
 // Backward weights: dw[co][ci][tap] += sum_v gy[v][co] * x[v + off(tap)][ci].
@@ -561,16 +752,87 @@ __global__ void k_weights_bf16(const float* __restrict__ wm, int ci, int co, int
 // ---- launch helpers ----------------------------------------------------------
 inline unsigned ew_grid(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16)); }
 
-// the tcgen05 kernel of one shape (dynamic shared memory: two A and two B tiles)
+// cuTensorMapEncodeTiled, through the runtime's driver entry point
+inline PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+inline CUtensorMapSwizzle swizzle_of(int span) {
+    return span == 32 ? CU_TENSOR_MAP_SWIZZLE_32B : span == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B;
+}
+// activations [n][D][H][W][C] BF16, copied as bricks of C x 8 x 4 x 4 x 1
+// (out-of-range voxels read as zeros); rows of C x 2 bytes, swizzled to match
+inline cudaError_t act_map(CUtensorMap* m, const __nv_bfloat16* x, Grid3 g, int C) {
+    const auto fn = encode_tiled();
+    if (!fn) return cudaErrorNotSupported;
+    const cuuint64_t row = (cuuint64_t)C * 2;
+    const cuuint64_t dims[5] = {(cuuint64_t)C, (cuuint64_t)g.W, (cuuint64_t)g.H, (cuuint64_t)g.D, (cuuint64_t)g.n};
+    const cuuint64_t strides[4] = {row, row * g.W, row * g.W * g.H, row * g.W * g.H * g.D};
+    const cuuint32_t box[5] = {(cuuint32_t)C, tc::kBW, tc::kBH, tc::kBD, 1};
+    const cuuint32_t es[5] = {1, 1, 1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<__nv_bfloat16*>(x), dims, strides, box, es,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle_of(C * 2), CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS
+               ? cudaSuccess
+               : cudaErrorInvalidValue;
+}
+// weights [27 * N][K] BF16, copied one tap (N rows of K) at a time
+inline cudaError_t weight_map(CUtensorMap* m, const __nv_bfloat16* w, int K, int N) {
+    const auto fn = encode_tiled();
+    if (!fn) return cudaErrorNotSupported;
+    const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)27 * N};
+    const cuuint64_t strides[1] = {(cuuint64_t)K * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)K, (cuuint32_t)N};
+    const cuuint32_t es[2] = {1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16*>(w), dims, strides, box, es,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle_of(K * 2), CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS
+               ? cudaSuccess
+               : cudaErrorInvalidValue;
+}
+inline int64_t bricks(Grid3 g) {
+    return (int64_t)g.n * ((g.D + tc::kBD - 1) / tc::kBD) * ((g.H + tc::kBH - 1) / tc::kBH) *
+           ((g.W + tc::kBW - 1) / tc::kBW);
+}
+// dynamic shared memory of a ring with A and B tiles (plus 1 KB to align it)
+constexpr uint32_t ring_bytes(uint32_t a, uint32_t b) { return tc::kStages * (tc::up1024(a) + tc::up1024(b)) + 1024u; }
+
 template <int K, int N, int MODE>
 cudaError_t conv_tc_launch(const __nv_bfloat16* x, Grid3 g, const __nv_bfloat16* w, const float* bias, int relu,
                            __nv_bfloat16* out16, float* out32, int32_t* err, cudaStream_t st) {
-    constexpr size_t smem = 2 * (128u * K * 2) + 2 * ((size_t)N * K * 2);
-    // with the kernel's static barriers, 64 x 64 tiles pass the 48 KB default
-    cudaError_t e = cudaFuncSetAttribute(k_conv_tc<K, N, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // the weight ring, then the halo (3 x 18 x 10 voxels of K channels)
+    constexpr uint32_t smem = tc::kConvStages * tc::up1024((uint32_t)N * K * 2) + 3u * (tc::kRowH + 2) * (tc::kRowW + 2) * K * 2 + 1024u;
+    CUtensorMap wm;
+    cudaError_t e = weight_map(&wm, w, K, N);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_conv_tc<K, N, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    const int64_t nv = (int64_t)g.n * g.D * g.H * g.W;
-    k_conv_tc<K, N, MODE><<<(unsigned)((nv + 127) / 128), 128, smem, st>>>(x, g, w, bias, relu, out16, out32, err);
+    const int64_t blocks = (int64_t)g.n * g.D * ((g.H + tc::kRowH - 1) / tc::kRowH) * ((g.W + tc::kRowW - 1) / tc::kRowW);
+    k_conv_tc<K, N, MODE><<<(unsigned)blocks, 128, smem, st>>>(x, wm, g, bias, relu, out16, out32, err);
+    return cudaGetLastError();
+}
+
+template <int CO, int CI>
+cudaError_t wgrad_tc_launch(const __nv_bfloat16* gy, const __nv_bfloat16* x, Grid3 g, int co_real, int ci_real,
+                            float* dw, int32_t* err, cudaStream_t st) {
+    constexpr uint32_t smem = ring_bytes(128u * CO * 2, 128u * CI * 2);
+    CUtensorMap gm, xm;
+    cudaError_t e = act_map(&gm, gy, g, CO);
+    if (e == cudaSuccess) e = act_map(&xm, x, g, CI);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_wgrad_tc<CO, CI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int64_t nb = bricks(g);
+    const int per = (int)std::max<int64_t>(1, std::min<int64_t>(16, nb / 64));   // bricks (K = 128 each) per CTA
+    const dim3 grid((unsigned)((nb + per - 1) / per), 27);
+    k_wgrad_tc<CO, CI><<<grid, 128, smem, st>>>(gm, xm, g, nb, per, co_real, ci_real, dw, err);
     return cudaGetLastError();
 }
 
@@ -594,12 +856,13 @@ cudaError_t conv_launch(int kc, int nc, const __nv_bfloat16* x, Grid3 g, const _
 }
 
 inline cudaError_t wgrad_launch(int co, int ci, const __nv_bfloat16* gy, const __nv_bfloat16* x, Grid3 g, int co_real,
-                                int ci_real, float* dw, cudaStream_t st) {
+                                int ci_real, float* dw, cudaStream_t st, bool tc = false, int32_t* err = nullptr) {
     const int64_t nv = (int64_t)g.n * g.D * g.H * g.W;
     const int chunk = 512;
     const dim3 grid((unsigned)((nv + chunk - 1) / chunk), 27);
 #define LCC_WG(CO, CI)                                                                                   \
     if (co == CO && ci == CI) {                                                                          \
+        if (tc) return wgrad_tc_launch<CO, CI>(gy, x, g, co_real, ci_real, dw, err, st);                 \
         k_conv_wgrad<CO, CI><<<grid, 128, 0, st>>>(gy, x, g, chunk, co_real, ci_real, dw);               \
         return cudaGetLastError();                                                                       \
     }
@@ -629,7 +892,7 @@ struct falcon_lcc {
     bf16 *wf[kLayers] = {}, *wb[kLayers] = {};
     int64_t adam_t = 0;
     Grid3 shape{0, 0, 0, 0};
-    bool use_tc = false;              // convolutions on tcgen05 (else mma.sync)
+    bool use_tc = true;               // convolutions on tcgen05 (else mma.sync)
     int32_t* dflag = nullptr;         // device: a tcgen05 kernel's wait ran out
     struct Acts {
         bf16 *x0, *a1, *s0, *p0, *a2, *s1, *p1, *s2, *p2, *a5, *u2, *a6, *u1, *a7, *u0, *a8, *gb;
@@ -746,7 +1009,7 @@ cudaError_t backward(falcon_lcc* net, cudaStream_t st) {
         const int64_t n = nv(g) * cop;
         k_relu_grad<<<ew_grid(n), 256, 0, st>>>(dy, y, n, kSpec[l].relu ? 1 : 0, A.gb);
         k_bias_grad<<<ew_grid(n), 256, 0, st>>>(A.gb, nv(g), cop, co, net->g + net->boff[l]);
-        cudaError_t e2 = wgrad_launch(cop, cip, A.gb, x, g, co, ci, net->g + net->woff[l], st);
+        cudaError_t e2 = wgrad_launch(cop, cip, A.gb, x, g, co, ci, net->g + net->woff[l], st, net->use_tc, net->dflag);
         if (e2 != cudaSuccess || !dx) return e2;
         return conv_launch<2>(cop, cip, A.gb, g, net->wb[l], nullptr, 0, nullptr, dx, st, net->use_tc, net->dflag);
     };

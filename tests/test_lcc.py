@@ -6,7 +6,8 @@ Tolerances: the GPU stores activations and activation gradients in BF16 and
 accumulates in FP32; the oracle rounds the same tensors to BF16 and
 accumulates in FP64, so the remaining differences are accumulation order and
 the BF16 roundings that it flips: relative L2 error <= 1e-2 for outputs and
-the loss, <= 3e-2 per layer for gradients.
+the loss; per layer, gradients within 5e-3 (last layer), 1e-2 (the one before)
+and 3e-2 (deeper layers, behind more BF16-rounded activation gradients).
 """
 import numpy as np
 import pytest
@@ -71,9 +72,15 @@ def test_gpu_forward_and_gradients_match_oracle(built_lib, path):
     lo, go = O.loss_and_grads(p.astype(np.float64), x, t)
     assert abs(loss - lo) <= 1e-2 * lo, (loss, lo)
     offs = np.cumsum([0] + [co * ci * 27 + co for ci, co in O.LAYERS])
-    for l in range(len(O.LAYERS)):
-        sl = slice(offs[l], offs[l + 1])
-        assert _rel(g[sl], go[sl]) <= 3e-2, (l, _rel(g[sl], go[sl]))
+    errs = [_rel(g[offs[l]:offs[l + 1]], go[offs[l]:offs[l + 1]]) for l in range(len(O.LAYERS))]
+    print("%s vs oracle: forward %.2e, loss %.2e, gradients per layer %s" % (
+        path, _rel(y, yo), abs(loss - lo) / lo, " ".join("%.1e" % e for e in errs)))
+    # the bound grows with the layers between the loss and the weights: each
+    # one rounds another activation gradient to BF16 (measured on this case:
+    # 1.4e-3 and 3.2e-3 for the last two layers, 2.2e-2 at most)
+    bounds = [3e-2] * 8 + [1e-2, 5e-3]
+    for l, e in enumerate(errs):
+        assert e <= bounds[l], (l, e)
 
 
 @pytest.mark.gpu
