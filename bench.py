@@ -506,6 +506,37 @@ def _smooth_field(shape, rs):
     return x
 
 
+def lcc_kernel_bench(x, t, device, reps=20):
+    """The learned correction's network on one training batch (8 panels of
+    16x32x96 coarse cells) through the host API, per tensor-core path: a
+    forward pass and a loss-and-gradient pass (wall time per call, inputs
+    copied in and results out), and one training step (device-resident)."""
+    from falcon_gb300 import lcc as L
+    out = {}
+    for path, name in ((L.TCGEN05, "tcgen05"), (L.MMA_SYNC, "mma_sync")):
+        net = L.LCC(device=device, seed=3)
+        net.set_tensor_path(path)
+        net.forward(x)
+        net.loss_grad(x, t)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            net.forward(x)
+        fwd = (time.perf_counter() - t0) / reps
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            net.loss_grad(x, t)
+        bwd = (time.perf_counter() - t0) / reps
+        X, T = np.repeat(x, 4, axis=0), np.repeat(t, 4, axis=0)
+        net.train(X, T, epochs=1, batch=8, lr=1e-4, seed=1)
+        t0 = time.perf_counter()
+        net.train(X, T, epochs=5, batch=8, lr=1e-4, seed=1)
+        step = (time.perf_counter() - t0) / 20
+        out[name] = {"forward_ms": round(fwd * 1e3, 3), "loss_grad_ms": round(bwd * 1e3, 3),
+                     "train_step_ms": round(step * 1e3, 3)}
+        net.close()
+    return out
+
+
 def solver_bench(device):
     """The implicit-solver workloads, each solved once after a warm-up solve:
     conduction MG-PCG at 64x128x384 cells per panel, the learned coarse
@@ -523,22 +554,30 @@ def solver_bench(device):
     out["conduction_64x128x384"] = {"cells": sv.nblocks * sv.nint, "tol": 1e-8, "mg_pcg": mg, "plain_cg": cg,
                                      "tile": sv.tuning()}
     sv.close()
-    # training pairs from real solves: 3 systems x 4 right-hand sides
-    X, T = [], []
-    for s in range(3):
-        sv = S.Solver(S.conduction_spec(seed=3101 + 17 * s, device=device))
+    # 2,000 training pairs (one panel's coarsest-level residual and exact
+    # coarse error each) from real solves of the 64x128x384 system: systems
+    # seeded 2000, 2001, ... (T and B), 8 smooth right-hand sides each
+    X, T, npairs, s = [], [], 2000, 0
+    t_rec = time.time()
+    while sum(len(x) for x in X) < npairs:
+        sv = S.Solver(S.conduction_spec(seed=2000 + s, device=device))
         rs = np.random.default_rng(200 + s)
-        for r in range(4):
+        for r in range(8):
             sv.set_rhs(sv.apply(_smooth_field((sv.nblocks,) + sv.m[::-1], rs)))
             x, t = sv.record(tol=1e-8, max_iter=100, max_records=16)
             X.append(x)
             T.append(t)
+            if sum(len(x) for x in X) >= npairs:
+                break
         sv.close()
-    X, T = np.concatenate(X), np.concatenate(T)
+        s += 1
+    X, T = np.concatenate(X)[:npairs], np.concatenate(T)[:npairs]
+    record_s = time.time() - t_rec
     net = LCC(device=device, seed=11)
     t1 = time.time()
     losses = net.train(X, T, epochs=20, batch=8, lr=1e-3, seed=3)
     train_s = time.time() - t1
+    lcc_kernels = lcc_kernel_bench(X[:8], T[:8], device)
     sv = S.Solver(S.conduction_spec(nr=96, nt=192, np_=576, seed=9999, device=device))
     sv.attach_lcc(net, sweeps=2)
     res = {}
@@ -546,7 +585,9 @@ def solver_bench(device):
         sv.solve(tol=1e-8, max_iter=600, precond=pc, check=False)
         res[name] = sv.solve(tol=1e-8, max_iter=600, precond=pc, check=False)
     out["learned_vs_mg_96x192x576"] = {
-        "cells": sv.nblocks * sv.nint, "tol": 1e-8, "training_pairs": int(len(X)), "train_s": round(train_s, 2),
+        "cells": sv.nblocks * sv.nint, "tol": 1e-8, "training_pairs": int(len(X)), "training_systems": s,
+        "record_s": round(record_s, 2), "train_s": round(train_s, 2), "train_epochs": 20,
+        "tensor_path": "tcgen05", "network_kernels": lcc_kernels,
         "epoch_loss_first_last": [float(losses[0]), float(losses[-1])], **res,
         "time_ratio_learned_over_mg": res["learned_fcg"]["ms"] / res["mg_pcg"]["ms"]}
     sv.close()
