@@ -99,3 +99,50 @@ class LCC:
                                          C.c_int32(W), C.c_int32(epochs), C.c_int32(batch), C.c_float(lr),
                                          C.c_uint64(seed), _ptr(losses)))
         return losses
+
+
+def _main(argv=None):
+    """Command line: the network's forward and loss-and-gradient passes on a
+    batch of seeded random panels, per tensor-core path, wall time per call.
+
+    python -m falcon_gb300.lcc --batch 2 --shape 16 32 96 --path tcgen05 --reps 1
+    """
+    import argparse
+    import json
+    import time
+
+    from . import build
+    ap = argparse.ArgumentParser(prog="python -m falcon_gb300.lcc")
+    ap.add_argument("--batch", type=int, default=8)
+    ap.add_argument("--shape", type=int, nargs=3, default=(16, 32, 96), metavar=("D", "H", "W"))
+    ap.add_argument("--path", choices=("tcgen05", "mma_sync", "both"), default="both")
+    ap.add_argument("--reps", type=int, default=20)
+    ap.add_argument("--device", type=int, default=0)
+    a = ap.parse_args(argv)
+    build()
+    rs = np.random.default_rng(1)
+    x = rs.normal(size=(a.batch,) + tuple(a.shape) + (CIN,)).astype(np.float32)
+    t = rs.normal(size=(a.batch,) + tuple(a.shape)).astype(np.float32)
+    paths = {"tcgen05": TCGEN05, "mma_sync": MMA_SYNC}
+    for name in (("tcgen05", "mma_sync") if a.path == "both" else (a.path,)):
+        net = LCC(device=a.device, seed=3)
+        net.set_tensor_path(paths[name])
+        net.forward(x)
+        net.loss_grad(x, t)
+        t0 = time.perf_counter()
+        for _ in range(a.reps):
+            net.forward(x)
+        t1 = time.perf_counter()
+        for _ in range(a.reps):
+            net.loss_grad(x, t)
+        t2 = time.perf_counter()
+        print(json.dumps({"path": name, "batch": a.batch, "shape": list(a.shape),
+                          "forward_ms": (t1 - t0) / max(a.reps, 1) * 1e3,
+                          "loss_grad_ms": (t2 - t1) / max(a.reps, 1) * 1e3}))
+        net.close()
+    return 0
+
+
+if __name__ == "__main__":
+    import sys
+    sys.exit(_main())
