@@ -83,17 +83,35 @@ cudaError_t stage_any(const StepDims& d, const Geometry& g, const T* in, const T
     return cudaErrorInvalidValue;
 }
 
+// FP32 16^3 blocks: the k-march kernel (any k-chunk depth asked for)
+inline cudaError_t diff_march16(const StepDims& d, const Geometry& g, const float* u, float* out, int8_t* lo,
+                                const PushTable& push, StepScalars* sc, int cfl_next, cudaStream_t st) {
+    using S = MShape<16, 16, 16>;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_diffusion_march<16, 16, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)S::smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    k_diffusion_march<16, 16, 16><<<d.nblocks, S::NT, S::smem, st>>>(u, out, lo, push, g, sc, cfl_next);
+    return cudaGetLastError();
+}
+
 template <class T>
 cudaError_t diff_any(const StepDims& d, const Geometry& g, const T* u, T* out, int8_t* lo, const PushTable& push,
                      StepScalars* sc, int kpar, cudaStream_t st, int cfl_next = 0) {
     if (push.tgt != nullptr && out == u) return cudaErrorInvalidValue;   // pushing needs out != u
+    if constexpr (!Pol<T>::exact) {
+        if (d.ni == 16 && d.nj == 16 && d.nk == 16) return diff_march16(d, g, u, out, lo, push, sc, cfl_next, st);
+    }
 #define FALCON_DIFF_CASE(N, K) \
     if (d.ni == N && kpar == K) return diff_n<T, N, K>(d, g, u, out, lo, push, sc, cfl_next, st);
     if (d.ni != d.nj || d.ni != d.nk) return cudaErrorInvalidValue;
     FALCON_DIFF_CASE(8, 2) FALCON_DIFF_CASE(8, 4)
     FALCON_DIFF_CASE(16, 1)
     // (16, 4) would need more than 227 KB of shared memory for its face arrays
-    if constexpr (!Pol<T>::exact) { FALCON_DIFF_CASE(8, 8) FALCON_DIFF_CASE(16, 2) }
+    if constexpr (!Pol<T>::exact) { FALCON_DIFF_CASE(8, 8) }
 #undef FALCON_DIFF_CASE
     return cudaErrorInvalidValue;
 }

@@ -1040,6 +1040,280 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
 }
 
 // ---------------------------------------------------------------------------
+// FP32 artificial diffusion of one 16^3 block as a march along k (the mixed
+// step's diffusion pass; same arguments and results as k_diffusion).
+//
+// One thread per (i, j) column of the block (256 threads), marching k over the
+// 16 interior planes. Along k everything stays in registers: the column's
+// values at planes kp and kp+1, its k slope at kp and the flux through the
+// face below kp; per plane the thread reads one new value per variable (plane
+// kp+2, from the ring), forms one k slope and one k face. Across the plane,
+// every i and j slope is formed once (phase A, into shared memory, ghost
+// columns and rows by the same threads), then every i and j face flux once
+// (phase B), then each cell sums its six faces and updates (phase C). Per
+// cell and variable that is 3 slopes and 3 fluxes, the minimum; the face
+// fluxes are the same functions of the same values as k_diffusion's, summed
+// in the same order.
+//
+// Planes arrive by bulk copy into a ring of 5 slots, one mbarrier each: the
+// column window needs planes kp..kp+2, and the slot of plane kp is refilled
+// with plane kp+5 once phase B of plane kp has passed its barrier (planes
+// kp+3 and kp+4 are in flight meanwhile). A warp
+// takes rows j and j+4 (half-warps of 16 cells): with a row pitch of 20
+// floats the two halves touch disjoint banks in the tile and in the slope and
+// face arrays; a half-warp holds one row, as the pushed radial faces need.
+template <int NI, int NJ, int NK>
+struct MShape {
+    static constexpr int NG = 2, NIP = NI + 4, NJP = NJ + 4, NKP = NK + 4;
+    static constexpr int PL = NIP * NJP, NCELL = PL * NKP, NT = NI * NJ;
+    static constexpr int W = 5;                          // plane ring slots
+    static constexpr int PLI = NI * NJ, NINT = PLI * NK;
+    static constexpr uint32_t PLB = PL * 4u;
+    static constexpr int P = 20;                         // row pitch of the slope and face arrays
+    // per variable: SI[NJ][P] slopes along i of cells i = -1..NI at i + 1;
+    // SJ[NJ + 2][P] slopes along j of rows j = -1..NJ at row j + 1;
+    // FI[NJ][P] fluxes through faces i - 1/2, i = 0..NI; FJ[NJ + 1][P] likewise along j
+    static constexpr int NSI = NJ * P, NSJ = (NJ + 2) * P, NFI = NJ * P, NFJ = (NJ + 1) * P;
+    // shared memory: mbarriers | tile[NV][W][PL] | SI | SJ | FI | FJ | gi | gj | gs
+    static constexpr size_t off_tile = 64;
+    static constexpr size_t off_si = off_tile + (size_t)NV * W * PL * 4;
+    static constexpr size_t off_sj = off_si + (size_t)NV * NSI * 4;
+    static constexpr size_t off_fi = off_sj + (size_t)NV * NSJ * 4;
+    static constexpr size_t off_fj = off_fi + (size_t)NV * NFI * 4;
+    static constexpr size_t off_gi = off_fj + (size_t)NV * NFJ * 4;
+    static constexpr size_t off_gj = off_gi + (size_t)GI_COUNT * NIP * 4;
+    static constexpr size_t off_gs = off_gj + (size_t)GJ_COUNT * NJP * 4;
+    static constexpr size_t smem = off_gs + GS_COUNT * 4;
+    static_assert(W * 8 <= (int)off_tile, "mbarriers");
+};
+
+template <int NI, int NJ, int NK>
+__global__ void __launch_bounds__(NI * NJ, 2)
+k_diffusion_march(const float* u, float* out, int8_t* ulo, PushTable push, Geometry g, StepScalars* sc, int cfl_next) {
+    using S = MShape<NI, NJ, NK>;
+    static_assert(NI == 16 && NJ == 16, "rows of 16 cells: one half-warp per row");
+    static_assert(2 * (S::smem + 1024) <= 233472, "two CTAs per SM");
+    constexpr int NIP = S::NIP, PL = S::PL, W = S::W, NCELL = S::NCELL, P = S::P;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
+    float* tile = reinterpret_cast<float*>(smem + S::off_tile);
+    float* SI = reinterpret_cast<float*>(smem + S::off_si);
+    float* SJ = reinterpret_cast<float*>(smem + S::off_sj);
+    float* FI = reinterpret_cast<float*>(smem + S::off_fi);
+    float* FJ = reinterpret_cast<float*>(smem + S::off_fj);
+    float* gi = reinterpret_cast<float*>(smem + S::off_gi);
+    float* gj = reinterpret_cast<float*>(smem + S::off_gj);
+    float* gs = reinterpret_cast<float*>(smem + S::off_gs);
+    const int b = blockIdx.x, tid = threadIdx.x;
+    const float* blk = u + (size_t)b * NV * NCELL;
+    float* oblk = out + (size_t)b * NV * NCELL;
+    const int flb = g.flags[b];
+    const bool copy_bc = out != u && (flb & 6);
+    __shared__ PushBlock pb;
+    load_push_block(push, b, &pb);
+    if (tid == 0) {
+        for (int s = 0; s < W; ++s) mbar_init(&bars[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    int issued = 0;   // thread 0: planes [0, issued) have been requested
+    if (tid == 0) {
+        for (int p = 0; p < W; ++p) issue_planes<float, S>(blk, tile, p, p + 1, &bars[p]);
+        issued = W;
+    }
+    const int8_t* blk_lo = ulo != nullptr ? ulo + (size_t)b * NV * S::NINT : nullptr;
+    if (blk_lo != nullptr && tid < NV) prefetch_l2(blk_lo + (size_t)tid * S::NINT, 2 * S::PLI);
+    load_geometry<float, S>(g, b, gi, gj, gs, nullptr);
+    __syncthreads();   // the geometry tables are read by every thread below
+    // this thread's column: warp w takes rows (w % 4) + 8 (w / 4) and that + 4
+    const int wq = tid >> 5, i = tid & 15;
+    const int j = (wq & 3) + 8 * (wq >> 2) + 4 * ((tid >> 4) & 1);
+    const int ii = i + 2, jj = j + 2;
+    const float* GCS = gi + GI_CS * NIP;
+    const float cs = GCS[ii];
+    const float rc = gi[GI_R * NIP + ii];
+    const float den[3] = {gs[GS_DXI], gs[GS_DXJ] * rc, gs[GS_DXK] * rc * gj[GJ_SIN * S::NJP + jj]};
+    const float dinv[3] = {1.f / den[0], 1.f / den[1], 1.f / den[2]};
+    const float hdt_f = sc->dt_half_f;
+    const int polls = sc->wait_polls;
+    int late = 0;   // a wait of this thread for a plane ran out
+    auto abort_cta = [&]() {   // after a uniform decision: flag, drain the copies in flight
+        if (tid != 0) return;
+        atomicOr(&sc->nan_flag, 2);
+        for (int p = issued - W < 0 ? 0 : issued - W; p < issued; ++p)
+            mbar_wait(&bars[p % W], (uint32_t)((p / W) & 1), kWaitPolls);
+    };
+    // radial boundary ghost columns of planes [plo, phi), u -> out
+    auto copy_cols = [&](int plo, int phi) {
+        const int total = (phi - plo) * S::NJP * NV * 4;
+        for (int x = tid; x < total; x += S::NT) {
+            const int c4 = x & 3, r = x >> 2;
+            const int v = r % NV, r2 = r / NV;
+            const int y = r2 % S::NJP, z = plo + r2 / S::NJP;
+            if (!((c4 < 2) ? (flb & 4) : (flb & 2))) continue;
+            const int xi = c4 < 2 ? c4 : NI + c4;   // 0, 1 (bottom) or NI+2, NI+3 (top)
+            oblk[((size_t)v * S::NKP + z) * PL + y * NIP + xi] = tile[(v * W + z % W) * PL + y * NIP + xi];
+        }
+    };
+    // the column window from planes 0..3: u at kp = 2 and 3, the k slope at 2,
+    // the flux through the face between planes 1 and 2
+    for (int p = 0; p < 4; ++p) late |= mbar_wait(&bars[p], 0u, polls) ? 0 : 1;
+    if (copy_bc) copy_cols(0, 4);
+    const float* col = tile + jj * NIP + ii;
+    float u0[NV], u1[NV], dk0[NV], fk0[NV];
+    {
+        const float cL = fabsf(col[(V_VP * W + 1) * PL]) + cs, cR = fabsf(col[(V_VP * W + 2) * PL]) + cs;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            const float a0 = col[(v * W + 0) * PL], a1 = col[(v * W + 1) * PL];
+            const float a2 = col[(v * W + 2) * PL], a3 = col[(v * W + 3) * PL];
+            const float d1 = face_slope(a0, a1, a2), d2 = face_slope(a1, a2, a3);
+            u0[v] = a2;
+            u1[v] = a3;
+            dk0[v] = d2;
+            fk0[v] = face_flux_s(a1, a2, d1, d2, cL, cR);
+        }
+    }
+    float cmin = INFINITY;   // next step's CFL ratio minimum over this column
+    int cnan = 0;
+    for (int kp = 2; kp < NK + 2; ++kp) {
+        const int p2 = kp + 2;
+        if (blk_lo != nullptr && tid < NV && kp < NK) prefetch_l2(blk_lo + (size_t)tid * S::NINT + (size_t)kp * S::PLI, S::PLI);
+        // this cell's int8 corrections, loaded before the wait
+        int8_t qlo[NV];
+        if (ulo != nullptr) {
+            const int8_t* q = blk_lo + ((size_t)(kp - 2) * NJ + j) * NI + i;
+#pragma unroll
+            for (int v = 0; v < NV; ++v) qlo[v] = q[(size_t)v * S::NINT];
+        }
+        // a wait that runs out finishes the plane on whatever the slot holds;
+        // the step is flagged and discarded
+        late |= mbar_wait(&bars[p2 % W], (uint32_t)((p2 / W) & 1), polls) ? 0 : 1;
+        if (copy_bc) copy_cols(p2, p2 + 1);
+        const int s0 = (kp % W) * PL, s2 = (p2 % W) * PL;
+        const float* tc = tile + s0 + jj * NIP + ii;   // this cell in plane kp (+ v W PL)
+        // ---- phase A: k slope and k face from the window; i and j slopes
+        float u2[NV], dk1[NV], fk1[NV];
+        {
+            const float cLk = fabsf(u0[V_VP]) + cs, cRk = fabsf(u1[V_VP]) + cs;
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+                u2[v] = col[v * W * PL + s2];
+                dk1[v] = face_slope(u0[v], u1[v], u2[v]);
+                fk1[v] = face_flux_s(u0[v], u1[v], dk0[v], dk1[v], cLk, cRk);
+                const float* a = tc + v * W * PL;
+                SI[v * S::NSI + j * P + i + 1] = face_slope(a[-1], u0[v], a[1]);
+                SJ[v * S::NSJ + (j + 1) * P + i] = face_slope(a[-NIP], u0[v], a[NIP]);
+            }
+        }
+        // slopes of the ghost cells next to the block: i = -1, NI of every row
+        // (items 0..255) and j = -1, NJ of every column (items 256..511)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int x = tid + h * S::NT;
+            const int side = x & 1, r = (x >> 1) & 15, v = (x >> 5) & 7;
+            const float* a = tile + v * W * PL + s0;
+            if (h == 0) {
+                const int xi = side ? NI + 2 : 1;
+                const float* q = a + (r + 2) * NIP + xi;
+                SI[v * S::NSI + r * P + (side ? NI + 1 : 0)] = face_slope(q[-1], q[0], q[1]);
+            } else {
+                const int yj = side ? NJ + 2 : 1;
+                const float* q = a + yj * NIP + r + 2;
+                SJ[v * S::NSJ + (side ? NJ + 1 : 0) * P + r] = face_slope(q[-NIP], q[0], q[NIP]);
+            }
+        }
+        if (__syncthreads_or(late)) {
+            abort_cta();
+            return;
+        }
+        // ---- phase B: the faces i - 1/2 and j - 1/2 of this cell, and the
+        // last faces of the rows (items 0..127) and columns (128..255)
+        float fi0[NV], fj0[NV];
+        {
+            const float cLi = fabsf(tc[V_VR * W * PL - 1]) + GCS[ii - 1], cRi = fabsf(tc[V_VR * W * PL]) + cs;
+            const float cLj = fabsf(tc[V_VT * W * PL - NIP]) + cs, cRj = fabsf(tc[V_VT * W * PL]) + cs;
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+                const float* a = tc + v * W * PL;
+                const float* si = SI + v * S::NSI + j * P + i;
+                const float* sj = SJ + v * S::NSJ + j * P + i;
+                fi0[v] = face_flux_s(a[-1], u0[v], si[0], si[1], cLi, cRi);
+                fj0[v] = face_flux_s(a[-NIP], u0[v], sj[0], sj[P], cLj, cRj);
+                FI[v * S::NFI + j * P + i] = fi0[v];
+                FJ[v * S::NFJ + j * P + i] = fj0[v];
+            }
+        }
+        {
+            const int x = tid, r = x & 15, v = (x >> 4) & 7;
+            if (x < 128) {
+                const float* a = tile + v * W * PL + s0 + (r + 2) * NIP + NI + 1;   // last interior cell of row r
+                const float* vr = tile + V_VR * W * PL + s0 + (r + 2) * NIP + NI + 1;
+                const float cL = fabsf(vr[0]) + GCS[NI + 1], cR = fabsf(vr[1]) + GCS[NI + 2];
+                const float* si = SI + v * S::NSI + r * P + NI;
+                FI[v * S::NFI + r * P + NI] = face_flux_s(a[0], a[1], si[0], si[1], cL, cR);
+            } else {
+                const float* a = tile + v * W * PL + s0 + (NJ + 1) * NIP + r + 2;   // last interior row, column r
+                const float* vt = tile + V_VT * W * PL + s0 + (NJ + 1) * NIP + r + 2;
+                const float c2 = GCS[r + 2];
+                const float cL = fabsf(vt[0]) + c2, cR = fabsf(vt[NIP]) + c2;
+                const float* sj = SJ + v * S::NSJ + NJ * P + r;
+                FJ[v * S::NFJ + NJ * P + r] = face_flux_s(a[0], a[NIP], sj[0], sj[P], cL, cR);
+            }
+        }
+        __syncthreads();
+        // planes below kp + 1 are done with: refill their slots, up to plane
+        // kp + W (at kp = 2 that is planes 5, 6, 7; then one plane a step)
+        if (tid == 0) {
+            for (; issued < S::NKP && issued <= kp + W; ++issued)
+                issue_planes<float, S>(blk, tile, issued, issued + 1, &bars[issued % W]);
+        }
+        // ---- phase C: sum the six faces in the reference's order, update
+        const size_t base = (size_t)kp * PL + jj * NIP + ii;
+        float o[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            float R = 0.f;
+            R = R + Pol<float>::dv(fi0[v] - FI[v * S::NFI + j * P + i + 1], den[0], dinv[0]);
+            R = R + Pol<float>::dv(fj0[v] - FJ[v * S::NFJ + (j + 1) * P + i], den[1], dinv[1]);
+            R = R + Pol<float>::dv(fk0[v] - fk1[v], den[2], dinv[2]);
+            if (ulo != nullptr) {
+                int8_t q1;
+                o[v] = ff_add(u0[v], qlo[v], __fmul_rn(hdt_f, R), q1);
+                ulo[((size_t)b * NV + v) * S::NINT + ((size_t)(kp - 2) * NJ + j) * NI + i] = q1;
+            } else {
+                o[v] = fmaf(hdt_f, R, u0[v]);
+            }
+            oblk[(size_t)v * NCELL + base] = o[v];
+        }
+        if (push.tgt != nullptr) push_faces_part<float, S, NV>(out, pb, ii, jj, kp, o, 0);
+        if (cfl_next) {   // uniform over the CTA
+#pragma unroll
+            for (int v = 0; v < NV; ++v) cnan |= (o[v] != o[v]);
+            const float v2 = cfl_sq3(o[V_VR], o[V_VT], o[V_VP]);
+            const float b2 = cfl_sq3(o[V_BR], o[V_BT], o[V_BP]);
+            float ratio = cfl_ratio_f(v2, b2, cs, gi[GI_RHO0 * NIP + ii], rc, gj[GJ_SIN * S::NJP + jj], gs[GS_DXI],
+                                      gs[GS_DXJ], gs[GS_DXK]);
+            if (ratio != ratio) { cnan = 1; ratio = INFINITY; }
+            cmin = fminf(cmin, ratio);
+        }
+        // the window moves up one plane
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            u0[v] = u1[v];
+            u1[v] = u2[v];
+            dk0[v] = dk1[v];
+            fk0[v] = fk1[v];
+        }
+    }
+    if (__syncthreads_or(late)) {
+        abort_cta();
+        return;
+    }
+    if (cfl_next) cfl_commit(cmin, cnan, sc);
+}
+
+// ---------------------------------------------------------------------------
 // Wave speed (3_6/ModWaveSpeed.f90:8-27), h/v_wave min-reduction
 // (3_6/ModTimeStep.f90:10-30) and the NaN scan of 3_6/ModCheck.f90:12-71.
 template <class T>
