@@ -1040,6 +1040,50 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
 }
 
 // ---------------------------------------------------------------------------
+// Packed FP32 pairs (Blackwell's two-lane FFMA2/FADD2/FMUL2): the diffusion
+// march below runs its slopes, fluxes and update on variables v and v+1 at
+// once. Each helper gives bit for bit what its scalar counterpart gives (a
+// difference a - b is formed as fma(b, -1, a), one rounding of the exact
+// difference, as FADD does).
+__device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
+__device__ __forceinline__ float2 f2(float x) { return make_float2(x, x); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.f), a); }
+__device__ __forceinline__ float2 max02(float2 a) { return f2(fmaxf(0.f, a.x), fmaxf(0.f, a.y)); }
+// minmod_sel for two variables
+__device__ __forceinline__ float2 minmod_sel2(float2 ul, float2 u, float2 ur) {
+    const float2 a = __fmul2_rn(sub2(ur, ul), f2(0.5f));
+    const float2 b = __fmul2_rn(sub2(ur, u), f2(2.f));
+    const float2 c = __fmul2_rn(sub2(u, ul), f2(2.f));
+    const float2 x = __fmul2_rn(__fmul2_rn(max02(__fmul2_rn(a, b)), f2(1.e10f)), max02(__fmul2_rn(b, c)));
+    const float mx = fminf(fminf(fabsf(a.x), fabsf(b.x)), fabsf(c.x));
+    const float my = fminf(fminf(fabsf(a.y), fabsf(b.y)), fabsf(c.y));
+    return f2(x.x >= 1.e-30f ? copysignf(mx, a.x) : 0.f, x.y >= 1.e-30f ? copysignf(my, a.y) : 0.f);
+}
+// face_flux_s<float> for two variables; cc = -0.25 (cR + cL), the face's
+// speed factor (the same for every variable; -0.25 scales exactly, so
+// (phi num) cc is the scalar form's ((-0.25 phi) num)(cR + cL) bit for bit)
+__device__ __forceinline__ float2 face_flux2(float2 fl, float2 fr, float2 dL, float2 dR, float2 cc) {
+    const float2 num = __ffma2_rn(dL, f2(-0.5f), sub2(__ffma2_rn(dR, f2(-0.5f), fr), fl));
+    const float2 den = sub2(fr, fl);
+    const float2 r = __ffma2_rn(f2(__fdividef(num.x, den.x), __fdividef(num.y, den.y)), f2(2.f), f2(-1.f));
+    return __fmul2_rn(__fmul2_rn(max02(r), num), cc);
+}
+// ff_add for two variables
+__device__ __forceinline__ float2 ff_add2(float2 hi, int8_t q0, int8_t q1, float2 d, int8_t& o0, int8_t& o1) {
+    const float2 l = f2(__fmul_rn((float)q0, lo_unit(hi.x)), __fmul_rn((float)q1, lo_unit(hi.y)));
+    const float2 s = __fadd2_rn(hi, d);
+    const float2 bs = sub2(s, hi);
+    const float2 es = __fadd2_rn(sub2(hi, sub2(s, bs)), sub2(d, bs));
+    const float2 t = __fadd2_rn(es, l);
+    const float2 h = __fadd2_rn(s, t);
+    const float2 bh = sub2(h, s);
+    const float2 r = __fadd2_rn(sub2(s, sub2(h, bh)), sub2(t, bh));
+    o0 = lo_encode(h.x, r.x);
+    o1 = lo_encode(h.y, r.y);
+    return h;
+}
+
+// ---------------------------------------------------------------------------
 // FP32 artificial diffusion of one 16^3 block as a march along k (the mixed
 // step's diffusion pass; same arguments and results as k_diffusion).
 //
@@ -1053,38 +1097,41 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
 // (phase B), then each cell sums its six faces and updates (phase C). Per
 // cell and variable that is 3 slopes and 3 fluxes, the minimum; the face
 // fluxes are the same functions of the same values as k_diffusion's, summed
-// in the same order.
+// in the same order. The arithmetic runs on pairs of variables (packed FP32
+// instructions, above), and the slope and face arrays hold the pairs side by
+// side, so their shared-memory accesses are 64-bit.
 //
 // Planes arrive by bulk copy into a ring of 5 slots, one mbarrier each: the
 // column window needs planes kp..kp+2, and the slot of plane kp is refilled
 // with plane kp+5 once phase B of plane kp has passed its barrier (planes
-// kp+3 and kp+4 are in flight meanwhile). A warp
-// takes rows j and j+4 (half-warps of 16 cells): with a row pitch of 20
-// floats the two halves touch disjoint banks in the tile and in the slope and
-// face arrays; a half-warp holds one row, as the pushed radial faces need.
+// kp+3 and kp+4 are in flight meanwhile). A warp takes rows j and j+4
+// (half-warps of 16 cells), so a half-warp holds one row, as the pushed
+// radial faces need.
 template <int NI, int NJ, int NK>
 struct MShape {
     static constexpr int NG = 2, NIP = NI + 4, NJP = NJ + 4, NKP = NK + 4;
     static constexpr int PL = NIP * NJP, NCELL = PL * NKP, NT = NI * NJ;
     static constexpr int W = 5;                          // plane ring slots
     static constexpr int PLI = NI * NJ, NINT = PLI * NK;
+    static constexpr int NP = NV / 2;                    // variable pairs
     static constexpr uint32_t PLB = PL * 4u;
-    static constexpr int P = 20;                         // row pitch of the slope and face arrays
-    // per variable: SI[NJ][P] slopes along i of cells i = -1..NI at i + 1;
+    static constexpr int P = 20;                         // row pitch (pairs) of the slope and face arrays
+    // per pair (float2): SI[NJ][P] slopes along i of cells i = -1..NI at i + 1;
     // SJ[NJ + 2][P] slopes along j of rows j = -1..NJ at row j + 1;
     // FI[NJ][P] fluxes through faces i - 1/2, i = 0..NI; FJ[NJ + 1][P] likewise along j
     static constexpr int NSI = NJ * P, NSJ = (NJ + 2) * P, NFI = NJ * P, NFJ = (NJ + 1) * P;
     // shared memory: mbarriers | tile[NV][W][PL] | SI | SJ | FI | FJ | gi | gj | gs
     static constexpr size_t off_tile = 64;
     static constexpr size_t off_si = off_tile + (size_t)NV * W * PL * 4;
-    static constexpr size_t off_sj = off_si + (size_t)NV * NSI * 4;
-    static constexpr size_t off_fi = off_sj + (size_t)NV * NSJ * 4;
-    static constexpr size_t off_fj = off_fi + (size_t)NV * NFI * 4;
-    static constexpr size_t off_gi = off_fj + (size_t)NV * NFJ * 4;
+    static constexpr size_t off_sj = off_si + (size_t)NP * NSI * 8;
+    static constexpr size_t off_fi = off_sj + (size_t)NP * NSJ * 8;
+    static constexpr size_t off_fj = off_fi + (size_t)NP * NFI * 8;
+    static constexpr size_t off_gi = off_fj + (size_t)NP * NFJ * 8;
     static constexpr size_t off_gj = off_gi + (size_t)GI_COUNT * NIP * 4;
     static constexpr size_t off_gs = off_gj + (size_t)GJ_COUNT * NJP * 4;
     static constexpr size_t smem = off_gs + GS_COUNT * 4;
     static_assert(W * 8 <= (int)off_tile, "mbarriers");
+    static_assert(off_si % 8 == 0, "float2 arrays");
 };
 
 template <int NI, int NJ, int NK>
@@ -1093,14 +1140,14 @@ k_diffusion_march(const float* u, float* out, int8_t* ulo, PushTable push, Geome
     using S = MShape<NI, NJ, NK>;
     static_assert(NI == 16 && NJ == 16, "rows of 16 cells: one half-warp per row");
     static_assert(2 * (S::smem + 1024) <= 233472, "two CTAs per SM");
-    constexpr int NIP = S::NIP, PL = S::PL, W = S::W, NCELL = S::NCELL, P = S::P;
+    constexpr int NIP = S::NIP, PL = S::PL, W = S::W, NCELL = S::NCELL, P = S::P, NP = S::NP;
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
     float* tile = reinterpret_cast<float*>(smem + S::off_tile);
-    float* SI = reinterpret_cast<float*>(smem + S::off_si);
-    float* SJ = reinterpret_cast<float*>(smem + S::off_sj);
-    float* FI = reinterpret_cast<float*>(smem + S::off_fi);
-    float* FJ = reinterpret_cast<float*>(smem + S::off_fj);
+    float2* SI = reinterpret_cast<float2*>(smem + S::off_si);
+    float2* SJ = reinterpret_cast<float2*>(smem + S::off_sj);
+    float2* FI = reinterpret_cast<float2*>(smem + S::off_fi);
+    float2* FJ = reinterpret_cast<float2*>(smem + S::off_fj);
     float* gi = reinterpret_cast<float*>(smem + S::off_gi);
     float* gj = reinterpret_cast<float*>(smem + S::off_gj);
     float* gs = reinterpret_cast<float*>(smem + S::off_gs);
@@ -1133,8 +1180,8 @@ k_diffusion_march(const float* u, float* out, int8_t* ulo, PushTable push, Geome
     const float cs = GCS[ii];
     const float rc = gi[GI_R * NIP + ii];
     const float den[3] = {gs[GS_DXI], gs[GS_DXJ] * rc, gs[GS_DXK] * rc * gj[GJ_SIN * S::NJP + jj]};
-    const float dinv[3] = {1.f / den[0], 1.f / den[1], 1.f / den[2]};
-    const float hdt_f = sc->dt_half_f;
+    const float2 dinv0 = f2(1.f / den[0]), dinv1 = f2(1.f / den[1]), dinv2 = f2(1.f / den[2]);
+    const float2 hdt2 = f2(sc->dt_half_f);
     const int polls = sc->wait_polls;
     int late = 0;   // a wait of this thread for a plane ran out
     auto abort_cta = [&]() {   // after a uniform decision: flag, drain the copies in flight
@@ -1155,23 +1202,24 @@ k_diffusion_march(const float* u, float* out, int8_t* ulo, PushTable push, Geome
             oblk[((size_t)v * S::NKP + z) * PL + y * NIP + xi] = tile[(v * W + z % W) * PL + y * NIP + xi];
         }
     };
+    // the pair (v, v+1) of a tile value at offset o from variable 0's
+    auto tv = [&](const float* base, int p) { return f2(base[2 * p * W * PL], base[(2 * p + 1) * W * PL]); };
     // the column window from planes 0..3: u at kp = 2 and 3, the k slope at 2,
     // the flux through the face between planes 1 and 2
     for (int p = 0; p < 4; ++p) late |= mbar_wait(&bars[p], 0u, polls) ? 0 : 1;
     if (copy_bc) copy_cols(0, 4);
     const float* col = tile + jj * NIP + ii;
-    float u0[NV], u1[NV], dk0[NV], fk0[NV];
+    float2 u0[NP], u1[NP], dk0[NP], fk0[NP];
     {
-        const float cL = fabsf(col[(V_VP * W + 1) * PL]) + cs, cR = fabsf(col[(V_VP * W + 2) * PL]) + cs;
+        const float2 cc = f2(-0.25f * ((fabsf(col[(V_VP * W + 2) * PL]) + cs) + (fabsf(col[(V_VP * W + 1) * PL]) + cs)));
 #pragma unroll
-        for (int v = 0; v < NV; ++v) {
-            const float a0 = col[(v * W + 0) * PL], a1 = col[(v * W + 1) * PL];
-            const float a2 = col[(v * W + 2) * PL], a3 = col[(v * W + 3) * PL];
-            const float d1 = face_slope(a0, a1, a2), d2 = face_slope(a1, a2, a3);
-            u0[v] = a2;
-            u1[v] = a3;
-            dk0[v] = d2;
-            fk0[v] = face_flux_s(a1, a2, d1, d2, cL, cR);
+        for (int p = 0; p < NP; ++p) {
+            const float2 a0 = tv(col, p), a1 = tv(col + PL, p), a2 = tv(col + 2 * PL, p), a3 = tv(col + 3 * PL, p);
+            const float2 d1 = minmod_sel2(a0, a1, a2), d2 = minmod_sel2(a1, a2, a3);
+            u0[p] = a2;
+            u1[p] = a3;
+            dk0[p] = d2;
+            fk0[p] = face_flux2(a1, a2, d1, d2, cc);
         }
     }
     float cmin = INFINITY;   // next step's CFL ratio minimum over this column
@@ -1193,17 +1241,17 @@ k_diffusion_march(const float* u, float* out, int8_t* ulo, PushTable push, Geome
         const int s0 = (kp % W) * PL, s2 = (p2 % W) * PL;
         const float* tc = tile + s0 + jj * NIP + ii;   // this cell in plane kp (+ v W PL)
         // ---- phase A: k slope and k face from the window; i and j slopes
-        float u2[NV], dk1[NV], fk1[NV];
+        float2 u2[NP], dk1[NP], fk1[NP];
         {
-            const float cLk = fabsf(u0[V_VP]) + cs, cRk = fabsf(u1[V_VP]) + cs;
+            const float2 cc = f2(-0.25f * ((fabsf(u1[V_VP / 2].y) + cs) + (fabsf(u0[V_VP / 2].y) + cs)));
+            static_assert(V_VP % 2 == 1, "v_phi is the second of its pair");
 #pragma unroll
-            for (int v = 0; v < NV; ++v) {
-                u2[v] = col[v * W * PL + s2];
-                dk1[v] = face_slope(u0[v], u1[v], u2[v]);
-                fk1[v] = face_flux_s(u0[v], u1[v], dk0[v], dk1[v], cLk, cRk);
-                const float* a = tc + v * W * PL;
-                SI[v * S::NSI + j * P + i + 1] = face_slope(a[-1], u0[v], a[1]);
-                SJ[v * S::NSJ + (j + 1) * P + i] = face_slope(a[-NIP], u0[v], a[NIP]);
+            for (int p = 0; p < NP; ++p) {
+                u2[p] = tv(col + s2, p);
+                dk1[p] = minmod_sel2(u0[p], u1[p], u2[p]);
+                fk1[p] = face_flux2(u0[p], u1[p], dk0[p], dk1[p], cc);
+                SI[p * S::NSI + j * P + i + 1] = minmod_sel2(tv(tc - 1, p), u0[p], tv(tc + 1, p));
+                SJ[p * S::NSJ + (j + 1) * P + i] = minmod_sel2(tv(tc - NIP, p), u0[p], tv(tc + NIP, p));
             }
         }
         // slopes of the ghost cells next to the block: i = -1, NI of every row
@@ -1213,15 +1261,18 @@ k_diffusion_march(const float* u, float* out, int8_t* ulo, PushTable push, Geome
             const int x = tid + h * S::NT;
             const int side = x & 1, r = (x >> 1) & 15, v = (x >> 5) & 7;
             const float* a = tile + v * W * PL + s0;
+            float* dst;
+            float val;
             if (h == 0) {
-                const int xi = side ? NI + 2 : 1;
-                const float* q = a + (r + 2) * NIP + xi;
-                SI[v * S::NSI + r * P + (side ? NI + 1 : 0)] = face_slope(q[-1], q[0], q[1]);
+                const float* q = a + (r + 2) * NIP + (side ? NI + 2 : 1);
+                val = face_slope(q[-1], q[0], q[1]);
+                dst = reinterpret_cast<float*>(SI + (v >> 1) * S::NSI + r * P + (side ? NI + 1 : 0));
             } else {
-                const int yj = side ? NJ + 2 : 1;
-                const float* q = a + yj * NIP + r + 2;
-                SJ[v * S::NSJ + (side ? NJ + 1 : 0) * P + r] = face_slope(q[-NIP], q[0], q[NIP]);
+                const float* q = a + (side ? NJ + 2 : 1) * NIP + r + 2;
+                val = face_slope(q[-NIP], q[0], q[NIP]);
+                dst = reinterpret_cast<float*>(SJ + (v >> 1) * S::NSJ + (side ? NJ + 1 : 0) * P + r);
             }
+            dst[v & 1] = val;
         }
         if (__syncthreads_or(late)) {
             abort_cta();
@@ -1229,36 +1280,39 @@ k_diffusion_march(const float* u, float* out, int8_t* ulo, PushTable push, Geome
         }
         // ---- phase B: the faces i - 1/2 and j - 1/2 of this cell, and the
         // last faces of the rows (items 0..127) and columns (128..255)
-        float fi0[NV], fj0[NV];
+        float2 fi0[NP], fj0[NP];
         {
             const float cLi = fabsf(tc[V_VR * W * PL - 1]) + GCS[ii - 1], cRi = fabsf(tc[V_VR * W * PL]) + cs;
             const float cLj = fabsf(tc[V_VT * W * PL - NIP]) + cs, cRj = fabsf(tc[V_VT * W * PL]) + cs;
+            const float2 cci = f2(-0.25f * (cRi + cLi)), ccj = f2(-0.25f * (cRj + cLj));
 #pragma unroll
-            for (int v = 0; v < NV; ++v) {
-                const float* a = tc + v * W * PL;
-                const float* si = SI + v * S::NSI + j * P + i;
-                const float* sj = SJ + v * S::NSJ + j * P + i;
-                fi0[v] = face_flux_s(a[-1], u0[v], si[0], si[1], cLi, cRi);
-                fj0[v] = face_flux_s(a[-NIP], u0[v], sj[0], sj[P], cLj, cRj);
-                FI[v * S::NFI + j * P + i] = fi0[v];
-                FJ[v * S::NFJ + j * P + i] = fj0[v];
+            for (int p = 0; p < NP; ++p) {
+                const float2* si = SI + p * S::NSI + j * P + i;
+                const float2* sj = SJ + p * S::NSJ + j * P + i;
+                fi0[p] = face_flux2(tv(tc - 1, p), u0[p], si[0], si[1], cci);
+                fj0[p] = face_flux2(tv(tc - NIP, p), u0[p], sj[0], sj[P], ccj);
+                FI[p * S::NFI + j * P + i] = fi0[p];
+                FJ[p * S::NFJ + j * P + i] = fj0[p];
             }
         }
         {
             const int x = tid, r = x & 15, v = (x >> 4) & 7;
+            const float* sl = reinterpret_cast<const float*>(x < 128 ? SI + (v >> 1) * S::NSI + r * P + NI
+                                                                     : SJ + (v >> 1) * S::NSJ + NJ * P + r);
+            float fv;
             if (x < 128) {
                 const float* a = tile + v * W * PL + s0 + (r + 2) * NIP + NI + 1;   // last interior cell of row r
                 const float* vr = tile + V_VR * W * PL + s0 + (r + 2) * NIP + NI + 1;
                 const float cL = fabsf(vr[0]) + GCS[NI + 1], cR = fabsf(vr[1]) + GCS[NI + 2];
-                const float* si = SI + v * S::NSI + r * P + NI;
-                FI[v * S::NFI + r * P + NI] = face_flux_s(a[0], a[1], si[0], si[1], cL, cR);
+                fv = face_flux_s(a[0], a[1], sl[v & 1], sl[2 + (v & 1)], cL, cR);
+                reinterpret_cast<float*>(FI + (v >> 1) * S::NFI + r * P + NI)[v & 1] = fv;
             } else {
                 const float* a = tile + v * W * PL + s0 + (NJ + 1) * NIP + r + 2;   // last interior row, column r
                 const float* vt = tile + V_VT * W * PL + s0 + (NJ + 1) * NIP + r + 2;
                 const float c2 = GCS[r + 2];
                 const float cL = fabsf(vt[0]) + c2, cR = fabsf(vt[NIP]) + c2;
-                const float* sj = SJ + v * S::NSJ + NJ * P + r;
-                FJ[v * S::NFJ + NJ * P + r] = face_flux_s(a[0], a[NIP], sj[0], sj[P], cL, cR);
+                fv = face_flux_s(a[0], a[NIP], sl[v & 1], sl[2 * P + (v & 1)], cL, cR);
+                reinterpret_cast<float*>(FJ + (v >> 1) * S::NFJ + NJ * P + r)[v & 1] = fv;
             }
         }
         __syncthreads();
@@ -1272,19 +1326,24 @@ k_diffusion_march(const float* u, float* out, int8_t* ulo, PushTable push, Geome
         const size_t base = (size_t)kp * PL + jj * NIP + ii;
         float o[NV];
 #pragma unroll
-        for (int v = 0; v < NV; ++v) {
-            float R = 0.f;
-            R = R + Pol<float>::dv(fi0[v] - FI[v * S::NFI + j * P + i + 1], den[0], dinv[0]);
-            R = R + Pol<float>::dv(fj0[v] - FJ[v * S::NFJ + (j + 1) * P + i], den[1], dinv[1]);
-            R = R + Pol<float>::dv(fk0[v] - fk1[v], den[2], dinv[2]);
+        for (int p = 0; p < NP; ++p) {
+            float2 R = __fmul2_rn(sub2(fi0[p], FI[p * S::NFI + j * P + i + 1]), dinv0);
+            R = __ffma2_rn(sub2(fj0[p], FJ[p * S::NFJ + (j + 1) * P + i]), dinv1, R);
+            R = __ffma2_rn(sub2(fk0[p], fk1[p]), dinv2, R);
+            float2 ov;
             if (ulo != nullptr) {
-                int8_t q1;
-                o[v] = ff_add(u0[v], qlo[v], __fmul_rn(hdt_f, R), q1);
-                ulo[((size_t)b * NV + v) * S::NINT + ((size_t)(kp - 2) * NJ + j) * NI + i] = q1;
+                int8_t q0, q1;
+                ov = ff_add2(u0[p], qlo[2 * p], qlo[2 * p + 1], __fmul2_rn(hdt2, R), q0, q1);
+                int8_t* qo = ulo + ((size_t)b * NV + 2 * p) * S::NINT + ((size_t)(kp - 2) * NJ + j) * NI + i;
+                qo[0] = q0;
+                qo[S::NINT] = q1;
             } else {
-                o[v] = fmaf(hdt_f, R, u0[v]);
+                ov = __ffma2_rn(hdt2, R, u0[p]);
             }
-            oblk[(size_t)v * NCELL + base] = o[v];
+            o[2 * p] = ov.x;
+            o[2 * p + 1] = ov.y;
+            oblk[(size_t)(2 * p) * NCELL + base] = ov.x;
+            oblk[(size_t)(2 * p + 1) * NCELL + base] = ov.y;
         }
         if (push.tgt != nullptr) push_faces_part<float, S, NV>(out, pb, ii, jj, kp, o, 0);
         if (cfl_next) {   // uniform over the CTA
@@ -1299,11 +1358,11 @@ k_diffusion_march(const float* u, float* out, int8_t* ulo, PushTable push, Geome
         }
         // the window moves up one plane
 #pragma unroll
-        for (int v = 0; v < NV; ++v) {
-            u0[v] = u1[v];
-            u1[v] = u2[v];
-            dk0[v] = dk1[v];
-            fk0[v] = fk1[v];
+        for (int p = 0; p < NP; ++p) {
+            u0[p] = u1[p];
+            u1[p] = u2[p];
+            dk0[p] = dk1[p];
+            fk0[p] = fk1[p];
         }
     }
     if (__syncthreads_or(late)) {
