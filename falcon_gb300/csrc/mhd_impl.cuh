@@ -444,7 +444,11 @@ k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, DivBArgs 
         // the output rows are written in part (interior cells only): their lines into L2 first
         if (out != un || stage == 1) prefetch_l2(blk_out + ((size_t)v * S::NKP + kp_first) * PL, KPAR * S::PLB);
         if (stage == 1) return;
-        prefetch_l2(blk_un + ((size_t)v * S::NKP + kp_first) * PL, KPAR * S::PLB);
+        // u^n is read at interior cells only: its interior rows (2 .. NJ+1 of
+        // each plane, one contiguous run) are enough
+#pragma unroll
+        for (int q = 0; q < KPAR; ++q)
+            prefetch_l2(blk_un + ((size_t)v * S::NKP + kp_first + q) * PL + 2 * NIP, (uint32_t)(NJ * NIP * sizeof(T)));
         if (blk_lo != nullptr && stage == 4)
             prefetch_l2(blk_lo + ((size_t)v * NK + (kp_first - 2)) * S::PLI, KPAR * S::PLI);
     };
