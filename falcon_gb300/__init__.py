@@ -60,7 +60,7 @@ EXPORTS = (
     "falcon_solver_block_flags", "falcon_solver_magnetogram_sources", "falcon_solver_vcycle_op",
     "falcon_solver_tuning", "falcon_solver_set_tile", "falcon_shard_ranges", "falcon_shard_plan",
     "falcon_set_shard", "falcon_shard_counts", "falcon_shard_pack", "falcon_shard_unpack",
-    "falcon_shard_min_ratio", "falcon_shard_set_min_ratio", "falcon_lcc_set_tensor_path",
+    "falcon_shard_min_ratio", "falcon_shard_set_min_ratio", "falcon_lcc_set_tensor_path", "falcon_set_tuning",
 )
 
 # size of the static device array behind falcon_download_state_range
@@ -335,6 +335,10 @@ class Falcon:
         ms = C.c_double()
         self._ck(self.L.falcon_timer_stop(self.h, C.byref(ms)))
         return ms.value
+
+    def set_tuning(self, kpar_stage, kpar_diffusion):
+        """Fix the k-chunk depths of the stage and diffusion kernels (no autotuning)."""
+        self._ck(self.L.falcon_set_tuning(self.h, C.c_int32(kpar_stage), C.c_int32(kpar_diffusion)))
 
     def tuning(self):
         a, b = C.c_int32(), C.c_int32()

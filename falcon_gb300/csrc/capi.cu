@@ -1837,6 +1837,31 @@ int falcon_tuning(falcon_ctx* ctx, int32_t* kpar_stage, int32_t* kpar_diffusion)
     return FALCON_OK;
 }
 
+int falcon_set_tuning(falcon_ctx* ctx, int32_t kpar_stage, int32_t kpar_diffusion) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    int cand[8];
+    const int n = ctx->mixed() ? kpar_candidates_mixed(ctx->dims, cand) : kpar_candidates_fp64(ctx->dims, cand);
+    bool ok_s = false, ok_d = false;
+    for (int q = 0; q < n; ++q) {
+        ok_s |= cand[q] == kpar_stage;
+        ok_d |= cand[q] == kpar_diffusion;
+    }
+    if (!ok_s || !ok_d)
+        return ctx->fail(FALCON_ERR_INVALID_ARG, "falcon_set_tuning: no compiled variant with k-chunk depths " +
+                                                     std::to_string(kpar_stage) + ", " + std::to_string(kpar_diffusion));
+    CK(cudaStreamSynchronize(ctx->st), "set tuning");
+    for (auto& row : ctx->graphs)   // captured with the previous depths
+        for (cudaGraphExec_t& gx : row)
+            if (gx) {
+                cudaGraphExecDestroy(gx);
+                gx = nullptr;
+            }
+    ctx->kpar_stage = kpar_stage;
+    ctx->kpar_diff = kpar_diffusion;
+    return FALCON_OK;
+}
+
 int falcon_exchange_stats(const falcon_ctx* ctx, int64_t* out) {
     if (!ctx || !out) return FALCON_ERR_INVALID_ARG;
     for (int q = 0; q < 3; ++q) out[q] = ctx->stage_counts[q];

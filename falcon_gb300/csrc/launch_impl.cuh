@@ -83,18 +83,20 @@ cudaError_t stage_any(const StepDims& d, const Geometry& g, const T* in, const T
     return cudaErrorInvalidValue;
 }
 
-// FP32 16^3 blocks: the k-march kernel (any k-chunk depth asked for)
-inline cudaError_t diff_march16(const StepDims& d, const Geometry& g, const float* u, float* out, int8_t* lo,
-                                const PushTable& push, StepScalars* sc, int cfl_next, cudaStream_t st) {
-    using S = MShape<16, 16, 16>;
+// FP32 16^3 blocks: the k-march kernel; the k-chunk depth asked for selects
+// one thread per column (1) or two (2 and 4)
+template <int TPC>
+cudaError_t diff_march16(const StepDims& d, const Geometry& g, const float* u, float* out, int8_t* lo,
+                         const PushTable& push, StepScalars* sc, int cfl_next, cudaStream_t st) {
+    using S = MShape<16, 16, 16, TPC>;
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_diffusion_march<16, 16, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)S::smem);
+        cudaError_t e = cudaFuncSetAttribute(k_diffusion_march<16, 16, 16, TPC>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::smem);
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    k_diffusion_march<16, 16, 16><<<d.nblocks, S::NT, S::smem, st>>>(u, out, lo, push, g, sc, cfl_next);
+    k_diffusion_march<16, 16, 16, TPC><<<d.nblocks, S::NT, S::smem, st>>>(u, out, lo, push, g, sc, cfl_next);
     return cudaGetLastError();
 }
 
@@ -103,7 +105,9 @@ cudaError_t diff_any(const StepDims& d, const Geometry& g, const T* u, T* out, i
                      StepScalars* sc, int kpar, cudaStream_t st, int cfl_next = 0) {
     if (push.tgt != nullptr && out == u) return cudaErrorInvalidValue;   // pushing needs out != u
     if constexpr (!Pol<T>::exact) {
-        if (d.ni == 16 && d.nj == 16 && d.nk == 16) return diff_march16(d, g, u, out, lo, push, sc, cfl_next, st);
+        if (d.ni == 16 && d.nj == 16 && d.nk == 16)
+            return kpar == 1 ? diff_march16<1>(d, g, u, out, lo, push, sc, cfl_next, st)
+                             : diff_march16<2>(d, g, u, out, lo, push, sc, cfl_next, st);
     }
 #define FALCON_DIFF_CASE(N, K) \
     if (d.ni == N && kpar == K) return diff_n<T, N, K>(d, g, u, out, lo, push, sc, cfl_next, st);

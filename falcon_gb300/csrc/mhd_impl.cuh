@@ -1111,13 +1111,14 @@ __device__ __forceinline__ float2 ff_add2(float2 hi, int8_t q0, int8_t q1, float
 // kp+3 and kp+4 are in flight meanwhile). A warp takes rows j and j+4
 // (half-warps of 16 cells), so a half-warp holds one row, as the pushed
 // radial faces need.
-template <int NI, int NJ, int NK>
+template <int NI, int NJ, int NK, int TPC>
 struct MShape {
     static constexpr int NG = 2, NIP = NI + 4, NJP = NJ + 4, NKP = NK + 4;
-    static constexpr int PL = NIP * NJP, NCELL = PL * NKP, NT = NI * NJ;
+    static constexpr int PL = NIP * NJP, NCELL = PL * NKP;
+    static constexpr int NCOL = NI * NJ, NT = NCOL * TPC;   // columns; threads (TPC per column)
     static constexpr int W = 5;                          // plane ring slots
     static constexpr int PLI = NI * NJ, NINT = PLI * NK;
-    static constexpr int NP = NV / 2;                    // variable pairs
+    static constexpr int NP = NV / 2, PPT = NP / TPC;    // variable pairs; pairs per thread
     static constexpr uint32_t PLB = PL * 4u;
     static constexpr int P = 20;                         // row pitch (pairs) of the slope and face arrays
     // per pair (float2): SI[NJ][P] slopes along i of cells i = -1..NI at i + 1;
@@ -1136,15 +1137,20 @@ struct MShape {
     static constexpr size_t smem = off_gs + GS_COUNT * 4;
     static_assert(W * 8 <= (int)off_tile, "mbarriers");
     static_assert(off_si % 8 == 0, "float2 arrays");
+    static_assert(TPC == 1 || TPC == 2, "one or two threads per column");
 };
 
-template <int NI, int NJ, int NK>
-__global__ void __launch_bounds__(NI * NJ, 2)
+// TPC threads per column: with two, thread half h = tid / 256 takes the
+// variable pairs 2h, 2h+1 (warps never mix halves), doubling the warps per SM
+// at half the registers; the CFL ratio, which needs v (first half) and B
+// (second half), takes |B|^2 through shared memory one plane later.
+template <int NI, int NJ, int NK, int TPC>
+__global__ void __launch_bounds__(NI * NJ * TPC, 2)
 k_diffusion_march(const float* u, float* out, int8_t* ulo, PushTable push, Geometry g, StepScalars* sc, int cfl_next) {
-    using S = MShape<NI, NJ, NK>;
+    using S = MShape<NI, NJ, NK, TPC>;
     static_assert(NI == 16 && NJ == 16, "rows of 16 cells: one half-warp per row");
-    static_assert(2 * (S::smem + 1024) <= 233472, "two CTAs per SM");
-    constexpr int NIP = S::NIP, PL = S::PL, W = S::W, NCELL = S::NCELL, P = S::P, NP = S::NP;
+    static_assert(2 * (S::smem + 2048 + 1024) <= 233472, "two CTAs per SM");
+    constexpr int NIP = S::NIP, PL = S::PL, W = S::W, NCELL = S::NCELL, P = S::P, PPT = S::PPT;
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
     float* tile = reinterpret_cast<float*>(smem + S::off_tile);
@@ -1155,6 +1161,7 @@ k_diffusion_march(const float* u, float* out, int8_t* ulo, PushTable push, Geome
     float* gi = reinterpret_cast<float*>(smem + S::off_gi);
     float* gj = reinterpret_cast<float*>(smem + S::off_gj);
     float* gs = reinterpret_cast<float*>(smem + S::off_gs);
+    __shared__ float sb2[TPC == 2 ? 2 * S::NCOL : 1];   // |B|^2 of the second half, by plane parity
     const int b = blockIdx.x, tid = threadIdx.x;
     const float* blk = u + (size_t)b * NV * NCELL;
     float* oblk = out + (size_t)b * NV * NCELL;
@@ -1176,9 +1183,11 @@ k_diffusion_march(const float* u, float* out, int8_t* ulo, PushTable push, Geome
     if (blk_lo != nullptr && tid < NV) prefetch_l2(blk_lo + (size_t)tid * S::NINT, 2 * S::PLI);
     load_geometry<float, S>(g, b, gi, gj, gs, nullptr);
     __syncthreads();   // the geometry tables are read by every thread below
-    // this thread's column: warp w takes rows (w % 4) + 8 (w / 4) and that + 4
-    const int wq = tid >> 5, i = tid & 15;
-    const int j = (wq & 3) + 8 * (wq >> 2) + 4 * ((tid >> 4) & 1);
+    // this thread's column: warp w takes rows (w % 4) + 8 (w / 4) and that + 4;
+    // its pairs p0 .. p0 + PPT - 1
+    const int c = tid % S::NCOL, half = tid / S::NCOL, p0 = half * PPT, v0 = 2 * p0;
+    const int wq = c >> 5, i = c & 15;
+    const int j = (wq & 3) + 8 * (wq >> 2) + 4 * ((c >> 4) & 1);
     const int ii = i + 2, jj = j + 2;
     const float* GCS = gi + GI_CS * NIP;
     const float cs = GCS[ii];
@@ -1206,68 +1215,76 @@ k_diffusion_march(const float* u, float* out, int8_t* ulo, PushTable push, Geome
             oblk[((size_t)v * S::NKP + z) * PL + y * NIP + xi] = tile[(v * W + z % W) * PL + y * NIP + xi];
         }
     };
-    // the pair (v, v+1) of a tile value at offset o from variable 0's
+    // the pair (v, v+1) of a tile value, p = v / 2, at offset o from variable 0's
     auto tv = [&](const float* base, int p) { return f2(base[2 * p * W * PL], base[(2 * p + 1) * W * PL]); };
     // the column window from planes 0..3: u at kp = 2 and 3, the k slope at 2,
     // the flux through the face between planes 1 and 2
     for (int p = 0; p < 4; ++p) late |= mbar_wait(&bars[p], 0u, polls) ? 0 : 1;
     if (copy_bc) copy_cols(0, 4);
     const float* col = tile + jj * NIP + ii;
-    float2 u0[NP], u1[NP], dk0[NP], fk0[NP];
+    const float* colvp = col + V_VP * W * PL;
+    float2 u0[PPT], u1[PPT], dk0[PPT], fk0[PPT];
     {
-        const float2 cc = f2(-0.25f * ((fabsf(col[(V_VP * W + 2) * PL]) + cs) + (fabsf(col[(V_VP * W + 1) * PL]) + cs)));
+        const float2 cc = f2(-0.25f * ((fabsf(colvp[2 * PL]) + cs) + (fabsf(colvp[PL]) + cs)));
 #pragma unroll
-        for (int p = 0; p < NP; ++p) {
+        for (int q = 0; q < PPT; ++q) {
+            const int p = p0 + q;
             const float2 a0 = tv(col, p), a1 = tv(col + PL, p), a2 = tv(col + 2 * PL, p), a3 = tv(col + 3 * PL, p);
             const float2 d1 = minmod_sel2(a0, a1, a2), d2 = minmod_sel2(a1, a2, a3);
-            u0[p] = a2;
-            u1[p] = a3;
-            dk0[p] = d2;
-            fk0[p] = face_flux2(a1, a2, d1, d2, cc);
+            u0[q] = a2;
+            u1[q] = a3;
+            dk0[q] = d2;
+            fk0[q] = face_flux2(a1, a2, d1, d2, cc);
         }
     }
     float cmin = INFINITY;   // next step's CFL ratio minimum over this column
     int cnan = 0;
+    float v2_prev = 0.f;     // two threads per column: the first half's |v|^2 of the previous plane
+    const float rho0c = gi[GI_RHO0 * NIP + ii], sin_c = gj[GJ_SIN * S::NJP + jj];
+    auto cfl_point = [&](float v2, float b2) {
+        float ratio = cfl_ratio_f(v2, b2, cs, rho0c, rc, sin_c, gs[GS_DXI], gs[GS_DXJ], gs[GS_DXK]);
+        if (ratio != ratio) { cnan = 1; ratio = INFINITY; }
+        cmin = fminf(cmin, ratio);
+    };
     for (int kp = 2; kp < NK + 2; ++kp) {
         const int p2 = kp + 2;
         if (blk_lo != nullptr && tid < NV && kp < NK) prefetch_l2(blk_lo + (size_t)tid * S::NINT + (size_t)kp * S::PLI, S::PLI);
         // this cell's int8 corrections, loaded before the wait
-        int8_t qlo[NV];
+        int8_t qlo[2 * PPT];
         if (ulo != nullptr) {
-            const int8_t* q = blk_lo + ((size_t)(kp - 2) * NJ + j) * NI + i;
+            const int8_t* q = blk_lo + (size_t)v0 * S::NINT + ((size_t)(kp - 2) * NJ + j) * NI + i;
 #pragma unroll
-            for (int v = 0; v < NV; ++v) qlo[v] = q[(size_t)v * S::NINT];
+            for (int v = 0; v < 2 * PPT; ++v) qlo[v] = q[(size_t)v * S::NINT];
         }
         // a wait that runs out finishes the plane on whatever the slot holds;
         // the step is flagged and discarded
         late |= mbar_wait(&bars[p2 % W], (uint32_t)((p2 / W) & 1), polls) ? 0 : 1;
         if (copy_bc) copy_cols(p2, p2 + 1);
-        const int s0 = (kp % W) * PL, s2 = (p2 % W) * PL;
+        const int s0 = (kp % W) * PL, s1 = ((kp + 1) % W) * PL, s2 = (p2 % W) * PL;
         const float* tc = tile + s0 + jj * NIP + ii;   // this cell in plane kp (+ v W PL)
         // ---- phase A: k slope and k face from the window; i and j slopes
-        float2 u2[NP], dk1[NP], fk1[NP];
+        float2 u2[PPT], dk1[PPT], fk1[PPT];
         {
-            const float2 cc = f2(-0.25f * ((fabsf(u1[V_VP / 2].y) + cs) + (fabsf(u0[V_VP / 2].y) + cs)));
-            static_assert(V_VP % 2 == 1, "v_phi is the second of its pair");
+            const float2 cc = f2(-0.25f * ((fabsf(colvp[s1]) + cs) + (fabsf(colvp[s0]) + cs)));
 #pragma unroll
-            for (int p = 0; p < NP; ++p) {
-                u2[p] = tv(col + s2, p);
-                dk1[p] = minmod_sel2(u0[p], u1[p], u2[p]);
-                fk1[p] = face_flux2(u0[p], u1[p], dk0[p], dk1[p], cc);
-                SI[p * S::NSI + j * P + i + 1] = minmod_sel2(tv(tc - 1, p), u0[p], tv(tc + 1, p));
-                SJ[p * S::NSJ + (j + 1) * P + i] = minmod_sel2(tv(tc - NIP, p), u0[p], tv(tc + NIP, p));
+            for (int q = 0; q < PPT; ++q) {
+                const int p = p0 + q;
+                u2[q] = tv(col + s2, p);
+                dk1[q] = minmod_sel2(u0[q], u1[q], u2[q]);
+                fk1[q] = face_flux2(u0[q], u1[q], dk0[q], dk1[q], cc);
+                SI[p * S::NSI + j * P + i + 1] = minmod_sel2(tv(tc - 1, p), u0[q], tv(tc + 1, p));
+                SJ[p * S::NSJ + (j + 1) * P + i] = minmod_sel2(tv(tc - NIP, p), u0[q], tv(tc + NIP, p));
             }
         }
         // slopes of the ghost cells next to the block: i = -1, NI of every row
         // (items 0..255) and j = -1, NJ of every column (items 256..511)
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int x = tid + h * S::NT;
+        for (int x = tid; x < 512; x += S::NT) {
             const int side = x & 1, r = (x >> 1) & 15, v = (x >> 5) & 7;
             const float* a = tile + v * W * PL + s0;
             float* dst;
             float val;
-            if (h == 0) {
+            if (x < 256) {
                 const float* q = a + (r + 2) * NIP + (side ? NI + 2 : 1);
                 val = face_slope(q[-1], q[0], q[1]);
                 dst = reinterpret_cast<float*>(SI + (v >> 1) * S::NSI + r * P + (side ? NI + 1 : 0));
@@ -1284,39 +1301,39 @@ k_diffusion_march(const float* u, float* out, int8_t* ulo, PushTable push, Geome
         }
         // ---- phase B: the faces i - 1/2 and j - 1/2 of this cell, and the
         // last faces of the rows (items 0..127) and columns (128..255)
-        float2 fi0[NP], fj0[NP];
+        float2 fi0[PPT], fj0[PPT];
         {
             const float cLi = fabsf(tc[V_VR * W * PL - 1]) + GCS[ii - 1], cRi = fabsf(tc[V_VR * W * PL]) + cs;
             const float cLj = fabsf(tc[V_VT * W * PL - NIP]) + cs, cRj = fabsf(tc[V_VT * W * PL]) + cs;
             const float2 cci = f2(-0.25f * (cRi + cLi)), ccj = f2(-0.25f * (cRj + cLj));
 #pragma unroll
-            for (int p = 0; p < NP; ++p) {
+            for (int q = 0; q < PPT; ++q) {
+                const int p = p0 + q;
                 const float2* si = SI + p * S::NSI + j * P + i;
                 const float2* sj = SJ + p * S::NSJ + j * P + i;
-                fi0[p] = face_flux2(tv(tc - 1, p), u0[p], si[0], si[1], cci);
-                fj0[p] = face_flux2(tv(tc - NIP, p), u0[p], sj[0], sj[P], ccj);
-                FI[p * S::NFI + j * P + i] = fi0[p];
-                FJ[p * S::NFJ + j * P + i] = fj0[p];
+                fi0[q] = face_flux2(tv(tc - 1, p), u0[q], si[0], si[1], cci);
+                fj0[q] = face_flux2(tv(tc - NIP, p), u0[q], sj[0], sj[P], ccj);
+                FI[p * S::NFI + j * P + i] = fi0[q];
+                FJ[p * S::NFJ + j * P + i] = fj0[q];
             }
         }
-        {
+        if (tid < 256) {
             const int x = tid, r = x & 15, v = (x >> 4) & 7;
             const float* sl = reinterpret_cast<const float*>(x < 128 ? SI + (v >> 1) * S::NSI + r * P + NI
                                                                      : SJ + (v >> 1) * S::NSJ + NJ * P + r);
-            float fv;
             if (x < 128) {
                 const float* a = tile + v * W * PL + s0 + (r + 2) * NIP + NI + 1;   // last interior cell of row r
                 const float* vr = tile + V_VR * W * PL + s0 + (r + 2) * NIP + NI + 1;
                 const float cL = fabsf(vr[0]) + GCS[NI + 1], cR = fabsf(vr[1]) + GCS[NI + 2];
-                fv = face_flux_s(a[0], a[1], sl[v & 1], sl[2 + (v & 1)], cL, cR);
-                reinterpret_cast<float*>(FI + (v >> 1) * S::NFI + r * P + NI)[v & 1] = fv;
+                reinterpret_cast<float*>(FI + (v >> 1) * S::NFI + r * P + NI)[v & 1] =
+                    face_flux_s(a[0], a[1], sl[v & 1], sl[2 + (v & 1)], cL, cR);
             } else {
                 const float* a = tile + v * W * PL + s0 + (NJ + 1) * NIP + r + 2;   // last interior row, column r
                 const float* vt = tile + V_VT * W * PL + s0 + (NJ + 1) * NIP + r + 2;
                 const float c2 = GCS[r + 2];
                 const float cL = fabsf(vt[0]) + c2, cR = fabsf(vt[NIP]) + c2;
-                fv = face_flux_s(a[0], a[NIP], sl[v & 1], sl[2 * P + (v & 1)], cL, cR);
-                reinterpret_cast<float*>(FJ + (v >> 1) * S::NFJ + NJ * P + r)[v & 1] = fv;
+                reinterpret_cast<float*>(FJ + (v >> 1) * S::NFJ + NJ * P + r)[v & 1] =
+                    face_flux_s(a[0], a[NIP], sl[v & 1], sl[2 * P + (v & 1)], cL, cR);
             }
         }
         __syncthreads();
@@ -1328,50 +1345,56 @@ k_diffusion_march(const float* u, float* out, int8_t* ulo, PushTable push, Geome
         }
         // ---- phase C: sum the six faces in the reference's order, update
         const size_t base = (size_t)kp * PL + jj * NIP + ii;
-        float o[NV];
+        float o[2 * PPT];
 #pragma unroll
-        for (int p = 0; p < NP; ++p) {
-            float2 R = __fmul2_rn(sub2(fi0[p], FI[p * S::NFI + j * P + i + 1]), dinv0);
-            R = __ffma2_rn(sub2(fj0[p], FJ[p * S::NFJ + (j + 1) * P + i]), dinv1, R);
-            R = __ffma2_rn(sub2(fk0[p], fk1[p]), dinv2, R);
+        for (int q = 0; q < PPT; ++q) {
+            const int p = p0 + q;
+            float2 R = __fmul2_rn(sub2(fi0[q], FI[p * S::NFI + j * P + i + 1]), dinv0);
+            R = __ffma2_rn(sub2(fj0[q], FJ[p * S::NFJ + (j + 1) * P + i]), dinv1, R);
+            R = __ffma2_rn(sub2(fk0[q], fk1[q]), dinv2, R);
             float2 ov;
             if (ulo != nullptr) {
                 int8_t q0, q1;
-                ov = ff_add2(u0[p], qlo[2 * p], qlo[2 * p + 1], __fmul2_rn(hdt2, R), q0, q1);
+                ov = ff_add2(u0[q], qlo[2 * q], qlo[2 * q + 1], __fmul2_rn(hdt2, R), q0, q1);
                 int8_t* qo = ulo + ((size_t)b * NV + 2 * p) * S::NINT + ((size_t)(kp - 2) * NJ + j) * NI + i;
                 qo[0] = q0;
                 qo[S::NINT] = q1;
             } else {
-                ov = __ffma2_rn(hdt2, R, u0[p]);
+                ov = __ffma2_rn(hdt2, R, u0[q]);
             }
-            o[2 * p] = ov.x;
-            o[2 * p + 1] = ov.y;
+            o[2 * q] = ov.x;
+            o[2 * q + 1] = ov.y;
             oblk[(size_t)(2 * p) * NCELL + base] = ov.x;
             oblk[(size_t)(2 * p + 1) * NCELL + base] = ov.y;
         }
-        if (push.tgt != nullptr) push_faces_part<float, S, NV>(out, pb, ii, jj, kp, o, 0);
+        if (push.tgt != nullptr) push_faces_part<float, S, 2 * PPT>(out, pb, ii, jj, kp, o, v0);
         if (cfl_next) {   // uniform over the CTA
 #pragma unroll
-            for (int v = 0; v < NV; ++v) cnan |= (o[v] != o[v]);
-            const float v2 = cfl_sq3(o[V_VR], o[V_VT], o[V_VP]);
-            const float b2 = cfl_sq3(o[V_BR], o[V_BT], o[V_BP]);
-            float ratio = cfl_ratio_f(v2, b2, cs, gi[GI_RHO0 * NIP + ii], rc, gj[GJ_SIN * S::NJP + jj], gs[GS_DXI],
-                                      gs[GS_DXJ], gs[GS_DXK]);
-            if (ratio != ratio) { cnan = 1; ratio = INFINITY; }
-            cmin = fminf(cmin, ratio);
+            for (int v = 0; v < 2 * PPT; ++v) cnan |= (o[v] != o[v]);
+            if constexpr (TPC == 1) {
+                cfl_point(cfl_sq3(o[V_VR], o[V_VT], o[V_VP]), cfl_sq3(o[V_BR], o[V_BT], o[V_BP]));
+            } else if (half == 0) {
+                if (kp > 2) cfl_point(v2_prev, sb2[((kp - 1) & 1) * S::NCOL + c]);
+                v2_prev = cfl_sq3(o[V_VR], o[V_VT], o[V_VP]);
+            } else {
+                sb2[(kp & 1) * S::NCOL + c] = cfl_sq3(o[V_BR - 4], o[V_BT - 4], o[V_BP - 4]);
+            }
         }
         // the window moves up one plane
 #pragma unroll
-        for (int p = 0; p < NP; ++p) {
-            u0[p] = u1[p];
-            u1[p] = u2[p];
-            dk0[p] = dk1[p];
-            fk0[p] = fk1[p];
+        for (int q = 0; q < PPT; ++q) {
+            u0[q] = u1[q];
+            u1[q] = u2[q];
+            dk0[q] = dk1[q];
+            fk0[q] = fk1[q];
         }
     }
     if (__syncthreads_or(late)) {
         abort_cta();
         return;
+    }
+    if constexpr (TPC == 2) {
+        if (cfl_next && half == 0) cfl_point(v2_prev, sb2[((NK + 1) & 1) * S::NCOL + c]);
     }
     if (cfl_next) cfl_commit(cmin, cnan, sc);
 }

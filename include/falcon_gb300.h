@@ -348,6 +348,12 @@ int  falcon_timer_stop(falcon_ctx* ctx, double* ms);
  * kernels. The autotuner runs once per context, before the first step: it
  * times every compiled variant on this grid, on the stage buffer only. */
 int  falcon_tuning(falcon_ctx* ctx, int32_t* kpar_stage, int32_t* kpar_diffusion);
+/* fix the k-chunk depths instead (no autotuning): one of the compiled
+ * variants, FP32 16^3 blocks 1, 2 or 4 (for the diffusion pass: 1 = one
+ * thread per cell column, 2 or 4 = two), FP32 8^3 blocks 2, 4 or 8, FP64 1
+ * (16^3) or 2, 4 (8^3); anything else is FALCON_ERR_INVALID_ARG. Every
+ * variant computes the same values bit for bit. */
+int  falcon_set_tuning(falcon_ctx* ctx, int32_t kpar_stage, int32_t kpar_diffusion);
 /* device ghost-fill lists: counts[0] exact copies, [1] 1-D blends, [2] trilinear/rotated */
 int  falcon_ghost_list_sizes(const falcon_ctx* ctx, int64_t* counts);
 /* the exchanges between RK stages (face ghosts only; every stencil of a step

@@ -182,6 +182,38 @@ def test_mixed_step_matches_phase_sequence_16(radial_option):
     assert np.array_equal(ua, ub)
 
 
+@pytest.mark.parametrize("blocks", ["8cube", "16cube"])
+def test_every_kchunk_variant_computes_the_same_step(blocks):
+    """Each compiled variant of the mixed stage and diffusion kernels (k-chunk
+    depths; for 16^3 diffusion one or two threads per cell column), fixed
+    with falcon_set_tuning instead of the autotuner, gives the same three
+    steps bit for bit, pushes, fused CFL minimum and dt included."""
+    blk = (8, 8, 8) if blocks == "8cube" else (16, 16, 16)
+    mk = lambda: config.make_config(block=blk, root_tiles=(1, 3, 9), radial_levels=1, amr=(),
+                                    precision=config.PREC_MIXED)
+    kp = (2, 4, 8) if blocks == "8cube" else (1, 2, 4)
+    ref = None
+    for ks, kd in [(kp[0], kp[0]), (kp[1], kp[1]), (kp[2], kp[0]), (kp[0], kp[2])]:
+        f = fg.Falcon(mk())
+        f.set_tuning(ks, kd)
+        assert f.tuning() == {"kpar_stage": ks, "kpar_diffusion": kd}
+        u0 = synth.initial_state(mk(), f.block_ranges(), f.block_flags(), seed=1031)
+        f.upload_state(u0)
+        f.exchange()
+        dts = [f.advance_rk4() for _ in range(3)]
+        out = (dts, f.download_state())
+        assert np.isfinite(out[1]).all()
+        if ref is None:
+            ref = out
+        else:
+            assert out[0] == ref[0], (ks, kd)
+            assert np.array_equal(out[1], ref[1]), (ks, kd)
+        f.close()
+    g = fg.Falcon(mk())
+    with pytest.raises(fg.FalconError):
+        g.set_tuning(3, kp[0])
+
+
 def test_full_size_mixed_properties():
     """21M cells, 5,184 blocks of 16^3: steps stay finite, the exchange is
     idempotent (bit-exact), dt is positive and stable."""
