@@ -334,8 +334,8 @@ def run_ours(args, rank, world, local, dist):
     f.set_kernel_timing(False)
     # launches per step, counted by the context's per-kernel timing over those
     # 2 steps: finalize_dt (the CFL minimum comes from the previous step's
-    # diffusion pass), 4 stages and the diffusion pass; the ghost entries that
-    # no kernel pushes are pulled by the kernels themselves (no exchange launch)
+    # diffusion pass), 4 stages and the diffusion pass, and after each of
+    # them the exchange of the ghost entries the kernels do not push
     launches_per_step = int(round(sum(v[1] for v in stats.values()) / 2.0))
     tot = sum(v[0] for v in stats.values()) or 1.0
     top = max(stats, key=lambda k: stats[k][0])
@@ -353,6 +353,25 @@ def run_ours(args, rank, world, local, dist):
                 "traffic": profile_traffic("%s_mixed_21m.txt" % top), "kernel": top,
                 "algorithmic_bytes_per_launch": cells * per_cell, "avg_launch_ms": avg_ms,
                 "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind}
+    # ---- the same step as one persistent cooperative launch (the kernel
+    # bodies over all blocks with grid barriers between the phases); timed
+    # like the graph above, on the same context
+    try:
+        f.set_step_mode(fg.STEP_PERSISTENT)
+        f.run_steps(args.warmup)
+        f.synchronize()
+        f.timer_start()
+        f.run_steps(args.steps)
+        pms = reduce_max(dist, f.timer_stop())
+        f.synchronize()
+        f.set_step_mode(fg.STEP_GRAPH)
+        persistent = {"ms_per_step": pms / args.steps, "launches_per_step": 1,
+                      "value": reduce_sum(dist, float(cells * args.steps)) / (pms / 1e3)}
+    except fg.FalconError as ex:
+        f.set_step_mode(fg.STEP_GRAPH)
+        persistent = {"unavailable": str(ex)}
+    step_modes = {"graph": {"ms_per_step": ms_max / args.steps, "launches_per_step": launches_per_step},
+                  "persistent": persistent}
     step_ach = cells * BYTES_PER_CELL_STEP / (ms_max / args.steps / 1e3) / 1e9
     shares = {k: round(v[0] / tot, 4) for k, v in stats.items()}
 
@@ -422,6 +441,7 @@ def run_ours(args, rank, world, local, dist):
             "setup_s": round(setup_s, 3),
             "e2e_resident": {"value": res_val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 8},
             "gpu_launches": launches_per_step * args.steps,
+            "step_modes": step_modes,
             "clocks": clk,
         }
     f.close()

@@ -34,6 +34,8 @@ ERR_UNCOVERED_GHOST = -7
 ERR_NO_DEVICE = -8
 SHARD_SEND = 0
 SHARD_RECV = 1
+STEP_GRAPH = 0        # falcon_set_step_mode: one captured graph per step
+STEP_PERSISTENT = 1   # one persistent cooperative launch per step
 
 # every symbol declared in include/falcon_gb300.h
 EXPORTS = (
@@ -61,6 +63,7 @@ EXPORTS = (
     "falcon_solver_tuning", "falcon_solver_set_tile", "falcon_shard_ranges", "falcon_shard_plan",
     "falcon_set_shard", "falcon_shard_counts", "falcon_shard_pack", "falcon_shard_unpack",
     "falcon_shard_min_ratio", "falcon_shard_set_min_ratio", "falcon_lcc_set_tensor_path", "falcon_set_tuning",
+    "falcon_set_step_mode",
 )
 
 # size of the static device array behind falcon_download_state_range
@@ -335,6 +338,11 @@ class Falcon:
         ms = C.c_double()
         self._ck(self.L.falcon_timer_stop(self.h, C.byref(ms)))
         return ms.value
+
+    def set_step_mode(self, mode):
+        """STEP_GRAPH (one captured graph per step) or STEP_PERSISTENT (one
+        persistent cooperative launch per step; mixed path, 16^3 blocks)."""
+        self._ck(self.L.falcon_set_step_mode(self.h, C.c_int32(mode)))
 
     def set_tuning(self, kpar_stage, kpar_diffusion):
         """Fix the k-chunk depths of the stage and diffusion kernels (no autotuning)."""

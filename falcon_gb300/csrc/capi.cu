@@ -63,6 +63,8 @@ struct falcon_ctx {
     int64_t final_counts[3] = {0, 0, 0};   // the same for the exchange ending a mixed step
     int64_t pushed_faces = 0, pushed_cells = 0;
     int kpar_stage = 0, kpar_diff = 0;      // chosen by the autotuner (0 = not tuned yet)
+    int step_mode = FALCON_STEP_GRAPH;      // FALCON_STEP_PERSISTENT: one cooperative launch per step
+    unsigned int* gbar = nullptr;           // persistent step: grid-barrier counter, generation, block tickets
     // step graphs: the mixed step writes u^{n+1} into the second stage buffer
     // and the two buffers swap roles, so one graph per assignment (index 0
     // while U is the first allocation)
@@ -1256,6 +1258,21 @@ static int run(falcon_ctx* ctx, int32_t n) {
         }
         return FALCON_OK;
     }
+    if (ctx->step_mode == FALCON_STEP_PERSISTENT) {
+        for (int32_t s = 0; s < n; ++s) {
+            // the CFL minimum of u^n: formed by the previous step's diffusion
+            // pass, else by k_cfl here (the persistent step starts at dt)
+            if (!ctx->cfl_ready)
+                CK(launch_cfl_mixed(ctx->dims, ctx->geom(), (const float*)ctx->U, ctx->sc, ctx->st), "cfl");
+            CK(launch_step_persistent_mixed(ctx->dims, ctx->geom(), (float*)ctx->U, (float*)ctx->RK, (float*)ctx->R2,
+                                            ctx->Ulo, ctx->push, ctx->gl_stage, ctx->gl_final, ctx->sc, ctx->gbar,
+                                            ctx->st),
+               "persistent step");
+            end_step(ctx);
+            ++ctx->steps_done;
+        }
+        return FALCON_OK;
+    }
     for (int32_t s = 0; s < n; ++s) {
         cudaGraphExec_t& gx = ctx->graphs[ctx->U == ctx->bufA ? 0 : 1][ctx->cfl_ready ? 1 : 0];
         if (!gx) {
@@ -1859,6 +1876,24 @@ int falcon_set_tuning(falcon_ctx* ctx, int32_t kpar_stage, int32_t kpar_diffusio
             }
     ctx->kpar_stage = kpar_stage;
     ctx->kpar_diff = kpar_diffusion;
+    return FALCON_OK;
+}
+
+int falcon_set_step_mode(falcon_ctx* ctx, int32_t mode) {
+    int rc = need_device(ctx);
+    if (rc) return rc;
+    if (mode != FALCON_STEP_GRAPH && mode != FALCON_STEP_PERSISTENT)
+        return ctx->fail(FALCON_ERR_INVALID_ARG, "falcon_set_step_mode: unknown mode");
+    if (mode == FALCON_STEP_PERSISTENT) {
+        if (!ctx->mixed() || !ctx->R2 || ctx->P || ctx->cfg.phys.divb_option != 0 || ctx->dims.ni != 16 ||
+            ctx->dims.nj != 16 || ctx->dims.nk != 16)
+            return ctx->fail(FALCON_ERR_INVALID_ARG,
+                             "falcon_set_step_mode: the persistent step covers the mixed path with 16^3 blocks and "
+                             "divb_option 0");
+        if (!ctx->gbar) CK(ctx->alloc(&ctx->gbar, 8 * sizeof(unsigned int)), "alloc grid barrier");
+        CK(cudaMemsetAsync(ctx->gbar, 0, 8 * sizeof(unsigned int), ctx->st), "grid barrier");
+    }
+    ctx->step_mode = mode;
     return FALCON_OK;
 }
 

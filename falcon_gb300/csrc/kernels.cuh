@@ -222,6 +222,14 @@ cudaError_t launch_psi_ghost_mixed(const StepDims& d, const GhostLists& gl, floa
 // diffusion of u into out: in place (out == u, push.tgt == nullptr) or out of
 // place with the regular faces pushed into out and the radial boundary ghost
 // columns copied (see k_diffusion)
+// One whole mixed step of 16^3 blocks as one persistent cooperative launch
+// (after the CFL minimum of u^n is formed): dt, four stages with their face
+// exchanges, diffusion into R2, the final exchange. bar: 8 device words
+// (reset here): grid-barrier counter and generation, the 5 block tickets.
+cudaError_t launch_step_persistent_mixed(const StepDims& d, const Geometry& g, float* U, float* RK, float* R2,
+                                         int8_t* lo, const PushTable& push, const GhostLists& gl_stage,
+                                         const GhostLists& gl_final, StepScalars* sc, unsigned int* bar,
+                                         cudaStream_t st);
 cudaError_t launch_diffusion_mixed(const StepDims& d, const Geometry& g, const float* u, float* out, int8_t* lo,
                                    const PushTable& push, StepScalars* sc, int kpar, cudaStream_t st,
                                    int cfl_next = 0);

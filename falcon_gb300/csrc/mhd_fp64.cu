@@ -46,16 +46,7 @@ cudaError_t launch_shard_unpack_fp64(const StepDims& d, const int32_t* dst, int6
 
 // dt = min(1.e20, CFL*min(h/v_wave)) (3_6/ModTimeStep.f90:20-29); also the
 // per-stage FP32 factors of the mixed path and the reset of the accumulator.
-__global__ void k_finalize_dt(StepScalars* sc) {
-    const double m = __longlong_as_double((long long)sc->min_ratio_bits);
-    const double dt = fmin((double)1.e20f, sc->cfl * m);
-    sc->dt = dt;
-    for (int s = 1; s <= 4; ++s) sc->dt_stage_f[s - 1] = (float)(dt / (double)(5.0f - (float)s));
-    sc->dt_half_f = (float)(0.5 * dt);
-    sc->min_ratio_bits = 0x7FF0000000000000ull;   // +inf for the next step
-    if (sc->nan_flag && sc->nan_step < 0) sc->nan_step = sc->step_counter;
-    sc->step_counter += 1;
-}
+__global__ void k_finalize_dt(StepScalars* sc) { impl::finalize_dt_body(sc); }
 cudaError_t launch_finalize_dt(StepScalars* sc, cudaStream_t st) {
     k_finalize_dt<<<1, 1, 0, st>>>(sc);
     return cudaGetLastError();

@@ -110,6 +110,11 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)_
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
+// a barrier object is invalidated before its shared memory is used for
+// anything else (the persistent step runs several kernel bodies in one CTA)
+__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 __device__ __forceinline__ void fence_mbar_init() {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
@@ -155,6 +160,8 @@ __device__ __forceinline__ void copy_wait_abort(StepScalars* sc, uint64_t* bars,
     if (threadIdx.x != 0) return;
     atomicOr(&sc->nan_flag, 2);
     for (int c = c0 < 0 ? 0 : c0; c <= c1; ++c) mbar_wait(&bars[c & 1], (uint32_t)((c >> 1) & 1), kWaitPolls);
+    mbar_inval(&bars[0]);
+    mbar_inval(&bars[1]);
 }
 
 template <class T, int NI, int NJ, int NK, int KPAR>
@@ -405,10 +412,12 @@ __device__ __forceinline__ void cell_of_thread(int tid, int& i, int& j, int& kq)
 // ---------------------------------------------------------------------------
 // One RK stage of one block: boundary -> RHS (3_6/ModEquation.f90:24-162) ->
 // u_out = u^n + dt*R/(5-s) (3_6/ModAdvance.f90:87-93).
+// The body runs block b with the CTA's threads (NI*NJ*KPAR of them): k_stage
+// calls it for blockIdx.x, the persistent step for each block it takes.
 template <class T, int NI, int NJ, int NK, int KPAR, int DIVB>
-__global__ void __launch_bounds__(NI* NJ* KPAR, (Shape<T, NI, NJ, NK, KPAR>::min_blocks))
-k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, DivBArgs psi, Geometry g, StepScalars* sc,
-        int stage, int bc_writeback, int heat_on) {
+__device__ __forceinline__ void stage_body(int b, const T* in, const T* un, T* out, int8_t* ulo, PushTable push,
+                                           DivBArgs psi, Geometry g, StepScalars* sc, int stage, int bc_writeback,
+                                           int heat_on) {
     using S = Shape<T, NI, NJ, NK, KPAR>;
     constexpr int NIP = S::NIP, PL = S::PL, W = S::W, WP = S::WP, NCELL = S::NCELL;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -420,7 +429,6 @@ k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, DivBArgs 
     T* gj = reinterpret_cast<T*>(smem + S::off_gj);
     T* gs = reinterpret_cast<T*>(smem + S::off_gs);
 
-    const int b = blockIdx.x;
     const int fl = g.flags[b];
     const T* blk_in = in + (size_t)b * NV * NCELL;
     T* wb = bc_writeback ? const_cast<T*>(blk_in) : nullptr;
@@ -709,7 +717,20 @@ k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, DivBArgs 
             if (push.tgt != nullptr) push_faces<T, S>(out, pb, ii, jj, kp, o);
         }
     }
-    if (__syncthreads_or(late)) copy_wait_abort(sc, bars, nchunk - 1, nchunk - 1);
+    if (__syncthreads_or(late)) {
+        copy_wait_abort(sc, bars, nchunk - 1, nchunk - 1);
+        return;
+    }
+    if (threadIdx.x == 0) {   // every copy has been waited for
+        mbar_inval(&bars[0]);
+        mbar_inval(&bars[1]);
+    }
+}
+template <class T, int NI, int NJ, int NK, int KPAR, int DIVB>
+__global__ void __launch_bounds__(NI* NJ* KPAR, (Shape<T, NI, NJ, NK, KPAR>::min_blocks))
+k_stage(const T* in, const T* un, T* out, int8_t* ulo, PushTable push, DivBArgs psi, Geometry g, StepScalars* sc,
+        int stage, int bc_writeback, int heat_on) {
+    stage_body<T, NI, NJ, NK, KPAR, DIVB>(blockIdx.x, in, un, out, ulo, push, psi, g, sc, stage, bc_writeback, heat_on);
 }
 
 // ---------------------------------------------------------------------------
@@ -1134,7 +1155,9 @@ struct MShape {
     static constexpr size_t off_gi = off_fj + (size_t)NP * NFJ * 8;
     static constexpr size_t off_gj = off_gi + (size_t)GI_COUNT * NIP * 4;
     static constexpr size_t off_gs = off_gj + (size_t)GJ_COUNT * NJP * 4;
-    static constexpr size_t smem = off_gs + GS_COUNT * 4;
+    // two threads per column: |B|^2 of the second half, [plane parity][column]
+    static constexpr size_t off_sb2 = off_gs + GS_COUNT * 4;
+    static constexpr size_t smem = off_sb2 + (TPC == 2 ? 2 * NCOL * 4 : 0);
     static_assert(W * 8 <= (int)off_tile, "mbarriers");
     static_assert(off_si % 8 == 0, "float2 arrays");
     static_assert(TPC == 1 || TPC == 2, "one or two threads per column");
@@ -1145,11 +1168,11 @@ struct MShape {
 // at half the registers; the CFL ratio, which needs v (first half) and B
 // (second half), takes |B|^2 through shared memory one plane later.
 template <int NI, int NJ, int NK, int TPC>
-__global__ void __launch_bounds__(NI * NJ * TPC, 2)
-k_diffusion_march(const float* u, float* out, int8_t* ulo, PushTable push, Geometry g, StepScalars* sc, int cfl_next) {
+__device__ __forceinline__ void march_body(int b, const float* u, float* out, int8_t* ulo, PushTable push, Geometry g,
+                                           StepScalars* sc, int cfl_next) {
     using S = MShape<NI, NJ, NK, TPC>;
     static_assert(NI == 16 && NJ == 16, "rows of 16 cells: one half-warp per row");
-    static_assert(2 * (S::smem + 2048 + 1024) <= 233472, "two CTAs per SM");
+    static_assert(2 * (S::smem + 1024) <= 233472, "two CTAs per SM");
     constexpr int NIP = S::NIP, PL = S::PL, W = S::W, NCELL = S::NCELL, P = S::P, PPT = S::PPT;
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
@@ -1161,8 +1184,8 @@ k_diffusion_march(const float* u, float* out, int8_t* ulo, PushTable push, Geome
     float* gi = reinterpret_cast<float*>(smem + S::off_gi);
     float* gj = reinterpret_cast<float*>(smem + S::off_gj);
     float* gs = reinterpret_cast<float*>(smem + S::off_gs);
-    __shared__ float sb2[TPC == 2 ? 2 * S::NCOL : 1];   // |B|^2 of the second half, by plane parity
-    const int b = blockIdx.x, tid = threadIdx.x;
+    float* sb2 = reinterpret_cast<float*>(smem + S::off_sb2);   // |B|^2 of the second half, by plane parity
+    const int tid = threadIdx.x;
     const float* blk = u + (size_t)b * NV * NCELL;
     float* oblk = out + (size_t)b * NV * NCELL;
     const int flb = g.flags[b];
@@ -1202,6 +1225,7 @@ k_diffusion_march(const float* u, float* out, int8_t* ulo, PushTable push, Geome
         atomicOr(&sc->nan_flag, 2);
         for (int p = issued - W < 0 ? 0 : issued - W; p < issued; ++p)
             mbar_wait(&bars[p % W], (uint32_t)((p / W) & 1), kWaitPolls);
+        for (int q = 0; q < W; ++q) mbar_inval(&bars[q]);
     };
     // radial boundary ghost columns of planes [plo, phi), u -> out
     auto copy_cols = [&](int plo, int phi) {
@@ -1396,7 +1420,29 @@ k_diffusion_march(const float* u, float* out, int8_t* ulo, PushTable push, Geome
     if constexpr (TPC == 2) {
         if (cfl_next && half == 0) cfl_point(v2_prev, sb2[((NK + 1) & 1) * S::NCOL + c]);
     }
+    if (tid == 0)   // every copy has been waited for
+        for (int q = 0; q < W; ++q) mbar_inval(&bars[q]);
     if (cfl_next) cfl_commit(cmin, cnan, sc);
+}
+template <int NI, int NJ, int NK, int TPC>
+__global__ void __launch_bounds__(NI * NJ * TPC, 2)
+k_diffusion_march(const float* u, float* out, int8_t* ulo, PushTable push, Geometry g, StepScalars* sc, int cfl_next) {
+    march_body<NI, NJ, NK, TPC>(blockIdx.x, u, out, ulo, push, g, sc, cfl_next);
+}
+
+// ---------------------------------------------------------------------------
+// dt = min(1.e20, CFL*min(h/v_wave)) (3_6/ModTimeStep.f90:20-29); also the
+// per-stage FP32 factors of the mixed path and the reset of the accumulator.
+// One thread (k_finalize_dt, or the first phase of the persistent step).
+__device__ __forceinline__ void finalize_dt_body(StepScalars* sc) {
+    const double m = __longlong_as_double((long long)sc->min_ratio_bits);
+    const double dt = fmin((double)1.e20f, sc->cfl * m);
+    sc->dt = dt;
+    for (int s = 1; s <= 4; ++s) sc->dt_stage_f[s - 1] = (float)(dt / (double)(5.0f - (float)s));
+    sc->dt_half_f = (float)(0.5 * dt);
+    sc->min_ratio_bits = 0x7FF0000000000000ull;   // +inf for the next step
+    if (sc->nan_flag && sc->nan_step < 0) sc->nan_step = sc->step_counter;
+    sc->step_counter += 1;
 }
 
 // ---------------------------------------------------------------------------
@@ -1463,19 +1509,27 @@ __global__ void __launch_bounds__(256) k_cfl(const T* u, Geometry g, StepScalars
 // (3_6/ModCommunication.f90:655-795). Exact copies first, then trilinear
 // entries (3_6/ModMath.f90:283-291) with the Yin-Yang vector rotation
 // (3_6/ModYinYang.f90:58-60).
-template <class T>
+// Source values are read with ld (CG false) or, in the persistent step,
+// with ld.global.cg (L2 only): there another SM wrote them in the phase
+// before, after this SM may have cached the same lines in its L1.
+template <bool CG, class T>
+__device__ __forceinline__ T ldsrc(const T* p) {
+    if constexpr (CG) return __ldcg(p);
+    else return *p;
+}
+template <class T, bool CG = false>
 __device__ __forceinline__ void ghost_copy_one(T* u, const GhostCopyList& L, int ncell, int64_t e) {
     const size_t d = (size_t)L.dst[e], s = (size_t)L.src[e];
     T v[NV];
 #pragma unroll
-    for (int q = 0; q < NV; ++q) v[q] = u[s + (size_t)q * ncell];
+    for (int q = 0; q < NV; ++q) v[q] = ldsrc<CG>(u + s + (size_t)q * ncell);
 #pragma unroll
     for (int q = 0; q < NV; ++q) u[d + (size_t)q * ncell] = v[q];
 }
 
 // one-dimensional linear interpolation (radial neighbours of different
 // spacing: the other two weights snapped to exactly 0), mixed path only
-template <class T>
+template <class T, bool CG = false>
 __device__ __forceinline__ void ghost_lin_one(T* u, const GhostLinList& L, int ncell, int64_t e) {
     const size_t d = (size_t)L.dst[e], s = (size_t)L.src[e], st = (size_t)L.stride[e];
     const T w = (T)L.w[e], uw = T(1) - w;
@@ -1483,7 +1537,7 @@ __device__ __forceinline__ void ghost_lin_one(T* u, const GhostLinList& L, int n
 #pragma unroll
     for (int q = 0; q < NV; ++q) {
         const T* f = u + s + (size_t)q * ncell;
-        v[q] = blend(f[0], f[st], uw, w);
+        v[q] = blend(ldsrc<CG>(f), ldsrc<CG>(f + st), uw, w);
     }
 #pragma unroll
     for (int q = 0; q < NV; ++q) u[d + (size_t)q * ncell] = v[q];
@@ -1491,20 +1545,20 @@ __device__ __forceinline__ void ghost_lin_one(T* u, const GhostLinList& L, int n
 
 // The values of one interpolated/rotated ghost entry (into val); the FP64
 // path is the reference's trilinear form and operand order.
-template <class T>
+template <class T, bool CG = false>
 __device__ __forceinline__ void ghost_interp_vals(const T* u, const GhostInterpList& L, int ncell, int nip, int pl,
                                                   int64_t e, T* val);
 
-template <class T>
+template <class T, bool CG = false>
 __device__ __forceinline__ void ghost_interp_one(T* u, const GhostInterpList& L, int ncell, int nip, int pl, int64_t e) {
     T val[NV];
-    ghost_interp_vals(u, L, ncell, nip, pl, e, val);
+    ghost_interp_vals<T, CG>(u, L, ncell, nip, pl, e, val);
     const size_t dd = (size_t)L.dst[e];
 #pragma unroll
     for (int v = 0; v < NV; ++v) u[dd + (size_t)v * ncell] = val[v];
 }
 
-template <class T>
+template <class T, bool CG>
 __device__ __forceinline__ void ghost_interp_vals(const T* u, const GhostInterpList& L, int ncell, int nip, int pl,
                                                   int64_t e, T* val) {
     const int kind = L.kind[e];
@@ -1516,20 +1570,20 @@ __device__ __forceinline__ void ghost_interp_vals(const T* u, const GhostInterpL
         const float ui = 1.f - wi, uj = 1.f - wj, uk = 1.f - wk;
         if (!(kind & 1)) {
 #pragma unroll
-            for (int v = 0; v < NV; ++v) val[v] = u[s + (size_t)v * ncell];
+            for (int v = 0; v < NV; ++v) val[v] = ldsrc<CG>(u + s + (size_t)v * ncell);
         } else if (wi == 0.f) {
 #pragma unroll
             for (int v = 0; v < NV; ++v) {
                 const T* f = u + s + (size_t)v * ncell;
-                val[v] = f[0] * uj * uk + f[nip] * wj * uk + f[pl] * uj * wk + f[nip + pl] * wj * wk;
+                val[v] = ldsrc<CG>(f + (0)) * uj * uk + ldsrc<CG>(f + (nip)) * wj * uk + ldsrc<CG>(f + (pl)) * uj * wk + ldsrc<CG>(f + (nip + pl)) * wj * wk;
             }
         } else {
 #pragma unroll
             for (int v = 0; v < NV; ++v) {
                 const T* f = u + s + (size_t)v * ncell;
-                val[v] = f[0] * ui * uj * uk + f[1] * wi * uj * uk + f[nip] * ui * wj * uk + f[pl] * ui * uj * wk +
-                         f[1 + nip] * wi * wj * uk + f[nip + pl] * ui * wj * wk + f[1 + pl] * wi * uj * wk +
-                         f[1 + nip + pl] * wi * wj * wk;
+                val[v] = ldsrc<CG>(f + (0)) * ui * uj * uk + ldsrc<CG>(f + (1)) * wi * uj * uk + ldsrc<CG>(f + (nip)) * ui * wj * uk + ldsrc<CG>(f + (pl)) * ui * uj * wk +
+                         ldsrc<CG>(f + (1 + nip)) * wi * wj * uk + ldsrc<CG>(f + (nip + pl)) * ui * wj * wk + ldsrc<CG>(f + (1 + pl)) * wi * uj * wk +
+                         ldsrc<CG>(f + (1 + nip + pl)) * wi * wj * wk;
             }
         }
         if (kind & 2) {
@@ -1549,13 +1603,13 @@ __device__ __forceinline__ void ghost_interp_vals(const T* u, const GhostInterpL
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
             const T* f = u + s + (size_t)v * ncell;
-            val[v] = f[0] * ui * uj * uk + f[1] * wi * uj * uk + f[nip] * ui * wj * uk + f[pl] * ui * uj * wk +
-                     f[1 + nip] * wi * wj * uk + f[nip + pl] * ui * wj * wk + f[1 + pl] * wi * uj * wk +
-                     f[1 + nip + pl] * wi * wj * wk;
+            val[v] = ldsrc<CG>(f + (0)) * ui * uj * uk + ldsrc<CG>(f + (1)) * wi * uj * uk + ldsrc<CG>(f + (nip)) * ui * wj * uk + ldsrc<CG>(f + (pl)) * ui * uj * wk +
+                     ldsrc<CG>(f + (1 + nip)) * wi * wj * uk + ldsrc<CG>(f + (nip + pl)) * ui * wj * wk + ldsrc<CG>(f + (1 + pl)) * wi * uj * wk +
+                     ldsrc<CG>(f + (1 + nip + pl)) * wi * wj * wk;
         }
     } else {
 #pragma unroll
-        for (int v = 0; v < NV; ++v) val[v] = u[s + (size_t)v * ncell];
+        for (int v = 0; v < NV; ++v) val[v] = ldsrc<CG>(u + s + (size_t)v * ncell);
     }
     if (kind & 2) {
         const T a = (T)L.rot[2 * e], c = (T)L.rot[2 * e + 1];
@@ -1566,6 +1620,116 @@ __device__ __forceinline__ void ghost_interp_vals(const T* u, const GhostInterpL
         val[V_VT] = -(a * x2) - c * x3;
         val[V_VP] = -(a * x3) + c * x2;
     }
+}
+
+// ---------------------------------------------------------------------------
+// A barrier over every CTA of a cooperative launch (all co-resident). Thread
+// 0 of each CTA reads the generation, arrives on the counter; the last one
+// resets the counter and advances the generation, the others poll it, at most
+// `polls` times (a poll that runs out flags the step: bit 1 of nan_flag, the
+// host returns FALCON_ERR_TIMEOUT, and the CTA goes on). Fences on both sides
+// make every CTA's writes before the barrier visible to every CTA after it.
+struct GridBarrier {
+    unsigned int* count;   // 0 between barriers
+    unsigned int* gen;
+    unsigned int* ticket;  // [5]: the next block of each block phase (4 stages, diffusion), 0 at launch
+};
+__device__ __forceinline__ void grid_sync(const GridBarrier& gb, StepScalars* sc, int polls) {
+    // the next phase reads this one's global writes also through bulk copies
+    // (the async proxy): order them across the proxies on both sides
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned int g0 = *(volatile unsigned int*)gb.gen;
+        __threadfence();
+        if (atomicAdd(gb.count, 1u) == gridDim.x - 1) {
+            atomicExch(gb.count, 0u);
+            __threadfence();
+            atomicAdd(gb.gen, 1u);
+        } else {
+            int it = 0;
+            while (*(volatile unsigned int*)gb.gen == g0) {
+                if (++it > polls) {
+                    atomicOr(&sc->nan_flag, 2);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
+// The pointers of one mixed step: u^n in U, the stage buffer RK, the second
+// state buffer R2 (u^{n+1} is written there, then the host swaps U and R2).
+struct StepBuffers {
+    float* U;
+    float* RK;
+    float* R2;
+    int8_t* ulo;
+};
+
+// One mixed RK4 step of 16^3 blocks in one persistent launch: the CTAs take
+// the blocks (and, in the exchanges, the ghost entries) in turn and meet at a
+// grid barrier between the phases the graph runs as separate launches:
+// dt, then per stage s the stage kernel's body into seq[s] (pushing the
+// regular ghost faces) and the exchange of the rest (face lists), then the
+// diffusion body into R2 (pushes, next step's CFL minimum) and the exchange
+// of the remaining entries. The bodies are the separate kernels' own
+// (KPAR 2 for the stages, two threads per column for the diffusion: 512
+// threads each, and every variant computes the same bits), so the step
+// equals the graph's bit for bit.
+template <int N>
+__global__ void __launch_bounds__(512, 2)
+k_step_persistent(StepBuffers sb, PushTable push, Geometry g, StepScalars* sc, GhostLists gl_stage,
+                  GhostLists gl_final, StepDims d, GridBarrier gb) {
+    static_assert(N == 16, "16^3 blocks");
+    const int polls = sc->wait_polls;
+    if (blockIdx.x == 0 && threadIdx.x == 0) finalize_dt_body(sc);
+    grid_sync(gb, sc, polls);
+    const int64_t tstride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    auto exchange = [&](const GhostLists& G, float* u) {
+        for (int64_t e = t0; e < G.ip.n; e += tstride)
+            ghost_interp_one<float, true>(u, G.ip, d.ncell, d.nip, d.nip * d.njp, e);
+        for (int64_t e = t0; e < G.ln.n; e += tstride) ghost_lin_one<float, true>(u, G.ln, d.ncell, e);
+        for (int64_t e = t0; e < G.cp.n; e += tstride) ghost_copy_one<float, true>(u, G.cp, d.ncell, e);
+    };
+    // between two bodies in one CTA: the generic writes of the one before
+    // are ordered before the bulk copies of the next into the same memory
+    auto next_body = [&]() {
+        fence_proxy_async();
+        __syncthreads();
+    };
+    // blocks are handed out one at a time from a ticket counter per phase, as
+    // the hardware scheduler hands CTAs to SMs: a CTA that finishes early
+    // takes the next block instead of waiting at the barrier
+    __shared__ int next_b;
+    auto take = [&](int phase) -> int {
+        if (threadIdx.x == 0) next_b = (int)atomicAdd(&gb.ticket[phase], 1u);
+        __syncthreads();
+        return next_b;   // read before the next take's write: a body or next_body() barrier lies between
+    };
+    for (int s = 1; s <= 4; ++s) {
+        float* in = s == 1 ? sb.U : (s == 3 ? sb.R2 : sb.RK);
+        float* out = s == 4 ? sb.U : (s == 2 ? sb.R2 : sb.RK);   // U -> RK -> R2 -> RK -> U
+        for (int b = take(s - 1); b < d.nblocks; b = take(s - 1)) {
+            stage_body<float, 16, 16, 16, 2, 0>(b, in, sb.U, out, sb.ulo, push, DivBArgs{nullptr, nullptr, nullptr, 0},
+                                                g, sc, s, 1, 1);
+            next_body();
+        }
+        grid_sync(gb, sc, polls);
+        exchange(gl_stage, out);
+        grid_sync(gb, sc, polls);
+    }
+    for (int b = take(4); b < d.nblocks; b = take(4)) {
+        march_body<16, 16, 16, 2>(b, sb.U, sb.R2, sb.ulo, push, g, sc, 1);
+        next_body();
+    }
+    grid_sync(gb, sc, polls);
+    exchange(gl_final, sb.R2);
 }
 
 // ---- block sharding: the entries that cross ranks ---------------------------

@@ -28,4 +28,48 @@ cudaError_t launch_ghost_mixed(const StepDims& d, const GhostLists& gl, float* u
 }
 int kpar_candidates_mixed(const StepDims& d, int* out) { return impl::candidates<float>(d, out); }
 
+cudaError_t launch_step_persistent_mixed(const StepDims& d, const Geometry& g, float* U, float* RK, float* R2,
+                                         int8_t* lo, const PushTable& push, const GhostLists& gl_stage,
+                                         const GhostLists& gl_final, StepScalars* sc, unsigned int* bar,
+                                         cudaStream_t st) {
+    if (d.ni != 16 || d.nj != 16 || d.nk != 16 || !bar) return cudaErrorInvalidValue;
+    using SS = impl::Shape<float, 16, 16, 16, 2>;
+    using SD = impl::MShape<16, 16, 16, 2>;
+    constexpr size_t smem = SS::smem_stage > SD::smem ? SS::smem_stage : SD::smem;
+    // two CTAs of 512 threads per SM, as the separate stage and diffusion
+    // launches run (228 KB per SM, 1 KB of it reserved per CTA, and about
+    // 0.5 KB of static shared memory in the bodies)
+    static_assert(2 * (smem + 512 + 1024) <= 233472, "two CTAs per SM");
+    auto kern = impl::k_step_persistent<16>;
+    static int grid_cap = 0, dev_cached = -1;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev != dev_cached) {
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int per_sm = 0, nsm = 0;
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 512, smem);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) return cudaErrorLaunchOutOfResources;
+        grid_cap = per_sm * nsm;   // every CTA resident at once: the grid barrier needs it
+        dev_cached = dev;
+    }
+    const unsigned grid = (unsigned)(d.nblocks < grid_cap ? d.nblocks : grid_cap);
+    e = cudaMemsetAsync(bar, 0, 8 * sizeof(unsigned int), st);   // arrival counter, generation, block tickets
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(512);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, impl::StepBuffers{U, RK, R2, lo}, push, g, sc, gl_stage, gl_final, d,
+                              impl::GridBarrier{bar, bar + 1, bar + 2});
+}
+
 }  // namespace falcon

@@ -354,6 +354,17 @@ int  falcon_tuning(falcon_ctx* ctx, int32_t* kpar_stage, int32_t* kpar_diffusion
  * (16^3) or 2, 4 (8^3); anything else is FALCON_ERR_INVALID_ARG. Every
  * variant computes the same values bit for bit. */
 int  falcon_set_tuning(falcon_ctx* ctx, int32_t kpar_stage, int32_t kpar_diffusion);
+/* How falcon_step_rk4 runs a step. FALCON_STEP_GRAPH (default): one captured
+ * CUDA graph of 11 launches (dt, 4 stages and their exchanges, diffusion, the
+ * final exchange). FALCON_STEP_PERSISTENT: one persistent cooperative launch
+ * that runs the same kernel bodies over all blocks with a bounded grid
+ * barrier between the phases (a barrier wait that runs out makes the step
+ * return FALCON_ERR_TIMEOUT); the same values bit for bit. The persistent
+ * step covers the mixed path with 16^3 blocks and divb_option 0; other
+ * contexts return FALCON_ERR_INVALID_ARG. */
+#define FALCON_STEP_GRAPH      0
+#define FALCON_STEP_PERSISTENT 1
+int  falcon_set_step_mode(falcon_ctx* ctx, int32_t mode);
 /* device ghost-fill lists: counts[0] exact copies, [1] 1-D blends, [2] trilinear/rotated */
 int  falcon_ghost_list_sizes(const falcon_ctx* ctx, int64_t* counts);
 /* the exchanges between RK stages (face ghosts only; every stencil of a step

@@ -214,6 +214,66 @@ def test_every_kchunk_variant_computes_the_same_step(blocks):
         g.set_tuning(3, kp[0])
 
 
+def test_persistent_step_equals_graph_step():
+    """The persistent step (one cooperative launch: dt, four stages with their
+    face exchanges, diffusion, final exchange, bounded grid barriers) against
+    the captured graph, from the same state, on 16^3 blocks split radially
+    (blended radial pushes) and on the 1,296-block shell: the same dt and the
+    same state bit for bit after four steps, the first of them starting from a
+    freshly uploaded state (its CFL minimum from k_cfl)."""
+    for mk in (lambda: config.make_config(block=(16, 16, 16), root_tiles=(1, 3, 9), radial_levels=1, radial_option=1,
+                                          amr=(), precision=config.PREC_MIXED),
+               lambda: config.make_config(block=(16, 16, 16), root_tiles=(3, 3, 9), radial_levels=1, radial_option=1,
+                                          amr=((0, 1, 1),), precision=config.PREC_MIXED)):
+        a, b = fg.Falcon(mk()), fg.Falcon(mk())
+        b.set_step_mode(fg.STEP_PERSISTENT)
+        u0 = synth.initial_state(mk(), a.block_ranges(), a.block_flags(), seed=1041)
+        for x in (a, b):
+            x.upload_state(u0)
+            x.exchange()
+        for _ in range(4):
+            assert a.advance_rk4() == b.advance_rk4()
+        ua, ub = a.download_state(), b.download_state()
+        assert np.isfinite(ua).all()
+        assert np.array_equal(ua, ub)
+        a.close()
+        b.close()
+    f = fg.Falcon(config.tiny(precision=config.PREC_MIXED))    # 8^3 blocks: not covered
+    with pytest.raises(fg.FalconError):
+        f.set_step_mode(fg.STEP_PERSISTENT)
+    f64 = fg.Falcon(config.make_config(block=(16, 16, 16), root_tiles=(1, 3, 9), radial_levels=1, amr=()))
+    with pytest.raises(fg.FalconError):
+        f64.set_step_mode(fg.STEP_PERSISTENT)
+
+
+def test_persistent_step_wait_that_runs_out_returns_timeout():
+    """With the poll limit at 0 every bounded wait of the persistent step runs
+    out at once (the copy waits in the kernel bodies and the grid barriers,
+    which then let their CTA go on): the step returns FALCON_ERR_TIMEOUT, not a
+    hang or a fault, and with the default limit restored and the state
+    uploaded again the next step equals the graph step's bit for bit."""
+    mk = lambda: config.make_config(block=(16, 16, 16), root_tiles=(1, 3, 9), radial_levels=1, amr=(),
+                                    precision=config.PREC_MIXED)
+    f, ref = fg.Falcon(mk()), fg.Falcon(mk())
+    f.set_step_mode(fg.STEP_PERSISTENT)
+    u0 = synth.initial_state(mk(), f.block_ranges(), f.block_flags(), seed=1042)
+    for x in (f, ref):
+        x.upload_state(u0)
+        x.exchange()
+    f.advance_rk4()
+    f.upload_state(u0)
+    f.exchange()
+    f.set_wait_limit(0)
+    with pytest.raises(fg.FalconError) as e:
+        f.advance_rk4()
+    assert e.value.code == fg.ERR_TIMEOUT, e.value
+    f.set_wait_limit(-1)
+    f.upload_state(u0)
+    f.exchange()
+    assert f.advance_rk4() == ref.advance_rk4()
+    assert np.array_equal(f.download_state(), ref.download_state())
+
+
 def test_full_size_mixed_properties():
     """21M cells, 5,184 blocks of 16^3: steps stay finite, the exchange is
     idempotent (bit-exact), dt is positive and stable."""

@@ -72,15 +72,19 @@ def test_range_download_matches_download_state(prec):
     f.exchange()
     before = f.device_bytes()
     a = _download_by_ranges(f, MAX_ELEMS)
-    # free device memory read through the CUDA runtime after the first calls
-    # (which may load the library's device code): a cudaMalloc on any path of
-    # the range call, the context's allocator or not, would lower it
+    _download_by_ranges(f, 1_000_003)
+    # free device memory read through the CUDA runtime after a first round of
+    # both chunk shapes (which may load the library's device code and set up
+    # the driver's copy paths for these sizes): a cudaMalloc on any path of the
+    # range call, the context's allocator or not, would lower it
     rt = _cudart()
     free0 = _free_bytes(rt) if rt is not None else None
-    b = _download_by_ranges(f, 1_000_003)          # ragged ranges, second call in a row
-    assert f.device_bytes() == before              # the range call allocated nothing
+    b = _download_by_ranges(f, 1_000_003)          # ragged ranges
+    a2 = _download_by_ranges(f, MAX_ELEMS)         # whole ranges, second call in a row
+    assert f.device_bytes() == before              # the range calls allocated nothing
     if rt is not None:
         assert _free_bytes(rt) == free0
+    assert np.array_equal(a2, a)
     ref = f.download_state()
     assert np.array_equal(a, ref)
     assert np.array_equal(b, ref)
