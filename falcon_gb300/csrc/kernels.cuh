@@ -39,10 +39,18 @@ __device__ __forceinline__ float lo_inv_unit(float hi) {   // 1/unit(hi) = 2^(15
     const int e = (__float_as_int(hi) >> 23) & 0xff;
     return e >= 32 ? __int_as_float((285 - e) << 23) : 0.f;
 }
-// q for the residual r = u - hi (|r| <= ulp(hi)/2); NaN residuals give -127
+// q for the residual r = u - hi (|r| <= ulp(hi)/2); NaN residuals give -127.
+// The clamp comes first (fmaxf of a NaN is -127) and the rounding to the
+// nearest integer, ties to even, is the add of 1.5 * 2^23, whose ulp is 1:
+// the same q as rintf then clamp then (int), on the full-rate FP32 and
+// integer pipes instead of the conversion pipe.
 __device__ __forceinline__ int8_t lo_encode(float hi, float r) {
-    const float q = rintf(__fmul_rn(r, lo_inv_unit(hi)));
-    return (int8_t)(int)fminf(fmaxf(q, -127.f), 127.f);
+    const float t = fminf(fmaxf(__fmul_rn(r, lo_inv_unit(hi)), -127.f), 127.f);
+    return (int8_t)(__float_as_int(__fadd_rn(t, 12582912.f)) - 0x4B400000);
+}
+// (float)q of a correction, exactly: 2^23 + (q + 128) has ulp 1
+__device__ __forceinline__ float lo_decode(int8_t q) {
+    return __fsub_rn(__int_as_float(0x4B000000 + (int)q + 128), 8388736.f);
 }
 __device__ __forceinline__ int8_t lo_encode64(float hi, double r) {
     const double q = rint(r * (double)lo_inv_unit(hi));
@@ -51,7 +59,7 @@ __device__ __forceinline__ int8_t lo_encode64(float hi, double r) {
 // (hi + q*unit(hi)) + d, rounded to the nearest (hi', q') pair: two error-free
 // FP32 sums (Knuth's TwoSum), no contraction (explicit _rn intrinsics)
 __device__ __forceinline__ float ff_add(float hi, int8_t q, float d, int8_t& q_out) {
-    const float l = __fmul_rn((float)q, lo_unit(hi));   // exact
+    const float l = __fmul_rn(lo_decode(q), lo_unit(hi));   // exact
     const float s = __fadd_rn(hi, d);
     const float bs = __fsub_rn(s, hi);
     const float es = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bs)), __fsub_rn(d, bs));

@@ -1095,7 +1095,7 @@ __device__ __forceinline__ float2 face_flux2(float2 fl, float2 fr, float2 dL, fl
 }
 // ff_add for two variables
 __device__ __forceinline__ float2 ff_add2(float2 hi, int8_t q0, int8_t q1, float2 d, int8_t& o0, int8_t& o1) {
-    const float2 l = f2(__fmul_rn((float)q0, lo_unit(hi.x)), __fmul_rn((float)q1, lo_unit(hi.y)));
+    const float2 l = __fmul2_rn(f2(lo_decode(q0), lo_decode(q1)), f2(lo_unit(hi.x), lo_unit(hi.y)));
     const float2 s = __fadd2_rn(hi, d);
     const float2 bs = sub2(s, hi);
     const float2 es = __fadd2_rn(sub2(hi, sub2(s, bs)), sub2(d, bs));

@@ -97,7 +97,8 @@ __global__ void k_synth(T* U, const double* xj, const double* xk, Geometry geo, 
         c[V_VT * n] = (T)vt;
         c[V_VP * n] = (T)vp;
     }
-    // block sum of |v|^2
+    // the CTA's sum of |v|^2 into its own slot (summed on the host in a fixed
+    // order, so the scale and the seeded state are the same on every run)
     for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
     __shared__ double ws[8];
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = local;
@@ -105,7 +106,7 @@ __global__ void k_synth(T* U, const double* xj, const double* xk, Geometry geo, 
     if (threadIdx.x == 0) {
         double s = 0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += ws[w];
-        atomicAdd(sumsq, s);
+        sumsq[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = s;
     }
 }
 
@@ -173,20 +174,22 @@ std::string synth_initial_state(const Grid& g, const Geometry& geo, void* U, boo
     auto cleanup = [&] { cudaFree(dxj); cudaFree(dxk); cudaFree(dsum); cudaFree(dmodes); };
     cudaError_t e = cudaMalloc(&dxj, g.xj.size() * 8);
     if (e == cudaSuccess) e = cudaMalloc(&dxk, g.xk.size() * 8);
-    if (e == cudaSuccess) e = cudaMalloc(&dsum, 8);
+    dim3 grid((g.ncell + 255) / 256, g.nblocks);
+    const size_t nslot = (size_t)grid.x * grid.y;   // one partial sum per CTA
+    if (e == cudaSuccess) e = cudaMalloc(&dsum, nslot * 8);
     if (e == cudaSuccess) e = cudaMalloc(&dmodes, sizeof(Mode) * NMODE);
     if (e == cudaSuccess) e = cudaMemcpy(dxj, g.xj.data(), g.xj.size() * 8, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(dxk, g.xk.data(), g.xk.size() * 8, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(dmodes, modes.data(), sizeof(Mode) * NMODE, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemset(dsum, 0, 8);
     if (e != cudaSuccess) { cleanup(); return std::string("synth setup: ") + cudaGetErrorString(e); }
-    dim3 grid((g.ncell + 255) / 256, g.nblocks);
     if (mixed) k_synth<float><<<grid, 256, 0, st>>>((float*)U, dxj, dxk, geo, d, sp, dmodes, dsum);
     else k_synth<double><<<grid, 256, 0, st>>>((double*)U, dxj, dxk, geo, d, sp, dmodes, dsum);
     double sumsq = 0;
+    std::vector<double> part(nslot);
     e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&sumsq, dsum, 8, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(part.data(), dsum, nslot * 8, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    for (double x : part) sumsq += x;
     if (e == cudaSuccess && kind == 1 && sumsq > 0) {
         const double nint = (double)g.nblocks * g.ni * g.nj * g.nk;
         const double vrms = std::sqrt(sumsq / nint);
