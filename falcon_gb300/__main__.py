@@ -13,6 +13,10 @@ Workloads:
                    5,308,416 cells): the profiling case
 Initial state: kind 1 of falcon_init_synthetic (entropy bump, dipole B and a
 random-phase Kolmogorov velocity at rms Mach 0.01, seed 1002).
+
+--tuning KS KD fixes the k-chunk variants of the stage and diffusion kernels
+(falcon_set_tuning) instead of the autotuner, whose timings a profiler would
+distort; --step-mode persistent runs each step as one persistent launch.
 """
 import argparse
 import json
@@ -36,9 +40,16 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--tuning", type=int, nargs=2, metavar=("KS", "KD"), default=None)
+    ap.add_argument("--step-mode", choices=("graph", "persistent"), default="graph")
     a = ap.parse_args(argv)
     build()
     f = Falcon(WORKLOADS[a.workload](a.device))
+    if a.tuning:
+        f.set_tuning(*a.tuning)
+    if a.step_mode == "persistent":
+        from . import STEP_PERSISTENT
+        f.set_step_mode(STEP_PERSISTENT)
     f.init_synthetic(kind=1, seed=1002, mach=0.01)
     f.exchange()
     f.exchange()
@@ -48,7 +59,7 @@ def main(argv=None):
     f.run_steps(a.steps)
     ms = f.timer_stop()
     f.synchronize()
-    print(json.dumps({"workload": a.workload, "cells": f.interior_cells, "steps": a.steps,
+    print(json.dumps({"workload": a.workload, "cells": f.interior_cells, "steps": a.steps, "step_mode": a.step_mode,
                       "ms_per_step": ms / max(a.steps, 1),
                       "cell_updates_per_s": f.interior_cells * a.steps / (ms / 1e3) if ms > 0 else None,
                       "tuning": f.tuning()}))
