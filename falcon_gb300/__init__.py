@@ -63,7 +63,7 @@ EXPORTS = (
     "falcon_solver_tuning", "falcon_solver_set_tile", "falcon_shard_ranges", "falcon_shard_plan",
     "falcon_set_shard", "falcon_shard_counts", "falcon_shard_pack", "falcon_shard_unpack",
     "falcon_shard_min_ratio", "falcon_shard_set_min_ratio", "falcon_lcc_set_tensor_path", "falcon_set_tuning",
-    "falcon_set_step_mode",
+    "falcon_set_step_mode", "falcon_lcc_set_wait_limit",
 )
 
 # size of the static device array behind falcon_download_state_range

@@ -203,8 +203,10 @@ __device__ __forceinline__ void mbar_init(uint64_t* b) {
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
 }
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
-    for (int it = 0; it < kPolls; ++it) {
+// polls: the caller's limit (the network's wait limit, or kPolls for the
+// drains after a wait ran out)
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, int polls = kPolls) {
+    for (int it = 0; it < polls; ++it) {
         uint32_t ok;
         asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
                      : "=r"(ok)
@@ -323,7 +325,7 @@ __global__ void __launch_bounds__(128) k_conv_tc(const __nv_bfloat16* __restrict
                                                  const __grid_constant__ CUtensorMap wmap, Grid3 g,
                                                  const float* __restrict__ bias, int relu,
                                                  __nv_bfloat16* __restrict__ out16, float* __restrict__ out32,
-                                                 int32_t* err) {
+                                                 int32_t* err, int polls) {
     using namespace tc;
     constexpr int ST = kConvStages;
     constexpr int HD = 3, HH = kRowH + 2, HW = kRowW + 2, HROWS = HD * HH * HW;
@@ -381,7 +383,7 @@ __global__ void __launch_bounds__(128) k_conv_tc(const __nv_bfloat16* __restrict
     // of those warps wait at __syncwarp, not in a polling loop beside them
     if (tid == 0) {                                  // weight copies of the later taps
         for (int t = ST; t < 27; ++t) {
-            if (!mbar_wait(&empty[t % ST], (uint32_t)((t / ST - 1) & 1))) { late = 1; break; }
+            if (!mbar_wait(&empty[t % ST], (uint32_t)((t / ST - 1) & 1), polls)) { late = 1; break; }
             issue_b(t);
         }
     } else if (tid == 32) {                          // MMAs
@@ -389,7 +391,7 @@ __global__ void __launch_bounds__(128) k_conv_tc(const __nv_bfloat16* __restrict
         const uint32_t a0 = smem_u32(abase);
         for (int t = 0; t < 27; ++t) {
             const int s = t % ST;
-            if (!mbar_wait(&full[s], (uint32_t)((t / ST) & 1))) { late = 1; break; }
+            if (!mbar_wait(&full[s], (uint32_t)((t / ST) & 1), polls)) { late = 1; break; }
             fence_after();
             const int sgn = MODE == 2 ? -1 : 1;
             const int dd = sgn * (t / 9 - 1), dh = sgn * ((t / 3) % 3 - 1), dw = sgn * (t % 3 - 1);
@@ -404,7 +406,12 @@ __global__ void __launch_bounds__(128) k_conv_tc(const __nv_bfloat16* __restrict
         commit(done);                                // completes when every MMA issued above has
     }
     if (warp < 2) __syncwarp();
-    if (!mbar_wait(done, 0u)) late = 1;
+    // the MMAs issued complete whatever the limit: after a wait that ran out
+    // they are drained with the default bound before tensor memory is read or freed
+    if (!mbar_wait(done, 0u, polls)) {
+        late = 1;
+        mbar_wait(done, 0u);
+    }
     late = __syncthreads_or(late);
     if (late && tid == 0) {
         drain_copies<ST>(full, issued);
@@ -452,7 +459,7 @@ template <int CO, int CI>
 __global__ void __launch_bounds__(128) k_wgrad_tc(const __grid_constant__ CUtensorMap gmap,
                                                   const __grid_constant__ CUtensorMap xmap, Grid3 g, int64_t nbricks,
                                                   int per_cta, int co_real, int ci_real, float* __restrict__ dw,
-                                                  int32_t* err) {
+                                                  int32_t* err, int polls) {
     using namespace tc;
     constexpr uint32_t SPAN_A = CO * 2, SPAN_B = CI * 2;
     constexpr uint32_t A_BYTES = 128u * SPAN_A, B_BYTES = 128u * SPAN_B;
@@ -475,7 +482,7 @@ __global__ void __launch_bounds__(128) k_wgrad_tc(const __grid_constant__ CUtens
     if (tid == 0) {
         for (int t = 0; t < nb; ++t) {
             const int s = t % kStages;
-            if (t >= kStages && !mbar_wait(&empty[s], (uint32_t)((t / kStages - 1) & 1))) { late = 1; break; }
+            if (t >= kStages && !mbar_wait(&empty[s], (uint32_t)((t / kStages - 1) & 1), polls)) { late = 1; break; }
             const Brick bk = brick_of(g, b0 + t);
             mbar_expect_tx(&full[s], A_BYTES + B_BYTES);
             tma_5d(abase + s * A_STRIDE, &gmap, &full[s], 0, bk.w0, bk.h0, bk.d0, bk.s);
@@ -485,7 +492,7 @@ __global__ void __launch_bounds__(128) k_wgrad_tc(const __grid_constant__ CUtens
     } else if (tid == 32) {
         for (int t = 0; t < nb; ++t) {
             const int s = t % kStages;
-            if (!mbar_wait(&full[s], (uint32_t)((t / kStages) & 1))) { late = 1; break; }
+            if (!mbar_wait(&full[s], (uint32_t)((t / kStages) & 1), polls)) { late = 1; break; }
             fence_after();
             const uint32_t a0 = smem_u32(abase + s * A_STRIDE), bb = smem_u32(bbase + s * B_STRIDE);
 #pragma unroll
@@ -498,7 +505,12 @@ __global__ void __launch_bounds__(128) k_wgrad_tc(const __grid_constant__ CUtens
         commit(done);
     }
     if (warp < 2) __syncwarp();                      // the role lanes' warps reconverge before polling
-    if (!mbar_wait(done, 0u)) late = 1;
+    // the MMAs issued complete whatever the limit: after a wait that ran out
+    // they are drained with the default bound before tensor memory is read or freed
+    if (!mbar_wait(done, 0u, polls)) {
+        late = 1;
+        mbar_wait(done, 0u);
+    }
     late = __syncthreads_or(late);
     if (late && tid == 0) {
         drain_copies<kStages>(full, issued);
@@ -806,7 +818,7 @@ constexpr uint32_t ring_bytes(uint32_t a, uint32_t b) { return tc::kStages * (tc
 
 template <int K, int N, int MODE>
 cudaError_t conv_tc_launch(const __nv_bfloat16* x, Grid3 g, const __nv_bfloat16* w, const float* bias, int relu,
-                           __nv_bfloat16* out16, float* out32, int32_t* err, cudaStream_t st) {
+                           __nv_bfloat16* out16, float* out32, int32_t* err, int polls, cudaStream_t st) {
     // the weight ring, then the halo (3 x 18 x 10 voxels of K channels)
     constexpr uint32_t smem = tc::kConvStages * tc::up1024((uint32_t)N * K * 2) + 3u * (tc::kRowH + 2) * (tc::kRowW + 2) * K * 2 + 1024u;
     CUtensorMap wm;
@@ -815,13 +827,13 @@ cudaError_t conv_tc_launch(const __nv_bfloat16* x, Grid3 g, const __nv_bfloat16*
         e = cudaFuncSetAttribute(k_conv_tc<K, N, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const int64_t blocks = (int64_t)g.n * g.D * ((g.H + tc::kRowH - 1) / tc::kRowH) * ((g.W + tc::kRowW - 1) / tc::kRowW);
-    k_conv_tc<K, N, MODE><<<(unsigned)blocks, 128, smem, st>>>(x, wm, g, bias, relu, out16, out32, err);
+    k_conv_tc<K, N, MODE><<<(unsigned)blocks, 128, smem, st>>>(x, wm, g, bias, relu, out16, out32, err, polls);
     return cudaGetLastError();
 }
 
 template <int CO, int CI>
 cudaError_t wgrad_tc_launch(const __nv_bfloat16* gy, const __nv_bfloat16* x, Grid3 g, int co_real, int ci_real,
-                            float* dw, int32_t* err, cudaStream_t st) {
+                            float* dw, int32_t* err, int polls, cudaStream_t st) {
     constexpr uint32_t smem = ring_bytes(128u * CO * 2, 128u * CI * 2);
     CUtensorMap gm, xm;
     cudaError_t e = act_map(&gm, gy, g, CO);
@@ -832,7 +844,7 @@ cudaError_t wgrad_tc_launch(const __nv_bfloat16* gy, const __nv_bfloat16* x, Gri
     const int64_t nb = bricks(g);
     const int per = (int)std::max<int64_t>(1, std::min<int64_t>(16, nb / 64));   // bricks (K = 128 each) per CTA
     const dim3 grid((unsigned)((nb + per - 1) / per), 27);
-    k_wgrad_tc<CO, CI><<<grid, 128, smem, st>>>(gm, xm, g, nb, per, co_real, ci_real, dw, err);
+    k_wgrad_tc<CO, CI><<<grid, 128, smem, st>>>(gm, xm, g, nb, per, co_real, ci_real, dw, err, polls);
     return cudaGetLastError();
 }
 
@@ -840,12 +852,12 @@ cudaError_t wgrad_tc_launch(const __nv_bfloat16* gy, const __nv_bfloat16* x, Gri
 template <int MODE>
 cudaError_t conv_launch(int kc, int nc, const __nv_bfloat16* x, Grid3 g, const __nv_bfloat16* w, const float* bias,
                         int relu, __nv_bfloat16* out16, float* out32, cudaStream_t st, bool tc = false,
-                        int32_t* err = nullptr) {
+                        int32_t* err = nullptr, int polls = tc::kPolls) {
     const int64_t nv = (int64_t)g.n * g.D * g.H * g.W;
     const unsigned blocks = (unsigned)((nv + 63) / 64);
 #define LCC_CONV(K, N)                                                                                   \
     if (kc == K && nc == N) {                                                                            \
-        if (tc) return conv_tc_launch<K, N, MODE>(x, g, w, bias, relu, out16, out32, err, st);           \
+        if (tc) return conv_tc_launch<K, N, MODE>(x, g, w, bias, relu, out16, out32, err, polls, st);    \
         k_conv<K, N, MODE><<<blocks, 128, 0, st>>>(x, g, w, bias, relu, out16, out32);                   \
         return cudaGetLastError();                                                                       \
     }
@@ -856,13 +868,14 @@ cudaError_t conv_launch(int kc, int nc, const __nv_bfloat16* x, Grid3 g, const _
 }
 
 inline cudaError_t wgrad_launch(int co, int ci, const __nv_bfloat16* gy, const __nv_bfloat16* x, Grid3 g, int co_real,
-                                int ci_real, float* dw, cudaStream_t st, bool tc = false, int32_t* err = nullptr) {
+                                int ci_real, float* dw, cudaStream_t st, bool tc = false, int32_t* err = nullptr,
+                                int polls = tc::kPolls) {
     const int64_t nv = (int64_t)g.n * g.D * g.H * g.W;
     const int chunk = 512;
     const dim3 grid((unsigned)((nv + chunk - 1) / chunk), 27);
 #define LCC_WG(CO, CI)                                                                                   \
     if (co == CO && ci == CI) {                                                                          \
-        if (tc) return wgrad_tc_launch<CO, CI>(gy, x, g, co_real, ci_real, dw, err, st);                 \
+        if (tc) return wgrad_tc_launch<CO, CI>(gy, x, g, co_real, ci_real, dw, err, polls, st);          \
         k_conv_wgrad<CO, CI><<<grid, 128, 0, st>>>(gy, x, g, chunk, co_real, ci_real, dw);               \
         return cudaGetLastError();                                                                       \
     }
@@ -894,6 +907,7 @@ struct falcon_lcc {
     Grid3 shape{0, 0, 0, 0};
     bool use_tc = true;               // convolutions on tcgen05 (else mma.sync)
     int32_t* dflag = nullptr;         // device: a tcgen05 kernel's wait ran out
+    int polls = tc::kPolls;           // the tcgen05 kernels' wait limit
     struct Acts {
         bf16 *x0, *a1, *s0, *p0, *a2, *s1, *p1, *s2, *p2, *a5, *u2, *a6, *u1, *a7, *u0, *a8, *gb;
         float *y, *xin, *t;
@@ -963,7 +977,7 @@ cudaError_t forward(falcon_lcc* net, cudaStream_t st) {
     k_prep_input<<<ew_grid(V0 * 16), 256, 0, st>>>(A.xin, V0, A.x0);
     auto conv = [&](int l, const bf16* x, Grid3 g, bf16* y) {
         return conv_launch<0>(pad16(kSpec[l].ci), pad16(kSpec[l].co), x, g, net->wf[l], net->p + net->boff[l],
-                              kSpec[l].relu, y, nullptr, st, net->use_tc, net->dflag);
+                              kSpec[l].relu, y, nullptr, st, net->use_tc, net->dflag, net->polls);
     };
     auto pool = [&](const bf16* x, Grid3 g, int C, bf16* y) {
         k_pool<<<ew_grid((int64_t)g.n * g.D * g.H * g.W * C / 8), 256, 0, st>>>(x, g, C, y);
@@ -989,7 +1003,7 @@ cudaError_t forward(falcon_lcc* net, cudaStream_t st) {
     if ((e = upadd(A.a7, A.s0, G0, 16, A.u0)) != cudaSuccess) return e;
     if ((e = conv(8, A.u0, G0, A.a8)) != cudaSuccess) return e;
     return conv_launch<1>(16, 16, A.a8, G0, net->wf[9], net->p + net->boff[9], 0, nullptr, A.y, st, net->use_tc,
-                          net->dflag);
+                          net->dflag, net->polls);
 }
 
 // loss and parameter gradients (net->g zeroed here) for targets in A.t
@@ -1009,9 +1023,11 @@ cudaError_t backward(falcon_lcc* net, cudaStream_t st) {
         const int64_t n = nv(g) * cop;
         k_relu_grad<<<ew_grid(n), 256, 0, st>>>(dy, y, n, kSpec[l].relu ? 1 : 0, A.gb);
         k_bias_grad<<<ew_grid(n), 256, 0, st>>>(A.gb, nv(g), cop, co, net->g + net->boff[l]);
-        cudaError_t e2 = wgrad_launch(cop, cip, A.gb, x, g, co, ci, net->g + net->woff[l], st, net->use_tc, net->dflag);
+        cudaError_t e2 =
+            wgrad_launch(cop, cip, A.gb, x, g, co, ci, net->g + net->woff[l], st, net->use_tc, net->dflag, net->polls);
         if (e2 != cudaSuccess || !dx) return e2;
-        return conv_launch<2>(cop, cip, A.gb, g, net->wb[l], nullptr, 0, nullptr, dx, st, net->use_tc, net->dflag);
+        return conv_launch<2>(cop, cip, A.gb, g, net->wb[l], nullptr, 0, nullptr, dx, st, net->use_tc, net->dflag,
+                              net->polls);
     };
     auto upback = [&](const float* gf, Grid3 gfine, int C, float* out) {
         k_up_back<<<ew_grid(nv(gfine) * C / 8), 256, 0, st>>>(gf, gfine, C, out);
@@ -1188,6 +1204,12 @@ int falcon_lcc_loss_grad(falcon_lcc* net, const float* x, const float* t, int32_
     LCK(cudaStreamSynchronize(net->st), "backward");
     *loss = sum / (double)V0;
     return check_flag(net);
+}
+
+int falcon_lcc_set_wait_limit(falcon_lcc* net, int32_t polls) {
+    if (!net) return FALCON_ERR_INVALID_ARG;
+    net->polls = polls < 0 ? tc::kPolls : polls;
+    return FALCON_OK;
 }
 
 int falcon_lcc_set_tensor_path(falcon_lcc* net, int32_t path) {

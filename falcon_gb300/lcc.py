@@ -56,6 +56,10 @@ class LCC:
         """TCGEN05 or MMA_SYNC for the forward and backward-data convolutions."""
         self._ck(self.L.falcon_lcc_set_tensor_path(self.h, C.c_int32(path)))
 
+    def set_wait_limit(self, polls):
+        """Poll limit of the tcgen05 kernels' waits (< 0: the default)."""
+        self._ck(self.L.falcon_lcc_set_wait_limit(self.h, C.c_int32(polls)))
+
     def params(self):
         p = np.zeros(self.nparams, dtype=np.float32)
         self._ck(self.L.falcon_lcc_get_params(self.h, _ptr(p)))

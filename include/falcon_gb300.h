@@ -597,6 +597,12 @@ int  falcon_lcc_train(falcon_lcc* net, const float* x, const float* t, int32_t n
 #define FALCON_LCC_MMA_SYNC 0
 #define FALCON_LCC_TCGEN05  1
 int  falcon_lcc_set_tensor_path(falcon_lcc* net, int32_t path);
+/* Poll limit of the tcgen05 kernels' mbarrier waits (default 4,194,304;
+ * polls < 0 restores it). A wait that runs out ends the tile: its copies and
+ * MMAs in flight are drained with the default bound before its tensor memory
+ * is freed, its results are discarded, and the call returns
+ * FALCON_ERR_TIMEOUT. */
+int  falcon_lcc_set_wait_limit(falcon_lcc* net, int32_t polls);
 
 #ifdef __cplusplus
 }

@@ -121,3 +121,30 @@ def test_gpu_tcgen05_convolutions_match_mma_sync(built_lib):
     for l in range(len(O.LAYERS)):
         sl = slice(offs[l], offs[l + 1])
         assert _rel(g1[sl], g0[sl]) <= 2e-2, (l, _rel(g1[sl], g0[sl]))
+
+
+@pytest.mark.gpu
+def test_gpu_tcgen05_wait_that_runs_out_returns_timeout(built_lib):
+    """With the poll limit at 0 the tcgen05 kernels' waits run out at once: the
+    copies and MMAs in flight are drained, the tiles discarded, and forward,
+    loss_grad and train return FALCON_ERR_TIMEOUT (no fault, no hang); with
+    the default restored a fresh network gives the same results as before."""
+    import falcon_gb300 as fg
+    from falcon_gb300 import lcc as L
+    x, t = _inputs(2, 8, 8, 24, 17)
+    net = L.LCC(device=0, seed=4)
+    y0 = net.forward(x)
+    l0, g0 = net.loss_grad(x, t)
+    net.set_wait_limit(0)
+    for call in (lambda: net.forward(x), lambda: net.loss_grad(x, t),
+                 lambda: net.train(x, t, epochs=1, batch=2, lr=1e-4, seed=1)):
+        with pytest.raises(fg.FalconError) as e:
+            call()
+        assert e.value.code == fg.ERR_TIMEOUT, e.value
+    net.set_wait_limit(-1)
+    net.set_params(net.params())       # the failed train step may have moved the weights: reset Adam too
+    assert np.isfinite(net.forward(x)).all()
+    ref = L.LCC(device=0, seed=4)
+    assert np.array_equal(ref.forward(x), y0)           # no atomics in the forward pass: the same bits
+    l1, g1 = ref.loss_grad(x, t)                        # FP32 atomic sums in the weight gradients
+    assert abs(l1 - l0) <= 1e-6 * l0 and _rel(g1, g0) <= 1e-5
