@@ -587,9 +587,10 @@ int  falcon_lcc_loss_grad(falcon_lcc* net, const float* x, const float* t, int32
  * epoch_loss[epochs] receives the mean training loss of each epoch */
 int  falcon_lcc_train(falcon_lcc* net, const float* x, const float* t, int32_t nsamples, int32_t D, int32_t H,
                       int32_t W, int32_t epochs, int32_t batch, float lr, uint64_t seed, float* epoch_loss);
-/* Tensor-core path of the forward and backward-data convolutions:
- * FALCON_LCC_TCGEN05 (5th-generation tensor cores: tcgen05.mma with the FP32
- * accumulator in tensor memory, operands staged in shared memory) or
+/* Tensor-core path of the convolutions (forward, backward data and weight
+ * gradients): FALCON_LCC_TCGEN05, the default (5th-generation tensor cores:
+ * tcgen05.mma with the FP32 accumulator in tensor memory, operands staged in
+ * shared memory, weight and activation tiles brought in by TMA), or
  * FALCON_LCC_MMA_SYNC (warp-level mma.sync). Same BF16 operands and FP32
  * accumulation; sums may differ in the last bits of their order. A tcgen05
  * kernel's bounded wait that runs out makes the call return
