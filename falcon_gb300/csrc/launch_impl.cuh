@@ -100,10 +100,28 @@ cudaError_t diff_march16(const StepDims& d, const Geometry& g, const float* u, f
     return cudaGetLastError();
 }
 
+// FP64 8^3 blocks: the k-march kernel, in place (any k-chunk depth asked for)
+inline cudaError_t diff_march64_8(const StepDims& d, const Geometry& g, double* u, StepScalars* sc, cudaStream_t st) {
+    using S = M64Shape<8, 8, 8>;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_diffusion_march64<8, 8, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)S::smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    k_diffusion_march64<8, 8, 8><<<d.nblocks, S::NT, S::smem, st>>>(u, g, sc);
+    return cudaGetLastError();
+}
+
 template <class T>
 cudaError_t diff_any(const StepDims& d, const Geometry& g, const T* u, T* out, int8_t* lo, const PushTable& push,
                      StepScalars* sc, int kpar, cudaStream_t st, int cfl_next = 0) {
     if (push.tgt != nullptr && out == u) return cudaErrorInvalidValue;   // pushing needs out != u
+    if constexpr (Pol<T>::exact) {
+        if (d.ni == 8 && d.nj == 8 && d.nk == 8 && out == u && push.tgt == nullptr)
+            return diff_march64_8(d, g, out, sc, st);
+    }
     if constexpr (!Pol<T>::exact) {
         if (d.ni == 16 && d.nj == 16 && d.nk == 16)
             return kpar == 1 ? diff_march16<1>(d, g, u, out, lo, push, sc, cfl_next, st)

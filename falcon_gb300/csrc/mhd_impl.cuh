@@ -1431,6 +1431,183 @@ k_diffusion_march(const float* u, float* out, int8_t* ulo, PushTable push, Geome
 }
 
 // ---------------------------------------------------------------------------
+// FP64 artificial diffusion (3_6/ModDiffusion.f90:9-150) of one block as a k
+// march, in place (the exact path: no pushes, no fused CFL minimum, no u^n
+// correction). One thread per (cell column, variable): NI*NJ*NV threads. The
+// k window, slope and face of the thread's column and variable stay in
+// registers; across each plane every i and j slope is formed once, then every
+// i and j face flux, then each cell sums its six faces. The fluxes are the
+// chunked kernel's functions of the same four values and the sum runs in the
+// reference's order (i, j, k, each as a division by its denominator), so the
+// result is the same bit for bit, with 3 minmod slopes per cell and variable
+// where the chunked kernel forms 5 or 6.
+template <int NI, int NJ, int NK>
+struct M64Shape {
+    static constexpr int NG = 2, NIP = NI + 4, NJP = NJ + 4, NKP = NK + 4;
+    static constexpr int PL = NIP * NJP, NCELL = PL * NKP;
+    static constexpr int NCOL = NI * NJ, NT = NCOL * NV;
+    static constexpr int W = 5;                          // plane ring slots
+    static constexpr uint32_t PLB = PL * 8u;
+    static constexpr int P = NI + 2;                     // row pitch of the slope and face arrays
+    // per variable: SI[NJ][P] (cells i = -1..NI at i + 1), SJ[NJ + 2][P]
+    // (rows j = -1..NJ at j + 1), FI[NJ][P] (faces i - 1/2, i = 0..NI), FJ[NJ + 1][P]
+    static constexpr int NSI = NJ * P, NSJ = (NJ + 2) * P, NFI = NJ * P, NFJ = (NJ + 1) * P;
+    // shared memory: mbarriers | tile[NV][W][PL] | SI | SJ | FI | FJ | gi | gj | gs
+    static constexpr size_t off_tile = 64;
+    static constexpr size_t off_si = off_tile + (size_t)NV * W * PL * 8;
+    static constexpr size_t off_sj = off_si + (size_t)NV * NSI * 8;
+    static constexpr size_t off_fi = off_sj + (size_t)NV * NSJ * 8;
+    static constexpr size_t off_fj = off_fi + (size_t)NV * NFI * 8;
+    static constexpr size_t off_gi = off_fj + (size_t)NV * NFJ * 8;
+    static constexpr size_t off_gj = off_gi + (size_t)GI_COUNT * NIP * 8;
+    static constexpr size_t off_gs = off_gj + (size_t)GJ_COUNT * NJP * 8;
+    static constexpr size_t smem = off_gs + GS_COUNT * 8;
+    static_assert(NT <= 1024, "one thread per column and variable");
+};
+
+template <int NI, int NJ, int NK>
+__global__ void __launch_bounds__(NI * NJ * NV)
+k_diffusion_march64(double* u, Geometry g, StepScalars* sc) {
+    using S = M64Shape<NI, NJ, NK>;
+    constexpr int NIP = S::NIP, PL = S::PL, W = S::W, NCELL = S::NCELL, P = S::P;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
+    double* tile = reinterpret_cast<double*>(smem + S::off_tile);
+    double* SI = reinterpret_cast<double*>(smem + S::off_si);
+    double* SJ = reinterpret_cast<double*>(smem + S::off_sj);
+    double* FI = reinterpret_cast<double*>(smem + S::off_fi);
+    double* FJ = reinterpret_cast<double*>(smem + S::off_fj);
+    double* gi = reinterpret_cast<double*>(smem + S::off_gi);
+    double* gj = reinterpret_cast<double*>(smem + S::off_gj);
+    double* gs = reinterpret_cast<double*>(smem + S::off_gs);
+    const int b = blockIdx.x, tid = threadIdx.x;
+    double* blk = u + (size_t)b * NV * NCELL;
+    if (tid == 0) {
+        for (int q = 0; q < W; ++q) mbar_init(&bars[q], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    int issued = 0;   // thread 0: planes [0, issued) have been requested
+    if (tid == 0) {
+        for (int p = 0; p < W; ++p) issue_planes<double, S>(blk, tile, p, p + 1, &bars[p]);
+        issued = W;
+    }
+    load_geometry<double, S>(g, b, gi, gj, gs, nullptr);
+    __syncthreads();
+    const int c = tid % S::NCOL, v = tid / S::NCOL;
+    const int i = c % NI, j = c / NI, ii = i + 2, jj = j + 2;
+    const double* GCS = gi + GI_CS * NIP;
+    const double cs = GCS[ii];
+    const double rc = gi[GI_R * NIP + ii];
+    const double den[3] = {gs[GS_DXI], gs[GS_DXJ] * rc, gs[GS_DXK] * rc * gj[GJ_SIN * S::NJP + jj]};
+    const double hdt = 0.5 * sc->dt;
+    const int polls = sc->wait_polls;
+    int late = 0;
+    auto abort_cta = [&]() {
+        if (tid != 0) return;
+        atomicOr(&sc->nan_flag, 2);
+        for (int p = issued - W < 0 ? 0 : issued - W; p < issued; ++p)
+            mbar_wait(&bars[p % W], (uint32_t)((p / W) & 1), kWaitPolls);
+        for (int q = 0; q < W; ++q) mbar_inval(&bars[q]);
+    };
+    double* SIv = SI + v * S::NSI;
+    double* SJv = SJ + v * S::NSJ;
+    double* FIv = FI + v * S::NFI;
+    double* FJv = FJ + v * S::NFJ;
+    const double* col = tile + (size_t)v * W * PL + jj * NIP + ii;         // this column, this variable
+    const double* colvp = tile + (size_t)V_VP * W * PL + jj * NIP + ii;    // this column's v_phi
+    for (int p = 0; p < 4; ++p) late |= mbar_wait(&bars[p], 0u, polls) ? 0 : 1;
+    double u0, u1, dk0, fk0;
+    {
+        const double a0 = col[0], a1 = col[PL], a2 = col[2 * PL], a3 = col[3 * PL];
+        const double d1 = face_slope(a0, a1, a2), d2 = face_slope(a1, a2, a3);
+        u0 = a2;
+        u1 = a3;
+        dk0 = d2;
+        fk0 = face_flux_s(a1, a2, d1, d2, fabs(colvp[PL]) + cs, fabs(colvp[2 * PL]) + cs);
+    }
+    for (int kp = 2; kp < NK + 2; ++kp) {
+        const int p2 = kp + 2;
+        late |= mbar_wait(&bars[p2 % W], (uint32_t)((p2 / W) & 1), polls) ? 0 : 1;
+        const int s0 = (kp % W) * PL, s1 = ((kp + 1) % W) * PL, s2 = (p2 % W) * PL;
+        const double* tc = col + s0;   // this cell in plane kp
+        // ---- phase A: k slope and face from the window; i and j slopes
+        const double u2 = col[s2];
+        const double dk1 = face_slope(u0, u1, u2);
+        const double fk1 = face_flux_s(u0, u1, dk0, dk1, fabs(colvp[s0]) + cs, fabs(colvp[s1]) + cs);
+        SIv[j * P + i + 1] = face_slope(tc[-1], u0, tc[1]);
+        SJv[(j + 1) * P + i] = face_slope(tc[-NIP], u0, tc[NIP]);
+        // ghost-cell slopes: i = -1, NI of every row, j = -1, NJ of every column
+        constexpr int NEI = 2 * NJ * NV, NEJ = 2 * NI * NV;
+        for (int x = tid; x < NEI + NEJ; x += S::NT) {
+            if (x < NEI) {
+                const int side = x & 1, r = (x >> 1) % NJ, w = (x >> 1) / NJ;
+                const double* q = tile + (size_t)w * W * PL + s0 + (r + 2) * NIP + (side ? NI + 2 : 1);
+                SI[w * S::NSI + r * P + (side ? NI + 1 : 0)] = face_slope(q[-1], q[0], q[1]);
+            } else {
+                const int y = x - NEI, side = y & 1, r = (y >> 1) % NI, w = (y >> 1) / NI;
+                const double* q = tile + (size_t)w * W * PL + s0 + (side ? NJ + 2 : 1) * NIP + r + 2;
+                SJ[w * S::NSJ + (side ? NJ + 1 : 0) * P + r] = face_slope(q[-NIP], q[0], q[NIP]);
+            }
+        }
+        if (__syncthreads_or(late)) {
+            abort_cta();
+            return;
+        }
+        // ---- phase B: this cell's faces i - 1/2 and j - 1/2; the last faces
+        // of the rows and columns
+        const double* vr = tile + (size_t)V_VR * W * PL + s0 + jj * NIP + ii;
+        const double* vt = tile + (size_t)V_VT * W * PL + s0 + jj * NIP + ii;
+        const double fi0 = face_flux_s(tc[-1], u0, SIv[j * P + i], SIv[j * P + i + 1], fabs(vr[-1]) + GCS[ii - 1],
+                                       fabs(vr[0]) + cs);
+        const double fj0 =
+            face_flux_s(tc[-NIP], u0, SJv[j * P + i], SJv[(j + 1) * P + i], fabs(vt[-NIP]) + cs, fabs(vt[0]) + cs);
+        FIv[j * P + i] = fi0;
+        FJv[j * P + i] = fj0;
+        constexpr int NFE = NJ * NV + NI * NV;
+        for (int x = tid; x < NFE; x += S::NT) {
+            if (x < NJ * NV) {
+                const int r = x % NJ, w = x / NJ;
+                const double* a = tile + (size_t)w * W * PL + s0 + (r + 2) * NIP + NI + 1;   // last interior cell of row r
+                const double* vrr = tile + (size_t)V_VR * W * PL + s0 + (r + 2) * NIP + NI + 1;
+                FI[w * S::NFI + r * P + NI] =
+                    face_flux_s(a[0], a[1], SI[w * S::NSI + r * P + NI], SI[w * S::NSI + r * P + NI + 1],
+                                fabs(vrr[0]) + GCS[NI + 1], fabs(vrr[1]) + GCS[NI + 2]);
+            } else {
+                const int y = x - NJ * NV, r = y % NI, w = y / NI;
+                const double* a = tile + (size_t)w * W * PL + s0 + (NJ + 1) * NIP + r + 2;   // last interior row, column r
+                const double* vtt = tile + (size_t)V_VT * W * PL + s0 + (NJ + 1) * NIP + r + 2;
+                const double c2 = GCS[r + 2];
+                FJ[w * S::NFJ + NJ * P + r] =
+                    face_flux_s(a[0], a[NIP], SJ[w * S::NSJ + NJ * P + r], SJ[w * S::NSJ + (NJ + 1) * P + r],
+                                fabs(vtt[0]) + c2, fabs(vtt[NIP]) + c2);
+            }
+        }
+        __syncthreads();
+        if (tid == 0) {
+            for (; issued < S::NKP && issued <= kp + W; ++issued)
+                issue_planes<double, S>(blk, tile, issued, issued + 1, &bars[issued % W]);
+        }
+        // ---- phase C: the six faces in the reference's order, the update in place
+        double R = 0.0;
+        R = R + Pol<double>::dv(fi0 - FIv[j * P + i + 1], den[0], 0.0);
+        R = R + Pol<double>::dv(fj0 - FJv[(j + 1) * P + i], den[1], 0.0);
+        R = R + Pol<double>::dv(fk0 - fk1, den[2], 0.0);
+        blk[(size_t)v * NCELL + (size_t)kp * PL + jj * NIP + ii] = u0 + hdt * R;
+        u0 = u1;
+        u1 = u2;
+        dk0 = dk1;
+        fk0 = fk1;
+    }
+    if (__syncthreads_or(late)) {
+        abort_cta();
+        return;
+    }
+    if (tid == 0)
+        for (int q = 0; q < W; ++q) mbar_inval(&bars[q]);
+}
+
+// ---------------------------------------------------------------------------
 // dt = min(1.e20, CFL*min(h/v_wave)) (3_6/ModTimeStep.f90:20-29); also the
 // per-stage FP32 factors of the mixed path and the reset of the accumulator.
 // One thread (k_finalize_dt, or the first phase of the persistent step).
