@@ -175,11 +175,16 @@ struct Shape {
     static constexpr uint32_t PLB = PL * (uint32_t)sizeof(T);   // bytes of one variable plane
     static_assert(PLB % 16 == 0, "plane must be a multiple of 16 bytes");
     static_assert(NK % KPAR == 0, "KPAR must divide NK");
-    // shared memory: mbarriers | A1/A2 (double) | tile[NV][W][PL] | p1[WP][PL] | gi | gj | gs
+    // FP64 path: Br/sin(theta) and (v x B)_r/sin(theta) per point, [2][WP][PL]
+    // (the k-derivatives of the curls divide them by the cell's sin(theta),
+    // which its k-neighbours share: formed once per point, not per use)
+    static constexpr int NXS = sizeof(T) == 8 ? 2 : 0;
+    // shared memory: mbarriers | A1/A2 (double) | tile[NV][W][PL] | p1[WP][PL] | xs[NXS][WP][PL] | gi | gj | gs
     static constexpr size_t off_a12 = 16;
     static constexpr size_t off_tile = off_a12 + ((2 * NIP * sizeof(double) + 15) / 16) * 16;
     static constexpr size_t off_p1 = off_tile + (size_t)NV * W * PL * sizeof(T);
-    static constexpr size_t off_gi = off_p1 + (size_t)WP * PL * sizeof(T);
+    static constexpr size_t off_xs = off_p1 + (size_t)WP * PL * sizeof(T);
+    static constexpr size_t off_gi = off_xs + (size_t)NXS * WP * PL * sizeof(T);
     static constexpr size_t off_gj = off_gi + (size_t)GI_COUNT * NIP * sizeof(T);
     static constexpr size_t off_gs = off_gj + (size_t)GJ_COUNT * NJP * sizeof(T);
     static constexpr size_t smem_stage = off_gs + GS_COUNT * sizeof(T);
@@ -425,6 +430,7 @@ __device__ __forceinline__ void stage_body(int b, const T* in, const T* un, T* o
     double* a12 = reinterpret_cast<double*>(smem + S::off_a12);
     T* tile = reinterpret_cast<T*>(smem + S::off_tile);
     T* tp1 = reinterpret_cast<T*>(smem + S::off_p1);
+    T* txs = reinterpret_cast<T*>(smem + S::off_xs);   // FP64: [0] Br/sin, [1] E_r/sin (E = v x B)
     T* gi = reinterpret_cast<T*>(smem + S::off_gi);
     T* gj = reinterpret_cast<T*>(smem + S::off_gj);
     T* gs = reinterpret_cast<T*>(smem + S::off_gs);
@@ -480,6 +486,11 @@ __device__ __forceinline__ void stage_body(int b, const T* in, const T* un, T* o
     const T gor0 = gi[GI_GOR0 * NIP + ii], heat = gi[GI_HEAT * NIP + ii], xi2inv = gi[GI_XI2INV * NIP + ii];
     const double dt = sc->dt;
     const double divs = (double)(5.0f - (float)stage);
+    // x / divs for divs = 4, 2, 1 (stages 1, 3, 4) is x times the exact
+    // reciprocal, the same bits without an FP64 division; stage 2 divides by 3
+    const bool div_pow2 = stage != 2;
+    const double rdivs = 1.0 / divs;
+    auto over_divs = [&](double x) { return div_pow2 ? x * rdivs : x / divs; };
     const float dtk = sc->dt_stage_f[stage - 1];
 
     constexpr int nchunk = NK / KPAR;
@@ -526,6 +537,14 @@ __device__ __forceinline__ void stage_body(int b, const T* in, const T* un, T* o
                 const double r1 = (double)tile[(V_RHO1 * W + slot) * PL + c];
                 const double s1v = (double)tile[(V_S1 * W + slot) * PL + c];
                 tp1[(kp % WP) * PL + c] = (T)(a12[ic] * r1 + a12[NIP + ic] * s1v);
+                const int jc = c / NIP;
+                if (ic >= 2 && ic < NI + 2 && jc >= 2 && jc < NJ + 2) {   // the k-neighbours of interior cells
+                    auto at = [&](int v) { return tile[(v * W + slot) * PL + c]; };
+                    const T sn = gj[GJ_SIN * S::NJP + jc];
+                    txs[(0 * WP + kp % WP) * PL + c] = Pol<T>::dv(at(V_BR), sn, T(0));
+                    txs[(1 * WP + kp % WP) * PL + c] =
+                        Pol<T>::dv(at(V_VT) * at(V_BP) - at(V_VP) * at(V_BT), sn, T(0));
+                }
             } else {
                 const float* f = reinterpret_cast<const float*>(a12);
                 tp1[(kp % WP) * PL + c] = p1_ff(f[ic], f[NIP + ic], f[2 * NIP + ic], f[3 * NIP + ic],
@@ -606,7 +625,11 @@ __device__ __forceinline__ void stage_body(int b, const T* in, const T* un, T* o
         {
             T k1 = D(c2, [&](int m) { return A(V_BP, 0, m, 0) * GSIN[jj + m]; }) -
                    D(c3, [&](int m) { return A(V_BT, 0, 0, m); });
-            T k2 = D(c3, [&](int m) { return Pol<T>::dv(A(V_BR, 0, 0, m), sin_c, sinv); }) -
+            auto brs = [&](int m) -> T {   // Br / sin(theta) at the k-neighbour m
+                if constexpr (Pol<T>::exact) return txs[(0 * WP + sp[m + 2]) * PL + jj * NIP + ii];
+                else return Pol<T>::dv(A(V_BR, 0, 0, m), sin_c, sinv);
+            };
+            T k2 = D(c3, brs) -
                    D(c1, [&](int m) { return A(V_BP, m, 0, 0) * GR[ii + m]; });
             T k3 = D(c1, [&](int m) { return A(V_BT, m, 0, 0) * GR[ii + m]; }) -
                    D(c2, [&](int m) { return A(V_BR, 0, m, 0); });
@@ -632,7 +655,11 @@ __device__ __forceinline__ void stage_body(int b, const T* in, const T* un, T* o
             auto E2 = [&](int a, int bq, int c) { return A(V_VP, a, bq, c) * A(V_BR, a, bq, c) - A(V_VR, a, bq, c) * A(V_BP, a, bq, c); };
             auto E3 = [&](int a, int bq, int c) { return A(V_VR, a, bq, c) * A(V_BT, a, bq, c) - A(V_VT, a, bq, c) * A(V_BR, a, bq, c); };
             T q1 = D(c2, [&](int m) { return E3(0, m, 0) * GSIN[jj + m]; }) - D(c3, [&](int m) { return E2(0, 0, m); });
-            T q2 = D(c3, [&](int m) { return Pol<T>::dv(E1(0, 0, m), sin_c, sinv); }) -
+            auto e1s = [&](int m) -> T {   // E1 / sin(theta) at the k-neighbour m
+                if constexpr (Pol<T>::exact) return txs[(1 * WP + sp[m + 2]) * PL + jj * NIP + ii];
+                else return Pol<T>::dv(E1(0, 0, m), sin_c, sinv);
+            };
+            T q2 = D(c3, e1s) -
                    D(c1, [&](int m) { return E3(m, 0, 0) * GR[ii + m]; });
             T q3 = D(c1, [&](int m) { return E2(m, 0, 0) * GR[ii + m]; }) - D(c2, [&](int m) { return E1(0, m, 0); });
             q1 = q1 * rinv; q2 = q2 * rinv; q3 = q3 * rinv;
@@ -684,7 +711,7 @@ __device__ __forceinline__ void stage_body(int b, const T* in, const T* un, T* o
             const size_t pc = (size_t)b * NCELL + (size_t)kp * PL + jj * NIP + ii;
             const T pn = static_cast<const T*>(psi.un)[pc];
             T po;
-            if constexpr (Pol<T>::exact) po = (T)((double)pn + (dt * (double)Rpsi) / divs);
+            if constexpr (Pol<T>::exact) po = (T)((double)pn + over_divs(dt * (double)Rpsi));
             else po = fmaf((float)dtk, (float)Rpsi, (float)pn);
             static_cast<T*>(psi.out)[pc] = po;
         }
@@ -694,7 +721,7 @@ __device__ __forceinline__ void stage_body(int b, const T* in, const T* un, T* o
         T o[NV];
         if constexpr (Pol<T>::exact) {
 #pragma unroll
-            for (int v = 0; v < NV; ++v) o[v] = (T)((double)u0s[v] + (dt * (double)R[v]) / divs);
+            for (int v = 0; v < NV; ++v) o[v] = (T)((double)u0s[v] + over_divs(dt * (double)R[v]));
         } else if (ulo != nullptr && stage == 4) {
             // u^{n+1} = u^n + dt*R with u^n and u^{n+1} compensated
             int8_t* ql = ulo + (size_t)b * NV * S::NINT + ((size_t)(kp - 2) * NJ + (jj - 2)) * NI + (ii - 2);
