@@ -8,13 +8,20 @@
 // V-cycle stays the fallback. The reference has no learned component.
 //
 // Layout: activations channels-last [n][D][H][W][C] in BF16, C padded to a
-// multiple of 16. 3x3x3 convolutions are
-// implicit GEMMs on mma.sync.m16n8k16 BF16 with FP32 accumulation: M =
-// voxels, N = output channels, K = 27 taps x input channels; the A fragments
-// are gathered straight from the (L2-resident) activation tensor with zero
-// padding at the grid edge, the B fragments from a per-tap weight copy laid
-// out so each fragment register is one 32-bit load. Weights have FP32 master
-// copies updated by Adam; BF16 copies are regenerated after every update.
+// multiple of 16. 3x3x3 convolutions are implicit GEMMs with BF16 operands
+// and FP32 accumulation: M = voxels, N = output channels, K = 27 taps x input
+// channels. Two tensor-core paths (falcon_lcc_set_tensor_path):
+//  - tcgen05 (the default): tcgen05.mma with the accumulator in tensor
+//    memory, one elected thread issuing the MMAs, operands in shared memory;
+//    the forward and backward-data kernels load a halo block once and view it
+//    per tap, weight tiles and weight-gradient bricks arrive by TMA
+//    (k_conv_tc, k_wgrad_tc, below);
+//  - mma.sync.m16n8k16: the A fragments gathered straight from the
+//    (L2-resident) activation tensor with zero padding at the grid edge, the
+//    B fragments from a per-tap weight copy laid out so each fragment
+//    register is one 32-bit load (k_conv, k_conv_wgrad).
+// Weights have FP32 master copies updated by Adam; BF16 copies are
+// regenerated after every update.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
