@@ -415,6 +415,50 @@ __device__ __forceinline__ void cell_of_thread(int tid, int& i, int& j, int& kq)
 }
 
 // ---------------------------------------------------------------------------
+// Packed FP32 pairs (Blackwell's two-lane FFMA2/FADD2/FMUL2): the diffusion
+// march runs its slopes, fluxes and update on variables v and v+1 at once,
+// the stage its stage-4 update. Each helper gives bit for bit what its scalar counterpart gives (a
+// difference a - b is formed as fma(b, -1, a), one rounding of the exact
+// difference, as FADD does).
+__device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
+__device__ __forceinline__ float2 f2(float x) { return make_float2(x, x); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.f), a); }
+__device__ __forceinline__ float2 max02(float2 a) { return f2(fmaxf(0.f, a.x), fmaxf(0.f, a.y)); }
+// minmod_sel for two variables
+__device__ __forceinline__ float2 minmod_sel2(float2 ul, float2 u, float2 ur) {
+    const float2 a = __fmul2_rn(sub2(ur, ul), f2(0.5f));
+    const float2 b = __fmul2_rn(sub2(ur, u), f2(2.f));
+    const float2 c = __fmul2_rn(sub2(u, ul), f2(2.f));
+    const float2 x = __fmul2_rn(__fmul2_rn(max02(__fmul2_rn(a, b)), f2(1.e10f)), max02(__fmul2_rn(b, c)));
+    const float mx = fminf(fminf(fabsf(a.x), fabsf(b.x)), fabsf(c.x));
+    const float my = fminf(fminf(fabsf(a.y), fabsf(b.y)), fabsf(c.y));
+    return f2(x.x >= 1.e-30f ? copysignf(mx, a.x) : 0.f, x.y >= 1.e-30f ? copysignf(my, a.y) : 0.f);
+}
+// face_flux_s<float> for two variables; cc = -0.25 (cR + cL), the face's
+// speed factor (the same for every variable; -0.25 scales exactly, so
+// (phi num) cc is the scalar form's ((-0.25 phi) num)(cR + cL) bit for bit)
+__device__ __forceinline__ float2 face_flux2(float2 fl, float2 fr, float2 dL, float2 dR, float2 cc) {
+    const float2 num = __ffma2_rn(dL, f2(-0.5f), sub2(__ffma2_rn(dR, f2(-0.5f), fr), fl));
+    const float2 den = sub2(fr, fl);
+    const float2 r = __ffma2_rn(f2(__fdividef(num.x, den.x), __fdividef(num.y, den.y)), f2(2.f), f2(-1.f));
+    return __fmul2_rn(__fmul2_rn(max02(r), num), cc);
+}
+// ff_add for two variables
+__device__ __forceinline__ float2 ff_add2(float2 hi, int8_t q0, int8_t q1, float2 d, int8_t& o0, int8_t& o1) {
+    const float2 l = __fmul2_rn(f2(lo_decode(q0), lo_decode(q1)), f2(lo_unit(hi.x), lo_unit(hi.y)));
+    const float2 s = __fadd2_rn(hi, d);
+    const float2 bs = sub2(s, hi);
+    const float2 es = __fadd2_rn(sub2(hi, sub2(s, bs)), sub2(d, bs));
+    const float2 t = __fadd2_rn(es, l);
+    const float2 h = __fadd2_rn(s, t);
+    const float2 bh = sub2(h, s);
+    const float2 r = __fadd2_rn(sub2(s, sub2(h, bh)), sub2(t, bh));
+    o0 = lo_encode(h.x, r.x);
+    o1 = lo_encode(h.y, r.y);
+    return h;
+}
+
+// ---------------------------------------------------------------------------
 // One RK stage of one block: boundary -> RHS (3_6/ModEquation.f90:24-162) ->
 // u_out = u^n + dt*R/(5-s) (3_6/ModAdvance.f90:87-93).
 // The body runs block b with the CTA's threads (NI*NJ*KPAR of them): k_stage
@@ -729,10 +773,14 @@ __device__ __forceinline__ void stage_body(int b, const T* in, const T* un, T* o
 #pragma unroll
             for (int v = 0; v < NV; ++v) q0[v] = ql[(size_t)v * S::NINT];
 #pragma unroll
-            for (int v = 0; v < NV; ++v) {
-                int8_t q1;
-                o[v] = ff_add((float)u0s[v], q0[v], __fmul_rn(dtk, (float)R[v]), q1);
-                ql[(size_t)v * S::NINT] = q1;
+            for (int v = 0; v < NV; v += 2) {   // pairs of variables: ff_add2 gives ff_add's bits
+                int8_t qa, qb;
+                const float2 ov = ff_add2(f2((float)u0s[v], (float)u0s[v + 1]), q0[v], q0[v + 1],
+                                          __fmul2_rn(f2(dtk), f2((float)R[v], (float)R[v + 1])), qa, qb);
+                o[v] = ov.x;
+                o[v + 1] = ov.y;
+                ql[(size_t)v * S::NINT] = qa;
+                ql[(size_t)(v + 1) * S::NINT] = qb;
             }
         } else {
 #pragma unroll
@@ -1089,50 +1137,6 @@ k_diffusion(const T* u, T* out, int8_t* ulo, PushTable push, Geometry g, StepSca
     if constexpr (!Pol<T>::exact) {
         if (cfl_next) cfl_commit(cmin, cnan, sc);
     }
-}
-
-// ---------------------------------------------------------------------------
-// Packed FP32 pairs (Blackwell's two-lane FFMA2/FADD2/FMUL2): the diffusion
-// march below runs its slopes, fluxes and update on variables v and v+1 at
-// once. Each helper gives bit for bit what its scalar counterpart gives (a
-// difference a - b is formed as fma(b, -1, a), one rounding of the exact
-// difference, as FADD does).
-__device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
-__device__ __forceinline__ float2 f2(float x) { return make_float2(x, x); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.f), a); }
-__device__ __forceinline__ float2 max02(float2 a) { return f2(fmaxf(0.f, a.x), fmaxf(0.f, a.y)); }
-// minmod_sel for two variables
-__device__ __forceinline__ float2 minmod_sel2(float2 ul, float2 u, float2 ur) {
-    const float2 a = __fmul2_rn(sub2(ur, ul), f2(0.5f));
-    const float2 b = __fmul2_rn(sub2(ur, u), f2(2.f));
-    const float2 c = __fmul2_rn(sub2(u, ul), f2(2.f));
-    const float2 x = __fmul2_rn(__fmul2_rn(max02(__fmul2_rn(a, b)), f2(1.e10f)), max02(__fmul2_rn(b, c)));
-    const float mx = fminf(fminf(fabsf(a.x), fabsf(b.x)), fabsf(c.x));
-    const float my = fminf(fminf(fabsf(a.y), fabsf(b.y)), fabsf(c.y));
-    return f2(x.x >= 1.e-30f ? copysignf(mx, a.x) : 0.f, x.y >= 1.e-30f ? copysignf(my, a.y) : 0.f);
-}
-// face_flux_s<float> for two variables; cc = -0.25 (cR + cL), the face's
-// speed factor (the same for every variable; -0.25 scales exactly, so
-// (phi num) cc is the scalar form's ((-0.25 phi) num)(cR + cL) bit for bit)
-__device__ __forceinline__ float2 face_flux2(float2 fl, float2 fr, float2 dL, float2 dR, float2 cc) {
-    const float2 num = __ffma2_rn(dL, f2(-0.5f), sub2(__ffma2_rn(dR, f2(-0.5f), fr), fl));
-    const float2 den = sub2(fr, fl);
-    const float2 r = __ffma2_rn(f2(__fdividef(num.x, den.x), __fdividef(num.y, den.y)), f2(2.f), f2(-1.f));
-    return __fmul2_rn(__fmul2_rn(max02(r), num), cc);
-}
-// ff_add for two variables
-__device__ __forceinline__ float2 ff_add2(float2 hi, int8_t q0, int8_t q1, float2 d, int8_t& o0, int8_t& o1) {
-    const float2 l = __fmul2_rn(f2(lo_decode(q0), lo_decode(q1)), f2(lo_unit(hi.x), lo_unit(hi.y)));
-    const float2 s = __fadd2_rn(hi, d);
-    const float2 bs = sub2(s, hi);
-    const float2 es = __fadd2_rn(sub2(hi, sub2(s, bs)), sub2(d, bs));
-    const float2 t = __fadd2_rn(es, l);
-    const float2 h = __fadd2_rn(s, t);
-    const float2 bh = sub2(h, s);
-    const float2 r = __fadd2_rn(sub2(s, sub2(h, bh)), sub2(t, bh));
-    o0 = lo_encode(h.x, r.x);
-    o1 = lo_encode(h.y, r.y);
-    return h;
 }
 
 // ---------------------------------------------------------------------------
