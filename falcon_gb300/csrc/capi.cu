@@ -322,15 +322,19 @@ int autotune(falcon_ctx* ctx) {
     int cand[8];
     const int n = ctx->mixed() ? kpar_candidates_mixed(ctx->dims, cand) : kpar_candidates_fp64(ctx->dims, cand);
     if (n == 0) return ctx->fail(FALCON_ERR_INVALID_ARG, "no kernel instantiation for this block size");
-    float best_s = 1e30f, best_d = 1e30f;
-    int ks = cand[0], kd = cand[0];
+    // the candidates take turns within each round of launches, so that a drift
+    // of the clocks over the tuning touches every candidate alike; the first
+    // round pays for set-up and is not counted
+    constexpr int kRounds = 5;
+    float tot[8][2] = {};
+    bool ok[8][2];
+    for (int q = 0; q < n; ++q) ok[q][0] = ok[q][1] = true;
     cudaEvent_t a = ctx->ev(), b = ctx->ev();
-    for (int q = 0; q < n; ++q) {
-        const int kp = cand[q];
-        for (int which = 0; which < 2; ++which) {
-            float tot = 0.f;
-            bool ok = true;
-            for (int rep = 0; rep < 4 && ok; ++rep) {
+    for (int rep = 0; rep < kRounds; ++rep)
+        for (int q = 0; q < n; ++q)
+            for (int which = 0; which < 2; ++which) {
+                if (!ok[q][which]) continue;
+                const int kp = cand[q];
                 cudaEventRecord(a, ctx->st);
                 cudaError_t e;
                 if (which == 0)
@@ -345,15 +349,16 @@ int autotune(falcon_ctx* ctx) {
                                                               (float*)ctx->RK, nullptr, PushTable{}, ctx->sc, kp, ctx->st)
                                      : launch_diffusion_fp64(ctx->dims, ctx->geom(), (double*)ctx->RK, ctx->sc, kp, ctx->st);
                 cudaEventRecord(b, ctx->st);
-                if (e != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess) { ok = false; cudaGetLastError(); break; }
+                if (e != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess) { ok[q][which] = false; cudaGetLastError(); continue; }
                 float ms = 0.f;
                 cudaEventElapsedTime(&ms, a, b);
-                if (rep > 0) tot += ms;   // the first launch pays for set-up
+                if (rep > 0) tot[q][which] += ms;
             }
-            if (!ok) continue;
-            if (which == 0 && tot < best_s) { best_s = tot; ks = kp; }
-            if (which == 1 && tot < best_d) { best_d = tot; kd = kp; }
-        }
+    float best_s = 1e30f, best_d = 1e30f;
+    int ks = cand[0], kd = cand[0];
+    for (int q = 0; q < n; ++q) {
+        if (ok[q][0] && tot[q][0] < best_s) { best_s = tot[q][0]; ks = cand[q]; }
+        if (ok[q][1] && tot[q][1] < best_d) { best_d = tot[q][1]; kd = cand[q]; }
     }
     ctx->pool.push_back(a);
     ctx->pool.push_back(b);

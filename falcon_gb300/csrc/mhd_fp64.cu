@@ -220,62 +220,73 @@ bool wide_ok(const void* p, int64_t ncell) { return ((uintptr_t)p % 16) == 0 && 
 // Core transfers: of every block and variable of the host array (9 per block,
 // psi last), the interior planes and within them the interior rows, each
 // row whole (its radial ghost columns, which hold the radial boundary
-// condition, included). Element x of the core enumerates (block, var, plane,
-// offset in the plane's run of rows); runs are NJ*NIP long and even, so the
-// pairs of the wide loop never straddle a run.
-struct CoreIdx {
-    int64_t host, cell, b;   // host element, cell offset in the block, block
-    int v;                   // 0..NV-1 state, NV psi
-    bool interior;           // not a radial ghost column
+// condition, included). The interior rows of one plane are one contiguous
+// run of (NJP-4)*NIP host elements: a warp moves one run at a time, block,
+// variable and plane from the run number, the cell from the offset in the
+// run, so no element pays a 64-bit division; each lane's 16-byte host
+// accesses of a pass (kRunVec, a whole 16^3 run of 320 elements) are issued
+// before any is used. Offsets are even and NIP is even, so a pair (ip, ip+1)
+// is either two radial ghost columns or two interior cells, and its device
+// side is one 8-byte (FP32) or 16-byte (FP64) access and one 2-byte access
+// of the correction.
+constexpr int kRunVec = 5;
+struct CoreRun {
+    int64_t host;   // host element of the run's first cell
+    int64_t dev;    // state element of that cell ((b NV + v) ncell + cell0), v < NV
+    int64_t psi;    // psi element of that cell (b ncell + cell0)
+    int64_t lo0;    // correction element of the run's first interior row
+    int v;          // 0..NV-1 state, NV psi
 };
-__device__ __forceinline__ CoreIdx core_index(int64_t x, const StepDims& dm) {
-    const int64_t run = (int64_t)(dm.njp - 4) * dm.nip, per = (int64_t)(dm.nkp - 4) * run;
-    const int64_t bv = x / per, r = x - bv * per;
-    const int64_t kp = 2 + r / run, o = r % run;
-    CoreIdx c;
-    c.b = bv / (NV + 1);
-    c.v = (int)(bv - c.b * (NV + 1));
-    c.cell = kp * dm.nip * dm.njp + 2 * dm.nip + o;
-    c.host = bv * dm.ncell + c.cell;
-    const int ip = (int)(o % dm.nip);
-    c.interior = ip >= 2 && ip < dm.nip - 2;
+__device__ __forceinline__ CoreRun core_run(int64_t r, const StepDims& dm) {
+    const int nkc = dm.nkp - 4;
+    const int64_t bv = r / nkc, b = bv / (NV + 1);
+    const int kp = 2 + (int)(r - bv * nkc);
+    const int64_t cell0 = (int64_t)kp * dm.nip * dm.njp + 2 * dm.nip;
+    CoreRun c;
+    c.v = (int)(bv - b * (NV + 1));
+    c.host = bv * dm.ncell + cell0;
+    c.dev = (b * NV + c.v) * dm.ncell + cell0;
+    c.psi = b * dm.ncell + cell0;
+    c.lo0 = ((b * NV + c.v) * dm.nk + (kp - 2)) * (int64_t)dm.nj * dm.ni;
     return c;
 }
 // host core -> device: state cells narrowed (FP32 with its correction) or
 // copied (FP64); psi converted into P, or, without P, tested for 0 (flag)
 template <class T>
-__global__ void k_core_up(const double* s, T* U, int8_t* lo, T* P, int32_t* flag, int64_t n, StepDims dm) {
-    const int64_t lane2 = 2 * (threadIdx.x & 31);
+__global__ void k_core_up(const double* s, T* U, int8_t* lo, T* P, int32_t* flag, int64_t nruns, StepDims dm) {
+    const int lane2 = 2 * (threadIdx.x & 31), len = (dm.njp - 4) * dm.nip;
     int any = 0;
-    for (int64_t w0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32 * kWide; w0 < n;
-         w0 += (((int64_t)gridDim.x * blockDim.x) >> 5) * 32 * kWide) {
-        double2 v[kWide / 2];
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < nruns;
+         r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+        const CoreRun c = core_run(r, dm);
+        for (int o0 = 0; o0 < len; o0 += 64 * kRunVec) {
+            double2 v[kRunVec];
 #pragma unroll
-        for (int q = 0; q < kWide / 2; ++q)
-            if (w0 + 64 * q + lane2 < n)
-                v[q] = *reinterpret_cast<const double2*>(s + core_index(w0 + 64 * q + lane2, dm).host);
+            for (int q = 0; q < kRunVec; ++q)
+                if (o0 + 64 * q + lane2 < len) v[q] = *reinterpret_cast<const double2*>(s + c.host + o0 + 64 * q + lane2);
 #pragma unroll
-        for (int q = 0; q < kWide / 2; ++q) {
-            if (w0 + 64 * q + lane2 >= n) continue;
-            const CoreIdx c = core_index(w0 + 64 * q + lane2, dm);
-            const double u2[2] = {v[q].x, v[q].y};
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int64_t cell = c.cell + h;
-                const bool in = h == 0 ? c.interior : (int)((cell % dm.nip)) >= 2 && (int)(cell % dm.nip) < dm.nip - 2;
+            for (int q = 0; q < kRunVec; ++q) {
+                const int o = o0 + 64 * q + lane2;
+                if (o >= len) continue;
                 if (c.v < NV) {
-                    const int64_t e = (c.b * NV + c.v) * dm.ncell + cell;
                     if constexpr (sizeof(T) == 4) {
-                        const float hi = (float)u2[h];
-                        U[e] = hi;
-                        if (lo && in) lo[lo_index(e, dm)] = lo_encode64(hi, u2[h] - (double)hi);
+                        const float h0 = (float)v[q].x, h1 = (float)v[q].y;
+                        *reinterpret_cast<float2*>(U + c.dev + o) = make_float2(h0, h1);
+                        const int jr = o / dm.nip, ip = o - jr * dm.nip;
+                        if (lo && ip >= 2 && ip < dm.nip - 2) {
+                            char2 q2;
+                            q2.x = lo_encode64(h0, v[q].x - (double)h0);
+                            q2.y = lo_encode64(h1, v[q].y - (double)h1);
+                            *reinterpret_cast<char2*>(lo + c.lo0 + jr * dm.ni + (ip - 2)) = q2;
+                        }
                     } else {
-                        U[e] = (T)u2[h];
+                        *reinterpret_cast<double2*>(U + c.dev + o) = v[q];
                     }
                 } else if (P) {
-                    P[c.b * dm.ncell + cell] = (T)u2[h];
+                    if constexpr (sizeof(T) == 4) *reinterpret_cast<float2*>(P + c.psi + o) = make_float2((float)v[q].x, (float)v[q].y);
+                    else *reinterpret_cast<double2*>(P + c.psi + o) = v[q];
                 } else {
-                    any |= u2[h] != 0.0;
+                    any |= (v[q].x != 0.0) | (v[q].y != 0.0);
                 }
             }
         }
@@ -284,46 +295,50 @@ __global__ void k_core_up(const double* s, T* U, int8_t* lo, T* P, int32_t* flag
 }
 // device -> host core (psi 0 without P)
 template <class T>
-__global__ void k_core_down(const T* U, const int8_t* lo, const T* P, double* out, int64_t n, StepDims dm) {
-    const int64_t lane2 = 2 * (threadIdx.x & 31);
-    for (int64_t w0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32 * kWide; w0 < n;
-         w0 += (((int64_t)gridDim.x * blockDim.x) >> 5) * 32 * kWide) {
-        double2 v[kWide / 2];
-        int64_t hs[kWide / 2];
+__global__ void k_core_down(const T* U, const int8_t* lo, const T* P, double* out, int64_t nruns, StepDims dm) {
+    const int lane2 = 2 * (threadIdx.x & 31), len = (dm.njp - 4) * dm.nip;
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < nruns;
+         r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+        const CoreRun c = core_run(r, dm);
+        for (int o0 = 0; o0 < len; o0 += 64 * kRunVec) {
+            double2 v[kRunVec];
 #pragma unroll
-        for (int q = 0; q < kWide / 2; ++q) {
-            if (w0 + 64 * q + lane2 >= n) continue;
-            const CoreIdx c = core_index(w0 + 64 * q + lane2, dm);
-            hs[q] = c.host;
-            double u2[2];
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int64_t cell = c.cell + h;
+            for (int q = 0; q < kRunVec; ++q) {
+                const int o = o0 + 64 * q + lane2;
+                if (o >= len) continue;
                 if (c.v < NV) {
-                    const int64_t e = (c.b * NV + c.v) * dm.ncell + cell;
-                    const T hi = U[e];
-                    double x = (double)hi;
                     if constexpr (sizeof(T) == 4) {
-                        const int64_t q = lo ? lo_index(e, dm) : -1;
-                        if (q >= 0) x += (double)lo[q] * (double)lo_unit((float)hi);
+                        const float2 h = *reinterpret_cast<const float2*>(U + c.dev + o);
+                        v[q] = make_double2((double)h.x, (double)h.y);
+                        const int jr = o / dm.nip, ip = o - jr * dm.nip;
+                        if (lo && ip >= 2 && ip < dm.nip - 2) {
+                            const char2 q2 = *reinterpret_cast<const char2*>(lo + c.lo0 + jr * dm.ni + (ip - 2));
+                            v[q].x += (double)q2.x * (double)lo_unit(h.x);
+                            v[q].y += (double)q2.y * (double)lo_unit(h.y);
+                        }
+                    } else {
+                        v[q] = *reinterpret_cast<const double2*>(U + c.dev + o);
                     }
-                    u2[h] = x;
+                } else if (P) {
+                    if constexpr (sizeof(T) == 4) {
+                        const float2 h = *reinterpret_cast<const float2*>(P + c.psi + o);
+                        v[q] = make_double2((double)h.x, (double)h.y);
+                    } else {
+                        v[q] = *reinterpret_cast<const double2*>(P + c.psi + o);
+                    }
                 } else {
-                    u2[h] = P ? (double)P[c.b * dm.ncell + cell] : 0.0;
+                    v[q] = make_double2(0.0, 0.0);
                 }
             }
-            v[q] = make_double2(u2[0], u2[1]);
-        }
 #pragma unroll
-        for (int q = 0; q < kWide / 2; ++q)
-            if (w0 + 64 * q + lane2 < n) *reinterpret_cast<double2*>(out + hs[q]) = v[q];
+            for (int q = 0; q < kRunVec; ++q)
+                if (o0 + 64 * q + lane2 < len) *reinterpret_cast<double2*>(out + c.host + o0 + 64 * q + lane2) = v[q];
+        }
     }
 }
-int64_t core_elems(const StepDims& dm) {
-    return (int64_t)dm.nblocks * (NV + 1) * (dm.nkp - 4) * (dm.njp - 4) * dm.nip;
-}
+int64_t core_runs(const StepDims& dm) { return (int64_t)dm.nblocks * (NV + 1) * (dm.nkp - 4); }
 bool core_ok(const void* host, const StepDims& dm) {
-    return ((uintptr_t)host % 16) == 0 && dm.ncell % 2 == 0 && dm.nip % 2 == 0 && ((dm.njp - 4) * dm.nip) % 2 == 0;
+    return ((uintptr_t)host % 16) == 0 && dm.ncell % 2 == 0 && dm.nip % 2 == 0;
 }
 
 cudaError_t launch_convert_state(const double* src, float* dst, int8_t* lo, int64_t n, const StepDims& dm,
@@ -366,7 +381,7 @@ cudaError_t launch_gather_host(const void* U, const int8_t* lo, const void* psi,
 cudaError_t launch_core_up(const double* host, void* U, int8_t* lo, void* P, int32_t* flag, bool fp32, const StepDims& dm,
                            cudaStream_t st) {
     if (!core_ok(host, dm)) return cudaErrorInvalidValue;
-    const int64_t n = core_elems(dm);
+    const int64_t n = core_runs(dm);
     if (flag) {
         cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int32_t), st);
         if (e != cudaSuccess) return e;
@@ -378,7 +393,7 @@ cudaError_t launch_core_up(const double* host, void* U, int8_t* lo, void* P, int
 cudaError_t launch_core_down(const void* U, const int8_t* lo, const void* P, bool fp32, double* host, const StepDims& dm,
                              cudaStream_t st) {
     if (!core_ok(host, dm)) return cudaErrorInvalidValue;
-    const int64_t n = core_elems(dm);
+    const int64_t n = core_runs(dm);
     if (fp32) k_core_down<float><<<1216, 256, 0, st>>>((const float*)U, lo, (const float*)P, host, n, dm);
     else k_core_down<double><<<1216, 256, 0, st>>>((const double*)U, nullptr, (const double*)P, host, n, dm);
     return cudaGetLastError();
