@@ -385,7 +385,7 @@ def run_ours(args, rank, world, local, dist):
     nbytes = full_bytes = 0
     k_e2e = max(1, min(args.steps, 10))
     if not args.no_e2e:
-        host = np.empty(f.shape, dtype=np.float64)
+        host = fg.host_array(f.shape)   # 4096-byte aligned: whole 64-byte lines over the host link
         f.pin_host(host)
         f.download_state_into(host)
         f.synchronize()
@@ -433,8 +433,8 @@ def run_ours(args, rank, world, local, dist):
             "tuning": f.tuning(), "ghost_lists": lists, "stage_exchange": f.exchange_stats(),
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
-                    "mode": "core of the FP64 state (interior planes x interior rows, pinned) uploaded and "
-                            "downloaded every step; theta/phi ghost layers recomputed on the device"},
+                    "mode": "core of the FP64 state (interior planes x interior rows, pinned, 4096-byte aligned) "
+                            "uploaded and downloaded every step; theta/phi ghost layers recomputed on the device"},
             "e2e_full_array": {"value": full_val, "unit": UNIT, "h2d_bytes_per_step": full_bytes,
                                "d2h_bytes_per_step": full_bytes,
                                "mode": "whole padded FP64 state (pinned) uploaded and downloaded every step"},

@@ -37,6 +37,21 @@ SHARD_RECV = 1
 STEP_GRAPH = 0        # falcon_set_step_mode: one captured graph per step
 STEP_PERSISTENT = 1   # one persistent cooperative launch per step
 
+def host_array(shape, dtype=np.float64, align=4096):
+    """An uninitialised host array whose first element sits on an `align`-byte
+    boundary. The core transfers (Falcon.upload_state_core/download_state_core)
+    move runs of whole rows that start 64-byte aligned when the array does; a
+    run that starts inside a 64-byte line leaves partial lines at both of its
+    ends, which the host link writes back at a lower rate (the core download of
+    the 21M-cell shell: 188 GB/s aligned, 175 GB/s at the 16-mod-64 address that
+    a large malloc returns)."""
+    n = int(np.prod(shape))
+    item = np.dtype(dtype).itemsize
+    raw = np.empty(n * item + align, dtype=np.uint8)
+    off = (-raw.ctypes.data) % align
+    return raw[off:off + n * item].view(dtype).reshape(shape)
+
+
 # every symbol declared in include/falcon_gb300.h
 EXPORTS = (
     "falcon_create", "falcon_destroy", "falcon_last_error", "falcon_num_blocks", "falcon_block_ranges",

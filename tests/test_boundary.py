@@ -237,3 +237,15 @@ def test_pfss_solution_is_linear_in_the_driver_magnetogram():
     x3 = sv.solution()
     assert rep["converged"] == 1
     assert np.abs(x3 + 3.0 * x1).max() <= 1e-8 * np.abs(x3).max()
+
+
+@pytest.mark.parametrize("shape,dtype", [((5, 9, 20, 20, 20), np.float64), ((7,), np.float32), ((3, 1), np.int8)])
+def test_host_array_is_aligned_contiguous_and_writable(shape, dtype):
+    """fg.host_array gives the driver-side state array at a 4096-byte
+    boundary (whole 64-byte lines for every core run), C-contiguous, of the
+    requested shape and type."""
+    a = fg.host_array(shape, dtype)
+    assert a.ctypes.data % 4096 == 0
+    assert a.shape == shape and a.dtype == np.dtype(dtype) and a.flags["C_CONTIGUOUS"]
+    a[...] = 1
+    assert int(a.sum()) == int(np.prod(shape))
