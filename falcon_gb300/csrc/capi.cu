@@ -55,6 +55,7 @@ struct falcon_ctx {
     GhostLists gl_stage{};    // face ghosts not pushed by the stage kernel (exchanges after stages)
     GhostLists gl_final{};    // mixed: ghost entries the exchange ending a step fills (see setup_device)
     bool stale_edges = false; // mixed: edge/corner ghosts not refreshed since the last step
+    bool rk_pending = false;  // the stage buffer is due a copy of the state (settle_stage_buffer)
     bool cfl_ready = false;   // mixed: the last diffusion pass formed this state's CFL minimum
     PushTable push{};         // mixed path: faces the stage kernel writes into its output
     void* R2 = nullptr;       // mixed path: second stage buffer (pushing needs out != in)
@@ -308,6 +309,30 @@ cudaError_t clear_step_flags(falcon_ctx* ctx) {
     return e;
 }
 
+// The state or its background changed outside the fused step (upload,
+// synthetic initial condition, restart, new background, phases): the CFL
+// minimum that the last diffusion pass left pending belongs to the state it
+// wrote, so it is dropped; the next minimum is formed from +inf.
+cudaError_t drop_pending_cfl(falcon_ctx* ctx) {
+    static const unsigned long long inf_bits = 0x7FF0000000000000ull;
+    ctx->cfl_ready = false;
+    return cudaMemcpyAsync(&ctx->sc->min_ratio_bits, &inf_bits, sizeof inf_bits, cudaMemcpyHostToDevice, ctx->st);
+}
+
+// The stage buffer starts as a copy of the state (primitive_rk_IV =
+// primitive_IV, as the reference's initialisation leaves it). The core upload
+// defers that copy: a step's first stage rewrites the buffer before anything
+// reads it, so the copy is made only when the buffer is read as it stands
+// (the phases, falcon_download_stage_state).
+cudaError_t settle_stage_buffer(falcon_ctx* ctx) {
+    if (!ctx->rk_pending) return cudaSuccess;
+    cudaError_t e = fresh_state(ctx);   // with its ghost cells complete, as an upload leaves it
+    if (e != cudaSuccess) return e;
+    ctx->rk_pending = false;
+    return cudaMemcpyAsync(ctx->RK, ctx->U, (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell * ctx->elem,
+                           cudaMemcpyDeviceToDevice, ctx->st);
+}
+
 cudaError_t mirror_state(falcon_ctx* ctx) {
     if (!ctx->R2) return cudaSuccess;
     return cudaMemcpyAsync(ctx->R2, ctx->U, (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell * ctx->elem,
@@ -370,6 +395,7 @@ int autotune(falcon_ctx* ctx) {
     CK(cudaMemsetAsync(&ctx->sc->nan_flag, 0, sizeof(int32_t), ctx->st), "autotune");
     const size_t nelem = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
     CK(cudaMemcpyAsync(ctx->RK, ctx->U, nelem * ctx->elem, cudaMemcpyDeviceToDevice, ctx->st), "autotune");
+    ctx->rk_pending = false;
     CK(cudaStreamSynchronize(ctx->st), "autotune");
     return FALCON_OK;
 }
@@ -953,7 +979,8 @@ int falcon_set_background(falcon_ctx* ctx, const double* p) {
     cudaSetDevice(ctx->device);
     const int rc = upload_tables(ctx, false);
     if (rc) return rc;
-    ctx->cfl_ready = false;   // the wave speed changed with the background
+    CK(drop_pending_cfl(ctx), "background");   // the wave speed changed with the background
+    CK(cudaStreamSynchronize(ctx->st), "background");
     return FALCON_OK;
 }
 
@@ -1071,11 +1098,12 @@ int falcon_upload_state(falcon_ctx* ctx, const double* u) {
     rc = put_state(ctx, u, ctx->U, ctx->Ulo, ctx->P);
     if (rc) return rc;
     ctx->stale_edges = false;   // the uploaded ghost cells are the state's
-    ctx->cfl_ready = false;
+    CK(drop_pending_cfl(ctx), "upload");
     CK(clear_step_flags(ctx), "upload");
     // primitive_rk_IV = primitive_IV, as the reference's initialisation leaves it
     const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
     CK(cudaMemcpyAsync(ctx->RK, ctx->U, n * ctx->elem, cudaMemcpyDeviceToDevice, ctx->st), "upload");
+    ctx->rk_pending = false;
     CK(mirror_state(ctx), "upload");
     // psi's stage array and the scratch it is copied from start equal too:
     // their ghost cells that no exchange writes (the radial boundary planes)
@@ -1147,16 +1175,23 @@ int falcon_upload_state_core(falcon_ctx* ctx, const double* u) {
     CK(cudaStreamSynchronize(ctx->st), "upload core");
     if (bad) {
         CK(mirror_state(ctx), "upload core");
+        ctx->rk_pending = true;   // the stage buffer held the corrections
         CK(cudaStreamSynchronize(ctx->st), "upload core");
         return ctx->fail(FALCON_ERR_INVALID_ARG, "psi must be 0 unless divb_option = 1");
     }
     std::swap(ctx->U, ctx->R2);
     CK(cudaMemcpyAsync(ctx->Ulo, lo_tmp, lo_elems(ctx->dims), cudaMemcpyDeviceToDevice, ctx->st), "upload core");
-    CK(ghost(ctx, ctx->U), "upload core");
-    ctx->stale_edges = false;
-    ctx->cfl_ready = false;
     CK(clear_step_flags(ctx), "upload core");
-    CK(cudaMemcpyAsync(ctx->RK, ctx->U, n * ctx->elem, cudaMemcpyDeviceToDevice, ctx->st), "upload core");
+    CK(drop_pending_cfl(ctx), "upload core");
+    // what the diffusion pass closing a step leaves besides u^{n+1}: the
+    // regular faces pushed, the other face entries filled (the final
+    // exchange) and the next step's CFL minimum formed; edge and corner
+    // ghosts are completed before the state is read (fresh_state)
+    CK(launch_push_state_mixed(ctx->dims, ctx->geom(), (float*)ctx->U, ctx->push, ctx->sc, ctx->st), "upload core");
+    CK(launch_ghost_mixed(ctx->dims, ctx->gl_final, (float*)ctx->U, ctx->st), "upload core");
+    ctx->stale_edges = true;
+    ctx->cfl_ready = true;
+    ctx->rk_pending = true;
     CK(mirror_state(ctx), "upload core");
     if (ctx->P) {
         const size_t np = (size_t)ctx->dims.nblocks * ctx->dims.ncell * ctx->elem;
@@ -1212,9 +1247,10 @@ int falcon_init_synthetic(falcon_ctx* ctx, int32_t kind, uint64_t seed, double m
     if (ctx->Ulo) CK(cudaMemsetAsync(ctx->Ulo, 0, lo_elems(ctx->dims), ctx->st), "init");
     const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
     CK(cudaMemcpyAsync(ctx->RK, ctx->U, n * ctx->elem, cudaMemcpyDeviceToDevice, ctx->st), "init");
+    ctx->rk_pending = false;
     CK(mirror_state(ctx), "init");
     ctx->stale_edges = false;
-    ctx->cfl_ready = false;
+    CK(drop_pending_cfl(ctx), "init");
     CK(clear_step_flags(ctx), "init");
     CK(cudaStreamSynchronize(ctx->st), "init");
     return FALCON_OK;
@@ -1255,6 +1291,7 @@ int falcon_timestep(falcon_ctx* ctx, double* dt_out) {
 static int run(falcon_ctx* ctx, int32_t n) {
     int rc = autotune(ctx);
     if (rc) return rc;
+    if (n > 0) ctx->rk_pending = false;   // the first stage rewrites the stage buffer
     if (ctx->ktiming) {
         for (int32_t s = 0; s < n; ++s) {
             CK(enqueue_step(ctx), "step");
@@ -1360,7 +1397,8 @@ int falcon_step_phase(falcon_ctx* ctx, int32_t phase) {
     rc = autotune(ctx);
     if (rc) return rc;
     if (ctx->shard.on) return shard_phase(ctx, phase);
-    ctx->cfl_ready = false;   // the phases change the state outside the fused step
+    CK(settle_stage_buffer(ctx), "phase");
+    CK(drop_pending_cfl(ctx), "phase");   // the phases change the state outside the fused step
     cudaError_t e = cudaSuccess;
     if (phase == 0) {
         e = cfl(ctx);
@@ -1388,6 +1426,7 @@ int falcon_download_stage_state(falcon_ctx* ctx, double* u) {
     int rc = need_device(ctx);
     if (rc) return rc;
     if (!u) return ctx->fail(FALCON_ERR_INVALID_ARG, "null state");
+    CK(settle_stage_buffer(ctx), "stage state");
     return get_state(ctx, ctx->RK, nullptr, ctx->Prk, u);
 }
 
@@ -1633,9 +1672,10 @@ int falcon_load_restart(falcon_ctx* ctx, const char* path) {
     if (!ok) return ctx->fail(FALCON_ERR_INVALID_ARG, std::string("restart ") + path + ": short read");
     // the stage arrays start equal to the state, as after falcon_upload_state
     CK(cudaMemcpyAsync(ctx->RK, ctx->U, h.bytes_state, cudaMemcpyDeviceToDevice, ctx->st), "restart");
+    ctx->rk_pending = false;
     CK(mirror_state(ctx), "restart");
     ctx->stale_edges = false;
-    ctx->cfl_ready = false;
+    CK(drop_pending_cfl(ctx), "restart");
     CK(clear_step_flags(ctx), "restart");
     if (ctx->P)
         for (void* q : {ctx->Prk, ctx->P2})

@@ -234,6 +234,10 @@ cudaError_t launch_psi_ghost_mixed(const StepDims& d, const GhostLists& gl, floa
 // (after the CFL minimum of u^n is formed): dt, four stages with their face
 // exchanges, diffusion into R2, the final exchange. bar: 8 device words
 // (reset here): grid-barrier counter and generation, the 5 block tickets.
+// the regular faces of a mixed state pushed and its CFL minimum formed, as the
+// diffusion pass closing a step leaves them (after a core upload)
+cudaError_t launch_push_state_mixed(const StepDims& d, const Geometry& g, float* u, const PushTable& push,
+                                    StepScalars* sc, cudaStream_t st);
 cudaError_t launch_step_persistent_mixed(const StepDims& d, const Geometry& g, float* U, float* RK, float* R2,
                                          int8_t* lo, const PushTable& push, const GhostLists& gl_stage,
                                          const GhostLists& gl_final, StepScalars* sc, unsigned int* bar,

@@ -1462,6 +1462,49 @@ k_diffusion_march(const float* u, float* out, int8_t* ulo, PushTable push, Geome
 }
 
 // ---------------------------------------------------------------------------
+// After the core of a mixed state has been replaced from the host (the core
+// upload), what the diffusion pass closing a mixed step leaves besides
+// u^{n+1} itself: the regular faces pushed into the neighbours' ghost layers
+// (the face entries left to the final exchange follow as a separate launch),
+// and the next step's CFL minimum with the NaN scan, each cell's ratio the
+// one k_cfl forms. One CTA per block and a thread per (i, j) column marching
+// k; a row of NI cells lies in consecutive lanes, as the pushed radial faces
+// need.
+template <int NI, int NJ, int NK>
+__global__ void __launch_bounds__(NI * NJ) k_push_state(float* u, PushTable push, Geometry g, StepScalars* sc) {
+    using S = MShape<NI, NJ, NK, 1>;
+    constexpr int NIP = S::NIP, NJP = S::NJP;
+    static_assert((NI * NJ) % 32 == 0 && 32 % NI == 0, "whole rows in every warp");
+    __shared__ PushBlock pb;
+    const int b = blockIdx.x, tid = threadIdx.x;
+    load_push_block(push, b, &pb);
+    __syncthreads();
+    const int ii = tid % NI + 2, jj = tid / NI + 2;
+    const float* Gi = gi_ptr<float>(g) + (size_t)b * GI_COUNT * NIP;
+    const float* Gj = gj_ptr<float>(g) + (size_t)b * GJ_COUNT * NJP;
+    const float* Gs = gs_ptr<float>(g) + (size_t)b * GS_COUNT;
+    const float cs = Gi[GI_CS * NIP + ii], rho0 = Gi[GI_RHO0 * NIP + ii], r = Gi[GI_R * NIP + ii];
+    const float sin_t = Gj[GJ_SIN * NJP + jj], dxi = Gs[GS_DXI], dxj = Gs[GS_DXJ], dxk = Gs[GS_DXK];
+    const float* blk = u + (size_t)b * NV * S::NCELL;
+    float cmin = INFINITY;
+    int cnan = 0;
+    for (int kp = 2; kp < NK + 2; ++kp) {
+        float o[NV];
+        const size_t base = ((size_t)kp * NJP + jj) * NIP + ii;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) o[v] = blk[(size_t)v * S::NCELL + base];
+        if (push.tgt != nullptr) push_faces_part<float, S, NV>(u, pb, ii, jj, kp, o, 0);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) cnan |= (o[v] != o[v]);
+        float ratio = cfl_ratio_f(cfl_sq3(o[V_VR], o[V_VT], o[V_VP]), cfl_sq3(o[V_BR], o[V_BT], o[V_BP]), cs, rho0, r,
+                                  sin_t, dxi, dxj, dxk);
+        if (ratio != ratio) { cnan = 1; ratio = INFINITY; }
+        cmin = fminf(cmin, ratio);
+    }
+    cfl_commit(cmin, cnan, sc);
+}
+
+// ---------------------------------------------------------------------------
 // FP64 artificial diffusion (3_6/ModDiffusion.f90:9-150) of one block as a k
 // march, in place (the exact path: no pushes, no fused CFL minimum, no u^n
 // correction). One thread per (cell column, variable): NI*NJ*NV threads. The

@@ -27,6 +27,14 @@ cudaError_t launch_ghost_mixed(const StepDims& d, const GhostLists& gl, float* u
     return impl::ghost_any<float>(d, gl, u, st);
 }
 int kpar_candidates_mixed(const StepDims& d, int* out) { return impl::candidates<float>(d, out); }
+cudaError_t launch_push_state_mixed(const StepDims& d, const Geometry& g, float* u, const PushTable& push,
+                                    StepScalars* sc, cudaStream_t st) {
+    if (d.ni == 16 && d.nj == 16 && d.nk == 16) impl::k_push_state<16, 16, 16><<<d.nblocks, 256, 0, st>>>(u, push, g, sc);
+    else if (d.ni == 8 && d.nj == 8 && d.nk == 8) impl::k_push_state<8, 8, 8><<<d.nblocks, 64, 0, st>>>(u, push, g, sc);
+    else return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
 
 cudaError_t launch_step_persistent_mixed(const StepDims& d, const Geometry& g, float* U, float* RK, float* R2,
                                          int8_t* lo, const PushTable& push, const GhostLists& gl_stage,

@@ -572,6 +572,44 @@ def _core_mask(shape):
     return m
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("how", ["upload", "upload_core", "init_synthetic"])
+def test_new_state_replaces_the_pending_cfl_minimum(how):
+    """A mixed step leaves the CFL minimum of u^{n+1}, formed by its diffusion
+    pass, pending for the next step. A state put in its place (full or core
+    upload, synthetic initial condition) is timed by its own minimum only:
+    after a step of a state with faster waves, the next dt equals the dt a
+    fresh context computes for the new state."""
+    mk = lambda: config.make_config(block=(16, 16, 16), root_tiles=(1, 3, 9), radial_levels=1, amr=(),
+                                    precision=config.PREC_MIXED)
+    a, b = fg.Falcon(mk()), fg.Falcon(mk())
+    if how == "init_synthetic":
+        a.init_synthetic(kind=1, seed=1002, mach=0.3)
+        a.advance_rk4()
+        a.init_synthetic(kind=1, seed=1002, mach=0.01)
+        b.init_synthetic(kind=1, seed=1002, mach=0.01)
+    else:
+        slow = synth.initial_state(mk(), a.block_ranges(), a.block_flags(), seed=1011, b_frac=1e-3)
+        fast = synth.initial_state(mk(), a.block_ranges(), a.block_flags(), seed=1011, b_frac=0.5)
+        a.upload_state(fast)
+        a.exchange()
+        a.advance_rk4()
+        if how == "upload":
+            a.upload_state(slow)
+        else:
+            host = np.ascontiguousarray(slow.copy())
+            a.pin_host(host)
+            try:
+                a.upload_state_core(host)
+            finally:
+                a.unpin_host(host)
+        b.upload_state(slow)
+        b.exchange()
+    dt_a, dt_b = a.advance_rk4(), b.advance_rk4()
+    assert dt_a == dt_b, (dt_a, dt_b)
+    assert a.advance_rk4() == b.advance_rk4()
+
+
 @pytest.mark.parametrize("divb", [0, 1])
 @pytest.mark.parametrize("grid", ["8cube", "16cube"])
 def test_core_transfers_match_full(divb, grid):
@@ -594,6 +632,9 @@ def test_core_transfers_match_full(divb, grid):
         a.upload_state_core(host)
         b.upload_state(u0)
         b.exchange()
+        # the stage buffer starts as a copy of the state after either upload
+        core = _core_mask(u0.shape)
+        assert np.array_equal(a.download_stage_state()[core], b.download_stage_state()[core])
         for x in (a, b):
             for _ in range(2):
                 x.advance_rk4(want_dt=False)
