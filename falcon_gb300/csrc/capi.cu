@@ -55,7 +55,6 @@ struct falcon_ctx {
     GhostLists gl_stage{};    // face ghosts not pushed by the stage kernel (exchanges after stages)
     GhostLists gl_final{};    // mixed: ghost entries the exchange ending a step fills (see setup_device)
     bool stale_edges = false; // mixed: edge/corner ghosts not refreshed since the last step
-    bool rk_pending = false;  // the stage buffer is due a copy of the state (settle_stage_buffer)
     bool cfl_ready = false;   // mixed: the last diffusion pass formed this state's CFL minimum
     PushTable push{};         // mixed path: faces the stage kernel writes into its output
     void* R2 = nullptr;       // mixed path: second stage buffer (pushing needs out != in)
@@ -319,24 +318,31 @@ cudaError_t drop_pending_cfl(falcon_ctx* ctx) {
     return cudaMemcpyAsync(&ctx->sc->min_ratio_bits, &inf_bits, sizeof inf_bits, cudaMemcpyHostToDevice, ctx->st);
 }
 
-// The stage buffer starts as a copy of the state (primitive_rk_IV =
-// primitive_IV, as the reference's initialisation leaves it). The core upload
-// defers that copy: a step's first stage rewrites the buffer before anything
-// reads it, so the copy is made only when the buffer is read as it stands
-// (the phases, falcon_download_stage_state).
-cudaError_t settle_stage_buffer(falcon_ctx* ctx) {
-    if (!ctx->rk_pending) return cudaSuccess;
-    cudaError_t e = fresh_state(ctx);   // with its ghost cells complete, as an upload leaves it
-    if (e != cudaSuccess) return e;
-    ctx->rk_pending = false;
-    return cudaMemcpyAsync(ctx->RK, ctx->U, (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell * ctx->elem,
-                           cudaMemcpyDeviceToDevice, ctx->st);
+// The state copied into the second state buffer and, with stage, into the
+// stage buffer too (primitive_rk_IV = primitive_IV, as the reference's
+// initialisation leaves it): one pass that reads the state once.
+__global__ void k_copy2(const uint4* __restrict__ src, uint4* __restrict__ a, uint4* __restrict__ b, size_t n) {
+    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (size_t)gridDim.x * blockDim.x) {
+        const uint4 v = src[x];
+        a[x] = v;
+        if (b) b[x] = v;
+    }
 }
-
-cudaError_t mirror_state(falcon_ctx* ctx) {
-    if (!ctx->R2) return cudaSuccess;
-    return cudaMemcpyAsync(ctx->R2, ctx->U, (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell * ctx->elem,
-                           cudaMemcpyDeviceToDevice, ctx->st);
+cudaError_t mirror_state(falcon_ctx* ctx, bool stage = false) {
+    const size_t bytes = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell * ctx->elem;
+    void* a = stage ? ctx->RK : ctx->R2;
+    void* b = stage ? ctx->R2 : nullptr;
+    if (!a) return cudaSuccess;
+    if (bytes % 16 != 0) {   // not for the supported block sizes (ncell even, 4- or 8-byte cells)
+        cudaError_t e = cudaMemcpyAsync(a, ctx->U, bytes, cudaMemcpyDeviceToDevice, ctx->st);
+        if (e == cudaSuccess && b) e = cudaMemcpyAsync(b, ctx->U, bytes, cudaMemcpyDeviceToDevice, ctx->st);
+        return e;
+    }
+    int nsm = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
+    if (e != cudaSuccess) return e;
+    k_copy2<<<nsm * 8, 256, 0, ctx->st>>>((const uint4*)ctx->U, (uint4*)a, (uint4*)b, bytes / 16);
+    return cudaGetLastError();
 }
 
 // Autotuner: time every instantiated k-chunk depth of the stage and diffusion
@@ -395,7 +401,6 @@ int autotune(falcon_ctx* ctx) {
     CK(cudaMemsetAsync(&ctx->sc->nan_flag, 0, sizeof(int32_t), ctx->st), "autotune");
     const size_t nelem = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
     CK(cudaMemcpyAsync(ctx->RK, ctx->U, nelem * ctx->elem, cudaMemcpyDeviceToDevice, ctx->st), "autotune");
-    ctx->rk_pending = false;
     CK(cudaStreamSynchronize(ctx->st), "autotune");
     return FALCON_OK;
 }
@@ -1101,10 +1106,7 @@ int falcon_upload_state(falcon_ctx* ctx, const double* u) {
     CK(drop_pending_cfl(ctx), "upload");
     CK(clear_step_flags(ctx), "upload");
     // primitive_rk_IV = primitive_IV, as the reference's initialisation leaves it
-    const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
-    CK(cudaMemcpyAsync(ctx->RK, ctx->U, n * ctx->elem, cudaMemcpyDeviceToDevice, ctx->st), "upload");
-    ctx->rk_pending = false;
-    CK(mirror_state(ctx), "upload");
+    CK(mirror_state(ctx, true), "upload");
     // psi's stage array and the scratch it is copied from start equal too:
     // their ghost cells that no exchange writes (the radial boundary planes)
     // then stay at the uploaded values, as the reference's arrays do.
@@ -1165,34 +1167,37 @@ int falcon_upload_state_core(falcon_ctx* ctx, const double* u) {
     // as it was
     if (!ctx->dflag) CK(ctx->alloc(&ctx->dflag, sizeof(int32_t)), "alloc flag");
     int8_t* lo_tmp = (int8_t*)ctx->RK;
-    const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
-
     CK(launch_core_up(src, ctx->R2, lo_tmp, ctx->P ? ctx->P2 : nullptr, ctx->P ? nullptr : ctx->dflag, true, ctx->dims,
                       ctx->st),
        "upload core");
     int32_t bad = 0;
     if (!ctx->P) CK(cudaMemcpyAsync(&bad, ctx->dflag, sizeof bad, cudaMemcpyDeviceToHost, ctx->st), "upload core");
     CK(cudaStreamSynchronize(ctx->st), "upload core");
-    if (bad) {
-        CK(mirror_state(ctx), "upload core");
-        ctx->rk_pending = true;   // the stage buffer held the corrections
+    if (bad) {   // the state is kept; both buffers written above start again from it
+        CK(mirror_state(ctx, true), "upload core");
         CK(cudaStreamSynchronize(ctx->st), "upload core");
         return ctx->fail(FALCON_ERR_INVALID_ARG, "psi must be 0 unless divb_option = 1");
     }
     std::swap(ctx->U, ctx->R2);
     CK(cudaMemcpyAsync(ctx->Ulo, lo_tmp, lo_elems(ctx->dims), cudaMemcpyDeviceToDevice, ctx->st), "upload core");
+    CK(launch_clear_outside_core_mixed(ctx->dims, (float*)ctx->U, NV, ctx->st), "upload core");
+    if (ctx->P) CK(launch_clear_outside_core_mixed(ctx->dims, (float*)ctx->P2, 1, ctx->st), "upload core");
     CK(clear_step_flags(ctx), "upload core");
     CK(drop_pending_cfl(ctx), "upload core");
     // what the diffusion pass closing a step leaves besides u^{n+1}: the
-    // regular faces pushed, the other face entries filled (the final
-    // exchange) and the next step's CFL minimum formed; edge and corner
-    // ghosts are completed before the state is read (fresh_state)
+    // regular faces pushed by k_push_state (which also forms the next step's
+    // CFL minimum, so the step that follows skips k_cfl) and the other face
+    // entries of the final exchange; edge and corner ghosts stay at the 0 set
+    // above until the state is read (fresh_state)
     CK(launch_push_state_mixed(ctx->dims, ctx->geom(), (float*)ctx->U, ctx->push, ctx->sc, ctx->st), "upload core");
     CK(launch_ghost_mixed(ctx->dims, ctx->gl_final, (float*)ctx->U, ctx->st), "upload core");
     ctx->stale_edges = true;
     ctx->cfl_ready = true;
-    ctx->rk_pending = true;
-    CK(mirror_state(ctx), "upload core");
+    // the stage buffer and the second state buffer start as copies of the
+    // state: ghost cells that a step reads without rewriting (with weight 0
+    // in an interpolation) hold its finite values, not the corrections staged
+    // in the stage buffer or an earlier state's
+    CK(mirror_state(ctx, true), "upload core");
     if (ctx->P) {
         const size_t np = (size_t)ctx->dims.nblocks * ctx->dims.ncell * ctx->elem;
         CK(cudaMemcpyAsync(ctx->P, ctx->P2, np, cudaMemcpyDeviceToDevice, ctx->st), "upload core");
@@ -1245,10 +1250,7 @@ int falcon_init_synthetic(falcon_ctx* ctx, int32_t kind, uint64_t seed, double m
     std::string e = synth_initial_state(ctx->grid, ctx->geom(), ctx->U, ctx->mixed(), kind, seed, mach, ctx->st);
     if (!e.empty()) return ctx->fail(FALCON_ERR_CUDA, e);
     if (ctx->Ulo) CK(cudaMemsetAsync(ctx->Ulo, 0, lo_elems(ctx->dims), ctx->st), "init");
-    const size_t n = (size_t)ctx->dims.nblocks * NV * ctx->dims.ncell;
-    CK(cudaMemcpyAsync(ctx->RK, ctx->U, n * ctx->elem, cudaMemcpyDeviceToDevice, ctx->st), "init");
-    ctx->rk_pending = false;
-    CK(mirror_state(ctx), "init");
+    CK(mirror_state(ctx, true), "init");
     ctx->stale_edges = false;
     CK(drop_pending_cfl(ctx), "init");
     CK(clear_step_flags(ctx), "init");
@@ -1291,7 +1293,6 @@ int falcon_timestep(falcon_ctx* ctx, double* dt_out) {
 static int run(falcon_ctx* ctx, int32_t n) {
     int rc = autotune(ctx);
     if (rc) return rc;
-    if (n > 0) ctx->rk_pending = false;   // the first stage rewrites the stage buffer
     if (ctx->ktiming) {
         for (int32_t s = 0; s < n; ++s) {
             CK(enqueue_step(ctx), "step");
@@ -1397,7 +1398,6 @@ int falcon_step_phase(falcon_ctx* ctx, int32_t phase) {
     rc = autotune(ctx);
     if (rc) return rc;
     if (ctx->shard.on) return shard_phase(ctx, phase);
-    CK(settle_stage_buffer(ctx), "phase");
     CK(drop_pending_cfl(ctx), "phase");   // the phases change the state outside the fused step
     cudaError_t e = cudaSuccess;
     if (phase == 0) {
@@ -1426,7 +1426,6 @@ int falcon_download_stage_state(falcon_ctx* ctx, double* u) {
     int rc = need_device(ctx);
     if (rc) return rc;
     if (!u) return ctx->fail(FALCON_ERR_INVALID_ARG, "null state");
-    CK(settle_stage_buffer(ctx), "stage state");
     return get_state(ctx, ctx->RK, nullptr, ctx->Prk, u);
 }
 
@@ -1671,9 +1670,7 @@ int falcon_load_restart(falcon_ctx* ctx, const char* path) {
     if (e != cudaSuccess) return ctx->cuda_fail(e, "restart");
     if (!ok) return ctx->fail(FALCON_ERR_INVALID_ARG, std::string("restart ") + path + ": short read");
     // the stage arrays start equal to the state, as after falcon_upload_state
-    CK(cudaMemcpyAsync(ctx->RK, ctx->U, h.bytes_state, cudaMemcpyDeviceToDevice, ctx->st), "restart");
-    ctx->rk_pending = false;
-    CK(mirror_state(ctx), "restart");
+    CK(mirror_state(ctx, true), "restart");
     ctx->stale_edges = false;
     CK(drop_pending_cfl(ctx), "restart");
     CK(clear_step_flags(ctx), "restart");

@@ -234,6 +234,9 @@ cudaError_t launch_psi_ghost_mixed(const StepDims& d, const GhostLists& gl, floa
 // (after the CFL minimum of u^n is formed): dt, four stages with their face
 // exchanges, diffusion into R2, the final exchange. bar: 8 device words
 // (reset here): grid-barrier counter and generation, the 5 block tickets.
+// every cell outside the core of each block and variable set to 0 (nvar
+// variables per block: NV for the state, 1 for psi)
+cudaError_t launch_clear_outside_core_mixed(const StepDims& d, float* u, int nvar, cudaStream_t st);
 // the regular faces of a mixed state pushed and its CFL minimum formed, as the
 // diffusion pass closing a step leaves them (after a core upload)
 cudaError_t launch_push_state_mixed(const StepDims& d, const Geometry& g, float* u, const PushTable& push,

@@ -54,9 +54,13 @@ __device__ __forceinline__ float minmod_sel(float ul, float u, float ur) {
     const float a = (ur - ul) * 0.5f;
     const float b = 2.f * (ur - u);
     const float c = 2.f * (u - ul);
-    const float x = (fmaxf(0.f, a * b) * 1.e10f) * fmaxf(0.f, b * c);
+    // max(0, ab) 1e10 max(0, bc) >= 1e-30 is the same test as ab > 0 and
+    // (ab 1e10) bc >= 1e-30: with ab > 0 the first max is ab, and with bc <= 0
+    // or NaN both products are <= 0 or NaN (0 or -0 times an infinity)
+    const float ab = a * b;
+    const float x = (ab * 1.e10f) * (b * c);
     const float m = fminf(fminf(fabsf(a), fabsf(b)), fabsf(c));
-    return x >= 1.e-30f ? copysignf(m, a) : 0.f;
+    return ab > 0.f && x >= 1.e-30f ? copysignf(m, a) : 0.f;
 }
 
 // The per-cell CFL ratio h_LLL / v_wave of the mixed path, shared by k_cfl and
@@ -429,10 +433,12 @@ __device__ __forceinline__ float2 minmod_sel2(float2 ul, float2 u, float2 ur) {
     const float2 a = __fmul2_rn(sub2(ur, ul), f2(0.5f));
     const float2 b = __fmul2_rn(sub2(ur, u), f2(2.f));
     const float2 c = __fmul2_rn(sub2(u, ul), f2(2.f));
-    const float2 x = __fmul2_rn(__fmul2_rn(max02(__fmul2_rn(a, b)), f2(1.e10f)), max02(__fmul2_rn(b, c)));
+    const float2 ab = __fmul2_rn(a, b);   // the test of minmod_sel
+    const float2 x = __fmul2_rn(__fmul2_rn(ab, f2(1.e10f)), __fmul2_rn(b, c));
     const float mx = fminf(fminf(fabsf(a.x), fabsf(b.x)), fabsf(c.x));
     const float my = fminf(fminf(fabsf(a.y), fabsf(b.y)), fabsf(c.y));
-    return f2(x.x >= 1.e-30f ? copysignf(mx, a.x) : 0.f, x.y >= 1.e-30f ? copysignf(my, a.y) : 0.f);
+    return f2(ab.x > 0.f && x.x >= 1.e-30f ? copysignf(mx, a.x) : 0.f,
+              ab.y > 0.f && x.y >= 1.e-30f ? copysignf(my, a.y) : 0.f);
 }
 // face_flux_s<float> for two variables; cc = -0.25 (cR + cL), the face's
 // speed factor (the same for every variable; -0.25 scales exactly, so
@@ -1462,6 +1468,36 @@ k_diffusion_march(const float* u, float* out, int8_t* ulo, PushTable push, Geome
 }
 
 // ---------------------------------------------------------------------------
+// Every cell outside the core of each block and variable set to 0 (the k ghost
+// planes and, in the interior planes, the j ghost rows: per block and
+// variable, (NJP-4)*NIP-wide gaps between the core runs). A core upload clears
+// them before its exchange refills the listed ones: the mixed interpolations
+// read some ghost cells of their source blocks with weight 0, which is
+// harmless for finite values only, and the buffer may hold an earlier state
+// with NaNs there. Cleared, the uploaded state's ghost cells are the same
+// whatever the buffer held (a new context starts with zeros too).
+template <class T>
+__global__ void __launch_bounds__(256) k_clear_outside_core(T* u, int64_t nbv, StepDims d) {
+    const int pl = d.nip * d.njp, lead = 2 * pl + 2 * d.nip, gap = 4 * d.nip;
+    const int per = 2 * lead + (d.nkp - 5) * gap;   // non-core cells per block and variable
+    for (int64_t bv = blockIdx.x; bv < nbv; bv += gridDim.x) {
+        T* base = u + bv * d.ncell;
+        for (int x = threadIdx.x; x < per; x += blockDim.x) {
+            int c;
+            if (x < lead) {
+                c = x;                                   // planes 0, 1 and rows 0, 1 of plane 2
+            } else if (x < per - lead) {
+                const int q = (x - lead) / gap, r = (x - lead) - q * gap;
+                c = (2 + q) * pl + (d.njp - 2) * d.nip + r;   // rows NJP-2, NJP-1 of plane 2+q, rows 0, 1 of the next
+            } else {
+                c = d.ncell - lead + (x - (per - lead));   // rows NJP-2, NJP-1 of the last interior plane, 2 ghost planes
+            }
+            base[c] = T(0);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // After the core of a mixed state has been replaced from the host (the core
 // upload), what the diffusion pass closing a mixed step leaves besides
 // u^{n+1} itself: the regular faces pushed into the neighbours' ghost layers
@@ -1488,18 +1524,26 @@ __global__ void __launch_bounds__(NI * NJ) k_push_state(float* u, PushTable push
     const float* blk = u + (size_t)b * NV * S::NCELL;
     float cmin = INFINITY;
     int cnan = 0;
-    for (int kp = 2; kp < NK + 2; ++kp) {
-        float o[NV];
-        const size_t base = ((size_t)kp * NJP + jj) * NIP + ii;
+    constexpr int G = 4;   // planes whose loads are all issued before the first push
+    static_assert(NK % G == 0, "whole plane groups");
+    for (int k0 = 2; k0 < NK + 2; k0 += G) {
+        float o[G][NV];
 #pragma unroll
-        for (int v = 0; v < NV; ++v) o[v] = blk[(size_t)v * S::NCELL + base];
-        if (push.tgt != nullptr) push_faces_part<float, S, NV>(u, pb, ii, jj, kp, o, 0);
+        for (int q = 0; q < G; ++q) {
+            const size_t base = ((size_t)(k0 + q) * NJP + jj) * NIP + ii;
 #pragma unroll
-        for (int v = 0; v < NV; ++v) cnan |= (o[v] != o[v]);
-        float ratio = cfl_ratio_f(cfl_sq3(o[V_VR], o[V_VT], o[V_VP]), cfl_sq3(o[V_BR], o[V_BT], o[V_BP]), cs, rho0, r,
-                                  sin_t, dxi, dxj, dxk);
-        if (ratio != ratio) { cnan = 1; ratio = INFINITY; }
-        cmin = fminf(cmin, ratio);
+            for (int v = 0; v < NV; ++v) o[q][v] = blk[(size_t)v * S::NCELL + base];
+        }
+#pragma unroll
+        for (int q = 0; q < G; ++q) {
+            if (push.tgt != nullptr) push_faces_part<float, S, NV>(u, pb, ii, jj, k0 + q, o[q], 0);
+#pragma unroll
+            for (int v = 0; v < NV; ++v) cnan |= (o[q][v] != o[q][v]);
+            float ratio = cfl_ratio_f(cfl_sq3(o[q][V_VR], o[q][V_VT], o[q][V_VP]),
+                                      cfl_sq3(o[q][V_BR], o[q][V_BT], o[q][V_BP]), cs, rho0, r, sin_t, dxi, dxj, dxk);
+            if (ratio != ratio) { cnan = 1; ratio = INFINITY; }
+            cmin = fminf(cmin, ratio);
+        }
     }
     cfl_commit(cmin, cnan, sc);
 }

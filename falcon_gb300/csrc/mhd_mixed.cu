@@ -27,6 +27,11 @@ cudaError_t launch_ghost_mixed(const StepDims& d, const GhostLists& gl, float* u
     return impl::ghost_any<float>(d, gl, u, st);
 }
 int kpar_candidates_mixed(const StepDims& d, int* out) { return impl::candidates<float>(d, out); }
+cudaError_t launch_clear_outside_core_mixed(const StepDims& d, float* u, int nvar, cudaStream_t st) {
+    const int64_t nbv = (int64_t)d.nblocks * nvar;
+    impl::k_clear_outside_core<float><<<(unsigned)(nbv < 65535 * 4 ? nbv : 65535 * 4), 256, 0, st>>>(u, nbv, d);
+    return cudaGetLastError();
+}
 cudaError_t launch_push_state_mixed(const StepDims& d, const Geometry& g, float* u, const PushTable& push,
                                     StepScalars* sc, cudaStream_t st) {
     if (d.ni == 16 && d.nj == 16 && d.nk == 16) impl::k_push_state<16, 16, 16><<<d.nblocks, 256, 0, st>>>(u, push, g, sc);

@@ -611,7 +611,7 @@ def test_new_state_replaces_the_pending_cfl_minimum(how):
 
 
 @pytest.mark.parametrize("divb", [0, 1])
-@pytest.mark.parametrize("grid", ["8cube", "16cube"])
+@pytest.mark.parametrize("grid", ["8cube", "16cube", "16amr"])
 def test_core_transfers_match_full(divb, grid):
     """Core upload (interior planes x interior rows moved, theta/phi ghost
     layers recomputed on the device) leaves the state that a full upload and
@@ -623,7 +623,8 @@ def test_core_transfers_match_full(divb, grid):
     if grid == "8cube":
         mk = lambda: config.tiny(**kw)
     else:
-        mk = lambda: config.make_config(block=(16, 16, 16), root_tiles=(1, 3, 9), radial_levels=1, amr=(), **kw)
+        amr = ((0, 1, 1),) if grid == "16amr" else ()
+        mk = lambda: config.make_config(block=(16, 16, 16), root_tiles=(1, 3, 9), radial_levels=1, amr=amr, **kw)
     a, b = fg.Falcon(mk()), fg.Falcon(mk())
     u0 = synth.initial_state(mk(), a.block_ranges(), a.block_flags(), seed=1011, psi_amp=1e-3 if divb else 0.0)
     host = np.ascontiguousarray(u0.copy())
@@ -633,8 +634,10 @@ def test_core_transfers_match_full(divb, grid):
         b.upload_state(u0)
         b.exchange()
         # the stage buffer starts as a copy of the state after either upload
-        core = _core_mask(u0.shape)
-        assert np.array_equal(a.download_stage_state()[core], b.download_stage_state()[core])
+        # (interior cells: the core's radial ghost columns are recomputed by
+        # the core upload's exchange, the full upload keeps u0's)
+        inner = (slice(None), slice(None), slice(2, -2), slice(2, -2), slice(2, -2))
+        assert np.array_equal(a.download_stage_state()[inner], b.download_stage_state()[inner])
         for x in (a, b):
             for _ in range(2):
                 x.advance_rk4(want_dt=False)
@@ -660,3 +663,39 @@ def test_core_transfers_match_full(divb, grid):
             assert np.array_equal(before, a.download_state())
     finally:
         a.unpin_host(host)
+
+
+@pytest.mark.gpu
+def test_core_upload_after_a_nan_step_starts_clean():
+    """A step that met a NaN leaves NaNs in both state buffers and the stage
+    buffer. A state put in place by the core upload must not read any of them
+    (some ghost cells enter the step's interpolations with weight 0): its next
+    steps equal, on every core and listed cell, those of a context that never
+    saw the NaN."""
+    mk = lambda: config.make_config(block=(16, 16, 16), root_tiles=(1, 3, 9), radial_levels=1, amr=((0, 1, 1),),
+                                    precision=config.PREC_MIXED)
+    a, b = fg.Falcon(mk()), fg.Falcon(mk())
+    u0 = synth.initial_state(mk(), a.block_ranges(), a.block_flags(), seed=1011)
+    bad = u0.copy()
+    bad[:, 0] = np.nan
+    a.upload_state(bad)
+    with pytest.raises(fg.FalconError) as e:
+        a.advance_rk4()
+    assert e.value.code == fg.ERR_NAN_DETECTED
+    host = np.ascontiguousarray(u0.copy())
+    a.pin_host(host)
+    try:
+        a.upload_state_core(host)
+    finally:
+        a.unpin_host(host)
+    b.upload_state(u0)
+    b.exchange()
+    for _ in range(2):
+        assert a.advance_rk4() == b.advance_rk4()
+    full = b.download_state()
+    ua = a.download_state()
+    gm = a.ghost_map()
+    sel = _core_mask(full.shape)
+    sel[gm["tblock"], :, gm["tk"] + 1, gm["tj"] + 1, gm["ti"] + 1] = True
+    assert np.isfinite(ua[sel]).all()
+    assert np.array_equal(ua[sel], full[sel])
