@@ -17,12 +17,17 @@ random-phase Kolmogorov velocity at rms Mach 0.01, seed 1002).
 --tuning KS KD fixes the k-chunk variants of the stage and diffusion kernels
 (falcon_set_tuning) instead of the autotuner, whose timings a profiler would
 distort; --step-mode persistent runs each step as one persistent launch.
+--end-to-end times, per step, the core of the FP64 state uploaded from pinned,
+page-aligned host memory (falcon_upload_state_core), the step, and the core
+downloaded again (falcon_download_state_core): the median of each part.
 """
 import argparse
 import json
 import sys
 
-from . import Falcon, build, config
+import time
+
+from . import Falcon, build, config, host_array
 
 WORKLOADS = {
     "shell_fp64_442k": lambda d: config.shell_fp64_cpu(device=d),
@@ -42,6 +47,7 @@ def main(argv=None):
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--tuning", type=int, nargs=2, metavar=("KS", "KD"), default=None)
     ap.add_argument("--step-mode", choices=("graph", "persistent"), default="graph")
+    ap.add_argument("--end-to-end", action="store_true")
     a = ap.parse_args(argv)
     build()
     f = Falcon(WORKLOADS[a.workload](a.device))
@@ -51,6 +57,8 @@ def main(argv=None):
         from . import STEP_PERSISTENT
         f.set_step_mode(STEP_PERSISTENT)
     f.init_synthetic(kind=1, seed=1002, mach=0.01)
+    if a.end_to_end:
+        return end_to_end(f, a)
     f.exchange()
     f.exchange()
     f.run_steps(a.warmup)
@@ -62,6 +70,38 @@ def main(argv=None):
     print(json.dumps({"workload": a.workload, "cells": f.interior_cells, "steps": a.steps, "step_mode": a.step_mode,
                       "ms_per_step": ms / max(a.steps, 1),
                       "cell_updates_per_s": f.interior_cells * a.steps / (ms / 1e3) if ms > 0 else None,
+                      "tuning": f.tuning()}))
+    f.close()
+    return 0
+
+
+def end_to_end(f, a):
+    import numpy as np
+    host = host_array(f.shape)
+    f.pin_host(host)
+    f.download_state_into(host)
+    f.synchronize()
+    parts = {"upload": [], "step": [], "download": []}
+    for s in range(a.warmup + a.steps):
+        t0 = time.perf_counter()
+        f.upload_state_core(host)
+        t1 = time.perf_counter()
+        f.advance_rk4(want_dt=True)
+        f.synchronize()
+        t2 = time.perf_counter()
+        f.download_state_core(host)
+        t3 = time.perf_counter()
+        if s >= a.warmup:
+            for k, t in (("upload", t1 - t0), ("step", t2 - t1), ("download", t3 - t2)):
+                parts[k].append(t)
+    f.unpin_host(host)
+    med = {k: float(np.median(v)) * 1e3 for k, v in parts.items()}
+    tot = sum(med.values())
+    core = host[:, :, 2:-2, 2:-2, :].nbytes
+    print(json.dumps({"workload": a.workload, "cells": f.interior_cells, "steps": a.steps, "end_to_end_ms": med,
+                      "core_bytes": core, "upload_gb_s": core / med["upload"] / 1e6,
+                      "download_gb_s": core / med["download"] / 1e6, "ms_per_step": tot,
+                      "cell_updates_per_s": f.interior_cells / (tot / 1e3) if tot > 0 else None,
                       "tuning": f.tuning()}))
     f.close()
     return 0
