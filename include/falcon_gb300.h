@@ -212,9 +212,13 @@ int  falcon_download_state_range(falcon_ctx* ctx, size_t first, size_t count, do
  * every step: of every block and variable, only the interior planes and,
  * within them, the interior rows (whole, radial ghost columns included) move,
  * 64% of a 16^3 block's padded cells. falcon_upload_state_core recomputes the
- * theta/phi ghost layers on the device with a full exchange (the values the
- * reference's ModCommunication_SendRecvGC leaves there) and rejects a non-zero
- * psi without GLM, leaving the state unchanged; falcon_download_state_core
+ * theta/phi ghost layers on the device (the values the reference's
+ * ModCommunication_SendRecvGC leaves there; the few ghost cells outside every
+ * exchange list, the radial boundary columns of ghost rows, read as 0 until a
+ * step's boundary condition rewrites them), forms the next step's CFL minimum,
+ * and rejects a non-zero psi without GLM, leaving the state unchanged; any
+ * earlier content of the device buffers (NaNs included) has no effect on the
+ * uploaded state or the steps that follow; falcon_download_state_core
  * leaves the array's other cells untouched. Same array layout as
  * falcon_upload_state. The array must lie in a falcon_pin_host buffer and be
  * 16-byte aligned; otherwise, and for a core upload into an FP64 context, the
